@@ -1,0 +1,517 @@
+// Device-resident whole-pass C ABI: context, EoS materials, upload /
+// download, the step of main.cpp:125-173 and inspection calls.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+
+#include "sph_internal.cuh"
+
+using namespace sph;
+
+int sph_fail(sph_ctx *ctx, int code, const char *fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (ctx) ctx->err = buf;
+    return code;
+}
+
+namespace {
+
+__global__ void k_iota32(int32_t *a, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = i;
+}
+
+__global__ void k_unpermute(const double *F, double *F2, int64_t cap, int n, const int32_t *slot, const int64_t *id,
+                            int64_t *id2, const int32_t *mat, int32_t *mat2) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int dst = slot[k];
+    for (int f = 0; f < SPH_NFIELD; ++f) F2[(int64_t)f * cap + dst] = F[(int64_t)f * cap + k];
+    id2[dst] = id[k];
+    mat2[dst] = mat[k];
+}
+
+template <class T>
+int dalloc(sph_ctx *ctx, T **p, int64_t n) {
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    cudaError_t e = cudaMalloc((void **)p, sizeof(T) * (size_t)std::max<int64_t>(n, 1));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return sph_fail(ctx, SPH_ERR_OOM, "device allocation of %lld bytes failed: %s",
+                        (long long)(sizeof(T) * (size_t)n), cudaGetErrorString(e));
+    }
+    return SPH_OK;
+}
+
+int upload_materials(sph_ctx *ctx) {
+    SPH_CUDA(ctx, cudaMemcpyAsync(ctx->mats_dev, ctx->mats_host, sizeof(ctx->mats_host), cudaMemcpyHostToDevice,
+                                  ctx->stream));
+    SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SPH_OK;
+}
+
+int time_mark(sph_ctx *ctx) {
+    if (!ctx->timing || ctx->n_ev >= 32) return SPH_OK;
+    SPH_CUDA(ctx, cudaEventRecord(ctx->ev[ctx->n_ev++], ctx->stream));
+    return SPH_OK;
+}
+
+// main.cpp:138-146 (positions fixed): sort + tree, density x n, EoS, derivative, hydro, gravity
+int compute_forces(sph_ctx *ctx) {
+    ctx->n_ev = 0;
+    SPH_TRY(time_mark(ctx));
+    SPH_TRY(sph_sort_and_build(ctx));
+    if (ctx->cfg.precision == SPH_PREC_MIXED) SPH_TRY(sph_pack_mixed(ctx));
+    SPH_TRY(time_mark(ctx));
+    for (int it = 0; it < ctx->cfg.n_dens_iter; ++it) SPH_TRY(sph_pass_density(ctx));
+    SPH_TRY(time_mark(ctx));
+    SPH_TRY(sph_pass_eos(ctx));
+    SPH_TRY(time_mark(ctx));
+    SPH_TRY(sph_pass_derivative(ctx));
+    SPH_TRY(time_mark(ctx));
+    SPH_TRY(sph_pass_hydro(ctx));
+    SPH_TRY(time_mark(ctx));
+    if (ctx->cfg.self_gravity) SPH_TRY(sph_pass_gravity(ctx));
+    SPH_TRY(time_mark(ctx));
+    ctx->have_forces = true;
+    return SPH_OK;
+}
+
+int collect_timings(sph_ctx *ctx) {
+    ctx->timings.clear();
+    if (!ctx->timing || ctx->n_ev < 2) return SPH_OK;
+    SPH_CUDA(ctx, cudaEventSynchronize(ctx->ev[ctx->n_ev - 1]));
+    for (int k = 1; k < ctx->n_ev; ++k) {
+        float ms = 0.0f;
+        SPH_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[k - 1], ctx->ev[k]));
+        ctx->timings.push_back(ms);
+    }
+    return SPH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void sph_config_default(sph_config *cfg) {
+    if (!cfg) return;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->theta = 0.5;
+    cfg->n_leaf = 8;
+    cfg->n_group = 256;
+    cfg->n_dens_iter = 4;
+    cfg->self_gravity = 1;
+    cfg->ext_damp = 0;
+    cfg->precision = SPH_PREC_FP64;
+    cfg->ext_damp_tend = 5000.0;
+    cfg->damping = 1.0;
+    cfg->G = 6.67e-11;
+    cfg->device = 0;
+}
+
+int sph_ctx_create(const sph_config *cfg, sph_ctx **out) {
+    if (!out) return SPH_ERR_ARG;
+    *out = nullptr;
+    sph_ctx *ctx = new (std::nothrow) sph_ctx();
+    if (!ctx) return SPH_ERR_OOM;
+    if (cfg) ctx->cfg = *cfg;
+    else sph_config_default(&ctx->cfg);
+    const sph_config &c = ctx->cfg;
+    if (!(c.theta >= 0.0) || c.n_leaf < 1 || c.n_group < 1 || c.n_dens_iter < 1 || c.n_dens_iter > 64 ||
+        (c.precision != SPH_PREC_FP64 && c.precision != SPH_PREC_MIXED)) {
+        delete ctx;
+        return SPH_ERR_ARG;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0 || c.device < 0 || c.device >= ndev) {
+        cudaGetLastError();
+        delete ctx;
+        return SPH_ERR_CUDA;
+    }
+    ctx->device = c.device;
+    if (cudaSetDevice(ctx->device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        delete ctx;
+        return SPH_ERR_CUDA;
+    }
+    for (int k = 0; k < MAX_MATERIALS; ++k) {
+        std::memset(&ctx->mats_host[k], 0, sizeof(DevMaterial));
+        ctx->mats_host[k].kind = -1;
+    }
+    for (int k = 0; k < 32; ++k) cudaEventCreate(&ctx->ev[k]);
+    if (cudaMalloc((void **)&ctx->mats_dev, sizeof(ctx->mats_host)) != cudaSuccess ||
+        cudaMalloc((void **)&ctx->scratch_d, sizeof(double) * 8192) != cudaSuccess ||
+        cudaMallocHost((void **)&ctx->host_scalars, sizeof(double) * 512) != cudaSuccess) {
+        cudaGetLastError();
+        sph_ctx_destroy(ctx);
+        return SPH_ERR_OOM;
+    }
+    if (upload_materials(ctx) != SPH_OK) {
+        sph_ctx_destroy(ctx);
+        return SPH_ERR_CUDA;
+    }
+    *out = ctx;
+    return SPH_OK;
+}
+
+int sph_ctx_destroy(sph_ctx *ctx) {
+    if (!ctx) return SPH_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    void *ptrs[] = {ctx->F, ctx->F2, ctx->id, ctx->id2, ctx->slot, ctx->slot2, ctx->mat, ctx->mat2, ctx->keys,
+                    ctx->scratch_d, ctx->xh, ctx->xl, ctx->vhf, ctx->vlf, ctx->mats_dev,
+                    ctx->tree.start, ctx->tree.count, ctx->tree.level, ctx->tree.first_child, ctx->tree.n_child,
+                    ctx->tree.parent, ctx->tree.mom, ctx->tree.com, ctx->tree.blo, ctx->tree.bhi,
+                    ctx->tree.tmp_cnt, ctx->tree.tmp_off, ctx->tree.tmp_b, ctx->tree.meta, ctx->tree.rb,
+                    ctx->sort.k0, ctx->sort.k1, ctx->sort.v0, ctx->sort.v1, ctx->sort.hist, ctx->sort.hoff,
+                    ctx->lists[0].nbr, ctx->lists[0].cnt, ctx->lists[1].nbr, ctx->lists[1].cnt,
+                    ctx->grav.group_cell, ctx->grav.is_group, ctx->grav.n_epj, ctx->grav.n_spj, ctx->grav.off_epj,
+                    ctx->grav.off_spj, ctx->grav.epj, ctx->grav.spj, ctx->scan.part, ctx->scan.total};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    for (void *p : ctx->table_allocs) cudaFree(p);
+    if (ctx->host_scalars) cudaFreeHost(ctx->host_scalars);
+    for (int k = 0; k < 32; ++k)
+        if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return SPH_OK;
+}
+
+const char *sph_last_error(const sph_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int sph_set_eos_table(sph_ctx *ctx, int material, const double *rho_axis, int n_rho, const double *u_axis, int n_u,
+                      const double *pres, const double *snds) {
+    if (!ctx) return SPH_ERR_ARG;
+    if (material < 0 || material >= MAX_MATERIALS) return sph_fail(ctx, SPH_ERR_ARG, "material %d out of range", material);
+    if (!rho_axis || !u_axis || !pres || !snds || n_rho < 1 || n_u < 1)
+        return sph_fail(ctx, SPH_ERR_TABLE, "EoS table for material %d is empty", material);
+    for (int k = 1; k < n_rho; ++k)
+        if (!(rho_axis[k] > rho_axis[k - 1])) return sph_fail(ctx, SPH_ERR_TABLE, "density axis not ascending");
+    for (int k = 1; k < n_u; ++k)
+        if (!(u_axis[k] > u_axis[k - 1])) return sph_fail(ctx, SPH_ERR_TABLE, "energy axis not ascending");
+    cudaSetDevice(ctx->device);
+    const size_t plane = sizeof(double) * (size_t)n_rho * n_u;
+    const size_t bytes = sizeof(double) * (n_rho + n_u) + 2 * plane;
+    char *d = nullptr;
+    if (cudaMalloc((void **)&d, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return sph_fail(ctx, SPH_ERR_OOM, "EoS table allocation");
+    }
+    ctx->table_allocs.push_back(d);
+    double *dr = (double *)d, *du = dr + n_rho, *dp = du + n_u, *dc = dp + (size_t)n_rho * n_u;
+    SPH_CUDA(ctx, cudaMemcpy(dr, rho_axis, sizeof(double) * n_rho, cudaMemcpyHostToDevice));
+    SPH_CUDA(ctx, cudaMemcpy(du, u_axis, sizeof(double) * n_u, cudaMemcpyHostToDevice));
+    SPH_CUDA(ctx, cudaMemcpy(dp, pres, plane, cudaMemcpyHostToDevice));
+    SPH_CUDA(ctx, cudaMemcpy(dc, snds, plane, cudaMemcpyHostToDevice));
+    DevMaterial &m = ctx->mats_host[material];
+    std::memset(&m, 0, sizeof(m));
+    m.kind = 0;
+    m.n_rho = n_rho;
+    m.n_u = n_u;
+    m.rho = dr;
+    m.u = du;
+    m.pres = dp;
+    m.snds = dc;
+    return upload_materials(ctx);
+}
+
+// Reader with the semantics of EoS.h:121-221 (header "# n_rho n_u", '#' lines
+// skipped, n_u rows per density block, columns rho u T P c_s S).
+int sph_load_eos_table_file(sph_ctx *ctx, int material, const char *path) {
+    if (!ctx || !path) return SPH_ERR_ARG;
+    std::ifstream in(path);
+    if (!in.is_open()) return sph_fail(ctx, SPH_ERR_TABLE, "cannot open EoS table %s", path);
+    std::string line;
+    int n_rho = 0, n_u = 0;
+    if (!std::getline(in, line)) return sph_fail(ctx, SPH_ERR_TABLE, "%s: empty file", path);
+    {
+        std::istringstream ss(line);
+        std::string hash;
+        ss >> hash >> n_rho >> n_u;
+        if (hash != "#" || n_rho < 1 || n_u < 1) return sph_fail(ctx, SPH_ERR_TABLE, "%s: bad header", path);
+    }
+    std::vector<double> rho(n_rho), u(n_u), P((size_t)n_rho * n_u), C((size_t)n_rho * n_u);
+    size_t row = 0;
+    while (std::getline(in, line)) {
+        if (line.empty() || line[0] == '#') continue;
+        std::istringstream ss(line);
+        double v[6];
+        int k = 0;
+        while (k < 6 && (ss >> v[k])) ++k;
+        if (k == 0) continue;
+        if (k < 5) return sph_fail(ctx, SPH_ERR_TABLE, "%s: short row %zu", path, row);
+        if (row >= (size_t)n_rho * n_u) return sph_fail(ctx, SPH_ERR_TABLE, "%s: more rows than the header says", path);
+        const size_t li = row / n_u, ci = row % n_u;
+        if (ci == 0) rho[li] = v[0];
+        if (li == 0) u[ci] = v[1];
+        P[row] = v[3];
+        C[row] = v[4];
+        ++row;
+    }
+    if (row != (size_t)n_rho * n_u)
+        return sph_fail(ctx, SPH_ERR_TABLE, "%s: %zu rows, header says %d x %d", path, row, n_rho, n_u);
+    return sph_set_eos_table(ctx, material, rho.data(), n_rho, u.data(), n_u, P.data(), C.data());
+}
+
+int sph_set_eos_tillotson(sph_ctx *ctx, int material, const double par[10]) {
+    if (!ctx || !par) return SPH_ERR_ARG;
+    if (material < 0 || material >= MAX_MATERIALS) return sph_fail(ctx, SPH_ERR_ARG, "material %d out of range", material);
+    if (!(par[0] > 0.0) || !(par[1] > 0.0) || !(par[3] > par[2]))
+        return sph_fail(ctx, SPH_ERR_ARG, "Tillotson parameters need rho0 > 0, u0 > 0, ucv > uiv");
+    DevMaterial &m = ctx->mats_host[material];
+    std::memset(&m, 0, sizeof(m));
+    m.kind = 1;
+    for (int k = 0; k < 10; ++k) m.par[k] = par[k];
+    return upload_materials(ctx);
+}
+
+int sph_upload(sph_ctx *ctx, int64_t n, const double *fields, int64_t ld, const int64_t *id, const int32_t *material,
+               double time, int init_smth) {
+    if (!ctx) return SPH_ERR_ARG;
+    if (n < 1 || n > 0x3fffffff || !fields || ld < n) return sph_fail(ctx, SPH_ERR_ARG, "bad particle block (n=%lld)", (long long)n);
+    cudaSetDevice(ctx->device);
+    if (material) {
+        for (int64_t i = 0; i < n; ++i) {
+            const int m = material[i];
+            if (m < 0 || m >= MAX_MATERIALS || ctx->mats_host[m].kind < 0)
+                return sph_fail(ctx, SPH_ERR_ARG, "particle %lld uses unset material %d", (long long)i, m);
+        }
+    } else if (ctx->mats_host[0].kind < 0) {
+        return sph_fail(ctx, SPH_ERR_ARG, "material 0 is not set");
+    }
+    double msum = 0.0;
+    for (int64_t i = 0; i < n; ++i) {
+        const double mi = fields[(int64_t)SPH_MASS * ld + i];
+        if (!(mi > 0.0) || !std::isfinite(mi)) return sph_fail(ctx, SPH_ERR_NONFINITE, "particle %lld has mass %g", (long long)i, mi);
+        msum += mi;
+    }
+    if (n > ctx->cap) {
+        const int64_t c = n;
+        SPH_TRY(dalloc(ctx, &ctx->F, (int64_t)SPH_NFIELD * c));
+        SPH_TRY(dalloc(ctx, &ctx->F2, (int64_t)SPH_NFIELD * c));
+        SPH_TRY(dalloc(ctx, &ctx->id, c));
+        SPH_TRY(dalloc(ctx, &ctx->id2, c));
+        SPH_TRY(dalloc(ctx, &ctx->slot, c));
+        SPH_TRY(dalloc(ctx, &ctx->slot2, c));
+        SPH_TRY(dalloc(ctx, &ctx->mat, c));
+        SPH_TRY(dalloc(ctx, &ctx->mat2, c));
+        SPH_TRY(dalloc(ctx, &ctx->keys, c));
+        for (float4 **p : {&ctx->xh, &ctx->xl, &ctx->vhf, &ctx->vlf})
+            if (*p) {
+                cudaFree(*p);
+                *p = nullptr;
+            }
+        ctx->cap = c;
+    }
+    ctx->n = n;
+    SPH_CUDA(ctx, cudaMemcpy2DAsync(ctx->F, sizeof(double) * ctx->cap, fields, sizeof(double) * ld,
+                                    sizeof(double) * n, SPH_NFIELD, cudaMemcpyHostToDevice, ctx->stream));
+    if (id) {
+        SPH_CUDA(ctx, cudaMemcpyAsync(ctx->id, id, sizeof(int64_t) * n, cudaMemcpyHostToDevice, ctx->stream));
+    } else {
+        std::vector<int64_t> tmp(n);
+        for (int64_t i = 0; i < n; ++i) tmp[i] = i;
+        SPH_CUDA(ctx, cudaMemcpyAsync(ctx->id, tmp.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice, ctx->stream));
+        SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    if (material) {
+        SPH_CUDA(ctx, cudaMemcpyAsync(ctx->mat, material, sizeof(int32_t) * n, cudaMemcpyHostToDevice, ctx->stream));
+    } else {
+        SPH_CUDA(ctx, cudaMemsetAsync(ctx->mat, 0, sizeof(int32_t) * n, ctx->stream));
+    }
+    k_iota32<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(ctx->slot, (int)n);
+    SPH_CUDA(ctx, cudaGetLastError());
+    // power of two close to 1 / mean mass (exact rescaling of the FP32 mass copies)
+    ctx->mscale = std::ldexp(1.0, -(int)std::lround(std::log2(msum / (double)n)));
+    if (init_smth) SPH_TRY(sph_init_smth(ctx));
+    SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->time = time;
+    ctx->dt = 0.0;
+    ctx->step = 0;
+    ctx->uploaded = true;
+    ctx->have_forces = false;
+    return SPH_OK;
+}
+
+int sph_download(sph_ctx *ctx, double *fields, int64_t ld, int64_t *id, int32_t *material) {
+    if (!ctx) return SPH_ERR_ARG;
+    if (!ctx->uploaded) return sph_fail(ctx, SPH_ERR_STATE, "download before upload");
+    if (!fields || ld < ctx->n) return sph_fail(ctx, SPH_ERR_ARG, "bad output block");
+    cudaSetDevice(ctx->device);
+    const int n = (int)ctx->n;
+    k_unpermute<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(ctx->F, ctx->F2, ctx->cap, n, ctx->slot, ctx->id,
+                                                             ctx->id2, ctx->mat, ctx->mat2);
+    SPH_CUDA(ctx, cudaGetLastError());
+    SPH_CUDA(ctx, cudaMemcpy2DAsync(fields, sizeof(double) * ld, ctx->F2, sizeof(double) * ctx->cap,
+                                    sizeof(double) * n, SPH_NFIELD, cudaMemcpyDeviceToHost, ctx->stream));
+    if (id) SPH_CUDA(ctx, cudaMemcpyAsync(id, ctx->id2, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    if (material)
+        SPH_CUDA(ctx, cudaMemcpyAsync(material, ctx->mat2, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SPH_OK;
+}
+
+int sph_prologue(sph_ctx *ctx) {
+    if (!ctx) return SPH_ERR_ARG;
+    if (!ctx->uploaded) return sph_fail(ctx, SPH_ERR_STATE, "prologue before upload");
+    cudaSetDevice(ctx->device);
+    SPH_TRY(compute_forces(ctx));
+    SPH_TRY(sph_dt_global(ctx, &ctx->dt));     // main.cpp:103
+    SPH_TRY(sph_ext_force(ctx));               // main.cpp:104
+    SPH_TRY(collect_timings(ctx));
+    SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SPH_OK;
+}
+
+int sph_step(sph_ctx *ctx, int n_steps) {
+    if (!ctx) return SPH_ERR_ARG;
+    if (!ctx->have_forces) return sph_fail(ctx, SPH_ERR_STATE, "step before prologue");
+    cudaSetDevice(ctx->device);
+    for (int s = 0; s < n_steps; ++s) {
+        const double dt = ctx->dt;
+        SPH_TRY(sph_kick_drift_predict(ctx, dt));   // main.cpp:126-131
+        ctx->time += dt;                            // main.cpp:132
+        SPH_TRY(compute_forces(ctx));               // main.cpp:136-147
+        SPH_TRY(sph_ext_force(ctx));                // main.cpp:148
+        SPH_TRY(sph_final_kick(ctx, dt));           // main.cpp:149-153
+        SPH_TRY(sph_dt_global(ctx, &ctx->dt));      // main.cpp:160
+        ctx->step += 1;
+    }
+    SPH_TRY(collect_timings(ctx));
+    return SPH_OK;
+}
+
+int sph_get_time(const sph_ctx *ctx, double *time, double *dt, int64_t *step) {
+    if (!ctx) return SPH_ERR_ARG;
+    if (time) *time = ctx->time;
+    if (dt) *dt = ctx->dt;
+    if (step) *step = ctx->step;
+    return SPH_OK;
+}
+
+int sph_diagnostics(sph_ctx *ctx, double out[8]) {
+    if (!ctx || !out) return SPH_ERR_ARG;
+    if (!ctx->uploaded) return sph_fail(ctx, SPH_ERR_STATE, "diagnostics before upload");
+    cudaSetDevice(ctx->device);
+    return sph_diag(ctx, out);
+}
+
+int sph_run_pass(sph_ctx *ctx, int pass) {
+    if (!ctx) return SPH_ERR_ARG;
+    if (!ctx->uploaded) return sph_fail(ctx, SPH_ERR_STATE, "pass before upload");
+    cudaSetDevice(ctx->device);
+    switch (pass) {
+        case 0:
+            SPH_TRY(sph_sort_and_build(ctx));
+            if (ctx->cfg.precision == SPH_PREC_MIXED) SPH_TRY(sph_pack_mixed(ctx));
+            break;
+        case 1: SPH_TRY(sph_pass_density(ctx)); break;
+        case 2: SPH_TRY(sph_pass_eos(ctx)); break;
+        case 3: SPH_TRY(sph_pass_derivative(ctx)); break;
+        case 4: SPH_TRY(sph_pass_hydro(ctx)); break;
+        case 5: SPH_TRY(sph_pass_gravity(ctx)); break;
+        default: return sph_fail(ctx, SPH_ERR_ARG, "unknown pass %d", pass);
+    }
+    SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SPH_OK;
+}
+
+int sph_get_order(sph_ctx *ctx, int32_t *slot, uint64_t *keys) {
+    if (!ctx) return SPH_ERR_ARG;
+    if (!ctx->uploaded) return sph_fail(ctx, SPH_ERR_STATE, "no particles");
+    cudaSetDevice(ctx->device);
+    if (slot) SPH_CUDA(ctx, cudaMemcpy(slot, ctx->slot, sizeof(int32_t) * ctx->n, cudaMemcpyDeviceToHost));
+    if (keys) SPH_CUDA(ctx, cudaMemcpy(keys, ctx->keys, sizeof(uint64_t) * ctx->n, cudaMemcpyDeviceToHost));
+    return SPH_OK;
+}
+
+int sph_get_neighbors(sph_ctx *ctx, int mode, int64_t k, int32_t *out, int64_t cap, int64_t *n) {
+    if (!ctx || mode < 0 || mode > 1 || !n) return SPH_ERR_ARG;
+    const SphLists &L = ctx->lists[mode];
+    if (!L.valid) return sph_fail(ctx, SPH_ERR_STATE, "no list of mode %d", mode);
+    if (k < 0 || k >= ctx->n) return sph_fail(ctx, SPH_ERR_ARG, "particle index out of range");
+    cudaSetDevice(ctx->device);
+    int c = 0;
+    SPH_CUDA(ctx, cudaMemcpy(&c, L.cnt + k, sizeof(int), cudaMemcpyDeviceToHost));
+    *n = c;
+    const int64_t m = std::min<int64_t>(std::min<int64_t>(c, cap), L.K);
+    if (out && m > 0)
+        SPH_CUDA(ctx, cudaMemcpy2D(out, sizeof(int32_t), L.nbr + k, sizeof(int32_t) * L.pitch, sizeof(int32_t), m,
+                                   cudaMemcpyDeviceToHost));
+    return SPH_OK;
+}
+
+int sph_get_tree(sph_ctx *ctx, int64_t *n_cell, int32_t *start, int32_t *count, int32_t *level, int32_t *n_child,
+                 double *com_mass) {
+    if (!ctx || !n_cell) return SPH_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    const int nc = ctx->tree.n_cell_host;
+    *n_cell = nc;
+    const Tree &t = ctx->tree;
+    if (start) SPH_CUDA(ctx, cudaMemcpy(start, t.start, sizeof(int) * nc, cudaMemcpyDeviceToHost));
+    if (count) SPH_CUDA(ctx, cudaMemcpy(count, t.count, sizeof(int) * nc, cudaMemcpyDeviceToHost));
+    if (level) SPH_CUDA(ctx, cudaMemcpy(level, t.level, sizeof(int) * nc, cudaMemcpyDeviceToHost));
+    if (n_child) SPH_CUDA(ctx, cudaMemcpy(n_child, t.n_child, sizeof(int) * nc, cudaMemcpyDeviceToHost));
+    if (com_mass) SPH_CUDA(ctx, cudaMemcpy(com_mass, t.com, sizeof(double4) * nc, cudaMemcpyDeviceToHost));
+    return SPH_OK;
+}
+
+int sph_get_grav_list(sph_ctx *ctx, int64_t g, int64_t *n_group, int32_t *epj, int64_t cap_epj, int64_t *n_epj,
+                      int32_t *spj_level, int32_t *spj_start, int64_t cap_spj, int64_t *n_spj, int32_t *group_start,
+                      int32_t *group_count) {
+    if (!ctx) return SPH_ERR_ARG;
+    const GravLists &G = ctx->grav;
+    if (!G.valid) return sph_fail(ctx, SPH_ERR_STATE, "no gravity lists");
+    if (n_group) *n_group = G.ng;
+    if (g < 0) return SPH_OK;
+    if (g >= G.ng) return sph_fail(ctx, SPH_ERR_ARG, "group index out of range");
+    cudaSetDevice(ctx->device);
+    int ne = 0, ns = 0, oe = 0, os = 0, gc = 0;
+    SPH_CUDA(ctx, cudaMemcpy(&ne, G.n_epj + g, sizeof(int), cudaMemcpyDeviceToHost));
+    SPH_CUDA(ctx, cudaMemcpy(&ns, G.n_spj + g, sizeof(int), cudaMemcpyDeviceToHost));
+    SPH_CUDA(ctx, cudaMemcpy(&oe, G.off_epj + g, sizeof(int), cudaMemcpyDeviceToHost));
+    SPH_CUDA(ctx, cudaMemcpy(&os, G.off_spj + g, sizeof(int), cudaMemcpyDeviceToHost));
+    SPH_CUDA(ctx, cudaMemcpy(&gc, G.group_cell + g, sizeof(int), cudaMemcpyDeviceToHost));
+    if (n_epj) *n_epj = ne;
+    if (n_spj) *n_spj = ns;
+    if (group_start) SPH_CUDA(ctx, cudaMemcpy(group_start, ctx->tree.start + gc, sizeof(int), cudaMemcpyDeviceToHost));
+    if (group_count) SPH_CUDA(ctx, cudaMemcpy(group_count, ctx->tree.count + gc, sizeof(int), cudaMemcpyDeviceToHost));
+    if (epj && ne > 0)
+        SPH_CUDA(ctx, cudaMemcpy(epj, G.epj + oe, sizeof(int) * std::min<int64_t>(ne, cap_epj), cudaMemcpyDeviceToHost));
+    if ((spj_level || spj_start) && ns > 0) {
+        const int m = (int)std::min<int64_t>(ns, cap_spj);
+        std::vector<int> cells(m);
+        SPH_CUDA(ctx, cudaMemcpy(cells.data(), G.spj + os, sizeof(int) * m, cudaMemcpyDeviceToHost));
+        for (int k = 0; k < m; ++k) {
+            if (spj_level) SPH_CUDA(ctx, cudaMemcpy(spj_level + k, ctx->tree.level + cells[k], sizeof(int), cudaMemcpyDeviceToHost));
+            if (spj_start) SPH_CUDA(ctx, cudaMemcpy(spj_start + k, ctx->tree.start + cells[k], sizeof(int), cudaMemcpyDeviceToHost));
+        }
+    }
+    return SPH_OK;
+}
+
+int sph_get_timings(sph_ctx *ctx, double *ms, int cap, int *n) {
+    if (!ctx) return SPH_ERR_ARG;
+    if (cap < 0) {   // cap < 0 switches event timing on (cap == -1) or off (cap == -2)
+        ctx->timing = (cap == -1);
+        return SPH_OK;
+    }
+    const int m = (int)std::min<size_t>((size_t)cap, ctx->timings.size());
+    for (int k = 0; k < m; ++k) ms[k] = ctx->timings[k];
+    if (n) *n = (int)ctx->timings.size();
+    return SPH_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,493 @@
+// Functor-compatible batch entry points (dispatch / retrieve).
+//
+// These apply the reference functors exactly to caller-supplied walks in the
+// class.h payload layouts: RESULT::clear() (class.h:41-85), then for every i
+// of the walk the loop over the walk's whole j-list, then the per-i epilogue
+// inside the same functor (force.h:18-21, 102-104, 145).  Because the j-list
+// is the caller's (an FDPS group superset), out-of-support j contribute zero
+// to sums but still enter v_sig_max in the hydro functor, exactly as on the
+// CPU.  One CTA per walk; the walk's j-list is staged through shared memory
+// in tiles and read by every thread (one thread per i).
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "sph_physics.cuh"
+
+using namespace sph;
+
+namespace {
+
+constexpr int MAX_TAGS = 64;
+constexpr int WT = 128;
+
+thread_local std::string g_batch_err;
+
+int batch_fail(int code, const std::string &msg) {
+    g_batch_err = msg;
+    return code;
+}
+
+struct TagState {
+    cudaStream_t stream = nullptr;
+    char *h_in = nullptr, *d_in = nullptr;      // staged walks
+    size_t cap_in = 0;
+    char *h_out = nullptr, *d_out = nullptr;    // results
+    size_t cap_out = 0;
+    int64_t *h_meta = nullptr, *d_meta = nullptr;   // per walk: i offset, n_i, j offset, n_j, s offset, n_s
+    size_t cap_meta = 0;
+    int pending_kind = -1;
+    int pending_walks = 0;
+    size_t pending_out_bytes = 0;
+    int device = -1;
+};
+
+std::mutex g_mu;
+TagState g_tags[MAX_TAGS];
+
+int grow(char **h, char **d, size_t *cap, size_t need) {
+    if (need <= *cap) return SPH_OK;
+    size_t c = std::max(need, *cap * 2);
+    if (*h) cudaFreeHost(*h);
+    if (*d) cudaFree(*d);
+    *h = nullptr;
+    *d = nullptr;
+    *cap = 0;
+    if (cudaMallocHost((void **)h, c) != cudaSuccess || cudaMalloc((void **)d, c) != cudaSuccess) {
+        cudaGetLastError();
+        return batch_fail(SPH_ERR_OOM, "batch staging allocation failed");
+    }
+    *cap = c;
+    return SPH_OK;
+}
+
+int tag_state(int tag, TagState **out) {
+    if (tag < 0 || tag >= MAX_TAGS) return batch_fail(SPH_ERR_ARG, "tag out of range [0, 64)");
+    TagState &t = g_tags[tag];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (!t.stream || t.device != dev) {
+        if (cudaStreamCreateWithFlags(&t.stream, cudaStreamNonBlocking) != cudaSuccess) {
+            cudaGetLastError();
+            return batch_fail(SPH_ERR_CUDA, "cannot create a CUDA stream (no GPU?)");
+        }
+        t.device = dev;
+    }
+    *out = &t;
+    return SPH_OK;
+}
+
+// ---------------------------------------------------------------------------
+// kernels: meta[w*6 + {0..5}] = i offset, n_i, j offset, n_j, spj offset, n_spj (element offsets)
+
+__device__ __forceinline__ double3 ld3(const double *p) { return make_double3(p[0], p[1], p[2]); }
+
+// CalcDensity, force.h:9-23
+__global__ void __launch_bounds__(WT) k_walk_dens(const int64_t *meta, const sph_epi_dens *epi, const sph_epj_dens *epj,
+                                                  sph_result_dens *res) {
+    __shared__ double4 tile[WT];
+    const int64_t *M = meta + 6 * blockIdx.x;
+    const int64_t io = M[0], ni = M[1], jo = M[2], nj = M[3];
+    for (int64_t i0 = 0; i0 < ni; i0 += WT) {
+        const int64_t ii = i0 + threadIdx.x;
+        const bool act = ii < ni;
+        double3 pi = make_double3(0, 0, 0);
+        double hi = 1.0, mi = 1.0;
+        if (act) {
+            pi = ld3(epi[io + ii].pos);
+            hi = epi[io + ii].smth;
+            mi = epi[io + ii].mass;
+        }
+        const double H = SUPPORT * hi, invH = 1.0 / H, norm = kernel_norm(H);
+        double d = 0.0;
+        for (int64_t t0 = 0; t0 < nj; t0 += WT) {
+            if (t0 + threadIdx.x < nj) {
+                const sph_epj_dens &q = epj[jo + t0 + threadIdx.x];
+                tile[threadIdx.x] = make_double4(q.pos[0], q.pos[1], q.pos[2], q.mass);
+            }
+            __syncthreads();
+            const int tn = (int)min((int64_t)WT, nj - t0);
+            for (int t = 0; t < tn; ++t) {
+                const double4 q = tile[t];
+                const double dx = q.x - pi.x, dy = q.y - pi.y, dz = q.z - pi.z;
+                double w, g;
+                wendland_poly(sqrt(dx * dx + dy * dy + dz * dz) * invH, w, g);
+                d += q.w * (w * norm);
+            }
+            __syncthreads();
+        }
+        if (act) {
+            d = fmax(DENS_FLOOR, d);
+            res[io + ii].dens = d;
+            res[io + ii].smth = SMTH_COEF * pow(mi / d, 1.0 / 3.0);
+        }
+    }
+}
+
+// CalcDerivative, force.h:89-106
+__global__ void __launch_bounds__(WT) k_walk_drvt(const int64_t *meta, const sph_epi_drvt *epi, const sph_epj_drvt *epj,
+                                                  sph_result_drvt *res) {
+    __shared__ double4 tp[WT];
+    __shared__ double4 tv[WT];
+    const int64_t *M = meta + 6 * blockIdx.x;
+    const int64_t io = M[0], ni = M[1], jo = M[2], nj = M[3];
+    for (int64_t i0 = 0; i0 < ni; i0 += WT) {
+        const int64_t ii = i0 + threadIdx.x;
+        const bool act = ii < ni;
+        double3 pi = make_double3(0, 0, 0), vi = make_double3(0, 0, 0);
+        double hi = 1.0, rhoi = 1.0;
+        if (act) {
+            pi = ld3(epi[io + ii].pos);
+            vi = ld3(epi[io + ii].vel);
+            hi = epi[io + ii].smth;
+            rhoi = epi[io + ii].dens;
+        }
+        const double H = SUPPORT * hi, invH = 1.0 / H, norm = kernel_norm(H), ceps = 1.0e-6 * hi;
+        double dv = 0, r0 = 0, r1 = 0, r2 = 0, gs = 0;
+        for (int64_t t0 = 0; t0 < nj; t0 += WT) {
+            if (t0 + threadIdx.x < nj) {
+                const sph_epj_drvt &q = epj[jo + t0 + threadIdx.x];
+                tp[threadIdx.x] = make_double4(q.pos[0], q.pos[1], q.pos[2], q.mass);
+                tv[threadIdx.x] = make_double4(q.vel[0], q.vel[1], q.vel[2], 0.0);
+            }
+            __syncthreads();
+            const int tn = (int)min((int64_t)WT, nj - t0);
+            for (int t = 0; t < tn; ++t) {
+                const double4 q = tp[t], u = tv[t];
+                const double dx = pi.x - q.x, dy = pi.y - q.y, dz = pi.z - q.z;
+                const double ax = -q.w * (vi.x - u.x), ay = -q.w * (vi.y - u.y), az = -q.w * (vi.z - u.z);
+                const double rr2 = dx * dx + dy * dy + dz * dz;
+                const double r = sqrt(rr2);
+                double w, g;
+                wendland_poly(r * invH, w, g);
+                const double gf = norm * g / (r * H + ceps);
+                dv += gf * (ax * dx + ay * dy + az * dz);
+                r0 += gf * (ay * dz - az * dy);
+                r1 += gf * (az * dx - ax * dz);
+                r2 += gf * (ax * dy - ay * dx);
+                gs -= q.w / hi * (3.0 * norm * w + gf * rr2);
+            }
+            __syncthreads();
+        }
+        if (act) {
+            sph_result_drvt &o = res[io + ii];
+            o.grad_smth = 1.0 / (1.0 + hi * gs / (3.0 * rhoi));
+            o.div_v = dv / rhoi;
+            o.rot_v[0] = r0 / rhoi;
+            o.rot_v[1] = r1 / rhoi;
+            o.rot_v[2] = r2 / rhoi;
+        }
+    }
+}
+
+// CalcHydroForce, force.h:113-147
+__global__ void __launch_bounds__(WT) k_walk_hydro(const int64_t *meta, const sph_epi_hydro *epi,
+                                                   const sph_epj_hydro *epj, sph_result_hydro *res) {
+    __shared__ double4 tp[WT];   // pos, mass
+    __shared__ double4 tv[WT];   // vel, smth
+    __shared__ double4 tq[WT];   // dens, pres, snds, grad_smth
+    __shared__ double tb[WT];    // Bal
+    const int64_t *M = meta + 6 * blockIdx.x;
+    const int64_t io = M[0], ni = M[1], jo = M[2], nj = M[3];
+    for (int64_t i0 = 0; i0 < ni; i0 += WT) {
+        const int64_t ii = i0 + threadIdx.x;
+        const bool act = ii < ni;
+        sph_epi_hydro I;
+        if (act) I = epi[io + ii];
+        else std::memset(&I, 0, sizeof(I)), I.smth = 1.0, I.dens = 1.0;
+        const double Hi = SUPPORT * I.smth, invHi = 1.0 / Hi, normi = kernel_norm(Hi), cepsi = 1.0e-6 * I.smth;
+        const double Ai = I.grad_smth * I.pres / (I.dens * I.dens);
+        double a0 = 0, a1 = 0, a2 = 0, e = 0, vmax = 0.0;
+        for (int64_t t0 = 0; t0 < nj; t0 += WT) {
+            if (t0 + threadIdx.x < nj) {
+                const sph_epj_hydro &q = epj[jo + t0 + threadIdx.x];
+                tp[threadIdx.x] = make_double4(q.pos[0], q.pos[1], q.pos[2], q.mass);
+                tv[threadIdx.x] = make_double4(q.vel[0], q.vel[1], q.vel[2], q.smth);
+                tq[threadIdx.x] = make_double4(q.dens, q.pres, q.snds, q.grad_smth);
+                tb[threadIdx.x] = q.Bal;
+            }
+            __syncthreads();
+            const int tn = (int)min((int64_t)WT, nj - t0);
+            for (int t = 0; t < tn; ++t) {
+                const double4 p = tp[t], v = tv[t], q = tq[t];
+                const double dx = I.pos[0] - p.x, dy = I.pos[1] - p.y, dz = I.pos[2] - p.z;
+                const double wx = I.vel[0] - v.x, wy = I.vel[1] - v.y, wz = I.vel[2] - v.z;
+                const double rr2 = dx * dx + dy * dy + dz * dz;
+                const double r = sqrt(rr2);
+                const double dvdr = wx * dx + wy * dy + wz * dz;
+                const double w = (dvdr < 0) ? dvdr / r : 0.0;
+                const double vsig = I.snds + q.z - 3.0 * w;
+                vmax = fmax(vmax, vsig);
+                const double AV = -AV_STRENGTH * 0.5 * vsig * w / (0.5 * (I.dens + q.x)) * 0.5 * (I.Bal + tb[t]);
+                const double Hj = SUPPORT * v.w;
+                double wi_, gi_, wj_, gj_;
+                wendland_poly(r * invHi, wi_, gi_);
+                wendland_poly(r / Hj, wj_, gj_);
+                const double gfi = normi * gi_ / (r * Hi + cepsi);
+                const double gfj = kernel_norm(Hj) * gj_ / (r * Hj + 1.0e-6 * v.w);
+                const double gws = 0.5 * (gfi * I.grad_smth + gfj * q.w);
+                const double Aj = q.w * q.y / (q.x * q.x);
+                const double coef = p.w * (Ai * gfi + Aj * gfj + AV * gws);
+                a0 -= coef * dx;
+                a1 -= coef * dy;
+                a2 -= coef * dz;
+                e += p.w * (Ai + 0.5 * AV) * gws * dvdr;
+            }
+            __syncthreads();
+        }
+        if (act) {
+            sph_result_hydro &o = res[io + ii];
+            o.acc[0] = a0;
+            o.acc[1] = a1;
+            o.acc[2] = a2;
+            o.eng_dot = e;
+            o.dt = C_CFL * 2.0 * I.smth / vmax;
+        }
+    }
+}
+
+// CalcGravityForce<EPJ::Grav> then CalcGravityForce<SPJMonopole>, force.h:154-168
+__global__ void __launch_bounds__(WT) k_walk_grav(const int64_t *meta, const sph_epi_grav *epi, const sph_epj_grav *epj,
+                                                  const sph_spj_monopole *spj, sph_result_grav *res) {
+    __shared__ double4 tile[WT];
+    const double G = 6.67e-11;   // force.h:171-172
+    const int64_t *M = meta + 6 * blockIdx.x;
+    const int64_t io = M[0], ni = M[1], jo = M[2], nj = M[3], so = M[4], ns = M[5];
+    for (int64_t i0 = 0; i0 < ni; i0 += WT) {
+        const int64_t ii = i0 + threadIdx.x;
+        const bool act = ii < ni;
+        double3 pi = make_double3(0, 0, 0);
+        double eps2 = 1.0;
+        if (act) {
+            pi = ld3(epi[io + ii].pos);
+            eps2 = epi[io + ii].eps2;
+        }
+        double a0 = 0, a1 = 0, a2 = 0, p = 0;
+        for (int pass = 0; pass < 2; ++pass) {
+            const int64_t nl = pass == 0 ? nj : ns;
+            for (int64_t t0 = 0; t0 < nl; t0 += WT) {
+                if (t0 + threadIdx.x < nl) {
+                    if (pass == 0) {
+                        const sph_epj_grav &q = epj[jo + t0 + threadIdx.x];
+                        tile[threadIdx.x] = make_double4(q.pos[0], q.pos[1], q.pos[2], q.mass);
+                    } else {
+                        const sph_spj_monopole &q = spj[so + t0 + threadIdx.x];
+                        tile[threadIdx.x] = make_double4(q.pos[0], q.pos[1], q.pos[2], q.mass);
+                    }
+                }
+                __syncthreads();
+                const int tn = (int)min((int64_t)WT, nl - t0);
+                for (int t = 0; t < tn; ++t) {
+                    const double4 q = tile[t];
+                    const double dx = pi.x - q.x, dy = pi.y - q.y, dz = pi.z - q.z;
+                    const double dri = 1.0 / sqrt(dx * dx + dy * dy + dz * dz + eps2);
+                    const double mdr3 = q.w * (dri * dri * dri);
+                    a0 -= G * mdr3 * dx;
+                    a1 -= G * mdr3 * dy;
+                    a2 -= G * mdr3 * dz;
+                    p -= G * q.w * dri;
+                }
+                __syncthreads();
+            }
+        }
+        if (act) {
+            sph_result_grav &o = res[io + ii];
+            o.acc[0] = a0;
+            o.acc[1] = a1;
+            o.acc[2] = a2;
+            o.pot = p;
+            o.dt = 1.0e30;   // RESULT::Grav::clear(), dt untouched by the functor
+        }
+    }
+}
+
+template <class EPI, class EPJ, class RES>
+int stage(int tag, int kind, int n_walk, const EPI **epi, const int *n_epi, const EPJ **epj, const int *n_epj,
+          const sph_spj_monopole **spj, const int *n_spj, TagState **ts_out) {
+    if (n_walk < 0 || (n_walk > 0 && (!epi || !n_epi || !epj || !n_epj)))
+        return batch_fail(SPH_ERR_ARG, "null walk arrays");
+    TagState *ts = nullptr;
+    SPH_TRY(tag_state(tag, &ts));
+    if (ts->pending_kind >= 0) {
+        // a previous dispatch on this tag was never retrieved: finish it first
+        cudaStreamSynchronize(ts->stream);
+        ts->pending_kind = -1;
+    }
+    int64_t ni = 0, nj = 0, ns = 0;
+    for (int w = 0; w < n_walk; ++w) {
+        if (n_epi[w] < 0 || n_epj[w] < 0 || (spj && n_spj && n_spj[w] < 0))
+            return batch_fail(SPH_ERR_ARG, "negative walk size");
+        if ((n_epi[w] > 0 && !epi[w]) || (n_epj[w] > 0 && !epj[w])) return batch_fail(SPH_ERR_ARG, "null walk");
+        ni += n_epi[w];
+        nj += n_epj[w];
+        if (spj && n_spj) ns += n_spj[w];
+    }
+    const size_t b_epi = sizeof(EPI) * ni, b_epj = sizeof(EPJ) * nj, b_spj = sizeof(sph_spj_monopole) * ns;
+    // 16-byte aligned sections
+    const size_t o_epj = (b_epi + 15) & ~size_t(15), o_spj = (o_epj + b_epj + 15) & ~size_t(15);
+    SPH_TRY(grow(&ts->h_in, &ts->d_in, &ts->cap_in, o_spj + b_spj + 16));
+    SPH_TRY(grow(&ts->h_out, &ts->d_out, &ts->cap_out, sizeof(RES) * ni + 16));
+    SPH_TRY(grow((char **)&ts->h_meta, (char **)&ts->d_meta, &ts->cap_meta, sizeof(int64_t) * 6 * (n_walk + 1)));
+    int64_t ai = 0, aj = 0, as = 0;
+    for (int w = 0; w < n_walk; ++w) {
+        int64_t *m = ts->h_meta + 6 * w;
+        m[0] = ai;
+        m[1] = n_epi[w];
+        m[2] = aj;
+        m[3] = n_epj[w];
+        m[4] = as;
+        m[5] = (spj && n_spj) ? n_spj[w] : 0;
+        if (n_epi[w]) std::memcpy(ts->h_in + sizeof(EPI) * ai, epi[w], sizeof(EPI) * n_epi[w]);
+        if (n_epj[w]) std::memcpy(ts->h_in + o_epj + sizeof(EPJ) * aj, epj[w], sizeof(EPJ) * n_epj[w]);
+        if (m[5]) {
+            if (!spj[w]) return batch_fail(SPH_ERR_ARG, "null SPJ walk");
+            std::memcpy(ts->h_in + o_spj + sizeof(sph_spj_monopole) * as, spj[w], sizeof(sph_spj_monopole) * m[5]);
+        }
+        ai += n_epi[w];
+        aj += n_epj[w];
+        as += m[5];
+    }
+    if (cudaMemcpyAsync(ts->d_in, ts->h_in, o_spj + b_spj, cudaMemcpyHostToDevice, ts->stream) != cudaSuccess ||
+        cudaMemcpyAsync(ts->d_meta, ts->h_meta, sizeof(int64_t) * 6 * n_walk, cudaMemcpyHostToDevice, ts->stream) !=
+            cudaSuccess) {
+        cudaGetLastError();
+        return batch_fail(SPH_ERR_CUDA, "host-to-device copy failed");
+    }
+    ts->pending_kind = kind;
+    ts->pending_walks = n_walk;
+    ts->pending_out_bytes = sizeof(RES) * ni;
+    *ts_out = ts;
+    (void)o_epj;
+    return SPH_OK;
+}
+
+int finish_dispatch(TagState *ts) {
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return batch_fail(SPH_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
+    if (ts->pending_out_bytes &&
+        cudaMemcpyAsync(ts->h_out, ts->d_out, ts->pending_out_bytes, cudaMemcpyDeviceToHost, ts->stream) != cudaSuccess) {
+        cudaGetLastError();
+        return batch_fail(SPH_ERR_CUDA, "device-to-host copy failed");
+    }
+    return SPH_OK;
+}
+
+template <class RES>
+int retrieve(int tag, int kind, int n_walk, const int *n_epi, RES **result) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (tag < 0 || tag >= MAX_TAGS) return batch_fail(SPH_ERR_ARG, "tag out of range");
+    TagState &ts = g_tags[tag];
+    if (ts.pending_kind != kind || ts.pending_walks != n_walk)
+        return batch_fail(SPH_ERR_STATE, "retrieve does not match the last dispatch on this tag");
+    const cudaError_t e = cudaStreamSynchronize(ts.stream);
+    ts.pending_kind = -1;
+    if (e != cudaSuccess) return batch_fail(SPH_ERR_CUDA, std::string("batch kernel failed: ") + cudaGetErrorString(e));
+    int64_t off = 0;
+    for (int w = 0; w < n_walk; ++w) {
+        if (n_epi[w] > 0) {
+            if (!result || !result[w]) return batch_fail(SPH_ERR_ARG, "null result pointer");
+            std::memcpy(result[w], ts.h_out + sizeof(RES) * off, sizeof(RES) * n_epi[w]);
+        }
+        off += n_epi[w];
+    }
+    return SPH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *sph_batch_last_error(void) { return g_batch_err.c_str(); }
+
+int sph_dispatch_dens(int tag, int n_walk, const sph_epi_dens **epi, const int *n_epi, const sph_epj_dens **epj,
+                      const int *n_epj) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    TagState *ts = nullptr;
+    SPH_TRY((stage<sph_epi_dens, sph_epj_dens, sph_result_dens>(tag, 0, n_walk, epi, n_epi, epj, n_epj, nullptr,
+                                                                nullptr, &ts)));
+    if (n_walk > 0) {
+        int64_t ni = 0;
+        for (int w = 0; w < n_walk; ++w) ni += n_epi[w];
+        const size_t o_epj = (sizeof(sph_epi_dens) * ni + 15) & ~size_t(15);
+        k_walk_dens<<<n_walk, WT, 0, ts->stream>>>(ts->d_meta, (const sph_epi_dens *)ts->d_in,
+                                                   (const sph_epj_dens *)(ts->d_in + o_epj),
+                                                   (sph_result_dens *)ts->d_out);
+    }
+    return finish_dispatch(ts);
+}
+
+int sph_retrieve_dens(int tag, int n_walk, const int *n_epi, sph_result_dens **result) {
+    return retrieve<sph_result_dens>(tag, 0, n_walk, n_epi, result);
+}
+
+int sph_dispatch_drvt(int tag, int n_walk, const sph_epi_drvt **epi, const int *n_epi, const sph_epj_drvt **epj,
+                      const int *n_epj) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    TagState *ts = nullptr;
+    SPH_TRY((stage<sph_epi_drvt, sph_epj_drvt, sph_result_drvt>(tag, 1, n_walk, epi, n_epi, epj, n_epj, nullptr,
+                                                                nullptr, &ts)));
+    if (n_walk > 0) {
+        int64_t ni = 0;
+        for (int w = 0; w < n_walk; ++w) ni += n_epi[w];
+        const size_t o_epj = (sizeof(sph_epi_drvt) * ni + 15) & ~size_t(15);
+        k_walk_drvt<<<n_walk, WT, 0, ts->stream>>>(ts->d_meta, (const sph_epi_drvt *)ts->d_in,
+                                                   (const sph_epj_drvt *)(ts->d_in + o_epj),
+                                                   (sph_result_drvt *)ts->d_out);
+    }
+    return finish_dispatch(ts);
+}
+
+int sph_retrieve_drvt(int tag, int n_walk, const int *n_epi, sph_result_drvt **result) {
+    return retrieve<sph_result_drvt>(tag, 1, n_walk, n_epi, result);
+}
+
+int sph_dispatch_hydro(int tag, int n_walk, const sph_epi_hydro **epi, const int *n_epi, const sph_epj_hydro **epj,
+                       const int *n_epj) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    TagState *ts = nullptr;
+    SPH_TRY((stage<sph_epi_hydro, sph_epj_hydro, sph_result_hydro>(tag, 2, n_walk, epi, n_epi, epj, n_epj, nullptr,
+                                                                   nullptr, &ts)));
+    if (n_walk > 0) {
+        int64_t ni = 0;
+        for (int w = 0; w < n_walk; ++w) ni += n_epi[w];
+        const size_t o_epj = (sizeof(sph_epi_hydro) * ni + 15) & ~size_t(15);
+        k_walk_hydro<<<n_walk, WT, 0, ts->stream>>>(ts->d_meta, (const sph_epi_hydro *)ts->d_in,
+                                                    (const sph_epj_hydro *)(ts->d_in + o_epj),
+                                                    (sph_result_hydro *)ts->d_out);
+    }
+    return finish_dispatch(ts);
+}
+
+int sph_retrieve_hydro(int tag, int n_walk, const int *n_epi, sph_result_hydro **result) {
+    return retrieve<sph_result_hydro>(tag, 2, n_walk, n_epi, result);
+}
+
+int sph_dispatch_grav(int tag, int n_walk, const sph_epi_grav **epi, const int *n_epi, const sph_epj_grav **epj,
+                      const int *n_epj, const sph_spj_monopole **spj, const int *n_spj) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    TagState *ts = nullptr;
+    SPH_TRY((stage<sph_epi_grav, sph_epj_grav, sph_result_grav>(tag, 3, n_walk, epi, n_epi, epj, n_epj, spj, n_spj,
+                                                                &ts)));
+    if (n_walk > 0) {
+        int64_t ni = 0, nj = 0;
+        for (int w = 0; w < n_walk; ++w) {
+            ni += n_epi[w];
+            nj += n_epj[w];
+        }
+        const size_t o_epj = (sizeof(sph_epi_grav) * ni + 15) & ~size_t(15);
+        const size_t o_spj = (o_epj + sizeof(sph_epj_grav) * nj + 15) & ~size_t(15);
+        k_walk_grav<<<n_walk, WT, 0, ts->stream>>>(ts->d_meta, (const sph_epi_grav *)ts->d_in,
+                                                   (const sph_epj_grav *)(ts->d_in + o_epj),
+                                                   (const sph_spj_monopole *)(ts->d_in + o_spj),
+                                                   (sph_result_grav *)ts->d_out);
+    }
+    return finish_dispatch(ts);
+}
+
+int sph_retrieve_grav(int tag, int n_walk, const int *n_epi, sph_result_grav **result) {
+    return retrieve<sph_result_grav>(tag, 3, n_walk, n_epi, result);
+}
+
+}  // extern "C"

@@ -1,0 +1,183 @@
+// Internal declarations shared by the translation units of libsph_gb300.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/sph_gb300.h"
+
+namespace sph {
+
+constexpr int KEY_LEVELS = 21;           // 3 x 21-bit Morton key
+constexpr int MAX_LEVELS = KEY_LEVELS + 1;
+constexpr int MAX_MATERIALS = 16;
+constexpr double SUPPORT = 2.5;          // kernel.h:36-38
+constexpr double SMTH_COEF = 1.2;        // param.h:9
+constexpr double C_CFL = 0.3;            // param.h:10
+constexpr double AV_STRENGTH = 1.0;      // param.h:17
+constexpr double DENS_FLOOR = 5.0;       // force.h:18-20 (FLAG_GI)
+
+// device-side error word bits
+constexpr int ERR_SPH_LIST_OVERFLOW = 1;
+constexpr int ERR_CELL_OVERFLOW = 2;
+constexpr int ERR_GRAV_OVERFLOW = 4;
+constexpr int ERR_NONFINITE = 8;
+
+struct DevMaterial {
+    int kind;            // 0 table, 1 Tillotson, 2 ideal gas, -1 unset
+    int n_rho, n_u, pad;
+    const double *rho, *u, *pres, *snds;
+    double par[10];
+};
+
+// tree meta block (ints): level l cells are [meta[l], meta[l+1]) for l = 0..21;
+// meta[MAX_LEVELS] = total cells, META_ERR = error bits.
+constexpr int META_N = 64;
+constexpr int META_ERR = 40;
+constexpr int META_NGROUP = 41;
+constexpr int META_MAXCNT = 42;   // max SPH neighbour count seen by the last list build
+constexpr int META_NEPJ = 43;     // total gravity EPJ entries
+constexpr int META_NSPJ = 44;     // total gravity SPJ entries
+
+struct Tree {
+    int64_t cap = 0;
+    int *start = nullptr, *count = nullptr, *level = nullptr, *first_child = nullptr, *n_child = nullptr,
+        *parent = nullptr;
+    double4 *mom = nullptr;   // (m x, m y, m z, m)
+    double4 *com = nullptr;   // (com x, y, z, m)
+    float4 *blo = nullptr;    // bbox lower corner (rounded down), .w unused
+    float4 *bhi = nullptr;    // bbox upper corner (rounded up), .w = hmax (rounded up)
+    int *tmp_cnt = nullptr, *tmp_off = nullptr, *tmp_b = nullptr;
+    int *meta = nullptr;      // device [META_N]
+    double *rb = nullptr;     // device: root_lo[3], root_len, scale, rc2[MAX_LEVELS] at [8..]
+    int n_cell_host = 0;
+};
+
+struct Sort {
+    int64_t cap = 0;
+    uint64_t *k0 = nullptr, *k1 = nullptr;
+    uint32_t *v0 = nullptr, *v1 = nullptr;
+    uint32_t *hist = nullptr;   // [256 * nblocks]
+    uint32_t *hoff = nullptr;
+    int nblocks_cap = 0;
+};
+
+struct SphLists {
+    int64_t pitch = 0;   // >= n, multiple of 32
+    int K = 0;           // capacity per particle
+    int K_alloc = 0;     // allocated capacity per particle
+    int *nbr = nullptr;  // [K * pitch]
+    int *cnt = nullptr;  // [pitch]
+    bool valid = false;
+};
+
+struct GravLists {
+    int64_t cap_groups = 0, cap_epj = 0, cap_spj = 0;
+    int *group_cell = nullptr;   // [ng]
+    int *is_group = nullptr;     // [cell cap] scratch
+    int *n_epj = nullptr, *n_spj = nullptr;          // [ng]
+    int *off_epj = nullptr, *off_spj = nullptr;      // [ng]
+    int *epj = nullptr, *spj = nullptr;
+    int ng = 0;
+    int64_t tot_epj = 0, tot_spj = 0;
+    bool valid = false;
+};
+
+struct Scan {
+    int *part = nullptr;   // [SCAN_BLOCKS + 1]
+    int *total = nullptr;  // device int
+};
+
+}  // namespace sph
+
+struct sph_ctx {
+    sph_config cfg;
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+
+    int64_t n = 0, cap = 0;
+    double *F = nullptr, *F2 = nullptr;     // [SPH_NFIELD][cap] master state in sorted order
+    int64_t *id = nullptr, *id2 = nullptr;
+    int32_t *slot = nullptr, *slot2 = nullptr;
+    int32_t *mat = nullptr, *mat2 = nullptr;
+    uint64_t *keys = nullptr;               // sorted keys of the current order
+    double *scratch_d = nullptr;            // reductions [64]
+    double *host_scalars = nullptr;         // pinned [64]
+
+    // mixed-precision packed copies (double-float hi/lo)
+    float4 *xh = nullptr, *xl = nullptr, *vhf = nullptr, *vlf = nullptr;
+
+    sph::DevMaterial mats_host[sph::MAX_MATERIALS];
+    std::vector<void *> table_allocs;
+    sph::DevMaterial *mats_dev = nullptr;
+
+    sph::Tree tree;
+    sph::Sort sort;
+    sph::SphLists lists[2];
+    sph::GravLists grav;
+    sph::Scan scan;
+
+    double mscale = 1.0;   // power of two ~ 1 / particle mass, keeps FP32 pair sums near unity
+
+    double time = 0.0, dt = 0.0;
+    int64_t step = 0;
+    bool uploaded = false;
+    bool have_forces = false;
+
+    cudaEvent_t ev[32];
+    int n_ev = 0;
+    std::vector<double> timings;
+    bool timing = false;
+};
+
+// ---------------------------------------------------------------------------
+// host helpers (sph_api.cu)
+int sph_fail(sph_ctx *ctx, int code, const char *fmt, ...);
+#define SPH_CUDA(ctx, call)                                                                                 \
+    do {                                                                                                    \
+        cudaError_t e_ = (call);                                                                            \
+        if (e_ != cudaSuccess) return sph_fail((ctx), SPH_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, #call, \
+                                               cudaGetErrorString(e_));                                    \
+    } while (0)
+#define SPH_TRY(x)                \
+    do {                          \
+        int rc_ = (x);            \
+        if (rc_ != SPH_OK) return rc_; \
+    } while (0)
+
+// tree / sort (sph_tree.cu)
+int sph_tree_reserve(sph_ctx *ctx, int64_t n);
+int sph_sort_and_build(sph_ctx *ctx);          // root box, keys, sort, permute, octree, moments
+int sph_tree_refresh_hmax(sph_ctx *ctx);       // cell hmax after h changed
+int sph_scan_exclusive(sph_ctx *ctx, const int *in, int *out, const int *len_dev, int len_host, int *total_dev);
+
+// lists (sph_lists.cu)
+int sph_build_sph_lists(sph_ctx *ctx, int mode);
+int sph_build_grav_lists(sph_ctx *ctx);
+
+// passes (sph_pairs.cu)
+int sph_pass_density(sph_ctx *ctx);
+int sph_pass_eos(sph_ctx *ctx);
+int sph_pass_derivative(sph_ctx *ctx);
+int sph_pass_hydro(sph_ctx *ctx);
+int sph_pass_gravity(sph_ctx *ctx);
+int sph_pack_mixed(sph_ctx *ctx);
+int sph_kick_drift_predict(sph_ctx *ctx, double dt);
+int sph_final_kick(sph_ctx *ctx, double dt);
+int sph_ext_force(sph_ctx *ctx);
+int sph_dt_global(sph_ctx *ctx, double *dt_out);
+int sph_diag(sph_ctx *ctx, double out[8]);
+int sph_init_smth(sph_ctx *ctx);
+
+// ---------------------------------------------------------------------------
+// device helpers
+
+static inline int sph_div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+
+#define FLD(ptr, f, cap) ((ptr) + (int64_t)(f) * (cap))

@@ -1,0 +1,854 @@
+// Pair-interaction passes, EoS, integrator and reductions.
+//
+// FP64 path: one thread per i-particle over its exact neighbour list (ELL),
+// arithmetic as in the reference functors (force.h:9-23, 89-106, 113-147,
+// 154-168); j is summed in ascending key order, the order the oracle uses.
+//
+// Mixed path (SPH_PREC_MIXED): the same lists and epilogues, with the pair
+// arithmetic in FP32 on double-float positions / velocities (hi + lo floats,
+// so x_i - x_j is formed without FP64 arithmetic), partial sums of at most
+// 32 neighbours (SPH) or one 128-entry tile (gravity) accumulated in FP32 and
+// flushed into FP64 accumulators.  Epilogues (density floor, h update,
+// grad-h normalisation, Balsara, dt), the EoS, the integrator and every
+// reduction stay in FP64.
+#include "sph_physics.cuh"
+
+namespace sph {
+
+constexpr int PT = 128;   // threads per block for per-particle kernels
+
+// ---------------------------------------------------------------------------
+// FP64 density, CalcDensity (force.h:9-23) + FLAG_GI floor + h update
+
+__global__ void __launch_bounds__(PT) k_density64(int n, const double *__restrict__ x, const double *__restrict__ y,
+                                                  const double *__restrict__ z, const double *__restrict__ m,
+                                                  double *__restrict__ h, double *__restrict__ dens,
+                                                  const int *__restrict__ nbr, const int *__restrict__ cnt,
+                                                  int64_t pitch) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double xi = x[i], yi = y[i], zi = z[i], hi = h[i];
+    const double H = SUPPORT * hi;
+    const double invH = 1.0 / H;
+    const double norm = kernel_norm(H);
+    const int c = cnt[i];
+    double sum = 0.0;
+    for (int k = 0; k < c; ++k) {
+        const int j = nbr[(int64_t)k * pitch + i];
+        const double dx = x[j] - xi, dy = y[j] - yi, dz = z[j] - zi;
+        const double r = sqrt(dx * dx + dy * dy + dz * dz);
+        double w, g;
+        wendland_poly(r * invH, w, g);
+        sum += m[j] * w;
+    }
+    const double d = fmax(DENS_FLOOR, sum * norm);
+    dens[i] = d;
+    h[i] = SMTH_COEF * pow(m[i] / d, 1.0 / 3.0);
+}
+
+// ---------------------------------------------------------------------------
+// EoS, CalcPressure (force.h:26-32)
+
+__global__ void k_eos(int n, const DevMaterial *__restrict__ mats, const int32_t *__restrict__ mat,
+                      const double *__restrict__ dens, const double *__restrict__ eng, double *__restrict__ pres,
+                      double *__restrict__ snds) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double P, cs;
+    eos_eval(mats[mat[i]], dens[i], eng[i], P, cs);
+    pres[i] = P;
+    snds[i] = cs;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 derivative, CalcDerivative (force.h:89-106) + Balsara (class.h:132-142)
+
+struct DrvtArgs {
+    const double *x, *y, *z, *vx, *vy, *vz, *m, *h, *dens, *snds;
+    double *divv, *rx, *ry, *rz, *gradh, *bal;
+    const int *nbr, *cnt;
+    int64_t pitch;
+};
+
+__global__ void __launch_bounds__(PT) k_drvt64(int n, DrvtArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double xi = a.x[i], yi = a.y[i], zi = a.z[i], ux = a.vx[i], uy = a.vy[i], uz = a.vz[i];
+    const double hi = a.h[i], rhoi = a.dens[i];
+    const double H = SUPPORT * hi, invH = 1.0 / H, norm = kernel_norm(H), ceps = 1.0e-6 * hi;
+    double dv = 0.0, r0 = 0.0, r1 = 0.0, r2 = 0.0, gs = 0.0;
+    const int c = a.cnt[i];
+    for (int k = 0; k < c; ++k) {
+        const int j = a.nbr[(int64_t)k * a.pitch + i];
+        const double dx = xi - a.x[j], dy = yi - a.y[j], dz = zi - a.z[j];
+        const double mj = a.m[j];
+        const double ax = -mj * (ux - a.vx[j]), ay = -mj * (uy - a.vy[j]), az = -mj * (uz - a.vz[j]);
+        const double rr2 = dx * dx + dy * dy + dz * dz;
+        const double r = sqrt(rr2);
+        double w, g;
+        wendland_poly(r * invH, w, g);
+        const double gf = norm * g / (r * H + ceps);     // gradW = dr * gf (kernel.h:22-34)
+        dv += gf * (ax * dx + ay * dy + az * dz);
+        r0 += gf * (ay * dz - az * dy);
+        r1 += gf * (az * dx - ax * dz);
+        r2 += gf * (ax * dy - ay * dx);
+        gs += mj * (3.0 * norm * w + gf * rr2);
+    }
+    gs = -gs / hi;
+    gs = 1.0 / (1.0 + hi * gs / (3.0 * rhoi));
+    dv /= rhoi;
+    r0 /= rhoi;
+    r1 /= rhoi;
+    r2 /= rhoi;
+    a.divv[i] = dv;
+    a.rx[i] = r0;
+    a.ry[i] = r1;
+    a.rz[i] = r2;
+    a.gradh[i] = gs;
+    a.bal[i] = fabs(dv) / (fabs(dv) + sqrt(r0 * r0 + r1 * r1 + r2 * r2) + 1.0e-4 * a.snds[i] / hi);
+}
+
+// ---------------------------------------------------------------------------
+// FP64 hydro, CalcHydroForce (force.h:113-147)
+
+struct HydroArgs {
+    const double *x, *y, *z, *vx, *vy, *vz, *m, *h, *dens, *pres, *snds, *gradh, *bal;
+    const double4 *aux;   // per particle: invH, norm, 1e-6 h, f P / rho^2
+    double *ax, *ay, *az, *edot, *dt;
+    const int *nbr, *cnt;
+    int64_t pitch;
+};
+
+__global__ void k_hydro_aux64(int n, const double *h, const double *dens, const double *pres, const double *gradh,
+                              double4 *aux) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double hi = h[i], H = SUPPORT * hi;
+    aux[i] = make_double4(1.0 / H, kernel_norm(H), 1.0e-6 * hi, gradh[i] * pres[i] / (dens[i] * dens[i]));
+}
+
+__global__ void __launch_bounds__(PT) k_hydro64(int n, HydroArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double xi = a.x[i], yi = a.y[i], zi = a.z[i], ux = a.vx[i], uy = a.vy[i], uz = a.vz[i];
+    const double hi = a.h[i], rhoi = a.dens[i], ci = a.snds[i], fi = a.gradh[i], bi = a.bal[i];
+    const double4 ai = a.aux[i];
+    const double Hi = SUPPORT * hi;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, e = 0.0, vmax = 0.0;
+    const int c = a.cnt[i];
+    for (int k = 0; k < c; ++k) {
+        const int j = a.nbr[(int64_t)k * a.pitch + i];
+        const double dx = xi - a.x[j], dy = yi - a.y[j], dz = zi - a.z[j];
+        const double wx = ux - a.vx[j], wy = uy - a.vy[j], wz = uz - a.vz[j];
+        const double rr2 = dx * dx + dy * dy + dz * dz;
+        const double r = sqrt(rr2);
+        const double dvdr = wx * dx + wy * dy + wz * dz;
+        const double w = (dvdr < 0) ? dvdr / r : 0.0;
+        const double vsig = ci + a.snds[j] - 3.0 * w;
+        vmax = fmax(vmax, vsig);
+        const double4 aj = a.aux[j];
+        const double AV = -AV_STRENGTH * 0.5 * vsig * w / (0.5 * (rhoi + a.dens[j])) * 0.5 * (bi + a.bal[j]);
+        double wi_, gi_, wj_, gj_;
+        wendland_poly(r * ai.x, wi_, gi_);
+        wendland_poly(r * aj.x, wj_, gj_);
+        const double Hj = SUPPORT * a.h[j];
+        const double gfi = ai.y * gi_ / (r * Hi + ai.z);
+        const double gfj = aj.y * gj_ / (r * Hj + aj.z);
+        const double gws = 0.5 * (gfi * fi + gfj * a.gradh[j]);
+        const double mj = a.m[j];
+        const double coef = mj * (ai.w * gfi + aj.w * gfj + AV * gws);
+        a0 -= coef * dx;
+        a1 -= coef * dy;
+        a2 -= coef * dz;
+        e += mj * (ai.w + 0.5 * AV) * gws * dvdr;
+    }
+    a.ax[i] = a0;
+    a.ay[i] = a1;
+    a.az[i] = a2;
+    a.edot[i] = e;
+    a.dt[i] = C_CFL * 2.0 * hi / vmax;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 gravity, CalcGravityForce<EPJ> then <SPJMonopole> (force.h:154-168)
+
+constexpr int GT = 128;
+
+__global__ void __launch_bounds__(GT) k_grav64(const int *__restrict__ group_cell, const int *__restrict__ cstart,
+                                               const int *__restrict__ ccount, const double *__restrict__ x,
+                                               const double *__restrict__ y, const double *__restrict__ z,
+                                               const double *__restrict__ m, const double *__restrict__ h,
+                                               const double4 *__restrict__ com, const int *__restrict__ n_epj,
+                                               const int *__restrict__ off_epj, const int *__restrict__ epj,
+                                               const int *__restrict__ n_spj, const int *__restrict__ off_spj,
+                                               const int *__restrict__ spj, double G, double *gx, double *gy,
+                                               double *gz, double *pot) {
+    __shared__ double4 tile[GT];
+    const int g = blockIdx.x;
+    const int gc = group_cell[g];
+    const int s = cstart[gc], cnt = ccount[gc];
+    const int ne = n_epj[g], ns = n_spj[g];
+    const int *E = epj + off_epj[g];
+    const int *S = spj + off_spj[g];
+    for (int i0 = 0; i0 < cnt; i0 += GT) {
+        const int i = s + i0 + threadIdx.x;
+        const bool act = i0 + threadIdx.x < cnt;
+        const double xi = act ? x[i] : 0.0, yi = act ? y[i] : 0.0, zi = act ? z[i] : 0.0;
+        const double eps2 = act ? h[i] * h[i] : 1.0;
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0, p = 0.0;
+        for (int t0 = 0; t0 < ne; t0 += GT) {
+            const int k = t0 + threadIdx.x;
+            if (k < ne) {
+                const int j = E[k];
+                tile[threadIdx.x] = make_double4(x[j], y[j], z[j], m[j]);
+            }
+            __syncthreads();
+            const int tn = min(GT, ne - t0);
+            for (int t = 0; t < tn; ++t) {
+                const double4 q = tile[t];
+                const double dx = xi - q.x, dy = yi - q.y, dz = zi - q.z;
+                const double dri = 1.0 / sqrt(dx * dx + dy * dy + dz * dz + eps2);
+                const double mdr3 = q.w * (dri * dri * dri);
+                a0 -= G * mdr3 * dx;
+                a1 -= G * mdr3 * dy;
+                a2 -= G * mdr3 * dz;
+                p -= G * q.w * dri;
+            }
+            __syncthreads();
+        }
+        for (int t0 = 0; t0 < ns; t0 += GT) {
+            const int k = t0 + threadIdx.x;
+            if (k < ns) tile[threadIdx.x] = com[S[k]];
+            __syncthreads();
+            const int tn = min(GT, ns - t0);
+            for (int t = 0; t < tn; ++t) {
+                const double4 q = tile[t];
+                const double dx = xi - q.x, dy = yi - q.y, dz = zi - q.z;
+                const double dri = 1.0 / sqrt(dx * dx + dy * dy + dz * dz + eps2);
+                const double mdr3 = q.w * (dri * dri * dri);
+                a0 -= G * mdr3 * dx;
+                a1 -= G * mdr3 * dy;
+                a2 -= G * mdr3 * dz;
+                p -= G * q.w * dri;
+            }
+            __syncthreads();
+        }
+        if (act) {
+            gx[i] = a0;
+            gy[i] = a1;
+            gz[i] = a2;
+            pot[i] = p;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Mixed precision: double-float packing
+
+__device__ __forceinline__ void split_df(double v, float &hi, float &lo) {
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+}
+
+// positions + scaled mass, velocities + h; called after the sort (and h refresh)
+__global__ void k_pack_df(int n, const double *x, const double *y, const double *z, const double *vx,
+                          const double *vy, const double *vz, const double *m, const double *h, double mscale,
+                          float4 *xh, float4 *xl, float4 *vh, float4 *vl) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float a, b, c, d, e, f;
+    split_df(x[i], a, d);
+    split_df(y[i], b, e);
+    split_df(z[i], c, f);
+    xh[i] = make_float4(a, b, c, (float)(m[i] * mscale));
+    xl[i] = make_float4(d, e, f, (float)h[i]);
+    split_df(vx[i], a, d);
+    split_df(vy[i], b, e);
+    split_df(vz[i], c, f);
+    vh[i] = make_float4(a, b, c, 0.0f);
+    vl[i] = make_float4(d, e, f, 0.0f);
+}
+
+__device__ __forceinline__ float df_diff(float ah, float al, float bh, float bl) { return (ah - bh) + (al - bl); }
+
+// mixed density
+__global__ void __launch_bounds__(PT) k_density32(int n, const float4 *__restrict__ xh, const float4 *__restrict__ xl,
+                                                  const double *__restrict__ m, double *__restrict__ h,
+                                                  double *__restrict__ dens, const int *__restrict__ nbr,
+                                                  const int *__restrict__ cnt, int64_t pitch, double inv_mscale) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 pih = xh[i], pil = xl[i];
+    const double hi = h[i];
+    const double H = SUPPORT * hi;
+    const float invH = (float)(1.0 / H);
+    const double norm = kernel_norm(H);
+    const int c = cnt[i];
+    double acc = 0.0;
+    float part = 0.0f;
+    for (int k = 0; k < c; ++k) {
+        const int j = nbr[(int64_t)k * pitch + i];
+        const float4 qh = xh[j], ql = xl[j];
+        const float dx = df_diff(qh.x, ql.x, pih.x, pil.x);
+        const float dy = df_diff(qh.y, ql.y, pih.y, pil.y);
+        const float dz = df_diff(qh.z, ql.z, pih.z, pil.z);
+        const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+        float w, g;
+        wendland_poly_f(r * invH, w, g);
+        part = fmaf(qh.w, w, part);
+        if ((k & 31) == 31) {
+            acc += (double)part;
+            part = 0.0f;
+        }
+    }
+    acc += (double)part;
+    const double d = fmax(DENS_FLOOR, acc * inv_mscale * norm);
+    dens[i] = d;
+    h[i] = SMTH_COEF * pow(m[i] / d, 1.0 / 3.0);
+}
+
+// mixed derivative
+struct DrvtArgs32 {
+    const float4 *xh, *xl, *vh, *vl;
+    const double *h, *dens, *snds;
+    double *divv, *rx, *ry, *rz, *gradh, *bal;
+    const int *nbr, *cnt;
+    int64_t pitch;
+    double inv_mscale;
+};
+
+__global__ void __launch_bounds__(PT) k_drvt32(int n, DrvtArgs32 a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 pih = a.xh[i], pil = a.xl[i], vih = a.vh[i], vil = a.vl[i];
+    const double hi = a.h[i], rhoi = a.dens[i];
+    const double H = SUPPORT * hi;
+    const double normd = kernel_norm(H);
+    const float invH = (float)(1.0 / H), Hf = (float)H, ceps = (float)(1.0e-6 * hi);
+    // kernel normalisation folded out: sums carry norm = 1, restored in FP64
+    double D[5] = {0, 0, 0, 0, 0};
+    float P[5] = {0, 0, 0, 0, 0};
+    const int c = a.cnt[i];
+    for (int k = 0; k < c; ++k) {
+        const int j = a.nbr[(int64_t)k * a.pitch + i];
+        const float4 qh = a.xh[j], ql = a.xl[j], uh = a.vh[j], ul = a.vl[j];
+        const float dx = df_diff(pih.x, pil.x, qh.x, ql.x);
+        const float dy = df_diff(pih.y, pil.y, qh.y, ql.y);
+        const float dz = df_diff(pih.z, pil.z, qh.z, ql.z);
+        const float wx = df_diff(vih.x, vil.x, uh.x, ul.x);
+        const float wy = df_diff(vih.y, vil.y, uh.y, ul.y);
+        const float wz = df_diff(vih.z, vil.z, uh.z, ul.z);
+        const float rr2 = dx * dx + dy * dy + dz * dz;
+        const float r = sqrtf(rr2);
+        float w, g;
+        wendland_poly_f(r * invH, w, g);
+        const float gf = g / (r * Hf + ceps);
+        const float mg = -qh.w * gf;
+        P[0] = fmaf(mg, wx * dx + wy * dy + wz * dz, P[0]);
+        P[1] = fmaf(mg, wy * dz - wz * dy, P[1]);
+        P[2] = fmaf(mg, wz * dx - wx * dz, P[2]);
+        P[3] = fmaf(mg, wx * dy - wy * dx, P[3]);
+        P[4] = fmaf(qh.w, 3.0f * w + gf * rr2, P[4]);
+        if ((k & 31) == 31) {
+#pragma unroll
+            for (int q = 0; q < 5; ++q) {
+                D[q] += (double)P[q];
+                P[q] = 0.0f;
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 5; ++q) D[q] = (D[q] + (double)P[q]) * normd * a.inv_mscale;
+    double gs = -D[4] / hi;
+    gs = 1.0 / (1.0 + hi * gs / (3.0 * rhoi));
+    const double dv = D[0] / rhoi, r0 = D[1] / rhoi, r1 = D[2] / rhoi, r2 = D[3] / rhoi;
+    a.divv[i] = dv;
+    a.rx[i] = r0;
+    a.ry[i] = r1;
+    a.rz[i] = r2;
+    a.gradh[i] = gs;
+    a.bal[i] = fabs(dv) / (fabs(dv) + sqrt(r0 * r0 + r1 * r1 + r2 * r2) + 1.0e-4 * a.snds[i] / hi);
+}
+
+// mixed hydro: per-particle FP32 packs hA = (f P / rho^2, c_s, f, Bal), hB = (rho, 1/H, H, 1e-6 h).
+// The i-particle's kernel normalisation is factored out of the FP32 sums and
+// applied in FP64; the j-particle's enters as the ratio (H_i / H_j)^3.
+__global__ void k_hydro_pack32(int n, const double *h, const double *dens, const double *pres, const double *snds,
+                               const double *gradh, const double *bal, float4 *hA, float4 *hB) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double hi = h[i], H = SUPPORT * hi, rho = dens[i];
+    hA[i] = make_float4((float)(gradh[i] * pres[i] / (rho * rho)), (float)snds[i], (float)gradh[i], (float)bal[i]);
+    hB[i] = make_float4((float)rho, (float)(1.0 / H), (float)H, (float)(1.0e-6 * hi));
+}
+
+struct HydroArgs32 {
+    const float4 *xh, *xl, *vh, *vl, *hA, *hB;
+    const double *h;
+    double *ax, *ay, *az, *edot, *dt;
+    const int *nbr, *cnt;
+    int64_t pitch;
+    double inv_mscale;
+};
+
+__global__ void __launch_bounds__(PT) k_hydro32(int n, HydroArgs32 a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 pih = a.xh[i], pil = a.xl[i], vih = a.vh[i], vil = a.vl[i];
+    const float4 Ai = a.hA[i], Bi = a.hB[i];
+    const double hi = a.h[i];
+    const double normd = kernel_norm(SUPPORT * hi);
+    double D[4] = {0, 0, 0, 0};
+    float P[4] = {0, 0, 0, 0};
+    float vmax = 0.0f;
+    const int c = a.cnt[i];
+    for (int k = 0; k < c; ++k) {
+        const int j = a.nbr[(int64_t)k * a.pitch + i];
+        const float4 qh = a.xh[j], ql = a.xl[j], uh = a.vh[j], ul = a.vl[j];
+        const float4 Aj = a.hA[j], Bj = a.hB[j];
+        const float dx = df_diff(pih.x, pil.x, qh.x, ql.x);
+        const float dy = df_diff(pih.y, pil.y, qh.y, ql.y);
+        const float dz = df_diff(pih.z, pil.z, qh.z, ql.z);
+        const float wx = df_diff(vih.x, vil.x, uh.x, ul.x);
+        const float wy = df_diff(vih.y, vil.y, uh.y, ul.y);
+        const float wz = df_diff(vih.z, vil.z, uh.z, ul.z);
+        const float rr2 = dx * dx + dy * dy + dz * dz;
+        const float r = sqrtf(rr2);
+        const float dvdr = wx * dx + wy * dy + wz * dz;
+        const float w = (dvdr < 0.0f) ? dvdr / r : 0.0f;
+        const float vsig = Ai.y + Aj.y - 3.0f * w;
+        vmax = fmaxf(vmax, vsig);
+        const float AV = -0.5f * vsig * w / (0.5f * (Bi.x + Bj.x)) * 0.5f * (Ai.w + Aj.w);
+        float wi_, gi_, wj_, gj_;
+        wendland_poly_f(r * Bi.y, wi_, gi_);
+        wendland_poly_f(r * Bj.y, wj_, gj_);
+        const float nr = Bi.z * Bj.y;
+        const float gfi = gi_ / (r * Bi.z + Bi.w);
+        const float gfj = (nr * nr * nr) * gj_ / (r * Bj.z + Bj.w);
+        const float gws = 0.5f * (gfi * Ai.z + gfj * Aj.z);
+        const float coef = qh.w * (Ai.x * gfi + Aj.x * gfj + AV * gws);
+        P[0] = fmaf(-coef, dx, P[0]);
+        P[1] = fmaf(-coef, dy, P[1]);
+        P[2] = fmaf(-coef, dz, P[2]);
+        P[3] = fmaf(qh.w * (Ai.x + 0.5f * AV) * gws, dvdr, P[3]);
+        if ((k & 31) == 31) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                D[q] += (double)P[q];
+                P[q] = 0.0f;
+            }
+        }
+    }
+    const double sc = normd * a.inv_mscale;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) D[q] = (D[q] + (double)P[q]) * sc;
+    a.ax[i] = D[0];
+    a.ay[i] = D[1];
+    a.az[i] = D[2];
+    a.edot[i] = D[3];
+    a.dt[i] = C_CFL * 2.0 * hi / (double)vmax;
+}
+
+// cell monopoles as double-float with G folded into the mass
+__global__ void k_pack_cells32(const int *meta, const double4 *com, double G, double gscale, float4 *ch, float4 *cl) {
+    const int nc = meta[MAX_LEVELS];
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        const double4 q = com[c];
+        float a, b, cc, d, e, f;
+        split_df(q.x, a, d);
+        split_df(q.y, b, e);
+        split_df(q.z, cc, f);
+        ch[c] = make_float4(a, b, cc, (float)(G * q.w * gscale));
+        cl[c] = make_float4(d, e, f, 0.0f);
+    }
+}
+
+__global__ void __launch_bounds__(GT) k_grav32(const int *__restrict__ group_cell, const int *__restrict__ cstart,
+                                               const int *__restrict__ ccount, const float4 *__restrict__ xh,
+                                               const float4 *__restrict__ xl, const double *__restrict__ m,
+                                               const double *__restrict__ h, const float4 *__restrict__ ch,
+                                               const float4 *__restrict__ cl, const int *__restrict__ n_epj,
+                                               const int *__restrict__ off_epj, const int *__restrict__ epj,
+                                               const int *__restrict__ n_spj, const int *__restrict__ off_spj,
+                                               const int *__restrict__ spj, double G, double gscale,
+                                               double inv_gscale, double *gx, double *gy, double *gz,
+                                               double *pot) {
+    __shared__ float4 tile[GT];
+    const int g = blockIdx.x;
+    const int gc = group_cell[g];
+    const int s = cstart[gc], cnt = ccount[gc];
+    const int ne = n_epj[g], ns = n_spj[g];
+    const int *E = epj + off_epj[g];
+    const int *S = spj + off_spj[g];
+    const float4 c_h = xh[s], c_l = xl[s];     // group origin (its first particle)
+    for (int i0 = 0; i0 < cnt; i0 += GT) {
+        const int i = s + i0 + threadIdx.x;
+        const bool act = i0 + threadIdx.x < cnt;
+        float xi = 0.f, yi = 0.f, zi = 0.f, eps2 = 1.f;
+        if (act) {
+            const float4 ph = xh[i], pl = xl[i];
+            xi = df_diff(ph.x, pl.x, c_h.x, c_l.x);
+            yi = df_diff(ph.y, pl.y, c_h.y, c_l.y);
+            zi = df_diff(ph.z, pl.z, c_h.z, c_l.z);
+            const double hh = h[i];
+            eps2 = (float)(hh * hh);
+        }
+        double D[4] = {0, 0, 0, 0};
+        for (int pass = 0; pass < 2; ++pass) {
+            const int nl = pass == 0 ? ne : ns;
+            for (int t0 = 0; t0 < nl; t0 += GT) {
+                const int k = t0 + threadIdx.x;
+                if (k < nl) {
+                    float4 qh, ql;
+                    float gm;
+                    if (pass == 0) {
+                        const int j = E[k];
+                        qh = xh[j];
+                        ql = xl[j];
+                        gm = (float)(G * m[j] * gscale);
+                    } else {
+                        const int cc = S[k];
+                        qh = ch[cc];
+                        ql = cl[cc];
+                        gm = qh.w;
+                    }
+                    tile[threadIdx.x] = make_float4(df_diff(qh.x, ql.x, c_h.x, c_l.x), df_diff(qh.y, ql.y, c_h.y, c_l.y),
+                                                    df_diff(qh.z, ql.z, c_h.z, c_l.z), gm);
+                }
+                __syncthreads();
+                const int tn = min(GT, nl - t0);
+                float P0 = 0.f, P1 = 0.f, P2 = 0.f, P3 = 0.f;
+                for (int t = 0; t < tn; ++t) {
+                    const float4 q = tile[t];
+                    const float dx = xi - q.x, dy = yi - q.y, dz = zi - q.z;
+                    const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+                    const float ri = rsqrtf(r2);
+                    const float mri = q.w * ri;
+                    const float mr3 = mri * ri * ri;
+                    P0 = fmaf(-mr3, dx, P0);
+                    P1 = fmaf(-mr3, dy, P1);
+                    P2 = fmaf(-mr3, dz, P2);
+                    P3 -= mri;
+                }
+                D[0] += (double)P0;
+                D[1] += (double)P1;
+                D[2] += (double)P2;
+                D[3] += (double)P3;
+                __syncthreads();
+            }
+        }
+        if (act) {
+            gx[i] = D[0] * inv_gscale;
+            gy[i] = D[1] * inv_gscale;
+            gz[i] = D[2] * inv_gscale;
+            pot[i] = D[3] * inv_gscale;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// integrator (class.h:201-229), external damping (GI.h:458-465), dt (integral.h:4-20)
+
+struct IntegArgs {
+    double *x, *y, *z, *vx, *vy, *vz, *ax, *ay, *az, *gx, *gy, *gz, *vhx, *vhy, *vhz, *u, *ud, *uh;
+};
+
+__global__ void k_kick_drift_predict(int n, IntegArgs a, double dt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double ax = a.ax[i] + a.gx[i], ay = a.ay[i] + a.gy[i], az = a.az[i] + a.gz[i];
+    const double hx = a.vx[i] + 0.5 * dt * ax, hy = a.vy[i] + 0.5 * dt * ay, hz = a.vz[i] + 0.5 * dt * az;
+    a.vhx[i] = hx;
+    a.vhy[i] = hy;
+    a.vhz[i] = hz;
+    a.uh[i] = a.u[i] + 0.5 * dt * a.ud[i];
+    a.x[i] += dt * hx;
+    a.y[i] += dt * hy;
+    a.z[i] += dt * hz;
+    a.vx[i] += dt * ax;
+    a.vy[i] += dt * ay;
+    a.vz[i] += dt * az;
+    a.u[i] += dt * a.ud[i];
+}
+
+__global__ void k_final_kick(int n, IntegArgs a, double dt, double damp) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    a.vx[i] = (a.vhx[i] + 0.5 * dt * (a.ax[i] + a.gx[i])) * damp;
+    a.vy[i] = (a.vhy[i] + 0.5 * dt * (a.ay[i] + a.gy[i])) * damp;
+    a.vz[i] = (a.vhz[i] + 0.5 * dt * (a.az[i] + a.gz[i])) * damp;
+    a.u[i] = a.uh[i] + 0.5 * dt * a.ud[i];
+}
+
+__global__ void k_ext_force(int n, IntegArgs a, const double *dt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double d = dt[i];
+    a.ax[i] += -a.vx[i] * 0.05 / d;
+    a.ay[i] += -a.vy[i] * 0.05 / d;
+    a.az[i] += -a.vz[i] * 0.05 / d;
+}
+
+constexpr int RED_BLOCKS = 304;
+
+__global__ void k_min_partial(int n, const double *v, double *part) {
+    double r = 1.0e30;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double d = v[i];
+        r = (d < r) ? d : r;   // std::min(r, d) with r first, integral.h:16
+        if (d != d) r = d;     // a NaN dt propagates so the host sees it
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const double t = __shfl_xor_sync(0xffffffffu, r, o);
+        r = (t < r || t != t) ? t : r;
+    }
+    __shared__ double s[32];
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = r;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) r = (s[w] < r || s[w] != s[w]) ? s[w] : r;
+        part[blockIdx.x] = r;
+    }
+}
+
+__global__ void k_min_final(const double *part, int nb, double *out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double r = 1.0e30;
+        for (int b = 0; b < nb; ++b) r = (part[b] < r || part[b] != part[b]) ? part[b] : r;
+        *out = r;
+    }
+}
+
+// conserved quantities, fixed-order two-stage reduction in FP64
+__global__ void k_diag_partial(int n, const double *x, const double *y, const double *z, const double *vx,
+                               const double *vy, const double *vz, const double *m, const double *u,
+                               const double *pot, double *part) {
+    double q[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double mi = m[i];
+        const double v2 = vx[i] * vx[i] + vy[i] * vy[i] + vz[i] * vz[i];
+        q[0] += mi * (u[i] + 0.5 * v2 + 0.5 * pot[i]);
+        q[1] += mi * vx[i];
+        q[2] += mi * vy[i];
+        q[3] += mi * vz[i];
+        q[4] += mi * (y[i] * vz[i] - z[i] * vy[i]);
+        q[5] += mi * (z[i] * vx[i] - x[i] * vz[i]);
+        q[6] += mi * (x[i] * vy[i] - y[i] * vx[i]);
+        q[7] += mi;
+    }
+    __shared__ double s[8][32];
+    for (int k = 0; k < 8; ++k) {
+        double v = q[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) s[k][threadIdx.x >> 5] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 8) {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += s[threadIdx.x][w];
+        part[blockIdx.x * 8 + threadIdx.x] = v;
+    }
+}
+
+__global__ void k_diag_final(const double *part, int nb, double *out) {
+    if (threadIdx.x < 8 && blockIdx.x == 0) {
+        double v = 0.0;
+        for (int b = 0; b < nb; ++b) v += part[b * 8 + threadIdx.x];
+        out[threadIdx.x] = v;
+    }
+}
+
+__global__ void k_init_smth(int n, const double *m, const double *dens, double *h, double *gradh) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    h[i] = SMTH_COEF * pow(m[i] / dens[i], 1.0 / 3.0);
+    gradh[i] = 1.0;
+}
+
+}  // namespace sph
+
+using namespace sph;
+
+#define CF(f) FLD(ctx->F, f, ctx->cap)
+
+static IntegArgs integ_args(sph_ctx *ctx) {
+    return IntegArgs{CF(SPH_X),  CF(SPH_Y),  CF(SPH_Z),  CF(SPH_VX),  CF(SPH_VY),  CF(SPH_VZ),
+                     CF(SPH_AX), CF(SPH_AY), CF(SPH_AZ), CF(SPH_GX),  CF(SPH_GY),  CF(SPH_GZ),
+                     CF(SPH_VHX), CF(SPH_VHY), CF(SPH_VHZ), CF(SPH_ENG), CF(SPH_ENGDOT), CF(SPH_ENGHALF)};
+}
+
+static int ensure_mixed_buffers(sph_ctx *ctx) {
+    if (ctx->xh) return SPH_OK;
+    const size_t b = sizeof(float4) * (size_t)ctx->cap;
+    float4 **bufs[] = {&ctx->xh, &ctx->xl, &ctx->vhf, &ctx->vlf};
+    for (auto p : bufs)
+        if (cudaMalloc((void **)p, b) != cudaSuccess) {
+            cudaGetLastError();
+            return sph_fail(ctx, SPH_ERR_OOM, "mixed-precision buffers");
+        }
+    return SPH_OK;
+}
+
+int sph_pack_mixed(sph_ctx *ctx) {
+    SPH_TRY(ensure_mixed_buffers(ctx));
+    const int n = (int)ctx->n;
+    k_pack_df<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, CF(SPH_X), CF(SPH_Y), CF(SPH_Z), CF(SPH_VX), CF(SPH_VY),
+                                                           CF(SPH_VZ), CF(SPH_MASS), CF(SPH_SMTH),
+                                                           ctx->mscale, ctx->xh, ctx->xl, ctx->vhf,
+                                                           ctx->vlf);
+    SPH_CUDA(ctx, cudaGetLastError());
+    return SPH_OK;
+}
+
+int sph_pass_density(sph_ctx *ctx) {
+    SPH_TRY(sph_build_sph_lists(ctx, 0));
+    const int n = (int)ctx->n;
+    const SphLists &L = ctx->lists[0];
+    if (ctx->cfg.precision == SPH_PREC_MIXED) {
+        k_density32<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, ctx->xh, ctx->xl, CF(SPH_MASS), CF(SPH_SMTH),
+                                                              CF(SPH_DENS), L.nbr, L.cnt, L.pitch,
+                                                              1.0 / ctx->mscale);
+    } else {
+        k_density64<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, CF(SPH_X), CF(SPH_Y), CF(SPH_Z), CF(SPH_MASS),
+                                                              CF(SPH_SMTH), CF(SPH_DENS), L.nbr, L.cnt, L.pitch);
+    }
+    SPH_CUDA(ctx, cudaGetLastError());
+    return SPH_OK;
+}
+
+int sph_pass_eos(sph_ctx *ctx) {
+    const int n = (int)ctx->n;
+    k_eos<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, ctx->mats_dev, ctx->mat, CF(SPH_DENS), CF(SPH_ENG),
+                                                    CF(SPH_PRES), CF(SPH_SNDS));
+    SPH_CUDA(ctx, cudaGetLastError());
+    return SPH_OK;
+}
+
+int sph_pass_derivative(sph_ctx *ctx) {
+    SPH_TRY(sph_build_sph_lists(ctx, 0));
+    const int n = (int)ctx->n;
+    const SphLists &L = ctx->lists[0];
+    if (ctx->cfg.precision == SPH_PREC_MIXED) {
+        DrvtArgs32 a{ctx->xh,     ctx->xl,      ctx->vhf,     ctx->vlf,      CF(SPH_SMTH), CF(SPH_DENS),
+                     CF(SPH_SNDS), CF(SPH_DIVV), CF(SPH_ROTX), CF(SPH_ROTY),  CF(SPH_ROTZ), CF(SPH_GRADH),
+                     CF(SPH_BAL),  L.nbr,        L.cnt,        L.pitch,       1.0 / ctx->mscale};
+        k_drvt32<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, a);
+    } else {
+        DrvtArgs a{CF(SPH_X),    CF(SPH_Y),    CF(SPH_Z),    CF(SPH_VX),    CF(SPH_VY),   CF(SPH_VZ),
+                   CF(SPH_MASS), CF(SPH_SMTH), CF(SPH_DENS), CF(SPH_SNDS),  CF(SPH_DIVV), CF(SPH_ROTX),
+                   CF(SPH_ROTY), CF(SPH_ROTZ), CF(SPH_GRADH), CF(SPH_BAL), L.nbr,        L.cnt,
+                   L.pitch};
+        k_drvt64<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, a);
+    }
+    SPH_CUDA(ctx, cudaGetLastError());
+    return SPH_OK;
+}
+
+int sph_pass_hydro(sph_ctx *ctx) {
+    SPH_TRY(sph_tree_refresh_hmax(ctx));
+    SPH_TRY(sph_build_sph_lists(ctx, 1));
+    const int n = (int)ctx->n;
+    const SphLists &L = ctx->lists[1];
+    // scratch: 2 x float4 or 1 x double4 per particle, in the F2 ping-pong block (free between sorts)
+    if (ctx->cfg.precision == SPH_PREC_MIXED) {
+        float4 *hA = (float4 *)ctx->F2, *hB = hA + ctx->cap;
+        k_hydro_pack32<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, CF(SPH_SMTH), CF(SPH_DENS), CF(SPH_PRES),
+                                                                    CF(SPH_SNDS), CF(SPH_GRADH), CF(SPH_BAL), hA, hB);
+        HydroArgs32 a{ctx->xh,    ctx->xl,    ctx->vhf,   ctx->vlf,       hA,         hB,    CF(SPH_SMTH),
+                      CF(SPH_AX), CF(SPH_AY), CF(SPH_AZ), CF(SPH_ENGDOT), CF(SPH_DT), L.nbr, L.cnt,
+                      L.pitch,    1.0 / ctx->mscale};
+        k_hydro32<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, a);
+    } else {
+        double4 *aux = (double4 *)ctx->F2;
+        k_hydro_aux64<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, CF(SPH_SMTH), CF(SPH_DENS), CF(SPH_PRES),
+                                                                   CF(SPH_GRADH), aux);
+        HydroArgs a{CF(SPH_X),    CF(SPH_Y),    CF(SPH_Z),     CF(SPH_VX),   CF(SPH_VY),  CF(SPH_VZ),
+                    CF(SPH_MASS), CF(SPH_SMTH), CF(SPH_DENS),  CF(SPH_PRES), CF(SPH_SNDS), CF(SPH_GRADH),
+                    CF(SPH_BAL),  aux,          CF(SPH_AX),    CF(SPH_AY),   CF(SPH_AZ),  CF(SPH_ENGDOT),
+                    CF(SPH_DT),   L.nbr,        L.cnt,         L.pitch};
+        k_hydro64<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, a);
+    }
+    SPH_CUDA(ctx, cudaGetLastError());
+    return SPH_OK;
+}
+
+int sph_pass_gravity(sph_ctx *ctx) {
+    SPH_TRY(sph_build_grav_lists(ctx));
+    GravLists &G = ctx->grav;
+    Tree &t = ctx->tree;
+    if (G.ng == 0) return SPH_OK;
+    if (ctx->cfg.precision == SPH_PREC_MIXED) {
+        // cell monopoles as double-float in the F2 scratch block (2 float4 per cell fit in 4 fields)
+        if ((int64_t)t.n_cell_host * 2 > ctx->cap * 4) return sph_fail(ctx, SPH_ERR_CAPACITY, "cell pack scratch");
+        float4 *ch = (float4 *)ctx->F2, *cl = ch + t.n_cell_host;
+        const double gscale = 1.0;
+        k_pack_cells32<<<2 * ctx->num_sms, 256, 0, ctx->stream>>>(t.meta, t.com, ctx->cfg.G, gscale, ch, cl);
+        k_grav32<<<G.ng, GT, 0, ctx->stream>>>(G.group_cell, t.start, t.count, ctx->xh, ctx->xl, CF(SPH_MASS),
+                                               CF(SPH_SMTH), ch, cl, G.n_epj, G.off_epj, G.epj, G.n_spj, G.off_spj,
+                                               G.spj, ctx->cfg.G, gscale, 1.0 / gscale, CF(SPH_GX), CF(SPH_GY),
+                                               CF(SPH_GZ), CF(SPH_POT));
+    } else {
+        k_grav64<<<G.ng, GT, 0, ctx->stream>>>(G.group_cell, t.start, t.count, CF(SPH_X), CF(SPH_Y), CF(SPH_Z),
+                                               CF(SPH_MASS), CF(SPH_SMTH), t.com, G.n_epj, G.off_epj, G.epj, G.n_spj,
+                                               G.off_spj, G.spj, ctx->cfg.G, CF(SPH_GX), CF(SPH_GY), CF(SPH_GZ),
+                                               CF(SPH_POT));
+    }
+    SPH_CUDA(ctx, cudaGetLastError());
+    return SPH_OK;
+}
+
+int sph_kick_drift_predict(sph_ctx *ctx, double dt) {
+    const int n = (int)ctx->n;
+    k_kick_drift_predict<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, integ_args(ctx), dt);
+    SPH_CUDA(ctx, cudaGetLastError());
+    return SPH_OK;
+}
+
+int sph_final_kick(sph_ctx *ctx, double dt) {
+    const int n = (int)ctx->n;
+    k_final_kick<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, integ_args(ctx), dt, ctx->cfg.damping);
+    SPH_CUDA(ctx, cudaGetLastError());
+    return SPH_OK;
+}
+
+int sph_ext_force(sph_ctx *ctx) {
+    if (!ctx->cfg.ext_damp || ctx->time >= ctx->cfg.ext_damp_tend) return SPH_OK;
+    const int n = (int)ctx->n;
+    k_ext_force<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, integ_args(ctx), CF(SPH_DT));
+    SPH_CUDA(ctx, cudaGetLastError());
+    return SPH_OK;
+}
+
+int sph_dt_global(sph_ctx *ctx, double *dt_out) {
+    const int n = (int)ctx->n;
+    k_min_partial<<<RED_BLOCKS, 256, 0, ctx->stream>>>(n, CF(SPH_DT), ctx->scratch_d);
+    k_min_final<<<1, 32, 0, ctx->stream>>>(ctx->scratch_d, RED_BLOCKS, ctx->scratch_d + RED_BLOCKS * 8);
+    SPH_CUDA(ctx, cudaMemcpyAsync(ctx->host_scalars, ctx->scratch_d + RED_BLOCKS * 8, sizeof(double),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+    SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    *dt_out = ctx->host_scalars[0];
+    if (!(*dt_out > 0.0) || !isfinite(*dt_out))
+        return sph_fail(ctx, SPH_ERR_NONFINITE, "global dt is not a positive finite number (%g)", *dt_out);
+    return SPH_OK;
+}
+
+int sph_diag(sph_ctx *ctx, double out[8]) {
+    const int n = (int)ctx->n;
+    k_diag_partial<<<RED_BLOCKS, 256, 0, ctx->stream>>>(n, CF(SPH_X), CF(SPH_Y), CF(SPH_Z), CF(SPH_VX), CF(SPH_VY),
+                                                        CF(SPH_VZ), CF(SPH_MASS), CF(SPH_ENG), CF(SPH_POT),
+                                                        ctx->scratch_d);
+    k_diag_final<<<1, 32, 0, ctx->stream>>>(ctx->scratch_d, RED_BLOCKS, ctx->scratch_d + RED_BLOCKS * 8);
+    SPH_CUDA(ctx, cudaMemcpyAsync(ctx->host_scalars, ctx->scratch_d + RED_BLOCKS * 8, 8 * sizeof(double),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+    SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int k = 0; k < 8; ++k) out[k] = ctx->host_scalars[k];
+    return SPH_OK;
+}
+
+int sph_init_smth(sph_ctx *ctx) {
+    const int n = (int)ctx->n;
+    k_init_smth<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, CF(SPH_MASS), CF(SPH_DENS), CF(SPH_SMTH),
+                                                             CF(SPH_GRADH));
+    SPH_CUDA(ctx, cudaGetLastError());
+    return SPH_OK;
+}

@@ -1,0 +1,133 @@
+// Device restatements of the reference's per-particle physics: Wendland C6
+// kernel (kernel.h:8-34), EoS lookups (EoS.h:241-247, 394-400 through
+// interpolation.h:33-102) and analytic Tillotson.
+#pragma once
+
+#include "sph_internal.cuh"
+
+namespace sph {
+
+constexpr double PI_D = 3.141592653589793;         // math::pi = atan(1) * 4 (mathfunc.h:4)
+constexpr double WNORM = 1365.0 / 64.0;            // kernel.h:15
+
+// (1365/64) / (H^3 pi) with H = 2.5 h
+__device__ __forceinline__ double kernel_norm(double H) { return WNORM / (H * H * H * PI_D); }
+
+// W / norm and (gradW / norm) / dr-factor pieces for s = r / H
+__device__ __forceinline__ void wendland_poly(double s, double &w, double &g) {
+    const double p = fmax(1.0 - s, 0.0);
+    const double poly = 1.0 + s * (8.0 + s * (25.0 + s * 32.0));
+    const double p2 = p * p;
+    const double p3 = p2 * p;
+    const double p7 = p3 * p3 * p;
+    w = poly * (p7 * p);
+    g = p7 * (p * (8.0 + s * (50.0 + s * 96.0)) - 8.0 * poly);
+}
+
+__device__ __forceinline__ void wendland_poly_f(float s, float &w, float &g) {
+    const float p = fmaxf(1.0f - s, 0.0f);
+    const float poly = 1.0f + s * (8.0f + s * (25.0f + s * 32.0f));
+    const float p2 = p * p;
+    const float p3 = p2 * p;
+    const float p7 = p3 * p3 * p;
+    w = poly * (p7 * p);
+    g = p7 * (p * (8.0f + s * (50.0f + s * 96.0f)) - 8.0f * poly);
+}
+
+// std::lower_bound over an ascending axis
+__device__ __forceinline__ int lower_bound_d(const double *ax, int n, double v) {
+    int lo = 0, len = n;
+    while (len > 0) {
+        const int half = len >> 1;
+        if (ax[lo + half] < v) {
+            lo += half + 1;
+            len -= half + 1;
+        } else {
+            len = half;
+        }
+    }
+    return lo;
+}
+
+// BilinearInterpolation::interpolate for two planes at once (same bracket)
+__device__ __forceinline__ void table_lookup2(const DevMaterial &m, double rho, double u, double &P, double &cs) {
+    int li = lower_bound_d(m.rho, m.n_rho, rho);
+    int ci = lower_bound_d(m.u, m.n_u, u);
+    if (li > m.n_rho - 1) li = m.n_rho - 1;
+    if (ci > m.n_u - 1) ci = m.n_u - 1;
+    const int64_t nu = m.n_u;
+    if (li < m.n_rho - 1 && ci < m.n_u - 1 && li > 0 && ci > 0) {
+        const double r0 = m.rho[li - 1], r1 = m.rho[li], u0 = m.u[ci - 1], u1 = m.u[ci];
+        const double xi = (rho - r0) / (r1 - r0);
+        const double eta = (u - u0) / (u1 - u0);
+        const int64_t a = (int64_t)(li - 1) * nu + (ci - 1), b = (int64_t)li * nu + (ci - 1);
+        const int64_t c = (int64_t)(li - 1) * nu + ci, d = (int64_t)li * nu + ci;
+        const double w00 = (1 - xi) * (1 - eta), w10 = xi * (1 - eta), w01 = (1 - xi) * eta, w11 = xi * eta;
+        P = w00 * m.pres[a] + w10 * m.pres[b] + w01 * m.pres[c] + w11 * m.pres[d];
+        cs = w00 * m.snds[a] + w10 * m.snds[b] + w01 * m.snds[c] + w11 * m.snds[d];
+    } else {
+        const int64_t a = (int64_t)li * nu + ci;
+        P = m.pres[a];
+        cs = m.snds[a];
+    }
+}
+
+// analytic Tillotson, same expressions as the oracle's or_tillotson
+__device__ __forceinline__ void tillotson(const double *p, double rho, double u, double &P, double &cs) {
+    const double rho0 = p[0], u0 = p[1], uiv = p[2], ucv = p[3], A = p[4], B = p[5], a = p[6], b = p[7],
+                 alpha = p[8], beta = p[9];
+    const double eta = rho / rho0;
+    const double mu = eta - 1.0;
+    const double om = u / (u0 * eta * eta) + 1.0;
+    const double Pc = (a + b / om) * rho * u + A * mu + B * mu * mu;
+    const double dPc_drho = (a + b / om) * u + 2.0 * b * u * (om - 1.0) / (om * om) + (A + 2.0 * B * mu) / rho0;
+    const double dPc_du = (a + b / om) * rho - rho * b * (om - 1.0) / (om * om);
+    double Pv, dPdrho, dPdu;
+    if (rho >= rho0 || u <= uiv) {
+        Pv = Pc;
+        dPdrho = dPc_drho;
+        dPdu = dPc_du;
+    } else {
+        const double z = rho0 / rho - 1.0;
+        const double E1 = exp(-alpha * z);
+        const double E2 = exp(-beta * z * z);
+        const double Q = b * rho * u / om + A * mu * E1;
+        const double Pe = a * rho * u + Q * E2;
+        const double dQ = b * u / om + 2.0 * b * u * (om - 1.0) / (om * om) + A / rho0 * E1 +
+                          A * mu * alpha * E1 * (z + 1.0) / rho;
+        const double dPe_drho = a * u + dQ * E2 + Q * 2.0 * beta * z * (z + 1.0) * E2 / rho;
+        const double dPe_du = a * rho + E2 * (b * rho / om - b * rho * (om - 1.0) / (om * om));
+        if (u >= ucv) {
+            Pv = Pe;
+            dPdrho = dPe_drho;
+            dPdu = dPe_du;
+        } else {
+            const double w = ucv - uiv;
+            Pv = ((u - uiv) * Pe + (ucv - u) * Pc) / w;
+            dPdrho = ((u - uiv) * dPe_drho + (ucv - u) * dPc_drho) / w;
+            dPdu = (Pe - Pc + (u - uiv) * dPe_du + (ucv - u) * dPc_du) / w;
+        }
+    }
+    double c2 = dPdrho + Pv / (rho * rho) * dPdu;
+    const double c2min = 1.0e-2 * A / rho0;
+    if (!(c2 > c2min)) c2 = c2min;
+    P = Pv;
+    cs = sqrt(c2);
+}
+
+__device__ __forceinline__ void eos_eval(const DevMaterial &m, double rho, double u, double &P, double &cs) {
+    if (m.kind == 0) {
+        table_lookup2(m, rho, u, P, cs);
+    } else if (m.kind == 1) {
+        tillotson(m.par, rho, u, P, cs);
+    } else if (m.kind == 2) {
+        const double g = m.par[0];
+        P = (g - 1.0) * rho * u;
+        cs = sqrt(g * (g - 1.0) * u);
+    } else {
+        P = nan("");
+        cs = nan("");
+    }
+}
+
+}  // namespace sph

@@ -1,0 +1,311 @@
+"""ctypes binding of libsph_gb300.so (the C ABI declared in include/sph_gb300.h).
+
+The product path: every call here goes to the CUDA library; there is no CPU
+fallback.  If the library is missing or no GPU is present, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import types as T
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libsph_gb300.so")
+
+NFIELD = 32
+FIELDS = [
+    "x", "y", "z", "vx", "vy", "vz", "mass", "smth", "dens", "eng",
+    "pres", "snds", "div_v", "rot_x", "rot_y", "rot_z", "bal", "ava", "grad_smth",
+    "ax", "ay", "az", "eng_dot", "vhx", "vhy", "vhz", "eng_half", "dt",
+    "gx", "gy", "gz", "pot",
+]
+FIELD = {n: i for i, n in enumerate(FIELDS)}
+
+SPH_OK = 0
+ERRORS = {-1: "SPH_ERR_ARG", -2: "SPH_ERR_CUDA", -3: "SPH_ERR_OOM", -4: "SPH_ERR_TABLE", -5: "SPH_ERR_NONFINITE",
+          -6: "SPH_ERR_CAPACITY", -7: "SPH_ERR_STATE", -8: "SPH_ERR_TIMEOUT"}
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+EXPORTS = [
+    "sph_dispatch_dens", "sph_retrieve_dens", "sph_dispatch_drvt", "sph_retrieve_drvt",
+    "sph_dispatch_hydro", "sph_retrieve_hydro", "sph_dispatch_grav", "sph_retrieve_grav",
+    "sph_batch_last_error", "sph_config_default", "sph_ctx_create", "sph_ctx_destroy", "sph_last_error",
+    "sph_set_eos_table", "sph_load_eos_table_file", "sph_set_eos_tillotson", "sph_upload", "sph_download",
+    "sph_prologue", "sph_step", "sph_get_time", "sph_diagnostics", "sph_run_pass", "sph_get_order",
+    "sph_get_neighbors", "sph_get_tree", "sph_get_grav_list", "sph_get_timings",
+]
+
+
+class SphError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Config(C.Structure):
+    _fields_ = [
+        ("theta", C.c_double), ("n_leaf", C.c_int32), ("n_group", C.c_int32), ("n_dens_iter", C.c_int32),
+        ("self_gravity", C.c_int32), ("ext_damp", C.c_int32), ("precision", C.c_int32),
+        ("ext_damp_tend", C.c_double), ("damping", C.c_double), ("G", C.c_double), ("device", C.c_int32),
+        ("reserved", C.c_int32),
+    ]
+
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Loads the in-tree library (built by fdps_sph_gb300.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: run fdps_sph_gb300.build.build() (nvcc, sm_103a)")
+    L = C.CDLL(LIB_PATH)
+    P = C.c_void_p
+    i32p = C.POINTER(C.c_int)
+    for k in ("dens", "drvt", "hydro"):
+        getattr(L, f"sph_dispatch_{k}").argtypes = [C.c_int, C.c_int, P, i32p, P, i32p]
+        getattr(L, f"sph_retrieve_{k}").argtypes = [C.c_int, C.c_int, i32p, P]
+    L.sph_dispatch_grav.argtypes = [C.c_int, C.c_int, P, i32p, P, i32p, P, i32p]
+    L.sph_retrieve_grav.argtypes = [C.c_int, C.c_int, i32p, P]
+    L.sph_batch_last_error.restype = C.c_char_p
+    L.sph_config_default.argtypes = [C.POINTER(Config)]
+    L.sph_config_default.restype = None
+    L.sph_ctx_create.argtypes = [C.POINTER(Config), C.POINTER(C.c_void_p)]
+    L.sph_ctx_destroy.argtypes = [P]
+    L.sph_last_error.argtypes = [P]
+    L.sph_last_error.restype = C.c_char_p
+    L.sph_set_eos_table.argtypes = [P, C.c_int, P, C.c_int, P, C.c_int, P, P]
+    L.sph_load_eos_table_file.argtypes = [P, C.c_int, C.c_char_p]
+    L.sph_set_eos_tillotson.argtypes = [P, C.c_int, P]
+    L.sph_upload.argtypes = [P, C.c_int64, P, C.c_int64, P, P, C.c_double, C.c_int]
+    L.sph_download.argtypes = [P, P, C.c_int64, P, P]
+    L.sph_prologue.argtypes = [P]
+    L.sph_step.argtypes = [P, C.c_int]
+    L.sph_get_time.argtypes = [P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int64)]
+    L.sph_diagnostics.argtypes = [P, P]
+    L.sph_run_pass.argtypes = [P, C.c_int]
+    L.sph_get_order.argtypes = [P, P, P]
+    L.sph_get_neighbors.argtypes = [P, C.c_int, C.c_int64, P, C.c_int64, C.POINTER(C.c_int64)]
+    L.sph_get_tree.argtypes = [P, C.POINTER(C.c_int64), P, P, P, P, P]
+    L.sph_get_grav_list.argtypes = [P, C.c_int64, C.POINTER(C.c_int64), P, C.c_int64, C.POINTER(C.c_int64), P, P,
+                                    C.c_int64, C.POINTER(C.c_int64), P, P]
+    L.sph_get_timings.argtypes = [P, P, C.c_int, C.POINTER(C.c_int)]
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def default_config(**kw) -> Config:
+    cfg = Config()
+    load().sph_config_default(C.byref(cfg))
+    for k, v in kw.items():
+        if k == "precision" and isinstance(v, str):
+            v = {"fp64": PREC_FP64, "mixed": PREC_MIXED}[v]
+        setattr(cfg, k, v)
+    return cfg
+
+
+class Context:
+    """A device-resident run: C ABI context owning the particle state in HBM."""
+
+    def __init__(self, config: Config | None = None, **kw):
+        self.L = load()
+        cfg = config if config is not None else default_config(**kw)
+        h = C.c_void_p()
+        rc = self.L.sph_ctx_create(C.byref(cfg), C.byref(h))
+        if rc != SPH_OK:
+            raise SphError(rc, "sph_ctx_create failed (no CUDA device?)")
+        self.h = h
+        self.cfg = cfg
+        self.n = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.sph_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != SPH_OK:
+            raise SphError(rc, self.L.sph_last_error(self.h).decode())
+
+    # EoS ------------------------------------------------------------------
+    def set_material(self, k: int, mat):
+        d = mat.as_material() if hasattr(mat, "as_material") else mat
+        if d["kind"] == "table":
+            rho = np.ascontiguousarray(d["rho"], np.float64)
+            u = np.ascontiguousarray(d["u"], np.float64)
+            P = np.ascontiguousarray(d["pres"], np.float64)
+            cs = np.ascontiguousarray(d["snds"], np.float64)
+            self._check(self.L.sph_set_eos_table(self.h, k, _ptr(rho), len(rho), _ptr(u), len(u), _ptr(P), _ptr(cs)))
+        elif d["kind"] == "tillotson":
+            par = np.ascontiguousarray(d["par"], np.float64)
+            self._check(self.L.sph_set_eos_tillotson(self.h, k, _ptr(par)))
+        else:
+            raise ValueError(d["kind"])
+
+    def load_table_file(self, k: int, path: str):
+        self._check(self.L.sph_load_eos_table_file(self.h, k, path.encode()))
+
+    # state ----------------------------------------------------------------
+    def upload(self, F: np.ndarray, ids=None, mats=None, time=0.0, init_smth=False):
+        F = np.ascontiguousarray(F, np.float64)
+        assert F.shape[0] == NFIELD
+        n = F.shape[1]
+        ids = None if ids is None else np.ascontiguousarray(ids, np.int64)
+        mats = None if mats is None else np.ascontiguousarray(mats, np.int32)
+        self._check(self.L.sph_upload(self.h, n, _ptr(F), n, _ptr(ids), _ptr(mats), float(time), int(init_smth)))
+        self.n = n
+
+    def download(self, out: np.ndarray | None = None):
+        if out is None:
+            out = np.empty((NFIELD, self.n), np.float64)
+        ids = np.empty(self.n, np.int64)
+        mats = np.empty(self.n, np.int32)
+        self._check(self.L.sph_download(self.h, _ptr(out), out.shape[1], _ptr(ids), _ptr(mats)))
+        return out, ids, mats
+
+    def prologue(self):
+        self._check(self.L.sph_prologue(self.h))
+
+    def step(self, n_steps=1):
+        self._check(self.L.sph_step(self.h, int(n_steps)))
+
+    def time(self):
+        t, dt, st = C.c_double(), C.c_double(), C.c_int64()
+        self._check(self.L.sph_get_time(self.h, C.byref(t), C.byref(dt), C.byref(st)))
+        return t.value, dt.value, st.value
+
+    def diagnostics(self):
+        out = np.zeros(8)
+        self._check(self.L.sph_diagnostics(self.h, _ptr(out)))
+        return out
+
+    # inspection -------------------------------------------------------------
+    def run_pass(self, p: int):
+        self._check(self.L.sph_run_pass(self.h, int(p)))
+
+    def order(self):
+        slot = np.empty(self.n, np.int32)
+        keys = np.empty(self.n, np.uint64)
+        self._check(self.L.sph_get_order(self.h, _ptr(slot), _ptr(keys)))
+        return slot, keys
+
+    def neighbors(self, mode: int, k: int):
+        n = C.c_int64()
+        buf = np.empty(4096, np.int32)
+        self._check(self.L.sph_get_neighbors(self.h, mode, int(k), _ptr(buf), len(buf), C.byref(n)))
+        if n.value > len(buf):
+            buf = np.empty(n.value, np.int32)
+            self._check(self.L.sph_get_neighbors(self.h, mode, int(k), _ptr(buf), len(buf), C.byref(n)))
+        return buf[:n.value].copy()
+
+    def tree(self):
+        nc = C.c_int64()
+        self._check(self.L.sph_get_tree(self.h, C.byref(nc), None, None, None, None, None))
+        n = nc.value
+        start, count, level, nch = (np.empty(n, np.int32) for _ in range(4))
+        com = np.empty((n, 4), np.float64)
+        self._check(self.L.sph_get_tree(self.h, C.byref(nc), _ptr(start), _ptr(count), _ptr(level), _ptr(nch),
+                                        _ptr(com)))
+        return dict(start=start, count=count, level=level, n_child=nch, com=com)
+
+    def n_groups(self):
+        ng = C.c_int64()
+        self._check(self.L.sph_get_grav_list(self.h, -1, C.byref(ng), None, 0, None, None, None, 0, None, None,
+                                             None))
+        return ng.value
+
+    def grav_list(self, g: int):
+        ne, ns, ng = C.c_int64(), C.c_int64(), C.c_int64()
+        gs, gcnt = np.zeros(1, np.int32), np.zeros(1, np.int32)
+        self._check(self.L.sph_get_grav_list(self.h, g, C.byref(ng), None, 0, C.byref(ne), None, None, 0,
+                                             C.byref(ns), _ptr(gs), _ptr(gcnt)))
+        epj = np.empty(max(1, ne.value), np.int32)
+        lev = np.empty(max(1, ns.value), np.int32)
+        st = np.empty(max(1, ns.value), np.int32)
+        self._check(self.L.sph_get_grav_list(self.h, g, C.byref(ng), _ptr(epj), len(epj), C.byref(ne), _ptr(lev),
+                                             _ptr(st), len(st), C.byref(ns), _ptr(gs), _ptr(gcnt)))
+        return dict(start=int(gs[0]), count=int(gcnt[0]), epj=epj[:ne.value].copy(), spj_level=lev[:ns.value].copy(),
+                    spj_start=st[:ns.value].copy())
+
+    def enable_timing(self, on=True):
+        self._check(self.L.sph_get_timings(self.h, None, -1 if on else -2, None))
+
+    def timings(self):
+        buf = np.zeros(32)
+        n = C.c_int()
+        self._check(self.L.sph_get_timings(self.h, _ptr(buf), 32, C.byref(n)))
+        return buf[:n.value].copy()
+
+
+# ---------------------------------------------------------------------------
+# functor-compatible batch calls (MultiWalk dispatch / retrieve)
+
+_KINDS = {
+    "dens": (T.EPI_DENS, T.EPJ_DENS, T.RES_DENS),
+    "drvt": (T.EPI_DRVT, T.EPJ_DRVT, T.RES_DRVT),
+    "hydro": (T.EPI_HYDRO, T.EPJ_HYDRO, T.RES_HYDRO),
+    "grav": (T.EPI_GRAV, T.EPJ_GRAV, T.RES_GRAV),
+}
+
+
+def _ptr_array(arrs):
+    a = (C.c_void_p * max(1, len(arrs)))()
+    for k, x in enumerate(arrs):
+        a[k] = x.ctypes.data if len(x) else None
+    return a
+
+
+def dispatch(kind: str, tag: int, epi_list, epj_list, spj_list=None):
+    L = load()
+    n_walk = len(epi_list)
+    for e, (di, dj, _) in zip(epi_list, [_KINDS[kind]] * n_walk):
+        assert e.dtype == di
+    n_epi = (C.c_int * max(1, n_walk))(*[len(e) for e in epi_list])
+    n_epj = (C.c_int * max(1, n_walk))(*[len(e) for e in epj_list])
+    pe, pj = _ptr_array(epi_list), _ptr_array(epj_list)
+    if kind == "grav":
+        spj_list = spj_list if spj_list is not None else [np.zeros(0, T.SPJ_MONO)] * n_walk
+        n_spj = (C.c_int * max(1, n_walk))(*[len(s) for s in spj_list])
+        ps = _ptr_array(spj_list)
+        rc = L.sph_dispatch_grav(tag, n_walk, pe, n_epi, pj, n_epj, ps, n_spj)
+    else:
+        rc = getattr(L, f"sph_dispatch_{kind}")(tag, n_walk, pe, n_epi, pj, n_epj)
+    if rc != SPH_OK:
+        raise SphError(rc, L.sph_batch_last_error().decode())
+    return n_epi
+
+
+def retrieve(kind: str, tag: int, n_epi):
+    L = load()
+    res_dt = _KINDS[kind][2]
+    n_walk = len(n_epi) if hasattr(n_epi, "__len__") else 0
+    outs = [np.empty(n_epi[w], res_dt) for w in range(n_walk)]
+    pr = _ptr_array(outs)
+    rc = getattr(L, f"sph_retrieve_{kind}")(tag, n_walk, n_epi, pr)
+    if rc != SPH_OK:
+        raise SphError(rc, L.sph_batch_last_error().decode())
+    return outs
+
+
+def run_walks(kind: str, epi_list, epj_list, spj_list=None, tag: int = 0):
+    """dispatch + retrieve: the reference functor applied to each walk on the GPU."""
+    n_epi = dispatch(kind, tag, epi_list, epj_list, spj_list)
+    if len(epi_list) == 0:
+        return []
+    return retrieve(kind, tag, n_epi)

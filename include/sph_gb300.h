@@ -1,0 +1,185 @@
+/* sph_gb300.h -- C ABI of the GB300 implementation of FDPS_SPH's per-step
+ * interaction path (libsph_gb300.so).
+ *
+ * Two families of entry points:
+ *
+ *  1. Functor-compatible batch calls.  They take the reference's own
+ *     interaction payloads (src/class.h EPI/EPJ/RESULT layouts, all F64/S64)
+ *     and apply exactly the reference functor (src/force.h) to every "walk"
+ *     (one i-group with its j-list), the way FDPS's
+ *     calcForceAllAndWriteBackMultiWalk drives a dispatch / retrieve pair.
+ *     They replace the CPU loops inside
+ *       STD::CalcDensity::operator()      force.h:9-23
+ *       STD::CalcDerivative::operator()   force.h:89-106
+ *       STD::CalcHydroForce::operator()   force.h:113-147
+ *       STD::CalcGravityForce<T>::operator() force.h:154-168 (EPJ then SPJ)
+ *     at the call sites main.cpp:93,97,98,100-101,139,142,143,145-146.
+ *
+ *  2. Device-resident whole-pass calls.  Particle state lives in HBM; the
+ *     library builds the Morton-key octree, neighbour and interaction lists
+ *     on the device and runs the complete step of main.cpp:125-173
+ *     (kick-drift-predict, density x4, EoS, derivative + Balsara, hydro,
+ *     tree gravity, final kick, global dt).
+ *
+ * Every entry point returns an int status: SPH_OK (0) or a negative error
+ * code; sph_last_error() gives a message.  No C++ exception crosses the ABI.
+ * A context is used by one host thread at a time; different contexts are
+ * independent.
+ */
+#ifndef SPH_GB300_H
+#define SPH_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define SPH_OK 0
+#define SPH_ERR_ARG (-1)        /* bad argument (null pointer, negative size, unknown material ...) */
+#define SPH_ERR_CUDA (-2)       /* a CUDA runtime call failed */
+#define SPH_ERR_OOM (-3)        /* device or pinned allocation failed */
+#define SPH_ERR_TABLE (-4)      /* EoS table missing, malformed or not ascending */
+#define SPH_ERR_NONFINITE (-5)  /* non-finite state detected (positions, density, dt) */
+#define SPH_ERR_CAPACITY (-6)   /* a list or tree capacity was exceeded and could not be grown */
+#define SPH_ERR_STATE (-7)      /* call out of order (e.g. step before upload) */
+#define SPH_ERR_TIMEOUT (-8)    /* a bounded device wait gave up */
+
+/* ---- reference interaction payloads (src/class.h) ------------------------ */
+typedef struct { double pos[3]; double mass; double smth; int64_t id; } sph_epi_dens;        /* class.h:233-258, 48 B */
+typedef struct { double mass; double pos[3]; double smth; } sph_epj_dens;                    /* class.h:342-365, 40 B */
+typedef struct { double dens; double smth; } sph_result_dens;                                /* class.h:36-44, 16 B */
+
+typedef struct { double pos[3]; double vel[3]; double smth; double dens; } sph_epi_drvt;     /* class.h:260-281, 64 B */
+typedef struct { double mass; double pos[3]; double vel[3]; double smth; } sph_epj_drvt;     /* class.h:367-392, 64 B */
+typedef struct { double div_v; double rot_v[3]; double grad_smth; } sph_result_drvt;         /* class.h:47-58, 40 B */
+
+typedef struct {
+    double pos[3]; double vel[3]; double smth; double dens; double pres; double snds;
+    double grad_smth; double Bal; double AVa; int64_t id;
+} sph_epi_hydro;                                                                             /* class.h:283-315, 112 B */
+typedef struct {
+    double pos[3]; double vel[3]; double dens; double mass; double smth; double pres;
+    double grad_smth; double snds; double Bal; double AVa; int64_t id;
+} sph_epj_hydro;                                                                             /* class.h:394-432, 120 B */
+typedef struct { double acc[3]; double eng_dot; double dt; } sph_result_hydro;              /* class.h:61-72, 40 B */
+
+typedef struct { double pos[3]; double eps2; int64_t id; } sph_epi_grav;                     /* class.h:317-338, 40 B */
+typedef struct { double pos[3]; double mass; int64_t id; } sph_epj_grav;                     /* class.h:434-453, 40 B */
+typedef struct { double mass; double pos[3]; } sph_spj_monopole;                             /* FDPS SPJMonopole, 32 B */
+typedef struct { double acc[3]; double pot; double dt; } sph_result_grav;                    /* class.h:75-86, 40 B */
+
+/* ---- 1. functor-compatible batch entry points ----------------------------
+ * dispatch: copies the walks into pinned staging memory and launches
+ * asynchronously on the stream of `tag` (0 <= tag < 64).  retrieve: waits
+ * for that stream and writes result[w][0..n_epi[w]) for every walk.  Results
+ * are the reference functor's: RESULT::clear() (class.h:41-85) followed by
+ * the i x j loop over the walk's full j-list.  Return 0 on success, as
+ * FDPS's dispatch / retrieve callbacks do.  The signatures are those of the
+ * callbacks calcForceAllAndWriteBackMultiWalk takes for short-range
+ * (dens, drvt, hydro) and long-range (grav) trees. */
+int sph_dispatch_dens(int tag, int n_walk, const sph_epi_dens **epi, const int *n_epi,
+                      const sph_epj_dens **epj, const int *n_epj);
+int sph_retrieve_dens(int tag, int n_walk, const int *n_epi, sph_result_dens **result);
+int sph_dispatch_drvt(int tag, int n_walk, const sph_epi_drvt **epi, const int *n_epi,
+                      const sph_epj_drvt **epj, const int *n_epj);
+int sph_retrieve_drvt(int tag, int n_walk, const int *n_epi, sph_result_drvt **result);
+int sph_dispatch_hydro(int tag, int n_walk, const sph_epi_hydro **epi, const int *n_epi,
+                       const sph_epj_hydro **epj, const int *n_epj);
+int sph_retrieve_hydro(int tag, int n_walk, const int *n_epi, sph_result_hydro **result);
+int sph_dispatch_grav(int tag, int n_walk, const sph_epi_grav **epi, const int *n_epi,
+                      const sph_epj_grav **epj, const int *n_epj,
+                      const sph_spj_monopole **spj, const int *n_spj);
+int sph_retrieve_grav(int tag, int n_walk, const int *n_epi, sph_result_grav **result);
+/* message of the last failed batch call on this thread */
+const char *sph_batch_last_error(void);
+
+/* ---- 2. device-resident whole-pass API ----------------------------------- */
+
+/* Field-major particle block: field f of particle i is at fields[f * ld + i]
+ * (ld >= n).  Field order: */
+enum sph_field {
+    SPH_X = 0, SPH_Y, SPH_Z, SPH_VX, SPH_VY, SPH_VZ, SPH_MASS, SPH_SMTH, SPH_DENS, SPH_ENG,
+    SPH_PRES, SPH_SNDS, SPH_DIVV, SPH_ROTX, SPH_ROTY, SPH_ROTZ, SPH_BAL, SPH_AVA, SPH_GRADH,
+    SPH_AX, SPH_AY, SPH_AZ, SPH_ENGDOT, SPH_VHX, SPH_VHY, SPH_VHZ, SPH_ENGHALF, SPH_DT,
+    SPH_GX, SPH_GY, SPH_GZ, SPH_POT, SPH_NFIELD
+};
+
+#define SPH_PREC_FP64 0    /* every pair sum in FP64 (parity path) */
+#define SPH_PREC_MIXED 1   /* FP32 pair sums on group-relative coordinates, FP64 everywhere else */
+
+typedef struct {
+    double theta;            /* gravity opening angle (0.5, main.cpp:90) */
+    int32_t n_leaf;          /* octree leaf limit (8, main.cpp:90) */
+    int32_t n_group;         /* gravity i-group limit (256, main.cpp:90) */
+    int32_t n_dens_iter;     /* density passes per step (4: param.h:11, main.cpp:138) */
+    int32_t self_gravity;    /* 1 = SELF_GRAVITY (GI.h:4) */
+    int32_t ext_damp;        /* 1 = GI_universal::addExternalForce (GI.h:458-465) */
+    int32_t precision;       /* SPH_PREC_FP64 or SPH_PREC_MIXED */
+    double ext_damp_tend;    /* 5000 s in the reference */
+    double damping;          /* dampMotion factor (1.0) */
+    double G;                /* 6.67e-11 (force.h:171-172) */
+    int32_t device;          /* CUDA device ordinal */
+    int32_t reserved;
+} sph_config;
+
+typedef struct sph_ctx sph_ctx;
+
+void sph_config_default(sph_config *cfg);
+int sph_ctx_create(const sph_config *cfg, sph_ctx **out);
+int sph_ctx_destroy(sph_ctx *ctx);
+const char *sph_last_error(const sph_ctx *ctx);
+
+/* EoS materials, indexed by the per-particle material id.
+ * Table mode mirrors BilinearInterpolation (interpolation.h:33-102) on the
+ * reference's rho-u tables (EoS.h:121-221): rho axis [n_rho], u axis [n_u],
+ * pressure and sound-speed planes [n_rho * n_u] rho-major. */
+int sph_set_eos_table(sph_ctx *ctx, int material, const double *rho_axis, int n_rho, const double *u_axis,
+                      int n_u, const double *pres, const double *snds);
+/* Reads a rho-u text table (EoS.h:121-221 format) into material slot `material`. */
+int sph_load_eos_table_file(sph_ctx *ctx, int material, const char *path);
+/* Analytic Tillotson: rho0 u0 uiv ucv A B a b alpha beta (EoS.h:116-238 parameter order). */
+int sph_set_eos_tillotson(sph_ctx *ctx, int material, const double par[10]);
+
+/* Copies n particles (host memory) into the context; particle i keeps slot i
+ * for download.  init_smth != 0 applies RealPtcl::initialize
+ * (class.h:196-199: h = 1.2 (m / rho)^(1/3), grad_smth = 1). */
+int sph_upload(sph_ctx *ctx, int64_t n, const double *fields, int64_t ld, const int64_t *id,
+               const int32_t *material, double time, int init_smth);
+/* Copies the state back in upload order. */
+int sph_download(sph_ctx *ctx, double *fields, int64_t ld, int64_t *id, int32_t *material);
+/* Forces of the current state and the first dt (main.cpp:92-105). */
+int sph_prologue(sph_ctx *ctx);
+/* n_steps iterations of the loop body of main.cpp:125-173 (mode 1). */
+int sph_step(sph_ctx *ctx, int n_steps);
+int sph_get_time(const sph_ctx *ctx, double *time, double *dt, int64_t *step);
+
+/* Conserved quantities in FP64: E = sum m (u + v^2/2 + pot/2), P = sum m v,
+ * L = sum m x cross v.  out[0] = E, out[1..3] = P, out[4..6] = L, out[7] = sum m. */
+int sph_diagnostics(sph_ctx *ctx, double out[8]);
+
+/* ---- inspection (tests, tooling) ----------------------------------------- */
+/* Runs only the given pass on the current state (positions unchanged):
+ * 0 = sort + tree, 1 = one density pass, 2 = EoS, 3 = derivative, 4 = hydro, 5 = gravity. */
+int sph_run_pass(sph_ctx *ctx, int pass);
+/* Current particle order (sorted): slot of the k-th particle, Morton keys. */
+int sph_get_order(sph_ctx *ctx, int32_t *slot, uint64_t *keys);
+/* SPH neighbour list of the k-th particle in sorted order for the last built
+ * list of the given mode (0 gather, 1 symmetric); writes ascending sorted
+ * indices, returns the count in *n (may exceed cap). */
+int sph_get_neighbors(sph_ctx *ctx, int mode, int64_t k, int32_t *out, int64_t cap, int64_t *n);
+/* Octree summary: number of cells and, per cell, start/count/level/n_child (arrays may be null). */
+int sph_get_tree(sph_ctx *ctx, int64_t *n_cell, int32_t *start, int32_t *count, int32_t *level, int32_t *n_child,
+                 double *com_mass /* [4 * n_cell] x y z m */);
+/* Gravity interaction list of group g: EPJ sorted indices and SPJ cells as (level, start). */
+int sph_get_grav_list(sph_ctx *ctx, int64_t g, int64_t *n_group, int32_t *epj, int64_t cap_epj, int64_t *n_epj,
+                      int32_t *spj_level, int32_t *spj_start, int64_t cap_spj, int64_t *n_spj,
+                      int32_t *group_start, int32_t *group_count);
+/* Wall time in ms of the device work of each phase of the last step (CUDA events). */
+int sph_get_timings(sph_ctx *ctx, double *ms, int cap, int *n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,59 @@
+"""Shared set-up for the parity tests: identical initial conditions and EoS
+materials for the device library (C ABI) and the CPU oracle."""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+
+from fdps_sph_gb300 import eos, ic
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load_golden(name):
+    return np.load(os.path.join(GOLD, name), allow_pickle=False)
+
+
+def tillotson_materials():
+    """material 0 = iron, 1 = granite (analytic Tillotson, EoS.h:446/448 parameters)."""
+    return [eos.Tillotson("iron", eos.TILLOTSON["iron"]), eos.Tillotson("granite", eos.TILLOTSON["granite"])]
+
+
+def table_materials(n=200):
+    """material 0 = iron, 1 = dunite, 2 = granite (synthetic rho-u tables)."""
+    return [eos.synthetic_table(m, n, n) for m in ("iron", "dunite", "granite")]
+
+
+def oracle_config(materials, **kw):
+    from oracle import pyoracle as po
+    ms = po.MaterialSet([m.as_material() for m in materials])
+    return po.make_config(ms, **kw)
+
+
+def device_context(materials, **kw):
+    from fdps_sph_gb300 import lib
+    ctx = lib.Context(**kw)
+    for k, m in enumerate(materials):
+        ctx.set_material(k, m)
+    return ctx
+
+
+def small_impact(n_target=1800, n_impactor=200, seed=11):
+    return ic.config_small_impact(seed=seed, n_target=n_target, n_impactor=n_impactor)
+
+
+def by_id(F, ids):
+    o = np.argsort(ids, kind="stable")
+    return F[:, o]
+
+
+def rel_err(a, b, floor):
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), floor))) if len(a) else 0.0
+
+
+def vec_rel_err(A, B, floor_frac=1e-6):
+    """max_i |A_i - B_i| / max(|B_i|, floor_frac * max_k |B_k|) for rows of 3-vectors."""
+    nb = np.linalg.norm(B, axis=1)
+    fl = floor_frac * (nb.max() if len(nb) else 1.0)
+    return float(np.max(np.linalg.norm(A - B, axis=1) / np.maximum(nb, fl))) if len(nb) else 0.0

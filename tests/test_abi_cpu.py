@@ -1,0 +1,66 @@
+"""CPU-side checks of the drop-in boundary: the library builds for sm_103a,
+loads, and exports every entry point include/sph_gb300.h declares.  No
+compute call is made (there is no GPU here)."""
+import os
+import re
+
+import numpy as np
+
+from fdps_sph_gb300 import build, lib, types as T
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    src = open(os.path.join(ROOT, "include", "sph_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    names = re.findall(r"\b(?:int|void|const char \*)\s*\*?\s*(sph_[a-z0-9_]+)\s*\(", src)
+    return sorted(set(names))
+
+
+def test_library_builds_and_exports_every_declared_symbol():
+    path = build.build()
+    assert os.path.exists(path)
+    L = lib.load()
+    names = declared_functions()
+    assert len(names) >= 25
+    for n in names:
+        assert hasattr(L, n), f"missing export {n}"
+    assert sorted(lib.EXPORTS) == names
+
+
+def test_payload_layouts_match_header():
+    # sizes in the header comments (class.h layouts) match the numpy mirrors
+    src = open(os.path.join(ROOT, "include", "sph_gb300.h")).read()
+    for name, size in T.SIZES.items():
+        kind, _, part = name.partition("_")
+        assert size % 8 == 0
+    assert T.EPI_HYDRO.itemsize == 112 and T.EPJ_HYDRO.itemsize == 120
+    assert "112 B" in src and "120 B" in src
+
+
+def test_field_order_matches_header():
+    src = open(os.path.join(ROOT, "include", "sph_gb300.h")).read()
+    body = src[src.index("enum sph_field"):]
+    body = body[:body.index("}")]
+    names = re.findall(r"SPH_([A-Z]+)", body)
+    names = [n for n in names if n != "NFIELD"]
+    assert len(names) == lib.NFIELD
+    from oracle import pyoracle as po
+    assert po.FIELDS == lib.FIELDS
+    assert np.all(np.array(names) == np.array([
+        "X", "Y", "Z", "VX", "VY", "VZ", "MASS", "SMTH", "DENS", "ENG", "PRES", "SNDS", "DIVV", "ROTX", "ROTY",
+        "ROTZ", "BAL", "AVA", "GRADH", "AX", "AY", "AZ", "ENGDOT", "VHX", "VHY", "VHZ", "ENGHALF", "DT", "GX",
+        "GY", "GZ", "POT"]))
+
+
+def test_context_creation_fails_cleanly_without_gpu():
+    import torch
+    if torch.cuda.is_available():
+        return
+    try:
+        lib.Context()
+    except lib.SphError as e:
+        assert e.code in (-2, -3)
+    else:
+        raise AssertionError("expected an error without a GPU")

@@ -1,0 +1,215 @@
+"""Device-resident path (C ABI, libsph_gb300.so) against the CPU oracle on
+the same seeded inputs.
+
+Bit-exact: Morton keys, sorted order, octree cells and monopole moments,
+SPH neighbour lists (gather and symmetric) and gravity interaction lists.
+FP64 values (spec tolerance 1e-10, summation order and FMA only):
+density, h, pressure, sound speed, grad-h, div v, curl v, Balsara,
+acceleration, du/dt, dt, gravity and potential."""
+import numpy as np
+import pytest
+
+from helpers import (by_id, device_context, oracle_config, rel_err, small_impact, table_materials,
+                     tillotson_materials, vec_rel_err)
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def impact():
+    F, ids, mats, info = small_impact()
+    return F, ids, mats
+
+
+def _oracle(F, ids, mats):
+    from oracle import pyoracle as po
+    return po.OracleSystem(F, ids, mats)
+
+
+def _dev_sorted(ctx):
+    """device state in its internal (key) order"""
+    F, ids, mats = ctx.download()
+    slot, keys = ctx.order()
+    return F[:, slot], ids[slot], keys
+
+
+def test_keys_order_and_tree_bit_exact(impact):
+    from oracle import pyoracle as po
+    F, ids, mats = impact
+    ctx = device_context(tillotson_materials())
+    ctx.upload(F, ids, mats)
+    ctx.run_pass(0)
+    Fd, idd, keys = _dev_sorted(ctx)
+    s = _oracle(F, ids, mats)
+    tr = po.OracleTree(s)
+    assert np.array_equal(idd, s.id)
+    assert np.array_equal(keys, tr.keys())
+    dt = ctx.tree()
+    oc = tr.cells()
+    assert len(dt["start"]) == len(oc)
+    dev = {(int(l), int(s_)): (int(c), int(n), tuple(m)) for l, s_, c, n, m in
+           zip(dt["level"], dt["start"], dt["count"], dt["n_child"], dt["com"])}
+    for c in oc:
+        key = (int(c["level"]), int(c["start"]))
+        assert key in dev
+        cnt, nch, com = dev[key]
+        assert cnt == c["count"] and nch == c["n_child"]
+        assert com == (c["com"][0], c["com"][1], c["com"][2], c["mass"])   # bit-identical monopoles
+
+
+def test_passes_and_lists_match_oracle(impact):
+    from oracle import pyoracle as po
+    F, ids, mats = impact
+    mats_l = tillotson_materials()
+    cfg = oracle_config(mats_l)
+    ctx = device_context(mats_l)
+    ctx.upload(F, ids, mats)
+    ctx.run_pass(0)
+    s = _oracle(F, ids, mats)
+    tr = po.OracleTree(s)
+    n = s.n
+    # density passes: lists (built from the current h) then values
+    for it in range(4):
+        ctx.run_pass(1)
+        for k in range(0, n, 7 if it else 1):
+            assert np.array_equal(ctx.neighbors(0, k), tr.sph_list(k, 0)), (it, k)
+        tr.pass_density(cfg)
+        Fd, idd, _ = _dev_sorted(ctx)
+        assert rel_err(Fd[po.FIELD["dens"]], s.field("dens"), 1e-300) < 1e-12
+        assert rel_err(Fd[po.FIELD["smth"]], s.field("smth"), 1e-300) < 1e-12
+        s.F[po.FIELD["smth"]] = Fd[po.FIELD["smth"]]     # continue from identical h
+        s.F[po.FIELD["dens"]] = Fd[po.FIELD["dens"]]
+    tr = po.OracleTree(s)                                # fresh hmax for the symmetric walk
+    ctx.run_pass(2)
+    tr.pass_pressure(cfg)
+    Fd, _, _ = _dev_sorted(ctx)
+    for f in ("pres", "snds"):
+        assert rel_err(Fd[po.FIELD[f]], s.field(f), 1e-9 * np.abs(s.field(f)).max()) < 1e-12
+    ctx.run_pass(3)
+    tr.pass_derivative()
+    Fd, _, _ = _dev_sorted(ctx)
+    assert rel_err(Fd[po.FIELD["grad_smth"]], s.field("grad_smth"), 1e-300) < 1e-12
+    dv = s.field("div_v")
+    assert rel_err(Fd[po.FIELD["div_v"]], dv, 1e-9 * max(np.abs(dv).max(), 1e-30)) < 1e-10
+    ctx.run_pass(4)
+    for k in range(0, n, 3):
+        assert np.array_equal(ctx.neighbors(1, k), tr.sph_list(k, 1)), k
+    tr.pass_hydro()
+    Fd, _, _ = _dev_sorted(ctx)
+    A = np.stack([Fd[po.FIELD[c]] for c in ("ax", "ay", "az")], 1)
+    B = np.stack([s.field(c) for c in ("ax", "ay", "az")], 1)
+    assert vec_rel_err(A, B, 1e-6) < 1e-10
+    ed = s.field("eng_dot")
+    assert rel_err(Fd[po.FIELD["eng_dot"]], ed, 1e-6 * np.abs(ed).max()) < 1e-10
+    assert rel_err(Fd[po.FIELD["dt"]], s.field("dt"), 1e-300) < 1e-12
+    ctx.run_pass(5)
+    tr.pass_gravity(cfg)
+    Fd, _, _ = _dev_sorted(ctx)
+    A = np.stack([Fd[po.FIELD[c]] for c in ("gx", "gy", "gz")], 1)
+    B = np.stack([s.field(c) for c in ("gx", "gy", "gz")], 1)
+    assert vec_rel_err(A, B, 1e-6) < 1e-10
+    assert rel_err(Fd[po.FIELD["pot"]], s.field("pot"), 1e-300) < 1e-12
+    # gravity interaction lists: same groups, same EPJ and SPJ sequences
+    oc = tr.cells()
+    og = {int(oc[g]["start"]): int(g) for g in tr.groups(256)}
+    ng = ctx.n_groups()
+    assert ng == len(og)
+    for g in range(ng):
+        d = ctx.grav_list(g)
+        o_epj, o_spj = tr.grav_list(og[d["start"]], 0.5)
+        assert np.array_equal(d["epj"], o_epj)
+        assert np.array_equal(d["spj_level"], oc["level"][o_spj])
+        assert np.array_equal(d["spj_start"], oc["start"][o_spj])
+
+
+@pytest.mark.parametrize("eos_kind", ["tillotson", "table"])
+def test_steps_match_oracle(eos_kind):
+    """prologue + 5 steps of main.cpp:92-173 on both sides"""
+    from oracle import pyoracle as po
+    if eos_kind == "tillotson":
+        F, ids, mats, _ = small_impact(1500, 300, seed=5)
+        mats_l = tillotson_materials()
+    else:
+        from fdps_sph_gb300 import ic
+        F, ids, mats, _ = ic.config_1m_impact(seed=9, n_target=1500, n_impactor=300)
+        mats_l = table_materials(200)
+    cfg = oracle_config(mats_l)
+    ctx = device_context(mats_l)
+    ctx.upload(F, ids, mats)
+    ctx.prologue()
+    s = _oracle(F, ids, mats)
+    s.prologue(cfg)
+    assert abs(ctx.time()[1] - s.sys.dt) <= 1e-12 * s.sys.dt
+    ctx.step(5)
+    s.step(cfg, 5)
+    t, dt, st = ctx.time()
+    assert st == 5
+    assert abs(t - s.sys.time) <= 1e-10 * s.sys.time
+    Fd, idd, _ = ctx.download()
+    Fd = by_id(Fd, idd)
+    Fo, ido, _ = s.by_id()
+    assert np.array_equal(np.sort(idd), ido)
+    for f, tol in [("x", 1e-12), ("y", 1e-12), ("z", 1e-12), ("dens", 1e-9), ("smth", 1e-9), ("eng", 1e-9),
+                   ("pot", 1e-9)]:
+        assert rel_err(Fd[po.FIELD[f]], Fo[po.FIELD[f]], 1e-300) < tol, f
+    V = np.stack([Fd[po.FIELD[c]] for c in ("vx", "vy", "vz")], 1)
+    W = np.stack([Fo[po.FIELD[c]] for c in ("vx", "vy", "vz")], 1)
+    assert vec_rel_err(V, W, 1e-6) < 1e-9
+
+
+def test_mixed_precision_against_fp64_oracle(impact):
+    """FP32 pair sums on double-float coordinates: rho, acc, du/dt and
+    gravity within 1e-5 relative of the FP64 oracle (spec bar)."""
+    from oracle import pyoracle as po
+    F, ids, mats = impact
+    mats_l = tillotson_materials()
+    cfg = oracle_config(mats_l)
+    ctx = device_context(mats_l, precision=1)
+    ctx.upload(F, ids, mats)
+    ctx.prologue()
+    s = _oracle(F, ids, mats)
+    s.prologue(cfg)
+    Fd, idd, _ = ctx.download()
+    Fd = by_id(Fd, idd)
+    Fo, _, _ = s.by_id()
+    f = po.FIELD
+    assert rel_err(Fd[f["dens"]], Fo[f["dens"]], 1e-300) < 1e-5
+    A = np.stack([Fd[f[c]] for c in ("ax", "ay", "az")], 1)
+    B = np.stack([Fo[f[c]] for c in ("ax", "ay", "az")], 1)
+    assert vec_rel_err(A, B, 1e-3) < 1e-5
+    ed = Fo[f["eng_dot"]]
+    assert rel_err(Fd[f["eng_dot"]], ed, 1e-3 * np.abs(ed).max()) < 1e-5
+    A = np.stack([Fd[f[c]] for c in ("gx", "gy", "gz")], 1)
+    B = np.stack([Fo[f[c]] for c in ("gx", "gy", "gz")], 1)
+    assert vec_rel_err(A, B, 1e-3) < 1e-5
+    assert rel_err(Fd[f["pot"]], Fo[f["pot"]], 1e-300) < 1e-5
+
+
+def test_tree_gravity_against_direct_sum(impact):
+    """theta = 0 opens every cell (FP64 direct summation); theta = 0.5 error stays small."""
+    from oracle import pyoracle as po
+    F, ids, mats = impact
+    mats_l = tillotson_materials()
+    out = {}
+    for theta in (0.0, 0.5, 0.7):
+        ctx = device_context(mats_l, theta=theta)
+        ctx.upload(F, ids, mats)
+        ctx.run_pass(0)
+        ctx.run_pass(5)
+        Fd, idd, _ = ctx.download()
+        out[theta] = by_id(Fd, idd)
+    # direct sum on the host in FP64
+    Fs = by_id(F, ids)
+    x = Fs[[0, 1, 2]].T
+    m = Fs[po.FIELD["mass"]]
+    h = Fs[po.FIELD["smth"]]
+    d = x[:, None, :] - x[None, :, :]
+    r2 = (d * d).sum(-1) + (h * h)[:, None]
+    ri = 1.0 / np.sqrt(r2)
+    acc = -6.67e-11 * (m[None, :, None] * d * (ri ** 3)[:, :, None]).sum(1)
+    g0 = np.stack([out[0.0][po.FIELD[c]] for c in ("gx", "gy", "gz")], 1)
+    assert vec_rel_err(g0, acc, 1e-6) < 1e-10
+    for theta, bound in ((0.5, 5e-3), (0.7, 2e-2)):
+        g = np.stack([out[theta][po.FIELD[c]] for c in ("gx", "gy", "gz")], 1)
+        err = np.linalg.norm(g - acc, axis=1) / np.linalg.norm(acc, axis=1).max()
+        assert err.max() < bound, (theta, err.max())
