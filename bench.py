@@ -1,0 +1,308 @@
+#!/usr/bin/env python
+"""Benchmark: SPH particle-steps/s on the 1M-particle impact (mixed
+precision, with the plain FP64 path beside it), through the C ABI of
+libsph_gb300.so.
+
+Workload: two-layer iron-core / dunite-mantle bodies, 900k + 100k particles,
+30 degrees at 1.2 v_esc, ANEOS-style synthetic 200 x 200 rho-u tables,
+theta = 0.5.  One step = one iteration of main.cpp:125-173 (kick-drift-
+predict, sort + octree, density x 4, EoS, derivative, hydro, tree gravity,
+final kick, global dt).  Inputs (1M particles x 256 B of state plus lists)
+are larger than the 129 MB L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Multi-GPU: the path does not shard within a run on this build (replicas
+only), so N > 1 runs N independent replicas, one per rank, and reports the
+aggregate.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# algorithmic flops per pair interaction (adds, muls, compares 1; FMA 2;
+# sqrt / div / rsqrt 1): density, derivative, hydro, gravity
+FLOPS_PER_PAIR = {"dens": 24, "drvt": 75, "hydro": 120, "grav": 24}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=1_000_000, help="total particles (default: the 1M workload)")
+    ap.add_argument("--cpu-n", type=int, default=100_000, help="particles of the bounded CPU sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if p[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def workload(n_total, seed=2024):
+    from fdps_sph_gb300 import eos, ic
+    nt = int(round(n_total * 0.9))
+    F, ids, mats, info = ic.config_1m_impact(seed=seed, n_target=nt, n_impactor=n_total - nt)
+    materials = [eos.synthetic_table("iron"), eos.synthetic_table("dunite")]
+    return F, ids, mats, materials
+
+
+def run_gpu(F, ids, mats, materials, precision, steps, warmup, device):
+    from fdps_sph_gb300 import lib
+    ctx = lib.Context(precision=precision, device=device)
+    for k, m in enumerate(materials):
+        ctx.set_material(k, m)
+    ctx.upload(F, ids, mats)
+    ctx.prologue()
+    for _ in range(warmup):
+        ctx.step(1)
+    ctx.enable_timing(True)
+    c0 = ctx.counters()["launches"]
+    with ClockSampler(device) as clk:
+        ms = ctx.step_timed(steps)
+    c1 = ctx.counters()
+    seg = ctx.timings()
+    ctx.enable_timing(False)
+    return ctx, ms, seg, c1, c1["launches"] - c0, clk.summary()
+
+
+def run_e2e(ctx, F, ids, mats, steps):
+    """upload (pinned host) -> one step -> download (pinned host), every step"""
+    import torch
+    n = F.shape[1]
+    hostF = torch.empty((F.shape[0], n), dtype=torch.float64).pin_memory().numpy()
+    outF = torch.empty((F.shape[0], n), dtype=torch.float64).pin_memory().numpy()
+    hid = torch.empty(n, dtype=torch.int64).pin_memory().numpy()
+    hmat = torch.empty(n, dtype=torch.int32).pin_memory().numpy()
+    # start from the context's current state (forces valid)
+    Fc, idc, matc = ctx.download()
+    hostF[:] = Fc
+    hid[:] = idc
+    hmat[:] = matc
+    t_now, dt, _ = ctx.time()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        ctx.upload(hostF, hid, hmat, time=t_now, dt=dt, forces_valid=True)
+        ctx.step(1)
+        t_now, dt, _ = ctx.time()
+        o, oid, om = ctx.download(outF)
+        hostF, outF = outF, hostF
+        hid, hmat = oid, om
+    el = time.perf_counter() - t0
+    h2d = hostF.nbytes + hid.nbytes + hmat.nbytes
+    return el, h2d, h2d
+
+
+def cpu_sample(n_cpu, steps, fast=True):
+    """the oracle restatement of the path (OpenMP, all host threads) on the
+    same body geometry at n_cpu particles: prologue untimed, `steps` timed"""
+    from oracle import pyoracle as po
+    F, ids, mats, materials = workload(n_cpu, seed=77)
+    ms = po.MaterialSet([m.as_material() for m in materials])
+    cfg = po.make_config(ms)
+    s = po.OracleSystem(F, ids, mats, fast=fast)
+    s.prologue(cfg)
+    t0 = time.perf_counter()
+    s.step(cfg, steps)
+    el = time.perf_counter() - t0
+    return n_cpu * steps / el, el, po.lib(fast).or_num_threads()
+
+
+def dist_init(n_gpus):
+    if n_gpus <= 1 and "WORLD_SIZE" not in os.environ:
+        return 0, 1, None
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", n_gpus))
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return rank, world, dist
+
+
+def main():
+    a = parse()
+    rank, world, dist = dist_init(a.gpus)
+    if a.impl == "reference":
+        if rank != 0:
+            return
+        # the reference's CPU path on this host: the oracle restatement (the reference itself
+        # needs FDPS, which is not vendored, so it cannot be built here); all host threads
+        n_cpu = a.cpu_n
+        from oracle import pyoracle as po
+        F, ids, mats, materials = workload(n_cpu, seed=77)
+        ms = po.MaterialSet([m.as_material() for m in materials])
+        cfg = po.make_config(ms)
+        s = po.OracleSystem(F, ids, mats, fast=True)
+        s.prologue(cfg)
+        if a.warmup:
+            s.step(cfg, a.warmup)
+        t0 = time.perf_counter()
+        s.step(cfg, a.steps)
+        el = time.perf_counter() - t0
+        v = n_cpu * a.steps / el
+        cores = po.lib(True).or_num_threads()
+        out = {"metric": "SPH particle-steps/s (1M two-layer impact; reference CPU path, bounded sample)",
+               "value": v, "unit": "particle-steps/s", "impl": "reference", "n_gpus": a.gpus, "steps": a.steps,
+               "warmup": a.warmup, "ms_per_step": 1e3 * el / a.steps, "higher_is_better": True,
+               "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded IC generator)",
+               "config": {"workload": f"1M-particle impact geometry at {n_cpu} particles (CPU sample)",
+                          "particles": n_cpu, "parallelism": f"OpenMP x{cores}"},
+               "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                                "sample": f"{n_cpu} particles, {a.steps} steps after {a.warmup} warm-up steps"},
+               "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(out))
+        return
+
+    from fdps_sph_gb300 import lib
+    import torch
+    device = int(os.environ.get("LOCAL_RANK", 0))
+    F, ids, mats, materials = workload(a.n)
+    n = F.shape[1]
+
+    results = {}
+    precisions = ["mixed"] if a.no_fp64 else ["mixed", "fp64"]
+    for prec in precisions:
+        ctx, ms, seg, cnt, launches, clocks = run_gpu(F, ids, mats, materials, prec, a.steps, a.warmup, device)
+        e2e = run_e2e(ctx, F, ids, mats, a.e2e_steps) if prec == "mixed" else None
+        results[prec] = dict(ms=ms, seg=seg, cnt=cnt, launches=launches, clocks=clocks, e2e=e2e)
+        ctx.close()
+
+    if dist is not None:
+        t = torch.tensor([results["mixed"]["ms"]], dtype=torch.float64, device=f"cuda:{device}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        results["mixed"]["ms"] = float(t.item())
+        dist.barrier()
+    if rank != 0:
+        return
+
+    peak32 = lib.probe_peak(False, device)
+    peak64 = lib.probe_peak(True, device)
+    mixed = results["mixed"]
+    ms_step = mixed["ms"] / a.steps
+    value = world * n / (ms_step * 1e-3)
+
+    # dominant pair kernel of the mixed path and its roofline
+    pairs = {"dens": mixed["cnt"]["pairs_gather"], "drvt": mixed["cnt"]["pairs_gather"],
+             "hydro": mixed["cnt"]["pairs_sym"], "grav": mixed["cnt"]["pairs_grav"]}
+    per_launch_ms = {"dens": mixed["seg"]["dens"] / (4 * a.steps), "drvt": mixed["seg"]["drvt"] / a.steps,
+                     "hydro": mixed["seg"]["hydro"] / a.steps, "grav": mixed["seg"]["grav"] / a.steps}
+    dom = max(("dens", "drvt", "hydro", "grav"), key=lambda k: mixed["seg"][k])
+    achieved = FLOPS_PER_PAIR[dom] * pairs[dom] / (per_launch_ms[dom] * 1e-3) / 1e12
+    seg_share = {k: round(v / max(sum(mixed["seg"].values()), 1e-9), 4) for k, v in mixed["seg"].items()}
+
+    out = {
+        "metric": "SPH particle-steps/s at 1M (mixed FP32/FP64; plain FP64 beside it)",
+        "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 pair sums + f64", "data": "synthetic (seeded IC generator, synthetic 200x200 rho-u tables)",
+        "config": {"workload": "1M-particle two-layer impact (900k + 100k, iron/dunite, 30 deg, 1.2 v_esc, "
+                               "theta 0.5)", "particles": n, "precision": "mixed",
+                   "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "gpu_launches": int(mixed["launches"]),
+        "clocks": mixed["clocks"],
+        "roofline": {"bound": "fp32", "kernel": dom, "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
+                     "frac": achieved / peak32 if peak32 else None, "traffic": None,
+                     "peak_source": "measured FMA-chain probe (sph_probe_peak), not in MEASURED_PEAKS.json",
+                     "flops_per_pair": FLOPS_PER_PAIR[dom], "pairs_per_launch": pairs[dom],
+                     "ms_per_launch": per_launch_ms[dom]},
+        "segments_ms_per_step": {k: v / a.steps for k, v in mixed["seg"].items()},
+        "segment_share": seg_share,
+        "work": {k: v for k, v in mixed["cnt"].items() if k != "launches"},
+    }
+    if mixed["e2e"] is not None:
+        el, h2d, d2h = mixed["e2e"]
+        out["e2e"] = {"value": world * n * a.e2e_steps / el, "unit": "particle-steps/s",
+                      "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": a.e2e_steps}
+    if "fp64" in results:
+        f = results["fp64"]
+        v64 = world * n / (f["ms"] / a.steps * 1e-3)
+        dom64 = max(("dens", "drvt", "hydro", "grav"), key=lambda k: f["seg"][k])
+        p64 = {"dens": f["cnt"]["pairs_gather"], "drvt": f["cnt"]["pairs_gather"], "hydro": f["cnt"]["pairs_sym"],
+               "grav": f["cnt"]["pairs_grav"]}[dom64]
+        pl64 = f["seg"][dom64] / (a.steps * (4 if dom64 == "dens" else 1))
+        ach64 = FLOPS_PER_PAIR[dom64] * p64 / (pl64 * 1e-3) / 1e12
+        out["fp64"] = {"value": v64, "ms_per_step": f["ms"] / a.steps, "speedup_mixed_over_fp64": value / v64,
+                       "segments_ms_per_step": {k: v / a.steps for k, v in f["seg"].items()},
+                       "roofline": {"bound": "fp64", "kernel": dom64, "achieved": ach64, "peak": peak64,
+                                    "unit": "TFLOP/s", "frac": ach64 / peak64 if peak64 else None},
+                       "clocks": f["clocks"], "gpu_launches": int(f["launches"])}
+    if not a.no_cpu:
+        v_cpu, el_cpu, cores = cpu_sample(a.cpu_n, 1)
+        out["cpu_baseline"] = {"value": v_cpu, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                               "sample": f"oracle restatement (OpenMP) on the same geometry at {a.cpu_n} particles, "
+                                         f"1 step after the prologue ({el_cpu:.1f} s)"}
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -59,42 +59,63 @@ int upload_materials(sph_ctx *ctx) {
     return SPH_OK;
 }
 
-int time_mark(sph_ctx *ctx) {
-    if (!ctx->timing || ctx->n_ev >= 32) return SPH_OK;
+// records an event ending timing segment `seg` (seg < 0: the start mark)
+int time_mark(sph_ctx *ctx, int seg) {
+    if (!ctx->timing || ctx->n_ev >= 64) return SPH_OK;
+    ctx->mark_seg[ctx->n_ev] = seg;
     SPH_CUDA(ctx, cudaEventRecord(ctx->ev[ctx->n_ev++], ctx->stream));
+    return SPH_OK;
+}
+
+// accumulates the elapsed time between consecutive marks into their segments
+int collect_timings(sph_ctx *ctx) {
+    if (!ctx->timing || ctx->n_ev < 2) {
+        ctx->n_ev = 0;
+        return SPH_OK;
+    }
+    SPH_CUDA(ctx, cudaEventSynchronize(ctx->ev[ctx->n_ev - 1]));
+    for (int k = 1; k < ctx->n_ev; ++k) {
+        float ms = 0.0f;
+        SPH_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[k - 1], ctx->ev[k]));
+        const int seg = ctx->mark_seg[k];
+        if (seg >= 0 && seg < SEG_N) {
+            ctx->seg_ms[seg] += ms;
+            ctx->seg_calls[seg] += 1;
+        }
+    }
+    ctx->n_ev = 0;
     return SPH_OK;
 }
 
 // main.cpp:138-146 (positions fixed): sort + tree, density x n, EoS, derivative, hydro, gravity
 int compute_forces(sph_ctx *ctx) {
-    ctx->n_ev = 0;
-    SPH_TRY(time_mark(ctx));
     SPH_TRY(sph_sort_and_build(ctx));
     if (ctx->cfg.precision == SPH_PREC_MIXED) SPH_TRY(sph_pack_mixed(ctx));
-    SPH_TRY(time_mark(ctx));
-    for (int it = 0; it < ctx->cfg.n_dens_iter; ++it) SPH_TRY(sph_pass_density(ctx));
-    SPH_TRY(time_mark(ctx));
-    SPH_TRY(sph_pass_eos(ctx));
-    SPH_TRY(time_mark(ctx));
-    SPH_TRY(sph_pass_derivative(ctx));
-    SPH_TRY(time_mark(ctx));
-    SPH_TRY(sph_pass_hydro(ctx));
-    SPH_TRY(time_mark(ctx));
-    if (ctx->cfg.self_gravity) SPH_TRY(sph_pass_gravity(ctx));
-    SPH_TRY(time_mark(ctx));
-    ctx->have_forces = true;
-    return SPH_OK;
-}
-
-int collect_timings(sph_ctx *ctx) {
-    ctx->timings.clear();
-    if (!ctx->timing || ctx->n_ev < 2) return SPH_OK;
-    SPH_CUDA(ctx, cudaEventSynchronize(ctx->ev[ctx->n_ev - 1]));
-    for (int k = 1; k < ctx->n_ev; ++k) {
-        float ms = 0.0f;
-        SPH_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[k - 1], ctx->ev[k]));
-        ctx->timings.push_back(ms);
+    SPH_TRY(time_mark(ctx, SEG_TREE));
+    for (int it = 0; it < ctx->cfg.n_dens_iter; ++it) {
+        SPH_TRY(sph_build_sph_lists(ctx, 0));
+        SPH_TRY(time_mark(ctx, SEG_DENS_LIST));
+        SPH_TRY(sph_pass_density(ctx, 0));
+        SPH_TRY(time_mark(ctx, SEG_DENS));
     }
+    SPH_TRY(sph_pass_eos(ctx));
+    SPH_TRY(time_mark(ctx, SEG_EOS));
+    SPH_TRY(sph_build_sph_lists(ctx, 0));
+    SPH_TRY(time_mark(ctx, SEG_DRVT_LIST));
+    SPH_TRY(sph_pass_derivative(ctx, 0));
+    SPH_TRY(time_mark(ctx, SEG_DRVT));
+    SPH_TRY(sph_tree_refresh_hmax(ctx));
+    SPH_TRY(sph_build_sph_lists(ctx, 1));
+    SPH_TRY(time_mark(ctx, SEG_HYDRO_LIST));
+    SPH_TRY(sph_pass_hydro(ctx, 0));
+    SPH_TRY(time_mark(ctx, SEG_HYDRO));
+    if (ctx->cfg.self_gravity) {
+        SPH_TRY(sph_build_grav_lists(ctx));
+        SPH_TRY(time_mark(ctx, SEG_GRAV_LIST));
+        SPH_TRY(sph_pass_gravity(ctx, 0));
+        SPH_TRY(time_mark(ctx, SEG_GRAV));
+    }
+    ctx->have_forces = true;
     return SPH_OK;
 }
 
@@ -149,7 +170,9 @@ int sph_ctx_create(const sph_config *cfg, sph_ctx **out) {
         std::memset(&ctx->mats_host[k], 0, sizeof(DevMaterial));
         ctx->mats_host[k].kind = -1;
     }
-    for (int k = 0; k < 32; ++k) cudaEventCreate(&ctx->ev[k]);
+    for (int k = 0; k < 64; ++k) cudaEventCreate(&ctx->ev[k]);
+    cudaEventCreate(&ctx->ev_begin);
+    cudaEventCreate(&ctx->ev_end);
     if (cudaMalloc((void **)&ctx->mats_dev, sizeof(ctx->mats_host)) != cudaSuccess ||
         cudaMalloc((void **)&ctx->scratch_d, sizeof(double) * 8192) != cudaSuccess ||
         cudaMallocHost((void **)&ctx->host_scalars, sizeof(double) * 512) != cudaSuccess) {
@@ -182,8 +205,10 @@ int sph_ctx_destroy(sph_ctx *ctx) {
         if (p) cudaFree(p);
     for (void *p : ctx->table_allocs) cudaFree(p);
     if (ctx->host_scalars) cudaFreeHost(ctx->host_scalars);
-    for (int k = 0; k < 32; ++k)
+    for (int k = 0; k < 64; ++k)
         if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
+    if (ctx->ev_begin) cudaEventDestroy(ctx->ev_begin);
+    if (ctx->ev_end) cudaEventDestroy(ctx->ev_end);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return SPH_OK;
@@ -278,7 +303,8 @@ int sph_set_eos_tillotson(sph_ctx *ctx, int material, const double par[10]) {
 }
 
 int sph_upload(sph_ctx *ctx, int64_t n, const double *fields, int64_t ld, const int64_t *id, const int32_t *material,
-               double time, int init_smth) {
+               double time, double dt, int flags) {
+    const int init_smth = flags & SPH_UPLOAD_INIT_SMTH;
     if (!ctx) return SPH_ERR_ARG;
     if (n < 1 || n > 0x3fffffff || !fields || ld < n) return sph_fail(ctx, SPH_ERR_ARG, "bad particle block (n=%lld)", (long long)n);
     cudaSetDevice(ctx->device);
@@ -331,17 +357,18 @@ int sph_upload(sph_ctx *ctx, int64_t n, const double *fields, int64_t ld, const 
     } else {
         SPH_CUDA(ctx, cudaMemsetAsync(ctx->mat, 0, sizeof(int32_t) * n, ctx->stream));
     }
-    k_iota32<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(ctx->slot, (int)n);
+    k_iota32<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(ctx->slot, (int)n); ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
     // power of two close to 1 / mean mass (exact rescaling of the FP32 mass copies)
     ctx->mscale = std::ldexp(1.0, -(int)std::lround(std::log2(msum / (double)n)));
     if (init_smth) SPH_TRY(sph_init_smth(ctx));
     SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     ctx->time = time;
-    ctx->dt = 0.0;
+    ctx->dt = dt;
     ctx->step = 0;
     ctx->uploaded = true;
-    ctx->have_forces = false;
+    // SPH_UPLOAD_FORCES_VALID: acc / grav / eng_dot / dt in the block are the forces of this state
+    ctx->have_forces = (flags & SPH_UPLOAD_FORCES_VALID) && dt > 0.0;
     return SPH_OK;
 }
 
@@ -352,7 +379,7 @@ int sph_download(sph_ctx *ctx, double *fields, int64_t ld, int64_t *id, int32_t 
     cudaSetDevice(ctx->device);
     const int n = (int)ctx->n;
     k_unpermute<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(ctx->F, ctx->F2, ctx->cap, n, ctx->slot, ctx->id,
-                                                             ctx->id2, ctx->mat, ctx->mat2);
+                                                             ctx->id2, ctx->mat, ctx->mat2); ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
     SPH_CUDA(ctx, cudaMemcpy2DAsync(fields, sizeof(double) * ld, ctx->F2, sizeof(double) * ctx->cap,
                                     sizeof(double) * n, SPH_NFIELD, cudaMemcpyDeviceToHost, ctx->stream));
@@ -367,9 +394,12 @@ int sph_prologue(sph_ctx *ctx) {
     if (!ctx) return SPH_ERR_ARG;
     if (!ctx->uploaded) return sph_fail(ctx, SPH_ERR_STATE, "prologue before upload");
     cudaSetDevice(ctx->device);
+    ctx->n_ev = 0;
+    SPH_TRY(time_mark(ctx, -1));
     SPH_TRY(compute_forces(ctx));
     SPH_TRY(sph_dt_global(ctx, &ctx->dt));     // main.cpp:103
     SPH_TRY(sph_ext_force(ctx));               // main.cpp:104
+    SPH_TRY(time_mark(ctx, SEG_FINAL));
     SPH_TRY(collect_timings(ctx));
     SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return SPH_OK;
@@ -381,15 +411,19 @@ int sph_step(sph_ctx *ctx, int n_steps) {
     cudaSetDevice(ctx->device);
     for (int s = 0; s < n_steps; ++s) {
         const double dt = ctx->dt;
+        ctx->n_ev = 0;
+        SPH_TRY(time_mark(ctx, -1));
         SPH_TRY(sph_kick_drift_predict(ctx, dt));   // main.cpp:126-131
+        SPH_TRY(time_mark(ctx, SEG_KDP));
         ctx->time += dt;                            // main.cpp:132
         SPH_TRY(compute_forces(ctx));               // main.cpp:136-147
         SPH_TRY(sph_ext_force(ctx));                // main.cpp:148
         SPH_TRY(sph_final_kick(ctx, dt));           // main.cpp:149-153
         SPH_TRY(sph_dt_global(ctx, &ctx->dt));      // main.cpp:160
+        SPH_TRY(time_mark(ctx, SEG_FINAL));
+        SPH_TRY(collect_timings(ctx));
         ctx->step += 1;
     }
-    SPH_TRY(collect_timings(ctx));
     return SPH_OK;
 }
 
@@ -417,11 +451,11 @@ int sph_run_pass(sph_ctx *ctx, int pass) {
             SPH_TRY(sph_sort_and_build(ctx));
             if (ctx->cfg.precision == SPH_PREC_MIXED) SPH_TRY(sph_pack_mixed(ctx));
             break;
-        case 1: SPH_TRY(sph_pass_density(ctx)); break;
+        case 1: SPH_TRY(sph_pass_density(ctx, 1)); break;
         case 2: SPH_TRY(sph_pass_eos(ctx)); break;
-        case 3: SPH_TRY(sph_pass_derivative(ctx)); break;
-        case 4: SPH_TRY(sph_pass_hydro(ctx)); break;
-        case 5: SPH_TRY(sph_pass_gravity(ctx)); break;
+        case 3: SPH_TRY(sph_pass_derivative(ctx, 1)); break;
+        case 4: SPH_TRY(sph_pass_hydro(ctx, 1)); break;
+        case 5: SPH_TRY(sph_pass_gravity(ctx, 1)); break;
         default: return sph_fail(ctx, SPH_ERR_ARG, "unknown pass %d", pass);
     }
     SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -504,13 +538,48 @@ int sph_get_grav_list(sph_ctx *ctx, int64_t g, int64_t *n_group, int32_t *epj, i
 
 int sph_get_timings(sph_ctx *ctx, double *ms, int cap, int *n) {
     if (!ctx) return SPH_ERR_ARG;
-    if (cap < 0) {   // cap < 0 switches event timing on (cap == -1) or off (cap == -2)
-        ctx->timing = (cap == -1);
+    if (cap < 0) {   // -1: switch event timing on and reset, -2: off, -3: reset
+        if (cap == -1) ctx->timing = true;
+        if (cap == -2) ctx->timing = false;
+        for (int k = 0; k < 16; ++k) {
+            ctx->seg_ms[k] = 0.0;
+            ctx->seg_calls[k] = 0;
+        }
         return SPH_OK;
     }
-    const int m = (int)std::min<size_t>((size_t)cap, ctx->timings.size());
-    for (int k = 0; k < m; ++k) ms[k] = ctx->timings[k];
-    if (n) *n = (int)ctx->timings.size();
+    const int m = std::min(cap, (int)SEG_N);
+    for (int k = 0; k < m; ++k) ms[k] = ctx->seg_ms[k];
+    if (n) *n = SEG_N;
+    return SPH_OK;
+}
+
+int sph_step_timed(sph_ctx *ctx, int n_steps, double *device_ms) {
+    if (!ctx || !device_ms) return SPH_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    SPH_CUDA(ctx, cudaEventRecord(ctx->ev_begin, ctx->stream));
+    SPH_TRY(sph_step(ctx, n_steps));
+    SPH_CUDA(ctx, cudaEventRecord(ctx->ev_end, ctx->stream));
+    SPH_CUDA(ctx, cudaEventSynchronize(ctx->ev_end));
+    float ms = 0.0f;
+    SPH_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev_begin, ctx->ev_end));
+    *device_ms = ms;
+    return SPH_OK;
+}
+
+int sph_get_counters(sph_ctx *ctx, int64_t out[8]) {
+    if (!ctx || !out) return SPH_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    int64_t w[8];
+    SPH_TRY(sph_work_counts(ctx, w));
+    out[0] = ctx->launches;
+    out[1] = w[0];
+    out[2] = w[1];
+    out[3] = w[2];
+    out[4] = w[3];
+    out[5] = w[4];
+    out[6] = w[5];
+    out[7] = w[6];
     return SPH_OK;
 }
 

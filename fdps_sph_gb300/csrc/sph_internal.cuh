@@ -130,10 +130,22 @@ struct sph_ctx {
     bool uploaded = false;
     bool have_forces = false;
 
-    cudaEvent_t ev[32];
+    // per-segment device timings (CUDA events on `stream`), accumulated until reset
+    cudaEvent_t ev[64];
+    int mark_seg[64];
     int n_ev = 0;
-    std::vector<double> timings;
+    double seg_ms[16] = {0};
+    int64_t seg_calls[16] = {0};
     bool timing = false;
+    cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
+
+    int64_t launches = 0;   // kernels launched by this context
+};
+
+// timing segments, in the order sph_get_timings reports them
+enum {
+    SEG_KDP = 0, SEG_TREE, SEG_DENS_LIST, SEG_DENS, SEG_EOS, SEG_DRVT_LIST, SEG_DRVT, SEG_HYDRO_LIST, SEG_HYDRO,
+    SEG_GRAV_LIST, SEG_GRAV, SEG_FINAL, SEG_N
 };
 
 // ---------------------------------------------------------------------------
@@ -162,11 +174,12 @@ int sph_build_sph_lists(sph_ctx *ctx, int mode);
 int sph_build_grav_lists(sph_ctx *ctx);
 
 // passes (sph_pairs.cu)
-int sph_pass_density(sph_ctx *ctx);
+int sph_pass_density(sph_ctx *ctx, int build_lists);
 int sph_pass_eos(sph_ctx *ctx);
-int sph_pass_derivative(sph_ctx *ctx);
-int sph_pass_hydro(sph_ctx *ctx);
-int sph_pass_gravity(sph_ctx *ctx);
+int sph_pass_derivative(sph_ctx *ctx, int build_lists);
+int sph_pass_hydro(sph_ctx *ctx, int build_lists);
+int sph_pass_gravity(sph_ctx *ctx, int build_lists);
+int sph_work_counts(sph_ctx *ctx, int64_t out[8]);
 int sph_pack_mixed(sph_ctx *ctx);
 int sph_kick_drift_predict(sph_ctx *ctx, double dt);
 int sph_final_kick(sph_ctx *ctx, double dt);

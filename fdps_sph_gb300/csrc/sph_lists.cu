@@ -351,6 +351,7 @@ int sph_build_sph_lists(sph_ctx *ctx, int mode) {
             k_sph_lists<1><<<blocks, LIST_WARPS * 32, 0, ctx->stream>>>(n, x, y, z, h, tree_view(ctx), L.nbr, L.cnt,
                                                                        L.K, L.pitch, meta + META_ERR,
                                                                        meta + META_MAXCNT);
+        ++ctx->launches;
         SPH_CUDA(ctx, cudaGetLastError());
         int *hs = (int *)ctx->host_scalars;
         SPH_CUDA(ctx, cudaMemcpyAsync(hs, meta + META_ERR, 4 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -373,8 +374,8 @@ int sph_build_grav_lists(sph_ctx *ctx) {
     const int nc = t.n_cell_host;
     const int grid = 2 * ctx->num_sms;
     cudaStream_t st = ctx->stream;
-    k_mark_groups<<<grid, 256, 0, st>>>(t.meta, t.count, t.parent, ctx->cfg.n_group, G.is_group);
-    k_mark_groups_fix<<<grid, 256, 0, st>>>(t.meta, t.count, t.parent, t.n_child, ctx->cfg.n_group, G.is_group);
+    k_mark_groups<<<grid, 256, 0, st>>>(t.meta, t.count, t.parent, ctx->cfg.n_group, G.is_group); ++ctx->launches;
+    k_mark_groups_fix<<<grid, 256, 0, st>>>(t.meta, t.count, t.parent, t.n_child, ctx->cfg.n_group, G.is_group); ++ctx->launches;
     SPH_TRY(sph_scan_exclusive(ctx, G.is_group, t.tmp_off, nullptr, nc, t.meta + META_NGROUP));
     if (G.cap_groups < nc) {
         const int64_t c = nc + nc / 4 + 64;
@@ -385,7 +386,7 @@ int sph_build_grav_lists(sph_ctx *ctx) {
         SPH_TRY(dalloc_l(ctx, &G.off_spj, c + 1));
         G.cap_groups = c;
     }
-    k_compact_groups<<<grid, 256, 0, st>>>(t.meta, G.is_group, t.tmp_off, G.group_cell);
+    k_compact_groups<<<grid, 256, 0, st>>>(t.meta, G.is_group, t.tmp_off, G.group_cell); ++ctx->launches;
     int *hs = (int *)ctx->host_scalars;
     SPH_CUDA(ctx, cudaMemcpyAsync(hs, t.meta + META_NGROUP, sizeof(int), cudaMemcpyDeviceToHost, st));
     SPH_CUDA(ctx, cudaStreamSynchronize(st));
@@ -397,7 +398,7 @@ int sph_build_grav_lists(sph_ctx *ctx) {
                                                            FLD(ctx->F, SPH_Y, ctx->cap),
                                                            FLD(ctx->F, SPH_Z, ctx->cap), tree_view(ctx), t.rb,
                                                            G.n_epj, G.n_spj, nullptr, nullptr, nullptr, nullptr,
-                                                           t.meta + META_ERR);
+                                                           t.meta + META_ERR); ++ctx->launches;
     SPH_TRY(sph_scan_exclusive(ctx, G.n_epj, G.off_epj, nullptr, ng, nullptr));
     SPH_TRY(sph_scan_exclusive(ctx, G.n_spj, G.off_spj, nullptr, ng, nullptr));
     SPH_CUDA(ctx, cudaMemcpyAsync(hs, G.off_epj + (ng - 1), sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -423,7 +424,7 @@ int sph_build_grav_lists(sph_ctx *ctx) {
     k_grav_lists<true><<<blocks, LIST_WARPS * 32, 0, st>>>(ng, G.group_cell, FLD(ctx->F, SPH_X, ctx->cap),
                                                           FLD(ctx->F, SPH_Y, ctx->cap), FLD(ctx->F, SPH_Z, ctx->cap),
                                                           tree_view(ctx), t.rb, G.n_epj, G.n_spj, G.off_epj,
-                                                          G.off_spj, G.epj, G.spj, t.meta + META_ERR);
+                                                          G.off_spj, G.epj, G.spj, t.meta + META_ERR); ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
     G.valid = true;
     return SPH_OK;

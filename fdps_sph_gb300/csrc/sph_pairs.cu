@@ -665,6 +665,22 @@ __global__ void k_init_smth(int n, const double *m, const double *dens, double *
     gradh[i] = 1.0;
 }
 
+__global__ void k_sum_cnt(int n, const int *cnt, unsigned long long *out) {
+    unsigned long long v = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v += (unsigned)cnt[i];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, v);
+}
+
+__global__ void k_sum_grav_pairs(int ng, const int *group_cell, const int *count, const int *ne, const int *ns,
+                                 unsigned long long *out) {
+    unsigned long long v = 0;
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x)
+        v += (unsigned long long)count[group_cell[g]] * (unsigned long long)(ne[g] + ns[g]);
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, v);
+}
+
 }  // namespace sph
 
 using namespace sph;
@@ -695,22 +711,22 @@ int sph_pack_mixed(sph_ctx *ctx) {
     k_pack_df<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, CF(SPH_X), CF(SPH_Y), CF(SPH_Z), CF(SPH_VX), CF(SPH_VY),
                                                            CF(SPH_VZ), CF(SPH_MASS), CF(SPH_SMTH),
                                                            ctx->mscale, ctx->xh, ctx->xl, ctx->vhf,
-                                                           ctx->vlf);
+                                                           ctx->vlf); ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
     return SPH_OK;
 }
 
-int sph_pass_density(sph_ctx *ctx) {
-    SPH_TRY(sph_build_sph_lists(ctx, 0));
+int sph_pass_density(sph_ctx *ctx, int build_lists) {
+    if (build_lists) SPH_TRY(sph_build_sph_lists(ctx, 0));
     const int n = (int)ctx->n;
     const SphLists &L = ctx->lists[0];
     if (ctx->cfg.precision == SPH_PREC_MIXED) {
         k_density32<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, ctx->xh, ctx->xl, CF(SPH_MASS), CF(SPH_SMTH),
                                                               CF(SPH_DENS), L.nbr, L.cnt, L.pitch,
-                                                              1.0 / ctx->mscale);
+                                                              1.0 / ctx->mscale); ++ctx->launches;
     } else {
         k_density64<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, CF(SPH_X), CF(SPH_Y), CF(SPH_Z), CF(SPH_MASS),
-                                                              CF(SPH_SMTH), CF(SPH_DENS), L.nbr, L.cnt, L.pitch);
+                                                              CF(SPH_SMTH), CF(SPH_DENS), L.nbr, L.cnt, L.pitch); ++ctx->launches;
     }
     SPH_CUDA(ctx, cudaGetLastError());
     return SPH_OK;
@@ -719,61 +735,63 @@ int sph_pass_density(sph_ctx *ctx) {
 int sph_pass_eos(sph_ctx *ctx) {
     const int n = (int)ctx->n;
     k_eos<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, ctx->mats_dev, ctx->mat, CF(SPH_DENS), CF(SPH_ENG),
-                                                    CF(SPH_PRES), CF(SPH_SNDS));
+                                                    CF(SPH_PRES), CF(SPH_SNDS)); ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
     return SPH_OK;
 }
 
-int sph_pass_derivative(sph_ctx *ctx) {
-    SPH_TRY(sph_build_sph_lists(ctx, 0));
+int sph_pass_derivative(sph_ctx *ctx, int build_lists) {
+    if (build_lists) SPH_TRY(sph_build_sph_lists(ctx, 0));
     const int n = (int)ctx->n;
     const SphLists &L = ctx->lists[0];
     if (ctx->cfg.precision == SPH_PREC_MIXED) {
         DrvtArgs32 a{ctx->xh,     ctx->xl,      ctx->vhf,     ctx->vlf,      CF(SPH_SMTH), CF(SPH_DENS),
                      CF(SPH_SNDS), CF(SPH_DIVV), CF(SPH_ROTX), CF(SPH_ROTY),  CF(SPH_ROTZ), CF(SPH_GRADH),
                      CF(SPH_BAL),  L.nbr,        L.cnt,        L.pitch,       1.0 / ctx->mscale};
-        k_drvt32<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, a);
+        k_drvt32<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, a); ++ctx->launches;
     } else {
         DrvtArgs a{CF(SPH_X),    CF(SPH_Y),    CF(SPH_Z),    CF(SPH_VX),    CF(SPH_VY),   CF(SPH_VZ),
                    CF(SPH_MASS), CF(SPH_SMTH), CF(SPH_DENS), CF(SPH_SNDS),  CF(SPH_DIVV), CF(SPH_ROTX),
                    CF(SPH_ROTY), CF(SPH_ROTZ), CF(SPH_GRADH), CF(SPH_BAL), L.nbr,        L.cnt,
                    L.pitch};
-        k_drvt64<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, a);
+        k_drvt64<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, a); ++ctx->launches;
     }
     SPH_CUDA(ctx, cudaGetLastError());
     return SPH_OK;
 }
 
-int sph_pass_hydro(sph_ctx *ctx) {
-    SPH_TRY(sph_tree_refresh_hmax(ctx));
-    SPH_TRY(sph_build_sph_lists(ctx, 1));
+int sph_pass_hydro(sph_ctx *ctx, int build_lists) {
+    if (build_lists) {
+        SPH_TRY(sph_tree_refresh_hmax(ctx));
+        SPH_TRY(sph_build_sph_lists(ctx, 1));
+    }
     const int n = (int)ctx->n;
     const SphLists &L = ctx->lists[1];
     // scratch: 2 x float4 or 1 x double4 per particle, in the F2 ping-pong block (free between sorts)
     if (ctx->cfg.precision == SPH_PREC_MIXED) {
         float4 *hA = (float4 *)ctx->F2, *hB = hA + ctx->cap;
         k_hydro_pack32<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, CF(SPH_SMTH), CF(SPH_DENS), CF(SPH_PRES),
-                                                                    CF(SPH_SNDS), CF(SPH_GRADH), CF(SPH_BAL), hA, hB);
+                                                                    CF(SPH_SNDS), CF(SPH_GRADH), CF(SPH_BAL), hA, hB); ++ctx->launches;
         HydroArgs32 a{ctx->xh,    ctx->xl,    ctx->vhf,   ctx->vlf,       hA,         hB,    CF(SPH_SMTH),
                       CF(SPH_AX), CF(SPH_AY), CF(SPH_AZ), CF(SPH_ENGDOT), CF(SPH_DT), L.nbr, L.cnt,
                       L.pitch,    1.0 / ctx->mscale};
-        k_hydro32<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, a);
+        k_hydro32<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, a); ++ctx->launches;
     } else {
         double4 *aux = (double4 *)ctx->F2;
         k_hydro_aux64<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, CF(SPH_SMTH), CF(SPH_DENS), CF(SPH_PRES),
-                                                                   CF(SPH_GRADH), aux);
+                                                                   CF(SPH_GRADH), aux); ++ctx->launches;
         HydroArgs a{CF(SPH_X),    CF(SPH_Y),    CF(SPH_Z),     CF(SPH_VX),   CF(SPH_VY),  CF(SPH_VZ),
                     CF(SPH_MASS), CF(SPH_SMTH), CF(SPH_DENS),  CF(SPH_PRES), CF(SPH_SNDS), CF(SPH_GRADH),
                     CF(SPH_BAL),  aux,          CF(SPH_AX),    CF(SPH_AY),   CF(SPH_AZ),  CF(SPH_ENGDOT),
                     CF(SPH_DT),   L.nbr,        L.cnt,         L.pitch};
-        k_hydro64<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, a);
+        k_hydro64<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, a); ++ctx->launches;
     }
     SPH_CUDA(ctx, cudaGetLastError());
     return SPH_OK;
 }
 
-int sph_pass_gravity(sph_ctx *ctx) {
-    SPH_TRY(sph_build_grav_lists(ctx));
+int sph_pass_gravity(sph_ctx *ctx, int build_lists) {
+    if (build_lists) SPH_TRY(sph_build_grav_lists(ctx));
     GravLists &G = ctx->grav;
     Tree &t = ctx->tree;
     if (G.ng == 0) return SPH_OK;
@@ -782,16 +800,16 @@ int sph_pass_gravity(sph_ctx *ctx) {
         if ((int64_t)t.n_cell_host * 2 > ctx->cap * 4) return sph_fail(ctx, SPH_ERR_CAPACITY, "cell pack scratch");
         float4 *ch = (float4 *)ctx->F2, *cl = ch + t.n_cell_host;
         const double gscale = 1.0;
-        k_pack_cells32<<<2 * ctx->num_sms, 256, 0, ctx->stream>>>(t.meta, t.com, ctx->cfg.G, gscale, ch, cl);
+        k_pack_cells32<<<2 * ctx->num_sms, 256, 0, ctx->stream>>>(t.meta, t.com, ctx->cfg.G, gscale, ch, cl); ++ctx->launches;
         k_grav32<<<G.ng, GT, 0, ctx->stream>>>(G.group_cell, t.start, t.count, ctx->xh, ctx->xl, CF(SPH_MASS),
                                                CF(SPH_SMTH), ch, cl, G.n_epj, G.off_epj, G.epj, G.n_spj, G.off_spj,
                                                G.spj, ctx->cfg.G, gscale, 1.0 / gscale, CF(SPH_GX), CF(SPH_GY),
-                                               CF(SPH_GZ), CF(SPH_POT));
+                                               CF(SPH_GZ), CF(SPH_POT)); ++ctx->launches;
     } else {
         k_grav64<<<G.ng, GT, 0, ctx->stream>>>(G.group_cell, t.start, t.count, CF(SPH_X), CF(SPH_Y), CF(SPH_Z),
                                                CF(SPH_MASS), CF(SPH_SMTH), t.com, G.n_epj, G.off_epj, G.epj, G.n_spj,
                                                G.off_spj, G.spj, ctx->cfg.G, CF(SPH_GX), CF(SPH_GY), CF(SPH_GZ),
-                                               CF(SPH_POT));
+                                               CF(SPH_POT)); ++ctx->launches;
     }
     SPH_CUDA(ctx, cudaGetLastError());
     return SPH_OK;
@@ -799,14 +817,14 @@ int sph_pass_gravity(sph_ctx *ctx) {
 
 int sph_kick_drift_predict(sph_ctx *ctx, double dt) {
     const int n = (int)ctx->n;
-    k_kick_drift_predict<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, integ_args(ctx), dt);
+    k_kick_drift_predict<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, integ_args(ctx), dt); ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
     return SPH_OK;
 }
 
 int sph_final_kick(sph_ctx *ctx, double dt) {
     const int n = (int)ctx->n;
-    k_final_kick<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, integ_args(ctx), dt, ctx->cfg.damping);
+    k_final_kick<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, integ_args(ctx), dt, ctx->cfg.damping); ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
     return SPH_OK;
 }
@@ -814,15 +832,15 @@ int sph_final_kick(sph_ctx *ctx, double dt) {
 int sph_ext_force(sph_ctx *ctx) {
     if (!ctx->cfg.ext_damp || ctx->time >= ctx->cfg.ext_damp_tend) return SPH_OK;
     const int n = (int)ctx->n;
-    k_ext_force<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, integ_args(ctx), CF(SPH_DT));
+    k_ext_force<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, integ_args(ctx), CF(SPH_DT)); ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
     return SPH_OK;
 }
 
 int sph_dt_global(sph_ctx *ctx, double *dt_out) {
     const int n = (int)ctx->n;
-    k_min_partial<<<RED_BLOCKS, 256, 0, ctx->stream>>>(n, CF(SPH_DT), ctx->scratch_d);
-    k_min_final<<<1, 32, 0, ctx->stream>>>(ctx->scratch_d, RED_BLOCKS, ctx->scratch_d + RED_BLOCKS * 8);
+    k_min_partial<<<RED_BLOCKS, 256, 0, ctx->stream>>>(n, CF(SPH_DT), ctx->scratch_d); ++ctx->launches;
+    k_min_final<<<1, 32, 0, ctx->stream>>>(ctx->scratch_d, RED_BLOCKS, ctx->scratch_d + RED_BLOCKS * 8); ++ctx->launches;
     SPH_CUDA(ctx, cudaMemcpyAsync(ctx->host_scalars, ctx->scratch_d + RED_BLOCKS * 8, sizeof(double),
                                   cudaMemcpyDeviceToHost, ctx->stream));
     SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -836,8 +854,8 @@ int sph_diag(sph_ctx *ctx, double out[8]) {
     const int n = (int)ctx->n;
     k_diag_partial<<<RED_BLOCKS, 256, 0, ctx->stream>>>(n, CF(SPH_X), CF(SPH_Y), CF(SPH_Z), CF(SPH_VX), CF(SPH_VY),
                                                         CF(SPH_VZ), CF(SPH_MASS), CF(SPH_ENG), CF(SPH_POT),
-                                                        ctx->scratch_d);
-    k_diag_final<<<1, 32, 0, ctx->stream>>>(ctx->scratch_d, RED_BLOCKS, ctx->scratch_d + RED_BLOCKS * 8);
+                                                        ctx->scratch_d); ++ctx->launches;
+    k_diag_final<<<1, 32, 0, ctx->stream>>>(ctx->scratch_d, RED_BLOCKS, ctx->scratch_d + RED_BLOCKS * 8); ++ctx->launches;
     SPH_CUDA(ctx, cudaMemcpyAsync(ctx->host_scalars, ctx->scratch_d + RED_BLOCKS * 8, 8 * sizeof(double),
                                   cudaMemcpyDeviceToHost, ctx->stream));
     SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -848,7 +866,34 @@ int sph_diag(sph_ctx *ctx, double out[8]) {
 int sph_init_smth(sph_ctx *ctx) {
     const int n = (int)ctx->n;
     k_init_smth<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, CF(SPH_MASS), CF(SPH_DENS), CF(SPH_SMTH),
-                                                             CF(SPH_GRADH));
+                                                             CF(SPH_GRADH)); ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
+    return SPH_OK;
+}
+
+// pair counts of the current lists: [0] gather-list pairs (one density or
+// derivative pass), [1] symmetric-list pairs (hydro), [2] gravity i x (EPJ + SPJ)
+// interactions, [3] cells, [4] gravity groups, [5] EPJ entries, [6] SPJ entries
+int sph_work_counts(sph_ctx *ctx, int64_t out[8]) {
+    for (int k = 0; k < 8; ++k) out[k] = 0;
+    unsigned long long *d = (unsigned long long *)(ctx->scratch_d + 4096);
+    SPH_CUDA(ctx, cudaMemsetAsync(d, 0, 3 * sizeof(unsigned long long), ctx->stream));
+    const int n = (int)ctx->n;
+    if (ctx->lists[0].valid) k_sum_cnt<<<2 * ctx->num_sms, 256, 0, ctx->stream>>>(n, ctx->lists[0].cnt, d);
+    if (ctx->lists[1].valid) k_sum_cnt<<<2 * ctx->num_sms, 256, 0, ctx->stream>>>(n, ctx->lists[1].cnt, d + 1);
+    if (ctx->grav.valid && ctx->grav.ng > 0)
+        k_sum_grav_pairs<<<2 * ctx->num_sms, 256, 0, ctx->stream>>>(ctx->grav.ng, ctx->grav.group_cell, ctx->tree.count,
+                                                                    ctx->grav.n_epj, ctx->grav.n_spj, d + 2);
+    SPH_CUDA(ctx, cudaGetLastError());
+    unsigned long long h[3];
+    SPH_CUDA(ctx, cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    out[0] = (int64_t)h[0];
+    out[1] = (int64_t)h[1];
+    out[2] = (int64_t)h[2];
+    out[3] = ctx->tree.n_cell_host;
+    out[4] = ctx->grav.ng;
+    out[5] = ctx->grav.tot_epj;
+    out[6] = ctx->grav.tot_spj;
     return SPH_OK;
 }

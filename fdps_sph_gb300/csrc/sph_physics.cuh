@@ -13,7 +13,11 @@ constexpr double WNORM = 1365.0 / 64.0;            // kernel.h:15
 // (1365/64) / (H^3 pi) with H = 2.5 h
 __device__ __forceinline__ double kernel_norm(double H) { return WNORM / (H * H * H * PI_D); }
 
-// W / norm and (gradW / norm) / dr-factor pieces for s = r / H
+// Wendland C6 pieces for s = r / H (kernel.h:8-34), without the kernel
+// normalisation: w = W / norm and g = (dW/ds) / norm.  The reference writes
+// g = p^7 (p (8 + 50 s + 96 s^2) - 8 (1 + 8 s + 25 s^2 + 32 s^3)) with
+// p = 1 - s; expanded, the bracket is exactly -22 s (1 + 7 s + 16 s^2), the
+// form used here because it has no cancellation at small s.
 __device__ __forceinline__ void wendland_poly(double s, double &w, double &g) {
     const double p = fmax(1.0 - s, 0.0);
     const double poly = 1.0 + s * (8.0 + s * (25.0 + s * 32.0));
@@ -21,7 +25,7 @@ __device__ __forceinline__ void wendland_poly(double s, double &w, double &g) {
     const double p3 = p2 * p;
     const double p7 = p3 * p3 * p;
     w = poly * (p7 * p);
-    g = p7 * (p * (8.0 + s * (50.0 + s * 96.0)) - 8.0 * poly);
+    g = -22.0 * s * (1.0 + s * (7.0 + s * 16.0)) * p7;
 }
 
 __device__ __forceinline__ void wendland_poly_f(float s, float &w, float &g) {
@@ -31,7 +35,7 @@ __device__ __forceinline__ void wendland_poly_f(float s, float &w, float &g) {
     const float p3 = p2 * p;
     const float p7 = p3 * p3 * p;
     w = poly * (p7 * p);
-    g = p7 * (p * (8.0f + s * (50.0f + s * 96.0f)) - 8.0f * poly);
+    g = -22.0f * s * (1.0f + s * (7.0f + s * 16.0f)) * p7;
 }
 
 // std::lower_bound over an ascending axis

@@ -105,18 +105,18 @@ using namespace sph;
 // exclusive scan of int32; length from device (len_dev, if non-null) or host
 int sph_scan_exclusive(sph_ctx *ctx, const int *in, int *out, const int *len_dev, int len_host, int *total_dev) {
     LenArg L{len_dev, len_host, 0};
-    k_scan_reduce<<<SCAN_BLOCKS, SCAN_THREADS, 0, ctx->stream>>>(in, L, ctx->scan.part);
-    k_scan_part<<<1, SCAN_BLOCKS, 0, ctx->stream>>>(ctx->scan.part, SCAN_BLOCKS, total_dev);
-    k_scan_down<<<SCAN_BLOCKS, SCAN_THREADS, 0, ctx->stream>>>(in, out, L, ctx->scan.part);
+    k_scan_reduce<<<SCAN_BLOCKS, SCAN_THREADS, 0, ctx->stream>>>(in, L, ctx->scan.part); ++ctx->launches;
+    k_scan_part<<<1, SCAN_BLOCKS, 0, ctx->stream>>>(ctx->scan.part, SCAN_BLOCKS, total_dev); ++ctx->launches;
+    k_scan_down<<<SCAN_BLOCKS, SCAN_THREADS, 0, ctx->stream>>>(in, out, L, ctx->scan.part); ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
     return SPH_OK;
 }
 
 static int scan_exclusive_diff(sph_ctx *ctx, const int *in, int *out, const int *pair_dev, int *total_dev) {
     LenArg L{pair_dev, 0, 1};
-    k_scan_reduce<<<SCAN_BLOCKS, SCAN_THREADS, 0, ctx->stream>>>(in, L, ctx->scan.part);
-    k_scan_part<<<1, SCAN_BLOCKS, 0, ctx->stream>>>(ctx->scan.part, SCAN_BLOCKS, total_dev);
-    k_scan_down<<<SCAN_BLOCKS, SCAN_THREADS, 0, ctx->stream>>>(in, out, L, ctx->scan.part);
+    k_scan_reduce<<<SCAN_BLOCKS, SCAN_THREADS, 0, ctx->stream>>>(in, L, ctx->scan.part); ++ctx->launches;
+    k_scan_part<<<1, SCAN_BLOCKS, 0, ctx->stream>>>(ctx->scan.part, SCAN_BLOCKS, total_dev); ++ctx->launches;
+    k_scan_down<<<SCAN_BLOCKS, SCAN_THREADS, 0, ctx->stream>>>(in, out, L, ctx->scan.part); ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
     return SPH_OK;
 }
@@ -557,9 +557,9 @@ static int radix_sort(sph_ctx *ctx, int n) {
     uint32_t *va = s.v0, *vb = s.v1;
     for (int pass = 0; pass < 8; ++pass) {
         const int shift = pass * 8;
-        k_rs_hist<<<nb, RS_THREADS, 0, ctx->stream>>>(ka, n, shift, s.hist, nb);
+        k_rs_hist<<<nb, RS_THREADS, 0, ctx->stream>>>(ka, n, shift, s.hist, nb); ++ctx->launches;
         SPH_TRY(sph_scan_exclusive(ctx, (const int *)s.hist, (int *)s.hoff, nullptr, 256 * nb, nullptr));
-        k_rs_scatter<<<nb, RS_THREADS, 0, ctx->stream>>>(ka, va, kb, vb, n, shift, s.hoff, nb);
+        k_rs_scatter<<<nb, RS_THREADS, 0, ctx->stream>>>(ka, va, kb, vb, n, shift, s.hoff, nb); ++ctx->launches;
         std::swap(ka, kb);
         std::swap(va, vb);
     }
@@ -576,14 +576,14 @@ int sph_sort_and_build(sph_ctx *ctx) {
     SPH_TRY(sph_tree_reserve(ctx, n));
     cudaStream_t st = ctx->stream;
     // root box
-    k_bbox_partial<<<BOX_BLOCKS, 256, 0, st>>>(x, y, z, n, ctx->scratch_d);
-    k_bbox_final<<<1, 32, 0, st>>>(ctx->scratch_d, BOX_BLOCKS, ctx->cfg.theta, t.rb);
-    k_tree_init<<<1, 32, 0, st>>>(n, t.meta, t.start, t.count, t.level, t.parent, t.first_child, t.n_child);
-    k_keys<<<sph_div_up(n, 256), 256, 0, st>>>(x, y, z, n, t.rb, ctx->sort.k0, ctx->sort.v0, t.meta + META_ERR);
+    k_bbox_partial<<<BOX_BLOCKS, 256, 0, st>>>(x, y, z, n, ctx->scratch_d); ++ctx->launches;
+    k_bbox_final<<<1, 32, 0, st>>>(ctx->scratch_d, BOX_BLOCKS, ctx->cfg.theta, t.rb); ++ctx->launches;
+    k_tree_init<<<1, 32, 0, st>>>(n, t.meta, t.start, t.count, t.level, t.parent, t.first_child, t.n_child); ++ctx->launches;
+    k_keys<<<sph_div_up(n, 256), 256, 0, st>>>(x, y, z, n, t.rb, ctx->sort.k0, ctx->sort.v0, t.meta + META_ERR); ++ctx->launches;
     SPH_TRY(radix_sort(ctx, n));
     // permute the particle state into key order
     k_permute<<<sph_div_up(n, 256), 256, 0, st>>>(ctx->F, ctx->F2, cap, n, ctx->sort.v0, ctx->id, ctx->id2,
-                                                  ctx->slot, ctx->slot2, ctx->mat, ctx->mat2);
+                                                  ctx->slot, ctx->slot2, ctx->mat, ctx->mat2); ++ctx->launches;
     std::swap(ctx->F, ctx->F2);
     std::swap(ctx->id, ctx->id2);
     std::swap(ctx->slot, ctx->slot2);
@@ -596,14 +596,14 @@ int sph_sort_and_build(sph_ctx *ctx) {
     // octree, level by level; level sizes stay on the device
     const int grid = 2 * ctx->num_sms;
     for (int l = 0; l < KEY_LEVELS; ++l) {
-        k_split<<<grid, 256, 0, st>>>(l, ctx->cfg.n_leaf, ctx->keys, t.meta, t.start, t.count, t.tmp_cnt, t.tmp_b);
+        k_split<<<grid, 256, 0, st>>>(l, ctx->cfg.n_leaf, ctx->keys, t.meta, t.start, t.count, t.tmp_cnt, t.tmp_b); ++ctx->launches;
         SPH_TRY(scan_exclusive_diff(ctx, t.tmp_cnt, t.tmp_off, t.meta + l, ctx->scan.total));
         k_emit<<<grid, 256, 0, st>>>(l, t.cap, t.meta, t.tmp_cnt, t.tmp_off, t.tmp_b, ctx->scan.total, t.start,
-                                     t.count, t.level, t.parent, t.first_child, t.n_child);
+                                     t.count, t.level, t.parent, t.first_child, t.n_child); ++ctx->launches;
     }
     for (int l = KEY_LEVELS; l >= 0; --l)
         k_moments<<<grid, 128, 0, st>>>(l, t.meta, x, y, z, m, h, t.start, t.count, t.first_child, t.n_child,
-                                        t.mom, t.com, t.blo, t.bhi);
+                                        t.mom, t.com, t.blo, t.bhi); ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
     // bring back the cell count and the error word (one small synchronous read per tree)
     int *hs = (int *)ctx->host_scalars;
@@ -622,7 +622,7 @@ int sph_tree_refresh_hmax(sph_ctx *ctx) {
     const double *h = FLD(ctx->F, SPH_SMTH, ctx->cap);
     const int grid = 2 * ctx->num_sms;
     for (int l = KEY_LEVELS; l >= 0; --l)
-        k_hmax<<<grid, 128, 0, ctx->stream>>>(l, t.meta, h, t.start, t.count, t.first_child, t.n_child, t.bhi);
+        k_hmax<<<grid, 128, 0, ctx->stream>>>(l, t.meta, h, t.start, t.count, t.first_child, t.n_child, t.bhi); ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
     return SPH_OK;
 }

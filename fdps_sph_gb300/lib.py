@@ -36,8 +36,11 @@ EXPORTS = [
     "sph_batch_last_error", "sph_config_default", "sph_ctx_create", "sph_ctx_destroy", "sph_last_error",
     "sph_set_eos_table", "sph_load_eos_table_file", "sph_set_eos_tillotson", "sph_upload", "sph_download",
     "sph_prologue", "sph_step", "sph_get_time", "sph_diagnostics", "sph_run_pass", "sph_get_order",
-    "sph_get_neighbors", "sph_get_tree", "sph_get_grav_list", "sph_get_timings",
+    "sph_get_neighbors", "sph_get_tree", "sph_get_grav_list", "sph_get_timings", "sph_step_timed",
+    "sph_get_counters", "sph_probe_peak",
 ]
+SEGMENTS = ["kdp", "tree", "dens_list", "dens", "eos", "drvt_list", "drvt", "hydro_list", "hydro", "grav_list",
+            "grav", "final"]
 
 
 class SphError(RuntimeError):
@@ -83,7 +86,10 @@ def load() -> C.CDLL:
     L.sph_set_eos_table.argtypes = [P, C.c_int, P, C.c_int, P, C.c_int, P, P]
     L.sph_load_eos_table_file.argtypes = [P, C.c_int, C.c_char_p]
     L.sph_set_eos_tillotson.argtypes = [P, C.c_int, P]
-    L.sph_upload.argtypes = [P, C.c_int64, P, C.c_int64, P, P, C.c_double, C.c_int]
+    L.sph_upload.argtypes = [P, C.c_int64, P, C.c_int64, P, P, C.c_double, C.c_double, C.c_int]
+    L.sph_step_timed.argtypes = [P, C.c_int, C.POINTER(C.c_double)]
+    L.sph_get_counters.argtypes = [P, P]
+    L.sph_probe_peak.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double)]
     L.sph_download.argtypes = [P, P, C.c_int64, P, P]
     L.sph_prologue.argtypes = [P]
     L.sph_step.argtypes = [P, C.c_int]
@@ -162,13 +168,15 @@ class Context:
         self._check(self.L.sph_load_eos_table_file(self.h, k, path.encode()))
 
     # state ----------------------------------------------------------------
-    def upload(self, F: np.ndarray, ids=None, mats=None, time=0.0, init_smth=False):
+    def upload(self, F: np.ndarray, ids=None, mats=None, time=0.0, init_smth=False, dt=0.0, forces_valid=False):
         F = np.ascontiguousarray(F, np.float64)
         assert F.shape[0] == NFIELD
         n = F.shape[1]
         ids = None if ids is None else np.ascontiguousarray(ids, np.int64)
         mats = None if mats is None else np.ascontiguousarray(mats, np.int32)
-        self._check(self.L.sph_upload(self.h, n, _ptr(F), n, _ptr(ids), _ptr(mats), float(time), int(init_smth)))
+        flags = (1 if init_smth else 0) | (2 if forces_valid else 0)
+        self._check(self.L.sph_upload(self.h, n, _ptr(F), F.shape[1], _ptr(ids), _ptr(mats), float(time), float(dt),
+                                      flags))
         self.n = n
 
     def download(self, out: np.ndarray | None = None):
@@ -246,11 +254,26 @@ class Context:
     def enable_timing(self, on=True):
         self._check(self.L.sph_get_timings(self.h, None, -1 if on else -2, None))
 
+    def reset_timing(self):
+        self._check(self.L.sph_get_timings(self.h, None, -3, None))
+
     def timings(self):
+        """accumulated device ms per segment (SEGMENTS order)"""
         buf = np.zeros(32)
         n = C.c_int()
         self._check(self.L.sph_get_timings(self.h, _ptr(buf), 32, C.byref(n)))
-        return buf[:n.value].copy()
+        return dict(zip(SEGMENTS, buf[:n.value].tolist()))
+
+    def step_timed(self, n_steps=1):
+        ms = C.c_double()
+        self._check(self.L.sph_step_timed(self.h, int(n_steps), C.byref(ms)))
+        return ms.value
+
+    def counters(self):
+        out = np.zeros(8, np.int64)
+        self._check(self.L.sph_get_counters(self.h, _ptr(out)))
+        keys = ["launches", "pairs_gather", "pairs_sym", "pairs_grav", "cells", "groups", "epj", "spj"]
+        return dict(zip(keys, out.tolist()))
 
 
 # ---------------------------------------------------------------------------
@@ -309,3 +332,13 @@ def run_walks(kind: str, epi_list, epj_list, spj_list=None, tag: int = 0):
     if len(epi_list) == 0:
         return []
     return retrieve(kind, tag, n_epi)
+
+
+def probe_peak(fp64: bool, device: int = 0) -> float:
+    """Measured FMA rate of the device, TFLOP/s."""
+    L = load()
+    t = C.c_double()
+    rc = L.sph_probe_peak(device, 1 if fp64 else 0, C.byref(t))
+    if rc != SPH_OK:
+        raise SphError(rc, "sph_probe_peak failed")
+    return t.value

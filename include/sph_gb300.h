@@ -143,10 +143,19 @@ int sph_load_eos_table_file(sph_ctx *ctx, int material, const char *path);
 int sph_set_eos_tillotson(sph_ctx *ctx, int material, const double par[10]);
 
 /* Copies n particles (host memory) into the context; particle i keeps slot i
- * for download.  init_smth != 0 applies RealPtcl::initialize
- * (class.h:196-199: h = 1.2 (m / rho)^(1/3), grad_smth = 1). */
+ * for download.  flags:
+ *   SPH_UPLOAD_INIT_SMTH    apply RealPtcl::initialize (class.h:196-199:
+ *                           h = 1.2 (m / rho)^(1/3), grad_smth = 1);
+ *   SPH_UPLOAD_FORCES_VALID the block's acc / grav / eng_dot / dt fields are
+ *                           the forces of this state and `dt` is the global
+ *                           step (system_t::dt, class.h:9), so sph_step may
+ *                           run without a prologue: a host that keeps its
+ *                           particles (as the reference's ParticleSystem does)
+ *                           can upload, step and download every step. */
+#define SPH_UPLOAD_INIT_SMTH 1
+#define SPH_UPLOAD_FORCES_VALID 2
 int sph_upload(sph_ctx *ctx, int64_t n, const double *fields, int64_t ld, const int64_t *id,
-               const int32_t *material, double time, int init_smth);
+               const int32_t *material, double time, double dt, int flags);
 /* Copies the state back in upload order. */
 int sph_download(sph_ctx *ctx, double *fields, int64_t ld, int64_t *id, int32_t *material);
 /* Forces of the current state and the first dt (main.cpp:92-105). */
@@ -176,8 +185,22 @@ int sph_get_tree(sph_ctx *ctx, int64_t *n_cell, int32_t *start, int32_t *count, 
 int sph_get_grav_list(sph_ctx *ctx, int64_t g, int64_t *n_group, int32_t *epj, int64_t cap_epj, int64_t *n_epj,
                       int32_t *spj_level, int32_t *spj_start, int64_t cap_spj, int64_t *n_spj,
                       int32_t *group_start, int32_t *group_count);
-/* Wall time in ms of the device work of each phase of the last step (CUDA events). */
+/* Device time (CUDA events on the context's stream) accumulated per segment
+ * since the last reset, in this order: kick-drift-predict, sort + tree,
+ * density lists, density kernels, EoS, derivative list, derivative kernel,
+ * hydro list, hydro kernel, gravity lists, gravity kernel, final kick + dt.
+ * cap = -1 switches timing on (and resets), -2 switches it off, -3 resets. */
 int sph_get_timings(sph_ctx *ctx, double *ms, int cap, int *n);
+/* sph_step bracketed by CUDA events on the context's stream; device_ms = elapsed. */
+int sph_step_timed(sph_ctx *ctx, int n_steps, double *device_ms);
+/* out[0] kernels launched by the context so far; out[1] gather-list pairs (one
+ * density / derivative pass); out[2] symmetric-list pairs (hydro); out[3]
+ * gravity interactions (sum over groups of n_i x (EPJ + SPJ)); out[4] cells;
+ * out[5] gravity groups; out[6] EPJ entries; out[7] SPJ entries. */
+int sph_get_counters(sph_ctx *ctx, int64_t out[8]);
+/* Measures the FP32 (fp64 = 0) or FP64 (fp64 = 1) fused-multiply-add rate of
+ * the device in TFLOP/s (2 flops per FMA): the roofline of the pair kernels. */
+int sph_probe_peak(int device, int fp64, double *tflops);
 
 #ifdef __cplusplus
 }

@@ -39,8 +39,16 @@ def device_context(materials, **kw):
     return ctx
 
 
-def small_impact(n_target=1800, n_impactor=200, seed=11):
-    return ic.config_small_impact(seed=seed, n_target=n_target, n_impactor=n_impactor)
+def small_impact(n_target=1800, n_impactor=200, seed=11, stir=True):
+    """Two-body impact; with ``stir`` each body also spins and carries a
+    seeded velocity noise, so div v, curl v, AV and du/dt are non-zero."""
+    F, ids, mats, info = ic.config_small_impact(seed=seed, n_target=n_target, n_impactor=n_impactor)
+    if stir:
+        rng = np.random.default_rng(seed + 1000)
+        X = F[[0, 1, 2]].T
+        V = 1.0e-4 * np.cross(np.array([0.3, -0.2, 1.0]), X) + rng.normal(scale=30.0, size=X.shape)
+        F[[3, 4, 5]] += V.T
+    return F, ids, mats, info
 
 
 def by_id(F, ids):
@@ -49,11 +57,12 @@ def by_id(F, ids):
 
 
 def rel_err(a, b, floor):
+    floor = max(float(floor), 1e-300)
     return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), floor))) if len(a) else 0.0
 
 
 def vec_rel_err(A, B, floor_frac=1e-6):
     """max_i |A_i - B_i| / max(|B_i|, floor_frac * max_k |B_k|) for rows of 3-vectors."""
     nb = np.linalg.norm(B, axis=1)
-    fl = floor_frac * (nb.max() if len(nb) else 1.0)
+    fl = max(floor_frac * (nb.max() if len(nb) else 1.0), 1e-300)
     return float(np.max(np.linalg.norm(A - B, axis=1) / np.maximum(nb, fl))) if len(nb) else 0.0
