@@ -104,7 +104,6 @@ int compute_forces(sph_ctx *ctx) {
     SPH_TRY(time_mark(ctx, SEG_DRVT_LIST));
     SPH_TRY(sph_pass_derivative(ctx, 0));
     SPH_TRY(time_mark(ctx, SEG_DRVT));
-    SPH_TRY(sph_tree_refresh_hmax(ctx));
     SPH_TRY(sph_build_sph_lists(ctx, 1));
     SPH_TRY(time_mark(ctx, SEG_HYDRO_LIST));
     SPH_TRY(sph_pass_hydro(ctx, 0));
@@ -200,7 +199,9 @@ int sph_ctx_destroy(sph_ctx *ctx) {
                     ctx->sort.k0, ctx->sort.k1, ctx->sort.v0, ctx->sort.v1, ctx->sort.hist, ctx->sort.hoff,
                     ctx->lists[0].nbr, ctx->lists[0].cnt, ctx->lists[1].nbr, ctx->lists[1].cnt,
                     ctx->grav.group_cell, ctx->grav.is_group, ctx->grav.n_epj, ctx->grav.n_spj, ctx->grav.off_epj,
-                    ctx->grav.off_spj, ctx->grav.epj, ctx->grav.spj, ctx->scan.part, ctx->scan.total};
+                    ctx->grav.off_spj, ctx->grav.epj, ctx->grav.spj, ctx->scan.part, ctx->scan.total,
+                    ctx->sup.nbr, ctx->sup.cnt, ctx->sup.hsup, ctx->sup.pxh, ctx->sup.pxl, ctx->sup.H2f,
+                    ctx->sup.units};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (void *p : ctx->table_allocs) cudaFree(p);

@@ -87,6 +87,21 @@ struct GravLists {
     bool valid = false;
 };
 
+// per-step SPH neighbour superset (sph_nbr.cu)
+struct SphSuper {
+    int64_t pitch = 0, cap_particles = 0, cap_units = 0;
+    int K = 0, K_alloc = 0;
+    int *nbr = nullptr, *cnt = nullptr;   // superset, ELL
+    double *hsup = nullptr;               // h when the superset was built
+    float4 *pxh = nullptr, *pxl = nullptr;  // double-float positions
+    float *H2f = nullptr;                 // (2.5 h)^2 rounded up
+    int2 *units = nullptr;                // (start, count) of the walk units
+    int n_units = 0;
+    bool valid = false;
+    int64_t rebuilds = 0;
+    int rebuilds_step = 0;   // superset builds since the last sort
+};
+
 struct Scan {
     int *part = nullptr;   // [SCAN_BLOCKS + 1]
     int *total = nullptr;  // device int
@@ -120,6 +135,7 @@ struct sph_ctx {
     sph::Tree tree;
     sph::Sort sort;
     sph::SphLists lists[2];
+    sph::SphSuper sup;
     sph::GravLists grav;
     sph::Scan scan;
 
@@ -169,7 +185,9 @@ int sph_sort_and_build(sph_ctx *ctx);          // root box, keys, sort, permute,
 int sph_tree_refresh_hmax(sph_ctx *ctx);       // cell hmax after h changed
 int sph_scan_exclusive(sph_ctx *ctx, const int *in, int *out, const int *len_dev, int len_host, int *total_dev);
 
-// lists (sph_lists.cu)
+// lists (sph_nbr.cu, sph_lists.cu)
+int sph_nbr_prepare(sph_ctx *ctx);       // after the sort
+int sph_nbr_refresh_h(sph_ctx *ctx);     // after h changed
 int sph_build_sph_lists(sph_ctx *ctx, int mode);
 int sph_build_grav_lists(sph_ctx *ctx);
 

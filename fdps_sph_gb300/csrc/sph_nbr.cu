@@ -1,0 +1,455 @@
+// SPH neighbour lists: one tree walk per step, exact lists per pass.
+//
+// The reference gets an i-group and a superset j-list from FDPS for every
+// density, derivative and hydro call (TreeForForceShort::Gather / Symmetry,
+// main.cpp:79-81, 139-143).  Here the j-sets are explicit: for particle i
+//   gather    : { j : |x_j - x_i|^2 < (2.5 h_i)^2 }            (density, derivative)
+//   symmetric : { j : |x_j - x_i|^2 < max(2.5 h_i, 2.5 h_j)^2 }  (hydro)
+// in ascending key order, identical to the oracle's (oracle/sph_oracle.c:
+// or_sph_walk).
+//
+// 1. Units: octree cells with at most 32 particles whose parent holds more;
+//    consecutive sibling units are packed into one warp while they fit.
+//    Units are spatially compact (inside one parent cell), so no warp sees
+//    a group box that straddles a jump of the Morton curve.
+// 2. Superset walk, once per step (after the sort): every warp walks the
+//    octree depth-first in octant order with its unit's bounding box and
+//    keeps j with r_ij < KAPPA * max(H_i, H_j) (FP32 with a generous margin),
+//    the h of that moment being recorded as h_sup.
+// 3. Per pass, a filter kernel keeps the exact set from the superset: FP32
+//    on double-float coordinates with an error band of 2^-19 relative, the
+//    exact FP64 test of the oracle inside the band.  The superset contains
+//    the exact set as long as every h <= KAPPA * h_sup; the filter raises a
+//    flag otherwise and the host rebuilds the superset with the current h.
+#include <algorithm>
+#include <cstring>
+
+#include "sph_internal.cuh"
+
+namespace sph {
+
+constexpr int UNIT = 32;
+constexpr float KAPPA = 1.15f;
+constexpr int NB_WARPS = 4;
+constexpr int NB_CAND = 512;
+constexpr int NB_STACK = 256;
+constexpr unsigned FULLM = 0xffffffffu;
+
+__device__ __forceinline__ float df_sub(float ah, float al, float bh, float bl) { return (ah - bh) + (al - bl); }
+
+// ---------------------------------------------------------------------------
+// units
+
+// number of units contributed by cell c (see file comment); EMIT writes them at off[c]
+template <bool EMIT>
+__global__ void k_units(const int *meta, const int *start, const int *count, const int *first_child,
+                        const int *n_child, int *nunits, const int *off, int2 *units) {
+    const int nc = meta[MAX_LEVELS];
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        const int cnt = count[c], nch = n_child[c];
+        int k = 0;
+        int2 *out = EMIT ? units + off[c] : nullptr;
+        if (c == 0 && cnt <= UNIT) {
+            if (EMIT) out[k] = make_int2(start[c], cnt);
+            ++k;
+        } else if (c == 0 && nch == 0) {
+            for (int s = 0; s < cnt; s += UNIT) {
+                if (EMIT) out[k] = make_int2(start[c] + s, min(UNIT, cnt - s));
+                ++k;
+            }
+        } else if (cnt > UNIT && nch > 0) {
+            const int f = first_child[c];
+            int us = -1, un = 0;
+            for (int q = 0; q < nch; ++q) {
+                const int ch = f + q, cc = count[ch];
+                if (cc <= UNIT) {
+                    if (us >= 0 && un + cc <= UNIT) {
+                        un += cc;
+                    } else {
+                        if (us >= 0) {
+                            if (EMIT) out[k] = make_int2(us, un);
+                            ++k;
+                        }
+                        us = start[ch];
+                        un = cc;
+                    }
+                } else {
+                    if (us >= 0) {
+                        if (EMIT) out[k] = make_int2(us, un);
+                        ++k;
+                    }
+                    us = -1;
+                    un = 0;
+                    if (n_child[ch] == 0) {   // a leaf above the unit size (only at the deepest level)
+                        for (int s = 0; s < cc; s += UNIT) {
+                            if (EMIT) out[k] = make_int2(start[ch] + s, min(UNIT, cc - s));
+                            ++k;
+                        }
+                    }
+                }
+            }
+            if (us >= 0) {
+                if (EMIT) out[k] = make_int2(us, un);
+                ++k;
+            }
+        }
+        if (!EMIT) nunits[c] = k;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// superset walk: one warp per unit
+
+struct WalkTree {
+    const int *start, *count, *first_child, *n_child;
+    const float4 *blo, *bhi;
+};
+
+__device__ __forceinline__ float gap2_rd(float4 a_lo, float4 a_hi, float3 glo, float3 ghi) {
+    const float gx = fmaxf(0.0f, fmaxf(__fsub_rd(a_lo.x, ghi.x), __fsub_rd(glo.x, a_hi.x)));
+    const float gy = fmaxf(0.0f, fmaxf(__fsub_rd(a_lo.y, ghi.y), __fsub_rd(glo.y, a_hi.y)));
+    const float gz = fmaxf(0.0f, fmaxf(__fsub_rd(a_lo.z, ghi.z), __fsub_rd(glo.z, a_hi.z)));
+    return __fadd_rd(__fadd_rd(__fmul_rd(gx, gx), __fmul_rd(gy, gy)), __fmul_rd(gz, gz));
+}
+
+__global__ void __launch_bounds__(NB_WARPS * 32)
+k_sup_walk(int n_units, const int2 *__restrict__ units, const double *__restrict__ x, const double *__restrict__ y,
+           const double *__restrict__ z, const double *__restrict__ h, const float4 *__restrict__ xh,
+           const float4 *__restrict__ xl, const float *__restrict__ H2f, WalkTree T, int *__restrict__ sup,
+           int *__restrict__ cnt, int K, int64_t pitch, int *err, int *maxcnt) {
+    __shared__ int s_stack[NB_WARPS][NB_STACK];
+    __shared__ int s_cand[NB_WARPS][NB_CAND];
+    __shared__ float4 s_ph[NB_WARPS][32];
+    __shared__ float4 s_pl[NB_WARPS][32];
+    __shared__ float s_h2[NB_WARPS][32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int u = blockIdx.x * NB_WARPS + warp;
+    if (u >= n_units) return;   // warp-uniform
+    const int2 U = units[u];
+    const bool valid = lane < U.y;
+    const int i = U.x + (valid ? lane : 0);
+    const double xi = x[i], yi = y[i], zi = z[i];
+    const float4 pih = xh[i], pil = xl[i];
+    const float H2i = valid ? H2f[i] : 0.0f;
+    double lo[3] = {valid ? xi : INFINITY, valid ? yi : INFINITY, valid ? zi : INFINITY};
+    double hi[3] = {valid ? xi : -INFINITY, valid ? yi : -INFINITY, valid ? zi : -INFINITY};
+    float R2 = H2i;
+    for (int o = 16; o > 0; o >>= 1) {
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = fmin(lo[d], __shfl_xor_sync(FULLM, lo[d], o));
+            hi[d] = fmax(hi[d], __shfl_xor_sync(FULLM, hi[d], o));
+        }
+        R2 = fmaxf(R2, __shfl_xor_sync(FULLM, R2, o));
+    }
+    const float3 glo = make_float3(__double2float_rd(lo[0]), __double2float_rd(lo[1]), __double2float_rd(lo[2]));
+    const float3 ghi = make_float3(__double2float_ru(hi[0]), __double2float_ru(hi[1]), __double2float_ru(hi[2]));
+    const float k2 = KAPPA * KAPPA * 1.00390625f;          // kappa^2 (1 + 2^-8): generous, only a superset is needed
+    const float Rg = __fmul_ru(KAPPA * 1.00390625f, __fsqrt_ru(R2));
+    int *stack = s_stack[warp];
+    int *cand = s_cand[warp];
+    int count = 0, nc = 0;
+
+    auto flush = [&]() {
+        for (int b = 0; b < nc; b += 32) {
+            const int k = b + lane;
+            int j = -1;
+            if (k < nc) {
+                j = cand[k];
+                s_ph[warp][lane] = xh[j];
+                s_pl[warp][lane] = xl[j];
+                s_h2[warp][lane] = H2f[j];
+            }
+            __syncwarp();
+            const int tc = min(32, nc - b);
+            for (int t = 0; t < tc; ++t) {
+                const float4 qh = s_ph[warp][t], ql = s_pl[warp][t];
+                const int jj = __shfl_sync(FULLM, j, t);
+                const float dx = df_sub(qh.x, ql.x, pih.x, pil.x);
+                const float dy = df_sub(qh.y, ql.y, pih.y, pil.y);
+                const float dz = df_sub(qh.z, ql.z, pih.z, pil.z);
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                if (valid && r2 < k2 * fmaxf(H2i, s_h2[warp][t])) {
+                    if (count < K) sup[(int64_t)count * pitch + i] = jj;
+                    ++count;
+                }
+            }
+            __syncwarp();
+        }
+        nc = 0;
+    };
+
+    int sp = 0;
+    {
+        const float4 a = T.blo[0], b = T.bhi[0];
+        const float R = fmaxf(Rg, __fmul_ru(2.5f * KAPPA * 1.00390625f, b.w));
+        if (gap2_rd(a, b, glo, ghi) < __fmul_ru(R, R)) {
+            if (lane == 0) stack[0] = 0;
+            sp = 1;
+        }
+        __syncwarp();
+    }
+    while (sp > 0) {
+        const int c = stack[--sp];
+        __syncwarp();
+        const int nch = T.n_child[c];
+        if (nch == 0) {
+            const int s = T.start[c], ct = T.count[c];
+            for (int b0 = 0; b0 < ct; b0 += 32) {
+                if (nc + 32 > NB_CAND) flush();
+                if (b0 + lane < ct) cand[nc + lane] = s + b0 + lane;
+                nc += min(32, ct - b0);
+                __syncwarp();
+            }
+        } else {
+            const int f = T.first_child[c];
+            bool ok = false;
+            if (lane < nch) {
+                const float4 a = T.blo[f + lane], b = T.bhi[f + lane];
+                const float R = fmaxf(Rg, __fmul_ru(2.5f * KAPPA * 1.00390625f, b.w));
+                ok = gap2_rd(a, b, glo, ghi) < __fmul_ru(R, R);
+            }
+            const unsigned mask = __ballot_sync(FULLM, ok);
+            const int np = __popc(mask);
+            if (sp + np > NB_STACK) {
+                if (lane == 0) atomicOr(err, ERR_SPH_LIST_OVERFLOW);
+                break;
+            }
+            if (ok) stack[sp + (np - 1 - __popc(mask & ((1u << lane) - 1u)))] = f + lane;
+            sp += np;
+            __syncwarp();
+        }
+    }
+    flush();
+    if (valid) {
+        cnt[i] = count;
+        if (count > K) atomicOr(err, ERR_SPH_LIST_OVERFLOW);
+    }
+    int m = valid ? count : 0;
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(FULLM, m, o));
+    if (lane == 0) atomicMax(maxcnt, m);
+}
+
+// ---------------------------------------------------------------------------
+// exact filter: one thread per particle
+
+constexpr int ERR_SKIN = 16;
+
+template <int MODE>
+__global__ void __launch_bounds__(128)
+k_filter(int n, const int *__restrict__ sup, const int *__restrict__ scnt, int64_t pitch,
+         const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
+         const double *__restrict__ h, const double *__restrict__ hsup, const float4 *__restrict__ xh,
+         const float4 *__restrict__ xl, const float *__restrict__ H2f, int *__restrict__ out, int *__restrict__ ocnt,
+         int *err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double hi = h[i];
+    if (hi > (double)KAPPA * hsup[i]) atomicOr(err, ERR_SKIN);
+    const double Hi = __dmul_rn(SUPPORT, hi);
+    const double H2 = __dmul_rn(Hi, Hi);
+    const float H2i = (float)H2;
+    const float4 pih = xh[i], pil = xl[i];
+    const double xi = x[i], yi = y[i], zi = z[i];
+    const int c = scnt[i];
+    int k2 = 0;
+    for (int k = 0; k < c; ++k) {
+        const int j = sup[(int64_t)k * pitch + i];
+        const float4 qh = xh[j], ql = xl[j];
+        const float dx = df_sub(qh.x, ql.x, pih.x, pil.x);
+        const float dy = df_sub(qh.y, ql.y, pih.y, pil.y);
+        const float dz = df_sub(qh.z, ql.z, pih.z, pil.z);
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        float thr = H2i;
+        if (MODE == 1) thr = fmaxf(thr, H2f[j]);
+        bool ok;
+        if (r2 < thr * (1.0f - 1.9073486328125e-06f)) {          // 1 - 2^-19
+            ok = true;
+        } else if (r2 > thr * (1.0f + 1.9073486328125e-06f)) {
+            ok = false;
+        } else {
+            // the oracle's exact FP64 decision
+            const double ex = __dsub_rn(x[j], xi), ey = __dsub_rn(y[j], yi), ez = __dsub_rn(z[j], zi);
+            const double rr = __dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez));
+            ok = rr < H2;
+            if (MODE == 1 && !ok) {
+                const double Hj = __dmul_rn(SUPPORT, h[j]);
+                ok = rr < __dmul_rn(Hj, Hj);
+            }
+        }
+        if (ok) out[(int64_t)(k2++) * pitch + i] = j;
+    }
+    ocnt[i] = k2;
+}
+
+// (2.5 h)^2 as float, rounded up so FP32 superset tests stay conservative
+__global__ void k_h2f(int n, const double *h, float *H2f) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double H = SUPPORT * h[i];
+    H2f[i] = __double2float_ru(H * H);
+}
+
+// double-float positions (hi / lo floats); .w of xh carries nothing here
+__global__ void k_pack_pos(int n, const double *x, const double *y, const double *z, float4 *xh, float4 *xl) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float ax = (float)x[i], ay = (float)y[i], az = (float)z[i];
+    xh[i] = make_float4(ax, ay, az, 0.0f);
+    xl[i] = make_float4((float)(x[i] - (double)ax), (float)(y[i] - (double)ay), (float)(z[i] - (double)az), 0.0f);
+}
+
+}  // namespace sph
+
+using namespace sph;
+
+template <class T>
+static int dalloc_n(sph_ctx *ctx, T **p, int64_t n) {
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    cudaError_t e = cudaMalloc((void **)p, sizeof(T) * (size_t)std::max<int64_t>(n, 1));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return sph_fail(ctx, SPH_ERR_OOM, "device allocation of %lld bytes failed", (long long)(sizeof(T) * n));
+    }
+    return SPH_OK;
+}
+
+// h-dependent float copies; called after every density pass and after the sort
+int sph_nbr_refresh_h(sph_ctx *ctx) {
+    SphSuper &S = ctx->sup;
+    const int n = (int)ctx->n;
+    k_h2f<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, FLD(ctx->F, SPH_SMTH, ctx->cap), S.H2f);
+    ++ctx->launches;
+    SPH_CUDA(ctx, cudaGetLastError());
+    return SPH_OK;
+}
+
+// after the sort: positions as double-float, units, and the superset marked stale
+int sph_nbr_prepare(sph_ctx *ctx) {
+    SphSuper &S = ctx->sup;
+    const int n = (int)ctx->n;
+    const int64_t pitch = ((int64_t)n + 31) / 32 * 32;
+    if (S.cap_particles < pitch) {
+        SPH_TRY(dalloc_n(ctx, &S.pxh, pitch));
+        SPH_TRY(dalloc_n(ctx, &S.pxl, pitch));
+        SPH_TRY(dalloc_n(ctx, &S.H2f, pitch));
+        SPH_TRY(dalloc_n(ctx, &S.hsup, pitch));
+        SPH_TRY(dalloc_n(ctx, &S.cnt, pitch));
+        S.cap_particles = pitch;
+    }
+    const int64_t cap = ctx->cap;
+    k_pack_pos<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap),
+                                                            FLD(ctx->F, SPH_Z, cap), S.pxh, S.pxl);
+    ++ctx->launches;
+    SPH_TRY(sph_nbr_refresh_h(ctx));
+    // units
+    Tree &t = ctx->tree;
+    const int nc = t.n_cell_host;
+    const int grid = 2 * ctx->num_sms;
+    k_units<false><<<grid, 256, 0, ctx->stream>>>(t.meta, t.start, t.count, t.first_child, t.n_child, t.tmp_cnt,
+                                                  nullptr, nullptr);
+    ++ctx->launches;
+    SPH_TRY(sph_scan_exclusive(ctx, t.tmp_cnt, t.tmp_off, nullptr, nc, ctx->scan.total));
+    int tot = 0;
+    SPH_CUDA(ctx, cudaMemcpyAsync(&ctx->host_scalars[0], ctx->scan.total, sizeof(int), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    std::memcpy(&tot, &ctx->host_scalars[0], sizeof(int));
+    if (S.cap_units < tot) {
+        S.cap_units = tot + tot / 4 + 64;
+        SPH_TRY(dalloc_n(ctx, &S.units, S.cap_units));
+    }
+    k_units<true><<<grid, 256, 0, ctx->stream>>>(t.meta, t.start, t.count, t.first_child, t.n_child, nullptr,
+                                                 t.tmp_off, S.units);
+    ++ctx->launches;
+    SPH_CUDA(ctx, cudaGetLastError());
+    S.n_units = tot;
+    S.valid = false;
+    S.rebuilds_step = 0;
+    ctx->lists[0].valid = ctx->lists[1].valid = false;
+    return SPH_OK;
+}
+
+static int build_superset(sph_ctx *ctx) {
+    SphSuper &S = ctx->sup;
+    const int n = (int)ctx->n;
+    const int64_t pitch = ((int64_t)n + 31) / 32 * 32;
+    const int64_t cap = ctx->cap;
+    int *meta = ctx->tree.meta;
+    Tree &t = ctx->tree;
+    if (S.K == 0) S.K = 192;
+    if (S.rebuilds_step > 0) SPH_TRY(sph_tree_refresh_hmax(ctx));   // cell hmax must follow the current h
+    S.rebuilds_step += 1;
+    SPH_CUDA(ctx, cudaMemcpyAsync(S.hsup, FLD(ctx->F, SPH_SMTH, cap), sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                                  ctx->stream));
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        if (!S.nbr || S.pitch < pitch || S.K_alloc < S.K) {
+            SPH_TRY(dalloc_n(ctx, &S.nbr, (int64_t)S.K * pitch));
+            for (int m = 0; m < 2; ++m) {
+                SPH_TRY(dalloc_n(ctx, &ctx->lists[m].nbr, (int64_t)S.K * pitch));
+                SPH_TRY(dalloc_n(ctx, &ctx->lists[m].cnt, pitch));
+                ctx->lists[m].K = ctx->lists[m].K_alloc = S.K;
+                ctx->lists[m].pitch = pitch;
+            }
+            S.pitch = pitch;
+            S.K_alloc = S.K;
+        }
+        SPH_CUDA(ctx, cudaMemsetAsync(meta + META_ERR, 0, sizeof(int), ctx->stream));
+        SPH_CUDA(ctx, cudaMemsetAsync(meta + META_MAXCNT, 0, sizeof(int), ctx->stream));
+        const int blocks = (S.n_units + NB_WARPS - 1) / NB_WARPS;
+        WalkTree T{t.start, t.count, t.first_child, t.n_child, t.blo, t.bhi};
+        k_sup_walk<<<blocks, NB_WARPS * 32, 0, ctx->stream>>>(
+            S.n_units, S.units, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
+            FLD(ctx->F, SPH_SMTH, cap), S.pxh, S.pxl, S.H2f, T, S.nbr, S.cnt, S.K, S.pitch, meta + META_ERR,
+            meta + META_MAXCNT);
+        ++ctx->launches;
+        SPH_CUDA(ctx, cudaGetLastError());
+        int *hs = (int *)ctx->host_scalars;
+        SPH_CUDA(ctx, cudaMemcpyAsync(hs, meta + META_ERR, 4 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        const int errw = hs[0], maxc = hs[META_MAXCNT - META_ERR];
+        if (errw & ERR_SPH_LIST_OVERFLOW) {
+            if (maxc <= S.K) return sph_fail(ctx, SPH_ERR_CAPACITY, "SPH walk stack overflow");
+            S.K = maxc + maxc / 4 + 16;
+            continue;
+        }
+        S.valid = true;
+        S.rebuilds += 1;
+        return SPH_OK;
+    }
+    return sph_fail(ctx, SPH_ERR_CAPACITY, "SPH superset capacity could not be grown");
+}
+
+// exact list of `mode` (0 gather, 1 symmetric) for the current h
+int sph_build_sph_lists(sph_ctx *ctx, int mode) {
+    SphSuper &S = ctx->sup;
+    const int n = (int)ctx->n;
+    const int64_t cap = ctx->cap;
+    int *meta = ctx->tree.meta;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        if (!S.valid) SPH_TRY(build_superset(ctx));
+        SphLists &L = ctx->lists[mode];
+        SPH_CUDA(ctx, cudaMemsetAsync(meta + META_ERR, 0, sizeof(int), ctx->stream));
+        if (mode == 0)
+            k_filter<0><<<sph_div_up(n, 128), 128, 0, ctx->stream>>>(
+                n, S.nbr, S.cnt, S.pitch, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
+                FLD(ctx->F, SPH_SMTH, cap), S.hsup, S.pxh, S.pxl, S.H2f, L.nbr, L.cnt, meta + META_ERR);
+        else
+            k_filter<1><<<sph_div_up(n, 128), 128, 0, ctx->stream>>>(
+                n, S.nbr, S.cnt, S.pitch, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
+                FLD(ctx->F, SPH_SMTH, cap), S.hsup, S.pxh, S.pxl, S.H2f, L.nbr, L.cnt, meta + META_ERR);
+        ++ctx->launches;
+        SPH_CUDA(ctx, cudaGetLastError());
+        int *hs = (int *)ctx->host_scalars;
+        SPH_CUDA(ctx, cudaMemcpyAsync(hs, meta + META_ERR, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (hs[0] & ERR_SKIN) {   // some h grew past the skin: walk again with the current h
+            S.valid = false;
+            continue;
+        }
+        L.valid = true;
+        return SPH_OK;
+    }
+    return sph_fail(ctx, SPH_ERR_CAPACITY, "SPH neighbour superset invalid after rebuild");
+}

@@ -729,7 +729,7 @@ int sph_pass_density(sph_ctx *ctx, int build_lists) {
                                                               CF(SPH_SMTH), CF(SPH_DENS), L.nbr, L.cnt, L.pitch); ++ctx->launches;
     }
     SPH_CUDA(ctx, cudaGetLastError());
-    return SPH_OK;
+    return sph_nbr_refresh_h(ctx);
 }
 
 int sph_pass_eos(sph_ctx *ctx) {
@@ -761,10 +761,7 @@ int sph_pass_derivative(sph_ctx *ctx, int build_lists) {
 }
 
 int sph_pass_hydro(sph_ctx *ctx, int build_lists) {
-    if (build_lists) {
-        SPH_TRY(sph_tree_refresh_hmax(ctx));
-        SPH_TRY(sph_build_sph_lists(ctx, 1));
-    }
+    if (build_lists) SPH_TRY(sph_build_sph_lists(ctx, 1));
     const int n = (int)ctx->n;
     const SphLists &L = ctx->lists[1];
     // scratch: 2 x float4 or 1 x double4 per particle, in the F2 ping-pong block (free between sorts)

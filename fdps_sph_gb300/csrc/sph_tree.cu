@@ -612,9 +612,8 @@ int sph_sort_and_build(sph_ctx *ctx) {
     if (hs[META_ERR] & ERR_NONFINITE) return sph_fail(ctx, SPH_ERR_NONFINITE, "non-finite particle position");
     if (hs[META_ERR] & ERR_CELL_OVERFLOW) return sph_fail(ctx, SPH_ERR_CAPACITY, "octree cell capacity exceeded");
     t.n_cell_host = hs[MAX_LEVELS];
-    ctx->lists[0].valid = ctx->lists[1].valid = false;
     ctx->grav.valid = false;
-    return SPH_OK;
+    return sph_nbr_prepare(ctx);
 }
 
 int sph_tree_refresh_hmax(sph_ctx *ctx) {

@@ -467,8 +467,10 @@ int64_t or_sph_list(const or_tree *t, const double *x, const double *y, const do
 /* Gravity interaction lists (TreeForForceLong::Monopole, main.cpp:83,90).
  * Walk from the root; a child cell is opened iff dmin^2(group box, child com)
  * <= (child side / theta)^2, i.e. rc2[level] = root_len^2/theta^2 * 0.25^level.
- * Opened leaves contribute their particles (EPJ, the group's own included);
- * unopened cells contribute their monopole (SPJ). */
+ * Opened leaves contribute their particles (EPJ, the group's own included).
+ * For every opened internal cell, its unopened children are emitted as
+ * monopoles (SPJ) in octant order, then the walk descends into its opened
+ * children in octant order (depth first). */
 
 typedef struct { or_ibuf epj, spj; } or_glist;
 
@@ -479,13 +481,15 @@ static void or_grav_walk(const or_tree *t, int32_t ci, const double blo[3], cons
         for (int32_t j = c->start; j < c->start + c->count; ++j) or_ibuf_push(&L->epj, j);
         return;
     }
+    int near[8];
     for (int k = 0; k < c->n_child; ++k) {
         const int32_t chi = c->first_child + k;
         const or_cell *ch = &t->c[chi];
-        const double d2 = or_dmin2(blo, bhi, ch->com);
-        if (d2 <= rc2[ch->level]) or_grav_walk(t, chi, blo, bhi, rc2, L);
-        else or_ibuf_push(&L->spj, chi);
+        near[k] = or_dmin2(blo, bhi, ch->com) <= rc2[ch->level];
+        if (!near[k]) or_ibuf_push(&L->spj, chi);
     }
+    for (int k = 0; k < c->n_child; ++k)
+        if (near[k]) or_grav_walk(t, c->first_child + k, blo, bhi, rc2, L);
 }
 
 static void or_rcrit_table(const or_tree *t, double theta, double rc2[OR_KEY_LEVELS + 1]) {
