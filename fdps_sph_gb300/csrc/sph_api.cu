@@ -93,9 +93,16 @@ int compute_forces(sph_ctx *ctx) {
     if (ctx->cfg.precision == SPH_PREC_MIXED) SPH_TRY(sph_pack_mixed(ctx));
     SPH_TRY(time_mark(ctx, SEG_TREE));
     for (int it = 0; it < ctx->cfg.n_dens_iter; ++it) {
-        SPH_TRY(sph_build_sph_lists(ctx, 0));
-        SPH_TRY(time_mark(ctx, SEG_DENS_LIST));
-        SPH_TRY(sph_pass_density(ctx, 0));
+        if (ctx->cfg.precision == SPH_PREC_MIXED) {
+            // the list-free pass makes the same neighbour decisions as the exact list
+            SPH_TRY(sph_nbr_ensure_superset(ctx));
+            SPH_TRY(time_mark(ctx, SEG_DENS_LIST));
+            SPH_TRY(sph_density_from_superset(ctx));
+        } else {
+            SPH_TRY(sph_build_sph_lists(ctx, 0));
+            SPH_TRY(time_mark(ctx, SEG_DENS_LIST));
+            SPH_TRY(sph_pass_density(ctx, 0));
+        }
         SPH_TRY(time_mark(ctx, SEG_DENS));
     }
     SPH_TRY(sph_pass_eos(ctx));
@@ -201,7 +208,7 @@ int sph_ctx_destroy(sph_ctx *ctx) {
                     ctx->grav.group_cell, ctx->grav.is_group, ctx->grav.n_epj, ctx->grav.n_spj, ctx->grav.off_epj,
                     ctx->grav.off_spj, ctx->grav.epj, ctx->grav.spj, ctx->scan.part, ctx->scan.total,
                     ctx->sup.nbr, ctx->sup.cnt, ctx->sup.hsup, ctx->sup.pxh, ctx->sup.pxl, ctx->sup.H2f,
-                    ctx->sup.units};
+                    ctx->sup.units, ctx->grav.cinfo, ctx->sup.r2, ctx->sup.mf};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (void *p : ctx->table_allocs) cudaFree(p);

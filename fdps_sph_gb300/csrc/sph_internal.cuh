@@ -82,6 +82,8 @@ struct GravLists {
     int *n_epj = nullptr, *n_spj = nullptr;          // [ng]
     int *off_epj = nullptr, *off_spj = nullptr;      // [ng]
     int *epj = nullptr, *spj = nullptr;
+    int4 *cinfo = nullptr;                           // [cells] first_child, n_child, start, count
+    int64_t cap_cinfo = 0;
     int ng = 0;
     int64_t tot_epj = 0, tot_spj = 0;
     bool valid = false;
@@ -92,6 +94,8 @@ struct SphSuper {
     int64_t pitch = 0, cap_particles = 0, cap_units = 0;
     int K = 0, K_alloc = 0;
     int *nbr = nullptr, *cnt = nullptr;   // superset, ELL
+    float *r2 = nullptr;                  // FP32 r^2 of every superset entry
+    float *mf = nullptr;                  // particle mass x mscale as float
     double *hsup = nullptr;               // h when the superset was built
     float4 *pxh = nullptr, *pxl = nullptr;  // double-float positions
     float *H2f = nullptr;                 // (2.5 h)^2 rounded up
@@ -189,6 +193,8 @@ int sph_scan_exclusive(sph_ctx *ctx, const int *in, int *out, const int *len_dev
 int sph_nbr_prepare(sph_ctx *ctx);       // after the sort
 int sph_nbr_refresh_h(sph_ctx *ctx);     // after h changed
 int sph_build_sph_lists(sph_ctx *ctx, int mode);
+int sph_density_from_superset(sph_ctx *ctx);
+int sph_nbr_ensure_superset(sph_ctx *ctx);   // mixed precision: density pass without an exact list
 int sph_build_grav_lists(sph_ctx *ctx);
 
 // passes (sph_pairs.cu)

@@ -5,10 +5,9 @@
 // (cells with <= n_group particles whose parent holds more) walks the tree
 // with the group's FP64 bounding box; a child is opened iff
 // dmin^2(box, com) <= (side / theta)^2.  Opened leaves give EPJ particle
-// ranges; for every opened internal cell its unopened children are emitted
-// as SPJ monopoles (octant order) before the walk descends into its opened
-// children (octant order, depth-first) -- the order of the oracle's
-// or_grav_walk.  Counting pass, scan, filling pass.
+// ranges, unopened children of opened cells give SPJ monopoles, in the
+// breadth-first order of the oracle's or_grav_walk.  Counting pass, scan,
+// filling pass.
 #include <algorithm>
 
 #include "sph_internal.cuh"
@@ -65,19 +64,26 @@ __global__ void k_compact_groups(const int *meta, const int *is_group, const int
         if (is_group[c]) group_cell[off[c]] = c;
 }
 
-constexpr int GSTACK = 256;
+constexpr int GQ_WARPS = 2;
+constexpr int GQCAP = 2048;   // ring buffer of opened cells per warp
 
+// Breadth-first walk, four opened cells per iteration (eight lanes each).
+// Order (shared with the oracle's or_grav_walk): cells are opened in FIFO
+// order starting at the root; an opened leaf appends its particles to EPJ;
+// an opened internal cell appends its unopened children to SPJ and its
+// opened children to the queue, both in octant order.
 template <bool FILL>
-__global__ void __launch_bounds__(LIST_WARPS * 32)
+__global__ void __launch_bounds__(GQ_WARPS * 32)
 k_grav_lists(int ng, const int *__restrict__ group_cell, const double *__restrict__ x,
-             const double *__restrict__ y, const double *__restrict__ z, TreeView T, const double *__restrict__ rb,
+             const double *__restrict__ y, const double *__restrict__ z, const int4 *__restrict__ cinfo,
+             const int *__restrict__ clevel, const double4 *__restrict__ com, const double *__restrict__ rb,
              int *n_epj, int *n_spj, const int *off_epj, const int *off_spj, int *epj, int *spj, int *err) {
-    __shared__ int s_stack[LIST_WARPS][GSTACK];
+    __shared__ int s_q[GQ_WARPS][GQCAP];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int g = blockIdx.x * LIST_WARPS + warp;
+    const int g = blockIdx.x * GQ_WARPS + warp;
     if (g >= ng) return;
-    const int gc = group_cell[g];
-    const int s = T.start[gc], cnt = T.count[gc];
+    const int4 gi = cinfo[group_cell[g]];
+    const int s = gi.z, cnt = gi.w;
     double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (int k = lane; k < cnt; k += 32) {
         const double p[3] = {x[s + k], y[s + k], z[s + k]};
@@ -90,53 +96,70 @@ k_grav_lists(int ng, const int *__restrict__ group_cell, const double *__restric
         lo[d] = warp_min_d(lo[d]);
         hi[d] = warp_max_d(hi[d]);
     }
-    int *stack = s_stack[warp];
+    int *Q = s_q[warp];
     int ne = 0, ns = 0;
     const int be = FILL ? off_epj[g] : 0, bs = FILL ? off_spj[g] : 0;
-    if (lane == 0) stack[0] = 0;
-    int sp = 1;
+    if (lane == 0) Q[0] = 0;
+    int head = 0, tail = 1;
+    const int q = lane >> 3, k = lane & 7;
+    const unsigned below = (1u << lane) - 1u;
     __syncwarp();
-    while (sp > 0) {
-        const int c = stack[--sp];
-        __syncwarp();
-        const int nch = T.n_child[c];
-        if (nch == 0) {
-            const int cs = T.start[c], ct = T.count[c];
-            if (FILL)
-                for (int k = lane; k < ct; k += 32) epj[be + ne + k] = cs + k;
-            ne += ct;
-            continue;
+    while (head < tail) {
+        const int nproc = min(4, tail - head);
+        const bool act = q < nproc;
+        const int c = act ? Q[(head + q) & (GQCAP - 1)] : 0;
+        const int4 ci = cinfo[c];                       // first_child, n_child, start, count
+        const bool leaf = act && ci.y == 0;
+        // opened leaves, in queue order
+        for (int qq = 0; qq < nproc; ++qq) {
+            const int cs = __shfl_sync(FULL, ci.z, qq * 8), ct = __shfl_sync(FULL, ci.w, qq * 8);
+            const int lf = __shfl_sync(FULL, (int)leaf, qq * 8);
+            if (lf) {
+                if (FILL)
+                    for (int t = lane; t < ct; t += 32) epj[be + ne + t] = cs + t;
+                ne += ct;
+            }
         }
-        const int f = T.first_child[c];
-        bool near = false;
-        if (lane < nch) {
-            const double4 cm = T.com[f + lane];
+        bool near = false, far = false;
+        int ch = 0;
+        if (act && !leaf && k < ci.y) {
+            ch = ci.x + k;
+            const double4 cm = com[ch];
             const double p[3] = {cm.x, cm.y, cm.z};
             double dd[3];
             for (int d = 0; d < 3; ++d)
                 dd[d] = (p[d] < lo[d]) ? __dsub_rn(lo[d], p[d]) : ((p[d] > hi[d]) ? __dsub_rn(p[d], hi[d]) : 0.0);
             const double d2 =
                 __dadd_rn(__dadd_rn(__dmul_rn(dd[0], dd[0]), __dmul_rn(dd[1], dd[1])), __dmul_rn(dd[2], dd[2]));
-            near = d2 <= rb[8 + T.level[f + lane]];
+            near = d2 <= rb[8 + clevel[ch]];
+            far = !near;
         }
-        const unsigned below = (1u << lane) - 1u;
         const unsigned nmask = __ballot_sync(FULL, near);
-        const unsigned fmask = __ballot_sync(FULL, lane < nch && !near);
-        if (FILL && lane < nch && !near) spj[bs + ns + __popc(fmask & below)] = f + lane;
+        const unsigned fmask = __ballot_sync(FULL, far);
+        if (FILL && far) spj[bs + ns + __popc(fmask & below)] = ch;
         ns += __popc(fmask);
-        const int np = __popc(nmask);
-        if (sp + np > GSTACK) {
+        const int nn = __popc(nmask);
+        if (tail - head - nproc + nn > GQCAP) {
             if (lane == 0) atomicOr(err, ERR_GRAV_OVERFLOW);
             break;
         }
-        if (near) stack[sp + (np - 1 - __popc(nmask & below))] = f + lane;
-        sp += np;
+        __syncwarp();
+        if (near) Q[(tail + __popc(nmask & below)) & (GQCAP - 1)] = ch;
+        tail += nn;
+        head += nproc;
         __syncwarp();
     }
     if (!FILL && lane == 0) {
         n_epj[g] = ne;
         n_spj[g] = ns;
     }
+}
+
+__global__ void k_pack_cinfo(const int *meta, const int *first_child, const int *n_child, const int *start,
+                             const int *count, int4 *cinfo) {
+    const int nc = meta[MAX_LEVELS];
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x)
+        cinfo[c] = make_int4(first_child[c], n_child[c], start[c], count[c]);
 }
 
 }  // namespace sph
@@ -155,11 +178,6 @@ static int dalloc_l(sph_ctx *ctx, T **p, int64_t n) {
         return sph_fail(ctx, SPH_ERR_OOM, "device allocation of %lld bytes failed", (long long)(sizeof(T) * n));
     }
     return SPH_OK;
-}
-
-static TreeView tree_view(sph_ctx *ctx) {
-    Tree &t = ctx->tree;
-    return TreeView{t.start, t.count, t.first_child, t.n_child, t.level, t.blo, t.bhi, t.com};
 }
 
 int sph_build_grav_lists(sph_ctx *ctx) {
@@ -186,13 +204,18 @@ int sph_build_grav_lists(sph_ctx *ctx) {
     SPH_CUDA(ctx, cudaStreamSynchronize(st));
     const int ng = hs[0];
     G.ng = ng;
-    const int blocks = (ng + LIST_WARPS - 1) / LIST_WARPS;
+    const int blocks = (ng + GQ_WARPS - 1) / GQ_WARPS;
+    if (G.cap_cinfo < nc) {
+        G.cap_cinfo = t.cap;
+        SPH_TRY(dalloc_l(ctx, &G.cinfo, G.cap_cinfo));
+    }
+    k_pack_cinfo<<<grid, 256, 0, st>>>(t.meta, t.first_child, t.n_child, t.start, t.count, G.cinfo);
+    ++ctx->launches;
     SPH_CUDA(ctx, cudaMemsetAsync(t.meta + META_ERR, 0, sizeof(int), st));
-    k_grav_lists<false><<<blocks, LIST_WARPS * 32, 0, st>>>(ng, G.group_cell, FLD(ctx->F, SPH_X, ctx->cap),
-                                                           FLD(ctx->F, SPH_Y, ctx->cap),
-                                                           FLD(ctx->F, SPH_Z, ctx->cap), tree_view(ctx), t.rb,
-                                                           G.n_epj, G.n_spj, nullptr, nullptr, nullptr, nullptr,
-                                                           t.meta + META_ERR); ++ctx->launches;
+    k_grav_lists<false><<<blocks, GQ_WARPS * 32, 0, st>>>(ng, G.group_cell, FLD(ctx->F, SPH_X, ctx->cap),
+                                                         FLD(ctx->F, SPH_Y, ctx->cap), FLD(ctx->F, SPH_Z, ctx->cap),
+                                                         G.cinfo, t.level, t.com, t.rb, G.n_epj, G.n_spj, nullptr,
+                                                         nullptr, nullptr, nullptr, t.meta + META_ERR); ++ctx->launches;
     SPH_TRY(sph_scan_exclusive(ctx, G.n_epj, G.off_epj, nullptr, ng, nullptr));
     SPH_TRY(sph_scan_exclusive(ctx, G.n_spj, G.off_spj, nullptr, ng, nullptr));
     SPH_CUDA(ctx, cudaMemcpyAsync(hs, G.off_epj + (ng - 1), sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -215,10 +238,10 @@ int sph_build_grav_lists(sph_ctx *ctx) {
     }
     G.tot_epj = tot_e;
     G.tot_spj = tot_s;
-    k_grav_lists<true><<<blocks, LIST_WARPS * 32, 0, st>>>(ng, G.group_cell, FLD(ctx->F, SPH_X, ctx->cap),
-                                                          FLD(ctx->F, SPH_Y, ctx->cap), FLD(ctx->F, SPH_Z, ctx->cap),
-                                                          tree_view(ctx), t.rb, G.n_epj, G.n_spj, G.off_epj,
-                                                          G.off_spj, G.epj, G.spj, t.meta + META_ERR); ++ctx->launches;
+    k_grav_lists<true><<<blocks, GQ_WARPS * 32, 0, st>>>(ng, G.group_cell, FLD(ctx->F, SPH_X, ctx->cap),
+                                                        FLD(ctx->F, SPH_Y, ctx->cap), FLD(ctx->F, SPH_Z, ctx->cap),
+                                                        G.cinfo, t.level, t.com, t.rb, G.n_epj, G.n_spj, G.off_epj,
+                                                        G.off_spj, G.epj, G.spj, t.meta + META_ERR); ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
     G.valid = true;
     return SPH_OK;

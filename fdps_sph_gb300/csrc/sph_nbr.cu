@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32)
 k_sup_walk(int n_units, const int2 *__restrict__ units, const double *__restrict__ x, const double *__restrict__ y,
            const double *__restrict__ z, const double *__restrict__ h, const float4 *__restrict__ xh,
            const float4 *__restrict__ xl, const float *__restrict__ H2f, WalkTree T, int *__restrict__ sup,
-           int *__restrict__ cnt, int K, int64_t pitch, int *err, int *maxcnt) {
+           float *__restrict__ sup_r2, int *__restrict__ cnt, int K, int64_t pitch, int *err, int *maxcnt) {
     __shared__ int s_stack[NB_WARPS][NB_STACK];
     __shared__ int s_cand[NB_WARPS][NB_CAND];
     __shared__ float4 s_ph[NB_WARPS][32];
@@ -169,7 +169,10 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const double *__restrict
                 const float dz = df_sub(qh.z, ql.z, pih.z, pil.z);
                 const float r2 = dx * dx + dy * dy + dz * dz;
                 if (valid && r2 < k2 * fmaxf(H2i, s_h2[warp][t])) {
-                    if (count < K) sup[(int64_t)count * pitch + i] = jj;
+                    if (count < K) {
+                        sup[(int64_t)count * pitch + i] = jj;
+                        sup_r2[(int64_t)count * pitch + i] = r2;
+                    }
                     ++count;
                 }
             }
@@ -234,13 +237,31 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const double *__restrict
 
 constexpr int ERR_SKIN = 16;
 
+// The FP32 r^2 stored by the walk is (x_j - x_i)^2 on double-float
+// coordinates, within 2^-21 of the exact value; outside a band of 2^-19
+// around the threshold it decides alone, inside it the oracle's FP64 test
+// decides.
+__device__ __forceinline__ bool exact_in(float r2, float thr, int j, double xi, double yi, double zi, double H2,
+                                         const double *__restrict__ x, const double *__restrict__ y,
+                                         const double *__restrict__ z, const double *__restrict__ h, bool sym) {
+    if (r2 < thr * (1.0f - 1.9073486328125e-06f)) return true;
+    if (r2 > thr * (1.0f + 1.9073486328125e-06f)) return false;
+    const double ex = __dsub_rn(x[j], xi), ey = __dsub_rn(y[j], yi), ez = __dsub_rn(z[j], zi);
+    const double rr = __dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez));
+    if (rr < H2) return true;
+    if (sym) {
+        const double Hj = __dmul_rn(SUPPORT, h[j]);
+        return rr < __dmul_rn(Hj, Hj);
+    }
+    return false;
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(128)
-k_filter(int n, const int *__restrict__ sup, const int *__restrict__ scnt, int64_t pitch,
-         const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
-         const double *__restrict__ h, const double *__restrict__ hsup, const float4 *__restrict__ xh,
-         const float4 *__restrict__ xl, const float *__restrict__ H2f, int *__restrict__ out, int *__restrict__ ocnt,
-         int *err) {
+k_filter(int n, const int *__restrict__ sup, const float *__restrict__ sup_r2, const int *__restrict__ scnt,
+         int64_t pitch, const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
+         const double *__restrict__ h, const double *__restrict__ hsup, const float *__restrict__ H2f,
+         int *__restrict__ out, int *__restrict__ ocnt, int *err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double hi = h[i];
@@ -248,37 +269,69 @@ k_filter(int n, const int *__restrict__ sup, const int *__restrict__ scnt, int64
     const double Hi = __dmul_rn(SUPPORT, hi);
     const double H2 = __dmul_rn(Hi, Hi);
     const float H2i = (float)H2;
-    const float4 pih = xh[i], pil = xl[i];
     const double xi = x[i], yi = y[i], zi = z[i];
     const int c = scnt[i];
     int k2 = 0;
     for (int k = 0; k < c; ++k) {
-        const int j = sup[(int64_t)k * pitch + i];
-        const float4 qh = xh[j], ql = xl[j];
-        const float dx = df_sub(qh.x, ql.x, pih.x, pil.x);
-        const float dy = df_sub(qh.y, ql.y, pih.y, pil.y);
-        const float dz = df_sub(qh.z, ql.z, pih.z, pil.z);
-        const float r2 = dx * dx + dy * dy + dz * dz;
-        float thr = H2i;
-        if (MODE == 1) thr = fmaxf(thr, H2f[j]);
-        bool ok;
-        if (r2 < thr * (1.0f - 1.9073486328125e-06f)) {          // 1 - 2^-19
-            ok = true;
-        } else if (r2 > thr * (1.0f + 1.9073486328125e-06f)) {
-            ok = false;
-        } else {
-            // the oracle's exact FP64 decision
-            const double ex = __dsub_rn(x[j], xi), ey = __dsub_rn(y[j], yi), ez = __dsub_rn(z[j], zi);
-            const double rr = __dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez));
-            ok = rr < H2;
-            if (MODE == 1 && !ok) {
-                const double Hj = __dmul_rn(SUPPORT, h[j]);
-                ok = rr < __dmul_rn(Hj, Hj);
-            }
-        }
-        if (ok) out[(int64_t)(k2++) * pitch + i] = j;
+        const int64_t e = (int64_t)k * pitch + i;
+        const int j = sup[e];
+        const float thr = MODE == 1 ? fmaxf(H2i, H2f[j]) : H2i;
+        if (exact_in(sup_r2[e], thr, j, xi, yi, zi, H2, x, y, z, h, MODE == 1)) out[(int64_t)(k2++) * pitch + i] = j;
     }
     ocnt[i] = k2;
+}
+
+// Mixed-precision density straight from the superset: the gather-set
+// decision of k_filter<0>, then CalcDensity's sum (force.h:9-23) in FP32
+// partial sums of 32 flushed to FP64, FLAG_GI floor and h update in FP64.
+__global__ void __launch_bounds__(128)
+k_density_sup32(int n, const int *__restrict__ sup, const float *__restrict__ sup_r2, const int *__restrict__ scnt,
+                int64_t pitch, const double *__restrict__ x, const double *__restrict__ y,
+                const double *__restrict__ z, const float *__restrict__ mf, const double *__restrict__ m,
+                double *__restrict__ h, const double *__restrict__ hsup, double *__restrict__ dens, double inv_mscale,
+                int *err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double hi = h[i];
+    if (hi > (double)KAPPA * hsup[i]) atomicOr(err, ERR_SKIN);
+    const double Hi = __dmul_rn(SUPPORT, hi);
+    const double H2 = __dmul_rn(Hi, Hi);
+    const float H2i = (float)H2;
+    const float invH = (float)(1.0 / Hi);
+    const double xi = x[i], yi = y[i], zi = z[i];
+    const int c = scnt[i];
+    double acc = 0.0;
+    float part = 0.0f;
+    int kept = 0;
+    for (int k = 0; k < c; ++k) {
+        const int64_t e = (int64_t)k * pitch + i;
+        const int j = sup[e];
+        const float r2 = sup_r2[e];
+        if (!exact_in(r2, H2i, j, xi, yi, zi, H2, x, y, z, h, false)) continue;
+        const float s = sqrtf(r2) * invH;
+        const float p = fmaxf(1.0f - s, 0.0f);
+        const float p2 = p * p, p4 = p2 * p2;
+        const float w = (1.0f + s * (8.0f + s * (25.0f + s * 32.0f))) * (p4 * p4);
+        part = fmaf(mf[j], w, part);
+        if ((++kept & 31) == 0) {
+            acc += (double)part;
+            part = 0.0f;
+        }
+    }
+    acc += (double)part;
+    const double d = fmax(DENS_FLOOR, acc * inv_mscale * (1365.0 / 64.0) / (Hi * Hi * Hi * 3.141592653589793));
+    dens[i] = d;
+    h[i] = SMTH_COEF * pow(m[i] / d, 1.0 / 3.0);
+}
+
+__global__ void k_skin_check(int n, const double *h, const double *hsup, int *err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && h[i] > (double)KAPPA * hsup[i]) atomicOr(err, ERR_SKIN);
+}
+
+__global__ void k_mass_f(int n, const double *m, double mscale, float *mf) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) mf[i] = (float)(m[i] * mscale);
 }
 
 // (2.5 h)^2 as float, rounded up so FP32 superset tests stay conservative
@@ -336,11 +389,14 @@ int sph_nbr_prepare(sph_ctx *ctx) {
         SPH_TRY(dalloc_n(ctx, &S.H2f, pitch));
         SPH_TRY(dalloc_n(ctx, &S.hsup, pitch));
         SPH_TRY(dalloc_n(ctx, &S.cnt, pitch));
+        SPH_TRY(dalloc_n(ctx, &S.mf, pitch));
         S.cap_particles = pitch;
     }
     const int64_t cap = ctx->cap;
     k_pack_pos<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap),
                                                             FLD(ctx->F, SPH_Z, cap), S.pxh, S.pxl);
+    ++ctx->launches;
+    k_mass_f<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, FLD(ctx->F, SPH_MASS, cap), ctx->mscale, S.mf);
     ++ctx->launches;
     SPH_TRY(sph_nbr_refresh_h(ctx));
     // units
@@ -386,6 +442,7 @@ static int build_superset(sph_ctx *ctx) {
     for (int attempt = 0; attempt < 4; ++attempt) {
         if (!S.nbr || S.pitch < pitch || S.K_alloc < S.K) {
             SPH_TRY(dalloc_n(ctx, &S.nbr, (int64_t)S.K * pitch));
+            SPH_TRY(dalloc_n(ctx, &S.r2, (int64_t)S.K * pitch));
             for (int m = 0; m < 2; ++m) {
                 SPH_TRY(dalloc_n(ctx, &ctx->lists[m].nbr, (int64_t)S.K * pitch));
                 SPH_TRY(dalloc_n(ctx, &ctx->lists[m].cnt, pitch));
@@ -401,7 +458,7 @@ static int build_superset(sph_ctx *ctx) {
         WalkTree T{t.start, t.count, t.first_child, t.n_child, t.blo, t.bhi};
         k_sup_walk<<<blocks, NB_WARPS * 32, 0, ctx->stream>>>(
             S.n_units, S.units, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
-            FLD(ctx->F, SPH_SMTH, cap), S.pxh, S.pxl, S.H2f, T, S.nbr, S.cnt, S.K, S.pitch, meta + META_ERR,
+            FLD(ctx->F, SPH_SMTH, cap), S.pxh, S.pxl, S.H2f, T, S.nbr, S.r2, S.cnt, S.K, S.pitch, meta + META_ERR,
             meta + META_MAXCNT);
         ++ctx->launches;
         SPH_CUDA(ctx, cudaGetLastError());
@@ -433,12 +490,12 @@ int sph_build_sph_lists(sph_ctx *ctx, int mode) {
         SPH_CUDA(ctx, cudaMemsetAsync(meta + META_ERR, 0, sizeof(int), ctx->stream));
         if (mode == 0)
             k_filter<0><<<sph_div_up(n, 128), 128, 0, ctx->stream>>>(
-                n, S.nbr, S.cnt, S.pitch, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
-                FLD(ctx->F, SPH_SMTH, cap), S.hsup, S.pxh, S.pxl, S.H2f, L.nbr, L.cnt, meta + META_ERR);
+                n, S.nbr, S.r2, S.cnt, S.pitch, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap),
+                FLD(ctx->F, SPH_Z, cap), FLD(ctx->F, SPH_SMTH, cap), S.hsup, S.H2f, L.nbr, L.cnt, meta + META_ERR);
         else
             k_filter<1><<<sph_div_up(n, 128), 128, 0, ctx->stream>>>(
-                n, S.nbr, S.cnt, S.pitch, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
-                FLD(ctx->F, SPH_SMTH, cap), S.hsup, S.pxh, S.pxl, S.H2f, L.nbr, L.cnt, meta + META_ERR);
+                n, S.nbr, S.r2, S.cnt, S.pitch, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap),
+                FLD(ctx->F, SPH_Z, cap), FLD(ctx->F, SPH_SMTH, cap), S.hsup, S.H2f, L.nbr, L.cnt, meta + META_ERR);
         ++ctx->launches;
         SPH_CUDA(ctx, cudaGetLastError());
         int *hs = (int *)ctx->host_scalars;
@@ -452,4 +509,41 @@ int sph_build_sph_lists(sph_ctx *ctx, int mode) {
         return SPH_OK;
     }
     return sph_fail(ctx, SPH_ERR_CAPACITY, "SPH neighbour superset invalid after rebuild");
+}
+
+// mixed-precision density pass straight from the superset (no exact list)
+int sph_density_from_superset(sph_ctx *ctx) {
+    SphSuper &S = ctx->sup;
+    const int n = (int)ctx->n;
+    const int64_t cap = ctx->cap;
+    int *meta = ctx->tree.meta;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        if (!S.valid) SPH_TRY(build_superset(ctx));
+        // the skin test needs the h the pass starts from; the kernel overwrites h, so test first
+        SPH_CUDA(ctx, cudaMemsetAsync(meta + META_ERR, 0, sizeof(int), ctx->stream));
+        k_skin_check<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, FLD(ctx->F, SPH_SMTH, cap), S.hsup,
+                                                                   meta + META_ERR);
+        ++ctx->launches;
+        int *hs = (int *)ctx->host_scalars;
+        SPH_CUDA(ctx, cudaMemcpyAsync(hs, meta + META_ERR, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (hs[0] & ERR_SKIN) {
+            S.valid = false;
+            continue;
+        }
+        k_density_sup32<<<sph_div_up(n, 128), 128, 0, ctx->stream>>>(
+            n, S.nbr, S.r2, S.cnt, S.pitch, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
+            S.mf, FLD(ctx->F, SPH_MASS, cap), FLD(ctx->F, SPH_SMTH, cap), S.hsup, FLD(ctx->F, SPH_DENS, cap),
+            1.0 / ctx->mscale, meta + META_ERR);
+        ++ctx->launches;
+        SPH_CUDA(ctx, cudaGetLastError());
+        ctx->lists[0].valid = false;
+        return sph_nbr_refresh_h(ctx);
+    }
+    return sph_fail(ctx, SPH_ERR_CAPACITY, "SPH neighbour superset invalid after rebuild");
+}
+
+int sph_nbr_ensure_superset(sph_ctx *ctx) {
+    if (!ctx->sup.valid) return build_superset(ctx);
+    return SPH_OK;
 }

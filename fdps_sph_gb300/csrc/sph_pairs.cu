@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(GT) k_grav64(const int *__restrict__ group_cel
                                                const int *__restrict__ n_spj, const int *__restrict__ off_spj,
                                                const int *__restrict__ spj, double G, double *gx, double *gy,
                                                double *gz, double *pot) {
-    __shared__ double4 tile[GT];
+    __shared__ double4 tile[GT];   // (x, y, z, G m)
     const int g = blockIdx.x;
     const int gc = group_cell[g];
     const int s = cstart[gc], cnt = ccount[gc];
@@ -196,42 +196,35 @@ __global__ void __launch_bounds__(GT) k_grav64(const int *__restrict__ group_cel
         const double xi = act ? x[i] : 0.0, yi = act ? y[i] : 0.0, zi = act ? z[i] : 0.0;
         const double eps2 = act ? h[i] * h[i] : 1.0;
         double a0 = 0.0, a1 = 0.0, a2 = 0.0, p = 0.0;
-        for (int t0 = 0; t0 < ne; t0 += GT) {
-            const int k = t0 + threadIdx.x;
-            if (k < ne) {
-                const int j = E[k];
-                tile[threadIdx.x] = make_double4(x[j], y[j], z[j], m[j]);
+        // EPJ then SPJ, each in list order (the two functor calls of main.cpp:145-146)
+        for (int pass = 0; pass < 2; ++pass) {
+            const int nl = pass == 0 ? ne : ns;
+            for (int t0 = 0; t0 < nl; t0 += GT) {
+                const int k = t0 + threadIdx.x;
+                if (k < nl) {
+                    if (pass == 0) {
+                        const int j = E[k];
+                        tile[threadIdx.x] = make_double4(x[j], y[j], z[j], G * m[j]);
+                    } else {
+                        const double4 q = com[S[k]];
+                        tile[threadIdx.x] = make_double4(q.x, q.y, q.z, G * q.w);
+                    }
+                }
+                __syncthreads();
+                const int tn = min(GT, nl - t0);
+                for (int t = 0; t < tn; ++t) {
+                    const double4 q = tile[t];
+                    const double dx = xi - q.x, dy = yi - q.y, dz = zi - q.z;
+                    const double dri = rsqrt(fma(dx, dx, fma(dy, dy, fma(dz, dz, eps2))));
+                    const double gmr = q.w * dri;
+                    const double gmr3 = gmr * (dri * dri);
+                    a0 = fma(-gmr3, dx, a0);
+                    a1 = fma(-gmr3, dy, a1);
+                    a2 = fma(-gmr3, dz, a2);
+                    p -= gmr;
+                }
+                __syncthreads();
             }
-            __syncthreads();
-            const int tn = min(GT, ne - t0);
-            for (int t = 0; t < tn; ++t) {
-                const double4 q = tile[t];
-                const double dx = xi - q.x, dy = yi - q.y, dz = zi - q.z;
-                const double dri = 1.0 / sqrt(dx * dx + dy * dy + dz * dz + eps2);
-                const double mdr3 = q.w * (dri * dri * dri);
-                a0 -= G * mdr3 * dx;
-                a1 -= G * mdr3 * dy;
-                a2 -= G * mdr3 * dz;
-                p -= G * q.w * dri;
-            }
-            __syncthreads();
-        }
-        for (int t0 = 0; t0 < ns; t0 += GT) {
-            const int k = t0 + threadIdx.x;
-            if (k < ns) tile[threadIdx.x] = com[S[k]];
-            __syncthreads();
-            const int tn = min(GT, ns - t0);
-            for (int t = 0; t < tn; ++t) {
-                const double4 q = tile[t];
-                const double dx = xi - q.x, dy = yi - q.y, dz = zi - q.z;
-                const double dri = 1.0 / sqrt(dx * dx + dy * dy + dz * dz + eps2);
-                const double mdr3 = q.w * (dri * dri * dri);
-                a0 -= G * mdr3 * dx;
-                a1 -= G * mdr3 * dy;
-                a2 -= G * mdr3 * dz;
-                p -= G * q.w * dri;
-            }
-            __syncthreads();
         }
         if (act) {
             gx[i] = a0;

@@ -465,31 +465,32 @@ int64_t or_sph_list(const or_tree *t, const double *x, const double *y, const do
 
 /* ------------------------------------------------------------------------ */
 /* Gravity interaction lists (TreeForForceLong::Monopole, main.cpp:83,90).
- * Walk from the root; a child cell is opened iff dmin^2(group box, child com)
- * <= (child side / theta)^2, i.e. rc2[level] = root_len^2/theta^2 * 0.25^level.
- * Opened leaves contribute their particles (EPJ, the group's own included).
- * For every opened internal cell, its unopened children are emitted as
- * monopoles (SPJ) in octant order, then the walk descends into its opened
- * children in octant order (depth first). */
+ * A child cell is opened iff dmin^2(group box, child com) <= (child side /
+ * theta)^2, i.e. rc2[level] = root_len^2/theta^2 * 0.25^level.  Cells are
+ * opened breadth-first in FIFO order from the root: an opened leaf appends
+ * its particles to EPJ (the group's own included); an opened internal cell
+ * appends its unopened children to SPJ (monopoles) and its opened children
+ * to the queue, both in octant order. */
 
-typedef struct { or_ibuf epj, spj; } or_glist;
+typedef struct { or_ibuf epj, spj, queue; } or_glist;
 
-static void or_grav_walk(const or_tree *t, int32_t ci, const double blo[3], const double bhi[3],
+static void or_grav_walk(const or_tree *t, int32_t root, const double blo[3], const double bhi[3],
                          const double *rc2, or_glist *L) {
-    const or_cell *c = &t->c[ci];
-    if (c->n_child == 0) {
-        for (int32_t j = c->start; j < c->start + c->count; ++j) or_ibuf_push(&L->epj, j);
-        return;
+    L->queue.n = 0;
+    or_ibuf_push(&L->queue, root);
+    for (int64_t head = 0; head < L->queue.n; ++head) {
+        const or_cell *c = &t->c[L->queue.a[head]];
+        if (c->n_child == 0) {
+            for (int32_t j = c->start; j < c->start + c->count; ++j) or_ibuf_push(&L->epj, j);
+            continue;
+        }
+        for (int k = 0; k < c->n_child; ++k) {
+            const int32_t chi = c->first_child + k;
+            const or_cell *ch = &t->c[chi];
+            if (or_dmin2(blo, bhi, ch->com) <= rc2[ch->level]) or_ibuf_push(&L->queue, chi);
+            else or_ibuf_push(&L->spj, chi);
+        }
     }
-    int near[8];
-    for (int k = 0; k < c->n_child; ++k) {
-        const int32_t chi = c->first_child + k;
-        const or_cell *ch = &t->c[chi];
-        near[k] = or_dmin2(blo, bhi, ch->com) <= rc2[ch->level];
-        if (!near[k]) or_ibuf_push(&L->spj, chi);
-    }
-    for (int k = 0; k < c->n_child; ++k)
-        if (near[k]) or_grav_walk(t, c->first_child + k, blo, bhi, rc2, L);
 }
 
 static void or_rcrit_table(const or_tree *t, double theta, double rc2[OR_KEY_LEVELS + 1]) {
@@ -525,6 +526,7 @@ int or_grav_list(const or_tree *t, const double *x, const double *y, const doubl
     *n_spj = L.spj.n;
     free(L.epj.a);
     free(L.spj.a);
+    free(L.queue.a);
     return 0;
 }
 
@@ -714,6 +716,7 @@ void or_pass_gravity(or_system *s, const or_tree *t, const or_config *cfg) {
         }
         free(L.epj.a);
         free(L.spj.a);
+        free(L.queue.a);
     }
     free(groups);
 }

@@ -66,3 +66,18 @@ def vec_rel_err(A, B, floor_frac=1e-6):
     nb = np.linalg.norm(B, axis=1)
     fl = max(floor_frac * (nb.max() if len(nb) else 1.0), 1e-300)
     return float(np.max(np.linalg.norm(A - B, axis=1) / np.maximum(nb, fl))) if len(nb) else 0.0
+
+
+def vec_err_rms(A, B):
+    """max_i |A_i - B_i| / max(|B_i|, rms_k |B_k|): relative error of each
+    particle's vector, floored at the RMS magnitude over all particles so
+    that vectors which nearly cancel (interior of a uniform layer) are not
+    judged by their own, arbitrarily small, magnitude."""
+    nb = np.linalg.norm(B, axis=1)
+    rms = float(np.sqrt(np.mean(nb * nb))) if len(nb) else 1.0
+    return float(np.max(np.linalg.norm(A - B, axis=1) / np.maximum(nb, max(rms, 1e-300)))) if len(nb) else 0.0
+
+
+def scalar_err_rms(a, b):
+    rms = float(np.sqrt(np.mean(b * b))) if len(b) else 1.0
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), max(rms, 1e-300)))) if len(b) else 0.0
