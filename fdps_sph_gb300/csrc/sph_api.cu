@@ -208,7 +208,8 @@ int sph_ctx_destroy(sph_ctx *ctx) {
                     ctx->grav.group_cell, ctx->grav.is_group, ctx->grav.n_epj, ctx->grav.n_spj, ctx->grav.off_epj,
                     ctx->grav.off_spj, ctx->grav.epj, ctx->grav.spj, ctx->scan.part, ctx->scan.total,
                     ctx->sup.nbr, ctx->sup.cnt, ctx->sup.hsup, ctx->sup.pxh, ctx->sup.pxl, ctx->sup.H2f,
-                    ctx->sup.units, ctx->grav.cinfo, ctx->sup.r2, ctx->sup.mf};
+                    ctx->sup.units, ctx->tree.cinfo, ctx->sup.r2, ctx->sup.mf, ctx->sup.vR, ctx->sup.cvR,
+                    ctx->sup.umark, ctx->sup.uoff, ctx->sup.uidx};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (void *p : ctx->table_allocs) cudaFree(p);
@@ -575,11 +576,19 @@ int sph_step_timed(sph_ctx *ctx, int n_steps, double *device_ms) {
     return SPH_OK;
 }
 
-int sph_get_counters(sph_ctx *ctx, int64_t out[8]) {
+int sph_get_counters(sph_ctx *ctx, int64_t out[16]) {
     if (!ctx || !out) return SPH_ERR_ARG;
     cudaSetDevice(ctx->device);
     int64_t w[8];
     SPH_TRY(sph_work_counts(ctx, w));
+    out[8] = ctx->sup.rebuilds;
+    out[9] = ctx->sup.repairs;
+    out[10] = ctx->sup.violators;
+    out[11] = ctx->sup.units_walked;
+    out[12] = ctx->sup.n_units;
+    out[13] = ctx->sup.K;
+    out[14] = 0;
+    out[15] = 0;
     out[0] = ctx->launches;
     out[1] = w[0];
     out[2] = w[1];

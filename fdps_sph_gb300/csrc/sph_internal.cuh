@@ -52,6 +52,7 @@ struct Tree {
     float4 *blo = nullptr;    // bbox lower corner (rounded down), .w unused
     float4 *bhi = nullptr;    // bbox upper corner (rounded up), .w = hmax (rounded up)
     int *tmp_cnt = nullptr, *tmp_off = nullptr, *tmp_b = nullptr;
+    int4 *cinfo = nullptr;    // per cell: first_child, n_child, start, count
     int *meta = nullptr;      // device [META_N]
     double *rb = nullptr;     // device: root_lo[3], root_len, scale, rc2[MAX_LEVELS] at [8..]
     int n_cell_host = 0;
@@ -82,8 +83,6 @@ struct GravLists {
     int *n_epj = nullptr, *n_spj = nullptr;          // [ng]
     int *off_epj = nullptr, *off_spj = nullptr;      // [ng]
     int *epj = nullptr, *spj = nullptr;
-    int4 *cinfo = nullptr;                           // [cells] first_child, n_child, start, count
-    int64_t cap_cinfo = 0;
     int ng = 0;
     int64_t tot_epj = 0, tot_spj = 0;
     bool valid = false;
@@ -102,8 +101,15 @@ struct SphSuper {
     int2 *units = nullptr;                // (start, count) of the walk units
     int n_units = 0;
     bool valid = false;
-    int64_t rebuilds = 0;
-    int rebuilds_step = 0;   // superset builds since the last sort
+    int64_t rebuilds = 0;    // full walks
+    int64_t repairs = 0;     // partial walks after h outgrew the skin
+    int64_t violators = 0;   // particles that outgrew the skin
+    int64_t units_walked = 0;
+    int rebuilds_step = 0;   // superset walks since the last sort
+    // repair scratch
+    float *vR = nullptr, *cvR = nullptr;
+    int *umark = nullptr, *uoff = nullptr, *uidx = nullptr;
+    int64_t cap_cells = 0;
 };
 
 struct Scan {

@@ -155,12 +155,6 @@ k_grav_lists(int ng, const int *__restrict__ group_cell, const double *__restric
     }
 }
 
-__global__ void k_pack_cinfo(const int *meta, const int *first_child, const int *n_child, const int *start,
-                             const int *count, int4 *cinfo) {
-    const int nc = meta[MAX_LEVELS];
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x)
-        cinfo[c] = make_int4(first_child[c], n_child[c], start[c], count[c]);
-}
 
 }  // namespace sph
 
@@ -205,16 +199,10 @@ int sph_build_grav_lists(sph_ctx *ctx) {
     const int ng = hs[0];
     G.ng = ng;
     const int blocks = (ng + GQ_WARPS - 1) / GQ_WARPS;
-    if (G.cap_cinfo < nc) {
-        G.cap_cinfo = t.cap;
-        SPH_TRY(dalloc_l(ctx, &G.cinfo, G.cap_cinfo));
-    }
-    k_pack_cinfo<<<grid, 256, 0, st>>>(t.meta, t.first_child, t.n_child, t.start, t.count, G.cinfo);
-    ++ctx->launches;
     SPH_CUDA(ctx, cudaMemsetAsync(t.meta + META_ERR, 0, sizeof(int), st));
     k_grav_lists<false><<<blocks, GQ_WARPS * 32, 0, st>>>(ng, G.group_cell, FLD(ctx->F, SPH_X, ctx->cap),
                                                          FLD(ctx->F, SPH_Y, ctx->cap), FLD(ctx->F, SPH_Z, ctx->cap),
-                                                         G.cinfo, t.level, t.com, t.rb, G.n_epj, G.n_spj, nullptr,
+                                                         t.cinfo, t.level, t.com, t.rb, G.n_epj, G.n_spj, nullptr,
                                                          nullptr, nullptr, nullptr, t.meta + META_ERR); ++ctx->launches;
     SPH_TRY(sph_scan_exclusive(ctx, G.n_epj, G.off_epj, nullptr, ng, nullptr));
     SPH_TRY(sph_scan_exclusive(ctx, G.n_spj, G.off_spj, nullptr, ng, nullptr));
@@ -240,7 +228,7 @@ int sph_build_grav_lists(sph_ctx *ctx) {
     G.tot_spj = tot_s;
     k_grav_lists<true><<<blocks, GQ_WARPS * 32, 0, st>>>(ng, G.group_cell, FLD(ctx->F, SPH_X, ctx->cap),
                                                         FLD(ctx->F, SPH_Y, ctx->cap), FLD(ctx->F, SPH_Z, ctx->cap),
-                                                        G.cinfo, t.level, t.com, t.rb, G.n_epj, G.n_spj, G.off_epj,
+                                                        t.cinfo, t.level, t.com, t.rb, G.n_epj, G.n_spj, G.off_epj,
                                                         G.off_spj, G.epj, G.spj, t.meta + META_ERR); ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
     G.valid = true;

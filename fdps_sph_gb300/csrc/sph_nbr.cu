@@ -113,8 +113,9 @@ __device__ __forceinline__ float gap2_rd(float4 a_lo, float4 a_hi, float3 glo, f
 }
 
 __global__ void __launch_bounds__(NB_WARPS * 32)
-k_sup_walk(int n_units, const int2 *__restrict__ units, const double *__restrict__ x, const double *__restrict__ y,
-           const double *__restrict__ z, const double *__restrict__ h, const float4 *__restrict__ xh,
+k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ uidx, const double *__restrict__ x,
+           const double *__restrict__ y, const double *__restrict__ z, const double *__restrict__ h,
+           double *__restrict__ hsup, const float4 *__restrict__ xh,
            const float4 *__restrict__ xl, const float *__restrict__ H2f, WalkTree T, int *__restrict__ sup,
            float *__restrict__ sup_r2, int *__restrict__ cnt, int K, int64_t pitch, int *err, int *maxcnt) {
     __shared__ int s_stack[NB_WARPS][NB_STACK];
@@ -123,12 +124,13 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const double *__restrict
     __shared__ float4 s_pl[NB_WARPS][32];
     __shared__ float s_h2[NB_WARPS][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int u = blockIdx.x * NB_WARPS + warp;
-    if (u >= n_units) return;   // warp-uniform
-    const int2 U = units[u];
+    const int w = blockIdx.x * NB_WARPS + warp;
+    if (w >= n_units) return;   // warp-uniform
+    const int2 U = units[uidx ? uidx[w] : w];
     const bool valid = lane < U.y;
     const int i = U.x + (valid ? lane : 0);
     const double xi = x[i], yi = y[i], zi = z[i];
+    if (valid) hsup[i] = h[i];   // the h this row is built for
     const float4 pih = xh[i], pil = xl[i];
     const float H2i = valid ? H2f[i] : 0.0f;
     double lo[3] = {valid ? xi : INFINITY, valid ? yi : INFINITY, valid ? zi : INFINITY};
@@ -233,6 +235,123 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const double *__restrict
 }
 
 // ---------------------------------------------------------------------------
+// incremental repair after h outgrew the skin
+//
+// A row built when particle j had smoothing length h_j(T) keeps every
+// neighbour as long as 2.5 h_j <= KAPPA * 2.5 h_j(T) for all j near it.  A
+// particle v that violates this (h_v > KAPPA * hsup_v) can be missing from
+// its own row and from the symmetric rows of particles within 2.5 h_v of it;
+// the rows of every unit within reach of a violator are walked again.
+
+__global__ void k_viol_mark(int n, const double *h, const double *hsup, float *vR, int *nviol) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool v = false;
+    if (i < n) {
+        v = h[i] > (double)KAPPA * hsup[i];
+        vR[i] = v ? __double2float_ru(SUPPORT * h[i] * 1.001) : 0.0f;
+    }
+    const unsigned b = __ballot_sync(FULLM, v);
+    if ((threadIdx.x & 31) == 0 && b) atomicAdd(nviol, __popc(b));
+}
+
+__global__ void k_cell_vmax(int l, const int *meta, const float *vR, const int4 *cinfo, float *cvR) {
+    const int L0 = meta[l], L1 = meta[l + 1];
+    for (int c = L0 + blockIdx.x * blockDim.x + threadIdx.x; c < L1; c += gridDim.x * blockDim.x) {
+        const int4 ci = cinfo[c];
+        float r = 0.0f;
+        if (ci.y == 0) {
+            for (int j = ci.z; j < ci.z + ci.w; ++j) r = fmaxf(r, vR[j]);
+        } else {
+            for (int k = 0; k < ci.y; ++k) r = fmaxf(r, cvR[ci.x + k]);
+        }
+        cvR[c] = r;
+    }
+}
+
+// warp per unit: is any violator within its reach of the unit's box?
+__global__ void __launch_bounds__(NB_WARPS * 32)
+k_unit_mark(int n_units, const int2 *__restrict__ units, const float4 *__restrict__ xh, const float4 *__restrict__ xl,
+            const float *__restrict__ vR, const float *__restrict__ cvR, const int4 *__restrict__ cinfo,
+            const float4 *__restrict__ blo, const float4 *__restrict__ bhi, int *umark) {
+    __shared__ int s_stack[NB_WARPS][NB_STACK];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int u = blockIdx.x * NB_WARPS + warp;
+    if (u >= n_units) return;
+    const int2 U = units[u];
+    const bool valid = lane < U.y;
+    const int i = U.x + (valid ? lane : 0);
+    const float4 ph = xh[i], pl = xl[i];
+    // unit box in float, widened by one ulp each way (the double-float sum rounds)
+    float lo[3] = {valid ? ph.x + pl.x : INFINITY, valid ? ph.y + pl.y : INFINITY, valid ? ph.z + pl.z : INFINITY};
+    float hi[3] = {valid ? ph.x + pl.x : -INFINITY, valid ? ph.y + pl.y : -INFINITY,
+                   valid ? ph.z + pl.z : -INFINITY};
+    for (int o = 16; o > 0; o >>= 1)
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = fminf(lo[d], __shfl_xor_sync(FULLM, lo[d], o));
+            hi[d] = fmaxf(hi[d], __shfl_xor_sync(FULLM, hi[d], o));
+        }
+    const float3 glo = make_float3(nextafterf(lo[0], -INFINITY), nextafterf(lo[1], -INFINITY),
+                                   nextafterf(lo[2], -INFINITY));
+    const float3 ghi = make_float3(nextafterf(hi[0], INFINITY), nextafterf(hi[1], INFINITY),
+                                   nextafterf(hi[2], INFINITY));
+    int *stack = s_stack[warp];
+    int sp = 0;
+    bool hit = false;
+    {
+        const float r = cvR[0];
+        if (r > 0.0f && gap2_rd(blo[0], bhi[0], glo, ghi) < __fmul_ru(r, r)) {
+            if (lane == 0) stack[0] = 0;
+            sp = 1;
+        }
+        __syncwarp();
+    }
+    while (sp > 0 && !hit) {
+        const int c = stack[--sp];
+        __syncwarp();
+        const int4 ci = cinfo[c];
+        if (ci.y == 0) {
+            bool h2 = false;
+            for (int j = ci.z + lane; j < ci.z + ci.w; j += 32) {
+                const float r = vR[j];
+                if (r > 0.0f) {
+                    const float4 qh = xh[j], ql = xl[j];
+                    const float px = qh.x + ql.x, py = qh.y + ql.y, pz = qh.z + ql.z;
+                    const float4 a = make_float4(nextafterf(px, -INFINITY), nextafterf(py, -INFINITY),
+                                                 nextafterf(pz, -INFINITY), 0.0f);
+                    const float4 b = make_float4(nextafterf(px, INFINITY), nextafterf(py, INFINITY),
+                                                 nextafterf(pz, INFINITY), 0.0f);
+                    if (gap2_rd(a, b, glo, ghi) < __fmul_ru(r, r)) h2 = true;
+                }
+            }
+            hit = __any_sync(FULLM, h2);
+        } else {
+            bool ok = false;
+            int ch = 0;
+            if (lane < ci.y) {
+                ch = ci.x + lane;
+                const float r = cvR[ch];
+                ok = r > 0.0f && gap2_rd(blo[ch], bhi[ch], glo, ghi) < __fmul_ru(r, r);
+            }
+            const unsigned mask = __ballot_sync(FULLM, ok);
+            const int np = __popc(mask);
+            if (sp + np > NB_STACK) {   // cannot happen for an octree of depth 21; be safe: mark
+                hit = true;
+                break;
+            }
+            if (ok) stack[sp + (np - 1 - __popc(mask & ((1u << lane) - 1u)))] = ch;
+            sp += np;
+            __syncwarp();
+        }
+    }
+    if (lane == 0) umark[u] = hit ? 1 : 0;
+}
+
+__global__ void k_unit_compact(int n_units, const int *umark, const int *off, int *uidx) {
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n_units; u += gridDim.x * blockDim.x)
+        if (umark[u]) uidx[off[u]] = u;
+}
+
+// ---------------------------------------------------------------------------
 // exact filter: one thread per particle
 
 constexpr int ERR_SKIN = 16;
@@ -265,7 +384,6 @@ k_filter(int n, const int *__restrict__ sup, const float *__restrict__ sup_r2, c
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double hi = h[i];
-    if (hi > (double)KAPPA * hsup[i]) atomicOr(err, ERR_SKIN);
     const double Hi = __dmul_rn(SUPPORT, hi);
     const double H2 = __dmul_rn(Hi, Hi);
     const float H2i = (float)H2;
@@ -293,7 +411,6 @@ k_density_sup32(int n, const int *__restrict__ sup, const float *__restrict__ su
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double hi = h[i];
-    if (hi > (double)KAPPA * hsup[i]) atomicOr(err, ERR_SKIN);
     const double Hi = __dmul_rn(SUPPORT, hi);
     const double H2 = __dmul_rn(Hi, Hi);
     const float H2i = (float)H2;
@@ -390,6 +507,7 @@ int sph_nbr_prepare(sph_ctx *ctx) {
         SPH_TRY(dalloc_n(ctx, &S.hsup, pitch));
         SPH_TRY(dalloc_n(ctx, &S.cnt, pitch));
         SPH_TRY(dalloc_n(ctx, &S.mf, pitch));
+        SPH_TRY(dalloc_n(ctx, &S.vR, pitch));
         S.cap_particles = pitch;
     }
     const int64_t cap = ctx->cap;
@@ -415,6 +533,13 @@ int sph_nbr_prepare(sph_ctx *ctx) {
     if (S.cap_units < tot) {
         S.cap_units = tot + tot / 4 + 64;
         SPH_TRY(dalloc_n(ctx, &S.units, S.cap_units));
+        SPH_TRY(dalloc_n(ctx, &S.umark, S.cap_units));
+        SPH_TRY(dalloc_n(ctx, &S.uoff, S.cap_units));
+        SPH_TRY(dalloc_n(ctx, &S.uidx, S.cap_units));
+    }
+    if (S.cap_cells < t.cap) {
+        S.cap_cells = t.cap;
+        SPH_TRY(dalloc_n(ctx, &S.cvR, S.cap_cells));
     }
     k_units<true><<<grid, 256, 0, ctx->stream>>>(t.meta, t.start, t.count, t.first_child, t.n_child, nullptr,
                                                  t.tmp_off, S.units);
@@ -427,7 +552,8 @@ int sph_nbr_prepare(sph_ctx *ctx) {
     return SPH_OK;
 }
 
-static int build_superset(sph_ctx *ctx) {
+// walks the units in uidx (or all units when uidx is null); grows the row capacity if needed
+static int walk_units(sph_ctx *ctx, const int *uidx, int n_walk) {
     SphSuper &S = ctx->sup;
     const int n = (int)ctx->n;
     const int64_t pitch = ((int64_t)n + 31) / 32 * 32;
@@ -437,10 +563,12 @@ static int build_superset(sph_ctx *ctx) {
     if (S.K == 0) S.K = 192;
     if (S.rebuilds_step > 0) SPH_TRY(sph_tree_refresh_hmax(ctx));   // cell hmax must follow the current h
     S.rebuilds_step += 1;
-    SPH_CUDA(ctx, cudaMemcpyAsync(S.hsup, FLD(ctx->F, SPH_SMTH, cap), sizeof(double) * n, cudaMemcpyDeviceToDevice,
-                                  ctx->stream));
     for (int attempt = 0; attempt < 4; ++attempt) {
         if (!S.nbr || S.pitch < pitch || S.K_alloc < S.K) {
+            if (uidx) {   // a partial walk cannot grow the rows: the others would be lost
+                uidx = nullptr;
+                n_walk = S.n_units;
+            }
             SPH_TRY(dalloc_n(ctx, &S.nbr, (int64_t)S.K * pitch));
             SPH_TRY(dalloc_n(ctx, &S.r2, (int64_t)S.K * pitch));
             for (int m = 0; m < 2; ++m) {
@@ -454,13 +582,15 @@ static int build_superset(sph_ctx *ctx) {
         }
         SPH_CUDA(ctx, cudaMemsetAsync(meta + META_ERR, 0, sizeof(int), ctx->stream));
         SPH_CUDA(ctx, cudaMemsetAsync(meta + META_MAXCNT, 0, sizeof(int), ctx->stream));
-        const int blocks = (S.n_units + NB_WARPS - 1) / NB_WARPS;
+        const int blocks = (n_walk + NB_WARPS - 1) / NB_WARPS;
         WalkTree T{t.start, t.count, t.first_child, t.n_child, t.blo, t.bhi};
-        k_sup_walk<<<blocks, NB_WARPS * 32, 0, ctx->stream>>>(
-            S.n_units, S.units, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
-            FLD(ctx->F, SPH_SMTH, cap), S.pxh, S.pxl, S.H2f, T, S.nbr, S.r2, S.cnt, S.K, S.pitch, meta + META_ERR,
-            meta + META_MAXCNT);
-        ++ctx->launches;
+        if (blocks > 0) {
+            k_sup_walk<<<blocks, NB_WARPS * 32, 0, ctx->stream>>>(
+                n_walk, S.units, uidx, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
+                FLD(ctx->F, SPH_SMTH, cap), S.hsup, S.pxh, S.pxl, S.H2f, T, S.nbr, S.r2, S.cnt, S.K, S.pitch,
+                meta + META_ERR, meta + META_MAXCNT);
+            ++ctx->launches;
+        }
         SPH_CUDA(ctx, cudaGetLastError());
         int *hs = (int *)ctx->host_scalars;
         SPH_CUDA(ctx, cudaMemcpyAsync(hs, meta + META_ERR, 4 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -469,13 +599,59 @@ static int build_superset(sph_ctx *ctx) {
         if (errw & ERR_SPH_LIST_OVERFLOW) {
             if (maxc <= S.K) return sph_fail(ctx, SPH_ERR_CAPACITY, "SPH walk stack overflow");
             S.K = maxc + maxc / 4 + 16;
+            uidx = nullptr;     // rows were truncated: rebuild everything with the larger capacity
+            n_walk = S.n_units;
             continue;
         }
         S.valid = true;
-        S.rebuilds += 1;
+        if (uidx) S.repairs += 1;
+        else S.rebuilds += 1;
+        S.units_walked += n_walk;
         return SPH_OK;
     }
     return sph_fail(ctx, SPH_ERR_CAPACITY, "SPH superset capacity could not be grown");
+}
+
+static int build_superset(sph_ctx *ctx) { return walk_units(ctx, nullptr, ctx->sup.n_units); }
+
+// makes the superset valid for the current h: full walk after a sort, otherwise a repair of
+// the units within reach of particles whose h outgrew the skin
+static int ensure_superset(sph_ctx *ctx) {
+    SphSuper &S = ctx->sup;
+    if (!S.valid) return build_superset(ctx);
+    const int n = (int)ctx->n;
+    const int64_t cap = ctx->cap;
+    int *meta = ctx->tree.meta;
+    Tree &t = ctx->tree;
+    float *vR = S.vR;
+    SPH_CUDA(ctx, cudaMemsetAsync(meta + META_ERR + 8, 0, sizeof(int), ctx->stream));
+    k_viol_mark<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, FLD(ctx->F, SPH_SMTH, cap), S.hsup, vR,
+                                                              meta + META_ERR + 8);
+    ++ctx->launches;
+    int *hs = (int *)ctx->host_scalars;
+    SPH_CUDA(ctx, cudaMemcpyAsync(hs, meta + META_ERR + 8, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const int nviol = hs[0];
+    if (nviol == 0) return SPH_OK;
+    S.violators += nviol;
+    if ((int64_t)nviol * 8 > n) return build_superset(ctx);   // widespread growth: walk everything
+    // influence radius per cell, bottom-up
+    const int grid = 2 * ctx->num_sms;
+    for (int l = KEY_LEVELS; l >= 0; --l) {
+        k_cell_vmax<<<grid, 128, 0, ctx->stream>>>(l, meta, vR, t.cinfo, S.cvR);
+        ++ctx->launches;
+    }
+    const int blocks = (S.n_units + NB_WARPS - 1) / NB_WARPS;
+    k_unit_mark<<<blocks, NB_WARPS * 32, 0, ctx->stream>>>(S.n_units, S.units, S.pxh, S.pxl, vR, S.cvR,
+                                                           t.cinfo, t.blo, t.bhi, S.umark);
+    ++ctx->launches;
+    SPH_TRY(sph_scan_exclusive(ctx, S.umark, S.uoff, nullptr, S.n_units, ctx->scan.total));
+    k_unit_compact<<<grid, 256, 0, ctx->stream>>>(S.n_units, S.umark, S.uoff, S.uidx);
+    ++ctx->launches;
+    SPH_CUDA(ctx, cudaMemcpyAsync(hs, ctx->scan.total, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const int nmark = hs[0];
+    return walk_units(ctx, S.uidx, nmark);
 }
 
 // exact list of `mode` (0 gather, 1 symmetric) for the current h
@@ -484,31 +660,20 @@ int sph_build_sph_lists(sph_ctx *ctx, int mode) {
     const int n = (int)ctx->n;
     const int64_t cap = ctx->cap;
     int *meta = ctx->tree.meta;
-    for (int attempt = 0; attempt < 2; ++attempt) {
-        if (!S.valid) SPH_TRY(build_superset(ctx));
-        SphLists &L = ctx->lists[mode];
-        SPH_CUDA(ctx, cudaMemsetAsync(meta + META_ERR, 0, sizeof(int), ctx->stream));
-        if (mode == 0)
-            k_filter<0><<<sph_div_up(n, 128), 128, 0, ctx->stream>>>(
-                n, S.nbr, S.r2, S.cnt, S.pitch, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap),
-                FLD(ctx->F, SPH_Z, cap), FLD(ctx->F, SPH_SMTH, cap), S.hsup, S.H2f, L.nbr, L.cnt, meta + META_ERR);
-        else
-            k_filter<1><<<sph_div_up(n, 128), 128, 0, ctx->stream>>>(
-                n, S.nbr, S.r2, S.cnt, S.pitch, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap),
-                FLD(ctx->F, SPH_Z, cap), FLD(ctx->F, SPH_SMTH, cap), S.hsup, S.H2f, L.nbr, L.cnt, meta + META_ERR);
-        ++ctx->launches;
-        SPH_CUDA(ctx, cudaGetLastError());
-        int *hs = (int *)ctx->host_scalars;
-        SPH_CUDA(ctx, cudaMemcpyAsync(hs, meta + META_ERR, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-        SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-        if (hs[0] & ERR_SKIN) {   // some h grew past the skin: walk again with the current h
-            S.valid = false;
-            continue;
-        }
-        L.valid = true;
-        return SPH_OK;
-    }
-    return sph_fail(ctx, SPH_ERR_CAPACITY, "SPH neighbour superset invalid after rebuild");
+    SPH_TRY(ensure_superset(ctx));
+    SphLists &L = ctx->lists[mode];
+    if (mode == 0)
+        k_filter<0><<<sph_div_up(n, 128), 128, 0, ctx->stream>>>(
+            n, S.nbr, S.r2, S.cnt, S.pitch, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
+            FLD(ctx->F, SPH_SMTH, cap), S.hsup, S.H2f, L.nbr, L.cnt, meta + META_ERR);
+    else
+        k_filter<1><<<sph_div_up(n, 128), 128, 0, ctx->stream>>>(
+            n, S.nbr, S.r2, S.cnt, S.pitch, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
+            FLD(ctx->F, SPH_SMTH, cap), S.hsup, S.H2f, L.nbr, L.cnt, meta + META_ERR);
+    ++ctx->launches;
+    SPH_CUDA(ctx, cudaGetLastError());
+    L.valid = true;
+    return SPH_OK;
 }
 
 // mixed-precision density pass straight from the superset (no exact list)
@@ -517,33 +682,15 @@ int sph_density_from_superset(sph_ctx *ctx) {
     const int n = (int)ctx->n;
     const int64_t cap = ctx->cap;
     int *meta = ctx->tree.meta;
-    for (int attempt = 0; attempt < 2; ++attempt) {
-        if (!S.valid) SPH_TRY(build_superset(ctx));
-        // the skin test needs the h the pass starts from; the kernel overwrites h, so test first
-        SPH_CUDA(ctx, cudaMemsetAsync(meta + META_ERR, 0, sizeof(int), ctx->stream));
-        k_skin_check<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, FLD(ctx->F, SPH_SMTH, cap), S.hsup,
-                                                                   meta + META_ERR);
-        ++ctx->launches;
-        int *hs = (int *)ctx->host_scalars;
-        SPH_CUDA(ctx, cudaMemcpyAsync(hs, meta + META_ERR, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-        SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-        if (hs[0] & ERR_SKIN) {
-            S.valid = false;
-            continue;
-        }
-        k_density_sup32<<<sph_div_up(n, 128), 128, 0, ctx->stream>>>(
-            n, S.nbr, S.r2, S.cnt, S.pitch, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
-            S.mf, FLD(ctx->F, SPH_MASS, cap), FLD(ctx->F, SPH_SMTH, cap), S.hsup, FLD(ctx->F, SPH_DENS, cap),
-            1.0 / ctx->mscale, meta + META_ERR);
-        ++ctx->launches;
-        SPH_CUDA(ctx, cudaGetLastError());
-        ctx->lists[0].valid = false;
-        return sph_nbr_refresh_h(ctx);
-    }
-    return sph_fail(ctx, SPH_ERR_CAPACITY, "SPH neighbour superset invalid after rebuild");
+    SPH_TRY(ensure_superset(ctx));
+    k_density_sup32<<<sph_div_up(n, 128), 128, 0, ctx->stream>>>(
+        n, S.nbr, S.r2, S.cnt, S.pitch, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
+        S.mf, FLD(ctx->F, SPH_MASS, cap), FLD(ctx->F, SPH_SMTH, cap), S.hsup, FLD(ctx->F, SPH_DENS, cap),
+        1.0 / ctx->mscale, meta + META_ERR);
+    ++ctx->launches;
+    SPH_CUDA(ctx, cudaGetLastError());
+    ctx->lists[0].valid = false;
+    return sph_nbr_refresh_h(ctx);
 }
 
-int sph_nbr_ensure_superset(sph_ctx *ctx) {
-    if (!ctx->sup.valid) return build_superset(ctx);
-    return SPH_OK;
-}
+int sph_nbr_ensure_superset(sph_ctx *ctx) { return ensure_superset(ctx); }

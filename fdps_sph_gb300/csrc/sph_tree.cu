@@ -470,6 +470,13 @@ __global__ void k_moments(int l, const int *meta, const double *x, const double 
     }
 }
 
+__global__ void k_pack_cinfo(const int *meta, const int *first_child, const int *n_child, const int *start,
+                             const int *count, int4 *cinfo) {
+    const int nc = meta[MAX_LEVELS];
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x)
+        cinfo[c] = make_int4(first_child[c], n_child[c], start[c], count[c]);
+}
+
 __global__ void k_hmax(int l, const int *meta, const double *h, const int *start, const int *count,
                        const int *first_child, const int *n_child, float4 *bhi) {
     const int L0 = meta[l], L1 = meta[l + 1];
@@ -525,6 +532,7 @@ int sph_tree_reserve(sph_ctx *ctx, int64_t n) {
         SPH_TRY(dalloc(ctx, &t.tmp_cnt, c));
         SPH_TRY(dalloc(ctx, &t.tmp_off, c));
         SPH_TRY(dalloc(ctx, &t.tmp_b, 9 * c));
+        SPH_TRY(dalloc(ctx, &t.cinfo, c));
         SPH_TRY(dalloc(ctx, &ctx->grav.is_group, c));
         t.cap = c;
     }
@@ -604,6 +612,8 @@ int sph_sort_and_build(sph_ctx *ctx) {
     for (int l = KEY_LEVELS; l >= 0; --l)
         k_moments<<<grid, 128, 0, st>>>(l, t.meta, x, y, z, m, h, t.start, t.count, t.first_child, t.n_child,
                                         t.mom, t.com, t.blo, t.bhi); ++ctx->launches;
+    k_pack_cinfo<<<grid, 256, 0, st>>>(t.meta, t.first_child, t.n_child, t.start, t.count, t.cinfo);
+    ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
     // bring back the cell count and the error word (one small synchronous read per tree)
     int *hs = (int *)ctx->host_scalars;

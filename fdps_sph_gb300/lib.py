@@ -270,9 +270,10 @@ class Context:
         return ms.value
 
     def counters(self):
-        out = np.zeros(8, np.int64)
+        out = np.zeros(16, np.int64)
         self._check(self.L.sph_get_counters(self.h, _ptr(out)))
-        keys = ["launches", "pairs_gather", "pairs_sym", "pairs_grav", "cells", "groups", "epj", "spj"]
+        keys = ["launches", "pairs_gather", "pairs_sym", "pairs_grav", "cells", "groups", "epj", "spj",
+                "walks_full", "walks_repair", "skin_violators", "units_walked", "units", "row_capacity"]
         return dict(zip(keys, out.tolist()))
 
 

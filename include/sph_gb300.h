@@ -196,8 +196,11 @@ int sph_step_timed(sph_ctx *ctx, int n_steps, double *device_ms);
 /* out[0] kernels launched by the context so far; out[1] gather-list pairs (one
  * density / derivative pass); out[2] symmetric-list pairs (hydro); out[3]
  * gravity interactions (sum over groups of n_i x (EPJ + SPJ)); out[4] cells;
- * out[5] gravity groups; out[6] EPJ entries; out[7] SPJ entries. */
-int sph_get_counters(sph_ctx *ctx, int64_t out[8]);
+ * out[5] gravity groups; out[6] EPJ entries; out[7] SPJ entries; out[8]
+ * full neighbour-superset walks; out[9] partial (repair) walks; out[10]
+ * particles whose h outgrew the superset skin; out[11] walk units walked;
+ * out[12] walk units; out[13] superset row capacity; out[14..15] reserved. */
+int sph_get_counters(sph_ctx *ctx, int64_t out[16]);
 /* Measures the FP32 (fp64 = 0) or FP64 (fp64 = 1) fused-multiply-add rate of
  * the device in TFLOP/s (2 flops per FMA): the roofline of the pair kernels. */
 int sph_probe_peak(int device, int fp64, double *tflops);

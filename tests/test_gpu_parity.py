@@ -221,3 +221,41 @@ def test_tree_gravity_against_direct_sum(impact):
         g = np.stack([out[theta][po.FIELD[c]] for c in ("gx", "gy", "gz")], 1)
         err = np.linalg.norm(g - acc, axis=1) / np.linalg.norm(acc, axis=1).max()
         assert err.max() < bound, (theta, err.max())
+
+
+@pytest.mark.parametrize("frac", [0.05, 1.0])
+def test_superset_repair_keeps_lists_exact(impact, frac):
+    """Shrink h of a fraction of the particles so that the first density pass
+    grows them past the superset skin: with a few violators the library
+    re-walks only the units in their reach, with many it walks everything.
+    Either way every later list equals the oracle's."""
+    from oracle import pyoracle as po
+    F, ids, mats = impact
+    F = F.copy()
+    rng = np.random.default_rng(7)
+    sel = rng.random(F.shape[1]) < frac
+    F[po.FIELD["smth"], sel] *= 0.6
+    mats_l = tillotson_materials()
+    cfg = oracle_config(mats_l)
+    ctx = device_context(mats_l)
+    ctx.upload(F, ids, mats)
+    ctx.run_pass(0)
+    s = _oracle(F, ids, mats)
+    tr = po.OracleTree(s)
+    for it in range(3):
+        ctx.run_pass(1)
+        for k in range(0, s.n, 5):
+            assert np.array_equal(ctx.neighbors(0, k), tr.sph_list(k, 0)), (it, k)
+        tr.pass_density(cfg)
+        Fd, _, _ = _dev_sorted(ctx)
+        s.F[po.FIELD["smth"]] = Fd[po.FIELD["smth"]]
+        s.F[po.FIELD["dens"]] = Fd[po.FIELD["dens"]]
+    tr = po.OracleTree(s)
+    ctx.run_pass(4)
+    for k in range(0, s.n, 5):
+        assert np.array_equal(ctx.neighbors(1, k), tr.sph_list(k, 1)), k
+    c = ctx.counters()
+    assert c["skin_violators"] > 0
+    if frac < 0.5:
+        assert c["walks_repair"] > 0
+        assert c["units_walked"] < (c["walks_full"] + c["walks_repair"]) * c["units"]
