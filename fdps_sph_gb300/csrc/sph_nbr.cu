@@ -101,7 +101,7 @@ __global__ void k_units(const int *meta, const int *start, const int *count, con
 // superset walk: one warp per unit
 
 struct WalkTree {
-    const int *start, *count, *first_child, *n_child;
+    const int4 *cinfo;   // first_child, n_child, start, count
     const float4 *blo, *bhi;
 };
 
@@ -112,7 +112,7 @@ __device__ __forceinline__ float gap2_rd(float4 a_lo, float4 a_hi, float3 glo, f
     return __fadd_rd(__fadd_rd(__fmul_rd(gx, gx), __fmul_rd(gy, gy)), __fmul_rd(gz, gz));
 }
 
-__global__ void __launch_bounds__(NB_WARPS * 32)
+__global__ void __launch_bounds__(NB_WARPS * 32, 10)
 k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ uidx, const double *__restrict__ x,
            const double *__restrict__ y, const double *__restrict__ z, const double *__restrict__ h,
            double *__restrict__ hsup, const float4 *__restrict__ xh,
@@ -196,9 +196,10 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
     while (sp > 0) {
         const int c = stack[--sp];
         __syncwarp();
-        const int nch = T.n_child[c];
+        const int4 ci = T.cinfo[c];
+        const int nch = ci.y;
         if (nch == 0) {
-            const int s = T.start[c], ct = T.count[c];
+            const int s = ci.z, ct = ci.w;
             for (int b0 = 0; b0 < ct; b0 += 32) {
                 if (nc + 32 > NB_CAND) flush();
                 if (b0 + lane < ct) cand[nc + lane] = s + b0 + lane;
@@ -206,7 +207,7 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
                 __syncwarp();
             }
         } else {
-            const int f = T.first_child[c];
+            const int f = ci.x;
             bool ok = false;
             if (lane < nch) {
                 const float4 a = T.blo[f + lane], b = T.bhi[f + lane];
@@ -390,7 +391,24 @@ k_filter(int n, const int *__restrict__ sup, const float *__restrict__ sup_r2, c
     const double xi = x[i], yi = y[i], zi = z[i];
     const int c = scnt[i];
     int k2 = 0;
-    for (int k = 0; k < c; ++k) {
+    int k = 0;
+    for (; k + 4 <= c; k += 4) {
+        int j[4];
+        float r2[4], thr[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int64_t e = (int64_t)(k + u) * pitch + i;
+            j[u] = sup[e];
+            r2[u] = sup_r2[e];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) thr[u] = MODE == 1 ? fmaxf(H2i, H2f[j[u]]) : H2i;
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (exact_in(r2[u], thr[u], j[u], xi, yi, zi, H2, x, y, z, h, MODE == 1))
+                out[(int64_t)(k2++) * pitch + i] = j[u];
+    }
+    for (; k < c; ++k) {
         const int64_t e = (int64_t)k * pitch + i;
         const int j = sup[e];
         const float thr = MODE == 1 ? fmaxf(H2i, H2f[j]) : H2i;
@@ -419,21 +437,41 @@ k_density_sup32(int n, const int *__restrict__ sup, const float *__restrict__ su
     const int c = scnt[i];
     double acc = 0.0;
     float part = 0.0f;
-    int kept = 0;
-    for (int k = 0; k < c; ++k) {
+    int k = 0;
+    // four entries in flight: row loads, then the mass gathers, then the arithmetic
+    for (; k + 4 <= c; k += 4) {
+        int j[4];
+        float r2[4], mj[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int64_t e = (int64_t)(k + u) * pitch + i;
+            j[u] = sup[e];
+            r2[u] = sup_r2[e];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) mj[u] = mf[j[u]];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (!exact_in(r2[u], H2i, j[u], xi, yi, zi, H2, x, y, z, h, false)) continue;
+            const float s_ = sqrtf(r2[u]) * invH;
+            const float p = fmaxf(1.0f - s_, 0.0f);
+            const float p2 = p * p, p4 = p2 * p2;
+            part = fmaf(mj[u], (1.0f + s_ * (8.0f + s_ * (25.0f + s_ * 32.0f))) * (p4 * p4), part);
+        }
+        if ((k & 31) == 28) {   // flush every 32 entries
+            acc += (double)part;
+            part = 0.0f;
+        }
+    }
+    for (; k < c; ++k) {
         const int64_t e = (int64_t)k * pitch + i;
         const int j = sup[e];
         const float r2 = sup_r2[e];
         if (!exact_in(r2, H2i, j, xi, yi, zi, H2, x, y, z, h, false)) continue;
-        const float s = sqrtf(r2) * invH;
-        const float p = fmaxf(1.0f - s, 0.0f);
+        const float s_ = sqrtf(r2) * invH;
+        const float p = fmaxf(1.0f - s_, 0.0f);
         const float p2 = p * p, p4 = p2 * p2;
-        const float w = (1.0f + s * (8.0f + s * (25.0f + s * 32.0f))) * (p4 * p4);
-        part = fmaf(mf[j], w, part);
-        if ((++kept & 31) == 0) {
-            acc += (double)part;
-            part = 0.0f;
-        }
+        part = fmaf(mf[j], (1.0f + s_ * (8.0f + s_ * (25.0f + s_ * 32.0f))) * (p4 * p4), part);
     }
     acc += (double)part;
     const double d = fmax(DENS_FLOOR, acc * inv_mscale * (1365.0 / 64.0) / (Hi * Hi * Hi * 3.141592653589793));
@@ -583,7 +621,7 @@ static int walk_units(sph_ctx *ctx, const int *uidx, int n_walk) {
         SPH_CUDA(ctx, cudaMemsetAsync(meta + META_ERR, 0, sizeof(int), ctx->stream));
         SPH_CUDA(ctx, cudaMemsetAsync(meta + META_MAXCNT, 0, sizeof(int), ctx->stream));
         const int blocks = (n_walk + NB_WARPS - 1) / NB_WARPS;
-        WalkTree T{t.start, t.count, t.first_child, t.n_child, t.blo, t.bhi};
+        WalkTree T{t.cinfo, t.blo, t.bhi};
         if (blocks > 0) {
             k_sup_walk<<<blocks, NB_WARPS * 32, 0, ctx->stream>>>(
                 n_walk, S.units, uidx, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),

@@ -310,6 +310,28 @@ struct DrvtArgs32 {
     double inv_mscale;
 };
 
+__device__ __forceinline__ void drvt_pair32(const float4 pih, const float4 pil, const float4 vih, const float4 vil,
+                                            const float4 qh, const float4 ql, const float4 uh, const float4 ul,
+                                            float invH, float Hf, float ceps, float P[5]) {
+    const float dx = df_diff(pih.x, pil.x, qh.x, ql.x);
+    const float dy = df_diff(pih.y, pil.y, qh.y, ql.y);
+    const float dz = df_diff(pih.z, pil.z, qh.z, ql.z);
+    const float wx = df_diff(vih.x, vil.x, uh.x, ul.x);
+    const float wy = df_diff(vih.y, vil.y, uh.y, ul.y);
+    const float wz = df_diff(vih.z, vil.z, uh.z, ul.z);
+    const float rr2 = dx * dx + dy * dy + dz * dz;
+    const float r = sqrtf(rr2);
+    float w, g;
+    wendland_poly_f(r * invH, w, g);
+    const float gf = g / (r * Hf + ceps);
+    const float mg = -qh.w * gf;
+    P[0] = fmaf(mg, wx * dx + wy * dy + wz * dz, P[0]);
+    P[1] = fmaf(mg, wy * dz - wz * dy, P[1]);
+    P[2] = fmaf(mg, wz * dx - wx * dz, P[2]);
+    P[3] = fmaf(mg, wx * dy - wy * dx, P[3]);
+    P[4] = fmaf(qh.w, 3.0f * w + gf * rr2, P[4]);
+}
+
 __global__ void __launch_bounds__(PT) k_drvt32(int n, DrvtArgs32 a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -322,33 +344,24 @@ __global__ void __launch_bounds__(PT) k_drvt32(int n, DrvtArgs32 a) {
     double D[5] = {0, 0, 0, 0, 0};
     float P[5] = {0, 0, 0, 0, 0};
     const int c = a.cnt[i];
-    for (int k = 0; k < c; ++k) {
-        const int j = a.nbr[(int64_t)k * a.pitch + i];
-        const float4 qh = a.xh[j], ql = a.xl[j], uh = a.vh[j], ul = a.vl[j];
-        const float dx = df_diff(pih.x, pil.x, qh.x, ql.x);
-        const float dy = df_diff(pih.y, pil.y, qh.y, ql.y);
-        const float dz = df_diff(pih.z, pil.z, qh.z, ql.z);
-        const float wx = df_diff(vih.x, vil.x, uh.x, ul.x);
-        const float wy = df_diff(vih.y, vil.y, uh.y, ul.y);
-        const float wz = df_diff(vih.z, vil.z, uh.z, ul.z);
-        const float rr2 = dx * dx + dy * dy + dz * dz;
-        const float r = sqrtf(rr2);
-        float w, g;
-        wendland_poly_f(r * invH, w, g);
-        const float gf = g / (r * Hf + ceps);
-        const float mg = -qh.w * gf;
-        P[0] = fmaf(mg, wx * dx + wy * dy + wz * dz, P[0]);
-        P[1] = fmaf(mg, wy * dz - wz * dy, P[1]);
-        P[2] = fmaf(mg, wz * dx - wx * dz, P[2]);
-        P[3] = fmaf(mg, wx * dy - wy * dx, P[3]);
-        P[4] = fmaf(qh.w, 3.0f * w + gf * rr2, P[4]);
-        if ((k & 31) == 31) {
+    int k = 0;
+    for (; k + 2 <= c; k += 2) {
+        const int j0 = a.nbr[(int64_t)k * a.pitch + i], j1 = a.nbr[(int64_t)(k + 1) * a.pitch + i];
+        const float4 qh0 = a.xh[j0], ql0 = a.xl[j0], uh0 = a.vh[j0], ul0 = a.vl[j0];
+        const float4 qh1 = a.xh[j1], ql1 = a.xl[j1], uh1 = a.vh[j1], ul1 = a.vl[j1];
+        drvt_pair32(pih, pil, vih, vil, qh0, ql0, uh0, ul0, invH, Hf, ceps, P);
+        drvt_pair32(pih, pil, vih, vil, qh1, ql1, uh1, ul1, invH, Hf, ceps, P);
+        if ((k & 31) == 30) {
 #pragma unroll
             for (int q = 0; q < 5; ++q) {
                 D[q] += (double)P[q];
                 P[q] = 0.0f;
             }
         }
+    }
+    if (k < c) {
+        const int j = a.nbr[(int64_t)k * a.pitch + i];
+        drvt_pair32(pih, pil, vih, vil, a.xh[j], a.xl[j], a.vh[j], a.vl[j], invH, Hf, ceps, P);
     }
 #pragma unroll
     for (int q = 0; q < 5; ++q) D[q] = (D[q] + (double)P[q]) * normd * a.inv_mscale;
@@ -384,6 +397,51 @@ struct HydroArgs32 {
     double inv_mscale;
 };
 
+struct HydroJ32 {
+    float4 qh, ql, uh, ul, A, B;
+};
+
+__device__ __forceinline__ void hydro_pair32(const float4 pih, const float4 pil, const float4 vih, const float4 vil,
+                                             const float4 Ai, const float4 Bi, const HydroJ32 &J, float P[4],
+                                             float &vmax) {
+    const float dx = df_diff(pih.x, pil.x, J.qh.x, J.ql.x);
+    const float dy = df_diff(pih.y, pil.y, J.qh.y, J.ql.y);
+    const float dz = df_diff(pih.z, pil.z, J.qh.z, J.ql.z);
+    const float wx = df_diff(vih.x, vil.x, J.uh.x, J.ul.x);
+    const float wy = df_diff(vih.y, vil.y, J.uh.y, J.ul.y);
+    const float wz = df_diff(vih.z, vil.z, J.uh.z, J.ul.z);
+    const float rr2 = dx * dx + dy * dy + dz * dz;
+    const float r = sqrtf(rr2);
+    const float dvdr = wx * dx + wy * dy + wz * dz;
+    const float w = (dvdr < 0.0f) ? dvdr / r : 0.0f;
+    const float vsig = Ai.y + J.A.y - 3.0f * w;
+    vmax = fmaxf(vmax, vsig);
+    const float AV = -0.5f * vsig * w / (0.5f * (Bi.x + J.B.x)) * 0.5f * (Ai.w + J.A.w);
+    float wi_, gi_, wj_, gj_;
+    wendland_poly_f(r * Bi.y, wi_, gi_);
+    wendland_poly_f(r * J.B.y, wj_, gj_);
+    const float nr = Bi.z * J.B.y;
+    const float gfi = gi_ / (r * Bi.z + Bi.w);
+    const float gfj = (nr * nr * nr) * gj_ / (r * J.B.z + J.B.w);
+    const float gws = 0.5f * (gfi * Ai.z + gfj * J.A.z);
+    const float coef = J.qh.w * (Ai.x * gfi + J.A.x * gfj + AV * gws);
+    P[0] = fmaf(-coef, dx, P[0]);
+    P[1] = fmaf(-coef, dy, P[1]);
+    P[2] = fmaf(-coef, dz, P[2]);
+    P[3] = fmaf(J.qh.w * (Ai.x + 0.5f * AV) * gws, dvdr, P[3]);
+}
+
+__device__ __forceinline__ HydroJ32 load_hydro_j(const HydroArgs32 &a, int j) {
+    HydroJ32 J;
+    J.qh = a.xh[j];
+    J.ql = a.xl[j];
+    J.uh = a.vh[j];
+    J.ul = a.vl[j];
+    J.A = a.hA[j];
+    J.B = a.hB[j];
+    return J;
+}
+
 __global__ void __launch_bounds__(PT) k_hydro32(int n, HydroArgs32 a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -395,42 +453,23 @@ __global__ void __launch_bounds__(PT) k_hydro32(int n, HydroArgs32 a) {
     float P[4] = {0, 0, 0, 0};
     float vmax = 0.0f;
     const int c = a.cnt[i];
-    for (int k = 0; k < c; ++k) {
-        const int j = a.nbr[(int64_t)k * a.pitch + i];
-        const float4 qh = a.xh[j], ql = a.xl[j], uh = a.vh[j], ul = a.vl[j];
-        const float4 Aj = a.hA[j], Bj = a.hB[j];
-        const float dx = df_diff(pih.x, pil.x, qh.x, ql.x);
-        const float dy = df_diff(pih.y, pil.y, qh.y, ql.y);
-        const float dz = df_diff(pih.z, pil.z, qh.z, ql.z);
-        const float wx = df_diff(vih.x, vil.x, uh.x, ul.x);
-        const float wy = df_diff(vih.y, vil.y, uh.y, ul.y);
-        const float wz = df_diff(vih.z, vil.z, uh.z, ul.z);
-        const float rr2 = dx * dx + dy * dy + dz * dz;
-        const float r = sqrtf(rr2);
-        const float dvdr = wx * dx + wy * dy + wz * dz;
-        const float w = (dvdr < 0.0f) ? dvdr / r : 0.0f;
-        const float vsig = Ai.y + Aj.y - 3.0f * w;
-        vmax = fmaxf(vmax, vsig);
-        const float AV = -0.5f * vsig * w / (0.5f * (Bi.x + Bj.x)) * 0.5f * (Ai.w + Aj.w);
-        float wi_, gi_, wj_, gj_;
-        wendland_poly_f(r * Bi.y, wi_, gi_);
-        wendland_poly_f(r * Bj.y, wj_, gj_);
-        const float nr = Bi.z * Bj.y;
-        const float gfi = gi_ / (r * Bi.z + Bi.w);
-        const float gfj = (nr * nr * nr) * gj_ / (r * Bj.z + Bj.w);
-        const float gws = 0.5f * (gfi * Ai.z + gfj * Aj.z);
-        const float coef = qh.w * (Ai.x * gfi + Aj.x * gfj + AV * gws);
-        P[0] = fmaf(-coef, dx, P[0]);
-        P[1] = fmaf(-coef, dy, P[1]);
-        P[2] = fmaf(-coef, dz, P[2]);
-        P[3] = fmaf(qh.w * (Ai.x + 0.5f * AV) * gws, dvdr, P[3]);
-        if ((k & 31) == 31) {
+    int k = 0;
+    for (; k + 2 <= c; k += 2) {
+        const int j0 = a.nbr[(int64_t)k * a.pitch + i], j1 = a.nbr[(int64_t)(k + 1) * a.pitch + i];
+        const HydroJ32 J0 = load_hydro_j(a, j0), J1 = load_hydro_j(a, j1);
+        hydro_pair32(pih, pil, vih, vil, Ai, Bi, J0, P, vmax);
+        hydro_pair32(pih, pil, vih, vil, Ai, Bi, J1, P, vmax);
+        if ((k & 31) == 30) {
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 D[q] += (double)P[q];
                 P[q] = 0.0f;
             }
         }
+    }
+    if (k < c) {
+        const HydroJ32 J = load_hydro_j(a, a.nbr[(int64_t)k * a.pitch + i]);
+        hydro_pair32(pih, pil, vih, vil, Ai, Bi, J, P, vmax);
     }
     const double sc = normd * a.inv_mscale;
 #pragma unroll
