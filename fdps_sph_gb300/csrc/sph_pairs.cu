@@ -644,9 +644,17 @@ __global__ void k_min_partial(int n, const double *v, double *part) {
 }
 
 __global__ void k_min_final(const double *part, int nb, double *out) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        double r = 1.0e30;
-        for (int b = 0; b < nb; ++b) r = (part[b] < r || part[b] != part[b]) ? part[b] : r;
+    double r = 1.0e30;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) r = (part[b] < r || part[b] != part[b]) ? part[b] : r;
+    for (int o = 16; o > 0; o >>= 1) {
+        const double t = __shfl_xor_sync(0xffffffffu, r, o);
+        r = (t < r || t != t) ? t : r;
+    }
+    __shared__ double s[32];
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = r;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) r = (s[w] < r || s[w] != s[w]) ? s[w] : r;
         *out = r;
     }
 }
@@ -869,7 +877,7 @@ int sph_ext_force(sph_ctx *ctx) {
 int sph_dt_global(sph_ctx *ctx, double *dt_out) {
     const int n = (int)ctx->n;
     k_min_partial<<<RED_BLOCKS, 256, 0, ctx->stream>>>(n, CF(SPH_DT), ctx->scratch_d); ++ctx->launches;
-    k_min_final<<<1, 32, 0, ctx->stream>>>(ctx->scratch_d, RED_BLOCKS, ctx->scratch_d + RED_BLOCKS * 8); ++ctx->launches;
+    k_min_final<<<1, 256, 0, ctx->stream>>>(ctx->scratch_d, RED_BLOCKS, ctx->scratch_d + RED_BLOCKS * 8); ++ctx->launches;
     SPH_CUDA(ctx, cudaMemcpyAsync(ctx->host_scalars, ctx->scratch_d + RED_BLOCKS * 8, sizeof(double),
                                   cudaMemcpyDeviceToHost, ctx->stream));
     SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

@@ -160,14 +160,33 @@ __global__ void k_bbox_partial(const double *x, const double *y, const double *z
     }
 }
 
-// single thread: the root cube exactly as or_root_box, plus the opening-radius table
+// one block reduces the partial boxes (min / max are exact in any order), then
+// one thread forms the root cube exactly as or_root_box and the opening-radius table
 __global__ void k_bbox_final(const double *part, int nb, double theta, double *rb) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    __shared__ double s[6][32];
     double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (int b = 0; b < nb; ++b)
+    for (int b = threadIdx.x; b < nb; b += blockDim.x)
         for (int d = 0; d < 3; ++d) {
             lo[d] = fmin(lo[d], part[b * 6 + d]);
             hi[d] = fmax(hi[d], part[b * 6 + 3 + d]);
+        }
+    for (int d = 0; d < 3; ++d)
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[d] = fmin(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
+            hi[d] = fmax(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+        }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0)
+        for (int d = 0; d < 3; ++d) {
+            s[d][wid] = lo[d];
+            s[3 + d][wid] = hi[d];
+        }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = fmin(lo[d], s[d][w]);
+            hi[d] = fmax(hi[d], s[3 + d][w]);
         }
     double L = 0.0;
     for (int d = 0; d < 3; ++d) {
@@ -585,7 +604,7 @@ int sph_sort_and_build(sph_ctx *ctx) {
     cudaStream_t st = ctx->stream;
     // root box
     k_bbox_partial<<<BOX_BLOCKS, 256, 0, st>>>(x, y, z, n, ctx->scratch_d); ++ctx->launches;
-    k_bbox_final<<<1, 32, 0, st>>>(ctx->scratch_d, BOX_BLOCKS, ctx->cfg.theta, t.rb); ++ctx->launches;
+    k_bbox_final<<<1, 256, 0, st>>>(ctx->scratch_d, BOX_BLOCKS, ctx->cfg.theta, t.rb); ++ctx->launches;
     k_tree_init<<<1, 32, 0, st>>>(n, t.meta, t.start, t.count, t.level, t.parent, t.first_child, t.n_child); ++ctx->launches;
     k_keys<<<sph_div_up(n, 256), 256, 0, st>>>(x, y, z, n, t.rb, ctx->sort.k0, ctx->sort.v0, t.meta + META_ERR); ++ctx->launches;
     SPH_TRY(radix_sort(ctx, n));
