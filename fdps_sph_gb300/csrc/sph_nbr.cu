@@ -32,7 +32,7 @@ constexpr int UNIT = 32;
 constexpr float KAPPA = 1.15f;
 constexpr int NB_WARPS = 4;
 constexpr int NB_CAND = 512;
-constexpr int NB_STACK = 256;
+constexpr int NB_STACK = 176;   // depth-first: at most 21 levels x 7 pending siblings + 8
 constexpr unsigned FULLM = 0xffffffffu;
 
 __device__ __forceinline__ float df_sub(float ah, float al, float bh, float bl) { return (ah - bh) + (al - bl); }
@@ -118,7 +118,7 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
            double *__restrict__ hsup, const float4 *__restrict__ xh,
            const float4 *__restrict__ xl, const float *__restrict__ H2f, WalkTree T, int *__restrict__ sup,
            float *__restrict__ sup_r2, int *__restrict__ cnt, int K, int64_t pitch, int *err, int *maxcnt) {
-    __shared__ int s_stack[NB_WARPS][NB_STACK];
+    __shared__ int4 s_stack[NB_WARPS][NB_STACK];   // records (first_child, n_child, start, count) of cells to visit
     __shared__ int s_cand[NB_WARPS][NB_CAND];
     __shared__ float4 s_ph[NB_WARPS][32];
     __shared__ float4 s_pl[NB_WARPS][32];
@@ -147,7 +147,7 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
     const float3 ghi = make_float3(__double2float_ru(hi[0]), __double2float_ru(hi[1]), __double2float_ru(hi[2]));
     const float k2 = KAPPA * KAPPA * 1.00390625f;          // kappa^2 (1 + 2^-8): generous, only a superset is needed
     const float Rg = __fmul_ru(KAPPA * 1.00390625f, __fsqrt_ru(R2));
-    int *stack = s_stack[warp];
+    int4 *stack = s_stack[warp];
     int *cand = s_cand[warp];
     int count = 0, nc = 0;
 
@@ -188,15 +188,14 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
         const float4 a = T.blo[0], b = T.bhi[0];
         const float R = fmaxf(Rg, __fmul_ru(2.5f * KAPPA * 1.00390625f, b.w));
         if (gap2_rd(a, b, glo, ghi) < __fmul_ru(R, R)) {
-            if (lane == 0) stack[0] = 0;
+            if (lane == 0) stack[0] = T.cinfo[0];
             sp = 1;
         }
         __syncwarp();
     }
     while (sp > 0) {
-        const int c = stack[--sp];
+        const int4 ci = stack[--sp];
         __syncwarp();
-        const int4 ci = T.cinfo[c];
         const int nch = ci.y;
         if (nch == 0) {
             const int s = ci.z, ct = ci.w;
@@ -209,8 +208,10 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
         } else {
             const int f = ci.x;
             bool ok = false;
+            int4 chi = make_int4(0, 0, 0, 0);
             if (lane < nch) {
                 const float4 a = T.blo[f + lane], b = T.bhi[f + lane];
+                chi = T.cinfo[f + lane];   // independent of the box loads: one round trip
                 const float R = fmaxf(Rg, __fmul_ru(2.5f * KAPPA * 1.00390625f, b.w));
                 ok = gap2_rd(a, b, glo, ghi) < __fmul_ru(R, R);
             }
@@ -220,7 +221,7 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
                 if (lane == 0) atomicOr(err, ERR_SPH_LIST_OVERFLOW);
                 break;
             }
-            if (ok) stack[sp + (np - 1 - __popc(mask & ((1u << lane) - 1u)))] = f + lane;
+            if (ok) stack[sp + (np - 1 - __popc(mask & ((1u << lane) - 1u)))] = chi;
             sp += np;
             __syncwarp();
         }
