@@ -491,8 +491,7 @@ int sph_get_neighbors(sph_ctx *ctx, int mode, int64_t k, int32_t *out, int64_t c
     *n = c;
     const int64_t m = std::min<int64_t>(std::min<int64_t>(c, cap), L.K);
     if (out && m > 0)
-        SPH_CUDA(ctx, cudaMemcpy2D(out, sizeof(int32_t), L.nbr + k, sizeof(int32_t) * L.pitch, sizeof(int32_t), m,
-                                   cudaMemcpyDeviceToHost));
+        SPH_CUDA(ctx, cudaMemcpy(out, L.nbr + (int64_t)k * L.pitch, sizeof(int32_t) * m, cudaMemcpyDeviceToHost));
     return SPH_OK;
 }
 

@@ -68,11 +68,11 @@ struct Sort {
 };
 
 struct SphLists {
-    int64_t pitch = 0;   // >= n, multiple of 32
+    int64_t pitch = 0;   // row stride: particle i's neighbours at nbr[i * pitch + k], k < cnt[i]
     int K = 0;           // capacity per particle
     int K_alloc = 0;     // allocated capacity per particle
-    int *nbr = nullptr;  // [K * pitch]
-    int *cnt = nullptr;  // [pitch]
+    int *nbr = nullptr;  // [n * K]
+    int *cnt = nullptr;  // [n]
     bool valid = false;
 };
 

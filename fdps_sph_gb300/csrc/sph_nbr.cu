@@ -117,12 +117,14 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
            const double *__restrict__ y, const double *__restrict__ z, const double *__restrict__ h,
            double *__restrict__ hsup, const float4 *__restrict__ xh,
            const float4 *__restrict__ xl, const float *__restrict__ H2f, WalkTree T, int *__restrict__ sup,
-           float *__restrict__ sup_r2, int *__restrict__ cnt, int K, int64_t pitch, int *err, int *maxcnt) {
+           float *__restrict__ sup_r2, int *__restrict__ cnt, int K, int64_t stride, int *err, int *maxcnt) {
     __shared__ int4 s_stack[NB_WARPS][NB_STACK];   // records (first_child, n_child, start, count) of cells to visit
     __shared__ int s_cand[NB_WARPS][NB_CAND];
     __shared__ float4 s_ph[NB_WARPS][32];
     __shared__ float4 s_pl[NB_WARPS][32];
     __shared__ float s_h2[NB_WARPS][32];
+    __shared__ int s_wj[NB_WARPS][8][32];     // per-lane write buffers: 8 entries = one 32-byte sector
+    __shared__ float s_wr[NB_WARPS][8][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int w = blockIdx.x * NB_WARPS + warp;
     if (w >= n_units) return;   // warp-uniform
@@ -150,6 +152,22 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
     int4 *stack = s_stack[warp];
     int *cand = s_cand[warp];
     int count = 0, nc = 0;
+    int *row = sup + (int64_t)i * stride;
+    float *rrow = sup_r2 + (int64_t)i * stride;
+    // writes the lane's 8 buffered entries ending at `count` as full sectors
+    auto put8 = [&]() {
+        const int k0 = count - 8;
+        if (k0 + 8 <= K) {
+            const int4 a = make_int4(s_wj[warp][0][lane], s_wj[warp][1][lane], s_wj[warp][2][lane], s_wj[warp][3][lane]);
+            const int4 b = make_int4(s_wj[warp][4][lane], s_wj[warp][5][lane], s_wj[warp][6][lane], s_wj[warp][7][lane]);
+            const float4 c = make_float4(s_wr[warp][0][lane], s_wr[warp][1][lane], s_wr[warp][2][lane], s_wr[warp][3][lane]);
+            const float4 d = make_float4(s_wr[warp][4][lane], s_wr[warp][5][lane], s_wr[warp][6][lane], s_wr[warp][7][lane]);
+            reinterpret_cast<int4 *>(row + k0)[0] = a;
+            reinterpret_cast<int4 *>(row + k0)[1] = b;
+            reinterpret_cast<float4 *>(rrow + k0)[0] = c;
+            reinterpret_cast<float4 *>(rrow + k0)[1] = d;
+        }
+    };
 
     auto flush = [&]() {
         for (int b = 0; b < nc; b += 32) {
@@ -171,11 +189,10 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
                 const float dz = df_sub(qh.z, ql.z, pih.z, pil.z);
                 const float r2 = dx * dx + dy * dy + dz * dz;
                 if (valid && r2 < k2 * fmaxf(H2i, s_h2[warp][t])) {
-                    if (count < K) {
-                        sup[(int64_t)count * pitch + i] = jj;
-                        sup_r2[(int64_t)count * pitch + i] = r2;
-                    }
+                    s_wj[warp][count & 7][lane] = jj;
+                    s_wr[warp][count & 7][lane] = r2;
                     ++count;
+                    if ((count & 7) == 0) put8();
                 }
             }
             __syncwarp();
@@ -228,6 +245,13 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
     }
     flush();
     if (valid) {
+        // the partial last block, entry by entry
+        const int k0 = count & ~7;
+        for (int q = 0; q < (count & 7); ++q)
+            if (k0 + q < K) {
+                row[k0 + q] = s_wj[warp][q][lane];
+                rrow[k0 + q] = s_wr[warp][q][lane];
+            }
         cnt[i] = count;
         if (count > K) atomicOr(err, ERR_SPH_LIST_OVERFLOW);
     }
@@ -380,9 +404,10 @@ __device__ __forceinline__ bool exact_in(float r2, float thr, int j, double xi, 
 template <int MODE>
 __global__ void __launch_bounds__(128)
 k_filter(int n, const int *__restrict__ sup, const float *__restrict__ sup_r2, const int *__restrict__ scnt,
-         int64_t pitch, const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
+         int64_t stride, const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
          const double *__restrict__ h, const double *__restrict__ hsup, const float *__restrict__ H2f,
          int *__restrict__ out, int *__restrict__ ocnt, int *err) {
+    __shared__ int s_buf[8][128];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double hi = h[i];
@@ -391,30 +416,34 @@ k_filter(int n, const int *__restrict__ sup, const float *__restrict__ sup_r2, c
     const float H2i = (float)H2;
     const double xi = x[i], yi = y[i], zi = z[i];
     const int c = scnt[i];
+    const int *row = sup + (int64_t)i * stride;
+    const float *rrow = sup_r2 + (int64_t)i * stride;
+    int *orow = out + (int64_t)i * stride;
+    const int t = threadIdx.x;
     int k2 = 0;
-    int k = 0;
-    for (; k + 4 <= c; k += 4) {
-        int j[4];
-        float r2[4], thr[4];
+    for (int k = 0; k < c; k += 8) {
+        const int4 j0 = reinterpret_cast<const int4 *>(row + k)[0], j1 = reinterpret_cast<const int4 *>(row + k)[1];
+        const float4 r0 = reinterpret_cast<const float4 *>(rrow + k)[0], r1 = reinterpret_cast<const float4 *>(rrow + k)[1];
+        const int jj[8] = {j0.x, j0.y, j0.z, j0.w, j1.x, j1.y, j1.z, j1.w};
+        const float rr[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
+        const int m = min(8, c - k);
+        float thr[8];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int64_t e = (int64_t)(k + u) * pitch + i;
-            j[u] = sup[e];
-            r2[u] = sup_r2[e];
+        for (int u = 0; u < 8; ++u) thr[u] = (MODE == 1 && u < m) ? fmaxf(H2i, H2f[jj[u]]) : H2i;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            if (u < m && exact_in(rr[u], thr[u], jj[u], xi, yi, zi, H2, x, y, z, h, MODE == 1)) {
+                s_buf[k2 & 7][t] = jj[u];
+                ++k2;
+                if ((k2 & 7) == 0) {
+                    int4 *dst = reinterpret_cast<int4 *>(orow + k2 - 8);
+                    dst[0] = make_int4(s_buf[0][t], s_buf[1][t], s_buf[2][t], s_buf[3][t]);
+                    dst[1] = make_int4(s_buf[4][t], s_buf[5][t], s_buf[6][t], s_buf[7][t]);
+                }
+            }
         }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) thr[u] = MODE == 1 ? fmaxf(H2i, H2f[j[u]]) : H2i;
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-            if (exact_in(r2[u], thr[u], j[u], xi, yi, zi, H2, x, y, z, h, MODE == 1))
-                out[(int64_t)(k2++) * pitch + i] = j[u];
     }
-    for (; k < c; ++k) {
-        const int64_t e = (int64_t)k * pitch + i;
-        const int j = sup[e];
-        const float thr = MODE == 1 ? fmaxf(H2i, H2f[j]) : H2i;
-        if (exact_in(sup_r2[e], thr, j, xi, yi, zi, H2, x, y, z, h, MODE == 1)) out[(int64_t)(k2++) * pitch + i] = j;
-    }
+    for (int q = 0; q < (k2 & 7); ++q) orow[(k2 & ~7) + q] = s_buf[q][t];
     ocnt[i] = k2;
 }
 
@@ -423,7 +452,7 @@ k_filter(int n, const int *__restrict__ sup, const float *__restrict__ sup_r2, c
 // partial sums of 32 flushed to FP64, FLAG_GI floor and h update in FP64.
 __global__ void __launch_bounds__(128)
 k_density_sup32(int n, const int *__restrict__ sup, const float *__restrict__ sup_r2, const int *__restrict__ scnt,
-                int64_t pitch, const double *__restrict__ x, const double *__restrict__ y,
+                int64_t stride, const double *__restrict__ x, const double *__restrict__ y,
                 const double *__restrict__ z, const float *__restrict__ mf, const double *__restrict__ m,
                 double *__restrict__ h, const double *__restrict__ hsup, double *__restrict__ dens, double inv_mscale,
                 int *err) {
@@ -436,45 +465,29 @@ k_density_sup32(int n, const int *__restrict__ sup, const float *__restrict__ su
     const float invH = (float)(1.0 / Hi);
     const double xi = x[i], yi = y[i], zi = z[i];
     const int c = scnt[i];
+    const int *row = sup + (int64_t)i * stride;
+    const float *rrow = sup_r2 + (int64_t)i * stride;
     double acc = 0.0;
-    float part = 0.0f;
-    int k = 0;
-    // four entries in flight: row loads, then the mass gathers, then the arithmetic
-    for (; k + 4 <= c; k += 4) {
-        int j[4];
-        float r2[4], mj[4];
+    for (int k = 0; k < c; k += 8) {
+        const int4 j0 = reinterpret_cast<const int4 *>(row + k)[0], j1 = reinterpret_cast<const int4 *>(row + k)[1];
+        const float4 r0 = reinterpret_cast<const float4 *>(rrow + k)[0], r1 = reinterpret_cast<const float4 *>(rrow + k)[1];
+        const int jj[8] = {j0.x, j0.y, j0.z, j0.w, j1.x, j1.y, j1.z, j1.w};
+        const float rr[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
+        const int m8 = min(8, c - k);
+        float mj[8];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int64_t e = (int64_t)(k + u) * pitch + i;
-            j[u] = sup[e];
-            r2[u] = sup_r2[e];
-        }
+        for (int u = 0; u < 8; ++u) mj[u] = (u < m8) ? mf[jj[u]] : 0.0f;
+        float part = 0.0f;
 #pragma unroll
-        for (int u = 0; u < 4; ++u) mj[u] = mf[j[u]];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            if (!exact_in(r2[u], H2i, j[u], xi, yi, zi, H2, x, y, z, h, false)) continue;
-            const float s_ = sqrtf(r2[u]) * invH;
+        for (int u = 0; u < 8; ++u) {
+            if (u >= m8 || !exact_in(rr[u], H2i, jj[u], xi, yi, zi, H2, x, y, z, h, false)) continue;
+            const float s_ = sqrtf(rr[u]) * invH;
             const float p = fmaxf(1.0f - s_, 0.0f);
             const float p2 = p * p, p4 = p2 * p2;
             part = fmaf(mj[u], (1.0f + s_ * (8.0f + s_ * (25.0f + s_ * 32.0f))) * (p4 * p4), part);
         }
-        if ((k & 31) == 28) {   // flush every 32 entries
-            acc += (double)part;
-            part = 0.0f;
-        }
+        acc += (double)part;   // partial sums of at most 8 terms
     }
-    for (; k < c; ++k) {
-        const int64_t e = (int64_t)k * pitch + i;
-        const int j = sup[e];
-        const float r2 = sup_r2[e];
-        if (!exact_in(r2, H2i, j, xi, yi, zi, H2, x, y, z, h, false)) continue;
-        const float s_ = sqrtf(r2) * invH;
-        const float p = fmaxf(1.0f - s_, 0.0f);
-        const float p2 = p * p, p4 = p2 * p2;
-        part = fmaf(mf[j], (1.0f + s_ * (8.0f + s_ * (25.0f + s_ * 32.0f))) * (p4 * p4), part);
-    }
-    acc += (double)part;
     const double d = fmax(DENS_FLOOR, acc * inv_mscale * (1365.0 / 64.0) / (Hi * Hi * Hi * 3.141592653589793));
     dens[i] = d;
     h[i] = SMTH_COEF * pow(m[i] / d, 1.0 / 3.0);
@@ -595,15 +608,16 @@ int sph_nbr_prepare(sph_ctx *ctx) {
 static int walk_units(sph_ctx *ctx, const int *uidx, int n_walk) {
     SphSuper &S = ctx->sup;
     const int n = (int)ctx->n;
-    const int64_t pitch = ((int64_t)n + 31) / 32 * 32;
+    const int64_t pitch = n;   // rows: particle i's entries at i * K .. i * K + K - 1
     const int64_t cap = ctx->cap;
     int *meta = ctx->tree.meta;
     Tree &t = ctx->tree;
     if (S.K == 0) S.K = 192;
+    S.K = (S.K + 7) & ~7;   // rows start on 32-byte boundaries
     if (S.rebuilds_step > 0) SPH_TRY(sph_tree_refresh_hmax(ctx));   // cell hmax must follow the current h
     S.rebuilds_step += 1;
     for (int attempt = 0; attempt < 4; ++attempt) {
-        if (!S.nbr || S.pitch < pitch || S.K_alloc < S.K) {
+        if (!S.nbr || S.pitch < pitch || S.K_alloc != S.K) {
             if (uidx) {   // a partial walk cannot grow the rows: the others would be lost
                 uidx = nullptr;
                 n_walk = S.n_units;
@@ -614,7 +628,7 @@ static int walk_units(sph_ctx *ctx, const int *uidx, int n_walk) {
                 SPH_TRY(dalloc_n(ctx, &ctx->lists[m].nbr, (int64_t)S.K * pitch));
                 SPH_TRY(dalloc_n(ctx, &ctx->lists[m].cnt, pitch));
                 ctx->lists[m].K = ctx->lists[m].K_alloc = S.K;
-                ctx->lists[m].pitch = pitch;
+                ctx->lists[m].pitch = S.K;   // row stride of the exact lists
             }
             S.pitch = pitch;
             S.K_alloc = S.K;
@@ -626,7 +640,7 @@ static int walk_units(sph_ctx *ctx, const int *uidx, int n_walk) {
         if (blocks > 0) {
             k_sup_walk<<<blocks, NB_WARPS * 32, 0, ctx->stream>>>(
                 n_walk, S.units, uidx, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
-                FLD(ctx->F, SPH_SMTH, cap), S.hsup, S.pxh, S.pxl, S.H2f, T, S.nbr, S.r2, S.cnt, S.K, S.pitch,
+                FLD(ctx->F, SPH_SMTH, cap), S.hsup, S.pxh, S.pxl, S.H2f, T, S.nbr, S.r2, S.cnt, S.K, (int64_t)S.K,
                 meta + META_ERR, meta + META_MAXCNT);
             ++ctx->launches;
         }
@@ -637,7 +651,7 @@ static int walk_units(sph_ctx *ctx, const int *uidx, int n_walk) {
         const int errw = hs[0], maxc = hs[META_MAXCNT - META_ERR];
         if (errw & ERR_SPH_LIST_OVERFLOW) {
             if (maxc <= S.K) return sph_fail(ctx, SPH_ERR_CAPACITY, "SPH walk stack overflow");
-            S.K = maxc + maxc / 4 + 16;
+            S.K = (maxc + maxc / 4 + 16 + 7) & ~7;
             uidx = nullptr;     // rows were truncated: rebuild everything with the larger capacity
             n_walk = S.n_units;
             continue;
@@ -703,11 +717,11 @@ int sph_build_sph_lists(sph_ctx *ctx, int mode) {
     SphLists &L = ctx->lists[mode];
     if (mode == 0)
         k_filter<0><<<sph_div_up(n, 128), 128, 0, ctx->stream>>>(
-            n, S.nbr, S.r2, S.cnt, S.pitch, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
+            n, S.nbr, S.r2, S.cnt, (int64_t)S.K, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
             FLD(ctx->F, SPH_SMTH, cap), S.hsup, S.H2f, L.nbr, L.cnt, meta + META_ERR);
     else
         k_filter<1><<<sph_div_up(n, 128), 128, 0, ctx->stream>>>(
-            n, S.nbr, S.r2, S.cnt, S.pitch, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
+            n, S.nbr, S.r2, S.cnt, (int64_t)S.K, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
             FLD(ctx->F, SPH_SMTH, cap), S.hsup, S.H2f, L.nbr, L.cnt, meta + META_ERR);
     ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
@@ -723,7 +737,7 @@ int sph_density_from_superset(sph_ctx *ctx) {
     int *meta = ctx->tree.meta;
     SPH_TRY(ensure_superset(ctx));
     k_density_sup32<<<sph_div_up(n, 128), 128, 0, ctx->stream>>>(
-        n, S.nbr, S.r2, S.cnt, S.pitch, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
+        n, S.nbr, S.r2, S.cnt, (int64_t)S.K, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
         S.mf, FLD(ctx->F, SPH_MASS, cap), FLD(ctx->F, SPH_SMTH, cap), S.hsup, FLD(ctx->F, SPH_DENS, cap),
         1.0 / ctx->mscale, meta + META_ERR);
     ++ctx->launches;

@@ -34,7 +34,7 @@ __global__ void __launch_bounds__(PT) k_density64(int n, const double *__restric
     const int c = cnt[i];
     double sum = 0.0;
     for (int k = 0; k < c; ++k) {
-        const int j = nbr[(int64_t)k * pitch + i];
+        const int j = nbr[(int64_t)i * pitch + k];
         const double dx = x[j] - xi, dy = y[j] - yi, dz = z[j] - zi;
         const double r = sqrt(dx * dx + dy * dy + dz * dz);
         double w, g;
@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(PT) k_drvt64(int n, DrvtArgs a) {
     double dv = 0.0, r0 = 0.0, r1 = 0.0, r2 = 0.0, gs = 0.0;
     const int c = a.cnt[i];
     for (int k = 0; k < c; ++k) {
-        const int j = a.nbr[(int64_t)k * a.pitch + i];
+        const int j = a.nbr[(int64_t)i * a.pitch + k];
         const double dx = xi - a.x[j], dy = yi - a.y[j], dz = zi - a.z[j];
         const double mj = a.m[j];
         const double ax = -mj * (ux - a.vx[j]), ay = -mj * (uy - a.vy[j]), az = -mj * (uz - a.vz[j]);
@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(PT) k_hydro64(int n, HydroArgs a) {
     double a0 = 0.0, a1 = 0.0, a2 = 0.0, e = 0.0, vmax = 0.0;
     const int c = a.cnt[i];
     for (int k = 0; k < c; ++k) {
-        const int j = a.nbr[(int64_t)k * a.pitch + i];
+        const int j = a.nbr[(int64_t)i * a.pitch + k];
         const double dx = xi - a.x[j], dy = yi - a.y[j], dz = zi - a.z[j];
         const double wx = ux - a.vx[j], wy = uy - a.vy[j], wz = uz - a.vz[j];
         const double rr2 = dx * dx + dy * dy + dz * dz;
@@ -280,7 +280,7 @@ __global__ void __launch_bounds__(PT) k_density32(int n, const float4 *__restric
     double acc = 0.0;
     float part = 0.0f;
     for (int k = 0; k < c; ++k) {
-        const int j = nbr[(int64_t)k * pitch + i];
+        const int j = nbr[(int64_t)i * pitch + k];
         const float4 qh = xh[j], ql = xl[j];
         const float dx = df_diff(qh.x, ql.x, pih.x, pil.x);
         const float dy = df_diff(qh.y, ql.y, pih.y, pil.y);
@@ -346,7 +346,8 @@ __global__ void __launch_bounds__(PT) k_drvt32(int n, DrvtArgs32 a) {
     const int c = a.cnt[i];
     int k = 0;
     for (; k + 2 <= c; k += 2) {
-        const int j0 = a.nbr[(int64_t)k * a.pitch + i], j1 = a.nbr[(int64_t)(k + 1) * a.pitch + i];
+        const int2 jp = *reinterpret_cast<const int2 *>(a.nbr + (int64_t)i * a.pitch + k);
+        const int j0 = jp.x, j1 = jp.y;
         const float4 qh0 = a.xh[j0], ql0 = a.xl[j0], uh0 = a.vh[j0], ul0 = a.vl[j0];
         const float4 qh1 = a.xh[j1], ql1 = a.xl[j1], uh1 = a.vh[j1], ul1 = a.vl[j1];
         drvt_pair32(pih, pil, vih, vil, qh0, ql0, uh0, ul0, invH, Hf, ceps, P);
@@ -360,7 +361,7 @@ __global__ void __launch_bounds__(PT) k_drvt32(int n, DrvtArgs32 a) {
         }
     }
     if (k < c) {
-        const int j = a.nbr[(int64_t)k * a.pitch + i];
+        const int j = a.nbr[(int64_t)i * a.pitch + k];
         drvt_pair32(pih, pil, vih, vil, a.xh[j], a.xl[j], a.vh[j], a.vl[j], invH, Hf, ceps, P);
     }
 #pragma unroll
@@ -455,7 +456,8 @@ __global__ void __launch_bounds__(PT) k_hydro32(int n, HydroArgs32 a) {
     const int c = a.cnt[i];
     int k = 0;
     for (; k + 2 <= c; k += 2) {
-        const int j0 = a.nbr[(int64_t)k * a.pitch + i], j1 = a.nbr[(int64_t)(k + 1) * a.pitch + i];
+        const int2 jp = *reinterpret_cast<const int2 *>(a.nbr + (int64_t)i * a.pitch + k);
+        const int j0 = jp.x, j1 = jp.y;
         const HydroJ32 J0 = load_hydro_j(a, j0), J1 = load_hydro_j(a, j1);
         hydro_pair32(pih, pil, vih, vil, Ai, Bi, J0, P, vmax);
         hydro_pair32(pih, pil, vih, vil, Ai, Bi, J1, P, vmax);
@@ -468,7 +470,7 @@ __global__ void __launch_bounds__(PT) k_hydro32(int n, HydroArgs32 a) {
         }
     }
     if (k < c) {
-        const HydroJ32 J = load_hydro_j(a, a.nbr[(int64_t)k * a.pitch + i]);
+        const HydroJ32 J = load_hydro_j(a, a.nbr[(int64_t)i * a.pitch + k]);
         hydro_pair32(pih, pil, vih, vil, Ai, Bi, J, P, vmax);
     }
     const double sc = normd * a.inv_mscale;
