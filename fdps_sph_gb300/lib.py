@@ -37,8 +37,9 @@ EXPORTS = [
     "sph_set_eos_table", "sph_load_eos_table_file", "sph_set_eos_tillotson", "sph_upload", "sph_download",
     "sph_prologue", "sph_step", "sph_get_time", "sph_diagnostics", "sph_run_pass", "sph_get_order",
     "sph_get_neighbors", "sph_get_tree", "sph_get_grav_list", "sph_get_timings", "sph_step_timed",
-    "sph_get_counters", "sph_probe_peak",
+    "sph_get_counters", "sph_probe_peak", "sph_morton_order_noalloc",
 ]
+NOALLOC_MAX_N = 131072
 SEGMENTS = ["kdp", "tree", "dens_list", "dens", "eos", "drvt_list", "drvt", "hydro_list", "hydro", "grav_list",
             "grav", "final"]
 
@@ -90,6 +91,7 @@ def load() -> C.CDLL:
     L.sph_step_timed.argtypes = [P, C.c_int, C.POINTER(C.c_double)]
     L.sph_get_counters.argtypes = [P, P]
     L.sph_probe_peak.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double)]
+    L.sph_morton_order_noalloc.argtypes = [P, P, P, C.c_int64, P, P, P]
     L.sph_download.argtypes = [P, P, C.c_int64, P, P]
     L.sph_prologue.argtypes = [P]
     L.sph_step.argtypes = [P, C.c_int]

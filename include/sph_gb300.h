@@ -201,6 +201,29 @@ int sph_step_timed(sph_ctx *ctx, int n_steps, double *device_ms);
  * particles whose h outgrew the superset skin; out[11] walk units walked;
  * out[12] walk units; out[13] superset row capacity; out[14..15] reserved. */
 int sph_get_counters(sph_ctx *ctx, int64_t out[16]);
+/* ---- allocation-free Morton ordering -------------------------------------
+ * No counterpart in the reference: FDPS builds its tree on the host.  This
+ * is the key-and-sort stage of the device octree build for callers that
+ * must not allocate device memory -- a host recording its step into its own
+ * CUDA graph (a cudaMalloc inside the capture would invalidate it), or a
+ * host with a fixed device-memory budget or a real-time step loop.  x, y, z
+ * (n doubles each), keys_out (n) and order_out (n) are device pointers;
+ * stream may be null (the legacy default stream).  keys_out[k] is the k-th
+ * smallest 63-bit Morton key over the octree's root cube and order_out[k]
+ * the index of that particle (stable: ties keep input order), bit-identical
+ * to the order sph_run_pass(ctx, 0) produces for the same positions.
+ * Scratch lives in one file-scope device array for at most
+ * SPH_NOALLOC_MAX_N particles (about 3.2 MB, present on every GPU that loads
+ * the library); larger n returns SPH_ERR_CAPACITY, null pointers or n < 1
+ * SPH_ERR_ARG, a non-finite position SPH_ERR_NONFINITE.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress), so make
+ * that first call before any stream capture.  Every call on a device shares
+ * the array: calls that overlap on the GPU race.  No device memory is
+ * allocated or freed. */
+#define SPH_NOALLOC_MAX_N 131072
+int sph_morton_order_noalloc(const double *x, const double *y, const double *z, int64_t n, uint64_t *keys_out,
+                             int32_t *order_out, void *stream);
+
 /* Measures the FP32 (fp64 = 0) or FP64 (fp64 = 1) fused-multiply-add rate of
  * the device in TFLOP/s (2 flops per FMA): the roofline of the pair kernels. */
 int sph_probe_peak(int device, int fp64, double *tflops);
