@@ -36,6 +36,17 @@ sys.path.insert(0, ROOT)
 # sqrt / div / rsqrt 1): density, derivative, hydro, gravity
 FLOPS_PER_PAIR = {"dens": 24, "drvt": 75, "hydro": 120, "grav": 24}
 
+# DRAM bytes (read + write) per launch per particle, from the ncu captures
+# summarised in profiles/ (dram__bytes_read.sum + dram__bytes_write.sum of one
+# launch divided by the particle count of that capture)
+NCU_TRAFFIC = {}
+_tf = os.path.join(ROOT, "profiles", "ncu_traffic_per_particle.txt")
+if os.path.exists(_tf):
+    for _ln in open(_tf):
+        _p = _ln.split()
+        if len(_p) >= 2 and not _ln.startswith("#"):
+            NCU_TRAFFIC[_p[0]] = float(_p[1])
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -247,18 +258,53 @@ def main():
 
     peak32 = lib.probe_peak(False, device)
     peak64 = lib.probe_peak(True, device)
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            peaks = json.load(fh)
+    except OSError:
+        peaks = {"hbm_gbs": 6800.0}   # the profiling recipe's fallback
     mixed = results["mixed"]
     ms_step = mixed["ms"] / a.steps
     value = world * n / (ms_step * 1e-3)
 
-    # dominant pair kernel of the mixed path and its roofline
-    pairs = {"dens": mixed["cnt"]["pairs_gather"], "drvt": mixed["cnt"]["pairs_gather"],
-             "hydro": mixed["cnt"]["pairs_sym"], "grav": mixed["cnt"]["pairs_grav"]}
-    per_launch_ms = {"dens": mixed["seg"]["dens"] / (4 * a.steps), "drvt": mixed["seg"]["drvt"] / a.steps,
-                     "hydro": mixed["seg"]["hydro"] / a.steps, "grav": mixed["seg"]["grav"] / a.steps}
-    dom = max(("dens", "drvt", "hydro", "grav"), key=lambda k: mixed["seg"][k])
-    achieved = FLOPS_PER_PAIR[dom] * pairs[dom] / (per_launch_ms[dom] * 1e-3) / 1e12
-    seg_share = {k: round(v / max(sum(mixed["seg"].values()), 1e-9), 4) for k, v in mixed["seg"].items()}
+    # algorithmic work of each segment of one step: flops on the FP32 pipe
+    # for the pair kernels, compulsory HBM bytes for the list / tree / streaming kernels
+    w = mixed["cnt"]
+    seg, st = mixed["seg"], a.steps
+    entries = w.get("superset_entries", 0)
+    kernels = {
+        "sup_walk": ("dens_list", "hbm", 8 * entries + 68 * n, 1),          # rows written + particle reads
+        "density": ("dens", "fp32", FLOPS_PER_PAIR["dens"] * w["pairs_gather"], 4),
+        "filters": (None, "hbm", 2 * (8 * entries + 4 * w["pairs_gather"]) // 2, 2),
+        "derivative": ("drvt", "fp32", FLOPS_PER_PAIR["drvt"] * w["pairs_gather"], 1),
+        "hydro": ("hydro", "fp32", FLOPS_PER_PAIR["hydro"] * w["pairs_sym"], 1),
+        "grav_lists": ("grav_list", "hbm", 2 * 4 * (w["epj"] + w["spj"]), 1),
+        "gravity": ("grav", "fp32", FLOPS_PER_PAIR["grav"] * w["pairs_grav"], 1),
+        "sort_tree": ("tree", "hbm", (36 + 8 * 24 + 2 * 32 * 8) * n, 1),
+    }
+    filt_ms = seg["drvt_list"] + seg["hydro_list"]
+    hbm = peaks.get("hbm_gbs")
+    rows = {}
+    for name, (sname, bound, work, launches_per_step) in kernels.items():
+        ms_step = filt_ms / st if name == "filters" else seg[sname] / st
+        per_launch_ms = ms_step / launches_per_step
+        if per_launch_ms <= 0:
+            continue
+        if bound == "fp32":
+            ach = work / (per_launch_ms * 1e-3) / 1e12
+            rows[name] = {"bound": "fp32", "achieved": ach, "peak": peak32, "unit": "TFLOP/s",
+                          "frac": ach / peak32, "work_per_launch": work, "ms_per_launch": per_launch_ms}
+        else:
+            ach = work / (per_launch_ms * 1e-3) / 1e9
+            rows[name] = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+                          "frac": ach / hbm if hbm else None, "work_per_launch": work, "ms_per_launch": per_launch_ms}
+    dom = max(rows, key=lambda k: rows[k]["ms_per_launch"] * kernels[k][3])
+    traffic = NCU_TRAFFIC.get(dom)
+    seg_share = {k: round(v / max(sum(seg.values()), 1e-9), 4) for k, v in seg.items()}
+    roof = dict(rows[dom])
+    roof.update({"kernel": dom, "traffic": traffic * n if traffic else None,
+                 "peak_source": ("MEASURED_PEAKS.json hbm_gbs (copy bandwidth)" if roof["bound"] == "hbm" else
+                                 "measured FMA-chain probe (sph_probe_peak); MEASURED_PEAKS.json has no FP32 figure")})
 
     out = {
         "metric": "SPH particle-steps/s at 1M (mixed FP32/FP64; plain FP64 beside it)",
@@ -270,14 +316,12 @@ def main():
                    "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas" if world > 1 else "1 GPU"},
         "gpu_launches": int(mixed["launches"]),
         "clocks": mixed["clocks"],
-        "roofline": {"bound": "fp32", "kernel": dom, "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
-                     "frac": achieved / peak32 if peak32 else None, "traffic": None,
-                     "peak_source": "measured FMA-chain probe (sph_probe_peak), not in MEASURED_PEAKS.json",
-                     "flops_per_pair": FLOPS_PER_PAIR[dom], "pairs_per_launch": pairs[dom],
-                     "ms_per_launch": per_launch_ms[dom]},
+        "roofline": roof,
+        "rooflines": rows,
         "segments_ms_per_step": {k: v / a.steps for k, v in mixed["seg"].items()},
         "segment_share": seg_share,
         "work": {k: v for k, v in mixed["cnt"].items() if k != "launches"},
+        "peaks": {"fp32_tflops_measured": peak32, "fp64_tflops_measured": peak64, "hbm_gbs": hbm},
     }
     if mixed["e2e"] is not None:
         el, h2d, d2h = mixed["e2e"]

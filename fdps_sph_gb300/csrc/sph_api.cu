@@ -586,7 +586,7 @@ int sph_get_counters(sph_ctx *ctx, int64_t out[16]) {
     out[11] = ctx->sup.units_walked;
     out[12] = ctx->sup.n_units;
     out[13] = ctx->sup.K;
-    out[14] = 0;
+    out[14] = w[7];
     out[15] = 0;
     out[0] = ctx->launches;
     out[1] = w[0];

@@ -916,15 +916,16 @@ int sph_init_smth(sph_ctx *ctx) {
 int sph_work_counts(sph_ctx *ctx, int64_t out[8]) {
     for (int k = 0; k < 8; ++k) out[k] = 0;
     unsigned long long *d = (unsigned long long *)(ctx->scratch_d + 4096);
-    SPH_CUDA(ctx, cudaMemsetAsync(d, 0, 3 * sizeof(unsigned long long), ctx->stream));
+    SPH_CUDA(ctx, cudaMemsetAsync(d, 0, 4 * sizeof(unsigned long long), ctx->stream));
     const int n = (int)ctx->n;
+    if (ctx->sup.valid) k_sum_cnt<<<2 * ctx->num_sms, 256, 0, ctx->stream>>>(n, ctx->sup.cnt, d + 3);
     if (ctx->lists[0].valid) k_sum_cnt<<<2 * ctx->num_sms, 256, 0, ctx->stream>>>(n, ctx->lists[0].cnt, d);
     if (ctx->lists[1].valid) k_sum_cnt<<<2 * ctx->num_sms, 256, 0, ctx->stream>>>(n, ctx->lists[1].cnt, d + 1);
     if (ctx->grav.valid && ctx->grav.ng > 0)
         k_sum_grav_pairs<<<2 * ctx->num_sms, 256, 0, ctx->stream>>>(ctx->grav.ng, ctx->grav.group_cell, ctx->tree.count,
                                                                     ctx->grav.n_epj, ctx->grav.n_spj, d + 2);
     SPH_CUDA(ctx, cudaGetLastError());
-    unsigned long long h[3];
+    unsigned long long h[4];
     SPH_CUDA(ctx, cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
     SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     out[0] = (int64_t)h[0];
@@ -934,5 +935,6 @@ int sph_work_counts(sph_ctx *ctx, int64_t out[8]) {
     out[4] = ctx->grav.ng;
     out[5] = ctx->grav.tot_epj;
     out[6] = ctx->grav.tot_spj;
+    out[7] = (int64_t)h[3];
     return SPH_OK;
 }

@@ -275,7 +275,8 @@ class Context:
         out = np.zeros(16, np.int64)
         self._check(self.L.sph_get_counters(self.h, _ptr(out)))
         keys = ["launches", "pairs_gather", "pairs_sym", "pairs_grav", "cells", "groups", "epj", "spj",
-                "walks_full", "walks_repair", "skin_violators", "units_walked", "units", "row_capacity"]
+                "walks_full", "walks_repair", "skin_violators", "units_walked", "units", "row_capacity",
+                "superset_entries"]
         return dict(zip(keys, out.tolist()))
 
 

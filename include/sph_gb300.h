@@ -199,7 +199,8 @@ int sph_step_timed(sph_ctx *ctx, int n_steps, double *device_ms);
  * out[5] gravity groups; out[6] EPJ entries; out[7] SPJ entries; out[8]
  * full neighbour-superset walks; out[9] partial (repair) walks; out[10]
  * particles whose h outgrew the superset skin; out[11] walk units walked;
- * out[12] walk units; out[13] superset row capacity; out[14..15] reserved. */
+ * out[12] walk units; out[13] superset row capacity; out[14] superset entries;
+ * out[15] reserved. */
 int sph_get_counters(sph_ctx *ctx, int64_t out[16]);
 /* ---- allocation-free Morton ordering -------------------------------------
  * No counterpart in the reference: FDPS builds its tree on the host.  This
