@@ -286,8 +286,8 @@ def main():
     hbm = peaks.get("hbm_gbs")
     rows = {}
     for name, (sname, bound, work, launches_per_step) in kernels.items():
-        ms_step = filt_ms / st if name == "filters" else seg[sname] / st
-        per_launch_ms = ms_step / launches_per_step
+        seg_ms_step = filt_ms / st if name == "filters" else seg[sname] / st
+        per_launch_ms = seg_ms_step / launches_per_step
         if per_launch_ms <= 0:
             continue
         if bound == "fp32":
