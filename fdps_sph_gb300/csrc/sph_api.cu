@@ -208,7 +208,7 @@ int sph_ctx_destroy(sph_ctx *ctx) {
                     ctx->grav.group_cell, ctx->grav.is_group, ctx->grav.n_epj, ctx->grav.n_spj, ctx->grav.off_epj,
                     ctx->grav.off_spj, ctx->grav.epj, ctx->grav.spj, ctx->scan.part, ctx->scan.total,
                     ctx->sup.nbr, ctx->sup.cnt, ctx->sup.hsup, ctx->sup.pxh, ctx->sup.pxl, ctx->sup.H2f,
-                    ctx->sup.units, ctx->tree.cinfo, ctx->sup.r2, ctx->sup.mf, ctx->sup.vR, ctx->sup.cvR,
+                    ctx->sup.units, ctx->tree.cinfo, ctx->sup.r2, ctx->sup.m, ctx->sup.vR, ctx->sup.cvR,
                     ctx->sup.umark, ctx->sup.uoff, ctx->sup.uidx};
     for (void *p : ptrs)
         if (p) cudaFree(p);

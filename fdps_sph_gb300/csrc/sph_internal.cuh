@@ -94,7 +94,7 @@ struct SphSuper {
     int K = 0, K_alloc = 0;
     int *nbr = nullptr, *cnt = nullptr;   // superset, ELL
     float *r2 = nullptr;                  // FP32 r^2 of every superset entry
-    float *mf = nullptr;                  // particle mass x mscale as float
+    float *m = nullptr;                   // neighbour mass x mscale of every superset entry
     double *hsup = nullptr;               // h when the superset was built
     float4 *pxh = nullptr, *pxl = nullptr;  // double-float positions
     float *H2f = nullptr;                 // (2.5 h)^2 rounded up

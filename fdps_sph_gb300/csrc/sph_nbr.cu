@@ -112,12 +112,13 @@ __device__ __forceinline__ float gap2_rd(float4 a_lo, float4 a_hi, float3 glo, f
     return __fadd_rd(__fadd_rd(__fmul_rd(gx, gx), __fmul_rd(gy, gy)), __fmul_rd(gz, gz));
 }
 
-__global__ void __launch_bounds__(NB_WARPS * 32, 10)
+__global__ void __launch_bounds__(NB_WARPS * 32, 6)
 k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ uidx, const double *__restrict__ x,
            const double *__restrict__ y, const double *__restrict__ z, const double *__restrict__ h,
            double *__restrict__ hsup, const float4 *__restrict__ xh,
            const float4 *__restrict__ xl, const float *__restrict__ H2f, WalkTree T, int *__restrict__ sup,
-           float *__restrict__ sup_r2, int *__restrict__ cnt, int K, int64_t stride, int *err, int *maxcnt) {
+           float *__restrict__ sup_r2, float *__restrict__ sup_m, int *__restrict__ cnt, int K, int64_t stride, int *err,
+           int *maxcnt) {
     __shared__ int4 s_stack[NB_WARPS][NB_STACK];   // records (first_child, n_child, start, count) of cells to visit
     __shared__ int s_cand[NB_WARPS][NB_CAND];
     __shared__ float4 s_ph[NB_WARPS][32];
@@ -125,6 +126,7 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
     __shared__ float s_h2[NB_WARPS][32];
     __shared__ int s_wj[NB_WARPS][8][32];     // per-lane write buffers: 8 entries = one 32-byte sector
     __shared__ float s_wr[NB_WARPS][8][32];
+    __shared__ float s_wm[NB_WARPS][8][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int w = blockIdx.x * NB_WARPS + warp;
     if (w >= n_units) return;   // warp-uniform
@@ -154,6 +156,7 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
     int count = 0, nc = 0;
     int *row = sup + (int64_t)i * stride;
     float *rrow = sup_r2 + (int64_t)i * stride;
+    float *mrow = sup_m + (int64_t)i * stride;
     // writes the lane's 8 buffered entries ending at `count` as full sectors
     auto put8 = [&]() {
         const int k0 = count - 8;
@@ -166,6 +169,10 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
             reinterpret_cast<int4 *>(row + k0)[1] = b;
             reinterpret_cast<float4 *>(rrow + k0)[0] = c;
             reinterpret_cast<float4 *>(rrow + k0)[1] = d;
+            reinterpret_cast<float4 *>(mrow + k0)[0] =
+                make_float4(s_wm[warp][0][lane], s_wm[warp][1][lane], s_wm[warp][2][lane], s_wm[warp][3][lane]);
+            reinterpret_cast<float4 *>(mrow + k0)[1] =
+                make_float4(s_wm[warp][4][lane], s_wm[warp][5][lane], s_wm[warp][6][lane], s_wm[warp][7][lane]);
         }
     };
 
@@ -191,6 +198,7 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
                 if (valid && r2 < k2 * fmaxf(H2i, s_h2[warp][t])) {
                     s_wj[warp][count & 7][lane] = jj;
                     s_wr[warp][count & 7][lane] = r2;
+                    s_wm[warp][count & 7][lane] = qh.w;
                     ++count;
                     if ((count & 7) == 0) put8();
                 }
@@ -251,6 +259,7 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
             if (k0 + q < K) {
                 row[k0 + q] = s_wj[warp][q][lane];
                 rrow[k0 + q] = s_wr[warp][q][lane];
+                mrow[k0 + q] = s_wm[warp][q][lane];
             }
         cnt[i] = count;
         if (count > K) atomicOr(err, ERR_SPH_LIST_OVERFLOW);
@@ -451,9 +460,9 @@ k_filter(int n, const int *__restrict__ sup, const float *__restrict__ sup_r2, c
 // decision of k_filter<0>, then CalcDensity's sum (force.h:9-23) in FP32
 // partial sums of 32 flushed to FP64, FLAG_GI floor and h update in FP64.
 __global__ void __launch_bounds__(128)
-k_density_sup32(int n, const int *__restrict__ sup, const float *__restrict__ sup_r2, const int *__restrict__ scnt,
-                int64_t stride, const double *__restrict__ x, const double *__restrict__ y,
-                const double *__restrict__ z, const float *__restrict__ mf, const double *__restrict__ m,
+k_density_sup32(int n, const int *__restrict__ sup, const float *__restrict__ sup_r2, const float *__restrict__ sup_m,
+                const int *__restrict__ scnt, int64_t stride, const double *__restrict__ x,
+                const double *__restrict__ y, const double *__restrict__ z, const double *__restrict__ m,
                 double *__restrict__ h, const double *__restrict__ hsup, double *__restrict__ dens, double inv_mscale,
                 int *err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -467,6 +476,7 @@ k_density_sup32(int n, const int *__restrict__ sup, const float *__restrict__ su
     const int c = scnt[i];
     const int *row = sup + (int64_t)i * stride;
     const float *rrow = sup_r2 + (int64_t)i * stride;
+    const float *mrow = sup_m + (int64_t)i * stride;
     double acc = 0.0;
     for (int k = 0; k < c; k += 8) {
         const int4 j0 = reinterpret_cast<const int4 *>(row + k)[0], j1 = reinterpret_cast<const int4 *>(row + k)[1];
@@ -474,9 +484,8 @@ k_density_sup32(int n, const int *__restrict__ sup, const float *__restrict__ su
         const int jj[8] = {j0.x, j0.y, j0.z, j0.w, j1.x, j1.y, j1.z, j1.w};
         const float rr[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
         const int m8 = min(8, c - k);
-        float mj[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) mj[u] = (u < m8) ? mf[jj[u]] : 0.0f;
+        const float4 m0 = reinterpret_cast<const float4 *>(mrow + k)[0], m1 = reinterpret_cast<const float4 *>(mrow + k)[1];
+        const float mj[8] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
         float part = 0.0f;
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
@@ -498,10 +507,6 @@ __global__ void k_skin_check(int n, const double *h, const double *hsup, int *er
     if (i < n && h[i] > (double)KAPPA * hsup[i]) atomicOr(err, ERR_SKIN);
 }
 
-__global__ void k_mass_f(int n, const double *m, double mscale, float *mf) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) mf[i] = (float)(m[i] * mscale);
-}
 
 // (2.5 h)^2 as float, rounded up so FP32 superset tests stay conservative
 __global__ void k_h2f(int n, const double *h, float *H2f) {
@@ -511,12 +516,13 @@ __global__ void k_h2f(int n, const double *h, float *H2f) {
     H2f[i] = __double2float_ru(H * H);
 }
 
-// double-float positions (hi / lo floats); .w of xh carries nothing here
-__global__ void k_pack_pos(int n, const double *x, const double *y, const double *z, float4 *xh, float4 *xl) {
+// double-float positions (hi / lo floats); .w of xh carries the mass x mscale
+__global__ void k_pack_pos(int n, const double *x, const double *y, const double *z, const double *m, double mscale,
+                           float4 *xh, float4 *xl) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float ax = (float)x[i], ay = (float)y[i], az = (float)z[i];
-    xh[i] = make_float4(ax, ay, az, 0.0f);
+    xh[i] = make_float4(ax, ay, az, (float)(m[i] * mscale));
     xl[i] = make_float4((float)(x[i] - (double)ax), (float)(y[i] - (double)ay), (float)(z[i] - (double)az), 0.0f);
 }
 
@@ -558,15 +564,13 @@ int sph_nbr_prepare(sph_ctx *ctx) {
         SPH_TRY(dalloc_n(ctx, &S.H2f, pitch));
         SPH_TRY(dalloc_n(ctx, &S.hsup, pitch));
         SPH_TRY(dalloc_n(ctx, &S.cnt, pitch));
-        SPH_TRY(dalloc_n(ctx, &S.mf, pitch));
         SPH_TRY(dalloc_n(ctx, &S.vR, pitch));
         S.cap_particles = pitch;
     }
     const int64_t cap = ctx->cap;
     k_pack_pos<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap),
-                                                            FLD(ctx->F, SPH_Z, cap), S.pxh, S.pxl);
-    ++ctx->launches;
-    k_mass_f<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, FLD(ctx->F, SPH_MASS, cap), ctx->mscale, S.mf);
+                                                            FLD(ctx->F, SPH_Z, cap), FLD(ctx->F, SPH_MASS, cap),
+                                                            ctx->mscale, S.pxh, S.pxl);
     ++ctx->launches;
     SPH_TRY(sph_nbr_refresh_h(ctx));
     // units
@@ -624,6 +628,7 @@ static int walk_units(sph_ctx *ctx, const int *uidx, int n_walk) {
             }
             SPH_TRY(dalloc_n(ctx, &S.nbr, (int64_t)S.K * pitch));
             SPH_TRY(dalloc_n(ctx, &S.r2, (int64_t)S.K * pitch));
+            SPH_TRY(dalloc_n(ctx, &S.m, (int64_t)S.K * pitch));
             for (int m = 0; m < 2; ++m) {
                 SPH_TRY(dalloc_n(ctx, &ctx->lists[m].nbr, (int64_t)S.K * pitch));
                 SPH_TRY(dalloc_n(ctx, &ctx->lists[m].cnt, pitch));
@@ -640,8 +645,8 @@ static int walk_units(sph_ctx *ctx, const int *uidx, int n_walk) {
         if (blocks > 0) {
             k_sup_walk<<<blocks, NB_WARPS * 32, 0, ctx->stream>>>(
                 n_walk, S.units, uidx, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
-                FLD(ctx->F, SPH_SMTH, cap), S.hsup, S.pxh, S.pxl, S.H2f, T, S.nbr, S.r2, S.cnt, S.K, (int64_t)S.K,
-                meta + META_ERR, meta + META_MAXCNT);
+                FLD(ctx->F, SPH_SMTH, cap), S.hsup, S.pxh, S.pxl, S.H2f, T, S.nbr, S.r2, S.m, S.cnt, S.K,
+                (int64_t)S.K, meta + META_ERR, meta + META_MAXCNT);
             ++ctx->launches;
         }
         SPH_CUDA(ctx, cudaGetLastError());
@@ -737,9 +742,9 @@ int sph_density_from_superset(sph_ctx *ctx) {
     int *meta = ctx->tree.meta;
     SPH_TRY(ensure_superset(ctx));
     k_density_sup32<<<sph_div_up(n, 128), 128, 0, ctx->stream>>>(
-        n, S.nbr, S.r2, S.cnt, (int64_t)S.K, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
-        S.mf, FLD(ctx->F, SPH_MASS, cap), FLD(ctx->F, SPH_SMTH, cap), S.hsup, FLD(ctx->F, SPH_DENS, cap),
-        1.0 / ctx->mscale, meta + META_ERR);
+        n, S.nbr, S.r2, S.m, S.cnt, (int64_t)S.K, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap),
+        FLD(ctx->F, SPH_Z, cap), FLD(ctx->F, SPH_MASS, cap), FLD(ctx->F, SPH_SMTH, cap), S.hsup,
+        FLD(ctx->F, SPH_DENS, cap), 1.0 / ctx->mscale, meta + META_ERR);
     ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
     ctx->lists[0].valid = false;
