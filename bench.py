@@ -278,8 +278,8 @@ def main():
         "filters": (None, "hbm", 2 * (8 * entries + 4 * w["pairs_gather"]) // 2, 2),
         "derivative": ("drvt", "fp32", FLOPS_PER_PAIR["drvt"] * w["pairs_gather"], 1),
         "hydro": ("hydro", "fp32", FLOPS_PER_PAIR["hydro"] * w["pairs_sym"], 1),
-        "grav_lists": ("grav_list", "hbm", 2 * 4 * (w["epj"] + w["spj"]), 1),
-        "gravity": ("grav", "fp32", FLOPS_PER_PAIR["grav"] * w["pairs_grav"], 1),
+        "grav_groups": ("grav_list", "hbm", 16 * w["cells"], 1),            # count / parent / flag per cell
+        "gravity": ("grav", "fp32", FLOPS_PER_PAIR["grav"] * w["pairs_grav"], 1),   # walk fused in
         "sort_tree": ("tree", "hbm", (36 + 8 * 24 + 2 * 32 * 8) * n, 1),
     }
     filt_ms = seg["drvt_list"] + seg["hydro_list"]

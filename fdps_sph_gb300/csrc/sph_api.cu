@@ -116,9 +116,14 @@ int compute_forces(sph_ctx *ctx) {
     SPH_TRY(sph_pass_hydro(ctx, 0));
     SPH_TRY(time_mark(ctx, SEG_HYDRO));
     if (ctx->cfg.self_gravity) {
-        SPH_TRY(sph_build_grav_lists(ctx));
-        SPH_TRY(time_mark(ctx, SEG_GRAV_LIST));
-        SPH_TRY(sph_pass_gravity(ctx, 0));
+        if (ctx->cfg.precision == SPH_PREC_MIXED) {
+            SPH_TRY(time_mark(ctx, SEG_GRAV_LIST));   // no lists: the walk runs inside the force kernel
+            SPH_TRY(sph_gravity_fused(ctx));
+        } else {
+            SPH_TRY(sph_build_grav_lists(ctx));
+            SPH_TRY(time_mark(ctx, SEG_GRAV_LIST));
+            SPH_TRY(sph_pass_gravity(ctx, 0));
+        }
         SPH_TRY(time_mark(ctx, SEG_GRAV));
     }
     ctx->have_forces = true;

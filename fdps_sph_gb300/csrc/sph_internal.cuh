@@ -27,6 +27,28 @@ constexpr int ERR_CELL_OVERFLOW = 2;
 constexpr int ERR_GRAV_OVERFLOW = 4;
 constexpr int ERR_NONFINITE = 8;
 
+// Double-float accumulation in FP32 (Knuth's TwoSum): hi + lo carries a
+// running sum to about 2^-44 relative without touching the FP64 pipe, which
+// on this GPU issues at a small fraction of the FP32 rate.
+__device__ __forceinline__ void df_add(float &hi, float &lo, float a) {
+    const float s = __fadd_rn(hi, a);
+    const float bp = __fsub_rn(s, hi);
+    const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(a, bp));
+    hi = s;
+    lo = __fadd_rn(lo, e);
+}
+
+// Mixed-precision tail of a density pass (force.h:32-41): rho = max(floor,
+// sum_j m_j w_j x norm) and h = 1.2 (m / rho)^(1/3), in FP32.  dscale =
+// (1365/64) / (pi mscale) carries the kernel constant and the mass scale;
+// invH = 1 / (2.5 h).
+__device__ __forceinline__ void density_tail32(float sum, float invH, float dscale, double m, double *rho,
+                                               double *h) {
+    const float d = fmaxf((float)DENS_FLOOR, sum * dscale * (invH * invH * invH));
+    *rho = (double)d;
+    *h = (double)((float)SMTH_COEF * cbrtf((float)m / d));
+}
+
 struct DevMaterial {
     int kind;            // 0 table, 1 Tillotson, 2 ideal gas, -1 unset
     int n_rho, n_u, pad;
@@ -85,7 +107,8 @@ struct GravLists {
     int *epj = nullptr, *spj = nullptr;
     int ng = 0;
     int64_t tot_epj = 0, tot_spj = 0;
-    bool valid = false;
+    bool valid = false;          // epj / spj lists filled
+    bool counts_valid = false;   // n_epj / n_spj filled (by the lists or by the fused walk)
 };
 
 // per-step SPH neighbour superset (sph_nbr.cu)
@@ -201,7 +224,9 @@ int sph_nbr_refresh_h(sph_ctx *ctx);     // after h changed
 int sph_build_sph_lists(sph_ctx *ctx, int mode);
 int sph_density_from_superset(sph_ctx *ctx);
 int sph_nbr_ensure_superset(sph_ctx *ctx);   // mixed precision: density pass without an exact list
+int sph_build_grav_groups(sph_ctx *ctx);   // gravity i-groups (cells with <= n_group particles)
 int sph_build_grav_lists(sph_ctx *ctx);
+int sph_gravity_fused(sph_ctx *ctx);       // mixed precision: walk + force in one kernel
 
 // passes (sph_pairs.cu)
 int sph_pass_density(sph_ctx *ctx, int build_lists);

@@ -174,7 +174,7 @@ static int dalloc_l(sph_ctx *ctx, T **p, int64_t n) {
     return SPH_OK;
 }
 
-int sph_build_grav_lists(sph_ctx *ctx) {
+int sph_build_grav_groups(sph_ctx *ctx) {
     GravLists &G = ctx->grav;
     Tree &t = ctx->tree;
     const int nc = t.n_cell_host;
@@ -198,6 +198,16 @@ int sph_build_grav_lists(sph_ctx *ctx) {
     SPH_CUDA(ctx, cudaStreamSynchronize(st));
     const int ng = hs[0];
     G.ng = ng;
+    return SPH_OK;
+}
+
+int sph_build_grav_lists(sph_ctx *ctx) {
+    SPH_TRY(sph_build_grav_groups(ctx));
+    GravLists &G = ctx->grav;
+    Tree &t = ctx->tree;
+    cudaStream_t st = ctx->stream;
+    const int ng = G.ng;
+    int *hs = (int *)ctx->host_scalars;
     const int blocks = (ng + GQ_WARPS - 1) / GQ_WARPS;
     SPH_CUDA(ctx, cudaMemsetAsync(t.meta + META_ERR, 0, sizeof(int), st));
     k_grav_lists<false><<<blocks, GQ_WARPS * 32, 0, st>>>(ng, G.group_cell, FLD(ctx->F, SPH_X, ctx->cap),
@@ -232,5 +242,6 @@ int sph_build_grav_lists(sph_ctx *ctx) {
                                                         G.off_spj, G.epj, G.spj, t.meta + META_ERR); ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
     G.valid = true;
+    G.counts_valid = true;
     return SPH_OK;
 }

@@ -463,7 +463,7 @@ __global__ void __launch_bounds__(128)
 k_density_sup32(int n, const int *__restrict__ sup, const float *__restrict__ sup_r2, const float *__restrict__ sup_m,
                 const int *__restrict__ scnt, int64_t stride, const double *__restrict__ x,
                 const double *__restrict__ y, const double *__restrict__ z, const double *__restrict__ m,
-                double *__restrict__ h, const double *__restrict__ hsup, double *__restrict__ dens, double inv_mscale,
+                double *__restrict__ h, const double *__restrict__ hsup, double *__restrict__ dens, float dscale,
                 int *err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -471,13 +471,13 @@ k_density_sup32(int n, const int *__restrict__ sup, const float *__restrict__ su
     const double Hi = __dmul_rn(SUPPORT, hi);
     const double H2 = __dmul_rn(Hi, Hi);
     const float H2i = (float)H2;
-    const float invH = (float)(1.0 / Hi);
+    const float invH = 1.0f / (float)Hi;
     const double xi = x[i], yi = y[i], zi = z[i];
     const int c = scnt[i];
     const int *row = sup + (int64_t)i * stride;
     const float *rrow = sup_r2 + (int64_t)i * stride;
     const float *mrow = sup_m + (int64_t)i * stride;
-    double acc = 0.0;
+    float acc_h = 0.0f, acc_l = 0.0f;
     for (int k = 0; k < c; k += 8) {
         const int4 j0 = reinterpret_cast<const int4 *>(row + k)[0], j1 = reinterpret_cast<const int4 *>(row + k)[1];
         const float4 r0 = reinterpret_cast<const float4 *>(rrow + k)[0], r1 = reinterpret_cast<const float4 *>(rrow + k)[1];
@@ -495,11 +495,9 @@ k_density_sup32(int n, const int *__restrict__ sup, const float *__restrict__ su
             const float p2 = p * p, p4 = p2 * p2;
             part = fmaf(mj[u], (1.0f + s_ * (8.0f + s_ * (25.0f + s_ * 32.0f))) * (p4 * p4), part);
         }
-        acc += (double)part;   // partial sums of at most 8 terms
+        df_add(acc_h, acc_l, part);   // partial sums of at most 8 terms
     }
-    const double d = fmax(DENS_FLOOR, acc * inv_mscale * (1365.0 / 64.0) / (Hi * Hi * Hi * 3.141592653589793));
-    dens[i] = d;
-    h[i] = SMTH_COEF * pow(m[i] / d, 1.0 / 3.0);
+    density_tail32(acc_h + acc_l, invH, dscale, m[i], dens + i, h + i);
 }
 
 __global__ void k_skin_check(int n, const double *h, const double *hsup, int *err) {
@@ -744,7 +742,7 @@ int sph_density_from_superset(sph_ctx *ctx) {
     k_density_sup32<<<sph_div_up(n, 128), 128, 0, ctx->stream>>>(
         n, S.nbr, S.r2, S.m, S.cnt, (int64_t)S.K, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap),
         FLD(ctx->F, SPH_Z, cap), FLD(ctx->F, SPH_MASS, cap), FLD(ctx->F, SPH_SMTH, cap), S.hsup,
-        FLD(ctx->F, SPH_DENS, cap), 1.0 / ctx->mscale, meta + META_ERR);
+        FLD(ctx->F, SPH_DENS, cap), (float)(1365.0 / 64.0 / (3.141592653589793 * ctx->mscale)), meta + META_ERR);
     ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
     ctx->lists[0].valid = false;

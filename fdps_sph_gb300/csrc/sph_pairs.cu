@@ -268,16 +268,15 @@ __device__ __forceinline__ float df_diff(float ah, float al, float bh, float bl)
 __global__ void __launch_bounds__(PT) k_density32(int n, const float4 *__restrict__ xh, const float4 *__restrict__ xl,
                                                   const double *__restrict__ m, double *__restrict__ h,
                                                   double *__restrict__ dens, const int *__restrict__ nbr,
-                                                  const int *__restrict__ cnt, int64_t pitch, double inv_mscale) {
+                                                  const int *__restrict__ cnt, int64_t pitch, float dscale) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4 pih = xh[i], pil = xl[i];
     const double hi = h[i];
     const double H = SUPPORT * hi;
-    const float invH = (float)(1.0 / H);
-    const double norm = kernel_norm(H);
+    const float invH = 1.0f / (float)H;
     const int c = cnt[i];
-    double acc = 0.0;
+    float acc_h = 0.0f, acc_l = 0.0f;
     float part = 0.0f;
     for (int k = 0; k < c; ++k) {
         const int j = nbr[(int64_t)i * pitch + k];
@@ -290,14 +289,12 @@ __global__ void __launch_bounds__(PT) k_density32(int n, const float4 *__restric
         wendland_poly_f(r * invH, w, g);
         part = fmaf(qh.w, w, part);
         if ((k & 31) == 31) {
-            acc += (double)part;
+            df_add(acc_h, acc_l, part);
             part = 0.0f;
         }
     }
-    acc += (double)part;
-    const double d = fmax(DENS_FLOOR, acc * inv_mscale * norm);
-    dens[i] = d;
-    h[i] = SMTH_COEF * pow(m[i] / d, 1.0 / 3.0);
+    df_add(acc_h, acc_l, part);
+    density_tail32(acc_h + acc_l, invH, dscale, m[i], dens + i, h + i);
 }
 
 // mixed derivative
@@ -307,7 +304,7 @@ struct DrvtArgs32 {
     double *divv, *rx, *ry, *rz, *gradh, *bal;
     const int *nbr, *cnt;
     int64_t pitch;
-    double inv_mscale;
+    float kscale;   // (1365/64) / (pi mscale)
 };
 
 __device__ __forceinline__ void drvt_pair32(const float4 pih, const float4 pil, const float4 vih, const float4 vil,
@@ -336,12 +333,10 @@ __global__ void __launch_bounds__(PT) k_drvt32(int n, DrvtArgs32 a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4 pih = a.xh[i], pil = a.xl[i], vih = a.vh[i], vil = a.vl[i];
-    const double hi = a.h[i], rhoi = a.dens[i];
-    const double H = SUPPORT * hi;
-    const double normd = kernel_norm(H);
-    const float invH = (float)(1.0 / H), Hf = (float)H, ceps = (float)(1.0e-6 * hi);
-    // kernel normalisation folded out: sums carry norm = 1, restored in FP64
-    double D[5] = {0, 0, 0, 0, 0};
+    const double hi = a.h[i];
+    const float Hf = (float)(SUPPORT * hi), invH = 1.0f / Hf, ceps = (float)(1.0e-6 * hi);
+    // kernel normalisation folded out of the pair sums and applied once at the end
+    float Dh[5] = {0, 0, 0, 0, 0}, Dl[5] = {0, 0, 0, 0, 0};
     float P[5] = {0, 0, 0, 0, 0};
     const int c = a.cnt[i];
     int k = 0;
@@ -355,7 +350,7 @@ __global__ void __launch_bounds__(PT) k_drvt32(int n, DrvtArgs32 a) {
         if ((k & 31) == 30) {
 #pragma unroll
             for (int q = 0; q < 5; ++q) {
-                D[q] += (double)P[q];
+                df_add(Dh[q], Dl[q], P[q]);
                 P[q] = 0.0f;
             }
         }
@@ -364,17 +359,23 @@ __global__ void __launch_bounds__(PT) k_drvt32(int n, DrvtArgs32 a) {
         const int j = a.nbr[(int64_t)i * a.pitch + k];
         drvt_pair32(pih, pil, vih, vil, a.xh[j], a.xl[j], a.vh[j], a.vl[j], invH, Hf, ceps, P);
     }
+    // per-particle tail of force.h:70-76 in FP32
+    const float sc = a.kscale * (invH * invH * invH);
+    float D[5];
 #pragma unroll
-    for (int q = 0; q < 5; ++q) D[q] = (D[q] + (double)P[q]) * normd * a.inv_mscale;
-    double gs = -D[4] / hi;
-    gs = 1.0 / (1.0 + hi * gs / (3.0 * rhoi));
-    const double dv = D[0] / rhoi, r0 = D[1] / rhoi, r1 = D[2] / rhoi, r2 = D[3] / rhoi;
+    for (int q = 0; q < 5; ++q) {
+        df_add(Dh[q], Dl[q], P[q]);
+        D[q] = (Dh[q] + Dl[q]) * sc;
+    }
+    const float rho = (float)a.dens[i], hf = (float)hi;
+    const float gs = 1.0f / (1.0f + hf * (-D[4] / hf) / (3.0f * rho));
+    const float dv = D[0] / rho, r0 = D[1] / rho, r1 = D[2] / rho, r2 = D[3] / rho;
     a.divv[i] = dv;
     a.rx[i] = r0;
     a.ry[i] = r1;
     a.rz[i] = r2;
     a.gradh[i] = gs;
-    a.bal[i] = fabs(dv) / (fabs(dv) + sqrt(r0 * r0 + r1 * r1 + r2 * r2) + 1.0e-4 * a.snds[i] / hi);
+    a.bal[i] = fabsf(dv) / (fabsf(dv) + sqrtf(r0 * r0 + r1 * r1 + r2 * r2) + 1.0e-4f * (float)a.snds[i] / hf);
 }
 
 // mixed hydro: per-particle FP32 packs hA = (f P / rho^2, c_s, f, Bal), hB = (rho, 1/H, H, 1e-6 h).
@@ -384,9 +385,9 @@ __global__ void k_hydro_pack32(int n, const double *h, const double *dens, const
                                const double *gradh, const double *bal, float4 *hA, float4 *hB) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double hi = h[i], H = SUPPORT * hi, rho = dens[i];
-    hA[i] = make_float4((float)(gradh[i] * pres[i] / (rho * rho)), (float)snds[i], (float)gradh[i], (float)bal[i]);
-    hB[i] = make_float4((float)rho, (float)(1.0 / H), (float)H, (float)(1.0e-6 * hi));
+    const float hi = (float)h[i], H = (float)SUPPORT * hi, rho = (float)dens[i], f = (float)gradh[i];
+    hA[i] = make_float4(f * (float)pres[i] / (rho * rho), (float)snds[i], f, (float)bal[i]);
+    hB[i] = make_float4(rho, 1.0f / H, H, 1.0e-6f * hi);
 }
 
 struct HydroArgs32 {
@@ -395,7 +396,7 @@ struct HydroArgs32 {
     double *ax, *ay, *az, *edot, *dt;
     const int *nbr, *cnt;
     int64_t pitch;
-    double inv_mscale;
+    float kscale;   // (1365/64) / (pi mscale)
 };
 
 struct HydroJ32 {
@@ -448,9 +449,7 @@ __global__ void __launch_bounds__(PT) k_hydro32(int n, HydroArgs32 a) {
     if (i >= n) return;
     const float4 pih = a.xh[i], pil = a.xl[i], vih = a.vh[i], vil = a.vl[i];
     const float4 Ai = a.hA[i], Bi = a.hB[i];
-    const double hi = a.h[i];
-    const double normd = kernel_norm(SUPPORT * hi);
-    double D[4] = {0, 0, 0, 0};
+    float Dh[4] = {0, 0, 0, 0}, Dl[4] = {0, 0, 0, 0};
     float P[4] = {0, 0, 0, 0};
     float vmax = 0.0f;
     const int c = a.cnt[i];
@@ -464,7 +463,7 @@ __global__ void __launch_bounds__(PT) k_hydro32(int n, HydroArgs32 a) {
         if ((k & 31) == 30) {
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                D[q] += (double)P[q];
+                df_add(Dh[q], Dl[q], P[q]);
                 P[q] = 0.0f;
             }
         }
@@ -473,14 +472,19 @@ __global__ void __launch_bounds__(PT) k_hydro32(int n, HydroArgs32 a) {
         const HydroJ32 J = load_hydro_j(a, a.nbr[(int64_t)i * a.pitch + k]);
         hydro_pair32(pih, pil, vih, vil, Ai, Bi, J, P, vmax);
     }
-    const double sc = normd * a.inv_mscale;
+    // kernel normalisation of i (Bi.y = 1 / H_i) and the mass scale, in FP32
+    const float sc = a.kscale * (Bi.y * Bi.y * Bi.y);
+    float D[4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) D[q] = (D[q] + (double)P[q]) * sc;
+    for (int q = 0; q < 4; ++q) {
+        df_add(Dh[q], Dl[q], P[q]);
+        D[q] = (Dh[q] + Dl[q]) * sc;
+    }
     a.ax[i] = D[0];
     a.ay[i] = D[1];
     a.az[i] = D[2];
     a.edot[i] = D[3];
-    a.dt[i] = C_CFL * 2.0 * hi / (double)vmax;
+    a.dt[i] = (float)(2.0 * C_CFL) * (float)a.h[i] / vmax;   // force.h:126
 }
 
 // cell monopoles as double-float with G folded into the mass
@@ -577,6 +581,310 @@ __global__ void __launch_bounds__(GT) k_grav32(const int *__restrict__ group_cel
             gz[i] = D[2] * inv_gscale;
             pot[i] = D[3] * inv_gscale;
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Mixed-precision tree gravity with the walk fused in: one CTA per i-group.
+// All warps walk the octree breadth-first together, 32 opened cells per
+// iteration (eight lanes per cell, one child per lane), with the opening rule
+// and append order of k_grav_lists / or_grav_walk, into shared-memory EPJ and
+// SPJ buffers; when the buffers are full, or the walk has ended, every thread
+// accumulates the buffered interactions.  No interaction list reaches global
+// memory.  The queue holds whole cell records (first child, children | level
+// << 8, start, count), loaded together with the child's centre of mass when
+// the child is tested, so an iteration waits on one global load.
+//
+// Accumulation: each thread carries two i-particles (ii and ii + Wt, Wt =
+// roundup(count / 2, 32)), and the block's P = 256 / Wt copies of the group
+// split each tile of j between them, four j per round; small groups keep the
+// FP32 lanes busy and every shared-memory read feeds two interactions.
+
+constexpr int GF_T = 256;
+constexpr int GF_Q = 2048;   // BFS ring of opened cell records (power of two)
+constexpr int GF_E = 2048;   // buffered EPJ particle indices
+constexpr int GF_S = 2048;   // buffered SPJ cell indices
+constexpr int GF_W = GF_T / 32;
+
+__device__ __forceinline__ void grav_acc(float px, float py, float pz, float e2, float4 q, float &a0, float &a1,
+                                         float &a2, float &a3) {
+    const float dx = px - q.x, dy = py - q.y, dz = pz - q.z;
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, e2)));
+    const float ri = rsqrtf(r2);
+    const float mri = q.w * ri;
+    const float mr3 = mri * ri * ri;
+    a0 = fmaf(-mr3, dx, a0);
+    a1 = fmaf(-mr3, dy, a1);
+    a2 = fmaf(-mr3, dz, a2);
+    a3 -= mri;
+}
+
+__global__ void __launch_bounds__(GF_T, 3)
+k_grav_fused32(const int *__restrict__ group_cell, const int4 *__restrict__ cinfo, const double4 *__restrict__ com,
+               const double *__restrict__ rb, const double *__restrict__ x, const double *__restrict__ y,
+               const double *__restrict__ z, const float4 *__restrict__ xh, const float4 *__restrict__ xl,
+               const double *__restrict__ h, const float4 *__restrict__ ch, const float4 *__restrict__ cl, float gms,
+               double *gx, double *gy, double *gz, double *pot, int *n_epj, int *n_spj, int *err) {
+    __shared__ int4 s_q[GF_Q];
+    __shared__ __align__(16) int s_e[GF_E];   // also the reduction buffer of the partitions
+    __shared__ int s_s[GF_S];
+    __shared__ float4 s_tile[GF_T];
+    __shared__ int s_w[2][GF_W][3];            // per warp: leaf particles, far children, near children
+    __shared__ double s_box[GF_W][6];
+    __shared__ double s_rb[MAX_LEVELS];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned below = (1u << lane) - 1u;
+    const int4 gi = cinfo[group_cell[blockIdx.x]];
+    const int s = gi.z, cnt_all = gi.w;
+    const float4 c_h = xh[s], c_l = xl[s];     // group origin: its first particle
+    for (int l = tid; l < MAX_LEVELS; l += GF_T) s_rb[l] = rb[8 + l];
+    // bounding box of the whole group
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int k = tid; k < cnt_all; k += GF_T) {
+        const double p[3] = {x[s + k], y[s + k], z[s + k]};
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = fmin(lo[d], p[d]);
+            hi[d] = fmax(hi[d], p[d]);
+        }
+    }
+    for (int d = 0; d < 3; ++d)
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[d] = fmin(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
+            hi[d] = fmax(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+        }
+    if (lane == 0)
+        for (int d = 0; d < 3; ++d) {
+            s_box[warp][d] = lo[d];
+            s_box[warp][3 + d] = hi[d];
+        }
+    __syncthreads();
+    __shared__ double s_gbox[6];   // the group's box in FP64, for the exact opening test
+    if (tid < 6) {
+        double v = tid < 3 ? INFINITY : -INFINITY;
+        for (int w = 0; w < GF_W; ++w) v = tid < 3 ? fmin(v, s_box[w][tid]) : fmax(v, s_box[w][tid]);
+        s_gbox[tid] = v;
+    }
+    __syncthreads();
+    // the box relative to the group origin, in FP32, for the fast opening test
+    float lof[3], hif[3];
+    {
+        const float oh[3] = {c_h.x, c_h.y, c_h.z}, ol[3] = {c_l.x, c_l.y, c_l.z};
+        for (int d = 0; d < 3; ++d) {
+            const double o = (double)oh[d] + (double)ol[d];
+            lof[d] = (float)(s_gbox[d] - o);
+            hif[d] = (float)(s_gbox[3 + d] - o);
+        }
+    }
+    const int q = tid >> 3, k = tid & 7, qw = lane >> 3;
+    int tot_e = 0, tot_s = 0;
+    for (int i_base = 0; i_base < cnt_all; i_base += 2 * GF_T) {
+        const int cnt = min(2 * GF_T, cnt_all - i_base);
+        const int Wt = ((cnt + 1) / 2 + 31) & ~31, P = GF_T / Wt;
+        const int part = tid / Wt, ii = tid - part * Wt;
+        const bool slot = part < P;   // warp-uniform
+        float px[2], py[2], pz[2], e2[2];
+        for (int u = 0; u < 2; ++u) {
+            const int iu = ii + u * Wt;
+            px[u] = py[u] = pz[u] = 0.f;
+            e2[u] = 1.f;
+            if (slot && iu < cnt) {
+                const int i = s + i_base + iu;
+                const float4 ph = xh[i], pl = xl[i];
+                px[u] = df_diff(ph.x, pl.x, c_h.x, c_l.x);
+                py[u] = df_diff(ph.y, pl.y, c_h.y, c_l.y);
+                pz[u] = df_diff(ph.z, pl.z, c_h.z, c_l.z);
+                const double hh = h[i];
+                e2[u] = (float)(hh * hh);
+            }
+        }
+        float Dh[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}}, Dl[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+        int head = 0, tail = 1, it = 0;
+        if (tid == 0) s_q[0] = cinfo[0];   // the root, level 0
+        __syncthreads();
+        for (;;) {
+            // ---- walk until the buffers are full or the queue is empty
+            int ne = 0, ns = 0, done = 0;
+            for (;; ++it) {
+                if (head >= tail) {
+                    done = 1;
+                    break;
+                }
+                const int nproc = min(GF_T / 8, tail - head);
+                const bool a = q < nproc;
+                const int4 ci = a ? s_q[(head + q) & (GF_Q - 1)] : make_int4(0, 0, 0, 0);
+                const int nch = ci.y & 255, lev = ci.y >> 8;
+                const bool leaf = a && nch == 0;
+                const int lc = leaf ? ci.w : 0;   // same in the eight lanes of a cell
+                bool near = false, far = false;
+                int chc = 0;
+                int4 crec = make_int4(0, 0, 0, 0);
+                if (a && k < nch) {
+                    chc = ci.x + k;
+                    const float4 qh = ch[chc], ql = cl[chc];
+                    crec = cinfo[chc];
+                    const double rbd = s_rb[lev + 1];
+                    const float rbf = (float)rbd;
+                    // FP32 distance from the box on coordinates relative to the group origin, with a
+                    // bound on its error; inside the bound the FP64 test of the list walk decides
+                    const float pr[3] = {df_diff(qh.x, ql.x, c_h.x, c_l.x), df_diff(qh.y, ql.y, c_h.y, c_l.y),
+                                         df_diff(qh.z, ql.z, c_h.z, c_l.z)};
+                    const float pa[3] = {fabsf(qh.x) + fabsf(c_h.x), fabsf(qh.y) + fabsf(c_h.y),
+                                         fabsf(qh.z) + fabsf(c_h.z)};
+                    float d2f = 0.0f, E = 0.0f;
+                    for (int d = 0; d < 3; ++d) {
+                        const float b = pr[d] < lof[d] ? lof[d] : (pr[d] > hif[d] ? hif[d] : pr[d]);
+                        const float dd = fabsf(b - pr[d]);
+                        const float ed = 2.384185791015625e-07f * (fabsf(pr[d]) + fabsf(b) + dd) +
+                                         2.842170943040401e-14f * pa[d];   // 2^-22 relative, 2^-45 absolute
+                        d2f = fmaf(dd, dd, d2f);
+                        E = fmaf(2.0f * dd + ed, ed, E);
+                    }
+                    E += 4.76837158203125e-07f * (d2f + rbf);   // 2^-21: sums and the rounding of rb
+                    if (fabsf(d2f - rbf) > E) {
+                        near = d2f <= rbf;
+                    } else {
+                        const double4 cm = com[chc];
+                        const double pp[3] = {cm.x, cm.y, cm.z};
+                        double dd[3];
+                        for (int d = 0; d < 3; ++d) {
+                            const double l = s_gbox[d], u = s_gbox[3 + d];
+                            dd[d] = (pp[d] < l) ? __dsub_rn(l, pp[d]) : ((pp[d] > u) ? __dsub_rn(pp[d], u) : 0.0);
+                        }
+                        const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dd[0], dd[0]), __dmul_rn(dd[1], dd[1])),
+                                                    __dmul_rn(dd[2], dd[2]));
+                        near = d2 <= rbd;
+                    }
+                    far = !near;
+                }
+                const unsigned nm = __ballot_sync(0xffffffffu, near);
+                const unsigned fm = __ballot_sync(0xffffffffu, far);
+                int lpre = 0, lsum = 0;
+                for (int g = 0; g < 4; ++g) {
+                    const int v = __shfl_sync(0xffffffffu, lc, g * 8);
+                    lpre += g < qw ? v : 0;
+                    lsum += v;
+                }
+                const int buf = it & 1;
+                if (lane == 0) {
+                    s_w[buf][warp][0] = lsum;
+                    s_w[buf][warp][1] = __popc(fm);
+                    s_w[buf][warp][2] = __popc(nm);
+                }
+                __syncthreads();
+                int oe = 0, of = 0, on = 0, te = 0, tf = 0, tn = 0;
+                for (int w = 0; w < GF_W; ++w) {
+                    const int e0 = s_w[buf][w][0], f0 = s_w[buf][w][1], n0 = s_w[buf][w][2];
+                    if (w < warp) {
+                        oe += e0;
+                        of += f0;
+                        on += n0;
+                    }
+                    te += e0;
+                    tf += f0;
+                    tn += n0;
+                }
+                if (ne + te > GF_E || ns + tf > GF_S) {   // flush first, then redo this batch
+                    if (ne == 0 && ns == 0) {              // a batch larger than the buffers: give up
+                        if (tid == 0) atomicOr(err, ERR_GRAV_OVERFLOW);
+                        done = 1;
+                    }
+                    ++it;
+                    break;
+                }
+                if (tail - head - nproc + tn > GF_Q) {
+                    if (tid == 0) atomicOr(err, ERR_GRAV_OVERFLOW);
+                    done = 1;
+                    ++it;
+                    break;
+                }
+                if (leaf)
+                    for (int t = k; t < lc; t += 8) s_e[ne + oe + lpre + t] = ci.z + t;
+                if (far) s_s[ns + of + __popc(fm & below)] = chc;
+                if (near) {
+                    crec.y = (crec.y & 255) | ((lev + 1) << 8);
+                    s_q[(tail + on + __popc(nm & below)) & (GF_Q - 1)] = crec;
+                }
+                ne += te;
+                ns += tf;
+                head += nproc;
+                tail += tn;
+                __syncthreads();   // the records and buffer entries written above
+            }
+            if (i_base == 0) {
+                tot_e += ne;
+                tot_s += ns;
+            }
+            // ---- accumulate the buffered EPJ, then SPJ
+            for (int pass = 0; pass < 2; ++pass) {
+                const int nl = pass == 0 ? ne : ns;
+                for (int t0 = 0; t0 < nl; t0 += GF_T) {
+                    const int kk = t0 + tid;
+                    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);   // zero mass pads the tile
+                    if (kk < nl) {
+                        float4 qh, ql;
+                        float gm;
+                        if (pass == 0) {
+                            const int j = s_e[kk];
+                            qh = xh[j];
+                            ql = xl[j];
+                            gm = qh.w * gms;
+                        } else {
+                            const int cc = s_s[kk];
+                            qh = ch[cc];
+                            ql = cl[cc];
+                            gm = qh.w;
+                        }
+                        v = make_float4(df_diff(qh.x, ql.x, c_h.x, c_l.x), df_diff(qh.y, ql.y, c_h.y, c_l.y),
+                                        df_diff(qh.z, ql.z, c_h.z, c_l.z), gm);
+                    }
+                    s_tile[tid] = v;
+                    __syncthreads();
+                    if (slot) {
+                        const int step = 4 * P;
+                        const int tnr = (min(GF_T, nl - t0) + step - 1) / step * step;   // <= GF_T: step divides it
+                        float A[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+                        for (int t = part; t < tnr; t += step) {
+                            const float4 q0 = s_tile[t], q1 = s_tile[t + P], q2 = s_tile[t + 2 * P],
+                                         q3 = s_tile[t + 3 * P];
+#pragma unroll
+                            for (int u = 0; u < 2; ++u) {
+                                grav_acc(px[u], py[u], pz[u], e2[u], q0, A[u][0], A[u][1], A[u][2], A[u][3]);
+                                grav_acc(px[u], py[u], pz[u], e2[u], q1, A[u][0], A[u][1], A[u][2], A[u][3]);
+                                grav_acc(px[u], py[u], pz[u], e2[u], q2, A[u][0], A[u][1], A[u][2], A[u][3]);
+                                grav_acc(px[u], py[u], pz[u], e2[u], q3, A[u][0], A[u][1], A[u][2], A[u][3]);
+                            }
+                        }
+#pragma unroll
+                        for (int u = 0; u < 2; ++u)
+                            for (int c4 = 0; c4 < 4; ++c4) df_add(Dh[u][c4], Dl[u][c4], A[u][c4]);
+                    }
+                    __syncthreads();
+                }
+            }
+            if (done) break;
+        }
+        // ---- sum the partitions of each i-particle
+        double *red = reinterpret_cast<double *>(s_e);   // GF_T x 4 doubles = the size of s_e
+        for (int u = 0; u < 2; ++u) {
+            for (int c4 = 0; c4 < 4; ++c4) red[c4 * GF_T + tid] = (double)Dh[u][c4] + (double)Dl[u][c4];
+            __syncthreads();
+            const int iu = ii + u * Wt;
+            if (slot && part == 0 && iu < cnt) {
+                double r[4] = {0, 0, 0, 0};
+                for (int p2 = 0; p2 < P; ++p2)
+                    for (int c4 = 0; c4 < 4; ++c4) r[c4] += red[c4 * GF_T + p2 * Wt + ii];
+                const int i = s + i_base + iu;
+                gx[i] = r[0];
+                gy[i] = r[1];
+                gz[i] = r[2];
+                pot[i] = r[3];
+            }
+            __syncthreads();
+        }
+    }
+    if (tid == 0) {
+        n_epj[blockIdx.x] = tot_e;   // of the first chunk of i when a group has more than 512 particles
+        n_spj[blockIdx.x] = tot_s;
     }
 }
 
@@ -765,7 +1073,7 @@ int sph_pass_density(sph_ctx *ctx, int build_lists) {
     if (ctx->cfg.precision == SPH_PREC_MIXED) {
         k_density32<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, ctx->xh, ctx->xl, CF(SPH_MASS), CF(SPH_SMTH),
                                                               CF(SPH_DENS), L.nbr, L.cnt, L.pitch,
-                                                              1.0 / ctx->mscale); ++ctx->launches;
+                                                              (float)(WNORM / (PI_D * ctx->mscale))); ++ctx->launches;
     } else {
         k_density64<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, CF(SPH_X), CF(SPH_Y), CF(SPH_Z), CF(SPH_MASS),
                                                               CF(SPH_SMTH), CF(SPH_DENS), L.nbr, L.cnt, L.pitch); ++ctx->launches;
@@ -789,7 +1097,8 @@ int sph_pass_derivative(sph_ctx *ctx, int build_lists) {
     if (ctx->cfg.precision == SPH_PREC_MIXED) {
         DrvtArgs32 a{ctx->xh,     ctx->xl,      ctx->vhf,     ctx->vlf,      CF(SPH_SMTH), CF(SPH_DENS),
                      CF(SPH_SNDS), CF(SPH_DIVV), CF(SPH_ROTX), CF(SPH_ROTY),  CF(SPH_ROTZ), CF(SPH_GRADH),
-                     CF(SPH_BAL),  L.nbr,        L.cnt,        L.pitch,       1.0 / ctx->mscale};
+                     CF(SPH_BAL),  L.nbr,        L.cnt,        L.pitch,
+                     (float)(WNORM / (PI_D * ctx->mscale))};
         k_drvt32<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, a); ++ctx->launches;
     } else {
         DrvtArgs a{CF(SPH_X),    CF(SPH_Y),    CF(SPH_Z),    CF(SPH_VX),    CF(SPH_VY),   CF(SPH_VZ),
@@ -813,7 +1122,7 @@ int sph_pass_hydro(sph_ctx *ctx, int build_lists) {
                                                                     CF(SPH_SNDS), CF(SPH_GRADH), CF(SPH_BAL), hA, hB); ++ctx->launches;
         HydroArgs32 a{ctx->xh,    ctx->xl,    ctx->vhf,   ctx->vlf,       hA,         hB,    CF(SPH_SMTH),
                       CF(SPH_AX), CF(SPH_AY), CF(SPH_AZ), CF(SPH_ENGDOT), CF(SPH_DT), L.nbr, L.cnt,
-                      L.pitch,    1.0 / ctx->mscale};
+                      L.pitch,    (float)(WNORM / (PI_D * ctx->mscale))};
         k_hydro32<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, a); ++ctx->launches;
     } else {
         double4 *aux = (double4 *)ctx->F2;
@@ -916,16 +1225,19 @@ int sph_init_smth(sph_ctx *ctx) {
 int sph_work_counts(sph_ctx *ctx, int64_t out[8]) {
     for (int k = 0; k < 8; ++k) out[k] = 0;
     unsigned long long *d = (unsigned long long *)(ctx->scratch_d + 4096);
-    SPH_CUDA(ctx, cudaMemsetAsync(d, 0, 4 * sizeof(unsigned long long), ctx->stream));
+    SPH_CUDA(ctx, cudaMemsetAsync(d, 0, 6 * sizeof(unsigned long long), ctx->stream));
     const int n = (int)ctx->n;
     if (ctx->sup.valid) k_sum_cnt<<<2 * ctx->num_sms, 256, 0, ctx->stream>>>(n, ctx->sup.cnt, d + 3);
     if (ctx->lists[0].valid) k_sum_cnt<<<2 * ctx->num_sms, 256, 0, ctx->stream>>>(n, ctx->lists[0].cnt, d);
     if (ctx->lists[1].valid) k_sum_cnt<<<2 * ctx->num_sms, 256, 0, ctx->stream>>>(n, ctx->lists[1].cnt, d + 1);
-    if (ctx->grav.valid && ctx->grav.ng > 0)
+    if (ctx->grav.counts_valid && ctx->grav.ng > 0) {
         k_sum_grav_pairs<<<2 * ctx->num_sms, 256, 0, ctx->stream>>>(ctx->grav.ng, ctx->grav.group_cell, ctx->tree.count,
                                                                     ctx->grav.n_epj, ctx->grav.n_spj, d + 2);
+        k_sum_cnt<<<2 * ctx->num_sms, 256, 0, ctx->stream>>>(ctx->grav.ng, ctx->grav.n_epj, d + 4);
+        k_sum_cnt<<<2 * ctx->num_sms, 256, 0, ctx->stream>>>(ctx->grav.ng, ctx->grav.n_spj, d + 5);
+    }
     SPH_CUDA(ctx, cudaGetLastError());
-    unsigned long long h[4];
+    unsigned long long h[6];
     SPH_CUDA(ctx, cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
     SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     out[0] = (int64_t)h[0];
@@ -933,8 +1245,35 @@ int sph_work_counts(sph_ctx *ctx, int64_t out[8]) {
     out[2] = (int64_t)h[2];
     out[3] = ctx->tree.n_cell_host;
     out[4] = ctx->grav.ng;
-    out[5] = ctx->grav.tot_epj;
-    out[6] = ctx->grav.tot_spj;
+    out[5] = (int64_t)h[4];
+    out[6] = (int64_t)h[5];
     out[7] = (int64_t)h[3];
+    return SPH_OK;
+}
+
+// mixed-precision gravity with the walk fused into the force kernel
+int sph_gravity_fused(sph_ctx *ctx) {
+    SPH_TRY(sph_build_grav_groups(ctx));
+    GravLists &G = ctx->grav;
+    Tree &t = ctx->tree;
+    if (G.ng == 0) return SPH_OK;
+    if ((int64_t)t.n_cell_host * 2 > ctx->cap * 4) return sph_fail(ctx, SPH_ERR_CAPACITY, "cell pack scratch");
+    float4 *chp = (float4 *)ctx->F2, *clp = chp + t.n_cell_host;
+    k_pack_cells32<<<2 * ctx->num_sms, 256, 0, ctx->stream>>>(t.meta, t.com, ctx->cfg.G, 1.0, chp, clp);
+    ++ctx->launches;
+    SPH_CUDA(ctx, cudaMemsetAsync(t.meta + META_ERR, 0, sizeof(int), ctx->stream));
+    // xh.w holds m * mscale: G m = xh.w * (G / mscale)
+    const float gms = (float)(ctx->cfg.G / ctx->mscale);
+    k_grav_fused32<<<G.ng, GF_T, 0, ctx->stream>>>(G.group_cell, t.cinfo, t.com, t.rb, CF(SPH_X), CF(SPH_Y), CF(SPH_Z),
+                                                   ctx->xh, ctx->xl, CF(SPH_SMTH), chp, clp, gms, CF(SPH_GX),
+                                                   CF(SPH_GY), CF(SPH_GZ), CF(SPH_POT), G.n_epj, G.n_spj,
+                                                   t.meta + META_ERR);
+    ++ctx->launches;
+    SPH_CUDA(ctx, cudaGetLastError());
+    int *hs = (int *)ctx->host_scalars;
+    SPH_CUDA(ctx, cudaMemcpyAsync(hs, t.meta + META_ERR, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (hs[0] & ERR_GRAV_OVERFLOW) return sph_fail(ctx, SPH_ERR_CAPACITY, "gravity walk buffers overflowed");
+    G.counts_valid = true;
     return SPH_OK;
 }

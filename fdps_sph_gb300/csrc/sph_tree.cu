@@ -642,6 +642,7 @@ int sph_sort_and_build(sph_ctx *ctx) {
     if (hs[META_ERR] & ERR_CELL_OVERFLOW) return sph_fail(ctx, SPH_ERR_CAPACITY, "octree cell capacity exceeded");
     t.n_cell_host = hs[MAX_LEVELS];
     ctx->grav.valid = false;
+    ctx->grav.counts_valid = false;
     return sph_nbr_prepare(ctx);
 }
 

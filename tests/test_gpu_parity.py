@@ -259,3 +259,29 @@ def test_superset_repair_keeps_lists_exact(impact, frac):
     if frac < 0.5:
         assert c["walks_repair"] > 0
         assert c["units_walked"] < (c["walks_full"] + c["walks_repair"]) * c["units"]
+
+
+def test_fused_gravity_walk_matches_lists(impact):
+    """The mixed step walks the gravity tree inside the force kernel.  Its
+    per-group interaction counts must equal those of the list walk (which
+    the list tests pin to the oracle), and its forces those of the list-based
+    FP32 kernel up to summation order."""
+    F, ids, mats = impact
+    mats_l = tillotson_materials()
+    ctx = device_context(mats_l, precision=1)
+    ctx.upload(F, ids, mats)
+    ctx.prologue()                       # tree gravity through the fused walk
+    c_fused = ctx.counters()
+    Fa, ida, _ = ctx.download()
+    ctx.run_pass(5)                      # list walk + list-based kernel on the same tree
+    c_list = ctx.counters()
+    Fb, idb, _ = ctx.download()
+    for k in ("groups", "epj", "spj", "pairs_grav"):
+        assert c_fused[k] == c_list[k] and c_list[k] > 0, (k, c_fused[k], c_list[k])
+    from oracle import pyoracle as po
+    Fa, Fb = by_id(Fa, ida), by_id(Fb, idb)
+    f = po.FIELD
+    A = np.stack([Fa[f[c]] for c in ("gx", "gy", "gz")], 1)
+    B = np.stack([Fb[f[c]] for c in ("gx", "gy", "gz")], 1)
+    assert vec_err_rms(A, B) < 1e-6
+    assert rel_err(Fa[f["pot"]], Fb[f["pot"]], 1e-300) < 1e-6
