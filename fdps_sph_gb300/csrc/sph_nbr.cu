@@ -31,7 +31,8 @@ namespace sph {
 constexpr int UNIT = 32;
 constexpr float KAPPA = 1.15f;
 constexpr int NB_WARPS = 4;
-constexpr int NB_CAND = 512;
+constexpr int NB_CAND = 256;   // raw candidate indices per warp
+constexpr int NB_SURV = 64;    // culled candidates staged for the pair test
 constexpr int NB_STACK = 176;   // depth-first: at most 21 levels x 7 pending siblings + 8
 constexpr unsigned FULLM = 0xffffffffu;
 
@@ -121,9 +122,10 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
            int *maxcnt) {
     __shared__ int4 s_stack[NB_WARPS][NB_STACK];   // records (first_child, n_child, start, count) of cells to visit
     __shared__ int s_cand[NB_WARPS][NB_CAND];
-    __shared__ float4 s_ph[NB_WARPS][32];
-    __shared__ float4 s_pl[NB_WARPS][32];
-    __shared__ float s_h2[NB_WARPS][32];
+    // candidates that survived the per-particle cull: index, hi, lo (.w = (2.5 h_j)^2 rounded up)
+    __shared__ int s_sj[NB_WARPS][NB_SURV];
+    __shared__ float4 s_ph[NB_WARPS][NB_SURV];
+    __shared__ float4 s_pl[NB_WARPS][NB_SURV];
     __shared__ int s_wj[NB_WARPS][8][32];     // per-lane write buffers: 8 entries = one 32-byte sector
     __shared__ float s_wr[NB_WARPS][8][32];
     __shared__ float s_wm[NB_WARPS][8][32];
@@ -151,6 +153,8 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
     const float3 ghi = make_float3(__double2float_ru(hi[0]), __double2float_ru(hi[1]), __double2float_ru(hi[2]));
     const float k2 = KAPPA * KAPPA * 1.00390625f;          // kappa^2 (1 + 2^-8): generous, only a superset is needed
     const float Rg = __fmul_ru(KAPPA * 1.00390625f, __fsqrt_ru(R2));
+    const float Rg2 = __fmul_ru(Rg, Rg);
+    const unsigned lt = (1u << lane) - 1u;
     int4 *stack = s_stack[warp];
     int *cand = s_cand[warp];
     int count = 0, nc = 0;
@@ -176,34 +180,59 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
         }
     };
 
+    // Candidates are culled 32 at a time, each against the unit's box grown by its own reach:
+    // a lower bound of the distance (the point's hi / lo interval, rounded down) against an
+    // upper bound of max(Rg, kappa' 2.5 h_j), so no pair the test below would accept is
+    // dropped.  Survivors are staged with their coordinates and tested against every lane.
     auto flush = [&]() {
+        int ns = 0;
         for (int b = 0; b < nc; b += 32) {
-            const int k = b + lane;
-            int j = -1;
-            if (k < nc) {
-                j = cand[k];
-                s_ph[warp][lane] = xh[j];
-                s_pl[warp][lane] = xl[j];
-                s_h2[warp][lane] = H2f[j];
+            const int kk = b + lane;
+            bool keep = false;
+            int j = 0;
+            float4 qh = make_float4(0.f, 0.f, 0.f, 0.f), ql = qh;
+            if (kk < nc) {
+                j = cand[kk];
+                qh = xh[j];
+                ql = xl[j];
+                ql.w = H2f[j];
+                const float ex = fabsf(ql.x), ey = fabsf(ql.y), ez = fabsf(ql.z);
+                const float gx = fmaxf(0.0f, fmaxf(__fsub_rd(__fsub_rd(qh.x, ex), ghi.x),
+                                                   __fsub_rd(glo.x, __fadd_ru(qh.x, ex))));
+                const float gy = fmaxf(0.0f, fmaxf(__fsub_rd(__fsub_rd(qh.y, ey), ghi.y),
+                                                   __fsub_rd(glo.y, __fadd_ru(qh.y, ey))));
+                const float gz = fmaxf(0.0f, fmaxf(__fsub_rd(__fsub_rd(qh.z, ez), ghi.z),
+                                                   __fsub_rd(glo.z, __fadd_ru(qh.z, ez))));
+                const float g2 = __fadd_rd(__fadd_rd(__fmul_rd(gx, gx), __fmul_rd(gy, gy)), __fmul_rd(gz, gz));
+                keep = g2 < fmaxf(Rg2, __fmul_ru(k2, ql.w));
             }
+            const unsigned km = __ballot_sync(FULLM, keep);
+            if (keep) {
+                const int p = ns + __popc(km & lt);
+                s_sj[warp][p] = j;
+                s_ph[warp][p] = qh;
+                s_pl[warp][p] = ql;
+            }
+            ns += __popc(km);
             __syncwarp();
-            const int tc = min(32, nc - b);
-            for (int t = 0; t < tc; ++t) {
-                const float4 qh = s_ph[warp][t], ql = s_pl[warp][t];
-                const int jj = __shfl_sync(FULLM, j, t);
-                const float dx = df_sub(qh.x, ql.x, pih.x, pil.x);
-                const float dy = df_sub(qh.y, ql.y, pih.y, pil.y);
-                const float dz = df_sub(qh.z, ql.z, pih.z, pil.z);
-                const float r2 = dx * dx + dy * dy + dz * dz;
-                if (valid && r2 < k2 * fmaxf(H2i, s_h2[warp][t])) {
-                    s_wj[warp][count & 7][lane] = jj;
-                    s_wr[warp][count & 7][lane] = r2;
-                    s_wm[warp][count & 7][lane] = qh.w;
-                    ++count;
-                    if ((count & 7) == 0) put8();
+            if (ns >= 32 || b + 32 >= nc) {
+                for (int t = 0; t < ns; ++t) {
+                    const float4 ph = s_ph[warp][t], pl = s_pl[warp][t];
+                    const float dx = df_sub(ph.x, pl.x, pih.x, pil.x);
+                    const float dy = df_sub(ph.y, pl.y, pih.y, pil.y);
+                    const float dz = df_sub(ph.z, pl.z, pih.z, pil.z);
+                    const float r2 = dx * dx + dy * dy + dz * dz;
+                    if (valid && r2 < k2 * fmaxf(H2i, pl.w)) {
+                        s_wj[warp][count & 7][lane] = s_sj[warp][t];
+                        s_wr[warp][count & 7][lane] = r2;
+                        s_wm[warp][count & 7][lane] = ph.w;
+                        ++count;
+                        if ((count & 7) == 0) put8();
+                    }
                 }
+                ns = 0;
+                __syncwarp();
             }
-            __syncwarp();
         }
         nc = 0;
     };
@@ -478,10 +507,10 @@ k_density_sup32(int n, const int *__restrict__ sup, const float *__restrict__ su
     const float *rrow = sup_r2 + (int64_t)i * stride;
     const float *mrow = sup_m + (int64_t)i * stride;
     float acc_h = 0.0f, acc_l = 0.0f;
+    // the index row is read only for the rare entries whose FP32 distance is too close to the
+    // threshold to decide (exact_in's band); the stream is r^2 and m_j
     for (int k = 0; k < c; k += 8) {
-        const int4 j0 = reinterpret_cast<const int4 *>(row + k)[0], j1 = reinterpret_cast<const int4 *>(row + k)[1];
         const float4 r0 = reinterpret_cast<const float4 *>(rrow + k)[0], r1 = reinterpret_cast<const float4 *>(rrow + k)[1];
-        const int jj[8] = {j0.x, j0.y, j0.z, j0.w, j1.x, j1.y, j1.z, j1.w};
         const float rr[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
         const int m8 = min(8, c - k);
         const float4 m0 = reinterpret_cast<const float4 *>(mrow + k)[0], m1 = reinterpret_cast<const float4 *>(mrow + k)[1];
@@ -489,7 +518,11 @@ k_density_sup32(int n, const int *__restrict__ sup, const float *__restrict__ su
         float part = 0.0f;
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
-            if (u >= m8 || !exact_in(rr[u], H2i, jj[u], xi, yi, zi, H2, x, y, z, h, false)) continue;
+            if (u >= m8) continue;
+            bool in = rr[u] < H2i * (1.0f - 1.9073486328125e-06f);
+            if (!in && !(rr[u] > H2i * (1.0f + 1.9073486328125e-06f)))
+                in = exact_in(rr[u], H2i, row[k + u], xi, yi, zi, H2, x, y, z, h, false);
+            if (!in) continue;
             const float s_ = sqrtf(rr[u]) * invH;
             const float p = fmaxf(1.0f - s_, 0.0f);
             const float p2 = p * p, p4 = p2 * p2;
