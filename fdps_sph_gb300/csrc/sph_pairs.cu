@@ -632,12 +632,16 @@ k_grav_fused32(const int *__restrict__ group_cell, const int4 *__restrict__ cinf
     __shared__ int s_w[2][GF_W][3];            // per warp: leaf particles, far children, near children
     __shared__ double s_box[GF_W][6];
     __shared__ double s_rb[MAX_LEVELS];
+    __shared__ float s_rbf[MAX_LEVELS];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned below = (1u << lane) - 1u;
     const int4 gi = cinfo[group_cell[blockIdx.x]];
     const int s = gi.z, cnt_all = gi.w;
     const float4 c_h = xh[s], c_l = xl[s];     // group origin: its first particle
-    for (int l = tid; l < MAX_LEVELS; l += GF_T) s_rb[l] = rb[8 + l];
+    for (int l = tid; l < MAX_LEVELS; l += GF_T) {
+        s_rb[l] = rb[8 + l];
+        s_rbf[l] = (float)rb[8 + l];
+    }
     // bounding box of the whole group
     double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (int k = tid; k < cnt_all; k += GF_T) {
@@ -722,8 +726,7 @@ k_grav_fused32(const int *__restrict__ group_cell, const int4 *__restrict__ cinf
                     chc = ci.x + k;
                     const float4 qh = ch[chc], ql = cl[chc];
                     crec = cinfo[chc];
-                    const double rbd = s_rb[lev + 1];
-                    const float rbf = (float)rbd;
+                    const float rbf = s_rbf[lev + 1];
                     // FP32 distance from the box on coordinates relative to the group origin, with a
                     // bound on its error; inside the bound the FP64 test of the list walk decides
                     const float pr[3] = {df_diff(qh.x, ql.x, c_h.x, c_l.x), df_diff(qh.y, ql.y, c_h.y, c_l.y),
@@ -752,7 +755,7 @@ k_grav_fused32(const int *__restrict__ group_cell, const int4 *__restrict__ cinf
                         }
                         const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dd[0], dd[0]), __dmul_rn(dd[1], dd[1])),
                                                     __dmul_rn(dd[2], dd[2]));
-                        near = d2 <= rbd;
+                        near = d2 <= s_rb[lev + 1];
                     }
                     far = !near;
                 }

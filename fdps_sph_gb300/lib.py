@@ -10,7 +10,7 @@ import os
 
 import numpy as np
 
-from . import types as T
+from . import layouts as T
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libsph_gb300.so")

@@ -33,7 +33,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-from fdps_sph_gb300 import eos, ic, types as T  # noqa: E402
+from fdps_sph_gb300 import eos, ic, layouts as T  # noqa: E402
 from oracle import build_oracle, pyoracle as po  # noqa: E402
 
 REF_ROOT = build_oracle.REF_ROOT

@@ -6,7 +6,7 @@ import re
 
 import numpy as np
 
-from fdps_sph_gb300 import build, lib, types as T
+from fdps_sph_gb300 import build, lib, layouts as T
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 

@@ -9,7 +9,7 @@ the reference's -ffast-math reassociation: 1e-12 relative for positive sums
 import numpy as np
 import pytest
 
-from fdps_sph_gb300 import ic, types as T
+from fdps_sph_gb300 import ic, layouts as T
 from helpers import load_golden, rel_err, vec_rel_err
 
 pytestmark = pytest.mark.gpu

@@ -9,7 +9,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from fdps_sph_gb300 import build, ic, types as T
+from fdps_sph_gb300 import build, ic, layouts as T
 from helpers import load_golden, rel_err, vec_rel_err
 
 pytestmark = pytest.mark.gpu
