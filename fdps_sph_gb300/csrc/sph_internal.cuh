@@ -38,6 +38,25 @@ __device__ __forceinline__ void df_add(float &hi, float &lo, float a) {
     lo = __fadd_rn(lo, e);
 }
 
+// Hardware approximations for the FP32 pair arithmetic of the mixed kernels
+// (relative error about 2^-22, denormals flushed): one MUFU instruction each
+// instead of the IEEE-rounded sequences that sqrtf and '/' compile to.
+__device__ __forceinline__ float rsqrt_a(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rcp_a(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float sqrt_a(float x) {
+    float y;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 // Mixed-precision tail of a density pass (force.h:32-41): rho = max(floor,
 // sum_j m_j w_j x norm) and h = 1.2 (m / rho)^(1/3), in FP32.  dscale =
 // (1365/64) / (pi mscale) carries the kernel constant and the mass scale;

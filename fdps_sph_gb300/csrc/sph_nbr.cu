@@ -523,7 +523,7 @@ k_density_sup32(int n, const int *__restrict__ sup, const float *__restrict__ su
             if (!in && !(rr[u] > H2i * (1.0f + 1.9073486328125e-06f)))
                 in = exact_in(rr[u], H2i, row[k + u], xi, yi, zi, H2, x, y, z, h, false);
             if (!in) continue;
-            const float s_ = sqrtf(rr[u]) * invH;
+            const float s_ = sqrt_a(rr[u]) * invH;
             const float p = fmaxf(1.0f - s_, 0.0f);
             const float p2 = p * p, p4 = p2 * p2;
             part = fmaf(mj[u], (1.0f + s_ * (8.0f + s_ * (25.0f + s_ * 32.0f))) * (p4 * p4), part);

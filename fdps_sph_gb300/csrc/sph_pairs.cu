@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(PT) k_density32(int n, const float4 *__restric
         const float dx = df_diff(qh.x, ql.x, pih.x, pil.x);
         const float dy = df_diff(qh.y, ql.y, pih.y, pil.y);
         const float dz = df_diff(qh.z, ql.z, pih.z, pil.z);
-        const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+        const float r = sqrt_a(dx * dx + dy * dy + dz * dz);
         float w, g;
         wendland_poly_f(r * invH, w, g);
         part = fmaf(qh.w, w, part);
@@ -317,10 +317,10 @@ __device__ __forceinline__ void drvt_pair32(const float4 pih, const float4 pil, 
     const float wy = df_diff(vih.y, vil.y, uh.y, ul.y);
     const float wz = df_diff(vih.z, vil.z, uh.z, ul.z);
     const float rr2 = dx * dx + dy * dy + dz * dz;
-    const float r = sqrtf(rr2);
+    const float r = sqrt_a(rr2);
     float w, g;
     wendland_poly_f(r * invH, w, g);
-    const float gf = g / (r * Hf + ceps);
+    const float gf = g * rcp_a(r * Hf + ceps);
     const float mg = -qh.w * gf;
     P[0] = fmaf(mg, wx * dx + wy * dy + wz * dz, P[0]);
     P[1] = fmaf(mg, wy * dz - wz * dy, P[1]);
@@ -413,18 +413,18 @@ __device__ __forceinline__ void hydro_pair32(const float4 pih, const float4 pil,
     const float wy = df_diff(vih.y, vil.y, J.uh.y, J.ul.y);
     const float wz = df_diff(vih.z, vil.z, J.uh.z, J.ul.z);
     const float rr2 = dx * dx + dy * dy + dz * dz;
-    const float r = sqrtf(rr2);
+    const float r = sqrt_a(rr2);   // 0 for the particle itself
     const float dvdr = wx * dx + wy * dy + wz * dz;
-    const float w = (dvdr < 0.0f) ? dvdr / r : 0.0f;
+    const float w = (dvdr < 0.0f) ? dvdr * rcp_a(r) : 0.0f;   // dvdr < 0 implies r > 0
     const float vsig = Ai.y + J.A.y - 3.0f * w;
     vmax = fmaxf(vmax, vsig);
-    const float AV = -0.5f * vsig * w / (0.5f * (Bi.x + J.B.x)) * 0.5f * (Ai.w + J.A.w);
+    const float AV = -0.5f * vsig * w * rcp_a(0.5f * (Bi.x + J.B.x)) * 0.5f * (Ai.w + J.A.w);
     float wi_, gi_, wj_, gj_;
     wendland_poly_f(r * Bi.y, wi_, gi_);
     wendland_poly_f(r * J.B.y, wj_, gj_);
     const float nr = Bi.z * J.B.y;
-    const float gfi = gi_ / (r * Bi.z + Bi.w);
-    const float gfj = (nr * nr * nr) * gj_ / (r * J.B.z + J.B.w);
+    const float gfi = gi_ * rcp_a(r * Bi.z + Bi.w);
+    const float gfj = (nr * nr * nr) * gj_ * rcp_a(r * J.B.z + J.B.w);
     const float gws = 0.5f * (gfi * Ai.z + gfj * J.A.z);
     const float coef = J.qh.w * (Ai.x * gfi + J.A.x * gfj + AV * gws);
     P[0] = fmaf(-coef, dx, P[0]);
@@ -560,7 +560,7 @@ __global__ void __launch_bounds__(GT) k_grav32(const int *__restrict__ group_cel
                     const float4 q = tile[t];
                     const float dx = xi - q.x, dy = yi - q.y, dz = zi - q.z;
                     const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-                    const float ri = rsqrtf(r2);
+                    const float ri = rsqrt_a(r2);
                     const float mri = q.w * ri;
                     const float mr3 = mri * ri * ri;
                     P0 = fmaf(-mr3, dx, P0);
@@ -610,7 +610,7 @@ __device__ __forceinline__ void grav_acc(float px, float py, float pz, float e2,
                                          float &a2, float &a3) {
     const float dx = px - q.x, dy = py - q.y, dz = pz - q.z;
     const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, e2)));
-    const float ri = rsqrtf(r2);
+    const float ri = rsqrt_a(r2);
     const float mri = q.w * ri;
     const float mr3 = mri * ri * ri;
     a0 = fmaf(-mr3, dx, a0);
@@ -630,7 +630,6 @@ k_grav_fused32(const int *__restrict__ group_cell, const int4 *__restrict__ cinf
     __shared__ int s_s[GF_S];
     __shared__ float4 s_tile[GF_T];
     __shared__ int s_w[2][GF_W][3];            // per warp: leaf particles, far children, near children
-    __shared__ double s_box[GF_W][6];
     __shared__ double s_rb[MAX_LEVELS];
     __shared__ float s_rbf[MAX_LEVELS];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -643,30 +642,27 @@ k_grav_fused32(const int *__restrict__ group_cell, const int4 *__restrict__ cinf
         s_rbf[l] = (float)rb[8 + l];
     }
     // bounding box of the whole group
-    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (int k = tid; k < cnt_all; k += GF_T) {
-        const double p[3] = {x[s + k], y[s + k], z[s + k]};
-        for (int d = 0; d < 3; ++d) {
-            lo[d] = fmin(lo[d], p[d]);
-            hi[d] = fmax(hi[d], p[d]);
-        }
-    }
-    for (int d = 0; d < 3; ++d)
-        for (int o = 16; o > 0; o >>= 1) {
-            lo[d] = fmin(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
-            hi[d] = fmax(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
-        }
-    if (lane == 0)
-        for (int d = 0; d < 3; ++d) {
-            s_box[warp][d] = lo[d];
-            s_box[warp][3 + d] = hi[d];
-        }
-    __syncthreads();
+    // (one warp: the FP64 min / max and their shuffles are slow on this GPU's FP64 pipe)
     __shared__ double s_gbox[6];   // the group's box in FP64, for the exact opening test
-    if (tid < 6) {
-        double v = tid < 3 ? INFINITY : -INFINITY;
-        for (int w = 0; w < GF_W; ++w) v = tid < 3 ? fmin(v, s_box[w][tid]) : fmax(v, s_box[w][tid]);
-        s_gbox[tid] = v;
+    if (warp == 0) {
+        double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int k = lane; k < cnt_all; k += 32) {
+            const double p[3] = {x[s + k], y[s + k], z[s + k]};
+            for (int d = 0; d < 3; ++d) {
+                lo[d] = fmin(lo[d], p[d]);
+                hi[d] = fmax(hi[d], p[d]);
+            }
+        }
+        for (int d = 0; d < 3; ++d)
+            for (int o = 16; o > 0; o >>= 1) {
+                lo[d] = fmin(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
+                hi[d] = fmax(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+            }
+        if (lane == 0)
+            for (int d = 0; d < 3; ++d) {
+                s_gbox[d] = lo[d];
+                s_gbox[3 + d] = hi[d];
+            }
     }
     __syncthreads();
     // the box relative to the group origin, in FP32, for the fast opening test
