@@ -280,9 +280,10 @@ def main():
         "hydro": ("hydro", "fp32", FLOPS_PER_PAIR["hydro"] * w["pairs_sym"], 1),
         "grav_groups": ("grav_list", "hbm", 16 * w["cells"], 1),            # count / parent / flag per cell
         "gravity": ("grav", "fp32", FLOPS_PER_PAIR["grav"] * w["pairs_grav"], 1),   # walk fused in
-        "sort_tree": ("tree", "hbm", (36 + 8 * 24 + 2 * 32 * 8) * n, 1),
+        "sort_tree": ("sort_tree", "hbm", (36 + 8 * 24 + 2 * 32 * 8) * n, 1),
     }
     filt_ms = seg["drvt_list"] + seg["hydro_list"]
+    seg = dict(seg, sort_tree=seg["sort"] + seg["tree"] + seg["nbr_prep"])
     hbm = peaks.get("hbm_gbs")
     rows = {}
     for name, (sname, bound, work, launches_per_step) in kernels.items():

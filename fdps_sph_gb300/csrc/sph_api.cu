@@ -21,6 +21,14 @@ int sph_fail(sph_ctx *ctx, int code, const char *fmt, ...) {
     return code;
 }
 
+// records an event ending timing segment `seg` (seg < 0: the start mark)
+int time_mark(sph_ctx *ctx, int seg) {
+    if (!ctx->timing || ctx->n_ev >= 64) return SPH_OK;
+    ctx->mark_seg[ctx->n_ev] = seg;
+    SPH_CUDA(ctx, cudaEventRecord(ctx->ev[ctx->n_ev++], ctx->stream));
+    return SPH_OK;
+}
+
 namespace {
 
 __global__ void k_iota32(int32_t *a, int n) {
@@ -59,14 +67,6 @@ int upload_materials(sph_ctx *ctx) {
     return SPH_OK;
 }
 
-// records an event ending timing segment `seg` (seg < 0: the start mark)
-int time_mark(sph_ctx *ctx, int seg) {
-    if (!ctx->timing || ctx->n_ev >= 64) return SPH_OK;
-    ctx->mark_seg[ctx->n_ev] = seg;
-    SPH_CUDA(ctx, cudaEventRecord(ctx->ev[ctx->n_ev++], ctx->stream));
-    return SPH_OK;
-}
-
 // accumulates the elapsed time between consecutive marks into their segments
 int collect_timings(sph_ctx *ctx) {
     if (!ctx->timing || ctx->n_ev < 2) {
@@ -89,9 +89,9 @@ int collect_timings(sph_ctx *ctx) {
 
 // main.cpp:138-146 (positions fixed): sort + tree, density x n, EoS, derivative, hydro, gravity
 int compute_forces(sph_ctx *ctx) {
-    SPH_TRY(sph_sort_and_build(ctx));
+    SPH_TRY(sph_sort_and_build(ctx));   // marks SEG_SORT and SEG_TREE
     if (ctx->cfg.precision == SPH_PREC_MIXED) SPH_TRY(sph_pack_mixed(ctx));
-    SPH_TRY(time_mark(ctx, SEG_TREE));
+    SPH_TRY(time_mark(ctx, SEG_NBR_PREP));
     for (int it = 0; it < ctx->cfg.n_dens_iter; ++it) {
         if (ctx->cfg.precision == SPH_PREC_MIXED) {
             // the list-free pass makes the same neighbour decisions as the exact list

@@ -213,7 +213,10 @@ struct sph_ctx {
 // timing segments, in the order sph_get_timings reports them
 enum {
     SEG_KDP = 0, SEG_TREE, SEG_DENS_LIST, SEG_DENS, SEG_EOS, SEG_DRVT_LIST, SEG_DRVT, SEG_HYDRO_LIST, SEG_HYDRO,
-    SEG_GRAV_LIST, SEG_GRAV, SEG_FINAL, SEG_N
+    SEG_GRAV_LIST, SEG_GRAV, SEG_FINAL,
+    SEG_SORT,       // root box, keys, radix sort, permutation (before SEG_TREE: levels and moments)
+    SEG_NBR_PREP,   // walk units, cell reach, mixed-precision packs (after SEG_TREE)
+    SEG_N
 };
 
 // ---------------------------------------------------------------------------
@@ -243,6 +246,7 @@ int sph_nbr_refresh_h(sph_ctx *ctx);     // after h changed
 int sph_build_sph_lists(sph_ctx *ctx, int mode);
 int sph_density_from_superset(sph_ctx *ctx);
 int sph_nbr_ensure_superset(sph_ctx *ctx);   // mixed precision: density pass without an exact list
+int time_mark(sph_ctx *ctx, int seg);      // event at the end of a timed segment (when timing is on)
 int sph_build_grav_groups(sph_ctx *ctx);   // gravity i-groups (cells with <= n_group particles)
 int sph_build_grav_lists(sph_ctx *ctx);
 int sph_gravity_fused(sph_ctx *ctx);       // mixed precision: walk + force in one kernel

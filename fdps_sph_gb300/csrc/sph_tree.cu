@@ -240,7 +240,7 @@ __global__ void k_keys(const double *x, const double *y, const double *z, int n,
 // ---------------------------------------------------------------------------
 // LSD radix sort of (key, value), 8 passes of 8 bits.  Each pass: per-tile
 // digit histogram, one exclusive scan over (digit, tile), then a stable
-// in-tile sort by eight 1-bit splits in shared memory and a scatter.
+// in-tile ranking and a scatter.
 
 constexpr int RS_THREADS = 256;
 constexpr int RS_ITEMS = 8;
@@ -260,72 +260,77 @@ __global__ void k_rs_hist(const uint64_t *keys, int n, int shift, uint32_t *hist
     hist[threadIdx.x * nb + blockIdx.x] = h[threadIdx.x];
 }
 
+// Stable in-tile ranking by warp multisplit: each warp ranks its 256 keys
+// (eight rounds of 32 consecutive keys) with __match_any_sync against
+// per-warp digit counters; the counters of the eight warps are then turned
+// into per-digit offsets, the tile is reordered by digit in shared memory and
+// written out in runs of equal digit.
+constexpr int RS_WARPS = RS_THREADS / 32;
+constexpr int RS_WKEYS = RS_TILE / RS_WARPS;
+static_assert(RS_THREADS == 256, "one thread per digit in the offset step");
+
 __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint64_t *kin, const uint32_t *vin, uint64_t *kout,
                                                            uint32_t *vout, int n, int shift, const uint32_t *off,
                                                            int nb) {
     __shared__ uint64_t sk[RS_TILE];
     __shared__ uint32_t sv[RS_TILE];
-    __shared__ int dstart[256];
-    const int t = threadIdx.x;
+    __shared__ uint32_t wc[RS_WARPS][256];   // per-warp digit counts, then per-warp offsets within a digit
+    __shared__ uint32_t dstart[256];         // first tile position of each digit
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const unsigned lt = (1u << lane) - 1u;
     const int base = blockIdx.x * RS_TILE;
     const int cnt = min(RS_TILE, n - base);
-    // coalesced load into shared memory; out-of-range items carry digit 255 and sort last (stable)
-    for (int k = 0; k < RS_ITEMS; ++k) {
-        const int p = k * RS_THREADS + t;
-        if (p < cnt) {
-            sk[p] = kin[base + p];
-            sv[p] = vin[base + p];
-        } else {
-            sk[p] = ~0ULL;
-            sv[p] = 0xffffffffu;
-        }
-    }
+    for (int k = t; k < RS_WARPS * 256; k += RS_THREADS) (&wc[0][0])[k] = 0u;
     __syncthreads();
     uint64_t key[RS_ITEMS];
-    uint32_t val[RS_ITEMS];
-    for (int k = 0; k < RS_ITEMS; ++k) {
-        key[k] = sk[t * RS_ITEMS + k];
-        val[k] = sv[t * RS_ITEMS + k];
+    uint32_t val[RS_ITEMS], rk[RS_ITEMS];
+    int dg[RS_ITEMS];
+#pragma unroll
+    for (int r = 0; r < RS_ITEMS; ++r) {
+        const int p = w * RS_WKEYS + r * 32 + lane;
+        const bool ok = p < cnt;
+        key[r] = ok ? kin[base + p] : 0ULL;
+        val[r] = ok ? vin[base + p] : 0u;
+        const int d = ok ? (int)((key[r] >> shift) & 255u) : 256;   // 256: no item
+        dg[r] = d;
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        uint32_t b0 = 0;
+        if (ok) b0 = wc[w][d];
+        rk[r] = b0 + (uint32_t)__popc(peers & lt);
+        __syncwarp();
+        if (ok && lane == __ffs(peers) - 1) wc[w][d] = b0 + (uint32_t)__popc(peers);
+        __syncwarp();
     }
     __syncthreads();
-    for (int b = 0; b < 8; ++b) {
-        int zeros = 0;
-#pragma unroll
-        for (int k = 0; k < RS_ITEMS; ++k) zeros += !((key[k] >> (shift + b)) & 1u);
+    {
+        uint32_t c = 0;
+        for (int ww = 0; ww < RS_WARPS; ++ww) {
+            const uint32_t v = wc[ww][t];
+            wc[ww][t] = c;
+            c += v;
+        }
         int tot;
-        const int incl = block_incl_scan(zeros, &tot);
-        int zpos = incl - zeros;                       // zeros before me
-        int opos = tot + (t * RS_ITEMS - (incl - zeros));  // ones go after all zeros
-#pragma unroll
-        for (int k = 0; k < RS_ITEMS; ++k) {
-            const bool one = (key[k] >> (shift + b)) & 1u;
-            const int p = one ? opos++ : zpos++;
-            sk[p] = key[k];
-            sv[p] = val[k];
-        }
-        __syncthreads();
-#pragma unroll
-        for (int k = 0; k < RS_ITEMS; ++k) {
-            key[k] = sk[t * RS_ITEMS + k];
-            val[k] = sv[t * RS_ITEMS + k];
-        }
-        __syncthreads();
+        const int incl = block_incl_scan((int)c, &tot);
+        dstart[t] = (uint32_t)incl - c;
     }
-    // sk/sv hold the tile sorted by digit (stable); find each digit's first position
-    for (int k = 0; k < RS_ITEMS; ++k) {
-        const int p = k * RS_THREADS + t;
-        if (p < cnt) {
-            const int d = (int)((sk[p] >> shift) & 255u);
-            if (p == 0 || (int)((sk[p - 1] >> shift) & 255u) != d) dstart[d] = p;
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < RS_ITEMS; ++r) {
+        const int d = dg[r];
+        if (d < 256) {
+            const uint32_t p = dstart[d] + wc[w][d] + rk[r];
+            sk[p] = key[r];
+            sv[p] = val[r];
         }
     }
     __syncthreads();
     for (int k = 0; k < RS_ITEMS; ++k) {
         const int p = k * RS_THREADS + t;
         if (p < cnt) {
-            const int d = (int)((sk[p] >> shift) & 255u);
-            const uint32_t g = off[d * nb + blockIdx.x] + (uint32_t)(p - dstart[d]);
-            kout[g] = sk[p];
+            const uint64_t kk = sk[p];
+            const int d = (int)((kk >> shift) & 255u);
+            const uint32_t g = off[d * nb + blockIdx.x] + (uint32_t)p - dstart[d];
+            kout[g] = kk;
             vout[g] = sv[p];
         }
     }
@@ -371,16 +376,52 @@ __device__ __forceinline__ int digit_at(uint64_t key, int level) {
     return (int)((key >> (3 * (KEY_LEVELS - level))) & 7ULL);
 }
 
-__global__ void k_split(int l, int n_leaf, const uint64_t *keys, const int *meta, const int *start, const int *count,
-                        int *tmp_cnt, int *tmp_b) {
+// Children of the cells of level l: the first position of each octant
+// (digit l + 1) in the cell's sorted key range.  Cells of up to SPLIT_SMALL
+// particles are searched by one thread each (binary searches over a range
+// that sits in L1); larger cells, the top of the tree, by a warp each with
+// 32-way searches, so level 0 over all n particles takes a few dependent
+// loads per octant instead of log2 n.
+constexpr int SPLIT_SMALL = 256;
+
+__device__ __forceinline__ void split_store(int *tb, int s, int e, const int *bnd, int *nch) {
+    int prev = s, k = 0;
+    tb[0] = s;
+    for (int oct = 1; oct < 8; ++oct) {
+        tb[oct] = bnd[oct];
+        k += (bnd[oct] > prev);
+        prev = bnd[oct];
+    }
+    tb[8] = e;
+    *nch = k + (e > prev);
+}
+
+constexpr int SPLIT_QUEUE = 512;   // big cells handed from a block's threads to its warps
+
+__global__ void __launch_bounds__(256) k_split(int l, int n_leaf, const uint64_t *keys, const int *meta,
+                                               const int *start, const int *count, int *tmp_cnt, int *tmp_b) {
+    __shared__ int s_big[SPLIT_QUEUE];
+    __shared__ int s_nbig;
     const int L0 = meta[l], L1 = meta[l + 1];
-    for (int c = L0 + blockIdx.x * blockDim.x + threadIdx.x; c < L1; c += gridDim.x * blockDim.x) {
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+    if (threadIdx.x == 0) s_nbig = 0;
+    __syncthreads();
+    // small cells: a thread each; big cells go to the block's queue (or, if it is full, stay here)
+    for (int c = L0 + gt; c < L1; c += nt) {
         const int s = start[c], cnt = count[c];
+        if (cnt > SPLIT_SMALL && l < KEY_LEVELS) {
+            const int q = atomicAdd(&s_nbig, 1);
+            if (q < SPLIT_QUEUE) {
+                s_big[q] = c;
+                continue;
+            }
+        }
         int nch = 0;
         if (cnt > n_leaf && l < KEY_LEVELS) {
+            int bnd[8];
             int lo = s;
-            int prev = s;
-            for (int oct = 0; oct < 8; ++oct) {
+            for (int oct = 1; oct < 8; ++oct) {
                 int a = lo, len = s + cnt - lo;
                 while (len > 0) {
                     const int half = len >> 1;
@@ -391,15 +432,50 @@ __global__ void k_split(int l, int n_leaf, const uint64_t *keys, const int *meta
                         len = half;
                     }
                 }
-                tmp_b[(int64_t)(c - L0) * 9 + oct] = a;
-                if (oct > 0) nch += (a > prev);
-                prev = a;
+                bnd[oct] = a;
                 lo = a;
             }
-            tmp_b[(int64_t)(c - L0) * 9 + 8] = s + cnt;
-            nch += (s + cnt > prev);
+            split_store(tmp_b + (int64_t)(c - L0) * 9, s, s + cnt, bnd, &nch);
         }
         tmp_cnt[c - L0] = nch;
+    }
+    __syncthreads();
+    // big cells: a warp each, 32-way searches
+    const int nbig = min(s_nbig, SPLIT_QUEUE);
+    for (int k = warp; k < nbig; k += nwb) {
+        const int c = s_big[k];
+        const int s = start[c], e = s + count[c];
+        int bnd[8];
+        int lo = s;
+        for (int oct = 1; oct < 8; ++oct) {
+            // first position in [lo, e) with digit >= oct; the answer lies in [a, b]
+            int a = lo, b = e;
+            while (b - a > 32) {
+                const int step = (b - a + 31) >> 5;
+                const int p = a + lane * step;
+                const bool below = p < b && digit_at(keys[p], l + 1) < oct;
+                const int kb = __popc(__ballot_sync(0xffffffffu, below));
+                if (kb == 0) {
+                    b = a;
+                } else {
+                    const int na = a + (kb - 1) * step + 1;
+                    b = min(b, a + kb * step);
+                    a = na;
+                }
+            }
+            if (b > a) {
+                const int p = a + lane;
+                const bool below = p < b && digit_at(keys[p], l + 1) < oct;
+                a += __popc(__ballot_sync(0xffffffffu, below));
+            }
+            bnd[oct] = a;
+            lo = a;
+        }
+        if (lane == 0) {
+            int nch = 0;
+            split_store(tmp_b + (int64_t)(c - L0) * 9, s, e, bnd, &nch);
+            tmp_cnt[c - L0] = nch;
+        }
     }
 }
 
@@ -616,6 +692,7 @@ int sph_sort_and_build(sph_ctx *ctx) {
     std::swap(ctx->slot, ctx->slot2);
     std::swap(ctx->mat, ctx->mat2);
     SPH_CUDA(ctx, cudaMemcpyAsync(ctx->keys, ctx->sort.k0, sizeof(uint64_t) * n, cudaMemcpyDeviceToDevice, st));
+    SPH_TRY(time_mark(ctx, SEG_SORT));
     x = FLD(ctx->F, SPH_X, cap);
     y = FLD(ctx->F, SPH_Y, cap);
     z = FLD(ctx->F, SPH_Z, cap);
@@ -643,6 +720,7 @@ int sph_sort_and_build(sph_ctx *ctx) {
     t.n_cell_host = hs[MAX_LEVELS];
     ctx->grav.valid = false;
     ctx->grav.counts_valid = false;
+    SPH_TRY(time_mark(ctx, SEG_TREE));
     return sph_nbr_prepare(ctx);
 }
 

@@ -41,7 +41,7 @@ EXPORTS = [
 ]
 NOALLOC_MAX_N = 131072
 SEGMENTS = ["kdp", "tree", "dens_list", "dens", "eos", "drvt_list", "drvt", "hydro_list", "hydro", "grav_list",
-            "grav", "final"]
+            "grav", "final", "sort", "nbr_prep"]
 
 
 class SphError(RuntimeError):

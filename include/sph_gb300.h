@@ -186,9 +186,11 @@ int sph_get_grav_list(sph_ctx *ctx, int64_t g, int64_t *n_group, int32_t *epj, i
                       int32_t *spj_level, int32_t *spj_start, int64_t cap_spj, int64_t *n_spj,
                       int32_t *group_start, int32_t *group_count);
 /* Device time (CUDA events on the context's stream) accumulated per segment
- * since the last reset, in this order: kick-drift-predict, sort + tree,
- * density lists, density kernels, EoS, derivative list, derivative kernel,
- * hydro list, hydro kernel, gravity lists, gravity kernel, final kick + dt.
+ * since the last reset, in this order: kick-drift-predict, octree levels and
+ * moments, density lists, density kernels, EoS, derivative list, derivative
+ * kernel, hydro list, hydro kernel, gravity groups (and lists on the FP64
+ * path), gravity kernel, final kick + dt, key sort + permutation, neighbour
+ * walk preparation.
  * cap = -1 switches timing on (and resets), -2 switches it off, -3 resets. */
 int sph_get_timings(sph_ctx *ctx, double *ms, int cap, int *n);
 /* sph_step bracketed by CUDA events on the context's stream; device_ms = elapsed. */
