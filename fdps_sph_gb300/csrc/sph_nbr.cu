@@ -31,7 +31,7 @@ namespace sph {
 constexpr int UNIT = 32;
 constexpr float KAPPA = 1.06f;   // measured at 1M: 1.15 -> 13.7 ms, 1.10 -> 12.9, 1.06 -> 12.6, 1.03 -> 13.0 (repairs)
 constexpr int NB_WARPS = 4;
-constexpr int NB_CAND = 256;   // raw candidate indices per warp
+constexpr int NB_CAND = 128;   // raw candidate indices per warp
 constexpr int NB_SURV = 64;    // culled candidates staged for the pair test
 constexpr int NB_STACK = 176;   // depth-first: at most 21 levels x 7 pending siblings + 8
 constexpr unsigned FULLM = 0xffffffffu;
@@ -113,20 +113,22 @@ __device__ __forceinline__ float gap2_rd(float4 a_lo, float4 a_hi, float3 glo, f
     return __fadd_rd(__fadd_rd(__fmul_rd(gx, gx), __fmul_rd(gy, gy)), __fmul_rd(gz, gz));
 }
 
-__global__ void __launch_bounds__(NB_WARPS * 32, 6)
+__global__ void __launch_bounds__(NB_WARPS * 32, 7)
 k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ uidx, const double *__restrict__ x,
            const double *__restrict__ y, const double *__restrict__ z, const double *__restrict__ h,
            double *__restrict__ hsup, const float4 *__restrict__ xh,
            const float4 *__restrict__ xl, const float *__restrict__ H2f, WalkTree T, int *__restrict__ sup,
            float *__restrict__ sup_r2, float *__restrict__ sup_m, int *__restrict__ cnt, int K, int64_t stride, int *err,
            int *maxcnt) {
-    __shared__ int4 s_stack[NB_WARPS][NB_STACK];   // records (first_child, n_child, start, count) of cells to visit
+    // cells to visit: (first_child, -n_child) for an internal cell, (start, count) for a leaf
+    __shared__ int2 s_stack[NB_WARPS][NB_STACK];
     __shared__ int s_cand[NB_WARPS][NB_CAND];
     // candidates that survived the per-particle cull: index, hi, lo (.w = (2.5 h_j)^2 rounded up)
     __shared__ int s_sj[NB_WARPS][NB_SURV];
     __shared__ float4 s_ph[NB_WARPS][NB_SURV];
     __shared__ float4 s_pl[NB_WARPS][NB_SURV];
-    __shared__ int s_wj[NB_WARPS][8][32];     // per-lane write buffers: 8 entries = one 32-byte sector
+    // per-lane write buffers: 8 entries = one 32-byte sector
+    __shared__ int s_wj[NB_WARPS][8][32];
     __shared__ float s_wr[NB_WARPS][8][32];
     __shared__ float s_wm[NB_WARPS][8][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -155,7 +157,7 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
     const float Rg = __fmul_ru(KAPPA * 1.00390625f, __fsqrt_ru(R2));
     const float Rg2 = __fmul_ru(Rg, Rg);
     const unsigned lt = (1u << lane) - 1u;
-    int4 *stack = s_stack[warp];
+    int2 *stack = s_stack[warp];
     int *cand = s_cand[warp];
     int count = 0, nc = 0;
     int *row = sup + (int64_t)i * stride;
@@ -242,17 +244,19 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
         const float4 a = T.blo[0], b = T.bhi[0];
         const float R = fmaxf(Rg, __fmul_ru(2.5f * KAPPA * 1.00390625f, b.w));
         if (gap2_rd(a, b, glo, ghi) < __fmul_ru(R, R)) {
-            if (lane == 0) stack[0] = T.cinfo[0];
+            if (lane == 0) {
+                const int4 r = T.cinfo[0];
+                stack[0] = r.y == 0 ? make_int2(r.z, r.w) : make_int2(r.x, -r.y);
+            }
             sp = 1;
         }
         __syncwarp();
     }
     while (sp > 0) {
-        const int4 ci = stack[--sp];
+        const int2 ci = stack[--sp];
         __syncwarp();
-        const int nch = ci.y;
-        if (nch == 0) {
-            const int s = ci.z, ct = ci.w;
+        if (ci.y > 0) {   // a leaf
+            const int s = ci.x, ct = ci.y;
             for (int b0 = 0; b0 < ct; b0 += 32) {
                 if (nc + 32 > NB_CAND) flush();
                 if (b0 + lane < ct) cand[nc + lane] = s + b0 + lane;
@@ -260,12 +264,13 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
                 __syncwarp();
             }
         } else {
-            const int f = ci.x;
+            const int f = ci.x, nch = -ci.y;
             bool ok = false;
-            int4 chi = make_int4(0, 0, 0, 0);
+            int2 chi = make_int2(0, 0);
             if (lane < nch) {
                 const float4 a = T.blo[f + lane], b = T.bhi[f + lane];
-                chi = T.cinfo[f + lane];   // independent of the box loads: one round trip
+                const int4 r = T.cinfo[f + lane];   // independent of the box loads: one round trip
+                chi = r.y == 0 ? make_int2(r.z, r.w) : make_int2(r.x, -r.y);
                 const float R = fmaxf(Rg, __fmul_ru(2.5f * KAPPA * 1.00390625f, b.w));
                 ok = gap2_rd(a, b, glo, ghi) < __fmul_ru(R, R);
             }
