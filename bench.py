@@ -273,7 +273,7 @@ def main():
     seg, st = mixed["seg"], a.steps
     entries = w.get("superset_entries", 0)
     kernels = {
-        "sup_walk": ("dens_list", "hbm", 8 * entries + 68 * n, 1),          # rows written + particle reads
+        "sup_walk": ("dens_list", "hbm", 12 * entries + 68 * n, 1),         # rows (idx, r2, m) + particle reads
         "density": ("dens", "fp32", FLOPS_PER_PAIR["dens"] * w["pairs_gather"], 4),
         "filters": (None, "hbm", 2 * (8 * entries + 4 * w["pairs_gather"]) // 2, 2),
         "derivative": ("drvt", "fp32", FLOPS_PER_PAIR["drvt"] * w["pairs_gather"], 1),
