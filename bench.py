@@ -137,12 +137,23 @@ def run_gpu(F, ids, mats, materials, precision, steps, warmup, device):
         ctx.step(1)
     ctx.enable_timing(True)
     c0 = ctx.counters()["launches"]
+    d0 = ctx.diagnostics()
     with ClockSampler(device) as clk:
         ms = ctx.step_timed(steps)
+    d1 = ctx.diagnostics()
     c1 = ctx.counters()
     seg = ctx.timings()
     ctx.enable_timing(False)
-    return ctx, ms, seg, c1, c1["launches"] - c0, clk.summary()
+    return ctx, ms, seg, c1, c1["launches"] - c0, clk.summary(), drift(d0, d1, steps)
+
+
+def drift(d0, d1, steps):
+    """relative change per step of the total energy and the angular momentum over the timed steps
+    (sph_diagnostics: E = sum m (u + v^2/2 + pot/2), L = sum m x cross v, both in FP64)"""
+    import numpy as np
+    e = abs(d1[0] - d0[0]) / max(abs(d0[0]), 1e-300) / steps
+    lv = float(np.linalg.norm(d1[4:7] - d0[4:7]) / max(np.linalg.norm(d0[4:7]), 1e-300)) / steps
+    return {"energy_rel_per_step": e, "angmom_rel_per_step": lv}
 
 
 def run_e2e(ctx, F, ids, mats, steps):
@@ -243,9 +254,9 @@ def main():
     results = {}
     precisions = ["mixed"] if a.no_fp64 else ["mixed", "fp64"]
     for prec in precisions:
-        ctx, ms, seg, cnt, launches, clocks = run_gpu(F, ids, mats, materials, prec, a.steps, a.warmup, device)
+        ctx, ms, seg, cnt, launches, clocks, dr = run_gpu(F, ids, mats, materials, prec, a.steps, a.warmup, device)
         e2e = run_e2e(ctx, F, ids, mats, a.e2e_steps) if prec == "mixed" else None
-        results[prec] = dict(ms=ms, seg=seg, cnt=cnt, launches=launches, clocks=clocks, e2e=e2e)
+        results[prec] = dict(ms=ms, seg=seg, cnt=cnt, launches=launches, clocks=clocks, e2e=e2e, drift=dr)
         ctx.close()
 
     if dist is not None:
@@ -324,6 +335,8 @@ def main():
         "work": {k: v for k, v in mixed["cnt"].items() if k != "launches"},
         "peaks": {"fp32_tflops_measured": peak32, "fp64_tflops_measured": peak64, "hbm_gbs": hbm},
     }
+    out["drift"] = {"mixed": mixed["drift"], "steps": a.steps,
+                    "note": "relative change per timed step of E and |L| (FP64 diagnostics)"}
     if mixed["e2e"] is not None:
         el, h2d, d2h = mixed["e2e"]
         out["e2e"] = {"value": world * n * a.e2e_steps / el, "unit": "particle-steps/s",
@@ -341,6 +354,7 @@ def main():
                        "roofline": {"bound": "fp64", "kernel": dom64, "achieved": ach64, "peak": peak64,
                                     "unit": "TFLOP/s", "frac": ach64 / peak64 if peak64 else None},
                        "clocks": f["clocks"], "gpu_launches": int(f["launches"])}
+        out["drift"]["fp64"] = f["drift"]
     if not a.no_cpu:
         v_cpu, el_cpu, cores = cpu_sample(a.cpu_n, 1)
         out["cpu_baseline"] = {"value": v_cpu, "unit": "particle-steps/s", "cores": cores, "kind": "port",

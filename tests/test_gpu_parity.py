@@ -285,3 +285,25 @@ def test_fused_gravity_walk_matches_lists(impact):
     B = np.stack([Fb[f[c]] for c in ("gx", "gy", "gz")], 1)
     assert vec_err_rms(A, B) < 1e-6
     assert rel_err(Fa[f["pot"]], Fb[f["pot"]], 1e-300) < 1e-6
+
+
+def test_mixed_energy_and_angular_momentum_drift(impact):
+    """Over 20 steps the mixed path's energy and angular-momentum drift stay
+    at the level of the FP64 path's (which is set by the time integration)."""
+    F, ids, mats = impact
+    mats_l = tillotson_materials()
+    drift = {}
+    for prec in (0, 1):
+        ctx = device_context(mats_l, precision=prec)
+        ctx.upload(F, ids, mats)
+        ctx.prologue()
+        d0 = ctx.diagnostics()
+        ctx.step(20)
+        d1 = ctx.diagnostics()
+        drift[prec] = (abs(d1[0] - d0[0]) / abs(d0[0]),
+                       float(np.linalg.norm(d1[4:7] - d0[4:7]) / np.linalg.norm(d0[4:7])))
+    print("drift over 20 steps (energy, angular momentum): fp64", drift[0], "mixed", drift[1])
+    e64, l64 = drift[0]
+    e32, l32 = drift[1]
+    assert e32 <= 1.1 * e64 + 1e-9, (e32, e64)
+    assert l32 <= 1.1 * l64 + 1e-9, (l32, l64)
