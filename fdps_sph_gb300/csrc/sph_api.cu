@@ -36,14 +36,42 @@ __global__ void k_iota32(int32_t *a, int n) {
     if (i < n) a[i] = i;
 }
 
-__global__ void k_unpermute(const double *F, double *F2, int64_t cap, int n, const int32_t *slot, const int64_t *id,
-                            int64_t *id2, const int32_t *mat, int32_t *mat2) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const int dst = slot[k];
+// back to upload order: particle k of run r goes to base + slot[k], base = the run's first particle
+// (all runs) or 0 (one run, k in [k0, k0 + n))
+__global__ void k_unpermute(const double *F, double *F2, int64_t cap, int k0, int n, const int32_t *slot,
+                            const int *prun, const int4 *info, const int64_t *id, int64_t *id2, const int32_t *mat,
+                            int32_t *mat2) {
+    const int k = k0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= k0 + n) return;
+    const int dst = (info ? info[prun[k]].x : 0) + slot[k];
     for (int f = 0; f < SPH_NFIELD; ++f) F2[(int64_t)f * cap + dst] = F[(int64_t)f * cap + k];
     id2[dst] = id[k];
     mat2[dst] = mat[k];
+}
+
+__global__ void k_fill32(int32_t *a, int n, int v) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = v;
+}
+
+__global__ void k_iota64(int64_t *a, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = i;
+}
+
+// drops the particles [off, off + cnt) of run r; later runs move down and are renumbered
+__global__ void k_remove_run(const double *F, double *F2, int64_t cap, int n_new, int off, int cnt, int r,
+                             const int64_t *id, int64_t *id2, const int32_t *slot, int32_t *slot2, const int32_t *mat,
+                             int32_t *mat2, const int *prun, int *prun2) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_new) return;
+    const int src = k < off ? k : k + cnt;
+    for (int f = 0; f < SPH_NFIELD; ++f) F2[(int64_t)f * cap + k] = F[(int64_t)f * cap + src];
+    id2[k] = id[src];
+    slot2[k] = slot[src];
+    mat2[k] = mat[src];
+    const int q = prun[src];
+    prun2[k] = q > r ? q - 1 : q;
 }
 
 template <class T>
@@ -132,6 +160,162 @@ int compute_forces(sph_ctx *ctx) {
 
 }  // namespace
 
+// offsets, tiles and device tables of the runs (after the run set changed)
+int sph_runs_layout(sph_ctx *ctx) {
+    Runs &R = ctx->runs;
+    R.off.assign(R.R, 0);
+    std::vector<int4> info(R.R), tiles;
+    int64_t o = 0;
+    int T = 0;
+    for (int r = 0; r < R.R; ++r) {
+        R.off[r] = o;
+        const int nt = (int)((R.n[r] + RUN_TILE - 1) / RUN_TILE);
+        info[r] = make_int4((int)o, (int)R.n[r], T, nt);
+        for (int k = 0; k < nt; ++k)
+            tiles.push_back(make_int4((int)(o + (int64_t)k * RUN_TILE), (int)std::min<int64_t>(RUN_TILE, R.n[r] - (int64_t)k * RUN_TILE),
+                                      256 * T + k, nt));
+        o += R.n[r];
+        T += nt;
+    }
+    R.T = T;
+    if (R.R > R.cap_R) {
+        const int c = std::max(16, std::max(R.R, 2 * R.cap_R));
+        SPH_TRY(dalloc(ctx, &R.info, c));
+        SPH_TRY(dalloc(ctx, &R.dt_dev, c));
+        SPH_TRY(dalloc(ctx, &R.out, 8 * (int64_t)c));
+        SPH_TRY(dalloc(ctx, &R.damp, c));
+        R.cap_R = c;
+    }
+    if (T > R.cap_T) {
+        const int c = std::max(64, std::max(T, R.cap_T + R.cap_T / 2));
+        SPH_TRY(dalloc(ctx, &R.tiles, c));
+        SPH_TRY(dalloc(ctx, &R.part, 8 * (int64_t)c));
+        R.cap_T = c;
+    }
+    if (R.R > 0) {
+        SPH_CUDA(ctx, cudaMemcpyAsync(R.info, info.data(), sizeof(int4) * R.R, cudaMemcpyHostToDevice, ctx->stream));
+        SPH_CUDA(ctx, cudaMemcpyAsync(R.dt_dev, R.dt.data(), sizeof(double) * R.R, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    if (T > 0)
+        SPH_CUDA(ctx, cudaMemcpyAsync(R.tiles, tiles.data(), sizeof(int4) * T, cudaMemcpyHostToDevice, ctx->stream));
+    SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));   // the host vectors are the copies' sources
+    // derived per-step structures are rebuilt by the next step
+    ctx->sup.valid = false;
+    ctx->lists[0].valid = ctx->lists[1].valid = false;
+    ctx->grav.valid = ctx->grav.counts_valid = false;
+    return SPH_OK;
+}
+
+namespace {
+
+// grows the particle arrays to hold `need`, keeping particles [0, n)
+int grow_particles(sph_ctx *ctx, int64_t need) {
+    if (need <= ctx->cap) return SPH_OK;
+    const int64_t c = std::max<int64_t>(need, ctx->cap + ctx->cap / 2);
+    const int64_t n = ctx->n;
+    double *F = nullptr;
+    int64_t *id = nullptr;
+    int32_t *slot = nullptr, *mat = nullptr;
+    int *prun = nullptr;
+    SPH_TRY(dalloc(ctx, &F, (int64_t)SPH_NFIELD * c));
+    SPH_TRY(dalloc(ctx, &id, c));
+    SPH_TRY(dalloc(ctx, &slot, c));
+    SPH_TRY(dalloc(ctx, &mat, c));
+    SPH_TRY(dalloc(ctx, &prun, c));
+    if (n > 0) {
+        SPH_CUDA(ctx, cudaMemcpy2DAsync(F, sizeof(double) * c, ctx->F, sizeof(double) * ctx->cap, sizeof(double) * n,
+                                        SPH_NFIELD, cudaMemcpyDeviceToDevice, ctx->stream));
+        SPH_CUDA(ctx, cudaMemcpyAsync(id, ctx->id, sizeof(int64_t) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+        SPH_CUDA(ctx, cudaMemcpyAsync(slot, ctx->slot, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+        SPH_CUDA(ctx, cudaMemcpyAsync(mat, ctx->mat, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+        SPH_CUDA(ctx, cudaMemcpyAsync(prun, ctx->runs.prun, sizeof(int) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+        SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    for (void *p : {(void *)ctx->F, (void *)ctx->id, (void *)ctx->slot, (void *)ctx->mat, (void *)ctx->runs.prun})
+        if (p) cudaFree(p);
+    ctx->F = F;
+    ctx->id = id;
+    ctx->slot = slot;
+    ctx->mat = mat;
+    ctx->runs.prun = prun;
+    SPH_TRY(dalloc(ctx, &ctx->F2, (int64_t)SPH_NFIELD * c));
+    SPH_TRY(dalloc(ctx, &ctx->id2, c));
+    SPH_TRY(dalloc(ctx, &ctx->slot2, c));
+    SPH_TRY(dalloc(ctx, &ctx->mat2, c));
+    SPH_TRY(dalloc(ctx, &ctx->runs.prun2, c));
+    SPH_TRY(dalloc(ctx, &ctx->keys, c));
+    for (float4 **p : {&ctx->xh, &ctx->xl, &ctx->vhf, &ctx->vlf})
+        if (*p) {
+            cudaFree(*p);
+            *p = nullptr;
+        }
+    ctx->cap = c;
+    return SPH_OK;
+}
+
+int find_run(sph_ctx *ctx, int64_t handle) {
+    for (int r = 0; r < ctx->runs.R; ++r)
+        if (ctx->runs.handle[r] == handle) return r;
+    return -1;
+}
+
+// appends a block of particles as a new run
+int append_run(sph_ctx *ctx, int64_t n, const double *fields, int64_t ld, const int64_t *id, const int32_t *material,
+               double time, double dt, int flags, int64_t *handle) {
+    if (n < 1 || n > 0x3fffffff || !fields || ld < n || ctx->n + n > 0x3fffffff)
+        return sph_fail(ctx, SPH_ERR_ARG, "bad particle block (n=%lld)", (long long)n);
+    if (material) {
+        for (int64_t i = 0; i < n; ++i) {
+            const int m = material[i];
+            if (m < 0 || m >= MAX_MATERIALS || ctx->mats_host[m].kind < 0)
+                return sph_fail(ctx, SPH_ERR_ARG, "particle %lld uses unset material %d", (long long)i, m);
+        }
+    } else if (ctx->mats_host[0].kind < 0) {
+        return sph_fail(ctx, SPH_ERR_ARG, "material 0 is not set");
+    }
+    double msum = 0.0;
+    for (int64_t i = 0; i < n; ++i) {
+        const double mi = fields[(int64_t)SPH_MASS * ld + i];
+        if (!(mi > 0.0) || !std::isfinite(mi)) return sph_fail(ctx, SPH_ERR_NONFINITE, "particle %lld has mass %g", (long long)i, mi);
+        msum += mi;
+    }
+    const int64_t o = ctx->n;
+    SPH_TRY(grow_particles(ctx, o + n));
+    SPH_CUDA(ctx, cudaMemcpy2DAsync(ctx->F + o, sizeof(double) * ctx->cap, fields, sizeof(double) * ld,
+                                    sizeof(double) * n, SPH_NFIELD, cudaMemcpyHostToDevice, ctx->stream));
+    if (id) {
+        SPH_CUDA(ctx, cudaMemcpyAsync(ctx->id + o, id, sizeof(int64_t) * n, cudaMemcpyHostToDevice, ctx->stream));
+    } else {
+        k_iota64<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(ctx->id + o, (int)n); ++ctx->launches;
+    }
+    if (material) {
+        SPH_CUDA(ctx, cudaMemcpyAsync(ctx->mat + o, material, sizeof(int32_t) * n, cudaMemcpyHostToDevice, ctx->stream));
+    } else {
+        SPH_CUDA(ctx, cudaMemsetAsync(ctx->mat + o, 0, sizeof(int32_t) * n, ctx->stream));
+    }
+    Runs &R = ctx->runs;
+    k_iota32<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(ctx->slot + o, (int)n); ++ctx->launches;
+    k_fill32<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(R.prun + o, (int)n, R.R); ++ctx->launches;
+    SPH_CUDA(ctx, cudaGetLastError());
+    // power of two close to 1 / mean mass (exact rescaling of the FP32 mass copies), fixed by the first run
+    if (o == 0) ctx->mscale = std::ldexp(1.0, -(int)std::lround(std::log2(msum / (double)n)));
+    if (flags & SPH_UPLOAD_INIT_SMTH) SPH_TRY(sph_init_smth(ctx, o, n));
+    SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const bool forces = (flags & SPH_UPLOAD_FORCES_VALID) && dt > 0.0;
+    R.n.push_back(n);
+    R.time.push_back(time);
+    R.dt.push_back(forces ? dt : 0.0);
+    R.steps.push_back(0);
+    R.handle.push_back(R.next_handle++);
+    R.fresh.push_back(forces ? 0 : 1);
+    R.R += 1;
+    ctx->n = o + n;
+    if (handle) *handle = R.handle.back();
+    return sph_runs_layout(ctx);
+}
+
+}  // namespace
+
 extern "C" {
 
 void sph_config_default(sph_config *cfg) {
@@ -214,7 +398,9 @@ int sph_ctx_destroy(sph_ctx *ctx) {
                     ctx->grav.off_spj, ctx->grav.epj, ctx->grav.spj, ctx->scan.part, ctx->scan.total,
                     ctx->sup.nbr, ctx->sup.cnt, ctx->sup.hsup, ctx->sup.pxh, ctx->sup.pxl, ctx->sup.H2f,
                     ctx->sup.units, ctx->tree.cinfo, ctx->sup.r2, ctx->sup.m, ctx->sup.vR, ctx->sup.cvR,
-                    ctx->sup.umark, ctx->sup.uoff, ctx->sup.uidx};
+                    ctx->sup.umark, ctx->sup.uoff, ctx->sup.uidx, ctx->runs.prun, ctx->runs.prun2,
+                    ctx->runs.tiles, ctx->runs.info, ctx->runs.dt_dev, ctx->runs.part, ctx->runs.out,
+                    ctx->runs.damp};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (void *p : ctx->table_allocs) cudaFree(p);
@@ -318,71 +504,120 @@ int sph_set_eos_tillotson(sph_ctx *ctx, int material, const double par[10]) {
 
 int sph_upload(sph_ctx *ctx, int64_t n, const double *fields, int64_t ld, const int64_t *id, const int32_t *material,
                double time, double dt, int flags) {
-    const int init_smth = flags & SPH_UPLOAD_INIT_SMTH;
     if (!ctx) return SPH_ERR_ARG;
-    if (n < 1 || n > 0x3fffffff || !fields || ld < n) return sph_fail(ctx, SPH_ERR_ARG, "bad particle block (n=%lld)", (long long)n);
     cudaSetDevice(ctx->device);
-    if (material) {
-        for (int64_t i = 0; i < n; ++i) {
-            const int m = material[i];
-            if (m < 0 || m >= MAX_MATERIALS || ctx->mats_host[m].kind < 0)
-                return sph_fail(ctx, SPH_ERR_ARG, "particle %lld uses unset material %d", (long long)i, m);
-        }
-    } else if (ctx->mats_host[0].kind < 0) {
-        return sph_fail(ctx, SPH_ERR_ARG, "material 0 is not set");
-    }
-    double msum = 0.0;
-    for (int64_t i = 0; i < n; ++i) {
-        const double mi = fields[(int64_t)SPH_MASS * ld + i];
-        if (!(mi > 0.0) || !std::isfinite(mi)) return sph_fail(ctx, SPH_ERR_NONFINITE, "particle %lld has mass %g", (long long)i, mi);
-        msum += mi;
-    }
-    if (n > ctx->cap) {
-        const int64_t c = n;
-        SPH_TRY(dalloc(ctx, &ctx->F, (int64_t)SPH_NFIELD * c));
-        SPH_TRY(dalloc(ctx, &ctx->F2, (int64_t)SPH_NFIELD * c));
-        SPH_TRY(dalloc(ctx, &ctx->id, c));
-        SPH_TRY(dalloc(ctx, &ctx->id2, c));
-        SPH_TRY(dalloc(ctx, &ctx->slot, c));
-        SPH_TRY(dalloc(ctx, &ctx->slot2, c));
-        SPH_TRY(dalloc(ctx, &ctx->mat, c));
-        SPH_TRY(dalloc(ctx, &ctx->mat2, c));
-        SPH_TRY(dalloc(ctx, &ctx->keys, c));
-        for (float4 **p : {&ctx->xh, &ctx->xl, &ctx->vhf, &ctx->vlf})
-            if (*p) {
-                cudaFree(*p);
-                *p = nullptr;
-            }
-        ctx->cap = c;
-    }
-    ctx->n = n;
-    SPH_CUDA(ctx, cudaMemcpy2DAsync(ctx->F, sizeof(double) * ctx->cap, fields, sizeof(double) * ld,
-                                    sizeof(double) * n, SPH_NFIELD, cudaMemcpyHostToDevice, ctx->stream));
-    if (id) {
-        SPH_CUDA(ctx, cudaMemcpyAsync(ctx->id, id, sizeof(int64_t) * n, cudaMemcpyHostToDevice, ctx->stream));
-    } else {
-        std::vector<int64_t> tmp(n);
-        for (int64_t i = 0; i < n; ++i) tmp[i] = i;
-        SPH_CUDA(ctx, cudaMemcpyAsync(ctx->id, tmp.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice, ctx->stream));
-        SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    }
-    if (material) {
-        SPH_CUDA(ctx, cudaMemcpyAsync(ctx->mat, material, sizeof(int32_t) * n, cudaMemcpyHostToDevice, ctx->stream));
-    } else {
-        SPH_CUDA(ctx, cudaMemsetAsync(ctx->mat, 0, sizeof(int32_t) * n, ctx->stream));
-    }
-    k_iota32<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(ctx->slot, (int)n); ++ctx->launches;
-    SPH_CUDA(ctx, cudaGetLastError());
-    // power of two close to 1 / mean mass (exact rescaling of the FP32 mass copies)
-    ctx->mscale = std::ldexp(1.0, -(int)std::lround(std::log2(msum / (double)n)));
-    if (init_smth) SPH_TRY(sph_init_smth(ctx));
-    SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    ctx->time = time;
-    ctx->dt = dt;
+    // one run: the context's previous particles and runs are replaced
+    Runs &R = ctx->runs;
+    R.R = 0;
+    R.n.clear();
+    R.time.clear();
+    R.dt.clear();
+    R.steps.clear();
+    R.handle.clear();
+    R.fresh.clear();
+    ctx->n = 0;
+    ctx->uploaded = false;
+    ctx->batch = false;
+    SPH_TRY(append_run(ctx, n, fields, ld, id, material, time, dt, flags, nullptr));
     ctx->step = 0;
     ctx->uploaded = true;
     // SPH_UPLOAD_FORCES_VALID: acc / grav / eng_dot / dt in the block are the forces of this state
     ctx->have_forces = (flags & SPH_UPLOAD_FORCES_VALID) && dt > 0.0;
+    return SPH_OK;
+}
+
+int sph_add_run(sph_ctx *ctx, int64_t n, const double *fields, int64_t ld, const int64_t *id, const int32_t *material,
+                double time, double dt, int flags, int64_t *handle) {
+    if (!ctx || !handle) return SPH_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (!ctx->uploaded) {   // an empty context: the run set starts here
+        ctx->runs.R = 0;
+        ctx->n = 0;
+    }
+    SPH_TRY(append_run(ctx, n, fields, ld, id, material, time, dt, flags, handle));
+    ctx->uploaded = true;
+    ctx->batch = true;
+    return SPH_OK;
+}
+
+int sph_remove_run(sph_ctx *ctx, int64_t handle) {
+    if (!ctx) return SPH_ERR_ARG;
+    const int r = find_run(ctx, handle);
+    if (r < 0) return sph_fail(ctx, SPH_ERR_ARG, "no run %lld", (long long)handle);
+    cudaSetDevice(ctx->device);
+    Runs &R = ctx->runs;
+    const int64_t cnt = R.n[r], off = R.off[r], n_new = ctx->n - cnt;
+    if (n_new > 0) {
+        k_remove_run<<<sph_div_up(n_new, 256), 256, 0, ctx->stream>>>(
+            ctx->F, ctx->F2, ctx->cap, (int)n_new, (int)off, (int)cnt, r, ctx->id, ctx->id2, ctx->slot, ctx->slot2,
+            ctx->mat, ctx->mat2, R.prun, R.prun2); ++ctx->launches;
+        SPH_CUDA(ctx, cudaGetLastError());
+        std::swap(ctx->F, ctx->F2);
+        std::swap(ctx->id, ctx->id2);
+        std::swap(ctx->slot, ctx->slot2);
+        std::swap(ctx->mat, ctx->mat2);
+        std::swap(R.prun, R.prun2);
+    }
+    R.n.erase(R.n.begin() + r);
+    R.time.erase(R.time.begin() + r);
+    R.dt.erase(R.dt.begin() + r);
+    R.steps.erase(R.steps.begin() + r);
+    R.handle.erase(R.handle.begin() + r);
+    R.fresh.erase(R.fresh.begin() + r);
+    R.R -= 1;
+    ctx->n = n_new;
+    if (R.R == 0) ctx->uploaded = false;
+    return sph_runs_layout(ctx);
+}
+
+int sph_run_info(sph_ctx *ctx, int64_t handle, int64_t *n, double *time, double *dt, int64_t *steps) {
+    if (!ctx) return SPH_ERR_ARG;
+    const int r = find_run(ctx, handle);
+    if (r < 0) return sph_fail(ctx, SPH_ERR_ARG, "no run %lld", (long long)handle);
+    if (n) *n = ctx->runs.n[r];
+    if (time) *time = ctx->runs.time[r];
+    if (dt) *dt = ctx->runs.dt[r];
+    if (steps) *steps = ctx->runs.steps[r];
+    return SPH_OK;
+}
+
+int sph_list_runs(sph_ctx *ctx, int64_t *handles, int cap, int *n_runs) {
+    if (!ctx || !n_runs) return SPH_ERR_ARG;
+    *n_runs = ctx->runs.R;
+    for (int r = 0; r < ctx->runs.R && r < cap; ++r)
+        if (handles) handles[r] = ctx->runs.handle[r];
+    return SPH_OK;
+}
+
+int sph_download_run(sph_ctx *ctx, int64_t handle, double *fields, int64_t ld, int64_t *id, int32_t *material) {
+    if (!ctx) return SPH_ERR_ARG;
+    const int r = find_run(ctx, handle);
+    if (r < 0) return sph_fail(ctx, SPH_ERR_ARG, "no run %lld", (long long)handle);
+    const Runs &R = ctx->runs;
+    const int n = (int)R.n[r];
+    if (!fields || ld < n) return sph_fail(ctx, SPH_ERR_ARG, "bad output block");
+    cudaSetDevice(ctx->device);
+    k_unpermute<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(ctx->F, ctx->F2, ctx->cap, (int)R.off[r], n, ctx->slot,
+                                                             R.prun, nullptr, ctx->id, ctx->id2, ctx->mat,
+                                                             ctx->mat2); ++ctx->launches;
+    SPH_CUDA(ctx, cudaGetLastError());
+    SPH_CUDA(ctx, cudaMemcpy2DAsync(fields, sizeof(double) * ld, ctx->F2, sizeof(double) * ctx->cap,
+                                    sizeof(double) * n, SPH_NFIELD, cudaMemcpyDeviceToHost, ctx->stream));
+    if (id) SPH_CUDA(ctx, cudaMemcpyAsync(id, ctx->id2, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    if (material)
+        SPH_CUDA(ctx, cudaMemcpyAsync(material, ctx->mat2, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SPH_OK;
+}
+
+int sph_run_diagnostics(sph_ctx *ctx, int64_t handle, double out[8]) {
+    if (!ctx || !out) return SPH_ERR_ARG;
+    const int r = find_run(ctx, handle);
+    if (r < 0) return sph_fail(ctx, SPH_ERR_ARG, "no run %lld", (long long)handle);
+    cudaSetDevice(ctx->device);
+    std::vector<double> per(8 * (size_t)ctx->runs.R);
+    SPH_TRY(sph_run_diag(ctx, per.data()));
+    for (int k = 0; k < 8; ++k) out[k] = per[(size_t)r * 8 + k];
     return SPH_OK;
 }
 
@@ -392,8 +627,9 @@ int sph_download(sph_ctx *ctx, double *fields, int64_t ld, int64_t *id, int32_t 
     if (!fields || ld < ctx->n) return sph_fail(ctx, SPH_ERR_ARG, "bad output block");
     cudaSetDevice(ctx->device);
     const int n = (int)ctx->n;
-    k_unpermute<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(ctx->F, ctx->F2, ctx->cap, n, ctx->slot, ctx->id,
-                                                             ctx->id2, ctx->mat, ctx->mat2); ++ctx->launches;
+    k_unpermute<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(ctx->F, ctx->F2, ctx->cap, 0, n, ctx->slot,
+                                                             ctx->runs.prun, ctx->runs.info, ctx->id, ctx->id2,
+                                                             ctx->mat, ctx->mat2); ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
     SPH_CUDA(ctx, cudaMemcpy2DAsync(fields, sizeof(double) * ld, ctx->F2, sizeof(double) * ctx->cap,
                                     sizeof(double) * n, SPH_NFIELD, cudaMemcpyDeviceToHost, ctx->stream));
@@ -411,40 +647,62 @@ int sph_prologue(sph_ctx *ctx) {
     ctx->n_ev = 0;
     SPH_TRY(time_mark(ctx, -1));
     SPH_TRY(compute_forces(ctx));
-    SPH_TRY(sph_dt_global(ctx, &ctx->dt));     // main.cpp:103
+    SPH_TRY(sph_run_reduce_dt(ctx));           // main.cpp:103
     SPH_TRY(sph_ext_force(ctx));               // main.cpp:104
     SPH_TRY(time_mark(ctx, SEG_FINAL));
     SPH_TRY(collect_timings(ctx));
     SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int r = 0; r < ctx->runs.R; ++r) ctx->runs.fresh[r] = 0;
+    ctx->have_forces = true;
     return SPH_OK;
 }
 
+// One loop iteration of main.cpp:125-173 for every run, each with its own dt.
+// A run added since the last step (no forces yet) takes this step as its
+// prologue: dt 0 in the kicks and the drift, then its forces and dt.
 int sph_step(sph_ctx *ctx, int n_steps) {
     if (!ctx) return SPH_ERR_ARG;
-    if (!ctx->have_forces) return sph_fail(ctx, SPH_ERR_STATE, "step before prologue");
+    if (!ctx->uploaded) return sph_fail(ctx, SPH_ERR_STATE, "step before upload");
+    if (!ctx->batch && !ctx->have_forces) return sph_fail(ctx, SPH_ERR_STATE, "step before prologue");
     cudaSetDevice(ctx->device);
+    Runs &R = ctx->runs;
     for (int s = 0; s < n_steps; ++s) {
-        const double dt = ctx->dt;
         ctx->n_ev = 0;
         SPH_TRY(time_mark(ctx, -1));
-        SPH_TRY(sph_kick_drift_predict(ctx, dt));   // main.cpp:126-131
+        bool fresh = false;
+        for (int r = 0; r < R.R; ++r) fresh = fresh || R.fresh[r];
+        std::vector<double> dt_step(R.dt);
+        if (fresh) {
+            for (int r = 0; r < R.R; ++r)
+                if (R.fresh[r]) dt_step[r] = 0.0;
+            SPH_CUDA(ctx, cudaMemcpyAsync(R.dt_dev, dt_step.data(), sizeof(double) * R.R, cudaMemcpyHostToDevice,
+                                          ctx->stream));
+        }
+        SPH_TRY(sph_kick_drift_predict(ctx));       // main.cpp:126-131
         SPH_TRY(time_mark(ctx, SEG_KDP));
-        ctx->time += dt;                            // main.cpp:132
+        for (int r = 0; r < R.R; ++r) R.time[r] += dt_step[r];   // main.cpp:132
         SPH_TRY(compute_forces(ctx));               // main.cpp:136-147
         SPH_TRY(sph_ext_force(ctx));                // main.cpp:148
-        SPH_TRY(sph_final_kick(ctx, dt));           // main.cpp:149-153
-        SPH_TRY(sph_dt_global(ctx, &ctx->dt));      // main.cpp:160
+        SPH_TRY(sph_final_kick(ctx));               // main.cpp:149-153
+        SPH_TRY(sph_run_reduce_dt(ctx));            // main.cpp:160
         SPH_TRY(time_mark(ctx, SEG_FINAL));
         SPH_TRY(collect_timings(ctx));
+        for (int r = 0; r < R.R; ++r) {
+            if (R.fresh[r]) R.fresh[r] = 0;
+            else R.steps[r] += 1;
+        }
         ctx->step += 1;
+        if (fresh) SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));   // dt_step is the copy's source
     }
+    ctx->have_forces = true;
     return SPH_OK;
 }
 
 int sph_get_time(const sph_ctx *ctx, double *time, double *dt, int64_t *step) {
     if (!ctx) return SPH_ERR_ARG;
-    if (time) *time = ctx->time;
-    if (dt) *dt = ctx->dt;
+    // the first run (the one of sph_upload)
+    if (time) *time = ctx->runs.R ? ctx->runs.time[0] : 0.0;
+    if (dt) *dt = ctx->runs.R ? ctx->runs.dt[0] : 0.0;
     if (step) *step = ctx->step;
     return SPH_OK;
 }

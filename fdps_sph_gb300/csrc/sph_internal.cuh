@@ -95,7 +95,8 @@ struct Tree {
     int *tmp_cnt = nullptr, *tmp_off = nullptr, *tmp_b = nullptr;
     int4 *cinfo = nullptr;    // per cell: first_child, n_child, start, count
     int *meta = nullptr;      // device [META_N]
-    double *rb = nullptr;     // device: root_lo[3], root_len, scale, rc2[MAX_LEVELS] at [8..]
+    double *rb = nullptr;     // device, per run (stride RB_STRIDE): root_lo[3], root_len, scale, rc2[MAX_LEVELS] at [8..]
+    int rb_cap = 0;           // runs rb has room for
     int n_cell_host = 0;
 };
 
@@ -159,6 +160,30 @@ struct Scan {
     int *total = nullptr;  // device int
 };
 
+// Runs: independent simulations advanced together by one context (one set of
+// launches per pass for all of them).  A run's particles are contiguous, runs
+// in index order, each in its own key order; every run has its own root cube,
+// octree root (cell r of level 0), dt and time.  sph_upload makes one run.
+constexpr int RUN_TILE = 2048;    // sort / reduction tile, aligned to run starts
+constexpr int RB_STRIDE = 32;     // doubles per run in Tree::rb
+struct Runs {
+    int R = 0;
+    std::vector<int64_t> n, off;            // particles per run, first particle
+    std::vector<double> time, dt;           // host copies; dt of the coming step
+    std::vector<int64_t> steps, handle;
+    std::vector<int> fresh;                 // joined since the last step: its first step is its prologue
+    int T = 0;                              // tiles over all runs
+    int cap_R = 0, cap_T = 0;
+    int4 *tiles = nullptr;                  // device [T]: start, length, histogram base, tiles of its run
+    int4 *info = nullptr;                   // device [R]: first particle, particles, first tile, tiles
+    double *dt_dev = nullptr;               // device [R]: dt of the coming step
+    double *part = nullptr;                 // device [T * 8]: per-tile partials
+    double *out = nullptr;                  // device [R * 8]: per-run results
+    unsigned char *damp = nullptr;          // device [R]: external damping applies
+    int *prun = nullptr, *prun2 = nullptr;  // device [cap]: run of each particle (permuted with it)
+    int64_t next_handle = 1;
+};
+
 }  // namespace sph
 
 struct sph_ctx {
@@ -190,13 +215,14 @@ struct sph_ctx {
     sph::SphSuper sup;
     sph::GravLists grav;
     sph::Scan scan;
+    sph::Runs runs;
 
     double mscale = 1.0;   // power of two ~ 1 / particle mass, keeps FP32 pair sums near unity
 
-    double time = 0.0, dt = 0.0;
-    int64_t step = 0;
+    int64_t step = 0;          // steps taken by sph_step (all runs)
     bool uploaded = false;
-    bool have_forces = false;
+    bool have_forces = false;   // sph_upload contexts: the prologue (or the uploaded forces) came first
+    bool batch = false;         // runs added with sph_add_run: a new run's first step is its prologue
 
     // per-segment device timings (CUDA events on `stream`), accumulated until reset
     cudaEvent_t ev[64];
@@ -247,6 +273,9 @@ int sph_build_sph_lists(sph_ctx *ctx, int mode);
 int sph_density_from_superset(sph_ctx *ctx);
 int sph_nbr_ensure_superset(sph_ctx *ctx);   // mixed precision: density pass without an exact list
 int time_mark(sph_ctx *ctx, int seg);      // event at the end of a timed segment (when timing is on)
+int sph_runs_layout(sph_ctx *ctx);        // offsets and tiles of the runs after a change of the run set
+int sph_run_reduce_dt(sph_ctx *ctx);      // per-run min dt into runs.dt_dev and runs.dt
+int sph_run_diag(sph_ctx *ctx, double *out);   // per-run conserved quantities, out[R * 8]
 int sph_build_grav_groups(sph_ctx *ctx);   // gravity i-groups (cells with <= n_group particles)
 int sph_build_grav_lists(sph_ctx *ctx);
 int sph_gravity_fused(sph_ctx *ctx);       // mixed precision: walk + force in one kernel
@@ -259,12 +288,11 @@ int sph_pass_hydro(sph_ctx *ctx, int build_lists);
 int sph_pass_gravity(sph_ctx *ctx, int build_lists);
 int sph_work_counts(sph_ctx *ctx, int64_t out[8]);
 int sph_pack_mixed(sph_ctx *ctx);
-int sph_kick_drift_predict(sph_ctx *ctx, double dt);
-int sph_final_kick(sph_ctx *ctx, double dt);
+int sph_kick_drift_predict(sph_ctx *ctx);   // with each run's dt in runs.dt_dev
+int sph_final_kick(sph_ctx *ctx);
 int sph_ext_force(sph_ctx *ctx);
-int sph_dt_global(sph_ctx *ctx, double *dt_out);
-int sph_diag(sph_ctx *ctx, double out[8]);
-int sph_init_smth(sph_ctx *ctx);
+int sph_diag(sph_ctx *ctx, double out[8]);   // summed over the runs
+int sph_init_smth(sph_ctx *ctx, int64_t off, int64_t n);
 
 // ---------------------------------------------------------------------------
 // device helpers

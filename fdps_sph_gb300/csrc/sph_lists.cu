@@ -76,14 +76,17 @@ template <bool FILL>
 __global__ void __launch_bounds__(GQ_WARPS * 32)
 k_grav_lists(int ng, const int *__restrict__ group_cell, const double *__restrict__ x,
              const double *__restrict__ y, const double *__restrict__ z, const int4 *__restrict__ cinfo,
-             const int *__restrict__ clevel, const double4 *__restrict__ com, const double *__restrict__ rb,
-             int *n_epj, int *n_spj, const int *off_epj, const int *off_spj, int *epj, int *spj, int *err) {
+             const int *__restrict__ clevel, const double4 *__restrict__ com, const double *__restrict__ rb_all,
+             const int *__restrict__ prun, int *n_epj, int *n_spj, const int *off_epj, const int *off_spj, int *epj,
+             int *spj, int *err) {
     __shared__ int s_q[GQ_WARPS][GQCAP];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int g = blockIdx.x * GQ_WARPS + warp;
     if (g >= ng) return;
     const int4 gi = cinfo[group_cell[g]];
     const int s = gi.z, cnt = gi.w;
+    const int root = prun[s];   // the group's run: its octree root and opening radii
+    const double *rb = rb_all + (int64_t)root * RB_STRIDE;
     double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (int k = lane; k < cnt; k += 32) {
         const double p[3] = {x[s + k], y[s + k], z[s + k]};
@@ -99,7 +102,7 @@ k_grav_lists(int ng, const int *__restrict__ group_cell, const double *__restric
     int *Q = s_q[warp];
     int ne = 0, ns = 0;
     const int be = FILL ? off_epj[g] : 0, bs = FILL ? off_spj[g] : 0;
-    if (lane == 0) Q[0] = 0;
+    if (lane == 0) Q[0] = root;
     int head = 0, tail = 1;
     const int q = lane >> 3, k = lane & 7;
     const unsigned below = (1u << lane) - 1u;
@@ -212,7 +215,7 @@ int sph_build_grav_lists(sph_ctx *ctx) {
     SPH_CUDA(ctx, cudaMemsetAsync(t.meta + META_ERR, 0, sizeof(int), st));
     k_grav_lists<false><<<blocks, GQ_WARPS * 32, 0, st>>>(ng, G.group_cell, FLD(ctx->F, SPH_X, ctx->cap),
                                                          FLD(ctx->F, SPH_Y, ctx->cap), FLD(ctx->F, SPH_Z, ctx->cap),
-                                                         t.cinfo, t.level, t.com, t.rb, G.n_epj, G.n_spj, nullptr,
+                                                         t.cinfo, t.level, t.com, t.rb, ctx->runs.prun, G.n_epj, G.n_spj, nullptr,
                                                          nullptr, nullptr, nullptr, t.meta + META_ERR); ++ctx->launches;
     SPH_TRY(sph_scan_exclusive(ctx, G.n_epj, G.off_epj, nullptr, ng, nullptr));
     SPH_TRY(sph_scan_exclusive(ctx, G.n_spj, G.off_spj, nullptr, ng, nullptr));
@@ -238,7 +241,7 @@ int sph_build_grav_lists(sph_ctx *ctx) {
     G.tot_spj = tot_s;
     k_grav_lists<true><<<blocks, GQ_WARPS * 32, 0, st>>>(ng, G.group_cell, FLD(ctx->F, SPH_X, ctx->cap),
                                                         FLD(ctx->F, SPH_Y, ctx->cap), FLD(ctx->F, SPH_Z, ctx->cap),
-                                                        t.cinfo, t.level, t.com, t.rb, G.n_epj, G.n_spj, G.off_epj,
+                                                        t.cinfo, t.level, t.com, t.rb, ctx->runs.prun, G.n_epj, G.n_spj, G.off_epj,
                                                         G.off_spj, G.epj, G.spj, t.meta + META_ERR); ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
     G.valid = true;

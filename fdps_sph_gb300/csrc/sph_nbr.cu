@@ -45,15 +45,16 @@ __device__ __forceinline__ float df_sub(float ah, float al, float bh, float bl) 
 template <bool EMIT>
 __global__ void k_units(const int *meta, const int *start, const int *count, const int *first_child,
                         const int *n_child, int *nunits, const int *off, int2 *units) {
-    const int nc = meta[MAX_LEVELS];
+    const int nc = meta[MAX_LEVELS], n_roots = meta[1];
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
         const int cnt = count[c], nch = n_child[c];
+        const bool root = c < n_roots;   // level 0: one root per run
         int k = 0;
         int2 *out = EMIT ? units + off[c] : nullptr;
-        if (c == 0 && cnt <= UNIT) {
+        if (root && cnt <= UNIT) {
             if (EMIT) out[k] = make_int2(start[c], cnt);
             ++k;
-        } else if (c == 0 && nch == 0) {
+        } else if (root && nch == 0) {
             for (int s = 0; s < cnt; s += UNIT) {
                 if (EMIT) out[k] = make_int2(start[c] + s, min(UNIT, cnt - s));
                 ++k;
@@ -117,7 +118,8 @@ __global__ void __launch_bounds__(NB_WARPS * 32, 7)
 k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ uidx, const double *__restrict__ x,
            const double *__restrict__ y, const double *__restrict__ z, const double *__restrict__ h,
            double *__restrict__ hsup, const float4 *__restrict__ xh,
-           const float4 *__restrict__ xl, const float *__restrict__ H2f, WalkTree T, int *__restrict__ sup,
+           const float4 *__restrict__ xl, const float *__restrict__ H2f, const int *__restrict__ prun, WalkTree T,
+           int *__restrict__ sup,
            float *__restrict__ sup_r2, float *__restrict__ sup_m, int *__restrict__ cnt, int K, int64_t stride, int *err,
            int *maxcnt) {
     // cells to visit: (first_child, -n_child) for an internal cell, (start, count) for a leaf
@@ -241,11 +243,12 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
 
     int sp = 0;
     {
-        const float4 a = T.blo[0], b = T.bhi[0];
+        const int root = prun[U.x];   // the unit's run's octree root
+        const float4 a = T.blo[root], b = T.bhi[root];
         const float R = fmaxf(Rg, __fmul_ru(2.5f * KAPPA * 1.00390625f, b.w));
         if (gap2_rd(a, b, glo, ghi) < __fmul_ru(R, R)) {
             if (lane == 0) {
-                const int4 r = T.cinfo[0];
+                const int4 r = T.cinfo[root];
                 stack[0] = r.y == 0 ? make_int2(r.z, r.w) : make_int2(r.x, -r.y);
             }
             sp = 1;
@@ -341,7 +344,8 @@ __global__ void k_cell_vmax(int l, const int *meta, const float *vR, const int4 
 __global__ void __launch_bounds__(NB_WARPS * 32)
 k_unit_mark(int n_units, const int2 *__restrict__ units, const float4 *__restrict__ xh, const float4 *__restrict__ xl,
             const float *__restrict__ vR, const float *__restrict__ cvR, const int4 *__restrict__ cinfo,
-            const float4 *__restrict__ blo, const float4 *__restrict__ bhi, int *umark) {
+            const float4 *__restrict__ blo, const float4 *__restrict__ bhi, const int *__restrict__ prun,
+            int *umark) {
     __shared__ int s_stack[NB_WARPS][NB_STACK];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int u = blockIdx.x * NB_WARPS + warp;
@@ -367,9 +371,10 @@ k_unit_mark(int n_units, const int2 *__restrict__ units, const float4 *__restric
     int sp = 0;
     bool hit = false;
     {
-        const float r = cvR[0];
-        if (r > 0.0f && gap2_rd(blo[0], bhi[0], glo, ghi) < __fmul_ru(r, r)) {
-            if (lane == 0) stack[0] = 0;
+        const int root = prun[U.x];   // the unit's run's octree root
+        const float r = cvR[root];
+        if (r > 0.0f && gap2_rd(blo[root], bhi[root], glo, ghi) < __fmul_ru(r, r)) {
+            if (lane == 0) stack[0] = root;
             sp = 1;
         }
         __syncwarp();
@@ -520,7 +525,9 @@ k_density_sup32(int n, const int *__restrict__ sup, const float *__restrict__ su
         const int m8 = min(8, c - k);
         const float4 m0 = reinterpret_cast<const float4 *>(mrow + k)[0], m1 = reinterpret_cast<const float4 *>(mrow + k)[1];
         const float mj[8] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
-        float part = 0.0f;
+        // every member goes straight into the compensated pair: the sum depends only on the
+        // sequence of members (the walk's order), not on where non-members sit in the row, so a
+        // row rebuilt with another skin (a repair, another run's violators) gives the same result
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
             if (u >= m8) continue;
@@ -531,9 +538,8 @@ k_density_sup32(int n, const int *__restrict__ sup, const float *__restrict__ su
             const float s_ = sqrt_a(rr[u]) * invH;
             const float p = fmaxf(1.0f - s_, 0.0f);
             const float p2 = p * p, p4 = p2 * p2;
-            part = fmaf(mj[u], (1.0f + s_ * (8.0f + s_ * (25.0f + s_ * 32.0f))) * (p4 * p4), part);
+            df_add(acc_h, acc_l, mj[u] * ((1.0f + s_ * (8.0f + s_ * (25.0f + s_ * 32.0f))) * (p4 * p4)));
         }
-        df_add(acc_h, acc_l, part);   // partial sums of at most 8 terms
     }
     density_tail32(acc_h + acc_l, invH, dscale, m[i], dens + i, h + i);
 }
@@ -681,7 +687,8 @@ static int walk_units(sph_ctx *ctx, const int *uidx, int n_walk) {
         if (blocks > 0) {
             k_sup_walk<<<blocks, NB_WARPS * 32, 0, ctx->stream>>>(
                 n_walk, S.units, uidx, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
-                FLD(ctx->F, SPH_SMTH, cap), S.hsup, S.pxh, S.pxl, S.H2f, T, S.nbr, S.r2, S.m, S.cnt, S.K,
+                FLD(ctx->F, SPH_SMTH, cap), S.hsup, S.pxh, S.pxl, S.H2f, ctx->runs.prun, T, S.nbr, S.r2, S.m,
+                S.cnt, S.K,
                 (int64_t)S.K, meta + META_ERR, meta + META_MAXCNT);
             ++ctx->launches;
         }
@@ -737,7 +744,7 @@ static int ensure_superset(sph_ctx *ctx) {
     }
     const int blocks = (S.n_units + NB_WARPS - 1) / NB_WARPS;
     k_unit_mark<<<blocks, NB_WARPS * 32, 0, ctx->stream>>>(S.n_units, S.units, S.pxh, S.pxl, vR, S.cvR,
-                                                           t.cinfo, t.blo, t.bhi, S.umark);
+                                                           t.cinfo, t.blo, t.bhi, ctx->runs.prun, S.umark);
     ++ctx->launches;
     SPH_TRY(sph_scan_exclusive(ctx, S.umark, S.uoff, nullptr, S.n_units, ctx->scan.total));
     k_unit_compact<<<grid, 256, 0, ctx->stream>>>(S.n_units, S.umark, S.uoff, S.uidx);

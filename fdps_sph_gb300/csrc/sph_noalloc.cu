@@ -38,9 +38,9 @@ __global__ void k_bbox_partial(const double *x, const double *y, const double *z
 __global__ void k_bbox_final(const double *part, int nb, double theta, double *rb);
 __global__ void k_keys(const double *x, const double *y, const double *z, int n, const double *rb, uint64_t *keys,
                        uint32_t *vals, int *err);
-__global__ void k_rs_hist(const uint64_t *keys, int n, int shift, uint32_t *hist, int nb);
+__global__ void k_rs_hist(const uint64_t *keys, int n, int shift, uint32_t *hist, int nb, const int4 *tiles);
 __global__ void k_rs_scatter(const uint64_t *kin, const uint32_t *vin, uint64_t *kout, uint32_t *vout, int n,
-                             int shift, const uint32_t *off, int nb);
+                             int shift, const uint32_t *off, int nb, const int4 *tiles);
 
 namespace {
 
@@ -130,12 +130,12 @@ extern "C" int sph_morton_order_noalloc(const double *x, const double *y, const 
     const LenArg L{nullptr, 256 * nb, 0};
     for (int pass = 0; pass < 8; ++pass) {
         const int shift = pass * 8;
-        k_rs_hist<<<nb, 256, 0, st>>>(ka, nn, shift, hist, nb);
+        k_rs_hist<<<nb, 256, 0, st>>>(ka, nn, shift, hist, nb, nullptr);
         k_scan_reduce<<<NA_SCAN, 256, 0, st>>>(reinterpret_cast<const int *>(hist), L, part);
         k_scan_part<<<1, NA_SCAN, 0, st>>>(part, NA_SCAN, nullptr);
         k_scan_down<<<NA_SCAN, 256, 0, st>>>(reinterpret_cast<const int *>(hist), reinterpret_cast<int *>(hoff), L,
                                              part);
-        k_rs_scatter<<<nb, 256, 0, st>>>(ka, va, kb, vb, nn, shift, hoff, nb);
+        k_rs_scatter<<<nb, 256, 0, st>>>(ka, va, kb, vb, nn, shift, hoff, nb, nullptr);
         uint64_t *tk = ka;
         ka = kb;
         kb = tk;

@@ -621,7 +621,8 @@ __device__ __forceinline__ void grav_acc(float px, float py, float pz, float e2,
 
 __global__ void __launch_bounds__(GF_T, 3)
 k_grav_fused32(const int *__restrict__ group_cell, const int4 *__restrict__ cinfo, const double4 *__restrict__ com,
-               const double *__restrict__ rb, const double *__restrict__ x, const double *__restrict__ y,
+               const double *__restrict__ rb_all, const int *__restrict__ prun, const double *__restrict__ x,
+               const double *__restrict__ y,
                const double *__restrict__ z, const float4 *__restrict__ xh, const float4 *__restrict__ xl,
                const double *__restrict__ h, const float4 *__restrict__ ch, const float4 *__restrict__ cl, float gms,
                double *gx, double *gy, double *gz, double *pot, int *n_epj, int *n_spj, int *err) {
@@ -637,6 +638,8 @@ k_grav_fused32(const int *__restrict__ group_cell, const int4 *__restrict__ cinf
     const int4 gi = cinfo[group_cell[blockIdx.x]];
     const int s = gi.z, cnt_all = gi.w;
     const float4 c_h = xh[s], c_l = xl[s];     // group origin: its first particle
+    const int root = prun[s];                  // the group's run: its octree root and opening radii
+    const double *rb = rb_all + (int64_t)root * RB_STRIDE;
     for (int l = tid; l < MAX_LEVELS; l += GF_T) {
         s_rb[l] = rb[8 + l];
         s_rbf[l] = (float)rb[8 + l];
@@ -699,7 +702,7 @@ k_grav_fused32(const int *__restrict__ group_cell, const int4 *__restrict__ cinf
         }
         float Dh[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}}, Dl[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
         int head = 0, tail = 1, it = 0;
-        if (tid == 0) s_q[0] = cinfo[0];   // the root, level 0
+        if (tid == 0) s_q[0] = cinfo[root];   // the run's root, level 0
         __syncthreads();
         for (;;) {
             // ---- walk until the buffers are full or the queue is empty
@@ -892,11 +895,14 @@ k_grav_fused32(const int *__restrict__ group_cell, const int4 *__restrict__ cinf
 
 struct IntegArgs {
     double *x, *y, *z, *vx, *vy, *vz, *ax, *ay, *az, *gx, *gy, *gz, *vhx, *vhy, *vhz, *u, *ud, *uh;
+    const int *prun;        // run of each particle
+    const double *run_dt;   // dt of the step, per run
 };
 
-__global__ void k_kick_drift_predict(int n, IntegArgs a, double dt) {
+__global__ void k_kick_drift_predict(int n, IntegArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const double dt = a.run_dt[a.prun[i]];
     const double ax = a.ax[i] + a.gx[i], ay = a.ay[i] + a.gy[i], az = a.az[i] + a.gz[i];
     const double hx = a.vx[i] + 0.5 * dt * ax, hy = a.vy[i] + 0.5 * dt * ay, hz = a.vz[i] + 0.5 * dt * az;
     a.vhx[i] = hx;
@@ -912,18 +918,20 @@ __global__ void k_kick_drift_predict(int n, IntegArgs a, double dt) {
     a.u[i] += dt * a.ud[i];
 }
 
-__global__ void k_final_kick(int n, IntegArgs a, double dt, double damp) {
+__global__ void k_final_kick(int n, IntegArgs a, double damp) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const double dt = a.run_dt[a.prun[i]];
+    if (dt == 0.0) damp = 1.0;   // a run's prologue step (dampMotion belongs to the loop body, main.cpp:152)
     a.vx[i] = (a.vhx[i] + 0.5 * dt * (a.ax[i] + a.gx[i])) * damp;
     a.vy[i] = (a.vhy[i] + 0.5 * dt * (a.ay[i] + a.gy[i])) * damp;
     a.vz[i] = (a.vhz[i] + 0.5 * dt * (a.az[i] + a.gz[i])) * damp;
     a.u[i] = a.uh[i] + 0.5 * dt * a.ud[i];
 }
 
-__global__ void k_ext_force(int n, IntegArgs a, const double *dt) {
+__global__ void k_ext_force(int n, IntegArgs a, const double *dt, const unsigned char *run_damp) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || !run_damp[a.prun[i]]) return;
     const double d = dt[i];
     a.ax[i] += -a.vx[i] * 0.05 / d;
     a.ay[i] += -a.vy[i] * 0.05 / d;
@@ -968,6 +976,40 @@ __global__ void k_min_final(const double *part, int nb, double *out) {
     }
 }
 
+// per run: one block per tile (tiles aligned to run starts), then one block per run over its tiles
+__device__ double block_min(double r) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const double t = __shfl_xor_sync(0xffffffffu, r, o);
+        r = (t < r || t != t) ? t : r;
+    }
+    __shared__ double s[32];
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = r;
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) r = (s[w] < r || s[w] != s[w]) ? s[w] : r;
+    return r;
+}
+
+__global__ void k_min_tiles(const double *v, const int4 *tiles, double *part) {
+    const int4 t = tiles[blockIdx.x];
+    double r = 1.0e30;
+    for (int i = t.x + threadIdx.x; i < t.x + t.y; i += blockDim.x) {
+        const double d = v[i];
+        r = (d < r) ? d : r;   // std::min(r, d) with r first, integral.h:16
+        if (d != d) r = d;     // a NaN dt propagates so the host sees it
+    }
+    r = block_min(r);
+    if (threadIdx.x == 0) part[blockIdx.x] = r;
+}
+
+__global__ void k_min_runs(const double *part, const int4 *info, double *out) {
+    const int4 q = info[blockIdx.x];
+    double r = 1.0e30;
+    for (int b = q.z + threadIdx.x; b < q.z + q.w; b += blockDim.x) r = (part[b] < r || part[b] != part[b]) ? part[b] : r;
+    r = block_min(r);
+    if (threadIdx.x == 0) out[blockIdx.x] = r;
+}
+
 // conserved quantities, fixed-order two-stage reduction in FP64
 __global__ void k_diag_partial(int n, const double *x, const double *y, const double *z, const double *vx,
                                const double *vy, const double *vz, const double *m, const double *u,
@@ -996,6 +1038,48 @@ __global__ void k_diag_partial(int n, const double *x, const double *y, const do
         double v = 0.0;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += s[threadIdx.x][w];
         part[blockIdx.x * 8 + threadIdx.x] = v;
+    }
+}
+
+// per run: tiles (k_diag_partial over one tile's range), then each run's tiles in order
+__global__ void k_diag_tiles(const double *x, const double *y, const double *z, const double *vx, const double *vy,
+                             const double *vz, const double *m, const double *u, const double *pot, const int4 *tiles,
+                             double *part) {
+    const int4 t = tiles[blockIdx.x];
+    double q[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int i = t.x + threadIdx.x; i < t.x + t.y; i += blockDim.x) {
+        const double mi = m[i];
+        const double v2 = vx[i] * vx[i] + vy[i] * vy[i] + vz[i] * vz[i];
+        q[0] += mi * (u[i] + 0.5 * v2 + 0.5 * pot[i]);
+        q[1] += mi * vx[i];
+        q[2] += mi * vy[i];
+        q[3] += mi * vz[i];
+        q[4] += mi * (y[i] * vz[i] - z[i] * vy[i]);
+        q[5] += mi * (z[i] * vx[i] - x[i] * vz[i]);
+        q[6] += mi * (x[i] * vy[i] - y[i] * vx[i]);
+        q[7] += mi;
+    }
+    __shared__ double s[8][32];
+    for (int k = 0; k < 8; ++k) {
+        double v = q[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) s[k][threadIdx.x >> 5] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 8) {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += s[threadIdx.x][w];
+        part[blockIdx.x * 8 + threadIdx.x] = v;
+    }
+}
+
+__global__ void k_diag_runs(const double *part, const int4 *info, int R, double *out) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < R * 8; k += gridDim.x * blockDim.x) {
+        const int r = k >> 3, c = k & 7;
+        const int4 q = info[r];
+        double v = 0.0;
+        for (int b = q.z; b < q.z + q.w; ++b) v += part[b * 8 + c];
+        out[k] = v;
     }
 }
 
@@ -1039,7 +1123,8 @@ using namespace sph;
 static IntegArgs integ_args(sph_ctx *ctx) {
     return IntegArgs{CF(SPH_X),  CF(SPH_Y),  CF(SPH_Z),  CF(SPH_VX),  CF(SPH_VY),  CF(SPH_VZ),
                      CF(SPH_AX), CF(SPH_AY), CF(SPH_AZ), CF(SPH_GX),  CF(SPH_GY),  CF(SPH_GZ),
-                     CF(SPH_VHX), CF(SPH_VHY), CF(SPH_VHZ), CF(SPH_ENG), CF(SPH_ENGDOT), CF(SPH_ENGHALF)};
+                     CF(SPH_VHX), CF(SPH_VHY), CF(SPH_VHZ), CF(SPH_ENG), CF(SPH_ENGDOT), CF(SPH_ENGHALF),
+                     ctx->runs.prun, ctx->runs.dt_dev};
 }
 
 static int ensure_mixed_buffers(sph_ctx *ctx) {
@@ -1162,58 +1247,84 @@ int sph_pass_gravity(sph_ctx *ctx, int build_lists) {
     return SPH_OK;
 }
 
-int sph_kick_drift_predict(sph_ctx *ctx, double dt) {
+// the step's dt of every run is in runs.dt_dev (set by sph_run_reduce_dt or the host)
+int sph_kick_drift_predict(sph_ctx *ctx) {
     const int n = (int)ctx->n;
-    k_kick_drift_predict<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, integ_args(ctx), dt); ++ctx->launches;
+    k_kick_drift_predict<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, integ_args(ctx)); ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
     return SPH_OK;
 }
 
-int sph_final_kick(sph_ctx *ctx, double dt) {
+int sph_final_kick(sph_ctx *ctx) {
     const int n = (int)ctx->n;
-    k_final_kick<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, integ_args(ctx), dt, ctx->cfg.damping); ++ctx->launches;
+    k_final_kick<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, integ_args(ctx), ctx->cfg.damping); ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
     return SPH_OK;
 }
 
+// GI_universal::addExternalForce (GI.h:458-465) for the runs whose time is before ext_damp_tend
 int sph_ext_force(sph_ctx *ctx) {
-    if (!ctx->cfg.ext_damp || ctx->time >= ctx->cfg.ext_damp_tend) return SPH_OK;
+    if (!ctx->cfg.ext_damp) return SPH_OK;
+    Runs &R = ctx->runs;
+    std::vector<unsigned char> on(R.R);
+    bool any = false;
+    for (int r = 0; r < R.R; ++r) {
+        on[r] = R.time[r] < ctx->cfg.ext_damp_tend;
+        any = any || on[r];
+    }
+    if (!any) return SPH_OK;
+    SPH_CUDA(ctx, cudaMemcpyAsync(R.damp, on.data(), R.R, cudaMemcpyHostToDevice, ctx->stream));
     const int n = (int)ctx->n;
-    k_ext_force<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, integ_args(ctx), CF(SPH_DT)); ++ctx->launches;
+    k_ext_force<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, integ_args(ctx), CF(SPH_DT), R.damp); ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
+    SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));   // `on` lives on the host stack
     return SPH_OK;
 }
 
-int sph_dt_global(sph_ctx *ctx, double *dt_out) {
-    const int n = (int)ctx->n;
-    k_min_partial<<<RED_BLOCKS, 256, 0, ctx->stream>>>(n, CF(SPH_DT), ctx->scratch_d); ++ctx->launches;
-    k_min_final<<<1, 256, 0, ctx->stream>>>(ctx->scratch_d, RED_BLOCKS, ctx->scratch_d + RED_BLOCKS * 8); ++ctx->launches;
-    SPH_CUDA(ctx, cudaMemcpyAsync(ctx->host_scalars, ctx->scratch_d + RED_BLOCKS * 8, sizeof(double),
-                                  cudaMemcpyDeviceToHost, ctx->stream));
+// getTimeStepGlobal (integral.h:4-20) for every run: min over the run's dt_i into runs.dt_dev and runs.dt
+int sph_run_reduce_dt(sph_ctx *ctx) {
+    Runs &R = ctx->runs;
+    k_min_tiles<<<R.T, 256, 0, ctx->stream>>>(CF(SPH_DT), R.tiles, R.part); ++ctx->launches;
+    k_min_runs<<<R.R, 256, 0, ctx->stream>>>(R.part, R.info, R.dt_dev); ++ctx->launches;
+    std::vector<double> h(R.R);
+    SPH_CUDA(ctx, cudaMemcpyAsync(h.data(), R.dt_dev, sizeof(double) * R.R, cudaMemcpyDeviceToHost, ctx->stream));
     SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    *dt_out = ctx->host_scalars[0];
-    if (!(*dt_out > 0.0) || !isfinite(*dt_out))
-        return sph_fail(ctx, SPH_ERR_NONFINITE, "global dt is not a positive finite number (%g)", *dt_out);
+    for (int r = 0; r < R.R; ++r) {
+        const double d = h[r];
+        if (!(d > 0.0) || !isfinite(d))
+            return sph_fail(ctx, SPH_ERR_NONFINITE, "run %d: global dt is not a positive finite number (%g)", r, d);
+        R.dt[r] = d;
+    }
+    return SPH_OK;
+}
+
+// conserved quantities per run: out[r * 8 + k] (k as sph_diagnostics)
+int sph_run_diag(sph_ctx *ctx, double *out) {
+    Runs &R = ctx->runs;
+    k_diag_tiles<<<R.T, 256, 0, ctx->stream>>>(CF(SPH_X), CF(SPH_Y), CF(SPH_Z), CF(SPH_VX), CF(SPH_VY), CF(SPH_VZ),
+                                               CF(SPH_MASS), CF(SPH_ENG), CF(SPH_POT), R.tiles, R.part);
+    ++ctx->launches;
+    k_diag_runs<<<sph_div_up(R.R * 8, 256), 256, 0, ctx->stream>>>(R.part, R.info, R.R, R.out); ++ctx->launches;
+    SPH_CUDA(ctx, cudaMemcpyAsync(out, R.out, sizeof(double) * 8 * R.R, cudaMemcpyDeviceToHost, ctx->stream));
+    SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return SPH_OK;
 }
 
 int sph_diag(sph_ctx *ctx, double out[8]) {
-    const int n = (int)ctx->n;
-    k_diag_partial<<<RED_BLOCKS, 256, 0, ctx->stream>>>(n, CF(SPH_X), CF(SPH_Y), CF(SPH_Z), CF(SPH_VX), CF(SPH_VY),
-                                                        CF(SPH_VZ), CF(SPH_MASS), CF(SPH_ENG), CF(SPH_POT),
-                                                        ctx->scratch_d); ++ctx->launches;
-    k_diag_final<<<1, 32, 0, ctx->stream>>>(ctx->scratch_d, RED_BLOCKS, ctx->scratch_d + RED_BLOCKS * 8); ++ctx->launches;
-    SPH_CUDA(ctx, cudaMemcpyAsync(ctx->host_scalars, ctx->scratch_d + RED_BLOCKS * 8, 8 * sizeof(double),
-                                  cudaMemcpyDeviceToHost, ctx->stream));
-    SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    for (int k = 0; k < 8; ++k) out[k] = ctx->host_scalars[k];
+    std::vector<double> per(8 * (size_t)ctx->runs.R);
+    SPH_TRY(sph_run_diag(ctx, per.data()));
+    for (int k = 0; k < 8; ++k) {
+        double v = 0.0;
+        for (int r = 0; r < ctx->runs.R; ++r) v += per[(size_t)r * 8 + k];
+        out[k] = v;
+    }
     return SPH_OK;
 }
 
-int sph_init_smth(sph_ctx *ctx) {
-    const int n = (int)ctx->n;
-    k_init_smth<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, CF(SPH_MASS), CF(SPH_DENS), CF(SPH_SMTH),
-                                                             CF(SPH_GRADH)); ++ctx->launches;
+// RealPtcl::initialize (class.h:196-199) for particles [off, off + n)
+int sph_init_smth(sph_ctx *ctx, int64_t off, int64_t n) {
+    k_init_smth<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>((int)n, CF(SPH_MASS) + off, CF(SPH_DENS) + off,
+                                                             CF(SPH_SMTH) + off, CF(SPH_GRADH) + off); ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
     return SPH_OK;
 }
@@ -1263,7 +1374,8 @@ int sph_gravity_fused(sph_ctx *ctx) {
     SPH_CUDA(ctx, cudaMemsetAsync(t.meta + META_ERR, 0, sizeof(int), ctx->stream));
     // xh.w holds m * mscale: G m = xh.w * (G / mscale)
     const float gms = (float)(ctx->cfg.G / ctx->mscale);
-    k_grav_fused32<<<G.ng, GF_T, 0, ctx->stream>>>(G.group_cell, t.cinfo, t.com, t.rb, CF(SPH_X), CF(SPH_Y), CF(SPH_Z),
+    k_grav_fused32<<<G.ng, GF_T, 0, ctx->stream>>>(G.group_cell, t.cinfo, t.com, t.rb, ctx->runs.prun, CF(SPH_X),
+                                                   CF(SPH_Y), CF(SPH_Z),
                                                    ctx->xh, ctx->xl, CF(SPH_SMTH), chp, clp, gms, CF(SPH_GX),
                                                    CF(SPH_GY), CF(SPH_GZ), CF(SPH_POT), G.n_epj, G.n_spj,
                                                    t.meta + META_ERR);

@@ -160,8 +160,29 @@ __global__ void k_bbox_partial(const double *x, const double *y, const double *z
     }
 }
 
+// the root cube from the particle box exactly as or_root_box, and the opening-radius table
+__device__ void root_cube(const double lo[3], const double hi[3], double theta, double *rb) {
+    double L = 0.0;
+    for (int d = 0; d < 3; ++d) {
+        const double e = __dsub_rn(hi[d], lo[d]);
+        if (e > L) L = e;
+    }
+    if (!(L > 0.0)) L = 1.0;
+    const double half = __dmul_rn(L, 0.50048828125);
+    for (int d = 0; d < 3; ++d) rb[d] = __dsub_rn(__dmul_rn(__dadd_rn(lo[d], hi[d]), 0.5), half);
+    const double len = __dadd_rn(half, half);
+    rb[3] = len;
+    rb[4] = __ddiv_rn(2097152.0, len);
+    // rc2[l] = (len / 2^l)^2 / theta^2, as or_rcrit_table
+    double r = __ddiv_rn(__dmul_rn(len, len), __dmul_rn(theta, theta));
+    for (int l = 0; l < MAX_LEVELS; ++l) {
+        rb[8 + l] = r;
+        r = __dmul_rn(r, 0.25);
+    }
+}
+
 // one block reduces the partial boxes (min / max are exact in any order), then
-// one thread forms the root cube exactly as or_root_box and the opening-radius table
+// one thread forms the root cube
 __global__ void k_bbox_final(const double *part, int nb, double theta, double *rb) {
     __shared__ double s[6][32];
     double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
@@ -188,23 +209,60 @@ __global__ void k_bbox_final(const double *part, int nb, double theta, double *r
             lo[d] = fmin(lo[d], s[d][w]);
             hi[d] = fmax(hi[d], s[3 + d][w]);
         }
-    double L = 0.0;
-    for (int d = 0; d < 3; ++d) {
-        const double e = __dsub_rn(hi[d], lo[d]);
-        if (e > L) L = e;
+    root_cube(lo, hi, theta, rb);
+}
+
+// per run: one block per tile reduces its particles' box, one block per run the tiles of the run
+__device__ void block_box(double lo[3], double hi[3]) {
+    __shared__ double s[6][32];
+    for (int d = 0; d < 3; ++d)
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[d] = fmin(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
+            hi[d] = fmax(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+        }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0)
+        for (int d = 0; d < 3; ++d) {
+            s[d][wid] = lo[d];
+            s[3 + d][wid] = hi[d];
+        }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+            for (int d = 0; d < 3; ++d) {
+                lo[d] = fmin(lo[d], s[d][w]);
+                hi[d] = fmax(hi[d], s[3 + d][w]);
+            }
+}
+
+__global__ void k_bbox_tiles(const double *x, const double *y, const double *z, const int4 *tiles, double *part) {
+    const int4 t = tiles[blockIdx.x];
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int i = t.x + threadIdx.x; i < t.x + t.y; i += blockDim.x) {
+        const double p[3] = {x[i], y[i], z[i]};
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = fmin(lo[d], p[d]);
+            hi[d] = fmax(hi[d], p[d]);
+        }
     }
-    if (!(L > 0.0)) L = 1.0;
-    const double half = __dmul_rn(L, 0.50048828125);
-    for (int d = 0; d < 3; ++d) rb[d] = __dsub_rn(__dmul_rn(__dadd_rn(lo[d], hi[d]), 0.5), half);
-    const double len = __dadd_rn(half, half);
-    rb[3] = len;
-    rb[4] = __ddiv_rn(2097152.0, len);
-    // rc2[l] = (len / 2^l)^2 / theta^2, as or_rcrit_table
-    double r = __ddiv_rn(__dmul_rn(len, len), __dmul_rn(theta, theta));
-    for (int l = 0; l < MAX_LEVELS; ++l) {
-        rb[8 + l] = r;
-        r = __dmul_rn(r, 0.25);
-    }
+    block_box(lo, hi);
+    if (threadIdx.x == 0)
+        for (int d = 0; d < 3; ++d) {
+            part[blockIdx.x * 8 + d] = lo[d];
+            part[blockIdx.x * 8 + 3 + d] = hi[d];
+        }
+}
+
+__global__ void k_bbox_runs(const double *part, const int4 *info, double theta, double *rb) {
+    const int4 r = info[blockIdx.x];
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int b = r.z + threadIdx.x; b < r.z + r.w; b += blockDim.x)
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = fmin(lo[d], part[b * 8 + d]);
+            hi[d] = fmax(hi[d], part[b * 8 + 3 + d]);
+        }
+    block_box(lo, hi);
+    if (threadIdx.x == 0) root_cube(lo, hi, theta, rb + (int64_t)blockIdx.x * RB_STRIDE);
 }
 
 __device__ __forceinline__ uint64_t spread3(uint64_t v) {
@@ -237,27 +295,52 @@ __global__ void k_keys(const double *x, const double *y, const double *z, int n,
     vals[i] = (uint32_t)i;
 }
 
+// keys against the particle's own run's root cube
+__global__ void k_keys_runs(const double *x, const double *y, const double *z, int n, const double *rb,
+                            const int *prun, uint64_t *keys, uint32_t *vals, int *err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double *q = rb + (int64_t)prun[i] * RB_STRIDE;
+    const double px = x[i], py = y[i], pz = z[i];
+    if (!isfinite(px) || !isfinite(py) || !isfinite(pz)) atomicOr(err, ERR_NONFINITE);
+    const uint64_t qx = cell_coord(px, q[0], q[4]);
+    const uint64_t qy = cell_coord(py, q[1], q[4]);
+    const uint64_t qz = cell_coord(pz, q[2], q[4]);
+    keys[i] = (spread3(qx) << 2) | (spread3(qy) << 1) | spread3(qz);
+    vals[i] = (uint32_t)i;
+}
+
 // ---------------------------------------------------------------------------
 // LSD radix sort of (key, value), 8 passes of 8 bits.  Each pass: per-tile
 // digit histogram, one exclusive scan over (digit, tile), then a stable
-// in-tile ranking and a scatter.
+// in-tile ranking and a scatter.  With a tile table (tiles aligned to run
+// starts; each entry: start, length, histogram base, tiles of its run) the
+// histogram is laid out run by run, digit-major within a run, so the one scan
+// yields offsets that keep every run in its own range: a segmented sort.
+// Without one, tile b covers [b * RS_TILE, ...) and the layout is digit-major.
 
 constexpr int RS_THREADS = 256;
 constexpr int RS_ITEMS = 8;
 constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
 
-__global__ void k_rs_hist(const uint64_t *keys, int n, int shift, uint32_t *hist, int nb) {
+__device__ __forceinline__ int4 rs_tile(const int4 *tiles, int n, int nb) {
+    if (tiles) return tiles[blockIdx.x];
+    const int s = blockIdx.x * RS_TILE;
+    return make_int4(s, min(RS_TILE, n - s), blockIdx.x, nb);
+}
+
+__global__ void k_rs_hist(const uint64_t *keys, int n, int shift, uint32_t *hist, int nb, const int4 *tiles) {
     __shared__ uint32_t h[256];
     h[threadIdx.x] = 0;
     __syncthreads();
-    const int base = blockIdx.x * RS_TILE;
+    const int4 tl = rs_tile(tiles, n, nb);
 #pragma unroll
     for (int k = 0; k < RS_ITEMS; ++k) {
-        const int i = base + k * RS_THREADS + threadIdx.x;
-        if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
+        const int p = k * RS_THREADS + threadIdx.x;
+        if (p < tl.y) atomicAdd(&h[(keys[tl.x + p] >> shift) & 255u], 1u);
     }
     __syncthreads();
-    hist[threadIdx.x * nb + blockIdx.x] = h[threadIdx.x];
+    hist[tl.z + threadIdx.x * tl.w] = h[threadIdx.x];
 }
 
 // Stable in-tile ranking by warp multisplit: each warp ranks its 256 keys
@@ -271,15 +354,16 @@ static_assert(RS_THREADS == 256, "one thread per digit in the offset step");
 
 __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint64_t *kin, const uint32_t *vin, uint64_t *kout,
                                                            uint32_t *vout, int n, int shift, const uint32_t *off,
-                                                           int nb) {
+                                                           int nb, const int4 *tiles) {
     __shared__ uint64_t sk[RS_TILE];
     __shared__ uint32_t sv[RS_TILE];
     __shared__ uint32_t wc[RS_WARPS][256];   // per-warp digit counts, then per-warp offsets within a digit
     __shared__ uint32_t dstart[256];         // first tile position of each digit
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     const unsigned lt = (1u << lane) - 1u;
-    const int base = blockIdx.x * RS_TILE;
-    const int cnt = min(RS_TILE, n - base);
+    const int4 tl = rs_tile(tiles, n, nb);
+    const int base = tl.x;
+    const int cnt = tl.y;
     for (int k = t; k < RS_WARPS * 256; k += RS_THREADS) (&wc[0][0])[k] = 0u;
     __syncthreads();
     uint64_t key[RS_ITEMS];
@@ -329,7 +413,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint64_t *kin, 
         if (p < cnt) {
             const uint64_t kk = sk[p];
             const int d = (int)((kk >> shift) & 255u);
-            const uint32_t g = off[d * nb + blockIdx.x] + (uint32_t)p - dstart[d];
+            const uint32_t g = off[tl.z + d * tl.w] + (uint32_t)p - dstart[d];
             kout[g] = kk;
             vout[g] = sv[p];
         }
@@ -343,7 +427,8 @@ __global__ void k_u32_to_i32_copy(const uint32_t *a, int *b, int n) {
 
 // gather all particle arrays through the permutation
 __global__ void k_permute(const double *F, double *F2, int64_t cap, int n, const uint32_t *perm, const int64_t *id,
-                          int64_t *id2, const int32_t *slot, int32_t *slot2, const int32_t *mat, int32_t *mat2) {
+                          int64_t *id2, const int32_t *slot, int32_t *slot2, const int32_t *mat, int32_t *mat2,
+                          const int *prun, int *prun2) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const int src = (int)perm[k];
@@ -352,23 +437,28 @@ __global__ void k_permute(const double *F, double *F2, int64_t cap, int n, const
     id2[k] = id[src];
     slot2[k] = slot[src];
     mat2[k] = mat[src];
+    prun2[k] = prun[src];
 }
 
 // ---------------------------------------------------------------------------
 // octree
 
-__global__ void k_tree_init(int n, int *meta, int *start, int *count, int *level, int *parent, int *first_child,
-                            int *n_child) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
+// level 0: one root per run (cell r = run r)
+__global__ void k_tree_init(int R, const int4 *info, int *meta, int *start, int *count, int *level, int *parent,
+                            int *first_child, int *n_child) {
+    for (int r = threadIdx.x; r < R; r += blockDim.x) {
+        const int4 q = info[r];
+        start[r] = q.x;
+        count[r] = q.y;
+        level[r] = 0;
+        parent[r] = -1;
+        first_child[r] = -1;
+        n_child[r] = 0;
+    }
+    if (threadIdx.x == 0) {
         for (int k = 0; k < META_N; ++k) meta[k] = 0;
         meta[0] = 0;
-        meta[1] = 1;
-        start[0] = 0;
-        count[0] = n;
-        level[0] = 0;
-        parent[0] = -1;
-        first_child[0] = -1;
-        n_child[0] = 0;
+        meta[1] = R;
     }
 }
 
@@ -632,7 +722,10 @@ int sph_tree_reserve(sph_ctx *ctx, int64_t n) {
         t.cap = c;
     }
     if (!t.meta) SPH_TRY(dalloc(ctx, &t.meta, META_N));
-    if (!t.rb) SPH_TRY(dalloc(ctx, &t.rb, 8 + MAX_LEVELS));
+    if (t.rb_cap < ctx->runs.cap_R) {
+        SPH_TRY(dalloc(ctx, &t.rb, (int64_t)RB_STRIDE * ctx->runs.cap_R));
+        t.rb_cap = ctx->runs.cap_R;
+    }
     Sort &s = ctx->sort;
     if (s.cap < n) {
         const int64_t c = n + n / 8 + 1024;
@@ -640,11 +733,12 @@ int sph_tree_reserve(sph_ctx *ctx, int64_t n) {
         SPH_TRY(dalloc(ctx, &s.k1, c));
         SPH_TRY(dalloc(ctx, &s.v0, c));
         SPH_TRY(dalloc(ctx, &s.v1, c));
-        const int nb = sph_div_up(c, RS_TILE);
-        SPH_TRY(dalloc(ctx, &s.hist, 256 * (int64_t)nb));
-        SPH_TRY(dalloc(ctx, &s.hoff, 256 * (int64_t)nb));
-        s.nblocks_cap = nb;
         s.cap = c;
+    }
+    if (s.nblocks_cap < ctx->runs.cap_T) {   // tiles of all runs (each run starts a tile)
+        SPH_TRY(dalloc(ctx, &s.hist, 256 * (int64_t)ctx->runs.cap_T));
+        SPH_TRY(dalloc(ctx, &s.hoff, 256 * (int64_t)ctx->runs.cap_T));
+        s.nblocks_cap = ctx->runs.cap_T;
     }
     if (!ctx->scan.part) {
         SPH_TRY(dalloc(ctx, &ctx->scan.part, SCAN_BLOCKS + 1));
@@ -655,14 +749,16 @@ int sph_tree_reserve(sph_ctx *ctx, int64_t n) {
 
 static int radix_sort(sph_ctx *ctx, int n) {
     Sort &s = ctx->sort;
-    const int nb = sph_div_up(n, RS_TILE);
+    const int nb = ctx->runs.T;
+    const int4 *tiles = ctx->runs.tiles;
+    static_assert(RS_TILE == RUN_TILE, "run tiles are radix tiles");
     uint64_t *ka = s.k0, *kb = s.k1;
     uint32_t *va = s.v0, *vb = s.v1;
     for (int pass = 0; pass < 8; ++pass) {
         const int shift = pass * 8;
-        k_rs_hist<<<nb, RS_THREADS, 0, ctx->stream>>>(ka, n, shift, s.hist, nb); ++ctx->launches;
+        k_rs_hist<<<nb, RS_THREADS, 0, ctx->stream>>>(ka, n, shift, s.hist, nb, tiles); ++ctx->launches;
         SPH_TRY(sph_scan_exclusive(ctx, (const int *)s.hist, (int *)s.hoff, nullptr, 256 * nb, nullptr));
-        k_rs_scatter<<<nb, RS_THREADS, 0, ctx->stream>>>(ka, va, kb, vb, n, shift, s.hoff, nb); ++ctx->launches;
+        k_rs_scatter<<<nb, RS_THREADS, 0, ctx->stream>>>(ka, va, kb, vb, n, shift, s.hoff, nb, tiles); ++ctx->launches;
         std::swap(ka, kb);
         std::swap(va, vb);
     }
@@ -679,15 +775,21 @@ int sph_sort_and_build(sph_ctx *ctx) {
     SPH_TRY(sph_tree_reserve(ctx, n));
     cudaStream_t st = ctx->stream;
     // root box
-    k_bbox_partial<<<BOX_BLOCKS, 256, 0, st>>>(x, y, z, n, ctx->scratch_d); ++ctx->launches;
-    k_bbox_final<<<1, 256, 0, st>>>(ctx->scratch_d, BOX_BLOCKS, ctx->cfg.theta, t.rb); ++ctx->launches;
-    k_tree_init<<<1, 32, 0, st>>>(n, t.meta, t.start, t.count, t.level, t.parent, t.first_child, t.n_child); ++ctx->launches;
-    k_keys<<<sph_div_up(n, 256), 256, 0, st>>>(x, y, z, n, t.rb, ctx->sort.k0, ctx->sort.v0, t.meta + META_ERR); ++ctx->launches;
+    // root cube of every run (one block per tile, then one per run)
+    const Runs &R = ctx->runs;
+    k_bbox_tiles<<<R.T, 256, 0, st>>>(x, y, z, R.tiles, R.part); ++ctx->launches;
+    k_bbox_runs<<<R.R, 256, 0, st>>>(R.part, R.info, ctx->cfg.theta, t.rb); ++ctx->launches;
+    k_tree_init<<<1, 256, 0, st>>>(R.R, R.info, t.meta, t.start, t.count, t.level, t.parent, t.first_child,
+                                   t.n_child); ++ctx->launches;
+    k_keys_runs<<<sph_div_up(n, 256), 256, 0, st>>>(x, y, z, n, t.rb, R.prun, ctx->sort.k0, ctx->sort.v0,
+                                                    t.meta + META_ERR); ++ctx->launches;
     SPH_TRY(radix_sort(ctx, n));
     // permute the particle state into key order
     k_permute<<<sph_div_up(n, 256), 256, 0, st>>>(ctx->F, ctx->F2, cap, n, ctx->sort.v0, ctx->id, ctx->id2,
-                                                  ctx->slot, ctx->slot2, ctx->mat, ctx->mat2); ++ctx->launches;
+                                                  ctx->slot, ctx->slot2, ctx->mat, ctx->mat2, R.prun,
+                                                  ctx->runs.prun2); ++ctx->launches;
     std::swap(ctx->F, ctx->F2);
+    std::swap(ctx->runs.prun, ctx->runs.prun2);
     std::swap(ctx->id, ctx->id2);
     std::swap(ctx->slot, ctx->slot2);
     std::swap(ctx->mat, ctx->mat2);

@@ -38,6 +38,7 @@ EXPORTS = [
     "sph_prologue", "sph_step", "sph_get_time", "sph_diagnostics", "sph_run_pass", "sph_get_order",
     "sph_get_neighbors", "sph_get_tree", "sph_get_grav_list", "sph_get_timings", "sph_step_timed",
     "sph_get_counters", "sph_probe_peak", "sph_morton_order_noalloc",
+    "sph_add_run", "sph_remove_run", "sph_list_runs", "sph_run_info", "sph_download_run", "sph_run_diagnostics",
 ]
 NOALLOC_MAX_N = 131072
 SEGMENTS = ["kdp", "tree", "dens_list", "dens", "eos", "drvt_list", "drvt", "hydro_list", "hydro", "grav_list",
@@ -104,6 +105,14 @@ def load() -> C.CDLL:
     L.sph_get_grav_list.argtypes = [P, C.c_int64, C.POINTER(C.c_int64), P, C.c_int64, C.POINTER(C.c_int64), P, P,
                                     C.c_int64, C.POINTER(C.c_int64), P, P]
     L.sph_get_timings.argtypes = [P, P, C.c_int, C.POINTER(C.c_int)]
+    L.sph_add_run.argtypes = [P, C.c_int64, P, C.c_int64, P, P, C.c_double, C.c_double, C.c_int,
+                              C.POINTER(C.c_int64)]
+    L.sph_remove_run.argtypes = [P, C.c_int64]
+    L.sph_list_runs.argtypes = [P, P, C.c_int, C.POINTER(C.c_int)]
+    L.sph_run_info.argtypes = [P, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                               C.POINTER(C.c_int64)]
+    L.sph_download_run.argtypes = [P, C.c_int64, P, C.c_int64, P, P]
+    L.sph_run_diagnostics.argtypes = [P, C.c_int64, P]
     _lib = L
     return L
 
@@ -191,6 +200,52 @@ class Context:
 
     def prologue(self):
         self._check(self.L.sph_prologue(self.h))
+
+    # several runs in one context ------------------------------------------------
+    def add_run(self, F: np.ndarray, ids=None, mats=None, time=0.0, init_smth=False, dt=0.0, forces_valid=False):
+        """appends a run (advanced with the others from the next step on); returns its handle"""
+        F = np.ascontiguousarray(F, np.float64)
+        assert F.shape[0] == NFIELD
+        ids = None if ids is None else np.ascontiguousarray(ids, np.int64)
+        mats = None if mats is None else np.ascontiguousarray(mats, np.int32)
+        flags = (1 if init_smth else 0) | (2 if forces_valid else 0)
+        h = C.c_int64()
+        self._check(self.L.sph_add_run(self.h, F.shape[1], _ptr(F), F.shape[1], _ptr(ids), _ptr(mats), float(time),
+                                       float(dt), flags, C.byref(h)))
+        self.n = self.n_particles()
+        return h.value
+
+    def remove_run(self, handle: int):
+        self._check(self.L.sph_remove_run(self.h, int(handle)))
+        self.n = self.n_particles()
+
+    def runs(self):
+        n = C.c_int()
+        self._check(self.L.sph_list_runs(self.h, None, 0, C.byref(n)))
+        hs = np.zeros(max(1, n.value), np.int64)
+        self._check(self.L.sph_list_runs(self.h, _ptr(hs), len(hs), C.byref(n)))
+        return hs[:n.value].tolist()
+
+    def run_info(self, handle: int):
+        n, t, dt, st = C.c_int64(), C.c_double(), C.c_double(), C.c_int64()
+        self._check(self.L.sph_run_info(self.h, int(handle), C.byref(n), C.byref(t), C.byref(dt), C.byref(st)))
+        return dict(n=n.value, time=t.value, dt=dt.value, steps=st.value)
+
+    def n_particles(self):
+        return sum(self.run_info(h)["n"] for h in self.runs())
+
+    def download_run(self, handle: int):
+        n = self.run_info(handle)["n"]
+        out = np.empty((NFIELD, n), np.float64)
+        ids = np.empty(n, np.int64)
+        mats = np.empty(n, np.int32)
+        self._check(self.L.sph_download_run(self.h, int(handle), _ptr(out), n, _ptr(ids), _ptr(mats)))
+        return out, ids, mats
+
+    def run_diagnostics(self, handle: int):
+        out = np.zeros(8)
+        self._check(self.L.sph_run_diagnostics(self.h, int(handle), _ptr(out)))
+        return out
 
     def step(self, n_steps=1):
         self._check(self.L.sph_step(self.h, int(n_steps)))

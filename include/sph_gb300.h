@@ -165,8 +165,28 @@ int sph_step(sph_ctx *ctx, int n_steps);
 int sph_get_time(const sph_ctx *ctx, double *time, double *dt, int64_t *step);
 
 /* Conserved quantities in FP64: E = sum m (u + v^2/2 + pot/2), P = sum m v,
- * L = sum m x cross v.  out[0] = E, out[1..3] = P, out[4..6] = L, out[7] = sum m. */
+ * L = sum m x cross v.  out[0] = E, out[1..3] = P, out[4..6] = L, out[7] = sum m.
+ * Summed over the context's runs. */
 int sph_diagnostics(sph_ctx *ctx, double out[8]);
+
+/* ---- several runs in one context (batching and serving) -------------------
+ * No counterpart in the reference, which advances one ParticleSystem per
+ * process (main.cpp:69-173).  A context holds any number of independent runs
+ * (impacts of their own size); each has its own root cube, octree, time and
+ * global dt (getTimeStepGlobal per run, integral.h:4-20), and one set of
+ * launches per pass advances all of them.  sph_upload makes a context with one
+ * run; sph_add_run appends a run (its handle is returned) and may be called
+ * between steps; a run added without valid forces takes its first sph_step as
+ * its prologue (main.cpp:92-105: forces and dt, no kick).  sph_remove_run
+ * drops a run's particles; sph_download_run copies one run back in its upload
+ * order.  Results of a run do not depend on the other runs in the context. */
+int sph_add_run(sph_ctx *ctx, int64_t n, const double *fields, int64_t ld, const int64_t *id,
+                const int32_t *material, double time, double dt, int flags, int64_t *handle);
+int sph_remove_run(sph_ctx *ctx, int64_t handle);
+int sph_list_runs(sph_ctx *ctx, int64_t *handles, int cap, int *n_runs);
+int sph_run_info(sph_ctx *ctx, int64_t handle, int64_t *n, double *time, double *dt, int64_t *steps);
+int sph_download_run(sph_ctx *ctx, int64_t handle, double *fields, int64_t ld, int64_t *id, int32_t *material);
+int sph_run_diagnostics(sph_ctx *ctx, int64_t handle, double out[8]);
 
 /* ---- inspection (tests, tooling) ----------------------------------------- */
 /* Runs only the given pass on the current state (positions unchanged):

@@ -1,0 +1,64 @@
+"""Several runs in one context (the batched path): each run's state after
+any sequence of steps is bit-identical to the same run advanced alone, in
+both precisions, including runs removed and runs added between steps."""
+import numpy as np
+import pytest
+
+from helpers import device_context, small_impact, tillotson_materials
+
+pytestmark = pytest.mark.gpu
+
+
+def _bodies():
+    return [small_impact(n_target=nt, n_impactor=ni, seed=sd)[:3]
+            for nt, ni, sd in ((1500, 150, 21), (700, 120, 22), (2400, 300, 23))]
+
+
+def _alone(body, prec, steps):
+    F, ids, mats = body
+    ctx = device_context(tillotson_materials(), precision=prec)
+    ctx.upload(F, ids, mats)
+    ctx.prologue()
+    ctx.step(steps)
+    out = ctx.download()
+    info = ctx.time()
+    ctx.close()
+    return out, info
+
+
+def _same(a, b):
+    (Fa, ida, ma), (Fb, idb, mb) = a, b
+    assert np.array_equal(ida, idb) and np.array_equal(ma, mb)
+    assert np.array_equal(Fa, Fb), float(np.max(np.abs(Fa - Fb)))
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_runs_in_a_mix_equal_runs_alone(prec):
+    bodies = _bodies()
+    ctx = device_context(tillotson_materials(), precision=prec)
+    hs = [ctx.add_run(*b) for b in bodies]
+    ctx.step(1 + 4)              # the first step is every run's prologue
+    for h, b in zip(hs, bodies):
+        alone, (t, dt, st) = _alone(b, prec, 4)
+        _same(ctx.download_run(h), alone)
+        info = ctx.run_info(h)
+        assert info["steps"] == 4 and info["time"] == t and info["dt"] == dt
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_runs_removed_and_added_between_steps(prec):
+    bodies = _bodies()
+    ctx = device_context(tillotson_materials(), precision=prec)
+    h0 = ctx.add_run(*bodies[0])
+    h1 = ctx.add_run(*bodies[1])
+    ctx.step(1 + 2)
+    ctx.remove_run(h0)           # the first run leaves, the second moves down
+    h2 = ctx.add_run(*bodies[2])  # a new run joins: its next step is its prologue
+    ctx.step(1 + 3)
+    assert ctx.runs() == [h1, h2]
+    _same(ctx.download_run(h1), _alone(bodies[1], prec, 6)[0])
+    _same(ctx.download_run(h2), _alone(bodies[2], prec, 3)[0])
+    # diagnostics per run add up to the context's
+    tot = ctx.diagnostics()
+    per = ctx.run_diagnostics(h1) + ctx.run_diagnostics(h2)
+    assert np.allclose(tot, per, rtol=1e-12, atol=0.0)
