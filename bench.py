@@ -59,6 +59,10 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched sweep and the serving window")
+    ap.add_argument("--batch-runs", type=int, default=256)
+    ap.add_argument("--batch-steps", type=int, default=100)
+    ap.add_argument("--serve-s", type=float, default=60.0, help="seconds of Poisson arrivals (2 per second)")
     return ap.parse_args()
 
 
@@ -355,12 +359,59 @@ def main():
                                     "unit": "TFLOP/s", "frac": ach64 / peak64 if peak64 else None},
                        "clocks": f["clocks"], "gpu_launches": int(f["launches"])}
         out["drift"]["fp64"] = f["drift"]
+    if not a.no_batch and world == 1:
+        out.update(batch_and_serving(a, device))
     if not a.no_cpu:
         v_cpu, el_cpu, cores = cpu_sample(a.cpu_n, 1)
         out["cpu_baseline"] = {"value": v_cpu, "unit": "particle-steps/s", "cores": cores, "kind": "port",
                                "sample": f"oracle restatement (OpenMP) on the same geometry at {a.cpu_n} particles, "
                                          f"1 step after the prologue ({el_cpu:.1f} s)"}
+        for k in ("batch", "serving"):
+            if k in out:
+                out[k]["vs_cpu_baseline"] = out[k]["value"] / v_cpu
     print(json.dumps(out))
+
+
+def batch_and_serving(a, device):
+    """the batched sweep (256 impacts of uneven size, 100 steps each, one context) and a window of
+    the serving loop (Poisson arrivals at 2 per second, continuous batching), both mixed precision"""
+    from fdps_sph_gb300 import ic, serve
+    res = {}
+    bt = serve.sweep(a.batch_runs, a.batch_steps, device=device)
+    res["batch"] = {"metric": "aggregate particle-steps/s, batched sweep", "value": bt["particle_steps_per_s"],
+                    "unit": "particle-steps/s", "runs": bt["runs"], "steps_per_run": bt["steps_per_run"],
+                    "particles": bt["particles"], "batched_steps": bt["batched_steps"], "wall_s": bt["wall_s"],
+                    "step_latency_s": bt["step_latency_s"], "time_to_completion_s": bt["time_to_completion_s"],
+                    "config": "impacts with N log-uniform 5e3-2e5, mass ratio U[0.05, 0.5], angle U[0, 75] deg, "
+                              "speed U[1, 2] v_esc, iron/dunite tables; wall time includes the host IC generation"}
+    # steps per request scaled by 1/10 (20-200) so that requests complete inside the short window;
+    # `python -m fdps_sph_gb300.serve serve --duration 600` runs the unscaled stream
+    reqs = serve.poisson_requests(4, 2.0, a.serve_s, 1e4, 5e5, 20, 200)
+    srv = serve.Server("mixed", device)
+    try:
+        rep = srv.run(reqs, duration=a.serve_s, drain=False)
+    finally:
+        srv.close()
+    # the plain FP64 per-run path on a request-sized impact (100k particles), alone
+    F, ids, mats, _ = ic.sweep_impact(np.random.default_rng(5), 1e5, 1e5 + 1, 5)
+    ctx = serve.make_context("fp64", device)
+    ctx.upload(F, ids, mats)
+    ctx.prologue()
+    ms = ctx.step_timed(3)
+    ctx.close()
+    v64 = F.shape[1] * 3 / (ms * 1e-3)
+    res["serving"] = {"metric": "aggregate particle-steps/s, serving loop", "value": rep["particle_steps_per_s"],
+                      "unit": "particle-steps/s", "requests_arrived": len(reqs), "completed": rep["completed"],
+                      "resident_at_end": rep["resident_at_end"], "queued_at_end": rep["queued_at_end"],
+                      "window_s": a.serve_s, "step_latency_s": rep["step_latency_s"],
+                      "time_to_completion_s": rep["time_to_completion_s"],
+                      "fp64_per_run_value": v64, "vs_fp64_per_run": rep["particle_steps_per_s"] / v64,
+                      "config": "Poisson arrivals at 2/s; N log-uniform 1e4-5e5; 20-200 steps per request (the "
+                                "serving configuration's 200-2000 scaled by 1/10 to fit the window); parameters as "
+                                "the sweep; initial states built by a client thread at arrival; admission by HBM "
+                                "footprint, state resident, backfill as runs finish; the window ends the "
+                                "measurement (runs still resident are not drained)"}
+    return res
 
 
 if __name__ == "__main__":

@@ -400,7 +400,7 @@ int sph_ctx_destroy(sph_ctx *ctx) {
                     ctx->sup.units, ctx->tree.cinfo, ctx->sup.r2, ctx->sup.m, ctx->sup.vR, ctx->sup.cvR,
                     ctx->sup.umark, ctx->sup.uoff, ctx->sup.uidx, ctx->runs.prun, ctx->runs.prun2,
                     ctx->runs.tiles, ctx->runs.info, ctx->runs.dt_dev, ctx->runs.part, ctx->runs.out,
-                    ctx->runs.damp};
+                    ctx->runs.damp, ctx->sup.soff, ctx->sup.need, ctx->sup.uover};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (void *p : ctx->table_allocs) cudaFree(p);
@@ -752,9 +752,17 @@ int sph_get_neighbors(sph_ctx *ctx, int mode, int64_t k, int32_t *out, int64_t c
     int c = 0;
     SPH_CUDA(ctx, cudaMemcpy(&c, L.cnt + k, sizeof(int), cudaMemcpyDeviceToHost));
     *n = c;
-    const int64_t m = std::min<int64_t>(std::min<int64_t>(c, cap), L.K);
-    if (out && m > 0)
-        SPH_CUDA(ctx, cudaMemcpy(out, L.nbr + (int64_t)k * L.pitch, sizeof(int32_t) * m, cudaMemcpyDeviceToHost));
+    const int64_t m = std::min<int64_t>(c, cap);
+    const int64_t m0 = std::min<int64_t>(m, L.K);   // the row; the rest is in the particle's spill range
+    if (out && m0 > 0)
+        SPH_CUDA(ctx, cudaMemcpy(out, L.nbr + (int64_t)k * L.pitch, sizeof(int32_t) * m0, cudaMemcpyDeviceToHost));
+    if (out && m > m0) {
+        const RowMap rm = ctx->sup.map();
+        if (!rm.soff) return sph_fail(ctx, SPH_ERR_STATE, "row of particle %lld has no spill range", (long long)k);
+        int so = 0;
+        SPH_CUDA(ctx, cudaMemcpy(&so, rm.soff + k, sizeof(int), cudaMemcpyDeviceToHost));
+        SPH_CUDA(ctx, cudaMemcpy(out + m0, L.nbr + rm.main + so, sizeof(int32_t) * (m - m0), cudaMemcpyDeviceToHost));
+    }
     return SPH_OK;
 }
 
@@ -850,7 +858,7 @@ int sph_get_counters(sph_ctx *ctx, int64_t out[16]) {
     out[12] = ctx->sup.n_units;
     out[13] = ctx->sup.K;
     out[14] = w[7];
-    out[15] = 0;
+    out[15] = ctx->sup.spill_on ? ctx->sup.spilled : 0;   // entries in spill ranges (rows longer than K)
     out[0] = ctx->launches;
     out[1] = w[0];
     out[2] = w[1];

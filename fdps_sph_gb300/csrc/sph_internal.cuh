@@ -26,6 +26,7 @@ constexpr int ERR_SPH_LIST_OVERFLOW = 1;
 constexpr int ERR_CELL_OVERFLOW = 2;
 constexpr int ERR_GRAV_OVERFLOW = 4;
 constexpr int ERR_NONFINITE = 8;
+constexpr int ERR_SPH_STACK = 32;         // SPH walk stack overflow
 
 // Double-float accumulation in FP32 (Knuth's TwoSum): hi + lo carries a
 // running sum to about 2^-44 relative without touching the FP64 pipe, which
@@ -55,6 +56,31 @@ __device__ __forceinline__ float sqrt_a(float x) {
     float y;
     asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
+}
+
+// Neighbour rows: particle i's first K entries at i * K; the rare particles
+// with more (isolated particles whose h grew towards the body's size have
+// thousands) continue in a spill range of the same allocation, entries K..
+// at main + soff[i] (main = the row block's size; soff: exclusive prefix of the
+// spill lengths, n + 1 entries, multiples of 8).  soff == nullptr: no spill.
+struct RowMap {
+    int K = 0;
+    int64_t main = 0;
+    const int *soff = nullptr;
+};
+
+// start of segment `seg` (0 = the row, 1 = its spill) of particle i's c entries, and its length
+__device__ __forceinline__ int64_t row_seg(const RowMap &m, int64_t i, int seg, int c, int *len) {
+    if (seg == 0) {
+        *len = c < m.K ? c : m.K;
+        return i * m.K;
+    }
+    *len = c - m.K;
+    return (*len > 0 && m.soff) ? m.main + m.soff[i] : 0;
+}
+
+__device__ __forceinline__ int row_spill_cap(const RowMap &m, int64_t i) {
+    return m.soff ? m.soff[i + 1] - m.soff[i] : 0;
 }
 
 // Mixed-precision tail of a density pass (force.h:32-41): rho = max(floor,
@@ -153,6 +179,23 @@ struct SphSuper {
     float *vR = nullptr, *cvR = nullptr;
     int *umark = nullptr, *uoff = nullptr, *uidx = nullptr;
     int64_t cap_cells = 0;
+    // spill of the rows longer than K (RowMap): offsets, their capacity, units holding such rows
+    int64_t main = 0;             // K * rows: where the spill ranges start in nbr / r2 / m / the lists
+    int64_t spill_cap = 0;        // entries each array holds beyond `main`
+    int *soff = nullptr;          // [n + 1]
+    int *need = nullptr;          // [n + 1] scratch
+    int *uover = nullptr;         // per unit: some row of the unit is longer than K
+    bool spill_on = false;        // soff holds this sort's spill layout
+    int64_t spill_alloc = 0;      // spill_cap the arrays were allocated with
+    int64_t cap_soff = 0, cap_uover = 0;
+    int64_t spilled = 0;          // entries spilled at the last layout (counter)
+    RowMap map() const {
+        RowMap r;
+        r.K = K;
+        r.main = main;
+        r.soff = spill_on ? soff : nullptr;
+        return r;
+    }
 };
 
 struct Scan {

@@ -31,6 +31,7 @@ namespace sph {
 constexpr int UNIT = 32;
 constexpr float KAPPA = 1.06f;   // measured at 1M: 1.15 -> 13.7 ms, 1.10 -> 12.9, 1.06 -> 12.6, 1.03 -> 13.0 (repairs)
 constexpr int NB_WARPS = 4;
+constexpr int ROW_K_MAX = 512;   // widest row block; longer rows continue in spill ranges (RowMap)
 constexpr int NB_CAND = 128;   // raw candidate indices per warp
 constexpr int NB_SURV = 64;    // culled candidates staged for the pair test
 constexpr int NB_STACK = 176;   // depth-first: at most 21 levels x 7 pending siblings + 8
@@ -120,8 +121,8 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
            double *__restrict__ hsup, const float4 *__restrict__ xh,
            const float4 *__restrict__ xl, const float *__restrict__ H2f, const int *__restrict__ prun, WalkTree T,
            int *__restrict__ sup,
-           float *__restrict__ sup_r2, float *__restrict__ sup_m, int *__restrict__ cnt, int K, int64_t stride, int *err,
-           int *maxcnt) {
+           float *__restrict__ sup_r2, float *__restrict__ sup_m, int *__restrict__ cnt, RowMap rm, int *uover,
+           int *err, int *maxcnt) {
     // cells to visit: (first_child, -n_child) for an internal cell, (start, count) for a leaf
     __shared__ int2 s_stack[NB_WARPS][NB_STACK];
     __shared__ int s_cand[NB_WARPS][NB_CAND];
@@ -136,7 +137,9 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int w = blockIdx.x * NB_WARPS + warp;
     if (w >= n_units) return;   // warp-uniform
-    const int2 U = units[uidx ? uidx[w] : w];
+    const int uid = uidx ? uidx[w] : w;
+    const int2 U = units[uid];
+    const int K = rm.K;
     const bool valid = lane < U.y;
     const int i = U.x + (valid ? lane : 0);
     const double xi = x[i], yi = y[i], zi = z[i];
@@ -162,24 +165,38 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
     int2 *stack = s_stack[warp];
     int *cand = s_cand[warp];
     int count = 0, nc = 0;
-    int *row = sup + (int64_t)i * stride;
-    float *rrow = sup_r2 + (int64_t)i * stride;
-    float *mrow = sup_m + (int64_t)i * stride;
-    // writes the lane's 8 buffered entries ending at `count` as full sectors
+    int *row = sup + (int64_t)i * K;
+    float *rrow = sup_r2 + (int64_t)i * K;
+    float *mrow = sup_m + (int64_t)i * K;
+    // the spill range continues the row at entry K (its capacity: scap entries)
+    const int scap = valid ? row_spill_cap(rm, i) : 0;
+    const int64_t sbase = scap > 0 ? rm.main + rm.soff[i] - K : 0;   // entry k >= K at sbase + k
+    // writes the lane's 8 buffered entries ending at `count` as full sectors (in the row, or in
+    // its spill range: K is a multiple of 8, so a sector never straddles the two)
     auto put8 = [&]() {
         const int k0 = count - 8;
-        if (k0 + 8 <= K) {
+        int *rw = row;
+        float *rr = rrow, *rm_ = mrow;
+        int kk = k0;
+        bool ok = k0 + 8 <= K;
+        if (!ok && k0 >= K && k0 + 8 <= K + scap) {
+            rw = sup + sbase;
+            rr = sup_r2 + sbase;
+            rm_ = sup_m + sbase;
+            ok = true;
+        }
+        if (ok) {
             const int4 a = make_int4(s_wj[warp][0][lane], s_wj[warp][1][lane], s_wj[warp][2][lane], s_wj[warp][3][lane]);
             const int4 b = make_int4(s_wj[warp][4][lane], s_wj[warp][5][lane], s_wj[warp][6][lane], s_wj[warp][7][lane]);
             const float4 c = make_float4(s_wr[warp][0][lane], s_wr[warp][1][lane], s_wr[warp][2][lane], s_wr[warp][3][lane]);
             const float4 d = make_float4(s_wr[warp][4][lane], s_wr[warp][5][lane], s_wr[warp][6][lane], s_wr[warp][7][lane]);
-            reinterpret_cast<int4 *>(row + k0)[0] = a;
-            reinterpret_cast<int4 *>(row + k0)[1] = b;
-            reinterpret_cast<float4 *>(rrow + k0)[0] = c;
-            reinterpret_cast<float4 *>(rrow + k0)[1] = d;
-            reinterpret_cast<float4 *>(mrow + k0)[0] =
+            reinterpret_cast<int4 *>(rw + kk)[0] = a;
+            reinterpret_cast<int4 *>(rw + kk)[1] = b;
+            reinterpret_cast<float4 *>(rr + kk)[0] = c;
+            reinterpret_cast<float4 *>(rr + kk)[1] = d;
+            reinterpret_cast<float4 *>(rm_ + kk)[0] =
                 make_float4(s_wm[warp][0][lane], s_wm[warp][1][lane], s_wm[warp][2][lane], s_wm[warp][3][lane]);
-            reinterpret_cast<float4 *>(mrow + k0)[1] =
+            reinterpret_cast<float4 *>(rm_ + kk)[1] =
                 make_float4(s_wm[warp][4][lane], s_wm[warp][5][lane], s_wm[warp][6][lane], s_wm[warp][7][lane]);
         }
     };
@@ -280,7 +297,7 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
             const unsigned mask = __ballot_sync(FULLM, ok);
             const int np = __popc(mask);
             if (sp + np > NB_STACK) {
-                if (lane == 0) atomicOr(err, ERR_SPH_LIST_OVERFLOW);
+                if (lane == 0) atomicOr(err, ERR_SPH_STACK);
                 break;
             }
             if (ok) stack[sp + (np - 1 - __popc(mask & ((1u << lane) - 1u)))] = chi;
@@ -292,18 +309,27 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
     if (valid) {
         // the partial last block, entry by entry
         const int k0 = count & ~7;
-        for (int q = 0; q < (count & 7); ++q)
-            if (k0 + q < K) {
-                row[k0 + q] = s_wj[warp][q][lane];
-                rrow[k0 + q] = s_wr[warp][q][lane];
-                mrow[k0 + q] = s_wm[warp][q][lane];
+        for (int q = 0; q < (count & 7); ++q) {
+            const int k = k0 + q;
+            if (k < K) {
+                row[k] = s_wj[warp][q][lane];
+                rrow[k] = s_wr[warp][q][lane];
+                mrow[k] = s_wm[warp][q][lane];
+            } else if (k < K + scap) {
+                sup[sbase + k] = s_wj[warp][q][lane];
+                sup_r2[sbase + k] = s_wr[warp][q][lane];
+                sup_m[sbase + k] = s_wm[warp][q][lane];
             }
-        cnt[i] = count;
-        if (count > K) atomicOr(err, ERR_SPH_LIST_OVERFLOW);
+        }
+        cnt[i] = count;   // the true count, also when the row had no room for all of it
+        if (count > K + scap) atomicOr(err, ERR_SPH_LIST_OVERFLOW);
     }
     int m = valid ? count : 0;
     for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(FULLM, m, o));
-    if (lane == 0) atomicMax(maxcnt, m);
+    if (lane == 0) {
+        atomicMax(maxcnt, m);
+        uover[uid] = m > K ? 1 : 0;   // the unit holds rows that need a spill range
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -452,7 +478,7 @@ __device__ __forceinline__ bool exact_in(float r2, float thr, int j, double xi, 
 template <int MODE>
 __global__ void __launch_bounds__(128)
 k_filter(int n, const int *__restrict__ sup, const float *__restrict__ sup_r2, const int *__restrict__ scnt,
-         int64_t stride, const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
+         RowMap rm, const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
          const double *__restrict__ h, const double *__restrict__ hsup, const float *__restrict__ H2f,
          int *__restrict__ out, int *__restrict__ ocnt, int *err) {
     __shared__ int s_buf[8][128];
@@ -464,34 +490,46 @@ k_filter(int n, const int *__restrict__ sup, const float *__restrict__ sup_r2, c
     const float H2i = (float)H2;
     const double xi = x[i], yi = y[i], zi = z[i];
     const int c = scnt[i];
-    const int *row = sup + (int64_t)i * stride;
-    const float *rrow = sup_r2 + (int64_t)i * stride;
-    int *orow = out + (int64_t)i * stride;
+    const int K = rm.K;
+    int *orow = out + (int64_t)i * K;
+    // the exact list is a subset of the superset row: it fits the row and the same spill range
+    int *ospill = (c > K && rm.soff) ? out + rm.main + rm.soff[i] - K : nullptr;   // entry k >= K at ospill + k
     const int t = threadIdx.x;
     int k2 = 0;
-    for (int k = 0; k < c; k += 8) {
-        const int4 j0 = reinterpret_cast<const int4 *>(row + k)[0], j1 = reinterpret_cast<const int4 *>(row + k)[1];
-        const float4 r0 = reinterpret_cast<const float4 *>(rrow + k)[0], r1 = reinterpret_cast<const float4 *>(rrow + k)[1];
-        const int jj[8] = {j0.x, j0.y, j0.z, j0.w, j1.x, j1.y, j1.z, j1.w};
-        const float rr[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
-        const int m = min(8, c - k);
-        float thr[8];
+    for (int seg = 0; seg < 2; ++seg) {
+        int cs;
+        const int64_t b = row_seg(rm, i, seg, c, &cs);
+        if (cs <= 0) break;
+        const int *row = sup + b;
+        const float *rrow = sup_r2 + b;
+        for (int k = 0; k < cs; k += 8) {
+            const int4 j0 = reinterpret_cast<const int4 *>(row + k)[0], j1 = reinterpret_cast<const int4 *>(row + k)[1];
+            const float4 r0 = reinterpret_cast<const float4 *>(rrow + k)[0],
+                         r1 = reinterpret_cast<const float4 *>(rrow + k)[1];
+            const int jj[8] = {j0.x, j0.y, j0.z, j0.w, j1.x, j1.y, j1.z, j1.w};
+            const float rr[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
+            const int m = min(8, cs - k);
+            float thr[8];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) thr[u] = (MODE == 1 && u < m) ? fmaxf(H2i, H2f[jj[u]]) : H2i;
+            for (int u = 0; u < 8; ++u) thr[u] = (MODE == 1 && u < m) ? fmaxf(H2i, H2f[jj[u]]) : H2i;
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            if (u < m && exact_in(rr[u], thr[u], jj[u], xi, yi, zi, H2, x, y, z, h, MODE == 1)) {
-                s_buf[k2 & 7][t] = jj[u];
-                ++k2;
-                if ((k2 & 7) == 0) {
-                    int4 *dst = reinterpret_cast<int4 *>(orow + k2 - 8);
-                    dst[0] = make_int4(s_buf[0][t], s_buf[1][t], s_buf[2][t], s_buf[3][t]);
-                    dst[1] = make_int4(s_buf[4][t], s_buf[5][t], s_buf[6][t], s_buf[7][t]);
+            for (int u = 0; u < 8; ++u) {
+                if (u < m && exact_in(rr[u], thr[u], jj[u], xi, yi, zi, H2, x, y, z, h, MODE == 1)) {
+                    s_buf[k2 & 7][t] = jj[u];
+                    ++k2;
+                    if ((k2 & 7) == 0) {
+                        int4 *dst = reinterpret_cast<int4 *>((k2 - 8 < K ? orow : ospill) + k2 - 8);
+                        dst[0] = make_int4(s_buf[0][t], s_buf[1][t], s_buf[2][t], s_buf[3][t]);
+                        dst[1] = make_int4(s_buf[4][t], s_buf[5][t], s_buf[6][t], s_buf[7][t]);
+                    }
                 }
             }
         }
     }
-    for (int q = 0; q < (k2 & 7); ++q) orow[(k2 & ~7) + q] = s_buf[q][t];
+    for (int q = 0; q < (k2 & 7); ++q) {
+        const int k = (k2 & ~7) + q;
+        (k < K ? orow : ospill)[k] = s_buf[q][t];
+    }
     ocnt[i] = k2;
 }
 
@@ -500,7 +538,7 @@ k_filter(int n, const int *__restrict__ sup, const float *__restrict__ sup_r2, c
 // partial sums of 32 flushed to FP64, FLAG_GI floor and h update in FP64.
 __global__ void __launch_bounds__(128)
 k_density_sup32(int n, const int *__restrict__ sup, const float *__restrict__ sup_r2, const float *__restrict__ sup_m,
-                const int *__restrict__ scnt, int64_t stride, const double *__restrict__ x,
+                const int *__restrict__ scnt, RowMap rm, const double *__restrict__ x,
                 const double *__restrict__ y, const double *__restrict__ z, const double *__restrict__ m,
                 double *__restrict__ h, const double *__restrict__ hsup, double *__restrict__ dens, float dscale,
                 int *err) {
@@ -512,13 +550,17 @@ k_density_sup32(int n, const int *__restrict__ sup, const float *__restrict__ su
     const float H2i = (float)H2;
     const float invH = 1.0f / (float)Hi;
     const double xi = x[i], yi = y[i], zi = z[i];
-    const int c = scnt[i];
-    const int *row = sup + (int64_t)i * stride;
-    const float *rrow = sup_r2 + (int64_t)i * stride;
-    const float *mrow = sup_m + (int64_t)i * stride;
+    const int c_all = scnt[i];
     float acc_h = 0.0f, acc_l = 0.0f;
     // the index row is read only for the rare entries whose FP32 distance is too close to the
     // threshold to decide (exact_in's band); the stream is r^2 and m_j
+    for (int seg = 0; seg < 2; ++seg) {
+    int c;
+    const int64_t b = row_seg(rm, i, seg, c_all, &c);
+    if (c <= 0) break;
+    const int *row = sup + b;
+    const float *rrow = sup_r2 + b;
+    const float *mrow = sup_m + b;
     for (int k = 0; k < c; k += 8) {
         const float4 r0 = reinterpret_cast<const float4 *>(rrow + k)[0], r1 = reinterpret_cast<const float4 *>(rrow + k)[1];
         const float rr[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
@@ -540,6 +582,7 @@ k_density_sup32(int n, const int *__restrict__ sup, const float *__restrict__ su
             const float p2 = p * p, p4 = p2 * p2;
             df_add(acc_h, acc_l, mj[u] * ((1.0f + s_ * (8.0f + s_ * (25.0f + s_ * 32.0f))) * (p4 * p4)));
         }
+    }
     }
     density_tail32(acc_h + acc_l, invH, dscale, m[i], dens + i, h + i);
 }
@@ -566,6 +609,13 @@ __global__ void k_pack_pos(int n, const double *x, const double *y, const double
     const float ax = (float)x[i], ay = (float)y[i], az = (float)z[i];
     xh[i] = make_float4(ax, ay, az, (float)(m[i] * mscale));
     xl[i] = make_float4((float)(x[i] - (double)ax), (float)(y[i] - (double)ay), (float)(z[i] - (double)az), 0.0f);
+}
+
+// spill range lengths: rows longer than K take round8(count - K) entries beyond the row block
+__global__ void k_spill_need(int n, const int *cnt, int K, int *need) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) need[i] = cnt[i] > K ? ((cnt[i] - K + 7) & ~7) : 0;
+    else if (i == n) need[i] = 0;
 }
 
 }  // namespace sph
@@ -660,25 +710,34 @@ static int walk_units(sph_ctx *ctx, const int *uidx, int n_walk) {
     Tree &t = ctx->tree;
     if (S.K == 0) S.K = 192;
     S.K = (S.K + 7) & ~7;   // rows start on 32-byte boundaries
+    if (!S.uover || S.n_units > S.cap_uover) {
+        SPH_TRY(dalloc_n(ctx, &S.uover, S.cap_units));
+        SPH_CUDA(ctx, cudaMemsetAsync(S.uover, 0, sizeof(int) * S.cap_units, ctx->stream));
+        S.cap_uover = S.cap_units;
+    }
     if (S.rebuilds_step > 0) SPH_TRY(sph_tree_refresh_hmax(ctx));   // cell hmax must follow the current h
     S.rebuilds_step += 1;
     for (int attempt = 0; attempt < 4; ++attempt) {
-        if (!S.nbr || S.pitch < pitch || S.K_alloc != S.K) {
-            if (uidx) {   // a partial walk cannot grow the rows: the others would be lost
+        if (!S.nbr || S.pitch < pitch || S.K_alloc != S.K || S.spill_alloc != S.spill_cap) {
+            if (uidx) {   // a partial walk cannot re-layout the rows: the others would be lost
                 uidx = nullptr;
                 n_walk = S.n_units;
             }
-            SPH_TRY(dalloc_n(ctx, &S.nbr, (int64_t)S.K * pitch));
-            SPH_TRY(dalloc_n(ctx, &S.r2, (int64_t)S.K * pitch));
-            SPH_TRY(dalloc_n(ctx, &S.m, (int64_t)S.K * pitch));
+            if (S.K_alloc != S.K || S.pitch < pitch) S.spill_on = false;   // spill offsets follow K and n
+            S.main = (int64_t)S.K * pitch;
+            const int64_t tot = S.main + S.spill_cap;
+            SPH_TRY(dalloc_n(ctx, &S.nbr, tot));
+            SPH_TRY(dalloc_n(ctx, &S.r2, tot));
+            SPH_TRY(dalloc_n(ctx, &S.m, tot));
             for (int m = 0; m < 2; ++m) {
-                SPH_TRY(dalloc_n(ctx, &ctx->lists[m].nbr, (int64_t)S.K * pitch));
+                SPH_TRY(dalloc_n(ctx, &ctx->lists[m].nbr, tot));
                 SPH_TRY(dalloc_n(ctx, &ctx->lists[m].cnt, pitch));
                 ctx->lists[m].K = ctx->lists[m].K_alloc = S.K;
                 ctx->lists[m].pitch = S.K;   // row stride of the exact lists
             }
             S.pitch = pitch;
             S.K_alloc = S.K;
+            S.spill_alloc = S.spill_cap;
         }
         SPH_CUDA(ctx, cudaMemsetAsync(meta + META_ERR, 0, sizeof(int), ctx->stream));
         SPH_CUDA(ctx, cudaMemsetAsync(meta + META_MAXCNT, 0, sizeof(int), ctx->stream));
@@ -688,8 +747,7 @@ static int walk_units(sph_ctx *ctx, const int *uidx, int n_walk) {
             k_sup_walk<<<blocks, NB_WARPS * 32, 0, ctx->stream>>>(
                 n_walk, S.units, uidx, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
                 FLD(ctx->F, SPH_SMTH, cap), S.hsup, S.pxh, S.pxl, S.H2f, ctx->runs.prun, T, S.nbr, S.r2, S.m,
-                S.cnt, S.K,
-                (int64_t)S.K, meta + META_ERR, meta + META_MAXCNT);
+                S.cnt, S.map(), S.uover, meta + META_ERR, meta + META_MAXCNT);
             ++ctx->launches;
         }
         SPH_CUDA(ctx, cudaGetLastError());
@@ -697,11 +755,42 @@ static int walk_units(sph_ctx *ctx, const int *uidx, int n_walk) {
         SPH_CUDA(ctx, cudaMemcpyAsync(hs, meta + META_ERR, 4 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
         SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         const int errw = hs[0], maxc = hs[META_MAXCNT - META_ERR];
+        if (errw & ERR_SPH_STACK) return sph_fail(ctx, SPH_ERR_CAPACITY, "SPH walk stack overflow");
         if (errw & ERR_SPH_LIST_OVERFLOW) {
-            if (maxc <= S.K) return sph_fail(ctx, SPH_ERR_CAPACITY, "SPH walk stack overflow");
-            S.K = (maxc + maxc / 4 + 16 + 7) & ~7;
-            uidx = nullptr;     // rows were truncated: rebuild everything with the larger capacity
-            n_walk = S.n_units;
+            if (maxc <= ROW_K_MAX && !S.spill_on) {
+                // every row fits a wider block: grow K and rebuild everything
+                S.K = std::min(ROW_K_MAX, (maxc + maxc / 4 + 16 + 7) & ~7);
+                uidx = nullptr;
+                n_walk = S.n_units;
+                continue;
+            }
+            // rows longer than K (the true counts are in cnt) get spill ranges; the units holding
+            // them are walked again (all of them if the spill block had to grow)
+            if (!S.soff || S.cap_soff < n + 1) {
+                SPH_TRY(dalloc_n(ctx, &S.soff, n + 1 + 1024));
+                SPH_TRY(dalloc_n(ctx, &S.need, n + 1 + 1024));
+                S.cap_soff = n + 1 + 1024;
+            }
+            k_spill_need<<<sph_div_up(n + 1, 256), 256, 0, ctx->stream>>>(n, S.cnt, S.K, S.need);
+            ++ctx->launches;
+            SPH_TRY(sph_scan_exclusive(ctx, S.need, S.soff, nullptr, n + 1, ctx->scan.total));
+            SPH_CUDA(ctx, cudaMemcpyAsync(hs, ctx->scan.total, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+            SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            const int64_t need = hs[0];
+            S.spill_on = true;
+            S.spilled = need;
+            if (need > S.spill_cap) {
+                S.spill_cap = need + need / 2 + 4096;   // reallocated at the top of the loop, rows rebuilt
+                continue;
+            }
+            const int grid = 2 * ctx->num_sms;
+            SPH_TRY(sph_scan_exclusive(ctx, S.uover, S.uoff, nullptr, S.n_units, ctx->scan.total));
+            k_unit_compact<<<grid, 256, 0, ctx->stream>>>(S.n_units, S.uover, S.uoff, S.uidx);
+            ++ctx->launches;
+            SPH_CUDA(ctx, cudaMemcpyAsync(hs, ctx->scan.total, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+            SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            uidx = S.uidx;
+            n_walk = hs[0];
             continue;
         }
         S.valid = true;
@@ -713,7 +802,11 @@ static int walk_units(sph_ctx *ctx, const int *uidx, int n_walk) {
     return sph_fail(ctx, SPH_ERR_CAPACITY, "SPH superset capacity could not be grown");
 }
 
-static int build_superset(sph_ctx *ctx) { return walk_units(ctx, nullptr, ctx->sup.n_units); }
+// a full walk after a sort: the previous spill layout belongs to the previous order
+static int build_superset(sph_ctx *ctx) {
+    ctx->sup.spill_on = false;
+    return walk_units(ctx, nullptr, ctx->sup.n_units);
+}
 
 // makes the superset valid for the current h: full walk after a sort, otherwise a repair of
 // the units within reach of particles whose h outgrew the skin
@@ -765,11 +858,11 @@ int sph_build_sph_lists(sph_ctx *ctx, int mode) {
     SphLists &L = ctx->lists[mode];
     if (mode == 0)
         k_filter<0><<<sph_div_up(n, 128), 128, 0, ctx->stream>>>(
-            n, S.nbr, S.r2, S.cnt, (int64_t)S.K, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
+            n, S.nbr, S.r2, S.cnt, S.map(), FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
             FLD(ctx->F, SPH_SMTH, cap), S.hsup, S.H2f, L.nbr, L.cnt, meta + META_ERR);
     else
         k_filter<1><<<sph_div_up(n, 128), 128, 0, ctx->stream>>>(
-            n, S.nbr, S.r2, S.cnt, (int64_t)S.K, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
+            n, S.nbr, S.r2, S.cnt, S.map(), FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
             FLD(ctx->F, SPH_SMTH, cap), S.hsup, S.H2f, L.nbr, L.cnt, meta + META_ERR);
     ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
@@ -785,7 +878,7 @@ int sph_density_from_superset(sph_ctx *ctx) {
     int *meta = ctx->tree.meta;
     SPH_TRY(ensure_superset(ctx));
     k_density_sup32<<<sph_div_up(n, 128), 128, 0, ctx->stream>>>(
-        n, S.nbr, S.r2, S.m, S.cnt, (int64_t)S.K, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap),
+        n, S.nbr, S.r2, S.m, S.cnt, S.map(), FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap),
         FLD(ctx->F, SPH_Z, cap), FLD(ctx->F, SPH_MASS, cap), FLD(ctx->F, SPH_SMTH, cap), S.hsup,
         FLD(ctx->F, SPH_DENS, cap), (float)(1365.0 / 64.0 / (3.141592653589793 * ctx->mscale)), meta + META_ERR);
     ++ctx->launches;

@@ -24,22 +24,24 @@ __global__ void __launch_bounds__(PT) k_density64(int n, const double *__restric
                                                   const double *__restrict__ z, const double *__restrict__ m,
                                                   double *__restrict__ h, double *__restrict__ dens,
                                                   const int *__restrict__ nbr, const int *__restrict__ cnt,
-                                                  int64_t pitch) {
+                                                  RowMap rm) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double xi = x[i], yi = y[i], zi = z[i], hi = h[i];
     const double H = SUPPORT * hi;
     const double invH = 1.0 / H;
     const double norm = kernel_norm(H);
-    const int c = cnt[i];
     double sum = 0.0;
+    for (int seg = 0, c; seg < 2; ++seg) {
+    const int *row = nbr + row_seg(rm, i, seg, cnt[i], &c);
     for (int k = 0; k < c; ++k) {
-        const int j = nbr[(int64_t)i * pitch + k];
+        const int j = row[k];
         const double dx = x[j] - xi, dy = y[j] - yi, dz = z[j] - zi;
         const double r = sqrt(dx * dx + dy * dy + dz * dz);
         double w, g;
         wendland_poly(r * invH, w, g);
         sum += m[j] * w;
+    }
     }
     const double d = fmax(DENS_FLOOR, sum * norm);
     dens[i] = d;
@@ -67,7 +69,7 @@ struct DrvtArgs {
     const double *x, *y, *z, *vx, *vy, *vz, *m, *h, *dens, *snds;
     double *divv, *rx, *ry, *rz, *gradh, *bal;
     const int *nbr, *cnt;
-    int64_t pitch;
+    RowMap rm;
 };
 
 __global__ void __launch_bounds__(PT) k_drvt64(int n, DrvtArgs a) {
@@ -77,9 +79,10 @@ __global__ void __launch_bounds__(PT) k_drvt64(int n, DrvtArgs a) {
     const double hi = a.h[i], rhoi = a.dens[i];
     const double H = SUPPORT * hi, invH = 1.0 / H, norm = kernel_norm(H), ceps = 1.0e-6 * hi;
     double dv = 0.0, r0 = 0.0, r1 = 0.0, r2 = 0.0, gs = 0.0;
-    const int c = a.cnt[i];
+    for (int seg = 0, c; seg < 2; ++seg) {
+    const int *row = a.nbr + row_seg(a.rm, i, seg, a.cnt[i], &c);
     for (int k = 0; k < c; ++k) {
-        const int j = a.nbr[(int64_t)i * a.pitch + k];
+        const int j = row[k];
         const double dx = xi - a.x[j], dy = yi - a.y[j], dz = zi - a.z[j];
         const double mj = a.m[j];
         const double ax = -mj * (ux - a.vx[j]), ay = -mj * (uy - a.vy[j]), az = -mj * (uz - a.vz[j]);
@@ -93,6 +96,7 @@ __global__ void __launch_bounds__(PT) k_drvt64(int n, DrvtArgs a) {
         r1 += gf * (az * dx - ax * dz);
         r2 += gf * (ax * dy - ay * dx);
         gs += mj * (3.0 * norm * w + gf * rr2);
+    }
     }
     gs = -gs / hi;
     gs = 1.0 / (1.0 + hi * gs / (3.0 * rhoi));
@@ -116,7 +120,7 @@ struct HydroArgs {
     const double4 *aux;   // per particle: invH, norm, 1e-6 h, f P / rho^2
     double *ax, *ay, *az, *edot, *dt;
     const int *nbr, *cnt;
-    int64_t pitch;
+    RowMap rm;
 };
 
 __global__ void k_hydro_aux64(int n, const double *h, const double *dens, const double *pres, const double *gradh,
@@ -135,9 +139,10 @@ __global__ void __launch_bounds__(PT) k_hydro64(int n, HydroArgs a) {
     const double4 ai = a.aux[i];
     const double Hi = SUPPORT * hi;
     double a0 = 0.0, a1 = 0.0, a2 = 0.0, e = 0.0, vmax = 0.0;
-    const int c = a.cnt[i];
+    for (int seg = 0, c; seg < 2; ++seg) {
+    const int *row = a.nbr + row_seg(a.rm, i, seg, a.cnt[i], &c);
     for (int k = 0; k < c; ++k) {
-        const int j = a.nbr[(int64_t)i * a.pitch + k];
+        const int j = row[k];
         const double dx = xi - a.x[j], dy = yi - a.y[j], dz = zi - a.z[j];
         const double wx = ux - a.vx[j], wy = uy - a.vy[j], wz = uz - a.vz[j];
         const double rr2 = dx * dx + dy * dy + dz * dz;
@@ -161,6 +166,7 @@ __global__ void __launch_bounds__(PT) k_hydro64(int n, HydroArgs a) {
         a1 -= coef * dy;
         a2 -= coef * dz;
         e += mj * (ai.w + 0.5 * AV) * gws * dvdr;
+    }
     }
     a.ax[i] = a0;
     a.ay[i] = a1;
@@ -268,18 +274,19 @@ __device__ __forceinline__ float df_diff(float ah, float al, float bh, float bl)
 __global__ void __launch_bounds__(PT) k_density32(int n, const float4 *__restrict__ xh, const float4 *__restrict__ xl,
                                                   const double *__restrict__ m, double *__restrict__ h,
                                                   double *__restrict__ dens, const int *__restrict__ nbr,
-                                                  const int *__restrict__ cnt, int64_t pitch, float dscale) {
+                                                  const int *__restrict__ cnt, RowMap rm, float dscale) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4 pih = xh[i], pil = xl[i];
     const double hi = h[i];
     const double H = SUPPORT * hi;
     const float invH = 1.0f / (float)H;
-    const int c = cnt[i];
     float acc_h = 0.0f, acc_l = 0.0f;
     float part = 0.0f;
+    for (int seg = 0, c; seg < 2; ++seg) {
+    const int *row = nbr + row_seg(rm, i, seg, cnt[i], &c);
     for (int k = 0; k < c; ++k) {
-        const int j = nbr[(int64_t)i * pitch + k];
+        const int j = row[k];
         const float4 qh = xh[j], ql = xl[j];
         const float dx = df_diff(qh.x, ql.x, pih.x, pil.x);
         const float dy = df_diff(qh.y, ql.y, pih.y, pil.y);
@@ -293,6 +300,7 @@ __global__ void __launch_bounds__(PT) k_density32(int n, const float4 *__restric
             part = 0.0f;
         }
     }
+    }
     df_add(acc_h, acc_l, part);
     density_tail32(acc_h + acc_l, invH, dscale, m[i], dens + i, h + i);
 }
@@ -303,7 +311,7 @@ struct DrvtArgs32 {
     const double *h, *dens, *snds;
     double *divv, *rx, *ry, *rz, *gradh, *bal;
     const int *nbr, *cnt;
-    int64_t pitch;
+    RowMap rm;
     float kscale;   // (1365/64) / (pi mscale)
 };
 
@@ -338,10 +346,11 @@ __global__ void __launch_bounds__(PT) k_drvt32(int n, DrvtArgs32 a) {
     // kernel normalisation folded out of the pair sums and applied once at the end
     float Dh[5] = {0, 0, 0, 0, 0}, Dl[5] = {0, 0, 0, 0, 0};
     float P[5] = {0, 0, 0, 0, 0};
-    const int c = a.cnt[i];
+    for (int seg = 0, c; seg < 2; ++seg) {
+    const int *row = a.nbr + row_seg(a.rm, i, seg, a.cnt[i], &c);
     int k = 0;
     for (; k + 2 <= c; k += 2) {
-        const int2 jp = *reinterpret_cast<const int2 *>(a.nbr + (int64_t)i * a.pitch + k);
+        const int2 jp = *reinterpret_cast<const int2 *>(row + k);
         const int j0 = jp.x, j1 = jp.y;
         const float4 qh0 = a.xh[j0], ql0 = a.xl[j0], uh0 = a.vh[j0], ul0 = a.vl[j0];
         const float4 qh1 = a.xh[j1], ql1 = a.xl[j1], uh1 = a.vh[j1], ul1 = a.vl[j1];
@@ -356,8 +365,9 @@ __global__ void __launch_bounds__(PT) k_drvt32(int n, DrvtArgs32 a) {
         }
     }
     if (k < c) {
-        const int j = a.nbr[(int64_t)i * a.pitch + k];
+        const int j = row[k];
         drvt_pair32(pih, pil, vih, vil, a.xh[j], a.xl[j], a.vh[j], a.vl[j], invH, Hf, ceps, P);
+    }
     }
     // per-particle tail of force.h:70-76 in FP32
     const float sc = a.kscale * (invH * invH * invH);
@@ -395,7 +405,7 @@ struct HydroArgs32 {
     const double *h;
     double *ax, *ay, *az, *edot, *dt;
     const int *nbr, *cnt;
-    int64_t pitch;
+    RowMap rm;
     float kscale;   // (1365/64) / (pi mscale)
 };
 
@@ -452,10 +462,11 @@ __global__ void __launch_bounds__(PT) k_hydro32(int n, HydroArgs32 a) {
     float Dh[4] = {0, 0, 0, 0}, Dl[4] = {0, 0, 0, 0};
     float P[4] = {0, 0, 0, 0};
     float vmax = 0.0f;
-    const int c = a.cnt[i];
+    for (int seg = 0, c; seg < 2; ++seg) {
+    const int *row = a.nbr + row_seg(a.rm, i, seg, a.cnt[i], &c);
     int k = 0;
     for (; k + 2 <= c; k += 2) {
-        const int2 jp = *reinterpret_cast<const int2 *>(a.nbr + (int64_t)i * a.pitch + k);
+        const int2 jp = *reinterpret_cast<const int2 *>(row + k);
         const int j0 = jp.x, j1 = jp.y;
         const HydroJ32 J0 = load_hydro_j(a, j0), J1 = load_hydro_j(a, j1);
         hydro_pair32(pih, pil, vih, vil, Ai, Bi, J0, P, vmax);
@@ -469,8 +480,9 @@ __global__ void __launch_bounds__(PT) k_hydro32(int n, HydroArgs32 a) {
         }
     }
     if (k < c) {
-        const HydroJ32 J = load_hydro_j(a, a.nbr[(int64_t)i * a.pitch + k]);
+        const HydroJ32 J = load_hydro_j(a, row[k]);
         hydro_pair32(pih, pil, vih, vil, Ai, Bi, J, P, vmax);
+    }
     }
     // kernel normalisation of i (Bi.y = 1 / H_i) and the mass scale, in FP32
     const float sc = a.kscale * (Bi.y * Bi.y * Bi.y);
@@ -1156,11 +1168,11 @@ int sph_pass_density(sph_ctx *ctx, int build_lists) {
     const SphLists &L = ctx->lists[0];
     if (ctx->cfg.precision == SPH_PREC_MIXED) {
         k_density32<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, ctx->xh, ctx->xl, CF(SPH_MASS), CF(SPH_SMTH),
-                                                              CF(SPH_DENS), L.nbr, L.cnt, L.pitch,
+                                                              CF(SPH_DENS), L.nbr, L.cnt, ctx->sup.map(),
                                                               (float)(WNORM / (PI_D * ctx->mscale))); ++ctx->launches;
     } else {
         k_density64<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, CF(SPH_X), CF(SPH_Y), CF(SPH_Z), CF(SPH_MASS),
-                                                              CF(SPH_SMTH), CF(SPH_DENS), L.nbr, L.cnt, L.pitch); ++ctx->launches;
+                                                              CF(SPH_SMTH), CF(SPH_DENS), L.nbr, L.cnt, ctx->sup.map()); ++ctx->launches;
     }
     SPH_CUDA(ctx, cudaGetLastError());
     return sph_nbr_refresh_h(ctx);
@@ -1181,14 +1193,14 @@ int sph_pass_derivative(sph_ctx *ctx, int build_lists) {
     if (ctx->cfg.precision == SPH_PREC_MIXED) {
         DrvtArgs32 a{ctx->xh,     ctx->xl,      ctx->vhf,     ctx->vlf,      CF(SPH_SMTH), CF(SPH_DENS),
                      CF(SPH_SNDS), CF(SPH_DIVV), CF(SPH_ROTX), CF(SPH_ROTY),  CF(SPH_ROTZ), CF(SPH_GRADH),
-                     CF(SPH_BAL),  L.nbr,        L.cnt,        L.pitch,
+                     CF(SPH_BAL),  L.nbr,        L.cnt,        ctx->sup.map(),
                      (float)(WNORM / (PI_D * ctx->mscale))};
         k_drvt32<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, a); ++ctx->launches;
     } else {
         DrvtArgs a{CF(SPH_X),    CF(SPH_Y),    CF(SPH_Z),    CF(SPH_VX),    CF(SPH_VY),   CF(SPH_VZ),
                    CF(SPH_MASS), CF(SPH_SMTH), CF(SPH_DENS), CF(SPH_SNDS),  CF(SPH_DIVV), CF(SPH_ROTX),
                    CF(SPH_ROTY), CF(SPH_ROTZ), CF(SPH_GRADH), CF(SPH_BAL), L.nbr,        L.cnt,
-                   L.pitch};
+                   ctx->sup.map()};
         k_drvt64<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, a); ++ctx->launches;
     }
     SPH_CUDA(ctx, cudaGetLastError());
@@ -1206,7 +1218,7 @@ int sph_pass_hydro(sph_ctx *ctx, int build_lists) {
                                                                     CF(SPH_SNDS), CF(SPH_GRADH), CF(SPH_BAL), hA, hB); ++ctx->launches;
         HydroArgs32 a{ctx->xh,    ctx->xl,    ctx->vhf,   ctx->vlf,       hA,         hB,    CF(SPH_SMTH),
                       CF(SPH_AX), CF(SPH_AY), CF(SPH_AZ), CF(SPH_ENGDOT), CF(SPH_DT), L.nbr, L.cnt,
-                      L.pitch,    (float)(WNORM / (PI_D * ctx->mscale))};
+                      ctx->sup.map(),    (float)(WNORM / (PI_D * ctx->mscale))};
         k_hydro32<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, a); ++ctx->launches;
     } else {
         double4 *aux = (double4 *)ctx->F2;
@@ -1215,7 +1227,7 @@ int sph_pass_hydro(sph_ctx *ctx, int build_lists) {
         HydroArgs a{CF(SPH_X),    CF(SPH_Y),    CF(SPH_Z),     CF(SPH_VX),   CF(SPH_VY),  CF(SPH_VZ),
                     CF(SPH_MASS), CF(SPH_SMTH), CF(SPH_DENS),  CF(SPH_PRES), CF(SPH_SNDS), CF(SPH_GRADH),
                     CF(SPH_BAL),  aux,          CF(SPH_AX),    CF(SPH_AY),   CF(SPH_AZ),  CF(SPH_ENGDOT),
-                    CF(SPH_DT),   L.nbr,        L.cnt,         L.pitch};
+                    CF(SPH_DT),   L.nbr,        L.cnt,         ctx->sup.map()};
         k_hydro64<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, a); ++ctx->launches;
     }
     SPH_CUDA(ctx, cudaGetLastError());

@@ -173,3 +173,27 @@ def config_4m_impact(seed=4096, n_target=3_600_000, n_impactor=400_000):
     (5% of mass); materials 0 iron, 1 dunite, 2 granite (synthetic tables)."""
     layers = [Layer(0, 0.3, 7800.0), Layer(1, 0.65, 3320.0), Layer(2, 0.05, 2700.0)]
     return make_impact(n_target, n_impactor, 0.89 * M_EARTH, 0.11 * M_EARTH, layers, layers, 45.0, 1.0, seed)
+
+
+def sweep_impact(rng: np.random.Generator, n_lo: float, n_hi: float, seed: int):
+    """One impact of the batched sweep and of the serving stream: total particles
+    log-uniform in [n_lo, n_hi], impactor / target mass ratio U[0.05, 0.5], impact
+    angle U[0, 75] degrees, speed U[1, 2] v_esc; iron core (30%) / dunite mantle
+    bodies of one Earth mass in total, equal-mass particles; materials 0 iron,
+    1 dunite (the 1M workload's synthetic tables).  Returns (F, ids, mats, params)."""
+    n = int(round(np.exp(rng.uniform(np.log(n_lo), np.log(n_hi)))))
+    q = float(rng.uniform(0.05, 0.5))
+    angle = float(rng.uniform(0.0, 75.0))
+    v = float(rng.uniform(1.0, 2.0))
+    n_i = max(64, int(round(n * q / (1.0 + q))))
+    n_t = max(64, n - n_i)
+    layers = [Layer(0, 0.3, 7800.0), Layer(1, 0.7, 3320.0)]
+    F, ids, mats, info = make_impact(n_t, n_i, M_EARTH / (1.0 + q), q * M_EARTH / (1.0 + q), layers, layers, angle, v,
+                                     seed)
+    return F, ids, mats, dict(n=int(F.shape[1]), mass_ratio=q, angle=angle, v_over_vesc=v, seed=seed)
+
+
+def config_sweep(seed=3, n_runs=256, n_lo=5_000, n_hi=200_000):
+    """The batched sweep: n_runs impacts drawn by sweep_impact from one seed."""
+    rng = np.random.default_rng(seed)
+    return [sweep_impact(rng, n_lo, n_hi, seed * 100_003 + k) for k in range(n_runs)]

@@ -331,7 +331,7 @@ class Context:
         self._check(self.L.sph_get_counters(self.h, _ptr(out)))
         keys = ["launches", "pairs_gather", "pairs_sym", "pairs_grav", "cells", "groups", "epj", "spj",
                 "walks_full", "walks_repair", "skin_violators", "units_walked", "units", "row_capacity",
-                "superset_entries"]
+                "superset_entries", "spilled_entries"]
         return dict(zip(keys, out.tolist()))
 
 

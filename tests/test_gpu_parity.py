@@ -307,3 +307,59 @@ def test_mixed_energy_and_angular_momentum_drift(impact):
     e32, l32 = drift[1]
     assert e32 <= 1.1 * e64 + 1e-9, (e32, e64)
     assert l32 <= 1.1 * l64 + 1e-9, (l32, l64)
+
+
+def _isolated_particle_system():
+    from oracle import pyoracle as po
+    F, ids, mats, info = small_impact(1500, 200, seed=31)
+    f = po.FIELD
+    extra = F[:, :1].copy()
+    R = float(np.max(np.abs(F[f["x"]])))
+    extra[f["x"], 0], extra[f["y"], 0], extra[f["z"], 0] = 1.5 * R, 0.3 * R, -0.2 * R
+    extra[f["vx"], 0] = extra[f["vy"], 0] = extra[f["vz"], 0] = 0.0
+    extra[f["smth"], 0] = 2.0 * R
+    return (np.concatenate([F, extra], axis=1), np.append(ids, ids.max() + 1), np.append(mats, mats[0]), R)
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_long_rows_spill(prec):
+    """An isolated particle outside the body (its density floors, its h grows
+    to cover the whole body) has a neighbour row far longer than the row
+    block: the row continues in a spill range.  Its gather list is the exact
+    FP64 set; the state after the prologue (whose first walk spills) and 3
+    steps matches the oracle (FP64: 1e-9; mixed: 1e-5)."""
+    from oracle import pyoracle as po
+    f = po.FIELD
+    F, ids, mats, R = _isolated_particle_system()
+    mats_l = tillotson_materials()
+    if prec == 0:
+        ctx = device_context(mats_l)
+        ctx.upload(F, ids, mats)
+        ctx.run_pass(0)
+        ctx.run_pass(1)          # gather lists for the uploaded h, then one density pass
+        slot, _ = ctx.order()
+        k = int(np.where(slot == F.shape[1] - 1)[0][0])
+        got = np.sort(ctx.neighbors(0, k))
+        X = F[[f["x"], f["y"], f["z"]]][:, slot]        # sorted order
+        d = X - X[:, k:k + 1]
+        r2 = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]
+        H = 2.5 * F[f["smth"], -1]
+        want = np.where(r2 < H * H)[0]
+        assert len(want) > 1000 and np.array_equal(got, want)
+        assert ctx.counters()["spilled_entries"] > 0
+        ctx.close()
+    cfg = oracle_config(mats_l)
+    ctx = device_context(mats_l, precision=prec)
+    ctx.upload(F, ids, mats)
+    ctx.prologue()
+    s = _oracle(F, ids, mats)
+    s.prologue(cfg)
+    assert ctx.counters()["row_capacity"] <= 512
+    ctx.step(3)
+    s.step(cfg, 3)
+    Fd, idd, _ = ctx.download()
+    Fd = by_id(Fd, idd)
+    Fo, _, _ = s.by_id()
+    tol = 1e-9 if prec == 0 else 1e-5
+    for name in ("dens", "smth", "eng", "pot"):
+        assert rel_err(Fd[f[name]], Fo[f[name]], 1e-300) < tol, name

@@ -62,3 +62,26 @@ def test_runs_removed_and_added_between_steps(prec):
     tot = ctx.diagnostics()
     per = ctx.run_diagnostics(h1) + ctx.run_diagnostics(h2)
     assert np.allclose(tot, per, rtol=1e-12, atol=0.0)
+
+
+def test_serving_loop_results_equal_runs_alone():
+    """Continuous batching: four requests through two run slots (so the batch
+    is backfilled as runs finish); every result equals its run advanced alone."""
+    from fdps_sph_gb300 import ic, serve
+    reqs = [serve.Request(k, 0.0, steps, 900 + k, 2000, 5000) for k, steps in enumerate((3, 5, 2, 4))]
+    srv = serve.Server("mixed", budget_bytes=1 << 34, max_runs=2, keep_results=True)
+    try:
+        rep = srv.run(reqs)
+    finally:
+        srv.close()
+    assert rep["completed"] == 4 and rep["resident_at_end"] == 0
+    assert rep["step_latency_s"]["p99"] is not None and rep["time_to_completion_s"]["p50"] is not None
+    for r in reqs:
+        F, ids, mats, _ = ic.sweep_impact(np.random.default_rng(r.rng_seed), r.n_lo, r.n_hi, r.rng_seed)
+        ctx = serve.make_context("mixed")
+        ctx.upload(F, ids, mats)
+        ctx.prologue()
+        ctx.step(r.steps)
+        alone = ctx.download()
+        ctx.close()
+        _same(r.result, alone)
