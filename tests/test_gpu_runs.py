@@ -85,3 +85,23 @@ def test_serving_loop_results_equal_runs_alone():
         alone = ctx.download()
         ctx.close()
         _same(r.result, alone)
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_checkpoint_resume_is_exact(prec, tmp_path):
+    """steps after a checkpoint and a restore into a new context give the same
+    state as stepping on without one"""
+    from fdps_sph_gb300 import snapshot
+    bodies = _bodies()
+    ctx = device_context(tillotson_materials(), precision=prec)
+    hs = [ctx.add_run(*b) for b in bodies[:2]]
+    ctx.step(1 + 3)
+    path = str(tmp_path / "c.ckpt")
+    snapshot.write_checkpoint(path, ctx)
+    ctx.step(2)
+    ctx2 = device_context(tillotson_materials(), precision=prec)
+    hs2 = snapshot.restore(ctx2, path)
+    ctx2.step(2)
+    for a, b in zip(hs, hs2):
+        _same(ctx.download_run(a), ctx2.download_run(b))
+        assert ctx.run_info(a)["time"] == ctx2.run_info(b)["time"]
