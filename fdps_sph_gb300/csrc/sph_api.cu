@@ -404,6 +404,8 @@ int sph_ctx_destroy(sph_ctx *ctx) {
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (void *p : ctx->table_allocs) cudaFree(p);
+    for (auto &g : ctx->tree_graphs)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
     if (ctx->host_scalars) cudaFreeHost(ctx->host_scalars);
     for (int k = 0; k < 64; ++k)
         if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);

@@ -229,6 +229,16 @@ struct Runs {
 
 }  // namespace sph
 
+namespace sph {
+constexpr int GRAPH_KEY_N = 20;
+// a captured sort + octree build and what it was captured for
+struct TreeGraph {
+    cudaGraphExec_t exec = nullptr;
+    uintptr_t key[GRAPH_KEY_N] = {0};
+    int64_t launches = 0;
+};
+}  // namespace sph
+
 struct sph_ctx {
     sph_config cfg;
     int device = 0;
@@ -277,6 +287,12 @@ struct sph_ctx {
     cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
 
     int64_t launches = 0;   // kernels launched by this context
+
+    // CUDA graphs of the sort + octree build: one per state-buffer parity and layout
+    bool use_graphs = true;
+    sph::TreeGraph tree_graphs[4];
+    int graph_next = 0;
+    int64_t graph_captures = 0, graph_replays = 0;
 };
 
 // timing segments, in the order sph_get_timings reports them

@@ -15,6 +15,8 @@
 //     over the children of a cell (octant order), each operation rounded once
 //     (no fused multiply-add), so that centres of mass and hence the gravity
 //     opening decisions are bit-identical to the oracle's.
+#include <algorithm>
+
 #include "sph_internal.cuh"
 
 namespace sph {
@@ -767,14 +769,15 @@ static int radix_sort(sph_ctx *ctx, int n) {
     return SPH_OK;
 }
 
-int sph_sort_and_build(sph_ctx *ctx) {
+// the device work of sph_sort_and_build up to the cell-count read: root cubes, keys, the
+// segmented radix sort, the permutation (and its host-side buffer swaps), the octree levels,
+// the moments.  No host synchronisation and no allocation inside, so it can be captured.
+static int enqueue_sort_tree(sph_ctx *ctx) {
     const int n = (int)ctx->n;
     const int64_t cap = ctx->cap;
     double *x = FLD(ctx->F, SPH_X, cap), *y = FLD(ctx->F, SPH_Y, cap), *z = FLD(ctx->F, SPH_Z, cap);
     Tree &t = ctx->tree;
-    SPH_TRY(sph_tree_reserve(ctx, n));
     cudaStream_t st = ctx->stream;
-    // root box
     // root cube of every run (one block per tile, then one per run)
     const Runs &R = ctx->runs;
     k_bbox_tiles<<<R.T, 256, 0, st>>>(x, y, z, R.tiles, R.part); ++ctx->launches;
@@ -813,6 +816,80 @@ int sph_sort_and_build(sph_ctx *ctx) {
     k_pack_cinfo<<<grid, 256, 0, st>>>(t.meta, t.first_child, t.n_child, t.start, t.count, t.cinfo);
     ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
+    return SPH_OK;
+}
+
+// Everything the captured work depends on: sizes and every buffer it touches.  The permutation
+// swaps the state buffers, so a step alternates between two keys.
+static void graph_key(const sph_ctx *ctx, uintptr_t key[GRAPH_KEY_N]) {
+    const Tree &t = ctx->tree;
+    const uintptr_t k[GRAPH_KEY_N] = {
+        (uintptr_t)ctx->n,         (uintptr_t)ctx->cap,        (uintptr_t)ctx->runs.R,   (uintptr_t)ctx->runs.T,
+        (uintptr_t)ctx->F,         (uintptr_t)ctx->F2,         (uintptr_t)ctx->id,       (uintptr_t)ctx->slot,
+        (uintptr_t)ctx->mat,       (uintptr_t)ctx->runs.prun,  (uintptr_t)ctx->keys,     (uintptr_t)ctx->sort.k0,
+        (uintptr_t)ctx->sort.hist, (uintptr_t)t.start,         (uintptr_t)t.rb,          (uintptr_t)t.cap,
+        (uintptr_t)ctx->runs.tiles, (uintptr_t)ctx->runs.part, (uintptr_t)ctx->scan.part, (uintptr_t)t.cinfo};
+    for (int i = 0; i < GRAPH_KEY_N; ++i) key[i] = k[i];
+}
+
+// replays the captured sort + octree for this key (capturing it the first time)
+static int sort_tree_graph(sph_ctx *ctx) {
+    uintptr_t key[GRAPH_KEY_N];
+    graph_key(ctx, key);
+    TreeGraph *g = nullptr;
+    for (TreeGraph &c : ctx->tree_graphs)
+        if (c.exec && std::equal(key, key + GRAPH_KEY_N, c.key)) g = &c;
+    if (g) {
+        // the captured work's host side: the buffer swaps of the permutation
+        std::swap(ctx->F, ctx->F2);
+        std::swap(ctx->runs.prun, ctx->runs.prun2);
+        std::swap(ctx->id, ctx->id2);
+        std::swap(ctx->slot, ctx->slot2);
+        std::swap(ctx->mat, ctx->mat2);
+        ctx->launches += g->launches;
+        ctx->graph_replays += 1;
+    } else {
+        g = &ctx->tree_graphs[ctx->graph_next];
+        ctx->graph_next = (ctx->graph_next + 1) % (int)(sizeof(ctx->tree_graphs) / sizeof(ctx->tree_graphs[0]));
+        if (g->exec) cudaGraphExecDestroy(g->exec);
+        g->exec = nullptr;
+        cudaGraph_t graph = nullptr;
+        const int64_t l0 = ctx->launches;
+        SPH_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        const int rc = enqueue_sort_tree(ctx);
+        const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+        if (rc != SPH_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        if (ce != cudaSuccess) {
+            cudaGetLastError();
+            return sph_fail(ctx, SPH_ERR_CUDA, "capture of the octree build failed: %s", cudaGetErrorString(ce));
+        }
+        const cudaError_t ie = cudaGraphInstantiate(&g->exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) {
+            g->exec = nullptr;
+            cudaGetLastError();
+            return sph_fail(ctx, SPH_ERR_CUDA, "instantiation of the octree build failed: %s", cudaGetErrorString(ie));
+        }
+        std::copy(key, key + GRAPH_KEY_N, g->key);
+        g->launches = ctx->launches - l0;
+        ctx->graph_captures += 1;
+    }
+    SPH_CUDA(ctx, cudaGraphLaunch(g->exec, ctx->stream));
+    return SPH_OK;
+}
+
+int sph_sort_and_build(sph_ctx *ctx) {
+    const int n = (int)ctx->n;
+    Tree &t = ctx->tree;
+    SPH_TRY(sph_tree_reserve(ctx, n));
+    cudaStream_t st = ctx->stream;
+    // With event timing on the work is launched directly (its segments are timed); otherwise the
+    // ~170 launches of the sort and the level loop replay as one CUDA graph.
+    if (ctx->timing || !ctx->use_graphs) SPH_TRY(enqueue_sort_tree(ctx));
+    else SPH_TRY(sort_tree_graph(ctx));
     // bring back the cell count and the error word (one small synchronous read per tree)
     int *hs = (int *)ctx->host_scalars;
     SPH_CUDA(ctx, cudaMemcpyAsync(hs, t.meta, sizeof(int) * META_N, cudaMemcpyDeviceToHost, st));
