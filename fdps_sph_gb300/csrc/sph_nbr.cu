@@ -115,6 +115,9 @@ __device__ __forceinline__ float gap2_rd(float4 a_lo, float4 a_hi, float3 glo, f
     return __fadd_rd(__fadd_rd(__fmul_rd(gx, gx), __fmul_rd(gy, gy)), __fmul_rd(gz, gz));
 }
 
+// SPILL: rows may continue in spill ranges (walks after this step's spill layout); without it
+// the hot loop carries no spill code (a row longer than K only raises the overflow flag)
+template <bool SPILL>
 __global__ void __launch_bounds__(NB_WARPS * 32, 7)
 k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ uidx, const double *__restrict__ x,
            const double *__restrict__ y, const double *__restrict__ z, const double *__restrict__ h,
@@ -168,36 +171,33 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
     int *row = sup + (int64_t)i * K;
     float *rrow = sup_r2 + (int64_t)i * K;
     float *mrow = sup_m + (int64_t)i * K;
-    // the spill range continues the row at entry K (its capacity: scap entries)
-    const int scap = valid ? row_spill_cap(rm, i) : 0;
-    const int64_t sbase = scap > 0 ? rm.main + rm.soff[i] - K : 0;   // entry k >= K at sbase + k
+    // the spill range continues the row at entry K: entry k >= K at spill_base() + k (computed
+    // on the rare paths that need it, so nothing stays live through the walk)
+    auto spill_cap = [&]() { return valid ? row_spill_cap(rm, i) : 0; };
+    auto spill_base = [&]() { return rm.main + rm.soff[i] - K; };
     // writes the lane's 8 buffered entries ending at `count` as full sectors (in the row, or in
     // its spill range: K is a multiple of 8, so a sector never straddles the two)
+    auto write8 = [&](int *rw, float *rr, float *rq, int k0) {
+        const int4 a = make_int4(s_wj[warp][0][lane], s_wj[warp][1][lane], s_wj[warp][2][lane], s_wj[warp][3][lane]);
+        const int4 b = make_int4(s_wj[warp][4][lane], s_wj[warp][5][lane], s_wj[warp][6][lane], s_wj[warp][7][lane]);
+        const float4 c = make_float4(s_wr[warp][0][lane], s_wr[warp][1][lane], s_wr[warp][2][lane], s_wr[warp][3][lane]);
+        const float4 d = make_float4(s_wr[warp][4][lane], s_wr[warp][5][lane], s_wr[warp][6][lane], s_wr[warp][7][lane]);
+        reinterpret_cast<int4 *>(rw + k0)[0] = a;
+        reinterpret_cast<int4 *>(rw + k0)[1] = b;
+        reinterpret_cast<float4 *>(rr + k0)[0] = c;
+        reinterpret_cast<float4 *>(rr + k0)[1] = d;
+        reinterpret_cast<float4 *>(rq + k0)[0] =
+            make_float4(s_wm[warp][0][lane], s_wm[warp][1][lane], s_wm[warp][2][lane], s_wm[warp][3][lane]);
+        reinterpret_cast<float4 *>(rq + k0)[1] =
+            make_float4(s_wm[warp][4][lane], s_wm[warp][5][lane], s_wm[warp][6][lane], s_wm[warp][7][lane]);
+    };
     auto put8 = [&]() {
         const int k0 = count - 8;
-        int *rw = row;
-        float *rr = rrow, *rm_ = mrow;
-        int kk = k0;
-        bool ok = k0 + 8 <= K;
-        if (!ok && k0 >= K && k0 + 8 <= K + scap) {
-            rw = sup + sbase;
-            rr = sup_r2 + sbase;
-            rm_ = sup_m + sbase;
-            ok = true;
-        }
-        if (ok) {
-            const int4 a = make_int4(s_wj[warp][0][lane], s_wj[warp][1][lane], s_wj[warp][2][lane], s_wj[warp][3][lane]);
-            const int4 b = make_int4(s_wj[warp][4][lane], s_wj[warp][5][lane], s_wj[warp][6][lane], s_wj[warp][7][lane]);
-            const float4 c = make_float4(s_wr[warp][0][lane], s_wr[warp][1][lane], s_wr[warp][2][lane], s_wr[warp][3][lane]);
-            const float4 d = make_float4(s_wr[warp][4][lane], s_wr[warp][5][lane], s_wr[warp][6][lane], s_wr[warp][7][lane]);
-            reinterpret_cast<int4 *>(rw + kk)[0] = a;
-            reinterpret_cast<int4 *>(rw + kk)[1] = b;
-            reinterpret_cast<float4 *>(rr + kk)[0] = c;
-            reinterpret_cast<float4 *>(rr + kk)[1] = d;
-            reinterpret_cast<float4 *>(rm_ + kk)[0] =
-                make_float4(s_wm[warp][0][lane], s_wm[warp][1][lane], s_wm[warp][2][lane], s_wm[warp][3][lane]);
-            reinterpret_cast<float4 *>(rm_ + kk)[1] =
-                make_float4(s_wm[warp][4][lane], s_wm[warp][5][lane], s_wm[warp][6][lane], s_wm[warp][7][lane]);
+        if (k0 + 8 <= K) {
+            write8(row, rrow, mrow, k0);
+        } else if (SPILL && k0 + 8 <= K + spill_cap()) {
+            const int64_t sb = spill_base();
+            write8(sup + sb, sup_r2 + sb, sup_m + sb, k0);
         }
     };
 
@@ -309,16 +309,18 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
     if (valid) {
         // the partial last block, entry by entry
         const int k0 = count & ~7;
+        const int scap = (SPILL && count > K) ? spill_cap() : 0;
         for (int q = 0; q < (count & 7); ++q) {
             const int k = k0 + q;
             if (k < K) {
                 row[k] = s_wj[warp][q][lane];
                 rrow[k] = s_wr[warp][q][lane];
                 mrow[k] = s_wm[warp][q][lane];
-            } else if (k < K + scap) {
-                sup[sbase + k] = s_wj[warp][q][lane];
-                sup_r2[sbase + k] = s_wr[warp][q][lane];
-                sup_m[sbase + k] = s_wm[warp][q][lane];
+            } else if (SPILL && k < K + scap) {
+                const int64_t sb = spill_base();
+                sup[sb + k] = s_wj[warp][q][lane];
+                sup_r2[sb + k] = s_wr[warp][q][lane];
+                sup_m[sb + k] = s_wm[warp][q][lane];
             }
         }
         cnt[i] = count;   // the true count, also when the row had no room for all of it
@@ -744,7 +746,8 @@ static int walk_units(sph_ctx *ctx, const int *uidx, int n_walk) {
         const int blocks = (n_walk + NB_WARPS - 1) / NB_WARPS;
         WalkTree T{t.cinfo, t.blo, t.bhi};
         if (blocks > 0) {
-            k_sup_walk<<<blocks, NB_WARPS * 32, 0, ctx->stream>>>(
+            auto walk = S.spill_on ? k_sup_walk<true> : k_sup_walk<false>;
+            walk<<<blocks, NB_WARPS * 32, 0, ctx->stream>>>(
                 n_walk, S.units, uidx, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
                 FLD(ctx->F, SPH_SMTH, cap), S.hsup, S.pxh, S.pxl, S.H2f, ctx->runs.prun, T, S.nbr, S.r2, S.m,
                 S.cnt, S.map(), S.uover, meta + META_ERR, meta + META_MAXCNT);
