@@ -139,6 +139,7 @@ def run_gpu(F, ids, mats, materials, precision, steps, warmup, device):
     ctx.prologue()
     for _ in range(warmup):
         ctx.step(1)
+    tune = ctx.autotune() if precision == "mixed" else None   # launch shapes, on this workload
     # segment breakdown: event marks between the passes (launched directly, not as graphs)
     ctx.enable_timing(True)
     ctx.step_timed(steps)
@@ -151,7 +152,7 @@ def run_gpu(F, ids, mats, materials, precision, steps, warmup, device):
         ms = ctx.step_timed(steps)
     d1 = ctx.diagnostics()
     c1 = ctx.counters()
-    return ctx, ms, seg, c1, c1["launches"] - c0, clk.summary(), drift(d0, d1, steps)
+    return ctx, ms, seg, c1, c1["launches"] - c0, clk.summary(), drift(d0, d1, steps), tune
 
 
 def drift(d0, d1, steps):
@@ -261,9 +262,10 @@ def main():
     results = {}
     precisions = ["mixed"] if a.no_fp64 else ["mixed", "fp64"]
     for prec in precisions:
-        ctx, ms, seg, cnt, launches, clocks, dr = run_gpu(F, ids, mats, materials, prec, a.steps, a.warmup, device)
+        ctx, ms, seg, cnt, launches, clocks, dr, tune = run_gpu(F, ids, mats, materials, prec, a.steps, a.warmup,
+                                                                device)
         e2e = run_e2e(ctx, F, ids, mats, a.e2e_steps) if prec == "mixed" else None
-        results[prec] = dict(ms=ms, seg=seg, cnt=cnt, launches=launches, clocks=clocks, e2e=e2e, drift=dr)
+        results[prec] = dict(ms=ms, seg=seg, cnt=cnt, launches=launches, clocks=clocks, e2e=e2e, drift=dr, tune=tune)
         ctx.close()
 
     if dist is not None:
@@ -342,6 +344,7 @@ def main():
         "work": {k: v for k, v in mixed["cnt"].items() if k != "launches"},
         "peaks": {"fp32_tflops_measured": peak32, "fp64_tflops_measured": peak64, "hbm_gbs": hbm},
     }
+    out["autotune"] = mixed["tune"]
     out["drift"] = {"mixed": mixed["drift"], "steps": a.steps,
                     "note": "relative change per timed step of E and |L| (FP64 diagnostics)"}
     if mixed["e2e"] is not None:

@@ -288,6 +288,11 @@ struct sph_ctx {
 
     int64_t launches = 0;   // kernels launched by this context
 
+    // launch shapes of the mixed kernels (sph_autotune); the defaults are the untuned choice
+    struct {
+        int drvt_tpi = 1, hydro_tpi = 1;   // threads per i-particle
+    } tune;
+
     // CUDA graphs of the sort + octree build: one per state-buffer parity and layout
     bool use_graphs = true;
     sph::TreeGraph tree_graphs[4];

@@ -337,9 +337,24 @@ __device__ __forceinline__ void drvt_pair32(const float4 pih, const float4 pil, 
     P[4] = fmaf(qh.w, 3.0f * w + gf * rr2, P[4]);
 }
 
+// TPI threads share one i-particle: thread `sub` takes the neighbour pairs 2 sub, 2 sub + 2 TPI, ...
+// and the compensated partial sums are combined by shuffles (TPI = 1: one thread per particle)
+template <int TPI>
+__device__ __forceinline__ void df_group_sum(float &hi, float &lo) {
+    const unsigned m = __activemask();
+#pragma unroll
+    for (int off = TPI / 2; off > 0; off >>= 1) {
+        const float oh = __shfl_xor_sync(m, hi, off, TPI), ol = __shfl_xor_sync(m, lo, off, TPI);
+        df_add(hi, lo, oh);
+        lo += ol;
+    }
+}
+
+template <int TPI>
 __global__ void __launch_bounds__(PT) k_drvt32(int n, DrvtArgs32 a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = gt / TPI, sub = gt % TPI;
+    if (i >= n) return;   // whole groups of TPI lanes leave together
     const float4 pih = a.xh[i], pil = a.xl[i], vih = a.vh[i], vil = a.vl[i];
     const double hi = a.h[i];
     const float Hf = (float)(SUPPORT * hi), invH = 1.0f / Hf, ceps = (float)(1.0e-6 * hi);
@@ -348,15 +363,15 @@ __global__ void __launch_bounds__(PT) k_drvt32(int n, DrvtArgs32 a) {
     float P[5] = {0, 0, 0, 0, 0};
     for (int seg = 0, c; seg < 2; ++seg) {
     const int *row = a.nbr + row_seg(a.rm, i, seg, a.cnt[i], &c);
-    int k = 0;
-    for (; k + 2 <= c; k += 2) {
+    int k = 2 * sub, it = 0;
+    for (; k + 2 <= c; k += 2 * TPI) {
         const int2 jp = *reinterpret_cast<const int2 *>(row + k);
         const int j0 = jp.x, j1 = jp.y;
         const float4 qh0 = a.xh[j0], ql0 = a.xl[j0], uh0 = a.vh[j0], ul0 = a.vl[j0];
         const float4 qh1 = a.xh[j1], ql1 = a.xl[j1], uh1 = a.vh[j1], ul1 = a.vl[j1];
         drvt_pair32(pih, pil, vih, vil, qh0, ql0, uh0, ul0, invH, Hf, ceps, P);
         drvt_pair32(pih, pil, vih, vil, qh1, ql1, uh1, ul1, invH, Hf, ceps, P);
-        if ((k & 31) == 30) {
+        if ((++it & 15) == 0) {
 #pragma unroll
             for (int q = 0; q < 5; ++q) {
                 df_add(Dh[q], Dl[q], P[q]);
@@ -375,8 +390,10 @@ __global__ void __launch_bounds__(PT) k_drvt32(int n, DrvtArgs32 a) {
 #pragma unroll
     for (int q = 0; q < 5; ++q) {
         df_add(Dh[q], Dl[q], P[q]);
+        if (TPI > 1) df_group_sum<TPI>(Dh[q], Dl[q]);
         D[q] = (Dh[q] + Dl[q]) * sc;
     }
+    if (sub != 0) return;
     const float rho = (float)a.dens[i], hf = (float)hi;
     const float gs = 1.0f / (1.0f + hf * (-D[4] / hf) / (3.0f * rho));
     const float dv = D[0] / rho, r0 = D[1] / rho, r1 = D[2] / rho, r2 = D[3] / rho;
@@ -454,9 +471,11 @@ __device__ __forceinline__ HydroJ32 load_hydro_j(const HydroArgs32 &a, int j) {
     return J;
 }
 
+template <int TPI>
 __global__ void __launch_bounds__(PT) k_hydro32(int n, HydroArgs32 a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = gt / TPI, sub = gt % TPI;
+    if (i >= n) return;   // whole groups of TPI lanes leave together
     const float4 pih = a.xh[i], pil = a.xl[i], vih = a.vh[i], vil = a.vl[i];
     const float4 Ai = a.hA[i], Bi = a.hB[i];
     float Dh[4] = {0, 0, 0, 0}, Dl[4] = {0, 0, 0, 0};
@@ -464,14 +483,14 @@ __global__ void __launch_bounds__(PT) k_hydro32(int n, HydroArgs32 a) {
     float vmax = 0.0f;
     for (int seg = 0, c; seg < 2; ++seg) {
     const int *row = a.nbr + row_seg(a.rm, i, seg, a.cnt[i], &c);
-    int k = 0;
-    for (; k + 2 <= c; k += 2) {
+    int k = 2 * sub, it = 0;
+    for (; k + 2 <= c; k += 2 * TPI) {
         const int2 jp = *reinterpret_cast<const int2 *>(row + k);
         const int j0 = jp.x, j1 = jp.y;
         const HydroJ32 J0 = load_hydro_j(a, j0), J1 = load_hydro_j(a, j1);
         hydro_pair32(pih, pil, vih, vil, Ai, Bi, J0, P, vmax);
         hydro_pair32(pih, pil, vih, vil, Ai, Bi, J1, P, vmax);
-        if ((k & 31) == 30) {
+        if ((++it & 15) == 0) {
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 df_add(Dh[q], Dl[q], P[q]);
@@ -490,8 +509,14 @@ __global__ void __launch_bounds__(PT) k_hydro32(int n, HydroArgs32 a) {
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         df_add(Dh[q], Dl[q], P[q]);
+        if (TPI > 1) df_group_sum<TPI>(Dh[q], Dl[q]);
         D[q] = (Dh[q] + Dl[q]) * sc;
     }
+    if (TPI > 1) {
+        const unsigned m = __activemask();
+        for (int off = TPI / 2; off > 0; off >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(m, vmax, off, TPI));
+    }
+    if (sub != 0) return;
     a.ax[i] = D[0];
     a.ay[i] = D[1];
     a.az[i] = D[2];
@@ -1195,7 +1220,10 @@ int sph_pass_derivative(sph_ctx *ctx, int build_lists) {
                      CF(SPH_SNDS), CF(SPH_DIVV), CF(SPH_ROTX), CF(SPH_ROTY),  CF(SPH_ROTZ), CF(SPH_GRADH),
                      CF(SPH_BAL),  L.nbr,        L.cnt,        ctx->sup.map(),
                      (float)(WNORM / (PI_D * ctx->mscale))};
-        k_drvt32<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, a); ++ctx->launches;
+        // threads per i-particle: chosen by sph_autotune (1 unless tuned)
+        const int tpi = ctx->tune.drvt_tpi;
+        auto kd = tpi == 4 ? k_drvt32<4> : (tpi == 2 ? k_drvt32<2> : k_drvt32<1>);
+        kd<<<sph_div_up((int64_t)n * tpi, PT), PT, 0, ctx->stream>>>(n, a); ++ctx->launches;
     } else {
         DrvtArgs a{CF(SPH_X),    CF(SPH_Y),    CF(SPH_Z),    CF(SPH_VX),    CF(SPH_VY),   CF(SPH_VZ),
                    CF(SPH_MASS), CF(SPH_SMTH), CF(SPH_DENS), CF(SPH_SNDS),  CF(SPH_DIVV), CF(SPH_ROTX),
@@ -1219,7 +1247,9 @@ int sph_pass_hydro(sph_ctx *ctx, int build_lists) {
         HydroArgs32 a{ctx->xh,    ctx->xl,    ctx->vhf,   ctx->vlf,       hA,         hB,    CF(SPH_SMTH),
                       CF(SPH_AX), CF(SPH_AY), CF(SPH_AZ), CF(SPH_ENGDOT), CF(SPH_DT), L.nbr, L.cnt,
                       ctx->sup.map(),    (float)(WNORM / (PI_D * ctx->mscale))};
-        k_hydro32<<<sph_div_up(n, PT), PT, 0, ctx->stream>>>(n, a); ++ctx->launches;
+        const int tpi = ctx->tune.hydro_tpi;
+        auto kh = tpi == 4 ? k_hydro32<4> : (tpi == 2 ? k_hydro32<2> : k_hydro32<1>);
+        kh<<<sph_div_up((int64_t)n * tpi, PT), PT, 0, ctx->stream>>>(n, a); ++ctx->launches;
     } else {
         double4 *aux = (double4 *)ctx->F2;
         k_hydro_aux64<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, CF(SPH_SMTH), CF(SPH_DENS), CF(SPH_PRES),
@@ -1398,5 +1428,73 @@ int sph_gravity_fused(sph_ctx *ctx) {
     SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (hs[0] & ERR_GRAV_OVERFLOW) return sph_fail(ctx, SPH_ERR_CAPACITY, "gravity walk buffers overflowed");
     G.counts_valid = true;
+    return SPH_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Launch-shape autotuner for the mixed derivative and hydro kernels: threads per
+// i-particle (1, 2 or 4) timed on the context's current state and lists, the
+// fastest kept.  The fields the trial launches write are saved and restored.
+extern "C" int sph_autotune(sph_ctx *ctx, int mode, int64_t params[8]) {
+    if (!ctx || !params) return SPH_ERR_ARG;
+    auto ok_tpi = [](int64_t v) { return v == 1 || v == 2 || v == 4; };
+    if (mode == 1) {   // apply given choices
+        if (!ok_tpi(params[0]) || !ok_tpi(params[1])) return sph_fail(ctx, SPH_ERR_ARG, "threads per particle must be 1, 2 or 4");
+        ctx->tune.drvt_tpi = (int)params[0];
+        ctx->tune.hydro_tpi = (int)params[1];
+        return SPH_OK;
+    }
+    if (mode != 0) return sph_fail(ctx, SPH_ERR_ARG, "unknown autotune mode %d", mode);
+    if (ctx->cfg.precision != SPH_PREC_MIXED) return sph_fail(ctx, SPH_ERR_STATE, "autotune tunes the mixed kernels");
+    if (!ctx->uploaded || !ctx->have_forces || !ctx->lists[0].valid || !ctx->lists[1].valid || !ctx->xh)
+        return sph_fail(ctx, SPH_ERR_STATE, "autotune needs the lists of a completed step (call it after sph_step)");
+    cudaSetDevice(ctx->device);
+    const int saved[] = {SPH_DIVV, SPH_ROTX, SPH_ROTY, SPH_ROTZ, SPH_GRADH, SPH_BAL,
+                         SPH_AX,   SPH_AY,   SPH_AZ,   SPH_ENGDOT, SPH_DT};
+    const int ns = (int)(sizeof(saved) / sizeof(saved[0]));
+    const int64_t n = ctx->n;
+    double *keep = nullptr;
+    if (cudaMalloc((void **)&keep, sizeof(double) * n * ns) != cudaSuccess) {
+        cudaGetLastError();
+        return sph_fail(ctx, SPH_ERR_OOM, "autotune scratch");
+    }
+    for (int f = 0; f < ns; ++f)
+        SPH_CUDA(ctx, cudaMemcpyAsync(keep + f * n, CF(saved[f]), sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                                      ctx->stream));
+    const int choices[3] = {1, 2, 4};
+    float best_ms[2] = {1e30f, 1e30f};
+    int best[2] = {1, 1};
+    int rc = SPH_OK;
+    for (int which = 0; which < 2 && rc == SPH_OK; ++which) {
+        for (int c = 0; c < 3 && rc == SPH_OK; ++c) {
+            if (which == 0) ctx->tune.drvt_tpi = choices[c];
+            else ctx->tune.hydro_tpi = choices[c];
+            float ms = 0.0f;
+            for (int rep = 0; rep < 4 && rc == SPH_OK; ++rep) {   // first launch warms up
+                cudaEventRecord(ctx->ev_begin, ctx->stream);
+                rc = which == 0 ? sph_pass_derivative(ctx, 0) : sph_pass_hydro(ctx, 0);
+                cudaEventRecord(ctx->ev_end, ctx->stream);
+                cudaEventSynchronize(ctx->ev_end);
+                float e = 0.0f;
+                cudaEventElapsedTime(&e, ctx->ev_begin, ctx->ev_end);
+                if (rep > 0) ms += e / 3.0f;
+            }
+            params[2 + which * 3 + c] = (int64_t)(ms * 1000.0f);   // microseconds
+            if (ms < best_ms[which]) {
+                best_ms[which] = ms;
+                best[which] = choices[c];
+            }
+        }
+    }
+    ctx->tune.drvt_tpi = best[0];
+    ctx->tune.hydro_tpi = best[1];
+    for (int f = 0; f < ns; ++f)
+        cudaMemcpyAsync(CF(saved[f]), keep + f * n, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(keep);
+    if (rc != SPH_OK) return rc;
+    SPH_CUDA(ctx, cudaGetLastError());
+    params[0] = best[0];
+    params[1] = best[1];
     return SPH_OK;
 }

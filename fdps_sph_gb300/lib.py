@@ -39,6 +39,7 @@ EXPORTS = [
     "sph_get_neighbors", "sph_get_tree", "sph_get_grav_list", "sph_get_timings", "sph_step_timed",
     "sph_get_counters", "sph_probe_peak", "sph_morton_order_noalloc",
     "sph_add_run", "sph_remove_run", "sph_list_runs", "sph_run_info", "sph_download_run", "sph_run_diagnostics",
+    "sph_autotune",
 ]
 NOALLOC_MAX_N = 131072
 SEGMENTS = ["kdp", "tree", "dens_list", "dens", "eos", "drvt_list", "drvt", "hydro_list", "hydro", "grav_list",
@@ -113,6 +114,7 @@ def load() -> C.CDLL:
                                C.POINTER(C.c_int64)]
     L.sph_download_run.argtypes = [P, C.c_int64, P, C.c_int64, P, P]
     L.sph_run_diagnostics.argtypes = [P, C.c_int64, P]
+    L.sph_autotune.argtypes = [P, C.c_int, P]
     _lib = L
     return L
 
@@ -241,6 +243,18 @@ class Context:
         mats = np.empty(n, np.int32)
         self._check(self.L.sph_download_run(self.h, int(handle), _ptr(out), n, _ptr(ids), _ptr(mats)))
         return out, ids, mats
+
+    def autotune(self):
+        """times the derivative / hydro kernels with 1, 2, 4 threads per particle on the current state
+        (after a step) and keeps the fastest; returns the choices and the times (microseconds)"""
+        p = np.zeros(8, np.int64)
+        self._check(self.L.sph_autotune(self.h, 0, _ptr(p)))
+        return {"drvt_tpi": int(p[0]), "hydro_tpi": int(p[1]), "drvt_us": p[2:5].tolist(), "hydro_us": p[5:8].tolist()}
+
+    def set_tune(self, drvt_tpi=1, hydro_tpi=1):
+        p = np.zeros(8, np.int64)
+        p[0], p[1] = drvt_tpi, hydro_tpi
+        self._check(self.L.sph_autotune(self.h, 1, _ptr(p)))
 
     def run_diagnostics(self, handle: int):
         out = np.zeros(8)

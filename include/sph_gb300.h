@@ -188,6 +188,16 @@ int sph_run_info(sph_ctx *ctx, int64_t handle, int64_t *n, double *time, double 
 int sph_download_run(sph_ctx *ctx, int64_t handle, double *fields, int64_t ld, int64_t *id, int32_t *material);
 int sph_run_diagnostics(sph_ctx *ctx, int64_t handle, double out[8]);
 
+/* ---- launch-shape autotuner (mixed precision) ------------------------------
+ * No counterpart in the reference.  mode 0: times the derivative and hydro
+ * kernels with 1, 2 and 4 threads per i-particle on the context's current
+ * state and lists (call after sph_step; the state is left unchanged), keeps
+ * the fastest and returns params[0] = derivative, params[1] = hydro threads
+ * per particle, params[2..4] / [5..7] = the measured times in microseconds.
+ * mode 1: applies params[0], params[1].  The choice changes the summation
+ * order of the FP32 pair sums only (rounding level). */
+int sph_autotune(sph_ctx *ctx, int mode, int64_t params[8]);
+
 /* ---- inspection (tests, tooling) ----------------------------------------- */
 /* Runs only the given pass on the current state (positions unchanged):
  * 0 = sort + tree, 1 = one density pass, 2 = EoS, 3 = derivative, 4 = hydro, 5 = gravity. */

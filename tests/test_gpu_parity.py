@@ -157,16 +157,19 @@ def test_steps_match_oracle(eos_kind):
     assert vec_rel_err(V, W, 1e-6) < 1e-9
 
 
-def test_mixed_precision_against_fp64_oracle(impact):
+@pytest.mark.parametrize("tpi", [1, 4])
+def test_mixed_precision_against_fp64_oracle(impact, tpi):
     """FP32 pair sums on double-float coordinates: rho, acc, du/dt and
-    gravity within 1e-5 relative of the FP64 oracle (spec bar).
-    Density: relative per particle.  Vectors and du/dt: relative per
-    particle, floored at the RMS over particles (vec_err_rms)."""
+    gravity within 1e-5 relative of the FP64 oracle (spec bar), with
+    one and with four threads per particle in the derivative and hydro
+    kernels.  Density: relative per particle.  Vectors and du/dt: relative
+    per particle, floored at the RMS over particles (vec_err_rms)."""
     from oracle import pyoracle as po
     F, ids, mats = impact
     mats_l = tillotson_materials()
     cfg = oracle_config(mats_l)
     ctx = device_context(mats_l, precision=1)
+    ctx.set_tune(tpi, tpi)
     ctx.upload(F, ids, mats)
     ctx.prologue()
     s = _oracle(F, ids, mats)
@@ -363,3 +366,37 @@ def test_long_rows_spill(prec):
     tol = 1e-9 if prec == 0 else 1e-5
     for name in ("dens", "smth", "eng", "pot"):
         assert rel_err(Fd[f[name]], Fo[f[name]], 1e-300) < tol, name
+
+
+def test_autotune_leaves_state_and_variants_agree(impact):
+    """sph_autotune leaves the state as it found it; every threads-per-particle
+    variant of the mixed derivative and hydro kernels agrees with the one-
+    thread version to the mixed path's rounding (RMS-floored relative 5e-6;
+    each variant is within 1e-5 of the FP64 oracle)."""
+    from oracle import pyoracle as po
+    F, ids, mats = impact
+    mats_l = tillotson_materials()
+    ctx = device_context(mats_l, precision=1)
+    ctx.upload(F, ids, mats)
+    ctx.prologue()
+    ctx.step(2)
+    before = ctx.download()
+    tune = ctx.autotune()
+    after = ctx.download()
+    assert all(np.array_equal(a, b) for a, b in zip(before, after))
+    assert tune["drvt_tpi"] in (1, 2, 4) and tune["hydro_tpi"] in (1, 2, 4)
+    f = po.FIELD
+    out = {}
+    for tpi in (1, 2, 4):
+        c = device_context(mats_l, precision=1)
+        c.set_tune(tpi, tpi)
+        c.upload(F, ids, mats)
+        c.prologue()
+        Fd, idd, _ = c.download()
+        out[tpi] = by_id(Fd, idd)
+    for tpi in (2, 4):
+        A = np.stack([out[tpi][f[k]] for k in ("ax", "ay", "az")], 1)
+        B = np.stack([out[1][f[k]] for k in ("ax", "ay", "az")], 1)
+        assert vec_err_rms(A, B) < 5e-6
+        assert scalar_err_rms(out[tpi][f["eng_dot"]], out[1][f["eng_dot"]]) < 5e-6
+        assert np.max(np.abs(out[tpi][f["bal"]] - out[1][f["bal"]])) < 1e-5   # the switch lies in [0, 1]
