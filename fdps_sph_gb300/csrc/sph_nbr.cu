@@ -563,12 +563,19 @@ k_density_sup32(int n, const int *__restrict__ sup, const float *__restrict__ su
     const int *row = sup + b;
     const float *rrow = sup_r2 + b;
     const float *mrow = sup_m + b;
+    // software-pipelined: the next chunk's four vector loads are in flight while this chunk is summed
+    float4 r0 = reinterpret_cast<const float4 *>(rrow)[0], r1 = reinterpret_cast<const float4 *>(rrow)[1];
+    float4 m0 = reinterpret_cast<const float4 *>(mrow)[0], m1 = reinterpret_cast<const float4 *>(mrow)[1];
     for (int k = 0; k < c; k += 8) {
-        const float4 r0 = reinterpret_cast<const float4 *>(rrow + k)[0], r1 = reinterpret_cast<const float4 *>(rrow + k)[1];
         const float rr[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
-        const int m8 = min(8, c - k);
-        const float4 m0 = reinterpret_cast<const float4 *>(mrow + k)[0], m1 = reinterpret_cast<const float4 *>(mrow + k)[1];
         const float mj[8] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
+        const int m8 = min(8, c - k);
+        if (k + 8 < c) {
+            r0 = reinterpret_cast<const float4 *>(rrow + k + 8)[0];
+            r1 = reinterpret_cast<const float4 *>(rrow + k + 8)[1];
+            m0 = reinterpret_cast<const float4 *>(mrow + k + 8)[0];
+            m1 = reinterpret_cast<const float4 *>(mrow + k + 8)[1];
+        }
         // every member goes straight into the compensated pair: the sum depends only on the
         // sequence of members (the walk's order), not on where non-members sit in the row, so a
         // row rebuilt with another skin (a repair, another run's violators) gives the same result
