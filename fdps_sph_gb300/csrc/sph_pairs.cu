@@ -719,9 +719,12 @@ k_grav_fused32(const int *__restrict__ group_cell, const int4 *__restrict__ cinf
     int tot_e = 0, tot_s = 0;
     for (int i_base = 0; i_base < cnt_all; i_base += 2 * GF_T) {
         const int cnt = min(2 * GF_T, cnt_all - i_base);
-        const int Wt = ((cnt + 1) / 2 + 31) & ~31, P = GF_T / Wt;
+        // partitions of 8-lane granularity (a warp may hold up to four; their tile reads then take a
+        // few shared-memory wavefronts): 84-96% of the slots carry an i-particle for groups of 48-256
+        const int Wt = ((cnt + 1) / 2 + 7) & ~7, P = GF_T / Wt;
+        const int TE = GF_T / (4 * P) * (4 * P);   // tile entries: a multiple of every partition's stride
         const int part = tid / Wt, ii = tid - part * Wt;
-        const bool slot = part < P;   // warp-uniform
+        const bool slot = part < P;
         float px[2], py[2], pz[2], e2[2];
         for (int u = 0; u < 2; ++u) {
             const int iu = ii + u * Wt;
@@ -856,10 +859,10 @@ k_grav_fused32(const int *__restrict__ group_cell, const int4 *__restrict__ cinf
             // ---- accumulate the buffered EPJ, then SPJ
             for (int pass = 0; pass < 2; ++pass) {
                 const int nl = pass == 0 ? ne : ns;
-                for (int t0 = 0; t0 < nl; t0 += GF_T) {
+                for (int t0 = 0; t0 < nl; t0 += TE) {
                     const int kk = t0 + tid;
                     float4 v = make_float4(0.f, 0.f, 0.f, 0.f);   // zero mass pads the tile
-                    if (kk < nl) {
+                    if (tid < TE && kk < nl) {
                         float4 qh, ql;
                         float gm;
                         if (pass == 0) {
@@ -880,7 +883,7 @@ k_grav_fused32(const int *__restrict__ group_cell, const int4 *__restrict__ cinf
                     __syncthreads();
                     if (slot) {
                         const int step = 4 * P;
-                        const int tnr = (min(GF_T, nl - t0) + step - 1) / step * step;   // <= GF_T: step divides it
+                        const int tnr = (min(TE, nl - t0) + step - 1) / step * step;   // <= TE: step divides it
                         float A[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
                         for (int t = part; t < tnr; t += step) {
                             const float4 q0 = s_tile[t], q1 = s_tile[t + P], q2 = s_tile[t + 2 * P],
