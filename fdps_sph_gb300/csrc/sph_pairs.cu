@@ -656,7 +656,7 @@ __device__ __forceinline__ void grav_acc(float px, float py, float pz, float e2,
     a3 -= mri;
 }
 
-__global__ void __launch_bounds__(GF_T, 3)
+__global__ void __launch_bounds__(GF_T, 4)
 k_grav_fused32(const int *__restrict__ group_cell, const int4 *__restrict__ cinfo, const double4 *__restrict__ com,
                const double *__restrict__ rb_all, const int *__restrict__ prun, const double *__restrict__ x,
                const double *__restrict__ y,
