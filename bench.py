@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-batch", action="store_true", help="skip the batched sweep and the serving window")
+    ap.add_argument("--tpi", type=int, default=0,
+                    help="threads per particle of the derivative / hydro kernels instead of autotuning (1, 2, 4)")
     ap.add_argument("--batch-runs", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=100)
     ap.add_argument("--serve-s", type=float, default=60.0, help="seconds of Poisson arrivals (2 per second)")
@@ -139,7 +141,13 @@ def run_gpu(F, ids, mats, materials, precision, steps, warmup, device):
     ctx.prologue()
     for _ in range(warmup):
         ctx.step(1)
-    tune = ctx.autotune() if precision == "mixed" else None   # launch shapes, on this workload
+    tune = None
+    if precision == "mixed":   # launch shapes: tuned on this workload, or given
+        if TPI:
+            ctx.set_tune(TPI, TPI)
+            tune = {"drvt_tpi": TPI, "hydro_tpi": TPI, "given": True}
+        else:
+            tune = ctx.autotune()
     # segment breakdown: event marks between the passes (launched directly, not as graphs)
     ctx.enable_timing(True)
     ctx.step_timed(steps)
@@ -219,8 +227,13 @@ def dist_init(n_gpus):
     return rank, world, dist
 
 
+TPI = 0
+
+
 def main():
+    global TPI
     a = parse()
+    TPI = a.tpi
     rank, world, dist = dist_init(a.gpus)
     if a.impl == "reference":
         if rank != 0:
