@@ -29,6 +29,8 @@ import time
 
 import numpy as np
 
+from fdps_sph_gb300.ic import FIELD
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -139,6 +141,9 @@ def run_gpu(F, ids, mats, materials, precision, steps, warmup, device):
         ctx.set_material(k, m)
     ctx.upload(F, ids, mats)
     ctx.prologue()
+    Fp, idp, _ = ctx.download()   # the forces of the initial state, for the mixed-vs-FP64 errors
+    first = Fp[:, np.argsort(idp, kind="stable")][[FIELD[k] for k in ERR_FIELDS]].copy()
+    del Fp
     for _ in range(warmup):
         ctx.step(1)
     tune = None
@@ -160,7 +165,37 @@ def run_gpu(F, ids, mats, materials, precision, steps, warmup, device):
         ms = ctx.step_timed(steps)
     d1 = ctx.diagnostics()
     c1 = ctx.counters()
-    return ctx, ms, seg, c1, c1["launches"] - c0, clk.summary(), drift(d0, d1, steps), tune
+    return ctx, ms, seg, c1, c1["launches"] - c0, clk.summary(), drift(d0, d1, steps), tune, first
+
+
+ERR_FIELDS = ("dens", "ax", "ay", "az", "eng_dot", "gx", "gy", "gz", "pot")
+
+
+def mixed_errors(mx, f64):
+    """per-quantity error of the mixed path's initial forces against the FP64 path's (pinned to
+    the oracle by the parity tests): density relative per particle; vectors and du/dt relative
+    per particle, floored at the RMS over particles"""
+    ix = {k: i for i, k in enumerate(ERR_FIELDS)}
+
+    def vec(X, keys):
+        return np.stack([X[ix[k]] for k in keys], 1)
+
+    def vrms(A, B):
+        nb = np.linalg.norm(B, axis=1)
+        rms = max(float(np.sqrt(np.mean(nb * nb))), 1e-300)
+        return float(np.max(np.linalg.norm(A - B, axis=1) / np.maximum(nb, rms)))
+
+    def srms(a, b):   # du/dt is zero in both paths while the bodies move rigidly: then 0
+        rms = max(float(np.sqrt(np.mean(b * b))), 1e-300)
+        return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), rms)))
+
+    return {"dens": float(np.max(np.abs(mx[0] - f64[0]) / np.abs(f64[0]))),
+            "acc_hydro": vrms(vec(mx, ("ax", "ay", "az")), vec(f64, ("ax", "ay", "az"))),
+            "eng_dot": srms(mx[ix["eng_dot"]], f64[ix["eng_dot"]]),
+            "acc_grav": vrms(vec(mx, ("gx", "gy", "gz")), vec(f64, ("gx", "gy", "gz"))),
+            "pot": float(np.max(np.abs(mx[ix["pot"]] - f64[ix["pot"]]) / np.abs(f64[ix["pot"]]))),
+            "acc_total": vrms(vec(mx, ("ax", "ay", "az")) + vec(mx, ("gx", "gy", "gz")),
+                              vec(f64, ("ax", "ay", "az")) + vec(f64, ("gx", "gy", "gz")))}
 
 
 def drift(d0, d1, steps):
@@ -275,10 +310,11 @@ def main():
     results = {}
     precisions = ["mixed"] if a.no_fp64 else ["mixed", "fp64"]
     for prec in precisions:
-        ctx, ms, seg, cnt, launches, clocks, dr, tune = run_gpu(F, ids, mats, materials, prec, a.steps, a.warmup,
-                                                                device)
+        ctx, ms, seg, cnt, launches, clocks, dr, tune, first = run_gpu(F, ids, mats, materials, prec, a.steps,
+                                                                       a.warmup, device)
         e2e = run_e2e(ctx, F, ids, mats, a.e2e_steps) if prec == "mixed" else None
-        results[prec] = dict(ms=ms, seg=seg, cnt=cnt, launches=launches, clocks=clocks, e2e=e2e, drift=dr, tune=tune)
+        results[prec] = dict(ms=ms, seg=seg, cnt=cnt, launches=launches, clocks=clocks, e2e=e2e, drift=dr, tune=tune,
+                             first=first)
         ctx.close()
 
     if dist is not None:
@@ -378,6 +414,9 @@ def main():
                                     "unit": "TFLOP/s", "frac": ach64 / peak64 if peak64 else None},
                        "clocks": f["clocks"], "gpu_launches": int(f["launches"])}
         out["drift"]["fp64"] = f["drift"]
+        out["mixed_error_vs_fp64"] = dict(mixed_errors(mixed["first"], f["first"]),
+                                          note="forces of the initial state (prologue), all particles; the FP64 "
+                                               "path is held to the oracle by the parity tests; bar 1e-5")
     if not a.no_batch and world == 1:
         out.update(batch_and_serving(a, device))
     if not a.no_cpu:

@@ -400,3 +400,45 @@ def test_autotune_leaves_state_and_variants_agree(impact):
         assert vec_err_rms(A, B) < 5e-6
         assert scalar_err_rms(out[tpi][f["eng_dot"]], out[1][f["eng_dot"]]) < 5e-6
         assert np.max(np.abs(out[tpi][f["bal"]] - out[1][f["bal"]])) < 1e-5   # the switch lies in [0, 1]
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_config0_fifty_steps(prec):
+    """The reference's CPU-runnable case: 9,000 + 1,000 particles (two-layer
+    iron / granite bodies, Tillotson), 45 degrees at 1.0 v_esc, theta 0.5,
+    prologue and 50 steps on the device and in the oracle.  FP64: the
+    trajectory stays within 1e-10 (measured: positions 6e-14, energies 7e-12).
+    Mixed: each step's forces are within 1e-5 (the per-step tests); along the
+    trajectory those differences change every dt and grow with the impact's
+    dynamics, to about 1e-4 - 1e-3 after 50 steps (bound 2e-3)."""
+    from fdps_sph_gb300 import ic
+    from oracle import pyoracle as po
+    F, ids, mats, _ = ic.config_small_impact()
+    mats_l = tillotson_materials()
+    cfg = oracle_config(mats_l)
+    ctx = device_context(mats_l, precision=prec)
+    ctx.upload(F, ids, mats)
+    ctx.prologue()
+    ctx.step(50)
+    s = _oracle(F, ids, mats)
+    s.prologue(cfg)
+    s.step(cfg, 50)
+    Fd, idd, _ = ctx.download()
+    Fd = by_id(Fd, idd)
+    Fo, _, _ = s.by_id()
+    f = po.FIELD
+    t, dt, st = ctx.time()
+    assert st == 50
+    errs = {"time": abs(t - s.sys.time) / s.sys.time}
+    X = np.stack([Fd[f[c]] for c in ("x", "y", "z")], 1)
+    Y = np.stack([Fo[f[c]] for c in ("x", "y", "z")], 1)
+    errs["pos"] = vec_err_rms(X, Y)
+    V = np.stack([Fd[f[c]] for c in ("vx", "vy", "vz")], 1)
+    W = np.stack([Fo[f[c]] for c in ("vx", "vy", "vz")], 1)
+    errs["vel"] = vec_err_rms(V, W)
+    for name in ("dens", "eng", "pot"):
+        errs[name] = rel_err(Fd[f[name]], Fo[f[name]], 1e-300)
+    print("config 0, 50 steps, precision", prec, errs)
+    bound = 1e-10 if prec == 0 else 2e-3
+    for k, v in errs.items():
+        assert v < bound, (k, v)
