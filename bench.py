@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-batch", action="store_true", help="skip the batched sweep and the serving window")
+    ap.add_argument("--config", default="1m", choices=["1m", "4m"], help="geometry of the workload (see workload())")
+    ap.add_argument("--theta", type=float, default=0.5, help="gravity opening angle")
     ap.add_argument("--tpi", type=int, default=0,
                     help="threads per particle of the derivative / hydro kernels instead of autotuning (1, 2, 4)")
     ap.add_argument("--batch-runs", type=int, default=256)
@@ -126,17 +128,27 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def workload(n_total, seed=2024):
+def workload(n_total, seed=2024, config="1m"):
+    """1m: two-layer iron / dunite impact, 30 deg, 1.2 v_esc (the headline workload, at n_total);
+    4m: three-layer iron / dunite / granite-crust impact, 45 deg, 1.0 v_esc"""
     from fdps_sph_gb300 import eos, ic
     nt = int(round(n_total * 0.9))
+    if config == "4m":
+        F, ids, mats, info = ic.config_4m_impact(n_target=nt, n_impactor=n_total - nt)
+        materials = [eos.synthetic_table(m) for m in ("iron", "dunite", "granite")]
+        return F, ids, mats, materials
     F, ids, mats, info = ic.config_1m_impact(seed=seed, n_target=nt, n_impactor=n_total - nt)
     materials = [eos.synthetic_table("iron"), eos.synthetic_table("dunite")]
     return F, ids, mats, materials
 
 
-def run_gpu(F, ids, mats, materials, precision, steps, warmup, device):
+WORKLOADS = {"1m": "two-layer impact (90% target, 10% impactor, iron/dunite, 30 deg, 1.2 v_esc)",
+             "4m": "three-layer impact (90% target, 10% impactor, iron/dunite/granite crust 5%, 45 deg, 1.0 v_esc)"}
+
+
+def run_gpu(F, ids, mats, materials, precision, steps, warmup, device, theta=0.5):
     from fdps_sph_gb300 import lib
-    ctx = lib.Context(precision=precision, device=device)
+    ctx = lib.Context(precision=precision, device=device, theta=theta)
     for k, m in enumerate(materials):
         ctx.set_material(k, m)
     ctx.upload(F, ids, mats)
@@ -304,14 +316,14 @@ def main():
     from fdps_sph_gb300 import lib
     import torch
     device = int(os.environ.get("LOCAL_RANK", 0))
-    F, ids, mats, materials = workload(a.n)
+    F, ids, mats, materials = workload(a.n, config=a.config)
     n = F.shape[1]
 
     results = {}
     precisions = ["mixed"] if a.no_fp64 else ["mixed", "fp64"]
     for prec in precisions:
         ctx, ms, seg, cnt, launches, clocks, dr, tune, first = run_gpu(F, ids, mats, materials, prec, a.steps,
-                                                                       a.warmup, device)
+                                                                       a.warmup, device, a.theta)
         e2e = run_e2e(ctx, F, ids, mats, a.e2e_steps) if prec == "mixed" else None
         results[prec] = dict(ms=ms, seg=seg, cnt=cnt, launches=launches, clocks=clocks, e2e=e2e, drift=dr, tune=tune,
                              first=first)
@@ -381,8 +393,8 @@ def main():
         "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 pair sums + f64", "data": "synthetic (seeded IC generator, synthetic 200x200 rho-u tables)",
-        "config": {"workload": "1M-particle two-layer impact (900k + 100k, iron/dunite, 30 deg, 1.2 v_esc, "
-                               "theta 0.5)", "particles": n, "precision": "mixed",
+        "config": {"workload": f"{n:,}-particle {WORKLOADS[a.config]}, theta {a.theta}", "particles": n,
+                   "precision": "mixed",
                    "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas" if world > 1 else "1 GPU"},
         "gpu_launches": int(mixed["launches"]),
         "clocks": mixed["clocks"],
