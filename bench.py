@@ -64,6 +64,8 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched sweep and the serving window")
     ap.add_argument("--config", default="1m", choices=["1m", "4m"], help="geometry of the workload (see workload())")
     ap.add_argument("--theta", type=float, default=0.5, help="gravity opening angle")
+    ap.add_argument("--mode", type=int, default=1, choices=[1, 2],
+                    help="2: every step ends with SetConstantEntropy + CalcAll (120 x 120 tables)")
     ap.add_argument("--tpi", type=int, default=0,
                     help="threads per particle of the derivative / hydro kernels instead of autotuning (1, 2, 4)")
     ap.add_argument("--batch-runs", type=int, default=256)
@@ -128,17 +130,22 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def workload(n_total, seed=2024, config="1m"):
+def workload(n_total, seed=2024, config="1m", mode=1):
     """1m: two-layer iron / dunite impact, 30 deg, 1.2 v_esc (the headline workload, at n_total);
-    4m: three-layer iron / dunite / granite-crust impact, 45 deg, 1.0 v_esc"""
+    4m: three-layer iron / dunite / granite-crust impact, 45 deg, 1.0 v_esc.  Mode 2 reads the
+    tables through the reference's 120-line slices, so it takes 120 x 120 tables (the size of the
+    reference's own) reaching down to 1e-3 kg/m^3 instead of the 200 x 200 ones."""
     from fdps_sph_gb300 import eos, ic
     nt = int(round(n_total * 0.9))
+    names = ("iron", "dunite", "granite") if config == "4m" else ("iron", "dunite")
+    if mode == 2:
+        materials = [eos.synthetic_table(m, 120, 120, rho_range=(1e-3, 3e4)) for m in names]
+    else:
+        materials = [eos.synthetic_table(m) for m in names]
     if config == "4m":
         F, ids, mats, info = ic.config_4m_impact(n_target=nt, n_impactor=n_total - nt)
-        materials = [eos.synthetic_table(m) for m in ("iron", "dunite", "granite")]
-        return F, ids, mats, materials
-    F, ids, mats, info = ic.config_1m_impact(seed=seed, n_target=nt, n_impactor=n_total - nt)
-    materials = [eos.synthetic_table("iron"), eos.synthetic_table("dunite")]
+    else:
+        F, ids, mats, info = ic.config_1m_impact(seed=seed, n_target=nt, n_impactor=n_total - nt)
     return F, ids, mats, materials
 
 
@@ -146,9 +153,9 @@ WORKLOADS = {"1m": "two-layer impact (90% target, 10% impactor, iron/dunite, 30 
              "4m": "three-layer impact (90% target, 10% impactor, iron/dunite/granite crust 5%, 45 deg, 1.0 v_esc)"}
 
 
-def run_gpu(F, ids, mats, materials, precision, steps, warmup, device, theta=0.5):
+def run_gpu(F, ids, mats, materials, precision, steps, warmup, device, theta=0.5, mode=1):
     from fdps_sph_gb300 import lib
-    ctx = lib.Context(precision=precision, device=device, theta=theta)
+    ctx = lib.Context(precision=precision, device=device, theta=theta, mode=mode)
     for k, m in enumerate(materials):
         ctx.set_material(k, m)
     ctx.upload(F, ids, mats)
@@ -316,14 +323,14 @@ def main():
     from fdps_sph_gb300 import lib
     import torch
     device = int(os.environ.get("LOCAL_RANK", 0))
-    F, ids, mats, materials = workload(a.n, config=a.config)
+    F, ids, mats, materials = workload(a.n, config=a.config, mode=a.mode)
     n = F.shape[1]
 
     results = {}
     precisions = ["mixed"] if a.no_fp64 else ["mixed", "fp64"]
     for prec in precisions:
         ctx, ms, seg, cnt, launches, clocks, dr, tune, first = run_gpu(F, ids, mats, materials, prec, a.steps,
-                                                                       a.warmup, device, a.theta)
+                                                                       a.warmup, device, a.theta, a.mode)
         e2e = run_e2e(ctx, F, ids, mats, a.e2e_steps) if prec == "mixed" else None
         results[prec] = dict(ms=ms, seg=seg, cnt=cnt, launches=launches, clocks=clocks, e2e=e2e, drift=dr, tune=tune,
                              first=first)
@@ -393,7 +400,8 @@ def main():
         "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 pair sums + f64", "data": "synthetic (seeded IC generator, synthetic 200x200 rho-u tables)",
-        "config": {"workload": f"{n:,}-particle {WORKLOADS[a.config]}, theta {a.theta}", "particles": n,
+        "config": {"workload": f"{n:,}-particle {WORKLOADS[a.config]}, theta {a.theta}" +
+                               (", mode 2 (constant entropy, 120 x 120 tables)" if a.mode == 2 else ""), "particles": n,
                    "precision": "mixed",
                    "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas" if world > 1 else "1 GPU"},
         "gpu_launches": int(mixed["launches"]),

@@ -332,6 +332,11 @@ void sph_config_default(sph_config *cfg) {
     cfg->damping = 1.0;
     cfg->G = 6.67e-11;
     cfg->device = 0;
+    cfg->mode = 1;
+    cfg->mantle_entropy = 3.12432609e+03;   // main.cpp:116-117
+    cfg->core_entropy = 3.12432609e+03;     // main.cpp:118-119
+    cfg->entropy_grid = 120;                // EoS.h:250-251, 403-404
+    cfg->entropy_abs = SPH_ENTROPY_ABS_INT;
 }
 
 int sph_ctx_create(const sph_config *cfg, sph_ctx **out) {
@@ -343,7 +348,9 @@ int sph_ctx_create(const sph_config *cfg, sph_ctx **out) {
     else sph_config_default(&ctx->cfg);
     const sph_config &c = ctx->cfg;
     if (!(c.theta >= 0.0) || c.n_leaf < 1 || c.n_group < 1 || c.n_dens_iter < 1 || c.n_dens_iter > 64 ||
-        (c.precision != SPH_PREC_FP64 && c.precision != SPH_PREC_MIXED)) {
+        (c.precision != SPH_PREC_FP64 && c.precision != SPH_PREC_MIXED) || (c.mode != 1 && c.mode != 2) ||
+        c.entropy_grid < 1 || (c.entropy_abs != SPH_ENTROPY_ABS_INT && c.entropy_abs != SPH_ENTROPY_ABS_REAL) ||
+        !std::isfinite(c.mantle_entropy) || !std::isfinite(c.core_entropy)) {
         delete ctx;
         return SPH_ERR_ARG;
     }
@@ -404,6 +411,7 @@ int sph_ctx_destroy(sph_ctx *ctx) {
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (void *p : ctx->table_allocs) cudaFree(p);
+    sph_entropy_free(ctx);
     for (auto &g : ctx->tree_graphs)
         if (g.exec) cudaGraphExecDestroy(g.exec);
     if (ctx->host_scalars) cudaFreeHost(ctx->host_scalars);
@@ -451,6 +459,64 @@ int sph_set_eos_table(sph_ctx *ctx, int material, const double *rho_axis, int n_
     m.u = du;
     m.pres = dp;
     m.snds = dc;
+    ctx->m2_dirty = true;
+    return upload_materials(ctx);
+}
+
+int sph_set_eos_entropy(sph_ctx *ctx, int material, const double *temp, const double *ent, const double *line_rho,
+                        const double *line_u) {
+    if (!ctx) return SPH_ERR_ARG;
+    if (material < 0 || material >= MAX_MATERIALS) return sph_fail(ctx, SPH_ERR_ARG, "material %d out of range", material);
+    DevMaterial &m = ctx->mats_host[material];
+    if (m.kind != 0) return sph_fail(ctx, SPH_ERR_STATE, "material %d is not a table (set it first)", material);
+    if (!temp || !ent) return sph_fail(ctx, SPH_ERR_TABLE, "material %d: temperature and entropy planes needed", material);
+    const size_t nl = (size_t)m.n_rho * m.n_u;
+    std::vector<double> lr(nl), lu(nl);
+    std::vector<double> rho_ax(m.n_rho), u_ax(m.n_u);
+    SPH_CUDA(ctx, cudaMemcpy(rho_ax.data(), m.rho, sizeof(double) * m.n_rho, cudaMemcpyDeviceToHost));
+    SPH_CUDA(ctx, cudaMemcpy(u_ax.data(), m.u, sizeof(double) * m.n_u, cudaMemcpyDeviceToHost));
+    for (size_t k = 0; k < nl; ++k) {
+        lr[k] = line_rho ? line_rho[k] : rho_ax[k / m.n_u];
+        lu[k] = line_u ? line_u[k] : u_ax[k % m.n_u];
+    }
+    // the binary searches of the mode-2 lookup stand for the reference's linear scans
+    // (interpolation.h:131-182) only over non-decreasing line densities
+    for (size_t k = 1; k < nl; ++k)
+        if (!(lr[k] >= lr[k - 1]))
+            return sph_fail(ctx, SPH_ERR_TABLE, "material %d: line densities not non-decreasing at line %zu", material, k);
+    for (size_t k = 0; k < nl; ++k)
+        if (!std::isfinite(lr[k]) || !std::isfinite(lu[k]) || !std::isfinite(ent[k]))
+            return sph_fail(ctx, SPH_ERR_TABLE, "material %d: non-finite mode-2 column at line %zu", material, k);
+    cudaSetDevice(ctx->device);
+    const size_t plane = sizeof(double) * nl;
+    char *d = nullptr;
+    if (cudaMalloc((void **)&d, 4 * plane) != cudaSuccess) {
+        cudaGetLastError();
+        return sph_fail(ctx, SPH_ERR_OOM, "mode-2 table columns");
+    }
+    ctx->table_allocs.push_back(d);
+    double *dt_ = (double *)d, *de = dt_ + nl, *dr = de + nl, *du = dr + nl;
+    SPH_CUDA(ctx, cudaMemcpy(dt_, temp, plane, cudaMemcpyHostToDevice));
+    SPH_CUDA(ctx, cudaMemcpy(de, ent, plane, cudaMemcpyHostToDevice));
+    SPH_CUDA(ctx, cudaMemcpy(dr, lr.data(), plane, cudaMemcpyHostToDevice));
+    SPH_CUDA(ctx, cudaMemcpy(du, lu.data(), plane, cudaMemcpyHostToDevice));
+    m.temp = dt_;
+    m.ent = de;
+    m.line_rho = dr;
+    m.line_u = du;
+    ctx->m2_dirty = true;
+    return upload_materials(ctx);
+}
+
+int sph_set_eos_ideal(sph_ctx *ctx, int material, double gamma) {
+    if (!ctx) return SPH_ERR_ARG;
+    if (material < 0 || material >= MAX_MATERIALS) return sph_fail(ctx, SPH_ERR_ARG, "material %d out of range", material);
+    if (!(gamma > 1.0) || !std::isfinite(gamma)) return sph_fail(ctx, SPH_ERR_ARG, "ideal gas needs gamma > 1");
+    DevMaterial &m = ctx->mats_host[material];
+    std::memset(&m, 0, sizeof(m));
+    m.kind = 2;
+    m.par[0] = gamma;
+    ctx->m2_dirty = true;
     return upload_materials(ctx);
 }
 
@@ -469,7 +535,9 @@ int sph_load_eos_table_file(sph_ctx *ctx, int material, const char *path) {
         ss >> hash >> n_rho >> n_u;
         if (hash != "#" || n_rho < 1 || n_u < 1) return sph_fail(ctx, SPH_ERR_TABLE, "%s: bad header", path);
     }
-    std::vector<double> rho(n_rho), u(n_u), P((size_t)n_rho * n_u), C((size_t)n_rho * n_u);
+    const size_t nl = (size_t)n_rho * n_u;
+    std::vector<double> rho(n_rho), u(n_u), P(nl), C(nl), T(nl), S(nl), LR(nl), LU(nl);
+    bool six = true;   // every line has the temperature and entropy columns
     size_t row = 0;
     while (std::getline(in, line)) {
         if (line.empty() || line[0] == '#') continue;
@@ -485,11 +553,17 @@ int sph_load_eos_table_file(sph_ctx *ctx, int material, const char *path) {
         if (li == 0) u[ci] = v[1];
         P[row] = v[3];
         C[row] = v[4];
+        LR[row] = v[0];
+        LU[row] = v[1];
+        T[row] = v[2];
+        if (k == 6) S[row] = v[5];
+        else six = false;
         ++row;
     }
-    if (row != (size_t)n_rho * n_u)
-        return sph_fail(ctx, SPH_ERR_TABLE, "%s: %zu rows, header says %d x %d", path, row, n_rho, n_u);
-    return sph_set_eos_table(ctx, material, rho.data(), n_rho, u.data(), n_u, P.data(), C.data());
+    if (row != nl) return sph_fail(ctx, SPH_ERR_TABLE, "%s: %zu rows, header says %d x %d", path, row, n_rho, n_u);
+    SPH_TRY(sph_set_eos_table(ctx, material, rho.data(), n_rho, u.data(), n_u, P.data(), C.data()));
+    if (!six) return SPH_OK;
+    return sph_set_eos_entropy(ctx, material, T.data(), S.data(), LR.data(), LU.data());
 }
 
 int sph_set_eos_tillotson(sph_ctx *ctx, int material, const double par[10]) {
@@ -501,6 +575,7 @@ int sph_set_eos_tillotson(sph_ctx *ctx, int material, const double par[10]) {
     std::memset(&m, 0, sizeof(m));
     m.kind = 1;
     for (int k = 0; k < 10; ++k) m.par[k] = par[k];
+    ctx->m2_dirty = true;
     return upload_materials(ctx);
 }
 
@@ -686,7 +761,13 @@ int sph_step(sph_ctx *ctx, int n_steps) {
         SPH_TRY(compute_forces(ctx));               // main.cpp:136-147
         SPH_TRY(sph_ext_force(ctx));                // main.cpp:148
         SPH_TRY(sph_final_kick(ctx));               // main.cpp:149-153
+        if (ctx->cfg.mode == 2) {                   // main.cpp:155-158
+            SPH_TRY(time_mark(ctx, SEG_FINAL));
+            SPH_TRY(sph_entropy_step(ctx));
+            SPH_TRY(time_mark(ctx, SEG_ENTROPY));
+        }
         SPH_TRY(sph_run_reduce_dt(ctx));            // main.cpp:160
+        if (ctx->cfg.mode == 2) SPH_TRY(sph_entropy_check(ctx));
         SPH_TRY(time_mark(ctx, SEG_FINAL));
         SPH_TRY(collect_timings(ctx));
         for (int r = 0; r < R.R; ++r) {

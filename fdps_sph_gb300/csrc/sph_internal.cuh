@@ -94,11 +94,25 @@ __device__ __forceinline__ void density_tail32(float sum, float invH, float dsca
     *h = (double)((float)SMTH_COEF * cbrtf((float)m / d));
 }
 
+// One slice of RestrictedBilinearInterpolation (interpolation.h:131-238) for a
+// fixed entropy: the slice's first line density and the energy interpolated
+// at that entropy between the slice's two entries nearest to it.
+struct EntropyEdge {
+    double p, u;
+    int undef, pad;      // undef: the reference indexes outside its vectors here
+};
+
 struct DevMaterial {
     int kind;            // 0 table, 1 Tillotson, 2 ideal gas, -1 unset
     int n_rho, n_u, pad;
     const double *rho, *u, *pres, *snds;
     double par[10];
+    // mode-2 columns of a table (null: none): temperature and entropy planes,
+    // density and energy of every line (file order)
+    const double *temp, *ent, *line_rho, *line_u;
+    // mode-2 slices at the material's entropy: lower by (last line <= rho) + 1,
+    // upper by (first line >= rho), n_rho * n_u + 1 entries each
+    const EntropyEdge *edge_lo, *edge_up;
 };
 
 // tree meta block (ints): level l cells are [meta[l], meta[l+1]) for l = 0..21;
@@ -293,6 +307,11 @@ struct sph_ctx {
         int drvt_tpi = 1, hydro_tpi = 1;   // threads per i-particle
     } tune;
 
+    // mode 2 (SetConstantEntropy + CalcAll, sph_entropy.cu)
+    int *m2_bad = nullptr;                             // device: failed lookups of the last entropy step
+    bool m2_dirty = true;                              // materials changed since the slices were built
+    void *m2_edges[sph::MAX_MATERIALS] = {nullptr};    // per material: edge_lo and edge_up
+
     // CUDA graphs of the sort + octree build: one per state-buffer parity and layout
     bool use_graphs = true;
     sph::TreeGraph tree_graphs[4];
@@ -306,6 +325,7 @@ enum {
     SEG_GRAV_LIST, SEG_GRAV, SEG_FINAL,
     SEG_SORT,       // root box, keys, radix sort, permutation (before SEG_TREE: levels and moments)
     SEG_NBR_PREP,   // walk units, cell reach, mixed-precision packs (after SEG_TREE)
+    SEG_ENTROPY,    // mode 2: SetConstantEntropy + CalcAll
     SEG_N
 };
 
@@ -354,6 +374,9 @@ int sph_work_counts(sph_ctx *ctx, int64_t out[8]);
 int sph_pack_mixed(sph_ctx *ctx);
 int sph_kick_drift_predict(sph_ctx *ctx);   // with each run's dt in runs.dt_dev
 int sph_final_kick(sph_ctx *ctx);
+int sph_entropy_step(sph_ctx *ctx);       // mode 2: SetConstantEntropy + CalcAll (sph_entropy.cu)
+int sph_entropy_check(sph_ctx *ctx);      // fails when the last entropy step had failed lookups
+void sph_entropy_free(sph_ctx *ctx);
 int sph_ext_force(sph_ctx *ctx);
 int sph_diag(sph_ctx *ctx, double out[8]);   // summed over the runs
 int sph_init_smth(sph_ctx *ctx, int64_t off, int64_t n);

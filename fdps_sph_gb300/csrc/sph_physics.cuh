@@ -76,6 +76,25 @@ __device__ __forceinline__ void table_lookup2(const DevMaterial &m, double rho, 
     }
 }
 
+// BilinearInterpolation::interpolate of one plane (EoS_t::Temperature / Entropy:
+// columns 2 / 5, EoS.h:254-260, 407-413)
+__device__ __forceinline__ double table_lookup1(const DevMaterial &m, const double *plane, double rho, double u) {
+    int li = lower_bound_d(m.rho, m.n_rho, rho);
+    int ci = lower_bound_d(m.u, m.n_u, u);
+    if (li > m.n_rho - 1) li = m.n_rho - 1;
+    if (ci > m.n_u - 1) ci = m.n_u - 1;
+    const int64_t nu = m.n_u;
+    if (li < m.n_rho - 1 && ci < m.n_u - 1 && li > 0 && ci > 0) {
+        const double r0 = m.rho[li - 1], r1 = m.rho[li], u0 = m.u[ci - 1], u1 = m.u[ci];
+        const double xi = (rho - r0) / (r1 - r0);
+        const double eta = (u - u0) / (u1 - u0);
+        const double w00 = (1 - xi) * (1 - eta), w10 = xi * (1 - eta), w01 = (1 - xi) * eta, w11 = xi * eta;
+        return w00 * plane[(int64_t)(li - 1) * nu + (ci - 1)] + w10 * plane[(int64_t)li * nu + (ci - 1)] +
+               w01 * plane[(int64_t)(li - 1) * nu + ci] + w11 * plane[(int64_t)li * nu + ci];
+    }
+    return plane[(int64_t)li * nu + ci];
+}
+
 // analytic Tillotson, same expressions as the oracle's or_tillotson
 __device__ __forceinline__ void tillotson(const double *p, double rho, double u, double &P, double &cs) {
     const double rho0 = p[0], u0 = p[1], uiv = p[2], ucv = p[3], A = p[4], B = p[5], a = p[6], b = p[7],

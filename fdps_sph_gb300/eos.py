@@ -40,9 +40,21 @@ class Table:
     temp: np.ndarray | None = None
     ent: np.ndarray | None = None
     name: str = ""
+    line_rho: np.ndarray | None = None   # column 0 of every line, file order (None: the axis repeated)
+    line_u: np.ndarray | None = None     # column 1 of every line
 
     def as_material(self) -> dict:
-        return {"kind": "table", "rho": self.rho, "u": self.u, "pres": self.pres, "snds": self.snds}
+        return {"kind": "table", "rho": self.rho, "u": self.u, "pres": self.pres, "snds": self.snds,
+                "temp": self.temp, "ent": self.ent, "line_rho": self.line_rho, "line_u": self.line_u}
+
+
+@dataclass
+class IdealGas:
+    """EoS::IdealGas (EoS.h:37-66): P = (gamma - 1) rho u, c_s = sqrt(gamma (gamma - 1) u)."""
+    gamma: float
+
+    def as_material(self) -> dict:
+        return {"kind": "ideal", "gamma": self.gamma}
 
 
 @dataclass
@@ -82,7 +94,8 @@ def read_rho_u(path: str) -> Table:
     if np.any(np.diff(rho) <= 0) or np.any(np.diff(u) <= 0):
         raise ValueError(f"{path}: axes must be strictly ascending")
     return Table(rho=rho, u=u, temp=data[:, :, 2].copy(), pres=data[:, :, 3].copy(),
-                 snds=data[:, :, 4].copy(), ent=data[:, :, 5].copy(), name=os.path.basename(path))
+                 snds=data[:, :, 4].copy(), ent=data[:, :, 5].copy(), name=os.path.basename(path),
+                 line_rho=data[:, :, 0].reshape(-1).copy(), line_u=data[:, :, 1].reshape(-1).copy())
 
 
 def write_rho_u(path: str, t: Table) -> None:
@@ -138,8 +151,10 @@ def synthetic_table(material: str, n_rho: int = 200, n_u: int = 200, rho_range=(
                     u_range=(1.0e3, 1.0e9)) -> Table:
     """Synthetic 'ANEOS-like' table: log-spaced density and energy axes, P and
     c_s from the analytic Tillotson parameters of ``material``.  Temperature
-    is u / (1000 J/kg/K) and entropy a smooth placeholder; neither is read by
-    the per-step path."""
+    is u / (1000 J/kg/K) and entropy 1000 ln(u / 1000) - 287 ln(rho / 1000)
+    (rising with u at fixed rho); both are read only by mode 2.  Every column
+    is rounded through the text format, so a written-then-read table is
+    bit-identical."""
     par = TILLOTSON[material]
     rho = np.geomspace(rho_range[0], rho_range[1], n_rho)
     u = np.geomspace(u_range[0], u_range[1], n_u)
@@ -150,8 +165,8 @@ def synthetic_table(material: str, n_rho: int = 200, n_u: int = 200, rho_range=(
     P, cs = tillotson_eval(par, R, U)
     P = np.vectorize(lambda v: float("%15.8E" % v))(P)
     cs = np.vectorize(lambda v: float("%15.8E" % v))(cs)
-    temp = U / 1.0e3
-    ent = 1.0e3 * np.log(U / 1.0e3) - 287.0 * np.log(R / 1.0e3)
+    temp = np.vectorize(lambda v: float("%15.8E" % v))(U / 1.0e3)
+    ent = np.vectorize(lambda v: float("%15.8E" % v))(1.0e3 * np.log(U / 1.0e3) - 287.0 * np.log(R / 1.0e3))
     return Table(rho=rho, u=u, pres=P, snds=cs, temp=temp, ent=ent, name=f"synthetic-{material}")
 
 

@@ -22,12 +22,12 @@ import numpy as np
 G = 6.67e-11
 M_EARTH = 5.972e24
 
-NFIELD = 32
+NFIELD = 34
 FIELDS = [
     "x", "y", "z", "vx", "vy", "vz", "mass", "smth", "dens", "eng",
     "pres", "snds", "div_v", "rot_x", "rot_y", "rot_z", "bal", "ava", "grad_smth",
     "ax", "ay", "az", "eng_dot", "vhx", "vhy", "vhz", "eng_half", "dt",
-    "gx", "gy", "gz", "pot",
+    "gx", "gy", "gz", "pot", "ent", "temp",
 ]
 FIELD = {n: i for i, n in enumerate(FIELDS)}
 

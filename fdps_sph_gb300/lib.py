@@ -15,12 +15,12 @@ from . import layouts as T
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libsph_gb300.so")
 
-NFIELD = 32
+NFIELD = 34
 FIELDS = [
     "x", "y", "z", "vx", "vy", "vz", "mass", "smth", "dens", "eng",
     "pres", "snds", "div_v", "rot_x", "rot_y", "rot_z", "bal", "ava", "grad_smth",
     "ax", "ay", "az", "eng_dot", "vhx", "vhy", "vhz", "eng_half", "dt",
-    "gx", "gy", "gz", "pot",
+    "gx", "gy", "gz", "pot", "ent", "temp",
 ]
 FIELD = {n: i for i, n in enumerate(FIELDS)}
 
@@ -39,11 +39,14 @@ EXPORTS = [
     "sph_get_neighbors", "sph_get_tree", "sph_get_grav_list", "sph_get_timings", "sph_step_timed",
     "sph_get_counters", "sph_probe_peak", "sph_morton_order_noalloc",
     "sph_add_run", "sph_remove_run", "sph_list_runs", "sph_run_info", "sph_download_run", "sph_run_diagnostics",
-    "sph_autotune",
+    "sph_autotune", "sph_set_eos_ideal", "sph_set_eos_entropy", "sph_eos_eval",
 ]
+EOS_QUANTITY = {"pressure": 0, "sound_speed": 1, "temperature": 2, "entropy": 3, "internal_energy": 4}
+ENTROPY_ABS_INT = 0
+ENTROPY_ABS_REAL = 1
 NOALLOC_MAX_N = 131072
 SEGMENTS = ["kdp", "tree", "dens_list", "dens", "eos", "drvt_list", "drvt", "hydro_list", "hydro", "grav_list",
-            "grav", "final", "sort", "nbr_prep"]
+            "grav", "final", "sort", "nbr_prep", "entropy"]
 
 
 class SphError(RuntimeError):
@@ -57,7 +60,8 @@ class Config(C.Structure):
         ("theta", C.c_double), ("n_leaf", C.c_int32), ("n_group", C.c_int32), ("n_dens_iter", C.c_int32),
         ("self_gravity", C.c_int32), ("ext_damp", C.c_int32), ("precision", C.c_int32),
         ("ext_damp_tend", C.c_double), ("damping", C.c_double), ("G", C.c_double), ("device", C.c_int32),
-        ("reserved", C.c_int32),
+        ("mode", C.c_int32), ("mantle_entropy", C.c_double), ("core_entropy", C.c_double),
+        ("entropy_grid", C.c_int32), ("entropy_abs", C.c_int32),
     ]
 
 
@@ -89,6 +93,9 @@ def load() -> C.CDLL:
     L.sph_set_eos_table.argtypes = [P, C.c_int, P, C.c_int, P, C.c_int, P, P]
     L.sph_load_eos_table_file.argtypes = [P, C.c_int, C.c_char_p]
     L.sph_set_eos_tillotson.argtypes = [P, C.c_int, P]
+    L.sph_set_eos_ideal.argtypes = [P, C.c_int, C.c_double]
+    L.sph_set_eos_entropy.argtypes = [P, C.c_int, P, P, P, P]
+    L.sph_eos_eval.argtypes = [P, C.c_int, C.c_int, C.c_int64, P, P, P, C.POINTER(C.c_int64)]
     L.sph_upload.argtypes = [P, C.c_int64, P, C.c_int64, P, P, C.c_double, C.c_double, C.c_int]
     L.sph_step_timed.argtypes = [P, C.c_int, C.POINTER(C.c_double)]
     L.sph_get_counters.argtypes = [P, P]
@@ -171,11 +178,33 @@ class Context:
             P = np.ascontiguousarray(d["pres"], np.float64)
             cs = np.ascontiguousarray(d["snds"], np.float64)
             self._check(self.L.sph_set_eos_table(self.h, k, _ptr(rho), len(rho), _ptr(u), len(u), _ptr(P), _ptr(cs)))
+            if d.get("temp") is not None and d.get("ent") is not None:
+                Tp = np.ascontiguousarray(d["temp"], np.float64)
+                Sp = np.ascontiguousarray(d["ent"], np.float64)
+                lr = d.get("line_rho")
+                lu = d.get("line_u")
+                lr = None if lr is None else np.ascontiguousarray(lr, np.float64)
+                lu = None if lu is None else np.ascontiguousarray(lu, np.float64)
+                self._check(self.L.sph_set_eos_entropy(self.h, k, _ptr(Tp), _ptr(Sp), _ptr(lr), _ptr(lu)))
         elif d["kind"] == "tillotson":
             par = np.ascontiguousarray(d["par"], np.float64)
             self._check(self.L.sph_set_eos_tillotson(self.h, k, _ptr(par)))
+        elif d["kind"] == "ideal":
+            self._check(self.L.sph_set_eos_ideal(self.h, k, float(d["gamma"])))
         else:
             raise ValueError(d["kind"])
+
+    def eos_eval(self, k: int, quantity: str, a, b):
+        """EoS_t quantity of material k on the device: (values, undefined count); a = rho, b = u
+        (or s for internal_energy)"""
+        a = np.ascontiguousarray(a, np.float64).reshape(-1)
+        b = np.ascontiguousarray(b, np.float64).reshape(-1)
+        assert a.shape == b.shape
+        out = np.empty_like(a)
+        undef = C.c_int64()
+        self._check(self.L.sph_eos_eval(self.h, k, EOS_QUANTITY[quantity], len(a), _ptr(a), _ptr(b), _ptr(out),
+                                        C.byref(undef)))
+        return out, int(undef.value)
 
     def load_table_file(self, k: int, path: str):
         self._check(self.L.sph_load_eos_table_file(self.h, k, path.encode()))

@@ -6,14 +6,14 @@
   and the particle count (``%d``) on two lines, then one line per particle,
   tab-separated, ``id tag mass x y z vx vy vz dens eng pres pot ent temp``
   (``%lld`` / ``%lf``).  ``tag`` carries the material slot; ``ent`` and
-  ``temp`` (entropy and temperature of the mode-2 path) are written as 0.
+  ``temp`` are the state's entropy and temperature (written by mode 2).
   The format rounds to 6 decimals, as the reference's does.
 * Checkpoints: a pointer-free binary file that restores a context exactly
   (the reference's restart file, io.h:7-23, writes raw structs including an
   EoS pointer).  Layout: the 8-byte magic ``SPHGB3CK``, a little-endian
   uint64 header length, a JSON header (format version, field names, per-run
   particle counts, times, dts, steps, and the byte offsets of the arrays),
-  then per run the field-major float64 state [32][n], int64 ids and int32
+  then per run the field-major float64 state [34][n], int64 ids and int32
   material slots.  Restored with forces valid, so the next step continues
   the same trajectory.
 """
@@ -27,7 +27,7 @@ from .ic import FIELD, FIELDS, NFIELD
 
 ASCII_COLUMNS = ["id", "tag", "mass", "x", "y", "z", "vx", "vy", "vz", "dens", "eng", "pres", "pot", "ent", "temp"]
 MAGIC = b"SPHGB3CK"
-VERSION = 1
+VERSION = 2   # 2: the state carries ent and temp (34 fields)
 
 
 def ascii_path(base: str, nproc: int = 1, rank: int = 0) -> str:
@@ -39,8 +39,7 @@ def write_ascii(base: str, F: np.ndarray, ids: np.ndarray, mats: np.ndarray, tim
     """writes one snapshot in the reference's text format; returns the file name"""
     n = F.shape[1]
     path = ascii_path(base)
-    zero = np.zeros(n)
-    cols = [F[FIELD[c]] if c in FIELD else zero for c in ASCII_COLUMNS[2:]]
+    cols = [F[FIELD[c]] for c in ASCII_COLUMNS[2:]]
     with open(path, "w") as fh:
         fh.write("%e\n%d\n" % (time, n))
         fmt = "%d\t%d\t" + "\t".join(["%f"] * len(cols)) + "\n"

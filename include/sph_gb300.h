@@ -103,7 +103,9 @@ enum sph_field {
     SPH_X = 0, SPH_Y, SPH_Z, SPH_VX, SPH_VY, SPH_VZ, SPH_MASS, SPH_SMTH, SPH_DENS, SPH_ENG,
     SPH_PRES, SPH_SNDS, SPH_DIVV, SPH_ROTX, SPH_ROTY, SPH_ROTZ, SPH_BAL, SPH_AVA, SPH_GRADH,
     SPH_AX, SPH_AY, SPH_AZ, SPH_ENGDOT, SPH_VHX, SPH_VHY, SPH_VHZ, SPH_ENGHALF, SPH_DT,
-    SPH_GX, SPH_GY, SPH_GZ, SPH_POT, SPH_NFIELD
+    SPH_GX, SPH_GY, SPH_GZ, SPH_POT,
+    SPH_ENT, SPH_TEMP,       /* entropy and temperature (class.h:96-98), written by mode 2 */
+    SPH_NFIELD
 };
 
 #define SPH_PREC_FP64 0    /* every pair sum in FP64 (parity path) */
@@ -121,8 +123,20 @@ typedef struct {
     double damping;          /* dampMotion factor (1.0) */
     double G;                /* 6.67e-11 (force.h:171-172) */
     int32_t device;          /* CUDA device ordinal */
-    int32_t reserved;
+    int32_t mode;            /* 1 or 2 ("mode", main.cpp:115): 2 ends every step with
+                                SetConstantEntropy + CalcAll (main.cpp:155-158, force.h:55-84) */
+    double mantle_entropy;   /* entropy of material 0 in mode 2 ("mantle_entropy", main.cpp:116-117) */
+    double core_entropy;     /* entropy of every other material ("core_entropy", main.cpp:118-119) */
+    int32_t entropy_grid;    /* grid_length of RestrictedBilinearInterpolation: 120, the constant
+                                EoS.h:250-251 and 403-404 pass */
+    int32_t entropy_abs;     /* distance in its nearest-entropy search (interpolation.h:199-200):
+                                SPH_ENTROPY_ABS_INT (the reference compiled with main.cpp's own
+                                includes: unqualified abs() of a double resolves to int abs(int),
+                                so distances are truncated to integers) or SPH_ENTROPY_ABS_REAL */
 } sph_config;
+
+#define SPH_ENTROPY_ABS_INT 0
+#define SPH_ENTROPY_ABS_REAL 1
 
 typedef struct sph_ctx sph_ctx;
 
@@ -141,6 +155,34 @@ int sph_set_eos_table(sph_ctx *ctx, int material, const double *rho_axis, int n_
 int sph_load_eos_table_file(sph_ctx *ctx, int material, const char *path);
 /* Analytic Tillotson: rho0 u0 uiv ucv A B a b alpha beta (EoS.h:116-238 parameter order). */
 int sph_set_eos_tillotson(sph_ctx *ctx, int material, const double par[10]);
+/* Ideal gas (EoS.h:37-66) with heat-capacity ratio gamma. */
+int sph_set_eos_ideal(sph_ctx *ctx, int material, double gamma);
+/* The columns of a table material that mode 2 reads (call after
+ * sph_set_eos_table for the same slot; sph_load_eos_table_file sets them):
+ * temperature (column 2) and entropy (column 5) planes [n_rho * n_u], and the
+ * density and energy columns of every table line, line_rho / line_u
+ * [n_rho * n_u] (columns 0 and 1 in file order; the reference's
+ * full_densities / full_energies, EoS.h:290-390; NULL = the axes repeated).
+ * line_rho must be non-decreasing. */
+int sph_set_eos_entropy(sph_ctx *ctx, int material, const double *temp, const double *ent,
+                        const double *line_rho, const double *line_u);
+
+/* The EoS surface of EoS_t (EoS.h:11-31) on the device, for n points in host
+ * memory: out[i] = quantity(a[i], b[i]) of `material`.  Quantities:
+ *   SPH_EOS_PRESSURE, SPH_EOS_SOUND_SPEED   (rho, u)  EoS.h:241-247, 394-400
+ *   SPH_EOS_TEMPERATURE, SPH_EOS_ENTROPY    (rho, u)  EoS.h:254-260, 407-413
+ *   SPH_EOS_INTERNAL_ENERGY                 (rho, s)  EoS.h:249-252, 402-405
+ * (ideal gas: EoS.h:43-61).  INTERNAL_ENERGY uses the context's entropy_grid
+ * and entropy_abs; a lookup whose reference evaluation would index outside
+ * its vectors (undefined there) returns NaN and is counted in *undefined
+ * (may be null). */
+#define SPH_EOS_PRESSURE 0
+#define SPH_EOS_SOUND_SPEED 1
+#define SPH_EOS_TEMPERATURE 2
+#define SPH_EOS_ENTROPY 3
+#define SPH_EOS_INTERNAL_ENERGY 4
+int sph_eos_eval(sph_ctx *ctx, int material, int quantity, int64_t n, const double *a, const double *b,
+                 double *out, int64_t *undefined);
 
 /* Copies n particles (host memory) into the context; particle i keeps slot i
  * for download.  flags:
@@ -160,7 +202,12 @@ int sph_upload(sph_ctx *ctx, int64_t n, const double *fields, int64_t ld, const 
 int sph_download(sph_ctx *ctx, double *fields, int64_t ld, int64_t *id, int32_t *material);
 /* Forces of the current state and the first dt (main.cpp:92-105). */
 int sph_prologue(sph_ctx *ctx);
-/* n_steps iterations of the loop body of main.cpp:125-173 (mode 1). */
+/* n_steps iterations of the loop body of main.cpp:125-173.  In mode 2 each
+ * step ends, after the final kick, with ent = mantle_entropy for material 0
+ * and core_entropy otherwise (SetConstantEntropy, force.h:55-65), then
+ * eng = InternalEnergy(dens, ent) and temp = Temperature(dens, eng) (CalcAll,
+ * force.h:73-84); a lookup that is undefined in the reference or gives a
+ * non-finite energy fails the step with SPH_ERR_NONFINITE. */
 int sph_step(sph_ctx *ctx, int n_steps);
 int sph_get_time(const sph_ctx *ctx, double *time, double *dt, int64_t *step);
 
@@ -220,7 +267,7 @@ int sph_get_grav_list(sph_ctx *ctx, int64_t g, int64_t *n_group, int32_t *epj, i
  * moments, density lists, density kernels, EoS, derivative list, derivative
  * kernel, hydro list, hydro kernel, gravity groups (and lists on the FP64
  * path), gravity kernel, final kick + dt, key sort + permutation, neighbour
- * walk preparation.
+ * walk preparation, mode-2 entropy step (SetConstantEntropy + CalcAll).
  * cap = -1 switches timing on (and resets), -2 switches it off, -3 resets. */
 int sph_get_timings(sph_ctx *ctx, double *ms, int cap, int *n);
 /* sph_step bracketed by CUDA events on the context's stream; device_ms = elapsed. */

@@ -13,12 +13,12 @@ import numpy as np
 
 from . import build_oracle
 
-NFIELD = 32
+NFIELD = 34
 FIELDS = [
     "x", "y", "z", "vx", "vy", "vz", "mass", "smth", "dens", "eng",
     "pres", "snds", "div_v", "rot_x", "rot_y", "rot_z", "bal", "ava", "grad_smth",
     "ax", "ay", "az", "eng_dot", "vhx", "vhy", "vhz", "eng_half", "dt",
-    "gx", "gy", "gz", "pot",
+    "gx", "gy", "gz", "pot", "ent", "temp",
 ]
 FIELD = {n: i for i, n in enumerate(FIELDS)}
 
@@ -29,6 +29,8 @@ class Material(C.Structure):
         ("rho", C.POINTER(C.c_double)), ("u", C.POINTER(C.c_double)),
         ("pres", C.POINTER(C.c_double)), ("snds", C.POINTER(C.c_double)),
         ("par", C.c_double * 10),
+        ("temp", C.POINTER(C.c_double)), ("ent", C.POINTER(C.c_double)),
+        ("line_rho", C.POINTER(C.c_double)), ("line_u", C.POINTER(C.c_double)),
     ]
 
 
@@ -38,6 +40,8 @@ class Config(C.Structure):
         ("n_dens_iter", C.c_int32), ("self_gravity", C.c_int32), ("ext_damp", C.c_int32),
         ("ext_damp_tend", C.c_double), ("damping", C.c_double), ("G", C.c_double),
         ("n_mat", C.c_int32), ("mat", C.POINTER(Material)),
+        ("mode", C.c_int32), ("entropy_grid", C.c_int32), ("entropy_abs", C.c_int32),
+        ("mantle_entropy", C.c_double), ("core_entropy", C.c_double),
     ]
 
 
@@ -88,6 +92,14 @@ def lib(fast: bool = False) -> C.CDLL:
                                       C.POINTER(C.c_double), C.c_double, C.c_double]
         L.or_eos_eval.argtypes = [C.POINTER(Material), C.c_double, C.c_double, C.POINTER(C.c_double),
                                   C.POINTER(C.c_double)]
+        for f in ("or_eos_temperature", "or_eos_entropy"):
+            getattr(L, f).restype = C.c_double
+            getattr(L, f).argtypes = [C.POINTER(Material), C.c_double, C.c_double]
+        L.or_eos_internal_energy.restype = C.c_double
+        L.or_eos_internal_energy.argtypes = [C.POINTER(Material), C.c_double, C.c_double, C.c_int, C.c_int,
+                                             C.POINTER(C.c_int)]
+        L.or_entropy_step.restype = C.c_int64
+        L.or_entropy_step.argtypes = [C.POINTER(System), C.POINTER(Config)]
         L.or_root_box.argtypes = [C.POINTER(C.c_double)] * 3 + [C.c_int64, C.POINTER(RootBox)]
         L.or_morton_keys.argtypes = [C.POINTER(C.c_double)] * 3 + [C.c_int64, C.POINTER(RootBox),
                                                                    C.POINTER(C.c_uint64)]
@@ -148,6 +160,15 @@ class MaterialSet:
                 mm.kind = 0
                 mm.n_rho, mm.n_u = len(rho), len(u)
                 mm.rho, mm.u, mm.pres, mm.snds = _p(rho), _p(u), _p(P), _p(cs)
+                if m.get("temp") is not None and m.get("ent") is not None:
+                    T = np.ascontiguousarray(m["temp"], dtype=np.float64).reshape(-1)
+                    S = np.ascontiguousarray(m["ent"], dtype=np.float64).reshape(-1)
+                    lr = m.get("line_rho")
+                    lu = m.get("line_u")
+                    lr = np.repeat(rho, len(u)) if lr is None else np.ascontiguousarray(lr, np.float64).reshape(-1)
+                    lu = np.tile(u, len(rho)) if lu is None else np.ascontiguousarray(lu, np.float64).reshape(-1)
+                    self._keep += [T, S, lr, lu]
+                    mm.temp, mm.ent, mm.line_rho, mm.line_u = _p(T), _p(S), _p(lr), _p(lu)
             elif m["kind"] == "tillotson":
                 mm.kind = 1
                 for q, v in enumerate(m["par"]):
@@ -166,9 +187,24 @@ class MaterialSet:
         lib().or_eos_eval(C.byref(self.arr[k]), float(rho), float(u), C.byref(P), C.byref(cs))
         return P.value, cs.value
 
+    def temperature(self, k, rho, u):
+        return lib().or_eos_temperature(C.byref(self.arr[k]), float(rho), float(u))
+
+    def entropy(self, k, rho, u):
+        return lib().or_eos_entropy(C.byref(self.arr[k]), float(rho), float(u))
+
+    def internal_energy(self, k, rho, s, grid=120, abs_mode=0):
+        """(u, undefined) of RestrictedBilinearInterpolation (literal O(lines) scans)"""
+        undef = C.c_int()
+        u = lib().or_eos_internal_energy(C.byref(self.arr[k]), float(rho), float(s), int(grid), int(abs_mode),
+                                         C.byref(undef))
+        return u, bool(undef.value)
+
 
 def make_config(materials: MaterialSet, theta=0.5, n_leaf=8, n_group=256, n_dens_iter=4, self_gravity=True,
-                ext_damp=False, ext_damp_tend=5000.0, damping=1.0, G=6.67e-11) -> Config:
+                ext_damp=False, ext_damp_tend=5000.0, damping=1.0, G=6.67e-11, mode=1,
+                mantle_entropy=3.12432609e3, core_entropy=3.12432609e3, entropy_grid=120,
+                entropy_abs=0) -> Config:
     cfg = Config()
     cfg.theta = theta
     cfg.n_leaf = n_leaf
@@ -181,6 +217,11 @@ def make_config(materials: MaterialSet, theta=0.5, n_leaf=8, n_group=256, n_dens
     cfg.G = G
     cfg.n_mat = materials.n
     cfg.mat = C.cast(materials.arr, C.POINTER(Material))
+    cfg.mode = mode
+    cfg.mantle_entropy = mantle_entropy
+    cfg.core_entropy = core_entropy
+    cfg.entropy_grid = entropy_grid
+    cfg.entropy_abs = entropy_abs
     cfg._materials = materials  # keep alive
     return cfg
 
@@ -212,8 +253,14 @@ class OracleSystem:
 
     def step(self, cfg, n_steps=1):
         rc = self.lib.or_step(C.byref(self.sys), C.byref(cfg), int(n_steps))
+        if rc == -2:
+            raise RuntimeError("oracle step: a mode-2 energy lookup is undefined or non-finite")
         if rc != 0:
             raise RuntimeError("oracle step failed")
+
+    def entropy_step(self, cfg):
+        """SetConstantEntropy + CalcAll on the current state; returns the undefined / non-finite count"""
+        return int(self.lib.or_entropy_step(C.byref(self.sys), C.byref(cfg)))
 
     def compute_forces(self, cfg):
         if self.lib.or_compute_forces(C.byref(self.sys), C.byref(cfg)) != 0:

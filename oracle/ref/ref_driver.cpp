@@ -12,6 +12,8 @@
 //   dens|drvt|hydro|grav : walk file (see read_walks) -> RESULT[sum n_i]
 //   eos_file : len, path, kind, n, {rho,u}[n]        -> {P, cs}[n]
 //   eos_static : which, n, {rho,u}[n]                -> {P, cs}[n]  (cwd = reference root)
+//   eos_mode2 : len, path, kind, grid, n, {rho,s,u}[n]
+//               -> {InternalEnergy(rho, s, grid), Temperature(rho, u), Entropy(rho, u)}[n]
 //   balsara  : n, {div_v, rx, ry, rz, grad_smth, snds, smth}[n] -> {Bal, grad_smth, div_v}[n]
 //   integ    : n, dt, damping, record[n]             -> record_out[n]
 //   dtglobal : n, {dt, ax, ay, az, gx, gy, gz}[n]    -> dt
@@ -163,6 +165,35 @@ int main(int argc, char **argv) {
             in.get(ru, 2);
             const double o[2] = {eos->Pressure(ru[0], ru[1]), eos->SoundSpeed(ru[0], ru[1])};
             out.put(o, 2);
+        }
+        delete an;
+        delete ti;
+    } else if (mode == "eos_mode2") {
+        // The mode-2 EoS surface (EoS.h:249-260, 402-413).  InternalEnergy
+        // ignores its grid_size argument and passes 120 (EoS.h:250-251).
+        const int len = in.get<int32_t>();
+        std::string path(len, '\0');
+        in.get(&path[0], len);
+        const int kind = in.get<int32_t>();
+        const int grid = in.get<int32_t>();
+        const int n = in.get<int32_t>();
+        const EoS::EoS_t<PS::F64> *eos = nullptr;
+        EoS::ANEOS<PS::F64> *an = nullptr;
+        EoS::Tillotson<PS::F64> *ti = nullptr;
+        if (kind == 0) {
+            an = new EoS::ANEOS<PS::F64>(path);
+            eos = an;
+        } else {
+            ti = new EoS::Tillotson<PS::F64>(2680.0, 16.0e+6, 3.5e+6, 18.00e+6, 18.0e+9, 18.0e+9, 0.5, 1.3, 5.0,
+                                             5.0, path);
+            eos = ti;
+        }
+        for (int i = 0; i < n; ++i) {
+            double rsu[3];
+            in.get(rsu, 3);
+            const double o[3] = {eos->InternalEnergy(rsu[0], rsu[1], grid), eos->Temperature(rsu[0], rsu[2]),
+                                 eos->Entropy(rsu[0], rsu[2])};
+            out.put(o, 3);
         }
         delete an;
         delete ti;

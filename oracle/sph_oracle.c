@@ -171,6 +171,176 @@ void or_eos_eval(const or_material *m, double rho, double u, double *P, double *
 }
 
 /* ------------------------------------------------------------------------ */
+/* Mode-2 EoS surface: Temperature, Entropy, InternalEnergy                  */
+
+/* EoS_t::Temperature / Entropy of the table classes: bilinear on columns 2 and
+ * 5 (EoS.h:254-260, 407-413); IdealGas returns 0 (EoS.h:55-61). */
+double or_eos_temperature(const or_material *m, double rho, double u) {
+    if (m->kind == 2) return 0.0;
+    if (m->kind != 0 || !m->temp) return NAN;
+    return or_table_lookup(m->rho, m->n_rho, m->u, m->n_u, m->temp, rho, u);
+}
+
+double or_eos_entropy(const or_material *m, double rho, double u) {
+    if (m->kind == 2) return 0.0;
+    if (m->kind != 0 || !m->ent) return NAN;
+    return or_table_lookup(m->rho, m->n_rho, m->u, m->n_u, m->ent, rho, u);
+}
+
+/* get_neighbors_restricted_indices(v, value, grid_length, bound)
+ * (interpolation.h:131-182), literally: a forward scan for the first line with
+ * v >= value ("upper"), a scan from the end for the last line with v <= value
+ * ("lower"), in the reference's unsigned 32-bit index arithmetic. */
+static void or_restricted_bounds(const double *v, int64_t size, double value, uint32_t G, int upper, uint32_t *b1,
+                                 uint32_t *b2) {
+    uint32_t lo = 0, hi = 0;
+    if (upper) {
+        for (int64_t a = 0; a < size; ++a)
+            if (v[a] >= value) {
+                lo = (uint32_t)a;
+                hi = (uint32_t)a + G;
+                if ((uint64_t)hi > (uint64_t)(size - 1)) hi = (uint32_t)(size - 1);
+                break;
+            }
+    } else {
+        for (int64_t a = 0; a < size; ++a)
+            if (v[size - 1 - a] <= value) {
+                lo = (uint32_t)(size - 1) - (uint32_t)a - (G - 1u);
+                hi = lo + G;
+                if (hi == 0) hi = G;
+                break;
+            }
+    }
+    if (lo == 0 && hi == 0) {
+        lo = 0;
+        hi = G;
+    }
+    *b1 = lo;
+    *b2 = hi;
+}
+
+/* slice(v, m, n) (interpolation.h:17-25) reads [m, n]: defined for 0 <= m <= n + 1 <= size */
+static int or_slice_ok(uint32_t b1, uint32_t b2, int64_t size) {
+    const int64_t m = (int32_t)b1, n = (int32_t)b2;
+    return m >= 0 && m <= n + 1 && n + 1 <= size;
+}
+
+/* abs() of a double as the reference's translation unit resolves it (int
+ * abs(int) of the truncated value): defined for -2^31 < d < 2^31 */
+static int or_int_abs(double d, int64_t *out) {
+    if (!(d > -2147483648.0 && d < 2147483648.0)) return 0;
+    const int64_t t = (int64_t)d;
+    *out = t < 0 ? -t : t;
+    return 1;
+}
+
+/* get_var2_neighbors (interpolation.h:186-238): positions (p0, p1) in the slice
+ * around its entry nearest to `given` (first nearest in scan order).  Returns
+ * 0 where the reference's distance arithmetic is undefined. */
+static int or_var2_pair(const double *sl, int64_t L, double given, uint32_t G, int abs_mode, int32_t *p0, int32_t *p1) {
+    double min_d = 0.0;
+    uint32_t idx = 0;
+    int ok = 1;
+    for (int64_t a = 0; a < L; ++a) {
+        const double d = given - sl[a];
+        if (a == 0) {
+            min_d = d;
+            idx = 0;
+            continue;
+        }
+        int closer;
+        if (abs_mode == 0) {
+            int64_t di = 0, dm = 0;
+            ok &= or_int_abs(d, &di);
+            ok &= or_int_abs(min_d, &dm);
+            closer = di < dm;
+        } else {
+            closer = fabs(d) < fabs(min_d);
+        }
+        if (closer) {
+            min_d = d;
+            idx = (uint32_t)a;
+        }
+    }
+    uint32_t f, s;
+    if (min_d < 0) {
+        if (idx <= 0) { f = idx; s = idx + 1; }
+        else if (idx + 1 == G) { f = idx - 2; s = idx - 1; }
+        else { f = idx - 1; s = idx; }
+    } else if (min_d > 0) {
+        if (idx + 1 == G) { f = idx - 2; s = idx - 1; }
+        else { f = idx; s = idx + 1; }
+    } else {
+        if (idx >= G - 1) { f = idx - 2; s = idx - 1; }
+        else { f = idx - 1; s = idx + 1; }
+    }
+    *p0 = (int32_t)f;
+    *p1 = (int32_t)s;
+    return ok;
+}
+
+/* linear_interpolate (interpolation.h:254-262) */
+static double or_lerp(double x1, double x2, double x, double q1, double q2) {
+    return (((x2 - x) / (x2 - x1)) * q1) + (((x - x1) / (x2 - x1)) * q2);
+}
+
+/* RestrictedBilinearInterpolation::interpolate (interpolation.h:265-334) with
+ * var1 = line densities, var2 = line entropies, var3 = line energies, as
+ * InternalEnergy calls it (EoS.h:249-252, 402-405); IdealGas returns 0
+ * (EoS.h:51-53).  The analytic Tillotson mode has no entropy data: NaN. */
+double or_eos_internal_energy(const or_material *m, double rho, double s, int grid, int abs_mode, int *undef) {
+    *undef = 0;
+    if (m->kind == 2) return 0.0;
+    if (m->kind != 0 || !m->ent || !m->line_rho || !m->line_u || grid < 1) {
+        *undef = 1;
+        return NAN;
+    }
+    const int64_t size = (int64_t)m->n_rho * m->n_u;
+    const double *vr = m->line_rho, *ve = m->ent, *vu = m->line_u;
+    const uint32_t G = (uint32_t)grid;
+    uint32_t l1, l2, h1, h2;
+    or_restricted_bounds(vr, size, rho, G, 0, &l1, &l2);
+    or_restricted_bounds(vr, size, rho, G, 1, &h1, &h2);
+    if (!or_slice_ok(l1, l2, size) || !or_slice_ok(h1, h2, size)) {
+        *undef = 1;
+        return NAN;
+    }
+    const int64_t Ll = (int64_t)(int32_t)l2 - (int32_t)l1 + 1, Lh = (int64_t)(int32_t)h2 - (int32_t)h1 + 1;
+    int32_t a0, a1, c0, c1;
+    const int ok = or_var2_pair(ve + l1, Ll, s, G, abs_mode, &a0, &a1) &
+                   or_var2_pair(ve + h1, Lh, s, G, abs_mode, &c0, &c1);
+    if (!ok || Ll < 1 || Lh < 1 || a0 < 0 || a1 < 0 || c0 < 0 || c1 < 0 || a0 >= Ll || a1 >= Ll || c0 >= Lh ||
+        c1 >= Lh) {
+        *undef = 1;
+        return NAN;
+    }
+    const double e1 = or_lerp(ve[l1 + a0], ve[l1 + a1], s, vu[l1 + a0], vu[l1 + a1]);
+    const double e2 = or_lerp(ve[h1 + c0], ve[h1 + c1], s, vu[h1 + c0], vu[h1 + c1]);
+    return or_lerp(vr[l1], vr[h1], rho, e1, e2);
+}
+
+/* SetConstantEntropy (force.h:55-65: tag 0 -> mantle, else core; the material
+ * slot is the tag) and CalcAll (force.h:73-84) */
+int64_t or_entropy_step(or_system *s, const or_config *cfg) {
+    const int64_t n = s->n;
+    const double *dens = F(s, OR_DENS);
+    double *eng = F(s, OR_ENG), *ent = F(s, OR_ENT), *temp = F(s, OR_TEMP);
+    int64_t bad = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : bad)
+    for (int64_t i = 0; i < n; ++i) {
+        const or_material *m = &cfg->mat[s->mat[i]];
+        const double e = s->mat[i] == 0 ? cfg->mantle_entropy : cfg->core_entropy;
+        int undef;
+        const double u = or_eos_internal_energy(m, dens[i], e, cfg->entropy_grid, cfg->entropy_abs, &undef);
+        ent[i] = e;
+        eng[i] = u;
+        temp[i] = or_eos_temperature(m, dens[i], u);
+        bad += (undef || !isfinite(u)) ? 1 : 0;
+    }
+    return bad;
+}
+
+/* ------------------------------------------------------------------------ */
 /* Morton keys and sort (FDPS tree construction; project specification)      */
 
 void or_root_box(const double *x, const double *y, const double *z, int64_t n, or_rootbox *rb) {
@@ -862,7 +1032,8 @@ void or_final_kick(or_system *s, double dt, double damp) {
     }
 }
 
-/* main.cpp:125-173 loop body (mode 1; output and mode-2 entropy path excluded) */
+/* main.cpp:125-173 loop body (output excluded); returns -2 when a mode-2
+ * lookup is undefined or non-finite */
 int or_step(or_system *s, const or_config *cfg, int n_steps) {
     for (int st = 0; st < n_steps; ++st) {
         const double dt = s->dt;
@@ -871,6 +1042,7 @@ int or_step(or_system *s, const or_config *cfg, int n_steps) {
         if (or_compute_forces(s, cfg) < 0) return -1;
         or_ext_force(s, cfg);
         or_final_kick(s, dt, cfg->damping);
+        if (cfg->mode == 2 && or_entropy_step(s, cfg) > 0) return -2;   /* main.cpp:155-158 */
         s->dt = or_dt_global(s);
         s->step += 1;
     }

@@ -29,7 +29,7 @@ enum or_field {
     OR_X = 0, OR_Y, OR_Z, OR_VX, OR_VY, OR_VZ, OR_MASS, OR_SMTH, OR_DENS, OR_ENG,
     OR_PRES, OR_SNDS, OR_DIVV, OR_ROTX, OR_ROTY, OR_ROTZ, OR_BAL, OR_AVA, OR_GRADH,
     OR_AX, OR_AY, OR_AZ, OR_ENGDOT, OR_VHX, OR_VHY, OR_VHZ, OR_ENGHALF, OR_DT,
-    OR_GX, OR_GY, OR_GZ, OR_POT, OR_NFIELD
+    OR_GX, OR_GY, OR_GZ, OR_POT, OR_ENT, OR_TEMP, OR_NFIELD
 };
 
 typedef struct {
@@ -40,6 +40,10 @@ typedef struct {
     const double *pres;    /* [n_rho * n_u], rho-major */
     const double *snds;    /* [n_rho * n_u] */
     double par[10];        /* Tillotson: rho0 u0 uiv ucv A B a b alpha beta; ideal gas: par[0] = gamma */
+    const double *temp;    /* [n_rho * n_u] column 2 (NULL: no mode-2 data) */
+    const double *ent;     /* [n_rho * n_u] column 5: the reference's full_entropies */
+    const double *line_rho;/* [n_rho * n_u] column 0 of every line: full_densities */
+    const double *line_u;  /* [n_rho * n_u] column 1 of every line: full_energies */
 } or_material;
 
 typedef struct {
@@ -54,6 +58,10 @@ typedef struct {
     double G;              /* 6.67e-11 (force.h:171-172) */
     int32_t n_mat;
     const or_material *mat;
+    int32_t mode;          /* 1 or 2 (main.cpp:115, 155-158) */
+    int32_t entropy_grid;  /* grid_length (120, EoS.h:250-251, 403-404) */
+    int32_t entropy_abs;   /* 0: int abs(int) of the truncated distance, 1: fabs */
+    double mantle_entropy, core_entropy;   /* main.cpp:116-119 */
 } or_config;
 
 typedef struct {
@@ -73,6 +81,16 @@ void or_kernel_gradW(double dx, double dy, double dz, double h, double g[3]);
 double or_table_lookup(const double *rho_ax, int n_rho, const double *u_ax, int n_u, const double *plane,
                        double rho, double u);
 void or_eos_eval(const or_material *m, double rho, double u, double *P, double *cs);
+/* EoS_t::Temperature / Entropy (bilinear on columns 2 / 5) and InternalEnergy
+ * (RestrictedBilinearInterpolation over every table line, literal O(lines)
+ * scans); *undef = 1 where the reference would index outside its vectors
+ * (the result is then NaN). */
+double or_eos_temperature(const or_material *m, double rho, double u);
+double or_eos_entropy(const or_material *m, double rho, double u);
+double or_eos_internal_energy(const or_material *m, double rho, double s, int grid, int abs_mode, int *undef);
+/* SetConstantEntropy + CalcAll (force.h:55-84) over the system; returns the
+ * number of undefined or non-finite lookups. */
+int64_t or_entropy_step(or_system *s, const or_config *cfg);
 
 /* --- tree --------------------------------------------------------------- */
 typedef struct {

@@ -16,6 +16,16 @@ Fixtures (npz):
                   with FDPS-style group-superset walks and exact-list walks
   integ.npz       initialKick/fullDrift/predict/finalKick/dampMotion records
   dtglobal.npz    getTimeStepGlobal
+  eos_mode2.npz   the mode-2 EoS surface: InternalEnergy(rho, s)
+                  (RestrictedBilinearInterpolation, interpolation.h:107-335),
+                  Temperature and Entropy (EoS.h:249-260, 402-413) through the
+                  reference's ANEOS class, on a 120 x 120 synthetic table, a
+                  12 x 120 table with sub-unit entropy steps (where the
+                  int abs(int) of the reference's translation unit and a
+                  floating abs pick different neighbours; both builds of the
+                  driver are run) and the 200 x 200 synthetic dunite table;
+                  plus points where the reference's lookup is undefined or
+                  not finite (checked against the oracle only)
 The particle state, the walks (group ranges and j indices) and the reference
 outputs are stored; tables are regenerated from their stored parameters.
 """
@@ -38,14 +48,15 @@ from oracle import build_oracle, pyoracle as po  # noqa: E402
 
 REF_ROOT = build_oracle.REF_ROOT
 DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+DRIVER_FABS = os.path.join(ROOT, "oracle", "_ref", "ref_driver_fabs")
 
 
-def run_ref(mode: str, payload: bytes, n_out_bytes: int | None = None) -> bytes:
+def run_ref(mode: str, payload: bytes, n_out_bytes: int | None = None, driver: str = DRIVER) -> bytes:
     with tempfile.TemporaryDirectory() as td:
         fi, fo = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
         with open(fi, "wb") as fh:
             fh.write(payload)
-        subprocess.run([DRIVER, mode, fi, fo], check=True, cwd=REF_ROOT)
+        subprocess.run([driver, mode, fi, fo], check=True, cwd=REF_ROOT)
         with open(fo, "rb") as fh:
             out = fh.read()
     if n_out_bytes is not None and len(out) != n_out_bytes:
@@ -350,6 +361,90 @@ def gen_integ(rng):
     np.savez_compressed(os.path.join(HERE, "dtglobal.npz"), rec=r2, dt=dtv[0])
 
 
+def fine_entropy_table():
+    """12 x 120 table whose entropy rises by 0.6 per energy column: nearest-entropy
+    distances below 1 truncate to 0 under int abs(int)"""
+    rho = np.array([float("%15.8E" % v) for v in np.geomspace(1.0e2, 2.0e4, 12)])
+    u = np.array([float("%15.8E" % v) for v in np.geomspace(1.0e4, 1.0e8, 120)])
+    R, U = np.meshgrid(rho, u, indexing="ij")
+    P, cs = eos.tillotson_eval(eos.TILLOTSON["iron"], R, U)
+    r8 = np.vectorize(lambda v: float("%15.8E" % v))
+    ent = r8(3000.0 + 0.6 * np.arange(120)[None, :] + 0.05 * np.arange(12)[:, None])
+    return eos.Table(rho=rho, u=u, pres=r8(P), snds=r8(cs), temp=r8(U / 1.0e3), ent=ent, name="fine-entropy")
+
+
+def mode2_tables():
+    """(name, table, spec) of the mode-2 fixture; spec rebuilds a synthetic table"""
+    out = []
+    spec = dict(material="iron", n_rho=120, n_u=120, rho_range=(1e-3, 3e4), u_range=(1e3, 1e9))
+    out.append(("iron120", eos.synthetic_table(**spec), spec))
+    out.append(("fine", fine_entropy_table(), None))
+    spec = dict(material="dunite", n_rho=200, n_u=200, rho_range=(1e1, 3e4), u_range=(1e3, 1e9))
+    out.append(("dunite200", eos.synthetic_table(**spec), spec))
+    return out
+
+
+def _mode2_points(rng, t: eos.Table, n=500):
+    lr = np.log(t.rho[1]), np.log(t.rho[-2])
+    lu = np.log(t.u[1]), np.log(t.u[-2])
+    e = t.ent.reshape(-1)
+    rho = np.exp(rng.uniform(*lr, n))
+    s = rng.uniform(np.percentile(e, 5), np.percentile(e, 95), n)
+    u = np.exp(rng.uniform(*lu, n))
+    return np.stack([rho, s, u], 1)
+
+
+def _mode2_edges(rng, t: eos.Table):
+    """points where the reference's lookup is NaN (density on a table row, below the
+    table) or undefined (above the table, entropies outside the slices)"""
+    e = t.ent.reshape(-1)
+    rows = t.rho[rng.integers(1, len(t.rho) - 1, 8)]
+    mid_s = float(np.median(e))
+    pts = [[r, mid_s, t.u[3]] for r in rows]
+    pts += [[t.rho[0] * 0.5, mid_s, t.u[3]], [t.rho[-1] * 2.0, mid_s, t.u[3]], [t.rho[-1], mid_s, t.u[3]],
+            [np.sqrt(t.rho[3] * t.rho[4]), e.min() - 1.0e4, t.u[3]],
+            [np.sqrt(t.rho[3] * t.rho[4]), e.max() + 1.0e4, t.u[3]],
+            [np.sqrt(t.rho[3] * t.rho[4]), 3.0e9, t.u[3]], [np.nan, mid_s, t.u[3]]]
+    return np.array(pts)
+
+
+def gen_eos_mode2():
+    rng = np.random.default_rng(120)
+    out = {}
+    for name, t, spec in mode2_tables():
+        ms = po.MaterialSet([t.as_material()])
+        pts = _mode2_points(rng, t)
+        defined = np.ones(len(pts), bool)
+        for k, (r, sv, _) in enumerate(pts):
+            for am in (0, 1):
+                v, undef = ms.internal_energy(0, r, sv, 120, am)
+                defined[k] &= (not undef) and bool(np.isfinite(v))
+        pts = pts[defined]
+        with tempfile.TemporaryDirectory() as td:
+            path = os.path.join(td, "t.rho_u.txt")
+            eos.write_rho_u(path, t)
+            back = eos.read_rho_u(path)
+            assert np.array_equal(back.ent, t.ent) and np.array_equal(back.temp, t.temp)
+            pb = path.encode()
+            payload = (struct.pack("<i", len(pb)) + pb + struct.pack("<iii", 0, 120, len(pts)) +
+                       np.ascontiguousarray(pts, "<f8").tobytes())
+            o_int = np.frombuffer(run_ref("eos_mode2", payload), "<f8").reshape(-1, 3)
+            o_real = np.frombuffer(run_ref("eos_mode2", payload, driver=DRIVER_FABS), "<f8").reshape(-1, 3)
+        out[f"{name}_points"] = pts
+        out[f"{name}_U_int"] = o_int[:, 0]
+        out[f"{name}_U_real"] = o_real[:, 0]
+        out[f"{name}_T"] = o_int[:, 1]
+        out[f"{name}_S"] = o_int[:, 2]
+        out[f"{name}_edges"] = _mode2_edges(rng, t)
+        out[f"{name}_spec"] = np.array(repr(spec))
+        if spec is None:   # not a synthetic_table: store the table itself
+            for f in ("rho", "u", "pres", "snds", "temp", "ent"):
+                out[f"{name}_table_{f}"] = getattr(t, f)
+        print(f"eos_mode2 {name}: {len(pts)} defined points, int/real abs differ at "
+              f"{int(np.sum(o_int[:, 0] != o_real[:, 0]))}")
+    np.savez_compressed(os.path.join(HERE, "eos_mode2.npz"), **out)
+
+
 def main():
     build_oracle.build()
     if not os.path.exists(DRIVER):
@@ -359,6 +454,7 @@ def main():
     gen_eos(rng)
     gen_functors()
     gen_integ(rng)
+    gen_eos_mode2()
     print("golden fixtures written to", HERE)
 
 

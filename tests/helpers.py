@@ -25,6 +25,25 @@ def table_materials(n=200):
     return [eos.synthetic_table(m, n, n) for m in ("iron", "dunite", "granite")]
 
 
+MODE2_TABLES = ("iron120", "fine", "dunite200")
+
+
+def mode2_table(g, name):
+    """a table of the eos_mode2.npz fixture: regenerated from its synthetic_table spec, or stored"""
+    import ast
+    spec = ast.literal_eval(str(g[f"{name}_spec"]))
+    if spec is not None:
+        return eos.synthetic_table(**spec)
+    a = {f: g[f"{name}_table_{f}"] for f in ("rho", "u", "pres", "snds", "temp", "ent")}
+    return eos.Table(name=name, **a)
+
+
+def mode2_materials():
+    """material 0 = iron, 1 = dunite: 120 x 120 synthetic tables that reach down to 1e-3 kg/m^3,
+    so every density above the floor (5) has a defined mode-2 lookup"""
+    return [eos.synthetic_table(m, 120, 120, rho_range=(1e-3, 3e4)) for m in ("iron", "dunite")]
+
+
 def oracle_config(materials, **kw):
     from oracle import pyoracle as po
     ms = po.MaterialSet([m.as_material() for m in materials])

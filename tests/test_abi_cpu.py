@@ -51,7 +51,7 @@ def test_field_order_matches_header():
     assert np.all(np.array(names) == np.array([
         "X", "Y", "Z", "VX", "VY", "VZ", "MASS", "SMTH", "DENS", "ENG", "PRES", "SNDS", "DIVV", "ROTX", "ROTY",
         "ROTZ", "BAL", "AVA", "GRADH", "AX", "AY", "AZ", "ENGDOT", "VHX", "VHY", "VHZ", "ENGHALF", "DT", "GX",
-        "GY", "GZ", "POT"]))
+        "GY", "GZ", "POT", "ENT", "TEMP"]))
 
 
 def test_context_creation_fails_cleanly_without_gpu():

@@ -147,3 +147,70 @@ def test_dt_global_matches_reference():
     F[po.FIELD["dt"]] = rec[:, 0]
     s = po.OracleSystem(F, np.arange(n), np.zeros(n, np.int32))
     assert po.dt_global(s) == float(g["dt"])
+
+
+# --- mode 2: SetConstantEntropy + CalcAll (main.cpp:155-158) ------------------
+@pytest.mark.parametrize("name", ["iron120", "fine", "dunite200"])
+def test_mode2_eos_matches_reference(name):
+    """InternalEnergy (RestrictedBilinearInterpolation), Temperature and Entropy of the
+    oracle against the reference's ANEOS class, for both resolutions of abs()"""
+    from helpers import mode2_table
+    g = load("eos_mode2.npz")
+    t = mode2_table(g, name)
+    ms = po.MaterialSet([t.as_material()])
+    pts = g[f"{name}_points"]
+    assert len(pts) > 150
+    for abs_mode, key in ((0, "U_int"), (1, "U_real")):
+        got = np.array([ms.internal_energy(0, r, s, 120, abs_mode) for r, s, _ in pts])
+        assert not got[:, 1].any()
+        assert relerr(got[:, 0], g[f"{name}_{key}"], 1e-300) <= 1e-15
+    T = np.array([ms.temperature(0, r, u) for r, _, u in pts])
+    S = np.array([ms.entropy(0, r, u) for r, _, u in pts])
+    assert relerr(T, g[f"{name}_T"], 1e-300) < 1e-13
+    assert relerr(S, g[f"{name}_S"], 1e-9 * np.abs(g[f"{name}_S"]).max()) < 1e-12
+    if name == "fine":   # the two abs() resolutions really differ on this table
+        assert np.sum(g["fine_U_int"] != g["fine_U_real"]) > 100
+
+
+def test_mode2_edges_are_flagged():
+    """densities on a table row give NaN (0/0 in the density interpolation), densities above
+    the table and entropies outside a slice index outside the reference's vectors"""
+    from helpers import mode2_table
+    g = load("eos_mode2.npz")
+    t = mode2_table(g, "iron120")
+    ms = po.MaterialSet([t.as_material()])
+    e = g["iron120_edges"]
+    res = [ms.internal_energy(0, r, s, 120, 0) for r, s, _ in e]
+    vals = np.array([v for v, _ in res])
+    und = np.array([u for _, u in res])
+    assert np.all(np.isnan(vals[:8])) and not und[:8].any()    # rows: defined, NaN
+    assert np.isnan(vals[8]) and not und[8]                      # below the table: p1 == p2
+    assert und[9] and und[10]                                    # at / above the last row
+    assert und[13] and np.isnan(vals[14])                        # |s - e| >= 2^31; NaN density
+    # the 200-column table with the reference's 120-line slices: many undefined lookups
+    t2 = mode2_table(g, "dunite200")
+    ms2 = po.MaterialSet([t2.as_material()])
+    rng = np.random.default_rng(1)
+    r = np.exp(rng.uniform(np.log(t2.rho[1]), np.log(t2.rho[-2]), 200))
+    und2 = [ms2.internal_energy(0, x, 3000.0, 120, 0)[1] for x in r]
+    assert 0 < sum(und2) < 200
+
+
+def test_mode2_step_sets_entropy_energy_temperature():
+    """or_step in mode 2 ends with ent = mantle / core entropy by material and eng, temp from
+    the tables at the step's density"""
+    from helpers import mode2_materials, oracle_config, small_impact
+    F, ids, mats, _ = small_impact(900, 100)
+    mat = mode2_materials()
+    cfg = oracle_config(mat, mode=2, mantle_entropy=3100.0, core_entropy=2500.0)
+    s = po.OracleSystem(F, ids, mats)
+    s.initialize_smth()
+    s.prologue(cfg)
+    s.step(cfg, 1)
+    ms = po.MaterialSet([m.as_material() for m in mat])
+    ent = s.field("ent")
+    assert np.all(ent[s.mat == 0] == 3100.0) and np.all(ent[s.mat == 1] == 2500.0)
+    for i in range(0, s.n, 97):
+        u, und = ms.internal_energy(s.mat[i], s.field("dens")[i], ent[i])
+        assert not und and u == s.field("eng")[i]
+        assert ms.temperature(s.mat[i], s.field("dens")[i], u) == s.field("temp")[i]
