@@ -399,7 +399,7 @@ def main():
         "metric": "SPH particle-steps/s at 1M (mixed FP32/FP64; plain FP64 beside it)",
         "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 pair sums + f64", "data": "synthetic (seeded IC generator, synthetic 200x200 rho-u tables)",
+        "dtype": "f32 pair sums + f64", "data": "synthetic (seeded IC generator, synthetic " + ("120x120" if a.mode == 2 else "200x200") + " rho-u tables)",
         "config": {"workload": f"{n:,}-particle {WORKLOADS[a.config]}, theta {a.theta}" +
                                (", mode 2 (constant entropy, 120 x 120 tables)" if a.mode == 2 else ""), "particles": n,
                    "precision": "mixed",
