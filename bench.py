@@ -227,8 +227,11 @@ def drift(d0, d1, steps):
 
 
 def run_e2e(ctx, F, ids, mats, steps):
-    """upload (pinned host) -> one step -> download (pinned host), every step"""
+    """upload (pinned host) -> one step -> download (pinned host), every step.  The upload
+    copies the fields the step reads or carries (SPH_UPLOAD_STEP_INPUTS); the download
+    returns every field, ids and materials."""
     import torch
+    from fdps_sph_gb300 import lib
     n = F.shape[1]
     hostF = torch.empty((F.shape[0], n), dtype=torch.float64).pin_memory().numpy()
     outF = torch.empty((F.shape[0], n), dtype=torch.float64).pin_memory().numpy()
@@ -242,15 +245,16 @@ def run_e2e(ctx, F, ids, mats, steps):
     t_now, dt, _ = ctx.time()
     t0 = time.perf_counter()
     for _ in range(steps):
-        ctx.upload(hostF, hid, hmat, time=t_now, dt=dt, forces_valid=True)
+        ctx.upload(hostF, hid, hmat, time=t_now, dt=dt, forces_valid=True, inputs_only=True)
         ctx.step(1)
         t_now, dt, _ = ctx.time()
         o, oid, om = ctx.download(outF)
         hostF, outF = outF, hostF
         hid, hmat = oid, om
     el = time.perf_counter() - t0
-    h2d = hostF.nbytes + hid.nbytes + hmat.nbytes
-    return el, h2d, h2d
+    h2d = 8 * n * len(lib.STEP_INPUT_FIELDS) + hid.nbytes + hmat.nbytes
+    d2h = hostF.nbytes + hid.nbytes + hmat.nbytes
+    return el, h2d, d2h
 
 
 def cpu_sample(n_cpu, steps, fast=True):

@@ -1,6 +1,7 @@
 // Device-resident whole-pass C ABI: context, EoS materials, upload /
 // download, the step of main.cpp:125-173 and inspection calls.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdarg>
 #include <cstring>
@@ -47,6 +48,33 @@ __global__ void k_unpermute(const double *F, double *F2, int64_t cap, int k0, in
     for (int f = 0; f < SPH_NFIELD; ++f) F2[(int64_t)f * cap + dst] = F[(int64_t)f * cap + k];
     id2[dst] = id[k];
     mat2[dst] = mat[k];
+}
+
+// checks of an uploaded block: bad[0] = first particle whose mass is not positive and finite,
+// bad[1] = first particle with an unset material (INT_MAX: none); part[b] = mass sum of block b's
+// contiguous chunk through a fixed reduction tree (the same sum for the same block every time)
+constexpr int CHECK_BLOCKS = 256;
+__global__ void __launch_bounds__(256) k_check_block(int n, const double *__restrict__ mass,
+                                                     const int32_t *__restrict__ mat,
+                                                     const DevMaterial *__restrict__ mats, double *part, int *bad) {
+    __shared__ double s[256];
+    const int chunk = (n + CHECK_BLOCKS - 1) / CHECK_BLOCKS;
+    const int lo = blockIdx.x * chunk, hi = min(n, lo + chunk);
+    double acc = 0.0;
+    for (int i = lo + (int)threadIdx.x; i < hi; i += blockDim.x) {
+        const double m = mass[i];
+        if (!(m > 0.0) || !isfinite(m)) atomicMin(&bad[0], i);
+        const int q = mat[i];
+        if (q < 0 || q >= MAX_MATERIALS || mats[q].kind < 0) atomicMin(&bad[1], i);
+        acc += m;
+    }
+    s[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = s[0];
 }
 
 __global__ void k_fill32(int32_t *a, int n, int v) {
@@ -264,25 +292,28 @@ int append_run(sph_ctx *ctx, int64_t n, const double *fields, int64_t ld, const 
                double time, double dt, int flags, int64_t *handle) {
     if (n < 1 || n > 0x3fffffff || !fields || ld < n || ctx->n + n > 0x3fffffff)
         return sph_fail(ctx, SPH_ERR_ARG, "bad particle block (n=%lld)", (long long)n);
-    if (material) {
-        for (int64_t i = 0; i < n; ++i) {
-            const int m = material[i];
-            if (m < 0 || m >= MAX_MATERIALS || ctx->mats_host[m].kind < 0)
-                return sph_fail(ctx, SPH_ERR_ARG, "particle %lld uses unset material %d", (long long)i, m);
-        }
-    } else if (ctx->mats_host[0].kind < 0) {
-        return sph_fail(ctx, SPH_ERR_ARG, "material 0 is not set");
-    }
-    double msum = 0.0;
-    for (int64_t i = 0; i < n; ++i) {
-        const double mi = fields[(int64_t)SPH_MASS * ld + i];
-        if (!(mi > 0.0) || !std::isfinite(mi)) return sph_fail(ctx, SPH_ERR_NONFINITE, "particle %lld has mass %g", (long long)i, mi);
-        msum += mi;
-    }
+    if (!material && ctx->mats_host[0].kind < 0) return sph_fail(ctx, SPH_ERR_ARG, "material 0 is not set");
+    if ((flags & SPH_UPLOAD_STEP_INPUTS) && (flags & SPH_UPLOAD_INIT_SMTH))
+        return sph_fail(ctx, SPH_ERR_ARG, "SPH_UPLOAD_INIT_SMTH reads the density, which SPH_UPLOAD_STEP_INPUTS leaves out");
     const int64_t o = ctx->n;
     SPH_TRY(grow_particles(ctx, o + n));
-    SPH_CUDA(ctx, cudaMemcpy2DAsync(ctx->F + o, sizeof(double) * ctx->cap, fields, sizeof(double) * ld,
-                                    sizeof(double) * n, SPH_NFIELD, cudaMemcpyHostToDevice, ctx->stream));
+    const int64_t c = ctx->cap;
+    // field rows: all of them, or (SPH_UPLOAD_STEP_INPUTS) the ones a step reads or carries, the
+    // others zeroed; consecutive rows go in one 2D copy
+    const uint64_t want = (flags & SPH_UPLOAD_STEP_INPUTS) ? (uint64_t)SPH_STEP_INPUT_FIELDS : ~0ull;
+    for (int f = 0; f < SPH_NFIELD;) {
+        const bool in = (want >> f) & 1;
+        int g = f;
+        while (g < SPH_NFIELD && (((want >> g) & 1) != 0) == in) ++g;
+        if (in)
+            SPH_CUDA(ctx, cudaMemcpy2DAsync(ctx->F + (int64_t)f * c + o, sizeof(double) * c, fields + (int64_t)f * ld,
+                                            sizeof(double) * ld, sizeof(double) * n, g - f, cudaMemcpyHostToDevice,
+                                            ctx->stream));
+        else
+            SPH_CUDA(ctx, cudaMemset2DAsync(ctx->F + (int64_t)f * c + o, sizeof(double) * c, 0, sizeof(double) * n,
+                                            g - f, ctx->stream));
+        f = g;
+    }
     if (id) {
         SPH_CUDA(ctx, cudaMemcpyAsync(ctx->id + o, id, sizeof(int64_t) * n, cudaMemcpyHostToDevice, ctx->stream));
     } else {
@@ -293,14 +324,40 @@ int append_run(sph_ctx *ctx, int64_t n, const double *fields, int64_t ld, const 
     } else {
         SPH_CUDA(ctx, cudaMemsetAsync(ctx->mat + o, 0, sizeof(int32_t) * n, ctx->stream));
     }
+    // masses and materials checked on the device, the mass summed in a fixed order
+    double *part = ctx->scratch_d;
+    int *bad = (int *)(ctx->scratch_d + CHECK_BLOCKS);
+    const int big[2] = {INT_MAX, INT_MAX};
+    std::memcpy(ctx->host_scalars + CHECK_BLOCKS, big, sizeof(big));
+    SPH_CUDA(ctx, cudaMemcpyAsync(bad, ctx->host_scalars + CHECK_BLOCKS, sizeof(big), cudaMemcpyHostToDevice,
+                                  ctx->stream));
+    k_check_block<<<CHECK_BLOCKS, 256, 0, ctx->stream>>>((int)n, ctx->F + (int64_t)SPH_MASS * c + o, ctx->mat + o,
+                                                         ctx->mats_dev, part, bad); ++ctx->launches;
+    SPH_CUDA(ctx, cudaGetLastError());
+    SPH_CUDA(ctx, cudaMemcpyAsync(ctx->host_scalars, part, sizeof(double) * CHECK_BLOCKS + sizeof(big),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
     Runs &R = ctx->runs;
     k_iota32<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(ctx->slot + o, (int)n); ++ctx->launches;
     k_fill32<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(R.prun + o, (int)n, R.R); ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
+    SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    int badh[2];
+    std::memcpy(badh, ctx->host_scalars + CHECK_BLOCKS, sizeof(badh));
+    if (badh[0] != INT_MAX) {
+        double mi = 0.0;
+        SPH_CUDA(ctx, cudaMemcpy(&mi, ctx->F + (int64_t)SPH_MASS * c + o + badh[0], sizeof(double),
+                                 cudaMemcpyDeviceToHost));
+        return sph_fail(ctx, SPH_ERR_NONFINITE, "particle %d has mass %g", badh[0], mi);
+    }
+    if (badh[1] != INT_MAX) return sph_fail(ctx, SPH_ERR_ARG, "particle %d uses an unset material", badh[1]);
+    double msum = 0.0;
+    for (int b = 0; b < CHECK_BLOCKS; ++b) msum += ctx->host_scalars[b];
     // power of two close to 1 / mean mass (exact rescaling of the FP32 mass copies), fixed by the first run
     if (o == 0) ctx->mscale = std::ldexp(1.0, -(int)std::lround(std::log2(msum / (double)n)));
-    if (flags & SPH_UPLOAD_INIT_SMTH) SPH_TRY(sph_init_smth(ctx, o, n));
-    SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (flags & SPH_UPLOAD_INIT_SMTH) {
+        SPH_TRY(sph_init_smth(ctx, o, n));
+        SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
     const bool forces = (flags & SPH_UPLOAD_FORCES_VALID) && dt > 0.0;
     R.n.push_back(n);
     R.time.push_back(time);

@@ -41,6 +41,9 @@ EXPORTS = [
     "sph_add_run", "sph_remove_run", "sph_list_runs", "sph_run_info", "sph_download_run", "sph_run_diagnostics",
     "sph_autotune", "sph_set_eos_ideal", "sph_set_eos_entropy", "sph_eos_eval",
 ]
+# fields a step reads or carries unchanged (SPH_STEP_INPUT_FIELDS): what SPH_UPLOAD_STEP_INPUTS copies
+STEP_INPUT_FIELDS = ["x", "y", "z", "vx", "vy", "vz", "mass", "smth", "eng", "ava", "ax", "ay", "az", "eng_dot",
+                     "gx", "gy", "gz", "ent", "temp"]
 EOS_QUANTITY = {"pressure": 0, "sound_speed": 1, "temperature": 2, "entropy": 3, "internal_energy": 4}
 ENTROPY_ABS_INT = 0
 ENTROPY_ABS_REAL = 1
@@ -210,13 +213,15 @@ class Context:
         self._check(self.L.sph_load_eos_table_file(self.h, k, path.encode()))
 
     # state ----------------------------------------------------------------
-    def upload(self, F: np.ndarray, ids=None, mats=None, time=0.0, init_smth=False, dt=0.0, forces_valid=False):
+    def upload(self, F: np.ndarray, ids=None, mats=None, time=0.0, init_smth=False, dt=0.0, forces_valid=False,
+               inputs_only=False):
+        """inputs_only: copy only STEP_INPUT_FIELDS (SPH_UPLOAD_STEP_INPUTS)"""
         F = np.ascontiguousarray(F, np.float64)
         assert F.shape[0] == NFIELD
         n = F.shape[1]
         ids = None if ids is None else np.ascontiguousarray(ids, np.int64)
         mats = None if mats is None else np.ascontiguousarray(mats, np.int32)
-        flags = (1 if init_smth else 0) | (2 if forces_valid else 0)
+        flags = (1 if init_smth else 0) | (2 if forces_valid else 0) | (4 if inputs_only else 0)
         self._check(self.L.sph_upload(self.h, n, _ptr(F), F.shape[1], _ptr(ids), _ptr(mats), float(time), float(dt),
                                       flags))
         self.n = n

@@ -193,9 +193,24 @@ int sph_eos_eval(sph_ctx *ctx, int material, int quantity, int64_t n, const doub
  *                           step (system_t::dt, class.h:9), so sph_step may
  *                           run without a prologue: a host that keeps its
  *                           particles (as the reference's ParticleSystem does)
- *                           can upload, step and download every step. */
+ *                           can upload, step and download every step;
+ *   SPH_UPLOAD_STEP_INPUTS  copy only the fields a step reads or carries
+ *                           unchanged (SPH_STEP_INPUT_FIELDS: positions,
+ *                           velocities, mass, smth, eng, AVa, acc, eng_dot,
+ *                           grav, ent, temp); the rest are outputs of the next
+ *                           step and read as zero until it has run.
+ * Masses must be positive and finite and every material set (checked on the
+ * device; SPH_ERR_NONFINITE / SPH_ERR_ARG). */
 #define SPH_UPLOAD_INIT_SMTH 1
 #define SPH_UPLOAD_FORCES_VALID 2
+#define SPH_UPLOAD_STEP_INPUTS 4
+#define SPH_FIELD_BIT(f) (1ull << (f))
+#define SPH_STEP_INPUT_FIELDS                                                                                     \
+    (SPH_FIELD_BIT(SPH_X) | SPH_FIELD_BIT(SPH_Y) | SPH_FIELD_BIT(SPH_Z) | SPH_FIELD_BIT(SPH_VX) |                \
+     SPH_FIELD_BIT(SPH_VY) | SPH_FIELD_BIT(SPH_VZ) | SPH_FIELD_BIT(SPH_MASS) | SPH_FIELD_BIT(SPH_SMTH) |         \
+     SPH_FIELD_BIT(SPH_ENG) | SPH_FIELD_BIT(SPH_AVA) | SPH_FIELD_BIT(SPH_AX) | SPH_FIELD_BIT(SPH_AY) |           \
+     SPH_FIELD_BIT(SPH_AZ) | SPH_FIELD_BIT(SPH_ENGDOT) | SPH_FIELD_BIT(SPH_GX) | SPH_FIELD_BIT(SPH_GY) |        \
+     SPH_FIELD_BIT(SPH_GZ) | SPH_FIELD_BIT(SPH_ENT) | SPH_FIELD_BIT(SPH_TEMP))
 int sph_upload(sph_ctx *ctx, int64_t n, const double *fields, int64_t ld, const int64_t *id,
                const int32_t *material, double time, double dt, int flags);
 /* Copies the state back in upload order. */

@@ -105,3 +105,54 @@ def test_checkpoint_resume_is_exact(prec, tmp_path):
     for a, b in zip(hs, hs2):
         _same(ctx.download_run(a), ctx2.download_run(b))
         assert ctx.run_info(a)["time"] == ctx2.run_info(b)["time"]
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_step_inputs_upload_equals_full_upload(prec):
+    """A host that keeps its particles uploads only the fields a step reads or carries
+    (SPH_UPLOAD_STEP_INPUTS); the step's results equal those after a full upload, bit for bit."""
+    from fdps_sph_gb300 import lib
+    F, ids, mats = _bodies()[0]
+    ctx = device_context(tillotson_materials(), precision=prec)
+    ctx.upload(F, ids, mats)
+    ctx.prologue()
+    ctx.step(2)
+    Fh, idh, mh = ctx.download()
+    t, dt, _ = ctx.time()
+    ctx.close()
+    out = []
+    for inputs_only in (False, True):
+        c = device_context(tillotson_materials(), precision=prec)
+        G = Fh.copy()
+        if inputs_only:   # what is not an input must not matter
+            keep = [lib.FIELD[f] for f in lib.STEP_INPUT_FIELDS]
+            drop = np.setdiff1d(np.arange(lib.NFIELD), keep)
+            G[drop] = np.nan
+        c.upload(G, idh, mh, time=t, dt=dt, forces_valid=True, inputs_only=inputs_only)
+        c.step(2)
+        out.append(c.download())
+        c.close()
+    _same(out[0], out[1])
+
+
+def test_upload_checks_masses_and_materials():
+    from fdps_sph_gb300 import lib
+    F, ids, mats = _bodies()[1]
+    ctx = device_context(tillotson_materials(), precision=1)
+    G = F.copy()
+    G[lib.FIELD["mass"], 17] = -1.0
+    with pytest.raises(lib.SphError) as ei:
+        ctx.upload(G, ids, mats)
+    assert ei.value.code == -5 and "particle 17" in str(ei.value)
+    G[lib.FIELD["mass"], 17] = np.inf
+    with pytest.raises(lib.SphError):
+        ctx.upload(G, ids, mats)
+    bad = mats.copy()
+    bad[40] = 9                      # a slot that was never set
+    with pytest.raises(lib.SphError) as ei:
+        ctx.upload(F, ids, bad)
+    assert ei.value.code == -1 and "particle 40" in str(ei.value)
+    ctx.upload(F, ids, mats)         # the context is usable after the refusals
+    ctx.prologue()
+    ctx.step(1)
+    ctx.close()
