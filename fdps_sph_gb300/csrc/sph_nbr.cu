@@ -133,10 +133,9 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
     __shared__ int s_sj[NB_WARPS][NB_SURV];
     __shared__ float4 s_ph[NB_WARPS][NB_SURV];
     __shared__ float4 s_pl[NB_WARPS][NB_SURV];
-    // per-lane write buffers: 8 entries = one 32-byte sector
-    __shared__ int s_wj[NB_WARPS][8][32];
-    __shared__ float s_wr[NB_WARPS][8][32];
-    __shared__ float s_wm[NB_WARPS][8][32];
+    // per-lane write buffers, one 32-byte sector (8 entries) of index, r^2 and mass each, the
+    // lane's 24 words contiguous so a full buffer is read back with six 16-byte loads
+    __shared__ __align__(16) int s_wb[NB_WARPS][32][24];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int w = blockIdx.x * NB_WARPS + warp;
     if (w >= n_units) return;   // warp-uniform
@@ -175,29 +174,37 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
     // on the rare paths that need it, so nothing stays live through the walk)
     auto spill_cap = [&]() { return valid ? row_spill_cap(rm, i) : 0; };
     auto spill_base = [&]() { return rm.main + rm.soff[i] - K; };
-    // writes the lane's 8 buffered entries ending at `count` as full sectors (in the row, or in
-    // its spill range: K is a multiple of 8, so a sector never straddles the two)
-    auto write8 = [&](int *rw, float *rr, float *rq, int k0) {
-        const int4 a = make_int4(s_wj[warp][0][lane], s_wj[warp][1][lane], s_wj[warp][2][lane], s_wj[warp][3][lane]);
-        const int4 b = make_int4(s_wj[warp][4][lane], s_wj[warp][5][lane], s_wj[warp][6][lane], s_wj[warp][7][lane]);
-        const float4 c = make_float4(s_wr[warp][0][lane], s_wr[warp][1][lane], s_wr[warp][2][lane], s_wr[warp][3][lane]);
-        const float4 d = make_float4(s_wr[warp][4][lane], s_wr[warp][5][lane], s_wr[warp][6][lane], s_wr[warp][7][lane]);
-        reinterpret_cast<int4 *>(rw + k0)[0] = a;
-        reinterpret_cast<int4 *>(rw + k0)[1] = b;
-        reinterpret_cast<float4 *>(rr + k0)[0] = c;
-        reinterpret_cast<float4 *>(rr + k0)[1] = d;
-        reinterpret_cast<float4 *>(rq + k0)[0] =
-            make_float4(s_wm[warp][0][lane], s_wm[warp][1][lane], s_wm[warp][2][lane], s_wm[warp][3][lane]);
-        reinterpret_cast<float4 *>(rq + k0)[1] =
-            make_float4(s_wm[warp][4][lane], s_wm[warp][5][lane], s_wm[warp][6][lane], s_wm[warp][7][lane]);
-    };
-    auto put8 = [&]() {
-        const int k0 = count - 8;
-        if (k0 + 8 <= K) {
-            write8(row, rrow, mrow, k0);
-        } else if (SPILL && k0 + 8 <= K + spill_cap()) {
-            const int64_t sb = spill_base();
-            write8(sup + sb, sup_r2 + sb, sup_m + sb, k0);
+    // appends one entry to the lane's buffer; a full buffer goes out as three sectors (in the
+    // row, or in its spill range: K is a multiple of 8, so a sector never straddles the two;
+    // entries past both are only counted, and the host grows the rows and walks again)
+    int *wb = s_wb[warp][lane];
+    auto put = [&](int j, float r2, float mj) {
+        const int q = count & 7;
+        wb[q] = j;
+        wb[8 + q] = __float_as_int(r2);
+        wb[16 + q] = __float_as_int(mj);
+        ++count;
+        if (q == 7) {
+            const int k0 = count - 8;
+            int *rw = row;
+            float *rr = rrow, *rq = mrow;
+            bool ok = k0 + 8 <= K;
+            if (!ok && SPILL && k0 + 8 <= K + spill_cap()) {
+                const int64_t sb = spill_base();
+                rw = sup + sb;
+                rr = sup_r2 + sb;
+                rq = sup_m + sb;
+                ok = true;
+            }
+            if (ok) {
+                const int4 *v = reinterpret_cast<const int4 *>(wb);
+                reinterpret_cast<int4 *>(rw + k0)[0] = v[0];
+                reinterpret_cast<int4 *>(rw + k0)[1] = v[1];
+                reinterpret_cast<int4 *>(rr + k0)[0] = v[2];
+                reinterpret_cast<int4 *>(rr + k0)[1] = v[3];
+                reinterpret_cast<int4 *>(rq + k0)[0] = v[4];
+                reinterpret_cast<int4 *>(rq + k0)[1] = v[5];
+            }
         }
     };
 
@@ -237,19 +244,27 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
             ns += __popc(km);
             __syncwarp();
             if (ns >= 32 || b + 32 >= nc) {
+                // every lane tests every survivor without branching (bit t of `am`), then writes
+                // its accepted ones in survivor order; the warp diverges only over those
+                unsigned long long am = 0ull;
+#pragma unroll 4
                 for (int t = 0; t < ns; ++t) {
                     const float4 ph = s_ph[warp][t], pl = s_pl[warp][t];
                     const float dx = df_sub(ph.x, pl.x, pih.x, pil.x);
                     const float dy = df_sub(ph.y, pl.y, pih.y, pil.y);
                     const float dz = df_sub(ph.z, pl.z, pih.z, pil.z);
                     const float r2 = dx * dx + dy * dy + dz * dz;
-                    if (valid && r2 < k2 * fmaxf(H2i, pl.w)) {
-                        s_wj[warp][count & 7][lane] = s_sj[warp][t];
-                        s_wr[warp][count & 7][lane] = r2;
-                        s_wm[warp][count & 7][lane] = ph.w;
-                        ++count;
-                        if ((count & 7) == 0) put8();
-                    }
+                    am |= (unsigned long long)(r2 < k2 * fmaxf(H2i, pl.w)) << t;
+                }
+                if (!valid) am = 0ull;
+                while (am) {
+                    const int t = __ffsll((long long)am) - 1;
+                    am &= am - 1ull;
+                    const float4 ph = s_ph[warp][t], pl = s_pl[warp][t];
+                    const float dx = df_sub(ph.x, pl.x, pih.x, pil.x);
+                    const float dy = df_sub(ph.y, pl.y, pih.y, pil.y);
+                    const float dz = df_sub(ph.z, pl.z, pih.z, pil.z);
+                    put(s_sj[warp][t], dx * dx + dy * dy + dz * dz, ph.w);
                 }
                 ns = 0;
                 __syncwarp();
@@ -313,14 +328,14 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
         for (int q = 0; q < (count & 7); ++q) {
             const int k = k0 + q;
             if (k < K) {
-                row[k] = s_wj[warp][q][lane];
-                rrow[k] = s_wr[warp][q][lane];
-                mrow[k] = s_wm[warp][q][lane];
+                row[k] = wb[q];
+                rrow[k] = __int_as_float(wb[8 + q]);
+                mrow[k] = __int_as_float(wb[16 + q]);
             } else if (SPILL && k < K + scap) {
                 const int64_t sb = spill_base();
-                sup[sb + k] = s_wj[warp][q][lane];
-                sup_r2[sb + k] = s_wr[warp][q][lane];
-                sup_m[sb + k] = s_wm[warp][q][lane];
+                sup[sb + k] = wb[q];
+                sup_r2[sb + k] = __int_as_float(wb[8 + q]);
+                sup_m[sb + k] = __int_as_float(wb[16 + q]);
             }
         }
         cnt[i] = count;   // the true count, also when the row had no room for all of it

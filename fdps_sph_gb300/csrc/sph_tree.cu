@@ -488,85 +488,146 @@ __device__ __forceinline__ void split_store(int *tb, int s, int e, const int *bn
     *nch = k + (e > prev);
 }
 
-constexpr int SPLIT_QUEUE = 512;   // big cells handed from a block's threads to its warps
+// first position in [a, e) whose digit at `lev` is >= oct (keys ascending within the range)
+__device__ __forceinline__ int split_search1(const uint64_t *keys, int lev, int a, int e, int oct) {
+    int len = e - a;
+    while (len > 0) {
+        const int half = len >> 1;
+        if (digit_at(keys[a + half], lev) < oct) {
+            a += half + 1;
+            len -= half + 1;
+        } else {
+            len = half;
+        }
+    }
+    return a;
+}
 
-__global__ void __launch_bounds__(256) k_split(int l, int n_leaf, const uint64_t *keys, const int *meta,
-                                               const int *start, const int *count, int *tmp_cnt, int *tmp_b) {
-    __shared__ int s_big[SPLIT_QUEUE];
-    __shared__ int s_nbig;
-    const int L0 = meta[l], L1 = meta[l + 1];
-    const int gt = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwb = blockDim.x >> 5;
-    if (threadIdx.x == 0) s_nbig = 0;
-    __syncthreads();
-    // small cells: a thread each; big cells go to the block's queue (or, if it is full, stay here)
-    for (int c = L0 + gt; c < L1; c += nt) {
-        const int s = start[c], cnt = count[c];
-        if (cnt > SPLIT_SMALL && l < KEY_LEVELS) {
-            const int q = atomicAdd(&s_nbig, 1);
-            if (q < SPLIT_QUEUE) {
-                s_big[q] = c;
-                continue;
+// K independent searches of split_search1 interleaved, so their loads overlap: search q looks
+// in [a[q], e[q]) for digit o[q] and leaves the answer in a[q]
+template <int K>
+__device__ __forceinline__ void split_searchK(const uint64_t *keys, int lev, int (&a)[K], const int (&e)[K],
+                                              const int (&o)[K]) {
+    int len[K];
+#pragma unroll
+    for (int q = 0; q < K; ++q) len[q] = e[q] - a[q];
+    for (;;) {
+        bool any = false;
+        bool lt[K];
+#pragma unroll
+        for (int q = 0; q < K; ++q) {
+            lt[q] = len[q] > 0 && digit_at(keys[a[q] + (len[q] >> 1)], lev) < o[q];
+            any = any || len[q] > 0;
+        }
+        if (!any) break;
+#pragma unroll
+        for (int q = 0; q < K; ++q) {
+            if (len[q] <= 0) continue;
+            const int h = len[q] >> 1;
+            if (lt[q]) {
+                a[q] += h + 1;
+                len[q] -= h + 1;
+            } else {
+                len[q] = h;
             }
         }
-        int nch = 0;
-        if (cnt > n_leaf && l < KEY_LEVELS) {
-            int bnd[8];
-            int lo = s;
-            for (int oct = 1; oct < 8; ++oct) {
-                int a = lo, len = s + cnt - lo;
-                while (len > 0) {
-                    const int half = len >> 1;
-                    if (digit_at(keys[a + half], l + 1) < oct) {
-                        a += half + 1;
-                        len -= half + 1;
-                    } else {
-                        len = half;
-                    }
-                }
-                bnd[oct] = a;
-                lo = a;
+    }
+}
+
+
+// the octant boundaries of one big cell [s, e) by a whole warp, 32-way searches
+__device__ __forceinline__ void split_big(const uint64_t *keys, int l, int lane, int c, int L0, int s, int e,
+                                          int *tmp_cnt, int *tmp_b) {
+    int bnd[8];
+    int lo = s;
+    for (int oct = 1; oct < 8; ++oct) {
+        // first position in [lo, e) with digit >= oct; the answer lies in [a, b]
+        int a = lo, b = e;
+        while (b - a > 32) {
+            const int step = (b - a + 31) >> 5;
+            const int p = a + lane * step;
+            const bool below = p < b && digit_at(keys[p], l + 1) < oct;
+            const int kb = __popc(__ballot_sync(0xffffffffu, below));
+            if (kb == 0) {
+                b = a;
+            } else {
+                const int na = a + (kb - 1) * step + 1;
+                b = min(b, a + kb * step);
+                a = na;
             }
-            split_store(tmp_b + (int64_t)(c - L0) * 9, s, s + cnt, bnd, &nch);
+        }
+        if (b > a) {
+            const int p = a + lane;
+            const bool below = p < b && digit_at(keys[p], l + 1) < oct;
+            a += __popc(__ballot_sync(0xffffffffu, below));
+        }
+        bnd[oct] = a;
+        lo = a;
+    }
+    if (lane == 0) {
+        int nch = 0;
+        split_store(tmp_b + (int64_t)(c - L0) * 9, s, e, bnd, &nch);
+        tmp_cnt[c - L0] = nch;
+    }
+}
+
+// Small cells (<= SPLIT_SMALL particles) go to one thread each, big ones to one warp each,
+// spread over all warps of the grid: a level with fewer cells than warps gives every cell its
+// own warp (the top levels hold a few hundred big cells), a larger one is scanned 32 cells at
+// a time per warp.
+__global__ void __launch_bounds__(256) k_split(int l, int n_leaf, const uint64_t *keys, const int *meta,
+                                               const int *start, const int *count, int *tmp_cnt, int *tmp_b) {
+    const int L0 = meta[l], L1 = meta[l + 1], nL = L1 - L0;
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
+    const int lane = threadIdx.x & 31, gw = gt >> 5, nw = nt >> 5;
+    const bool deep = l < KEY_LEVELS;
+    for (int c = L0 + gt; c < L1; c += nt) {
+        const int s = start[c], cnt = count[c];
+        if (cnt > SPLIT_SMALL && deep) continue;   // a warp's
+        int nch = 0;
+        if (cnt > n_leaf && deep) {
+            // the seven octant boundaries in three rounds of independent searches (octant 4;
+            // then 2 and 6; then 1, 3, 5, 7), each search over the range its neighbours bound
+            int bnd[8];
+            const int e = s + cnt;
+            bnd[4] = split_search1(keys, l + 1, s, e, 4);
+            {
+                int a2[2] = {s, bnd[4]};
+                split_searchK<2>(keys, l + 1, a2, {bnd[4], e}, {2, 6});
+                bnd[2] = a2[0];
+                bnd[6] = a2[1];
+            }
+            {
+                int a4[4] = {s, bnd[2], bnd[4], bnd[6]};
+                split_searchK<4>(keys, l + 1, a4, {bnd[2], bnd[4], bnd[6], e}, {1, 3, 5, 7});
+                bnd[1] = a4[0];
+                bnd[3] = a4[1];
+                bnd[5] = a4[2];
+                bnd[7] = a4[3];
+            }
+            split_store(tmp_b + (int64_t)(c - L0) * 9, s, e, bnd, &nch);
         }
         tmp_cnt[c - L0] = nch;
     }
-    __syncthreads();
-    // big cells: a warp each, 32-way searches
-    const int nbig = min(s_nbig, SPLIT_QUEUE);
-    for (int k = warp; k < nbig; k += nwb) {
-        const int c = s_big[k];
-        const int s = start[c], e = s + count[c];
-        int bnd[8];
-        int lo = s;
-        for (int oct = 1; oct < 8; ++oct) {
-            // first position in [lo, e) with digit >= oct; the answer lies in [a, b]
-            int a = lo, b = e;
-            while (b - a > 32) {
-                const int step = (b - a + 31) >> 5;
-                const int p = a + lane * step;
-                const bool below = p < b && digit_at(keys[p], l + 1) < oct;
-                const int kb = __popc(__ballot_sync(0xffffffffu, below));
-                if (kb == 0) {
-                    b = a;
-                } else {
-                    const int na = a + (kb - 1) * step + 1;
-                    b = min(b, a + kb * step);
-                    a = na;
-                }
-            }
-            if (b > a) {
-                const int p = a + lane;
-                const bool below = p < b && digit_at(keys[p], l + 1) < oct;
-                a += __popc(__ballot_sync(0xffffffffu, below));
-            }
-            bnd[oct] = a;
-            lo = a;
+    if (!deep) return;
+    if (nL <= nw) {
+        if (gw < nL) {
+            const int c = L0 + gw;
+            const int s = start[c], cnt = count[c];
+            if (cnt > SPLIT_SMALL) split_big(keys, l, lane, c, L0, s, s + cnt, tmp_cnt, tmp_b);
         }
-        if (lane == 0) {
-            int nch = 0;
-            split_store(tmp_b + (int64_t)(c - L0) * 9, s, e, bnd, &nch);
-            tmp_cnt[c - L0] = nch;
+        return;
+    }
+    for (int q0 = gw * 32; q0 < nL; q0 += nw * 32) {
+        const int q = q0 + lane;
+        const int cl = q < nL ? count[L0 + q] : 0;
+        unsigned big = __ballot_sync(0xffffffffu, cl > SPLIT_SMALL);
+        while (big) {
+            const int k = __ffs(big) - 1;
+            big &= big - 1;
+            const int c = L0 + q0 + k;
+            const int s = start[c];
+            split_big(keys, l, lane, c, L0, s, s + __shfl_sync(0xffffffffu, cl, k), tmp_cnt, tmp_b);
         }
     }
 }

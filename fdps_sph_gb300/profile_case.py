@@ -18,6 +18,8 @@ def main(argv=None):
     ap.add_argument("--n", type=int, default=400_000, help="total particles")
     ap.add_argument("--steps", type=int, default=2, help="steps after the prologue")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--tpi", type=int, default=4, choices=[1, 2, 4],
+                    help="threads per particle of the mixed derivative / hydro kernels")
     a = ap.parse_args(argv)
     n_t = int(a.n * 0.9)
     F, ids, mats, _ = ic.config_1m_impact(seed=2024, n_target=n_t, n_impactor=a.n - n_t)
@@ -25,6 +27,8 @@ def main(argv=None):
     for k, name in enumerate(("iron", "dunite")):
         ctx.set_material(k, eos.synthetic_table(name))
     ctx.upload(F, ids, mats)
+    if a.precision == "mixed":
+        ctx.set_tune(a.tpi, a.tpi)
     t = time.time()
     ctx.prologue()
     print(f"prologue {1e3 * (time.time() - t):.1f} ms (host clock)", flush=True)
