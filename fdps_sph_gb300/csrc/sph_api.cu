@@ -163,11 +163,10 @@ int compute_forces(sph_ctx *ctx) {
     }
     SPH_TRY(sph_pass_eos(ctx));
     SPH_TRY(time_mark(ctx, SEG_EOS));
-    SPH_TRY(sph_build_sph_lists(ctx, 0));
+    SPH_TRY(sph_build_sph_lists(ctx, 2));   // gather and symmetric lists of the final h, one pass
     SPH_TRY(time_mark(ctx, SEG_DRVT_LIST));
     SPH_TRY(sph_pass_derivative(ctx, 0));
     SPH_TRY(time_mark(ctx, SEG_DRVT));
-    SPH_TRY(sph_build_sph_lists(ctx, 1));
     SPH_TRY(time_mark(ctx, SEG_HYDRO_LIST));
     SPH_TRY(sph_pass_hydro(ctx, 0));
     SPH_TRY(time_mark(ctx, SEG_HYDRO));

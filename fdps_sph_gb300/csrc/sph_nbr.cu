@@ -550,6 +550,75 @@ k_filter(int n, const int *__restrict__ sup, const float *__restrict__ sup_r2, c
     ocnt[i] = k2;
 }
 
+// Both exact lists in one pass over the superset (the gather set is a subset of the symmetric
+// set, so the gather test runs only on symmetric members); same decisions and order as
+// k_filter<0> and k_filter<1>.
+__global__ void __launch_bounds__(128)
+k_filter2(int n, const int *__restrict__ sup, const float *__restrict__ sup_r2, const int *__restrict__ scnt,
+          RowMap rm, const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
+          const double *__restrict__ h, const float *__restrict__ H2f, int *__restrict__ out0,
+          int *__restrict__ ocnt0, int *__restrict__ out1, int *__restrict__ ocnt1) {
+    __shared__ int s_b0[8][128], s_b1[8][128];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double hi = h[i];
+    const double Hi = __dmul_rn(SUPPORT, hi);
+    const double H2 = __dmul_rn(Hi, Hi);
+    const float H2i = (float)H2;
+    const double xi = x[i], yi = y[i], zi = z[i];
+    const int c = scnt[i];
+    const int K = rm.K;
+    int *orow0 = out0 + (int64_t)i * K, *orow1 = out1 + (int64_t)i * K;
+    const bool sp = c > K && rm.soff;
+    int *osp0 = sp ? out0 + rm.main + rm.soff[i] - K : nullptr, *osp1 = sp ? out1 + rm.main + rm.soff[i] - K : nullptr;
+    const int t = threadIdx.x;
+    int k0 = 0, k1 = 0;
+    auto put = [&](int (*buf)[128], int &kk, int *orow, int *osp, int j) {
+        buf[kk & 7][t] = j;
+        ++kk;
+        if ((kk & 7) == 0) {
+            int4 *dst = reinterpret_cast<int4 *>((kk - 8 < K ? orow : osp) + kk - 8);
+            dst[0] = make_int4(buf[0][t], buf[1][t], buf[2][t], buf[3][t]);
+            dst[1] = make_int4(buf[4][t], buf[5][t], buf[6][t], buf[7][t]);
+        }
+    };
+    for (int seg = 0; seg < 2; ++seg) {
+        int cs;
+        const int64_t b = row_seg(rm, i, seg, c, &cs);
+        if (cs <= 0) break;
+        const int *row = sup + b;
+        const float *rrow = sup_r2 + b;
+        for (int k = 0; k < cs; k += 8) {
+            const int4 j0 = reinterpret_cast<const int4 *>(row + k)[0], j1 = reinterpret_cast<const int4 *>(row + k)[1];
+            const float4 r0 = reinterpret_cast<const float4 *>(rrow + k)[0],
+                         r1 = reinterpret_cast<const float4 *>(rrow + k)[1];
+            const int jj[8] = {j0.x, j0.y, j0.z, j0.w, j1.x, j1.y, j1.z, j1.w};
+            const float rr[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
+            const int m = min(8, cs - k);
+            float thr[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) thr[u] = u < m ? fmaxf(H2i, H2f[jj[u]]) : H2i;
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                if (u < m && exact_in(rr[u], thr[u], jj[u], xi, yi, zi, H2, x, y, z, h, true)) {
+                    put(s_b1, k1, orow1, osp1, jj[u]);
+                    if (exact_in(rr[u], H2i, jj[u], xi, yi, zi, H2, x, y, z, h, false)) put(s_b0, k0, orow0, osp0, jj[u]);
+                }
+            }
+        }
+    }
+    for (int q = 0; q < (k0 & 7); ++q) {
+        const int k = (k0 & ~7) + q;
+        (k < K ? orow0 : osp0)[k] = s_b0[q][t];
+    }
+    for (int q = 0; q < (k1 & 7); ++q) {
+        const int k = (k1 & ~7) + q;
+        (k < K ? orow1 : osp1)[k] = s_b1[q][t];
+    }
+    ocnt0[i] = k0;
+    ocnt1[i] = k1;
+}
+
 // Mixed-precision density straight from the superset: the gather-set
 // decision of k_filter<0>, then CalcDensity's sum (force.h:9-23) in FP32
 // partial sums of 32 flushed to FP64, FLAG_GI floor and h update in FP64.
@@ -873,13 +942,23 @@ static int ensure_superset(sph_ctx *ctx) {
     return walk_units(ctx, S.uidx, nmark);
 }
 
-// exact list of `mode` (0 gather, 1 symmetric) for the current h
+// exact list of `mode` (0 gather, 1 symmetric, 2 both) for the current h
 int sph_build_sph_lists(sph_ctx *ctx, int mode) {
     SphSuper &S = ctx->sup;
     const int n = (int)ctx->n;
     const int64_t cap = ctx->cap;
     int *meta = ctx->tree.meta;
     SPH_TRY(ensure_superset(ctx));
+    if (mode == 2) {   // both lists in one pass
+        SphLists &L0 = ctx->lists[0], &L1 = ctx->lists[1];
+        k_filter2<<<sph_div_up(n, 128), 128, 0, ctx->stream>>>(
+            n, S.nbr, S.r2, S.cnt, S.map(), FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
+            FLD(ctx->F, SPH_SMTH, cap), S.H2f, L0.nbr, L0.cnt, L1.nbr, L1.cnt);
+        ++ctx->launches;
+        SPH_CUDA(ctx, cudaGetLastError());
+        L0.valid = L1.valid = true;
+        return SPH_OK;
+    }
     SphLists &L = ctx->lists[mode];
     if (mode == 0)
         k_filter<0><<<sph_div_up(n, 128), 128, 0, ctx->stream>>>(
