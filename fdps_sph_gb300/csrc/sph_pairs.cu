@@ -633,9 +633,10 @@ __global__ void __launch_bounds__(GT) k_grav32(const int *__restrict__ group_cel
 // the child is tested, so an iteration waits on one global load.
 //
 // Accumulation: each thread carries two i-particles (ii and ii + Wt, Wt =
-// roundup(count / 2, 32)), and the block's P = 256 / Wt copies of the group
-// split each tile of j between them, four j per round; small groups keep the
-// FP32 lanes busy and every shared-memory read feeds two interactions.
+// roundup(count / 2, 8)), and the block's P = 256 / Wt copies of the group
+// split each tile of j between them, four consecutive j per round in paired
+// FP32 arithmetic; small groups keep the FP32 lanes busy and every
+// shared-memory read feeds two interactions.
 
 constexpr int GF_T = 256;
 constexpr int GF_Q = 2048;   // BFS ring of opened cell records (power of two)
@@ -656,6 +657,52 @@ __device__ __forceinline__ void grav_acc(float px, float py, float pz, float e2,
     a3 -= mri;
 }
 
+// packed pairs of FP32 values in one 64-bit register (low half first) and the paired FP32
+// arithmetic of sm_100+ (one instruction, two IEEE round-to-nearest results)
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 f2_pack(float a, float b) {
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(f32x2 r, float &a, float &b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ f32x2 f2_add(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 f2_mul(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 f2_fma(f32x2 a, f32x2 b, f32x2 c) {
+    f32x2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
+// grav_acc for two j at once (x, y, z, m: the pair's coordinates relative to the group origin and
+// masses), with the i-particle's negated coordinates and softening paired with themselves.  Per
+// interaction the same operations and roundings as grav_acc (q - p = -(p - q) exactly); the two j
+// accumulate in the two halves of a0..a3, and a3 sums +m / r (the potential's negative).
+__device__ __forceinline__ void grav_acc2(f32x2 nx, f32x2 ny, f32x2 nz, f32x2 e2, f32x2 x, f32x2 y, f32x2 z,
+                                          f32x2 m, f32x2 &a0, f32x2 &a1, f32x2 &a2, f32x2 &a3) {
+    const f32x2 dx = f2_add(x, nx), dy = f2_add(y, ny), dz = f2_add(z, nz);
+    const f32x2 r2 = f2_fma(dx, dx, f2_fma(dy, dy, f2_fma(dz, dz, e2)));
+    float ra, rb;
+    f2_unpack(r2, ra, rb);
+    const f32x2 ri = f2_pack(rsqrt_a(ra), rsqrt_a(rb));
+    const f32x2 mri = f2_mul(m, ri);
+    const f32x2 mr3 = f2_mul(f2_mul(mri, ri), ri);
+    a0 = f2_fma(mr3, dx, a0);
+    a1 = f2_fma(mr3, dy, a1);
+    a2 = f2_fma(mr3, dz, a2);
+    a3 = f2_add(a3, mri);
+}
+
 __global__ void __launch_bounds__(GF_T, 4)
 k_grav_fused32(const int *__restrict__ group_cell, const int4 *__restrict__ cinfo, const double4 *__restrict__ com,
                const double *__restrict__ rb_all, const int *__restrict__ prun, const double *__restrict__ x,
@@ -666,7 +713,8 @@ k_grav_fused32(const int *__restrict__ group_cell, const int4 *__restrict__ cinf
     __shared__ int4 s_q[GF_Q];
     __shared__ __align__(16) int s_e[GF_E];   // also the reduction buffer of the partitions
     __shared__ int s_s[GF_S];
-    __shared__ float4 s_tile[GF_T];
+    // the j tile as four arrays, so a thread's four consecutive entries load as two packed pairs
+    __shared__ __align__(16) float s_tx[GF_T], s_ty[GF_T], s_tz[GF_T], s_tm[GF_T];
     __shared__ int s_w[2][GF_W][3];            // per warp: leaf particles, far children, near children
     __shared__ double s_rb[MAX_LEVELS];
     __shared__ float s_rbf[MAX_LEVELS];
@@ -879,26 +927,35 @@ k_grav_fused32(const int *__restrict__ group_cell, const int4 *__restrict__ cinf
                         v = make_float4(df_diff(qh.x, ql.x, c_h.x, c_l.x), df_diff(qh.y, ql.y, c_h.y, c_l.y),
                                         df_diff(qh.z, ql.z, c_h.z, c_l.z), gm);
                     }
-                    s_tile[tid] = v;
+                    s_tx[tid] = v.x;
+                    s_ty[tid] = v.y;
+                    s_tz[tid] = v.z;
+                    s_tm[tid] = v.w;
                     __syncthreads();
                     if (slot) {
                         const int step = 4 * P;
                         const int tnr = (min(TE, nl - t0) + step - 1) / step * step;   // <= TE: step divides it
-                        float A[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
-                        for (int t = part; t < tnr; t += step) {
-                            const float4 q0 = s_tile[t], q1 = s_tile[t + P], q2 = s_tile[t + 2 * P],
-                                         q3 = s_tile[t + 3 * P];
+                        f32x2 A[2][4] = {{0ull, 0ull, 0ull, 0ull}, {0ull, 0ull, 0ull, 0ull}};
+                        for (int t = 4 * part; t < tnr; t += step) {
+                            const ulonglong2 X = *reinterpret_cast<const ulonglong2 *>(s_tx + t);
+                            const ulonglong2 Y = *reinterpret_cast<const ulonglong2 *>(s_ty + t);
+                            const ulonglong2 Z = *reinterpret_cast<const ulonglong2 *>(s_tz + t);
+                            const ulonglong2 M = *reinterpret_cast<const ulonglong2 *>(s_tm + t);
 #pragma unroll
                             for (int u = 0; u < 2; ++u) {
-                                grav_acc(px[u], py[u], pz[u], e2[u], q0, A[u][0], A[u][1], A[u][2], A[u][3]);
-                                grav_acc(px[u], py[u], pz[u], e2[u], q1, A[u][0], A[u][1], A[u][2], A[u][3]);
-                                grav_acc(px[u], py[u], pz[u], e2[u], q2, A[u][0], A[u][1], A[u][2], A[u][3]);
-                                grav_acc(px[u], py[u], pz[u], e2[u], q3, A[u][0], A[u][1], A[u][2], A[u][3]);
+                                const f32x2 nx = f2_pack(-px[u], -px[u]), ny = f2_pack(-py[u], -py[u]),
+                                            nz = f2_pack(-pz[u], -pz[u]), ee = f2_pack(e2[u], e2[u]);
+                                grav_acc2(nx, ny, nz, ee, X.x, Y.x, Z.x, M.x, A[u][0], A[u][1], A[u][2], A[u][3]);
+                                grav_acc2(nx, ny, nz, ee, X.y, Y.y, Z.y, M.y, A[u][0], A[u][1], A[u][2], A[u][3]);
                             }
                         }
 #pragma unroll
                         for (int u = 0; u < 2; ++u)
-                            for (int c4 = 0; c4 < 4; ++c4) df_add(Dh[u][c4], Dl[u][c4], A[u][c4]);
+                            for (int c4 = 0; c4 < 4; ++c4) {
+                                float lo, hi;
+                                f2_unpack(A[u][c4], lo, hi);
+                                df_add(Dh[u][c4], Dl[u][c4], c4 == 3 ? -(lo + hi) : lo + hi);
+                            }
                     }
                     __syncthreads();
                 }
