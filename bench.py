@@ -367,7 +367,8 @@ def main():
     kernels = {
         "sup_walk": ("dens_list", "hbm", 12 * entries + 68 * n, 1),         # rows (idx, r2, m) + particle reads
         "density": ("dens", "fp32", FLOPS_PER_PAIR["dens"] * w["pairs_gather"], 4),
-        "filters": (None, "hbm", 2 * (8 * entries + 4 * w["pairs_gather"]) // 2, 2),
+        # one pass: superset (idx, r2) read once, gather and symmetric lists written
+        "filters": (None, "hbm", 8 * entries + 4 * (w["pairs_gather"] + w["pairs_sym"]), 1),
         "derivative": ("drvt", "fp32", FLOPS_PER_PAIR["drvt"] * w["pairs_gather"], 1),
         "hydro": ("hydro", "fp32", FLOPS_PER_PAIR["hydro"] * w["pairs_sym"], 1),
         "grav_groups": ("grav_list", "hbm", 16 * w["cells"], 1),            # count / parent / flag per cell
