@@ -118,7 +118,7 @@ __device__ __forceinline__ float gap2_rd(float4 a_lo, float4 a_hi, float3 glo, f
 // SPILL: rows may continue in spill ranges (walks after this step's spill layout); without it
 // the hot loop carries no spill code (a row longer than K only raises the overflow flag)
 template <bool SPILL>
-__global__ void __launch_bounds__(NB_WARPS * 32, 7)
+__global__ void __launch_bounds__(NB_WARPS * 32, 8)
 k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ uidx, const double *__restrict__ x,
            const double *__restrict__ y, const double *__restrict__ z, const double *__restrict__ h,
            double *__restrict__ hsup, const float4 *__restrict__ xh,
@@ -133,9 +133,8 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
     __shared__ int s_sj[NB_WARPS][NB_SURV];
     __shared__ float4 s_ph[NB_WARPS][NB_SURV];
     __shared__ float4 s_pl[NB_WARPS][NB_SURV];
-    // per-lane write buffers, one 32-byte sector (8 entries) of index, r^2 and mass each, the
-    // lane's 24 words contiguous so a full buffer is read back with six 16-byte loads
-    __shared__ __align__(16) int s_wb[NB_WARPS][32][24];
+    // every lane's double-float position, for the lanes that write another lane's entries
+    __shared__ float4 s_pih[NB_WARPS][32], s_pil[NB_WARPS][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int w = blockIdx.x * NB_WARPS + warp;
     if (w >= n_units) return;   // warp-uniform
@@ -167,46 +166,12 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
     int2 *stack = s_stack[warp];
     int *cand = s_cand[warp];
     int count = 0, nc = 0;
-    int *row = sup + (int64_t)i * K;
-    float *rrow = sup_r2 + (int64_t)i * K;
-    float *mrow = sup_m + (int64_t)i * K;
-    // the spill range continues the row at entry K: entry k >= K at spill_base() + k (computed
-    // on the rare paths that need it, so nothing stays live through the walk)
+    // the spill range continues a row at entry K: entry k >= K of particle p at
+    // rm.main + rm.soff[p] - K + k (computed on the rare paths that need it)
     auto spill_cap = [&]() { return valid ? row_spill_cap(rm, i) : 0; };
-    auto spill_base = [&]() { return rm.main + rm.soff[i] - K; };
-    // appends one entry to the lane's buffer; a full buffer goes out as three sectors (in the
-    // row, or in its spill range: K is a multiple of 8, so a sector never straddles the two;
-    // entries past both are only counted, and the host grows the rows and walks again)
-    int *wb = s_wb[warp][lane];
-    auto put = [&](int j, float r2, float mj) {
-        const int q = count & 7;
-        wb[q] = j;
-        wb[8 + q] = __float_as_int(r2);
-        wb[16 + q] = __float_as_int(mj);
-        ++count;
-        if (q == 7) {
-            const int k0 = count - 8;
-            int *rw = row;
-            float *rr = rrow, *rq = mrow;
-            bool ok = k0 + 8 <= K;
-            if (!ok && SPILL && k0 + 8 <= K + spill_cap()) {
-                const int64_t sb = spill_base();
-                rw = sup + sb;
-                rr = sup_r2 + sb;
-                rq = sup_m + sb;
-                ok = true;
-            }
-            if (ok) {
-                const int4 *v = reinterpret_cast<const int4 *>(wb);
-                reinterpret_cast<int4 *>(rw + k0)[0] = v[0];
-                reinterpret_cast<int4 *>(rw + k0)[1] = v[1];
-                reinterpret_cast<int4 *>(rr + k0)[0] = v[2];
-                reinterpret_cast<int4 *>(rr + k0)[1] = v[3];
-                reinterpret_cast<int4 *>(rq + k0)[0] = v[4];
-                reinterpret_cast<int4 *>(rq + k0)[1] = v[5];
-            }
-        }
-    };
+    s_pih[warp][lane] = pih;
+    s_pil[warp][lane] = pil;
+    __syncwarp();
 
     // Candidates are culled 32 at a time, each against the unit's box grown by its own reach:
     // a lower bound of the distance (the point's hi / lo interval, rounded down) against an
@@ -257,15 +222,54 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
                     am |= (unsigned long long)(r2 < k2 * fmaxf(H2i, pl.w)) << t;
                 }
                 if (!valid) am = 0ull;
-                while (am) {
-                    const int t = __ffsll((long long)am) - 1;
-                    am &= am - 1ull;
-                    const float4 ph = s_ph[warp][t], pl = s_pl[warp][t];
-                    const float dx = df_sub(ph.x, pl.x, pih.x, pil.x);
-                    const float dy = df_sub(ph.y, pl.y, pih.y, pil.y);
-                    const float dz = df_sub(ph.z, pl.z, pih.z, pil.z);
-                    put(s_sj[warp][t], dx * dx + dy * dy + dz * dz, ph.w);
+                // The batch's accepted entries, lane by lane and in survivor order within a lane,
+                // are numbered e = 0 .. total - 1 and written by the whole warp, 32 at a time: a
+                // lane's run of entries lands contiguously in its row, so every store covers a few
+                // runs instead of 32 rows.  Entry e belongs to lane L (prefix[L] <= e < prefix[L]
+                // + nacc[L]) and is that lane's k-th accepted survivor, k = e - prefix[L].
+                const unsigned alo = (unsigned)am, ahi = (unsigned)(am >> 32);
+                const int nacc = __popc(alo) + __popc(ahi);
+                int incl = nacc;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int v = __shfl_up_sync(FULLM, incl, o);
+                    if (lane >= o) incl += v;
                 }
+                const int total = __shfl_sync(FULLM, incl, 31);
+                for (int e0 = 0; e0 < total; e0 += 32) {
+                    const int e = e0 + lane;
+                    int L = 0;   // the owner: the number of lanes whose inclusive prefix is <= e
+                    for (int st = 16; st > 0; st >>= 1) {
+                        const int v = __shfl_sync(FULLM, incl, L + st - 1);
+                        if (v <= e) L += st;
+                    }
+                    L = min(L, 31);
+                    const int excl = __shfl_sync(FULLM, incl - nacc, L);
+                    const unsigned lo = __shfl_sync(FULLM, alo, L), hi = __shfl_sync(FULLM, ahi, L);
+                    const int base = __shfl_sync(FULLM, count, L);
+                    if (e < total) {
+                        const int k = e - excl, plo = __popc(lo);
+                        const int t = k < plo ? (int)__fns(lo, 0, k + 1) : 32 + (int)__fns(hi, 0, k - plo + 1);
+                        const float4 ph = s_ph[warp][t], pl = s_pl[warp][t];
+                        const float4 qh = s_pih[warp][L], ql = s_pil[warp][L];
+                        const float dx = df_sub(ph.x, pl.x, qh.x, ql.x);
+                        const float dy = df_sub(ph.y, pl.y, qh.y, ql.y);
+                        const float dz = df_sub(ph.z, pl.z, qh.z, ql.z);
+                        const float r2 = dx * dx + dy * dy + dz * dz;
+                        const int iL = U.x + L, pos = base + k;
+                        if (pos < K) {
+                            const int64_t o = (int64_t)iL * K + pos;
+                            sup[o] = s_sj[warp][t];
+                            sup_r2[o] = r2;
+                            sup_m[o] = ph.w;
+                        } else if (SPILL && pos < K + row_spill_cap(rm, iL)) {
+                            const int64_t o = rm.main + rm.soff[iL] - K + pos;
+                            sup[o] = s_sj[warp][t];
+                            sup_r2[o] = r2;
+                            sup_m[o] = ph.w;
+                        }
+                    }
+                }
+                count += nacc;
                 ns = 0;
                 __syncwarp();
             }
@@ -322,22 +326,7 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
     }
     flush();
     if (valid) {
-        // the partial last block, entry by entry
-        const int k0 = count & ~7;
         const int scap = (SPILL && count > K) ? spill_cap() : 0;
-        for (int q = 0; q < (count & 7); ++q) {
-            const int k = k0 + q;
-            if (k < K) {
-                row[k] = wb[q];
-                rrow[k] = __int_as_float(wb[8 + q]);
-                mrow[k] = __int_as_float(wb[16 + q]);
-            } else if (SPILL && k < K + scap) {
-                const int64_t sb = spill_base();
-                sup[sb + k] = wb[q];
-                sup_r2[sb + k] = __int_as_float(wb[8 + q]);
-                sup_m[sb + k] = __int_as_float(wb[16 + q]);
-            }
-        }
         cnt[i] = count;   // the true count, also when the row had no room for all of it
         if (count > K + scap) atomicOr(err, ERR_SPH_LIST_OVERFLOW);
     }
