@@ -148,18 +148,16 @@ int compute_forces(sph_ctx *ctx) {
     SPH_TRY(sph_sort_and_build(ctx));   // marks SEG_SORT and SEG_TREE
     if (ctx->cfg.precision == SPH_PREC_MIXED) SPH_TRY(sph_pack_mixed(ctx));
     SPH_TRY(time_mark(ctx, SEG_NBR_PREP));
-    for (int it = 0; it < ctx->cfg.n_dens_iter; ++it) {
-        if (ctx->cfg.precision == SPH_PREC_MIXED) {
-            // the list-free pass makes the same neighbour decisions as the exact list
-            SPH_TRY(sph_nbr_ensure_superset(ctx));
-            SPH_TRY(time_mark(ctx, SEG_DENS_LIST));
-            SPH_TRY(sph_density_from_superset(ctx));
-        } else {
+    if (ctx->cfg.precision == SPH_PREC_MIXED) {
+        // all passes straight from the superset, with the same neighbour decisions as the exact list
+        SPH_TRY(sph_density_fused(ctx));
+    } else {
+        for (int it = 0; it < ctx->cfg.n_dens_iter; ++it) {
             SPH_TRY(sph_build_sph_lists(ctx, 0));
             SPH_TRY(time_mark(ctx, SEG_DENS_LIST));
             SPH_TRY(sph_pass_density(ctx, 0));
+            SPH_TRY(time_mark(ctx, SEG_DENS));
         }
-        SPH_TRY(time_mark(ctx, SEG_DENS));
     }
     SPH_TRY(sph_pass_eos(ctx));
     SPH_TRY(time_mark(ctx, SEG_EOS));
@@ -463,7 +461,7 @@ int sph_ctx_destroy(sph_ctx *ctx) {
                     ctx->sup.units, ctx->tree.cinfo, ctx->sup.r2, ctx->sup.m, ctx->sup.vR, ctx->sup.cvR,
                     ctx->sup.umark, ctx->sup.uoff, ctx->sup.uidx, ctx->runs.prun, ctx->runs.prun2,
                     ctx->runs.tiles, ctx->runs.info, ctx->runs.dt_dev, ctx->runs.part, ctx->runs.out,
-                    ctx->runs.damp, ctx->sup.soff, ctx->sup.need, ctx->sup.uover};
+                    ctx->runs.damp, ctx->sup.soff, ctx->sup.need, ctx->sup.uover, ctx->sup.npass};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (void *p : ctx->table_allocs) cudaFree(p);

@@ -199,6 +199,7 @@ struct SphSuper {
     int *soff = nullptr;          // [n + 1]
     int *need = nullptr;          // [n + 1] scratch
     int *uover = nullptr;         // per unit: some row of the unit is longer than K
+    int *npass = nullptr;         // [pitch] density passes a particle has completed this step
     bool spill_on = false;        // soff holds this sort's spill layout
     int64_t spill_alloc = 0;      // spill_cap the arrays were allocated with
     int64_t cap_soff = 0, cap_uover = 0;
@@ -355,6 +356,7 @@ int sph_nbr_prepare(sph_ctx *ctx);       // after the sort
 int sph_nbr_refresh_h(sph_ctx *ctx);     // after h changed
 int sph_build_sph_lists(sph_ctx *ctx, int mode);
 int sph_density_from_superset(sph_ctx *ctx);
+int sph_density_fused(sph_ctx *ctx);     // mixed precision: all density passes of a step
 int sph_nbr_ensure_superset(sph_ctx *ctx);   // mixed precision: density pass without an exact list
 int time_mark(sph_ctx *ctx, int seg);      // event at the end of a timed segment (when timing is on)
 int sph_runs_layout(sph_ctx *ctx);        // offsets and tiles of the runs after a change of the run set

@@ -669,6 +669,81 @@ k_density_sup32(int n, const int *__restrict__ sup, const float *__restrict__ su
     density_tail32(acc_h + acc_l, invH, dscale, m[i], dens + i, h + i);
 }
 
+// Every density pass of a step (CalcDensity, force.h:9-23, main.cpp:138-139) for a particle
+// in one go: the passes only use the particle's own h, and its row holds its gather set as
+// long as h <= KAPPA h_sup.  DT threads share a particle (entries 4 sub .. 4 sub + 3 in steps
+// of 4 DT; measured at 1M: DT 1 1.23 ms, 2 1.22, 4 1.36, 8 1.72 for the four passes, the
+// rows being too many for the passes to find them in L1 or L2); a particle whose new h
+// leaves the skin stops after that pass, to go on once its row is walked again.  Each term
+// m_j W_ij is rounded to a multiple of 2^-40 and summed as an integer, so the sum depends on
+// neither the order of the terms nor where non-members sit in the row.
+constexpr int DT = 2;
+constexpr float FIX_SCALE = 1099511627776.0f;   // 2^40
+__global__ void __launch_bounds__(128)
+k_density_fused32(int n, int n_pass, const int *__restrict__ sup, const float *__restrict__ sup_r2,
+                  const float *__restrict__ sup_m, const int *__restrict__ scnt, RowMap rm,
+                  const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
+                  const double *__restrict__ m, double *__restrict__ h, const double *__restrict__ hsup,
+                  double *__restrict__ dens, float dscale, int *__restrict__ npass, int *n_stopped) {
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = gt / DT, sub = gt % DT;
+    if (i >= n) return;   // whole groups leave together
+    int p = npass[i];
+    if (p >= n_pass) return;
+    const unsigned gm = __activemask();
+    double hi = h[i];
+    const double hs = hsup[i], xi = x[i], yi = y[i], zi = z[i], mi = m[i];
+    const int c_all = scnt[i];
+    bool stopped = false;
+    for (; p < n_pass && !stopped; ++p) {
+        const double Hi = __dmul_rn(SUPPORT, hi);
+        const double H2 = __dmul_rn(Hi, Hi);
+        const float H2i = (float)H2;
+        const float invH = 1.0f / (float)Hi;
+        const float lo_b = H2i * (1.0f - 1.9073486328125e-06f), hi_b = H2i * (1.0f + 1.9073486328125e-06f);
+        long long acc = 0;
+        for (int seg = 0; seg < 2; ++seg) {
+            int c;
+            const int64_t b = row_seg(rm, i, seg, c_all, &c);
+            if (c <= 0) break;
+            const float *rrow = sup_r2 + b, *mrow = sup_m + b;
+            for (int k = 4 * sub; k < c; k += 4 * DT) {
+                const float4 r4 = *reinterpret_cast<const float4 *>(rrow + k);
+                const float4 m4 = *reinterpret_cast<const float4 *>(mrow + k);
+                const float rr[4] = {r4.x, r4.y, r4.z, r4.w}, mj[4] = {m4.x, m4.y, m4.z, m4.w};
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    if (k + u >= c) break;
+                    bool in = rr[u] < lo_b;
+                    if (!in && !(rr[u] > hi_b))
+                        in = exact_in(rr[u], H2i, sup[b + k + u], xi, yi, zi, H2, x, y, z, h, false);
+                    if (!in) continue;
+                    const float s_ = sqrt_a(rr[u]) * invH;
+                    const float q = fmaxf(1.0f - s_, 0.0f);
+                    const float q2 = q * q, q4 = q2 * q2;
+                    const float term = mj[u] * ((1.0f + s_ * (8.0f + s_ * (25.0f + s_ * 32.0f))) * (q4 * q4));
+                    acc += __float2ll_rn(term * FIX_SCALE);
+                }
+            }
+        }
+#pragma unroll
+        for (int o = DT / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(gm, acc, o, DT);
+        double rho, hn;
+        density_tail32((float)((double)acc * (1.0 / 1099511627776.0)), invH, dscale, mi, &rho, &hn);
+        hi = hn;
+        if (sub == 0) {
+            dens[i] = rho;
+            h[i] = hn;
+        }
+        // the row can miss members of the next pass's set: the same test as k_viol_mark
+        stopped = p + 1 < n_pass && hn > (double)KAPPA * hs;
+    }
+    if (sub == 0) {
+        npass[i] = p;
+        if (stopped) atomicAdd(n_stopped, 1);
+    }
+}
+
 __global__ void k_skin_check(int n, const double *h, const double *hsup, int *err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n && h[i] > (double)KAPPA * hsup[i]) atomicOr(err, ERR_SKIN);
@@ -739,6 +814,7 @@ int sph_nbr_prepare(sph_ctx *ctx) {
         SPH_TRY(dalloc_n(ctx, &S.hsup, pitch));
         SPH_TRY(dalloc_n(ctx, &S.cnt, pitch));
         SPH_TRY(dalloc_n(ctx, &S.vR, pitch));
+        SPH_TRY(dalloc_n(ctx, &S.npass, pitch));
         S.cap_particles = pitch;
     }
     const int64_t cap = ctx->cap;
@@ -981,3 +1057,36 @@ int sph_density_from_superset(sph_ctx *ctx) {
 }
 
 int sph_nbr_ensure_superset(sph_ctx *ctx) { return ensure_superset(ctx); }
+
+// all density passes of the mixed path: rounds of k_density_fused32, the rows of the particles
+// that left their skin walked again between rounds (each round takes every unfinished particle
+// at least one pass further, so there are at most n_dens_iter rounds)
+int sph_density_fused(sph_ctx *ctx) {
+    SphSuper &S = ctx->sup;
+    const int n = (int)ctx->n;
+    const int64_t cap = ctx->cap;
+    const int np = ctx->cfg.n_dens_iter;
+    int *stopped = ctx->tree.meta + META_ERR + 9;
+    int *hs = (int *)ctx->host_scalars;
+    SPH_CUDA(ctx, cudaMemsetAsync(S.npass, 0, sizeof(int) * n, ctx->stream));
+    for (int round = 0; round <= np; ++round) {
+        SPH_TRY(ensure_superset(ctx));
+        SPH_TRY(time_mark(ctx, SEG_DENS_LIST));
+        SPH_CUDA(ctx, cudaMemsetAsync(stopped, 0, sizeof(int), ctx->stream));
+        k_density_fused32<<<sph_div_up((int64_t)n * DT, 128), 128, 0, ctx->stream>>>(
+            n, np, S.nbr, S.r2, S.m, S.cnt, S.map(), FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap),
+            FLD(ctx->F, SPH_Z, cap), FLD(ctx->F, SPH_MASS, cap), FLD(ctx->F, SPH_SMTH, cap), S.hsup,
+            FLD(ctx->F, SPH_DENS, cap), (float)(1365.0 / 64.0 / (3.141592653589793 * ctx->mscale)), S.npass,
+            stopped);
+        ++ctx->launches;
+        SPH_CUDA(ctx, cudaGetLastError());
+        SPH_TRY(time_mark(ctx, SEG_DENS));
+        SPH_CUDA(ctx, cudaMemcpyAsync(hs, stopped, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        SPH_TRY(sph_nbr_refresh_h(ctx));   // H2f of the current h, for the walks and the filters
+        if (hs[0] == 0) break;
+        if (round == np) return sph_fail(ctx, SPH_ERR_STATE, "density passes did not converge over the skin repairs");
+    }
+    ctx->lists[0].valid = false;
+    return SPH_OK;
+}
