@@ -763,7 +763,10 @@ k_grav_fused32(const int *__restrict__ group_cell, const int4 *__restrict__ cinf
             hif[d] = (float)(s_gbox[3 + d] - o);
         }
     }
-    const int q = tid >> 3, k = tid & 7, qw = lane >> 3;
+    // walk lanes: 64 opened cells per iteration, four lanes per cell, two children per lane
+    // (octants k and k + 4); appends go cell by cell, first children before second children
+    const int q = tid >> 2, k = tid & 3, qw = lane >> 2;
+    const unsigned cellm = 0xFu << (qw * 4), before = (1u << (qw * 4)) - 1u;
     int tot_e = 0, tot_s = 0;
     for (int i_base = 0; i_base < cnt_all; i_base += 2 * GF_T) {
         const int cnt = min(2 * GF_T, cnt_all - i_base);
@@ -800,19 +803,22 @@ k_grav_fused32(const int *__restrict__ group_cell, const int4 *__restrict__ cinf
                     done = 1;
                     break;
                 }
-                const int nproc = min(GF_T / 8, tail - head);
+                const int nproc = min(GF_T / 4, tail - head);
                 const bool a = q < nproc;
                 const int4 ci = a ? s_q[(head + q) & (GF_Q - 1)] : make_int4(0, 0, 0, 0);
                 const int nch = ci.y & 255, lev = ci.y >> 8;
                 const bool leaf = a && nch == 0;
-                const int lc = leaf ? ci.w : 0;   // same in the eight lanes of a cell
-                bool near = false, far = false;
-                int chc = 0;
-                int4 crec = make_int4(0, 0, 0, 0);
-                if (a && k < nch) {
-                    chc = ci.x + k;
-                    const float4 qh = ch[chc], ql = cl[chc];
-                    crec = cinfo[chc];
+                const int lc = leaf ? ci.w : 0;   // same in the four lanes of a cell
+                bool near[2] = {false, false}, far[2] = {false, false};
+                int chc[2] = {0, 0};
+                int4 crec[2] = {make_int4(0, 0, 0, 0), make_int4(0, 0, 0, 0)};
+#pragma unroll
+                for (int hh = 0; hh < 2; ++hh) {
+                    const int kk = k + 4 * hh;
+                    if (!(a && kk < nch)) continue;
+                    chc[hh] = ci.x + kk;
+                    const float4 qh = ch[chc[hh]], ql = cl[chc[hh]];
+                    crec[hh] = cinfo[chc[hh]];
                     const float rbf = s_rbf[lev + 1];
                     // FP32 distance from the box on coordinates relative to the group origin, with a
                     // bound on its error; inside the bound the FP64 test of the list walk decides
@@ -830,10 +836,11 @@ k_grav_fused32(const int *__restrict__ group_cell, const int4 *__restrict__ cinf
                         E = fmaf(2.0f * dd + ed, ed, E);
                     }
                     E += 4.76837158203125e-07f * (d2f + rbf);   // 2^-21: sums and the rounding of rb
+                    bool nr;
                     if (fabsf(d2f - rbf) > E) {
-                        near = d2f <= rbf;
+                        nr = d2f <= rbf;
                     } else {
-                        const double4 cm = com[chc];
+                        const double4 cm = com[chc[hh]];
                         const double pp[3] = {cm.x, cm.y, cm.z};
                         double dd[3];
                         for (int d = 0; d < 3; ++d) {
@@ -842,23 +849,24 @@ k_grav_fused32(const int *__restrict__ group_cell, const int4 *__restrict__ cinf
                         }
                         const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dd[0], dd[0]), __dmul_rn(dd[1], dd[1])),
                                                     __dmul_rn(dd[2], dd[2]));
-                        near = d2 <= s_rb[lev + 1];
+                        nr = d2 <= s_rb[lev + 1];
                     }
-                    far = !near;
+                    near[hh] = nr;
+                    far[hh] = !nr;
                 }
-                const unsigned nm = __ballot_sync(0xffffffffu, near);
-                const unsigned fm = __ballot_sync(0xffffffffu, far);
+                const unsigned nm0 = __ballot_sync(0xffffffffu, near[0]), nm1 = __ballot_sync(0xffffffffu, near[1]);
+                const unsigned fm0 = __ballot_sync(0xffffffffu, far[0]), fm1 = __ballot_sync(0xffffffffu, far[1]);
                 int lpre = 0, lsum = 0;
-                for (int g = 0; g < 4; ++g) {
-                    const int v = __shfl_sync(0xffffffffu, lc, g * 8);
+                for (int g = 0; g < 8; ++g) {
+                    const int v = __shfl_sync(0xffffffffu, lc, g * 4);
                     lpre += g < qw ? v : 0;
                     lsum += v;
                 }
                 const int buf = it & 1;
                 if (lane == 0) {
                     s_w[buf][warp][0] = lsum;
-                    s_w[buf][warp][1] = __popc(fm);
-                    s_w[buf][warp][2] = __popc(nm);
+                    s_w[buf][warp][1] = __popc(fm0) + __popc(fm1);
+                    s_w[buf][warp][2] = __popc(nm0) + __popc(nm1);
                 }
                 __syncthreads();
                 int oe = 0, of = 0, on = 0, te = 0, tf = 0, tn = 0;
@@ -888,11 +896,24 @@ k_grav_fused32(const int *__restrict__ group_cell, const int4 *__restrict__ cinf
                     break;
                 }
                 if (leaf)
-                    for (int t = k; t < lc; t += 8) s_e[ne + oe + lpre + t] = ci.z + t;
-                if (far) s_s[ns + of + __popc(fm & below)] = chc;
-                if (near) {
-                    crec.y = (crec.y & 255) | ((lev + 1) << 8);
-                    s_q[(tail + on + __popc(nm & below)) & (GF_Q - 1)] = crec;
+                    for (int t = k; t < lc; t += 4) s_e[ne + oe + lpre + t] = ci.z + t;
+                {
+                    // order within the warp: cell by cell, a cell's first children, then its second
+                    const int f_pre = __popc(fm0 & before) + __popc(fm1 & before);
+                    const int n_pre = __popc(nm0 & before) + __popc(nm1 & before);
+                    const int f_pos[2] = {f_pre + __popc(fm0 & cellm & below),
+                                          f_pre + __popc(fm0 & cellm) + __popc(fm1 & cellm & below)};
+                    const int n_pos[2] = {n_pre + __popc(nm0 & cellm & below),
+                                          n_pre + __popc(nm0 & cellm) + __popc(nm1 & cellm & below)};
+#pragma unroll
+                    for (int hh = 0; hh < 2; ++hh) {
+                        if (far[hh]) s_s[ns + of + f_pos[hh]] = chc[hh];
+                        if (near[hh]) {
+                            int4 r = crec[hh];
+                            r.y = (r.y & 255) | ((lev + 1) << 8);
+                            s_q[(tail + on + n_pos[hh]) & (GF_Q - 1)] = r;
+                        }
+                    }
                 }
                 ne += te;
                 ns += tf;
