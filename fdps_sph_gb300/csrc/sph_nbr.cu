@@ -769,10 +769,15 @@ __global__ void k_pack_pos(int n, const double *x, const double *y, const double
 }
 
 // spill range lengths: rows longer than K take round8(count - K) entries beyond the row block
-__global__ void k_spill_need(int n, const int *cnt, int K, int *need) {
+__global__ void k_spill_need(int n, const int *cnt, int K, int *need, unsigned long long *total) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) need[i] = cnt[i] > K ? ((cnt[i] - K + 7) & ~7) : 0;
-    else if (i == n) need[i] = 0;
+    int v = 0;
+    if (i < n) v = cnt[i] > K ? ((cnt[i] - K + 7) & ~7) : 0;
+    if (i <= n) need[i] = v;
+    // the sum in 64 bits: the offsets are 32-bit, so a total past 2^31 must be refused, not wrapped
+    unsigned long long w = (unsigned long long)v;
+    for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+    if ((threadIdx.x & 31) == 0 && w) atomicAdd(total, w);
 }
 
 }  // namespace sph
@@ -930,12 +935,21 @@ static int walk_units(sph_ctx *ctx, const int *uidx, int n_walk) {
                 SPH_TRY(dalloc_n(ctx, &S.need, n + 1 + 1024));
                 S.cap_soff = n + 1 + 1024;
             }
-            k_spill_need<<<sph_div_up(n + 1, 256), 256, 0, ctx->stream>>>(n, S.cnt, S.K, S.need);
+            unsigned long long *tot64 = reinterpret_cast<unsigned long long *>(ctx->scratch_d);
+            SPH_CUDA(ctx, cudaMemsetAsync(tot64, 0, sizeof(unsigned long long), ctx->stream));
+            k_spill_need<<<sph_div_up(n + 1, 256), 256, 0, ctx->stream>>>(n, S.cnt, S.K, S.need, tot64);
             ++ctx->launches;
-            SPH_TRY(sph_scan_exclusive(ctx, S.need, S.soff, nullptr, n + 1, ctx->scan.total));
-            SPH_CUDA(ctx, cudaMemcpyAsync(hs, ctx->scan.total, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+            SPH_CUDA(ctx, cudaMemcpyAsync(&ctx->host_scalars[1], tot64, sizeof(unsigned long long),
+                                          cudaMemcpyDeviceToHost, ctx->stream));
             SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-            const int64_t need = hs[0];
+            unsigned long long need64 = 0;
+            std::memcpy(&need64, &ctx->host_scalars[1], sizeof(need64));
+            if (need64 > (unsigned long long)INT32_MAX - 4096)
+                return sph_fail(ctx, SPH_ERR_CAPACITY,
+                                "neighbour rows need %llu entries beyond the row block (smoothing lengths out of "
+                                "range?)", need64);
+            SPH_TRY(sph_scan_exclusive(ctx, S.need, S.soff, nullptr, n + 1, ctx->scan.total));
+            const int64_t need = (int64_t)need64;
             S.spill_on = true;
             S.spilled = need;
             if (need > S.spill_cap) {
