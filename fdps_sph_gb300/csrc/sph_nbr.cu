@@ -1004,7 +1004,7 @@ static int ensure_superset(sph_ctx *ctx) {
     if ((int64_t)nviol * 8 > n) return build_superset(ctx);   // widespread growth: walk everything
     // influence radius per cell, bottom-up
     const int grid = 2 * ctx->num_sms;
-    for (int l = KEY_LEVELS; l >= 0; --l) {
+    for (int l = t.depth; l >= 0; --l) {
         k_cell_vmax<<<grid, 128, 0, ctx->stream>>>(l, meta, vR, t.cinfo, S.cvR);
         ++ctx->launches;
     }

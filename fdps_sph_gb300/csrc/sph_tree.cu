@@ -725,6 +725,17 @@ __global__ void k_pack_cinfo(const int *meta, const int *first_child, const int 
         cinfo[c] = make_int4(first_child[c], n_child[c], start[c], count[c]);
 }
 
+// after the levels [0, Lb) were split: flags a cell of level Lb that would still split (the tree
+// is deeper than this build went) and marks the levels below Lb empty
+__global__ void k_tree_tail(int Lb, int n_leaf, int *meta, const int *count) {
+    const int L0 = meta[Lb], L1 = meta[Lb + 1];
+    if (Lb < KEY_LEVELS)
+        for (int c = L0 + blockIdx.x * blockDim.x + threadIdx.x; c < L1; c += gridDim.x * blockDim.x)
+            if (count[c] > n_leaf) atomicOr(&meta[META_ERR], ERR_TREE_DEEPER);
+    if (blockIdx.x == 0)
+        for (int l = Lb + 2 + threadIdx.x; l <= MAX_LEVELS; l += blockDim.x) meta[l] = L1;
+}
+
 __global__ void k_hmax(int l, const int *meta, const double *h, const int *start, const int *count,
                        const int *first_child, const int *n_child, float4 *bhi) {
     const int L0 = meta[l], L1 = meta[l + 1];
@@ -830,6 +841,32 @@ static int radix_sort(sph_ctx *ctx, int n) {
     return SPH_OK;
 }
 
+// the octree over the sorted particles, level by level (level sizes stay on the device): the
+// levels [0, Lb) are split, then a tail kernel checks that level Lb needs no split (else the
+// host builds again with every level) and marks the deeper levels empty; moments bottom-up
+static int enqueue_tree(sph_ctx *ctx, int Lb) {
+    const int64_t cap = ctx->cap;
+    Tree &t = ctx->tree;
+    cudaStream_t st = ctx->stream;
+    const double *x = FLD(ctx->F, SPH_X, cap), *y = FLD(ctx->F, SPH_Y, cap), *z = FLD(ctx->F, SPH_Z, cap);
+    const double *m = FLD(ctx->F, SPH_MASS, cap), *h = FLD(ctx->F, SPH_SMTH, cap);
+    const int grid = 2 * ctx->num_sms;
+    for (int l = 0; l < Lb; ++l) {
+        k_split<<<grid, 256, 0, st>>>(l, ctx->cfg.n_leaf, ctx->keys, t.meta, t.start, t.count, t.tmp_cnt, t.tmp_b); ++ctx->launches;
+        SPH_TRY(scan_exclusive_diff(ctx, t.tmp_cnt, t.tmp_off, t.meta + l, ctx->scan.total));
+        k_emit<<<grid, 256, 0, st>>>(l, t.cap, t.meta, t.tmp_cnt, t.tmp_off, t.tmp_b, ctx->scan.total, t.start,
+                                     t.count, t.level, t.parent, t.first_child, t.n_child); ++ctx->launches;
+    }
+    k_tree_tail<<<grid, 256, 0, st>>>(Lb, ctx->cfg.n_leaf, t.meta, t.count); ++ctx->launches;
+    for (int l = Lb; l >= 0; --l)
+        k_moments<<<grid, 128, 0, st>>>(l, t.meta, x, y, z, m, h, t.start, t.count, t.first_child, t.n_child,
+                                        t.mom, t.com, t.blo, t.bhi); ++ctx->launches;
+    k_pack_cinfo<<<grid, 256, 0, st>>>(t.meta, t.first_child, t.n_child, t.start, t.count, t.cinfo);
+    ++ctx->launches;
+    SPH_CUDA(ctx, cudaGetLastError());
+    return SPH_OK;
+}
+
 // the device work of sph_sort_and_build up to the cell-count read: root cubes, keys, the
 // segmented radix sort, the permutation (and its host-side buffer swaps), the octree levels,
 // the moments.  No host synchronisation and no allocation inside, so it can be captured.
@@ -859,25 +896,7 @@ static int enqueue_sort_tree(sph_ctx *ctx) {
     std::swap(ctx->mat, ctx->mat2);
     SPH_CUDA(ctx, cudaMemcpyAsync(ctx->keys, ctx->sort.k0, sizeof(uint64_t) * n, cudaMemcpyDeviceToDevice, st));
     SPH_TRY(time_mark(ctx, SEG_SORT));
-    x = FLD(ctx->F, SPH_X, cap);
-    y = FLD(ctx->F, SPH_Y, cap);
-    z = FLD(ctx->F, SPH_Z, cap);
-    const double *m = FLD(ctx->F, SPH_MASS, cap), *h = FLD(ctx->F, SPH_SMTH, cap);
-    // octree, level by level; level sizes stay on the device
-    const int grid = 2 * ctx->num_sms;
-    for (int l = 0; l < KEY_LEVELS; ++l) {
-        k_split<<<grid, 256, 0, st>>>(l, ctx->cfg.n_leaf, ctx->keys, t.meta, t.start, t.count, t.tmp_cnt, t.tmp_b); ++ctx->launches;
-        SPH_TRY(scan_exclusive_diff(ctx, t.tmp_cnt, t.tmp_off, t.meta + l, ctx->scan.total));
-        k_emit<<<grid, 256, 0, st>>>(l, t.cap, t.meta, t.tmp_cnt, t.tmp_off, t.tmp_b, ctx->scan.total, t.start,
-                                     t.count, t.level, t.parent, t.first_child, t.n_child); ++ctx->launches;
-    }
-    for (int l = KEY_LEVELS; l >= 0; --l)
-        k_moments<<<grid, 128, 0, st>>>(l, t.meta, x, y, z, m, h, t.start, t.count, t.first_child, t.n_child,
-                                        t.mom, t.com, t.blo, t.bhi); ++ctx->launches;
-    k_pack_cinfo<<<grid, 256, 0, st>>>(t.meta, t.first_child, t.n_child, t.start, t.count, t.cinfo);
-    ++ctx->launches;
-    SPH_CUDA(ctx, cudaGetLastError());
-    return SPH_OK;
+    return enqueue_tree(ctx, t.levels);
 }
 
 // Everything the captured work depends on: sizes and every buffer it touches.  The permutation
@@ -889,7 +908,8 @@ static void graph_key(const sph_ctx *ctx, uintptr_t key[GRAPH_KEY_N]) {
         (uintptr_t)ctx->F,         (uintptr_t)ctx->F2,         (uintptr_t)ctx->id,       (uintptr_t)ctx->slot,
         (uintptr_t)ctx->mat,       (uintptr_t)ctx->runs.prun,  (uintptr_t)ctx->keys,     (uintptr_t)ctx->sort.k0,
         (uintptr_t)ctx->sort.hist, (uintptr_t)t.start,         (uintptr_t)t.rb,          (uintptr_t)t.cap,
-        (uintptr_t)ctx->runs.tiles, (uintptr_t)ctx->runs.part, (uintptr_t)ctx->scan.part, (uintptr_t)t.cinfo};
+        (uintptr_t)ctx->runs.tiles, (uintptr_t)ctx->runs.part, (uintptr_t)ctx->scan.part, (uintptr_t)t.cinfo,
+        (uintptr_t)t.levels};
     for (int i = 0; i < GRAPH_KEY_N; ++i) key[i] = k[i];
 }
 
@@ -957,7 +977,20 @@ int sph_sort_and_build(sph_ctx *ctx) {
     SPH_CUDA(ctx, cudaStreamSynchronize(st));
     if (hs[META_ERR] & ERR_NONFINITE) return sph_fail(ctx, SPH_ERR_NONFINITE, "non-finite particle position");
     if (hs[META_ERR] & ERR_CELL_OVERFLOW) return sph_fail(ctx, SPH_ERR_CAPACITY, "octree cell capacity exceeded");
+    if (hs[META_ERR] & ERR_TREE_DEEPER) {   // deeper than the last tree plus two levels: every level
+        SPH_CUDA(ctx, cudaMemsetAsync(t.meta + META_ERR, 0, sizeof(int), st));
+        t.levels = KEY_LEVELS;
+        SPH_TRY(enqueue_tree(ctx, KEY_LEVELS));
+        SPH_CUDA(ctx, cudaMemcpyAsync(hs, t.meta, sizeof(int) * META_N, cudaMemcpyDeviceToHost, st));
+        SPH_CUDA(ctx, cudaStreamSynchronize(st));
+        if (hs[META_ERR] & ERR_CELL_OVERFLOW) return sph_fail(ctx, SPH_ERR_CAPACITY, "octree cell capacity exceeded");
+    }
     t.n_cell_host = hs[MAX_LEVELS];
+    int depth = 0;
+    for (int l = 0; l < MAX_LEVELS; ++l)
+        if (hs[l + 1] > hs[l]) depth = l;
+    t.depth = depth;
+    t.levels = std::min(KEY_LEVELS, depth + 2);
     ctx->grav.valid = false;
     ctx->grav.counts_valid = false;
     SPH_TRY(time_mark(ctx, SEG_TREE));
@@ -968,7 +1001,7 @@ int sph_tree_refresh_hmax(sph_ctx *ctx) {
     Tree &t = ctx->tree;
     const double *h = FLD(ctx->F, SPH_SMTH, ctx->cap);
     const int grid = 2 * ctx->num_sms;
-    for (int l = KEY_LEVELS; l >= 0; --l)
+    for (int l = t.depth; l >= 0; --l)
         k_hmax<<<grid, 128, 0, ctx->stream>>>(l, t.meta, h, t.start, t.count, t.first_child, t.n_child, t.bhi); ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
     return SPH_OK;

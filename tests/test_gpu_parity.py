@@ -57,6 +57,35 @@ def test_keys_order_and_tree_bit_exact(impact):
         assert com == (c["com"][0], c["com"][1], c["com"][2], c["mass"])   # bit-identical monopoles
 
 
+def test_tree_deeper_than_the_last_one(impact):
+    """A build splits only as many levels as the last tree had, plus two; a tree that needs more
+    (here: a clump of particles 1e-4 m apart uploaded into a context whose last tree was
+    shallow) is built again with every level and equals the oracle's."""
+    from oracle import pyoracle as po
+    F, ids, mats = impact
+    ctx = device_context(tillotson_materials())
+    ctx.upload(F[:, :300].copy(), ids[:300], mats[:300])   # a shallow tree first
+    ctx.run_pass(0)
+    G = F.copy()
+    G[0, :40] = G[0, 0] + 1.0e-4 * np.arange(40)             # a clump: many more levels
+    G[1, :40] = G[1, 0]
+    G[2, :40] = G[2, 0]
+    ctx.upload(G, ids, mats)
+    ctx.run_pass(0)
+    _, idd, keys = _dev_sorted(ctx)
+    s = _oracle(G, ids, mats)
+    tr = po.OracleTree(s)
+    assert np.array_equal(idd, s.id) and np.array_equal(keys, tr.keys())
+    dt = ctx.tree()
+    oc = tr.cells()
+    assert len(dt["start"]) == len(oc) and int(max(dt["level"])) > 12
+    dev = {(int(l), int(s_)): (int(c), int(n)) for l, s_, c, n in
+           zip(dt["level"], dt["start"], dt["count"], dt["n_child"])}
+    for c in oc:
+        assert dev[(int(c["level"]), int(c["start"]))] == (c["count"], c["n_child"])
+    ctx.close()
+
+
 def test_passes_and_lists_match_oracle(impact):
     from oracle import pyoracle as po
     F, ids, mats = impact
