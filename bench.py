@@ -60,7 +60,7 @@ def parse():
     ap.add_argument("--cpu-n", type=int, default=100_000, help="particles of the bounded CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-batch", action="store_true", help="skip the batched sweep and the serving window")
     ap.add_argument("--config", default="1m", choices=["1m", "4m"], help="geometry of the workload (see workload())")
     ap.add_argument("--theta", type=float, default=0.5, help="gravity opening angle")
@@ -226,15 +226,17 @@ def drift(d0, d1, steps):
     return {"energy_rel_per_step": e, "angmom_rel_per_step": lv}
 
 
-def run_e2e(ctx, F, ids, mats, steps):
-    """upload (pinned host) -> one step -> download (pinned host), every step.  The upload
-    copies the fields the step reads or carries (SPH_UPLOAD_STEP_INPUTS); the download
-    returns every field, ids and materials."""
+def run_e2e(ctx, F, ids, mats, steps, warmup=2):
+    """upload (pinned host) -> one step -> download (pinned host), every step.  The upload copies
+    the fields the step reads or carries (SPH_UPLOAD_STEP_INPUTS); the download copies every
+    field the step writes (SPH_STEP_OUTPUT_FIELDS) into the host's block, whose other rows (mass,
+    AVa, entropy, temperature; ids and materials, in upload order) the step leaves unchanged.
+    `warmup` round trips run untimed first (the first ones capture the CUDA graphs of the new
+    buffer layout)."""
     import torch
     from fdps_sph_gb300 import lib
     n = F.shape[1]
     hostF = torch.empty((F.shape[0], n), dtype=torch.float64).pin_memory().numpy()
-    outF = torch.empty((F.shape[0], n), dtype=torch.float64).pin_memory().numpy()
     hid = torch.empty(n, dtype=torch.int64).pin_memory().numpy()
     hmat = torch.empty(n, dtype=torch.int32).pin_memory().numpy()
     # start from the context's current state (forces valid)
@@ -242,18 +244,24 @@ def run_e2e(ctx, F, ids, mats, steps):
     hostF[:] = Fc
     hid[:] = idc
     hmat[:] = matc
+    outs = lib.STEP_OUTPUT_FIELDS + (["ent", "temp"] if ctx.cfg.mode == 2 else [])
     t_now, dt, _ = ctx.time()
-    t0 = time.perf_counter()
-    for _ in range(steps):
+
+    def round_trip():
+        nonlocal t_now, dt
         ctx.upload(hostF, hid, hmat, time=t_now, dt=dt, forces_valid=True, inputs_only=True)
         ctx.step(1)
         t_now, dt, _ = ctx.time()
-        o, oid, om = ctx.download(outF)
-        hostF, outF = outF, hostF
-        hid, hmat = oid, om
+        ctx.download_fields(hostF, outs)
+
+    for _ in range(warmup):
+        round_trip()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        round_trip()
     el = time.perf_counter() - t0
     h2d = 8 * n * len(lib.STEP_INPUT_FIELDS) + hid.nbytes + hmat.nbytes
-    d2h = hostF.nbytes + hid.nbytes + hmat.nbytes
+    d2h = 8 * n * len(outs)
     return el, h2d, d2h
 
 

@@ -752,23 +752,41 @@ int sph_run_diagnostics(sph_ctx *ctx, int64_t handle, double out[8]) {
     return SPH_OK;
 }
 
-int sph_download(sph_ctx *ctx, double *fields, int64_t ld, int64_t *id, int32_t *material) {
+int sph_download_fields(sph_ctx *ctx, double *fields, int64_t ld, uint64_t field_mask, int64_t *id,
+                        int32_t *material) {
     if (!ctx) return SPH_ERR_ARG;
     if (!ctx->uploaded) return sph_fail(ctx, SPH_ERR_STATE, "download before upload");
-    if (!fields || ld < ctx->n) return sph_fail(ctx, SPH_ERR_ARG, "bad output block");
+    if ((field_mask && !fields) || ld < ctx->n) return sph_fail(ctx, SPH_ERR_ARG, "bad output block");
     cudaSetDevice(ctx->device);
     const int n = (int)ctx->n;
     k_unpermute<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(ctx->F, ctx->F2, ctx->cap, 0, n, ctx->slot,
                                                              ctx->runs.prun, ctx->runs.info, ctx->id, ctx->id2,
                                                              ctx->mat, ctx->mat2); ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
-    SPH_CUDA(ctx, cudaMemcpy2DAsync(fields, sizeof(double) * ld, ctx->F2, sizeof(double) * ctx->cap,
-                                    sizeof(double) * n, SPH_NFIELD, cudaMemcpyDeviceToHost, ctx->stream));
+    // rows of consecutive requested fields in one 2D copy each
+    for (int f = 0; f < SPH_NFIELD;) {
+        if (!((field_mask >> f) & 1)) {
+            ++f;
+            continue;
+        }
+        int g = f;
+        while (g < SPH_NFIELD && ((field_mask >> g) & 1)) ++g;
+        SPH_CUDA(ctx, cudaMemcpy2DAsync(fields + (int64_t)f * ld, sizeof(double) * ld, ctx->F2 + (int64_t)f * ctx->cap,
+                                        sizeof(double) * ctx->cap, sizeof(double) * n, g - f, cudaMemcpyDeviceToHost,
+                                        ctx->stream));
+        f = g;
+    }
     if (id) SPH_CUDA(ctx, cudaMemcpyAsync(id, ctx->id2, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, ctx->stream));
     if (material)
         SPH_CUDA(ctx, cudaMemcpyAsync(material, ctx->mat2, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, ctx->stream));
     SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return SPH_OK;
+}
+
+int sph_download(sph_ctx *ctx, double *fields, int64_t ld, int64_t *id, int32_t *material) {
+    if (!ctx) return SPH_ERR_ARG;
+    if (!fields) return sph_fail(ctx, SPH_ERR_ARG, "bad output block");
+    return sph_download_fields(ctx, fields, ld, ~0ull, id, material);
 }
 
 int sph_prologue(sph_ctx *ctx) {

@@ -39,11 +39,13 @@ EXPORTS = [
     "sph_get_neighbors", "sph_get_tree", "sph_get_grav_list", "sph_get_timings", "sph_step_timed",
     "sph_get_counters", "sph_probe_peak", "sph_morton_order_noalloc",
     "sph_add_run", "sph_remove_run", "sph_list_runs", "sph_run_info", "sph_download_run", "sph_run_diagnostics",
-    "sph_autotune", "sph_set_eos_ideal", "sph_set_eos_entropy", "sph_eos_eval",
+    "sph_autotune", "sph_set_eos_ideal", "sph_set_eos_entropy", "sph_eos_eval", "sph_download_fields",
 ]
 # fields a step reads or carries unchanged (SPH_STEP_INPUT_FIELDS): what SPH_UPLOAD_STEP_INPUTS copies
 STEP_INPUT_FIELDS = ["x", "y", "z", "vx", "vy", "vz", "mass", "smth", "eng", "ava", "ax", "ay", "az", "eng_dot",
                      "gx", "gy", "gz", "ent", "temp"]
+# fields a step writes (SPH_STEP_OUTPUT_FIELDS; mode 2 adds ent and temp)
+STEP_OUTPUT_FIELDS = [f for f in FIELDS if f not in ("mass", "ava", "ent", "temp")]
 EOS_QUANTITY = {"pressure": 0, "sound_speed": 1, "temperature": 2, "entropy": 3, "internal_energy": 4}
 ENTROPY_ABS_INT = 0
 ENTROPY_ABS_REAL = 1
@@ -105,6 +107,7 @@ def load() -> C.CDLL:
     L.sph_probe_peak.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double)]
     L.sph_morton_order_noalloc.argtypes = [P, P, P, C.c_int64, P, P, P]
     L.sph_download.argtypes = [P, P, C.c_int64, P, P]
+    L.sph_download_fields.argtypes = [P, P, C.c_int64, C.c_uint64, P, P]
     L.sph_prologue.argtypes = [P]
     L.sph_step.argtypes = [P, C.c_int]
     L.sph_get_time.argtypes = [P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int64)]
@@ -233,6 +236,16 @@ class Context:
         mats = np.empty(self.n, np.int32)
         self._check(self.L.sph_download(self.h, _ptr(out), out.shape[1], _ptr(ids), _ptr(mats)))
         return out, ids, mats
+
+    def download_fields(self, out: np.ndarray, names):
+        """copies the named fields (e.g. STEP_OUTPUT_FIELDS) into the rows of `out` (field-major,
+        upload order); the other rows are left as they are"""
+        mask = 0
+        for f in names:
+            mask |= 1 << FIELD[f]
+        assert out.shape[0] == NFIELD and out.flags["C_CONTIGUOUS"]
+        self._check(self.L.sph_download_fields(self.h, _ptr(out), out.shape[1], mask, None, None))
+        return out
 
     def prologue(self):
         self._check(self.L.sph_prologue(self.h))

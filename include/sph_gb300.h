@@ -215,6 +215,14 @@ int sph_upload(sph_ctx *ctx, int64_t n, const double *fields, int64_t ld, const 
                const int32_t *material, double time, double dt, int flags);
 /* Copies the state back in upload order. */
 int sph_download(sph_ctx *ctx, double *fields, int64_t ld, int64_t *id, int32_t *material);
+/* The same for the fields in field_mask only (bit f = field f; the other rows of `fields` are
+ * left as they are; id / material may be NULL).  A host that keeps its particles can read back
+ * SPH_STEP_OUTPUT_FIELDS after each step: every field a step writes. */
+int sph_download_fields(sph_ctx *ctx, double *fields, int64_t ld, uint64_t field_mask, int64_t *id,
+                        int32_t *material);
+#define SPH_STEP_OUTPUT_FIELDS (~(SPH_FIELD_BIT(SPH_MASS) | SPH_FIELD_BIT(SPH_AVA) | SPH_FIELD_BIT(SPH_ENT) | \
+                                  SPH_FIELD_BIT(SPH_TEMP)) & (SPH_FIELD_BIT(SPH_NFIELD) - 1))
+#define SPH_STEP_OUTPUT_FIELDS_MODE2 (SPH_STEP_OUTPUT_FIELDS | SPH_FIELD_BIT(SPH_ENT) | SPH_FIELD_BIT(SPH_TEMP))
 /* Forces of the current state and the first dt (main.cpp:92-105). */
 int sph_prologue(sph_ctx *ctx);
 /* n_steps iterations of the loop body of main.cpp:125-173.  In mode 2 each

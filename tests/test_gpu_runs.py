@@ -156,3 +156,24 @@ def test_upload_checks_masses_and_materials():
     ctx.prologue()
     ctx.step(1)
     ctx.close()
+
+
+def test_download_fields_copies_only_the_masked_rows():
+    from fdps_sph_gb300 import lib
+    F, ids, mats = _bodies()[1]
+    ctx = device_context(tillotson_materials(), precision=1)
+    ctx.upload(F, ids, mats)
+    ctx.prologue()
+    ctx.step(1)
+    full, _, _ = ctx.download()
+    part = np.full_like(full, -7.0)
+    ctx.download_fields(part, lib.STEP_OUTPUT_FIELDS)
+    for k, f in enumerate(lib.FIELDS):
+        if f in lib.STEP_OUTPUT_FIELDS:
+            assert np.array_equal(part[k], full[k]), f
+        else:
+            assert np.all(part[k] == -7.0), f
+    # what the step does not write is what was uploaded
+    for f in ("mass", "ava", "ent", "temp"):
+        assert np.array_equal(full[lib.FIELD[f]], F[lib.FIELD[f]]), f
+    ctx.close()
