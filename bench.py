@@ -228,9 +228,11 @@ def drift(d0, d1, steps):
 
 def run_e2e(ctx, F, ids, mats, steps, warmup=2):
     """upload (pinned host) -> one step -> download (pinned host), every step.  The upload copies
-    the fields the step reads or carries (SPH_UPLOAD_STEP_INPUTS); the download copies every
-    field the step writes (SPH_STEP_OUTPUT_FIELDS) into the host's block, whose other rows (mass,
-    AVa, entropy, temperature; ids and materials, in upload order) the step leaves unchanged.
+    the fields the step reads or carries (SPH_UPLOAD_STEP_INPUTS); every field the step writes
+    (SPH_STEP_OUTPUT_FIELDS) goes back into the host's block as soon as the step has written it
+    (sph_step_download, the copies overlapping the rest of the step); the block's other rows
+    (mass, AVa, entropy, temperature; ids and materials, in upload order) the step leaves
+    unchanged.
     `warmup` round trips run untimed first (the first ones capture the CUDA graphs of the new
     buffer layout)."""
     import torch
@@ -250,9 +252,8 @@ def run_e2e(ctx, F, ids, mats, steps, warmup=2):
     def round_trip():
         nonlocal t_now, dt
         ctx.upload(hostF, hid, hmat, time=t_now, dt=dt, forces_valid=True, inputs_only=True)
-        ctx.step(1)
+        ctx.step_download(hostF, outs)   # each field to the host as soon as the step has written it
         t_now, dt, _ = ctx.time()
-        ctx.download_fields(hostF, outs)
 
     for _ in range(warmup):
         round_trip()

@@ -77,6 +77,16 @@ __global__ void __launch_bounds__(256) k_check_block(int n, const double *__rest
     if (threadIdx.x == 0) part[blockIdx.x] = s[0];
 }
 
+// k_unpermute for the fields in `mask` only, into a block in upload order
+__global__ void k_unpermute_fields(const double *F, double *out, int64_t cap, int n, uint64_t mask,
+                                   const int32_t *slot, const int *prun, const int4 *info) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int dst = (info ? info[prun[k]].x : 0) + slot[k];
+    for (int f = 0; f < SPH_NFIELD; ++f)
+        if ((mask >> f) & 1) out[(int64_t)f * cap + dst] = F[(int64_t)f * cap + k];
+}
+
 __global__ void k_fill32(int32_t *a, int n, int v) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) a[i] = v;
@@ -143,9 +153,48 @@ int collect_timings(sph_ctx *ctx) {
     return SPH_OK;
 }
 
+}  // namespace
+
+// sph_step_download: the requested fields that the step has finished writing go to the host now,
+// on the copy stream, while the step goes on (the state is in key order in F after the sort;
+// nothing swaps the buffers again within the step)
+int dl_milestone(sph_ctx *ctx, uint64_t final_fields) {
+    const uint64_t send = ctx->dl_left & final_fields;
+    if (!ctx->dl_host || !send) return SPH_OK;
+    cudaEvent_t ev = ctx->dl_ev[ctx->dl_next++ & 7];
+    SPH_CUDA(ctx, cudaEventRecord(ev, ctx->stream));
+    SPH_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ev, 0));
+    const int n = (int)ctx->n;
+    k_unpermute_fields<<<sph_div_up(n, 256), 256, 0, ctx->copy_stream>>>(ctx->F, ctx->dl_buf, ctx->dl_cap, n, send,
+                                                                         ctx->slot, ctx->runs.prun, ctx->runs.info);
+    ++ctx->launches;
+    SPH_CUDA(ctx, cudaGetLastError());
+    for (int f = 0; f < SPH_NFIELD;) {
+        if (!((send >> f) & 1)) {
+            ++f;
+            continue;
+        }
+        int g = f;
+        while (g < SPH_NFIELD && ((send >> g) & 1)) ++g;
+        SPH_CUDA(ctx, cudaMemcpy2DAsync(ctx->dl_host + (int64_t)f * ctx->dl_ld, sizeof(double) * ctx->dl_ld,
+                                        ctx->dl_buf + (int64_t)f * ctx->dl_cap, sizeof(double) * ctx->dl_cap,
+                                        sizeof(double) * n, g - f, cudaMemcpyDeviceToHost, ctx->copy_stream));
+        f = g;
+    }
+    ctx->dl_left &= ~send;
+    return SPH_OK;
+}
+
+namespace {
+
+#define FB(f) (1ull << (f))
+
 // main.cpp:138-146 (positions fixed): sort + tree, density x n, EoS, derivative, hydro, gravity
 int compute_forces(sph_ctx *ctx) {
     SPH_TRY(sph_sort_and_build(ctx));   // marks SEG_SORT and SEG_TREE
+    // final from here on: positions, half-step velocities and energies (kick-drift, then sorted)
+    SPH_TRY(dl_milestone(ctx, FB(SPH_X) | FB(SPH_Y) | FB(SPH_Z) | FB(SPH_VHX) | FB(SPH_VHY) | FB(SPH_VHZ) |
+                                  FB(SPH_ENGHALF)));
     if (ctx->cfg.precision == SPH_PREC_MIXED) SPH_TRY(sph_pack_mixed(ctx));
     SPH_TRY(time_mark(ctx, SEG_NBR_PREP));
     if (ctx->cfg.precision == SPH_PREC_MIXED) {
@@ -161,13 +210,19 @@ int compute_forces(sph_ctx *ctx) {
     }
     SPH_TRY(sph_pass_eos(ctx));
     SPH_TRY(time_mark(ctx, SEG_EOS));
+    SPH_TRY(dl_milestone(ctx, FB(SPH_DENS) | FB(SPH_SMTH) | FB(SPH_PRES) | FB(SPH_SNDS)));
     SPH_TRY(sph_build_sph_lists(ctx, 2));   // gather and symmetric lists of the final h, one pass
     SPH_TRY(time_mark(ctx, SEG_DRVT_LIST));
     SPH_TRY(sph_pass_derivative(ctx, 0));
     SPH_TRY(time_mark(ctx, SEG_DRVT));
+    SPH_TRY(dl_milestone(ctx, FB(SPH_DIVV) | FB(SPH_ROTX) | FB(SPH_ROTY) | FB(SPH_ROTZ) | FB(SPH_GRADH) |
+                                  FB(SPH_BAL)));
     SPH_TRY(time_mark(ctx, SEG_HYDRO_LIST));
     SPH_TRY(sph_pass_hydro(ctx, 0));
     SPH_TRY(time_mark(ctx, SEG_HYDRO));
+    // the external damping (GI.h:458-465) adds to acc after this, at the end of the step
+    SPH_TRY(dl_milestone(ctx, FB(SPH_ENGDOT) | FB(SPH_DT) |
+                                  (ctx->cfg.ext_damp ? 0ull : FB(SPH_AX) | FB(SPH_AY) | FB(SPH_AZ))));
     if (ctx->cfg.self_gravity) {
         if (ctx->cfg.precision == SPH_PREC_MIXED) {
             SPH_TRY(time_mark(ctx, SEG_GRAV_LIST));   // no lists: the walk runs inside the force kernel
@@ -178,6 +233,7 @@ int compute_forces(sph_ctx *ctx) {
             SPH_TRY(sph_pass_gravity(ctx, 0));
         }
         SPH_TRY(time_mark(ctx, SEG_GRAV));
+        SPH_TRY(dl_milestone(ctx, FB(SPH_GX) | FB(SPH_GY) | FB(SPH_GZ) | FB(SPH_POT)));
     }
     ctx->have_forces = true;
     return SPH_OK;
@@ -417,7 +473,8 @@ int sph_ctx_create(const sph_config *cfg, sph_ctx **out) {
     ctx->device = c.device;
     if (cudaSetDevice(ctx->device) != cudaSuccess ||
         cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
         delete ctx;
         return SPH_ERR_CUDA;
@@ -427,6 +484,7 @@ int sph_ctx_create(const sph_config *cfg, sph_ctx **out) {
         ctx->mats_host[k].kind = -1;
     }
     for (int k = 0; k < 64; ++k) cudaEventCreate(&ctx->ev[k]);
+    for (int k = 0; k < 8; ++k) cudaEventCreateWithFlags(&ctx->dl_ev[k], cudaEventDisableTiming);
     cudaEventCreate(&ctx->ev_begin);
     cudaEventCreate(&ctx->ev_end);
     if (cudaMalloc((void **)&ctx->mats_dev, sizeof(ctx->mats_host)) != cudaSuccess ||
@@ -448,6 +506,7 @@ int sph_ctx_destroy(sph_ctx *ctx) {
     if (!ctx) return SPH_OK;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
     void *ptrs[] = {ctx->F, ctx->F2, ctx->id, ctx->id2, ctx->slot, ctx->slot2, ctx->mat, ctx->mat2, ctx->keys,
                     ctx->scratch_d, ctx->xh, ctx->xl, ctx->vhf, ctx->vlf, ctx->mats_dev,
                     ctx->tree.start, ctx->tree.count, ctx->tree.level, ctx->tree.first_child, ctx->tree.n_child,
@@ -461,7 +520,7 @@ int sph_ctx_destroy(sph_ctx *ctx) {
                     ctx->sup.units, ctx->tree.cinfo, ctx->sup.r2, ctx->sup.m, ctx->sup.vR, ctx->sup.cvR,
                     ctx->sup.umark, ctx->sup.uoff, ctx->sup.uidx, ctx->runs.prun, ctx->runs.prun2,
                     ctx->runs.tiles, ctx->runs.info, ctx->runs.dt_dev, ctx->runs.part, ctx->runs.out,
-                    ctx->runs.damp, ctx->sup.soff, ctx->sup.need, ctx->sup.uover, ctx->sup.npass};
+                    ctx->runs.damp, ctx->sup.soff, ctx->sup.need, ctx->sup.uover, ctx->sup.npass, ctx->dl_buf};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (void *p : ctx->table_allocs) cudaFree(p);
@@ -473,6 +532,9 @@ int sph_ctx_destroy(sph_ctx *ctx) {
         if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
     if (ctx->ev_begin) cudaEventDestroy(ctx->ev_begin);
     if (ctx->ev_end) cudaEventDestroy(ctx->ev_end);
+    for (int k = 0; k < 8; ++k)
+        if (ctx->dl_ev[k]) cudaEventDestroy(ctx->dl_ev[k]);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return SPH_OK;
@@ -850,6 +912,36 @@ int sph_step(sph_ctx *ctx, int n_steps) {
         if (fresh) SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));   // dt_step is the copy's source
     }
     ctx->have_forces = true;
+    return SPH_OK;
+}
+
+int sph_step_download(sph_ctx *ctx, double *fields, int64_t ld, uint64_t field_mask) {
+    if (!ctx) return SPH_ERR_ARG;
+    if (!ctx->uploaded) return sph_fail(ctx, SPH_ERR_STATE, "step before upload");
+    if ((field_mask && !fields) || ld < ctx->n) return sph_fail(ctx, SPH_ERR_ARG, "bad output block");
+    cudaSetDevice(ctx->device);
+    if (ctx->dl_cap < ctx->cap) {
+        if (ctx->dl_buf) cudaFree(ctx->dl_buf);
+        ctx->dl_buf = nullptr;
+        ctx->dl_cap = 0;
+        if (cudaMalloc((void **)&ctx->dl_buf, sizeof(double) * SPH_NFIELD * (size_t)ctx->cap) != cudaSuccess) {
+            cudaGetLastError();
+            return sph_fail(ctx, SPH_ERR_OOM, "download staging block");
+        }
+        ctx->dl_cap = ctx->cap;
+    }
+    // the copy stream must not run ahead into staging rows an earlier call is still reading
+    SPH_CUDA(ctx, cudaStreamSynchronize(ctx->copy_stream));
+    ctx->dl_host = fields;
+    ctx->dl_ld = ld;
+    ctx->dl_left = field_mask & ((1ull << SPH_NFIELD) - 1);
+    int rc = sph_step(ctx, 1);
+    if (rc == SPH_OK) rc = dl_milestone(ctx, ~0ull);   // what the end of the step wrote
+    ctx->dl_host = nullptr;
+    ctx->dl_left = 0;
+    const cudaError_t e = cudaStreamSynchronize(ctx->copy_stream);
+    if (rc != SPH_OK) return rc;
+    if (e != cudaSuccess) return sph_fail(ctx, SPH_ERR_CUDA, "download stream: %s", cudaGetErrorString(e));
     return SPH_OK;
 }
 

@@ -264,6 +264,16 @@ struct sph_ctx {
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
+    // sph_step_download: fields go to the host on their own stream as soon as the step has
+    // finished writing them (unpermuted into dl_buf first)
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t dl_ev[8] = {nullptr};
+    int dl_next = 0;
+    double *dl_buf = nullptr;      // [SPH_NFIELD][cap], upload order
+    int64_t dl_cap = 0;
+    double *dl_host = nullptr;     // the request: host block, its leading dimension, fields left
+    int64_t dl_ld = 0;
+    uint64_t dl_left = 0;
     std::string err;
 
     int64_t n = 0, cap = 0;
@@ -363,7 +373,8 @@ int sph_build_sph_lists(sph_ctx *ctx, int mode);
 int sph_density_from_superset(sph_ctx *ctx);
 int sph_density_fused(sph_ctx *ctx);     // mixed precision: all density passes of a step
 int sph_nbr_ensure_superset(sph_ctx *ctx);   // mixed precision: density pass without an exact list
-int time_mark(sph_ctx *ctx, int seg);      // event at the end of a timed segment (when timing is on)
+int time_mark(sph_ctx *ctx, int seg);
+int dl_milestone(sph_ctx *ctx, uint64_t final_fields);   // sph_step_download: send what is final      // event at the end of a timed segment (when timing is on)
 int sph_runs_layout(sph_ctx *ctx);        // offsets and tiles of the runs after a change of the run set
 int sph_run_reduce_dt(sph_ctx *ctx);      // per-run min dt into runs.dt_dev and runs.dt
 int sph_run_diag(sph_ctx *ctx, double *out);   // per-run conserved quantities, out[R * 8]

@@ -40,6 +40,7 @@ EXPORTS = [
     "sph_get_counters", "sph_probe_peak", "sph_morton_order_noalloc",
     "sph_add_run", "sph_remove_run", "sph_list_runs", "sph_run_info", "sph_download_run", "sph_run_diagnostics",
     "sph_autotune", "sph_set_eos_ideal", "sph_set_eos_entropy", "sph_eos_eval", "sph_download_fields",
+    "sph_step_download",
 ]
 # fields a step reads or carries unchanged (SPH_STEP_INPUT_FIELDS): what SPH_UPLOAD_STEP_INPUTS copies
 STEP_INPUT_FIELDS = ["x", "y", "z", "vx", "vy", "vz", "mass", "smth", "eng", "ava", "ax", "ay", "az", "eng_dot",
@@ -108,6 +109,7 @@ def load() -> C.CDLL:
     L.sph_morton_order_noalloc.argtypes = [P, P, P, C.c_int64, P, P, P]
     L.sph_download.argtypes = [P, P, C.c_int64, P, P]
     L.sph_download_fields.argtypes = [P, P, C.c_int64, C.c_uint64, P, P]
+    L.sph_step_download.argtypes = [P, P, C.c_int64, C.c_uint64]
     L.sph_prologue.argtypes = [P]
     L.sph_step.argtypes = [P, C.c_int]
     L.sph_get_time.argtypes = [P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int64)]
@@ -245,6 +247,16 @@ class Context:
             mask |= 1 << FIELD[f]
         assert out.shape[0] == NFIELD and out.flags["C_CONTIGUOUS"]
         self._check(self.L.sph_download_fields(self.h, _ptr(out), out.shape[1], mask, None, None))
+        return out
+
+    def step_download(self, out: np.ndarray, names):
+        """one step whose named fields reach `out` (field-major, upload order) as soon as the step
+        has written them (pin `out` for the copies to overlap the step)"""
+        mask = 0
+        for f in names:
+            mask |= 1 << FIELD[f]
+        assert out.shape[0] == NFIELD and out.flags["C_CONTIGUOUS"]
+        self._check(self.L.sph_step_download(self.h, _ptr(out), out.shape[1], mask))
         return out
 
     def prologue(self):

@@ -232,6 +232,11 @@ int sph_prologue(sph_ctx *ctx);
  * force.h:73-84); a lookup that is undefined in the reference or gives a
  * non-finite energy fails the step with SPH_ERR_NONFINITE. */
 int sph_step(sph_ctx *ctx, int n_steps);
+/* One sph_step that also copies the fields in field_mask (e.g. SPH_STEP_OUTPUT_FIELDS) into the
+ * host block `fields` (field-major, leading dimension ld, upload order), each as soon as the
+ * step has finished writing it, so the copies overlap the rest of the step (host memory should
+ * be pinned for that).  The other rows of `fields` are left as they are. */
+int sph_step_download(sph_ctx *ctx, double *fields, int64_t ld, uint64_t field_mask);
 int sph_get_time(const sph_ctx *ctx, double *time, double *dt, int64_t *step);
 
 /* Conserved quantities in FP64: E = sum m (u + v^2/2 + pot/2), P = sum m v,

@@ -177,3 +177,32 @@ def test_download_fields_copies_only_the_masked_rows():
     for f in ("mass", "ava", "ent", "temp"):
         assert np.array_equal(full[lib.FIELD[f]], F[lib.FIELD[f]]), f
     ctx.close()
+
+
+@pytest.mark.parametrize("prec,ext_damp,n_runs", [(1, False, 1), (0, True, 1), (1, False, 2)])
+def test_step_download_equals_step_then_download(prec, ext_damp, n_runs):
+    """fields streamed out during the step equal a download after it, bit for bit"""
+    from fdps_sph_gb300 import lib
+    bodies = _bodies()[:n_runs]
+    out = []
+    for streamed in (False, True):
+        ctx = device_context(tillotson_materials(), precision=prec, ext_damp=int(ext_damp))
+        if n_runs == 1:
+            ctx.upload(*bodies[0])
+            ctx.prologue()
+        else:
+            for b in bodies:
+                ctx.add_run(*b)
+            ctx.step(1)   # the runs' prologue
+        ctx.step(1)
+        n = ctx.n_particles()
+        blk = np.full((lib.NFIELD, n), -3.0)
+        if streamed:
+            ctx.step_download(blk, lib.STEP_OUTPUT_FIELDS)
+        else:
+            ctx.step(1)
+            ctx.download_fields(blk, lib.STEP_OUTPUT_FIELDS)
+        out.append(blk)
+        ctx.close()
+    assert np.array_equal(out[0], out[1])
+    assert np.all(out[1][lib.FIELD["mass"]] == -3.0)
