@@ -678,25 +678,20 @@ __global__ void k_moments(int l, const int *meta, const double *x, const double 
         float hm = 0.0f;
         const int nch = n_child[c];
         if (nch == 0) {
+            // the box and hmax in FP32: rounding down (up) is monotone, so the min (max) of the
+            // rounded values is the rounded min (max), without FP64 comparisons
             const int s = start[c], e = s + count[c];
-            double dlo[3] = {INFINITY, INFINITY, INFINITY}, dhi[3] = {-INFINITY, -INFINITY, -INFINITY};
-            double dh = 0.0;
             for (int j = s; j < e; ++j) {
                 const double mj = m[j], xj = x[j], yj = y[j], zj = z[j];
                 ms = __dadd_rn(ms, mj);
                 mx = __dadd_rn(mx, __dmul_rn(mj, xj));
                 my = __dadd_rn(my, __dmul_rn(mj, yj));
                 mz = __dadd_rn(mz, __dmul_rn(mj, zj));
-                dlo[0] = fmin(dlo[0], xj); dhi[0] = fmax(dhi[0], xj);
-                dlo[1] = fmin(dlo[1], yj); dhi[1] = fmax(dhi[1], yj);
-                dlo[2] = fmin(dlo[2], zj); dhi[2] = fmax(dhi[2], zj);
-                dh = fmax(dh, h[j]);
+                lo[0] = fminf(lo[0], __double2float_rd(xj)); hi[0] = fmaxf(hi[0], __double2float_ru(xj));
+                lo[1] = fminf(lo[1], __double2float_rd(yj)); hi[1] = fmaxf(hi[1], __double2float_ru(yj));
+                lo[2] = fminf(lo[2], __double2float_rd(zj)); hi[2] = fmaxf(hi[2], __double2float_ru(zj));
+                hm = fmaxf(hm, __double2float_ru(h[j]));
             }
-            for (int d = 0; d < 3; ++d) {
-                lo[d] = __double2float_rd(dlo[d]);
-                hi[d] = __double2float_ru(dhi[d]);
-            }
-            hm = __double2float_ru(dh);
         } else {
             const int f = first_child[c];
             for (int k = 0; k < nch; ++k) {
@@ -743,9 +738,7 @@ __global__ void k_hmax(int l, const int *meta, const double *h, const int *start
         float hm = 0.0f;
         const int nch = n_child[c];
         if (nch == 0) {
-            double dh = 0.0;
-            for (int j = start[c]; j < start[c] + count[c]; ++j) dh = fmax(dh, h[j]);
-            hm = __double2float_ru(dh);
+            for (int j = start[c]; j < start[c] + count[c]; ++j) hm = fmaxf(hm, __double2float_ru(h[j]));
         } else {
             for (int k = 0; k < nch; ++k) hm = fmaxf(hm, bhi[first_child[c] + k].w);
         }
