@@ -153,7 +153,7 @@ WORKLOADS = {"1m": "two-layer impact (90% target, 10% impactor, iron/dunite, 30 
              "4m": "three-layer impact (90% target, 10% impactor, iron/dunite/granite crust 5%, 45 deg, 1.0 v_esc)"}
 
 
-def run_gpu(F, ids, mats, materials, precision, steps, warmup, device, theta=0.5, mode=1):
+def run_gpu(F, ids, mats, materials, precision, steps, warmup, device, theta=0.5, mode=1, dist=None):
     from fdps_sph_gb300 import lib
     ctx = lib.Context(precision=precision, device=device, theta=theta, mode=mode)
     for k, m in enumerate(materials):
@@ -180,6 +180,7 @@ def run_gpu(F, ids, mats, materials, precision, steps, warmup, device, theta=0.5
     # the timed steps (the octree build replays as a CUDA graph); events around the steps only
     c0 = ctx.counters()["launches"]
     d0 = ctx.diagnostics()
+    replica_barrier(dist)
     with ClockSampler(device) as clk:
         ms = ctx.step_timed(steps)
     d1 = ctx.diagnostics()
@@ -226,7 +227,7 @@ def drift(d0, d1, steps):
     return {"energy_rel_per_step": e, "angmom_rel_per_step": lv}
 
 
-def run_e2e(ctx, F, ids, mats, steps, warmup=2):
+def run_e2e(ctx, F, ids, mats, steps, warmup=2, dist=None):
     """upload (pinned host) -> one step -> download (pinned host), every step.  The upload copies
     the fields the step reads or carries (SPH_UPLOAD_STEP_INPUTS); every field the step writes
     (SPH_STEP_OUTPUT_FIELDS) goes back into the host's block as soon as the step has written it
@@ -257,6 +258,7 @@ def run_e2e(ctx, F, ids, mats, steps, warmup=2):
 
     for _ in range(warmup):
         round_trip()
+    replica_barrier(dist)
     t0 = time.perf_counter()
     for _ in range(steps):
         round_trip()
@@ -289,9 +291,32 @@ def dist_init(n_gpus):
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", n_gpus))
     local = int(os.environ.get("LOCAL_RANK", rank))
-    torch.cuda.set_device(local)
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
     dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     return rank, world, dist
+
+
+def replica_barrier(dist):
+    """every replica enters its timed steps together (a no-op for one process)"""
+    if dist is not None:
+        dist.barrier()
+
+
+def replica_max(x, dist, device=None):
+    """the slowest replica's time: the job ends when the last replica does (x for one process)"""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
+
+
+def replica_throughput(world, n, ms_per_step):
+    """whole-job particle-steps/s: every replica advances its own n particles per step"""
+    return world * n / (ms_per_step * 1e-3)
 
 
 TPI = 0
@@ -343,17 +368,17 @@ def main():
     precisions = ["mixed"] if a.no_fp64 else ["mixed", "fp64"]
     for prec in precisions:
         ctx, ms, seg, cnt, launches, clocks, dr, tune, first = run_gpu(F, ids, mats, materials, prec, a.steps,
-                                                                       a.warmup, device, a.theta, a.mode)
-        e2e = run_e2e(ctx, F, ids, mats, a.e2e_steps) if prec == "mixed" else None
+                                                                       a.warmup, device, a.theta, a.mode,
+                                                                       dist if prec == "mixed" else None)
+        e2e = run_e2e(ctx, F, ids, mats, a.e2e_steps, dist=dist) if prec == "mixed" else None
         results[prec] = dict(ms=ms, seg=seg, cnt=cnt, launches=launches, clocks=clocks, e2e=e2e, drift=dr, tune=tune,
                              first=first)
         ctx.close()
 
-    if dist is not None:
-        t = torch.tensor([results["mixed"]["ms"]], dtype=torch.float64, device=f"cuda:{device}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        results["mixed"]["ms"] = float(t.item())
-        dist.barrier()
+    results["mixed"]["ms"] = replica_max(results["mixed"]["ms"], dist, f"cuda:{device}")
+    if results["mixed"]["e2e"] is not None:
+        el, h2d, d2h = results["mixed"]["e2e"]
+        results["mixed"]["e2e"] = (replica_max(el, dist, f"cuda:{device}"), h2d, d2h)
     if rank != 0:
         return
 
@@ -366,7 +391,7 @@ def main():
         peaks = {"hbm_gbs": 6800.0}   # the profiling recipe's fallback
     mixed = results["mixed"]
     ms_step = mixed["ms"] / a.steps
-    value = world * n / (ms_step * 1e-3)
+    value = replica_throughput(world, n, ms_step)
 
     # algorithmic work of each segment of one step: flops on the FP32 pipe
     # for the pair kernels, compulsory HBM bytes for the list / tree / streaming kernels
