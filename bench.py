@@ -53,11 +53,12 @@ if os.path.exists(_tf):
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=1_000_000, help="total particles (default: the 1M workload)")
     ap.add_argument("--cpu-n", type=int, default=100_000, help="particles of the bounded CPU sample")
+    ap.add_argument("--cpu-steps", type=int, default=10, help="timed steps of the bounded CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
@@ -75,34 +76,50 @@ def parse():
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks / throttle reasons sampled during the timed region: sampling is running
+    (its first line read) before the region starts, and only the lines that arrive between the
+    start and one interval after the end are summarised."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index):
+    def __init__(self, gpu_index, interval_ms=20):
         self.gpu = gpu_index
+        self.interval = interval_ms
         self.proc = None
         self.lines = []
+        self.t0 = self.t1 = None
+
+    def _start(self, interval_ms):
+        self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits", "-lms", str(interval_ms)],
+                                     stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+        deadline = time.perf_counter() + 5.0
+        while not self.lines and self.proc.poll() is None and time.perf_counter() < deadline:
+            time.sleep(0.005)
+        return bool(self.lines)
 
     def __enter__(self):
         try:
-            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
-                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.t = threading.Thread(target=self._read, daemon=True)
-            self.t.start()
+            if not self._start(self.interval):   # an interval nvidia-smi refuses: its default-style one
+                self.interval = 200
+                self._start(self.interval)
         except Exception:
             self.proc = None
+        self.t0 = time.perf_counter()
         return self
 
     def _read(self):
         for ln in self.proc.stdout:
-            self.lines.append(ln.strip())
+            self.lines.append((time.perf_counter(), ln.strip()))
 
     def __exit__(self, *a):
+        self.t1 = time.perf_counter()
         if self.proc:
+            time.sleep(1.5 * self.interval * 1e-3)   # the sample that closes the region
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -112,7 +129,10 @@ class ClockSampler:
     def summary(self):
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        lim = (self.t1 or time.perf_counter()) + 1.5 * self.interval * 1e-3
+        for t, ln in self.lines:
+            if self.t0 is None or t < self.t0 or t > lim:
+                continue
             p = [x.strip() for x in ln.split(",")]
             if len(p) < 9:
                 continue
@@ -127,7 +147,7 @@ class ClockSampler:
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "interval_ms": self.interval}
 
 
 def workload(n_total, seed=2024, config="1m", mode=1):
@@ -479,10 +499,10 @@ def main():
     if not a.no_batch and world == 1:
         out.update(batch_and_serving(a, device))
     if not a.no_cpu:
-        v_cpu, el_cpu, cores = cpu_sample(a.cpu_n, 1)
+        v_cpu, el_cpu, cores = cpu_sample(a.cpu_n, a.cpu_steps)
         out["cpu_baseline"] = {"value": v_cpu, "unit": "particle-steps/s", "cores": cores, "kind": "port",
                                "sample": f"oracle restatement (OpenMP) on the same geometry at {a.cpu_n} particles, "
-                                         f"1 step after the prologue ({el_cpu:.1f} s)"}
+                                         f"{a.cpu_steps} steps after the prologue ({el_cpu:.1f} s on {cores} threads)"}
         for k in ("batch", "serving"):
             if k in out:
                 out[k]["vs_cpu_baseline"] = out[k]["value"] / v_cpu

@@ -56,25 +56,38 @@ __global__ void k_unpermute(const double *F, double *F2, int64_t cap, int k0, in
 constexpr int CHECK_BLOCKS = 256;
 __global__ void __launch_bounds__(256) k_check_block(int n, const double *__restrict__ mass,
                                                      const int32_t *__restrict__ mat,
-                                                     const DevMaterial *__restrict__ mats, double *part, int *bad) {
+                                                     const DevMaterial *__restrict__ mats, double *part, int *bad,
+                                                     unsigned long long *mmax) {
     __shared__ double s[256];
+    __shared__ unsigned long long s_mx[256];   // positive doubles order like their bit patterns
+    unsigned long long mx = 0;
     const int chunk = (n + CHECK_BLOCKS - 1) / CHECK_BLOCKS;
     const int lo = blockIdx.x * chunk, hi = min(n, lo + chunk);
     double acc = 0.0;
     for (int i = lo + (int)threadIdx.x; i < hi; i += blockDim.x) {
         const double m = mass[i];
-        if (!(m > 0.0) || !isfinite(m)) atomicMin(&bad[0], i);
+        if (!(m > 0.0) || !isfinite(m))
+            atomicMin(&bad[0], i);
+        else
+            mx = max(mx, (unsigned long long)__double_as_longlong(m));
         const int q = mat[i];
         if (q < 0 || q >= MAX_MATERIALS || mats[q].kind < 0) atomicMin(&bad[1], i);
         acc += m;
     }
     s[threadIdx.x] = acc;
+    s_mx[threadIdx.x] = mx;
     __syncthreads();
     for (int w = 128; w > 0; w >>= 1) {
-        if ((int)threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+        if ((int)threadIdx.x < w) {
+            s[threadIdx.x] += s[threadIdx.x + w];
+            s_mx[threadIdx.x] = max(s_mx[threadIdx.x], s_mx[threadIdx.x + w]);
+        }
         __syncthreads();
     }
-    if (threadIdx.x == 0) part[blockIdx.x] = s[0];
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = s[0];
+        atomicMax(mmax, s_mx[0]);
+    }
 }
 
 // k_unpermute for the fields in `mask` only, into a block in upload order
@@ -265,6 +278,7 @@ int sph_runs_layout(sph_ctx *ctx) {
         SPH_TRY(dalloc(ctx, &R.dt_dev, c));
         SPH_TRY(dalloc(ctx, &R.out, 8 * (int64_t)c));
         SPH_TRY(dalloc(ctx, &R.damp, c));
+        SPH_TRY(dalloc(ctx, &R.fixd, c));
         R.cap_R = c;
     }
     if (T > R.cap_T) {
@@ -273,8 +287,15 @@ int sph_runs_layout(sph_ctx *ctx) {
         SPH_TRY(dalloc(ctx, &R.part, 8 * (int64_t)c));
         R.cap_T = c;
     }
+    std::vector<int> fixd(R.R);
+    R.fix_split = true;
+    for (int r = 0; r < R.R; ++r) {
+        fixd[r] = ctx->mexp - R.mexp[r];
+        R.fix_split = R.fix_split && std::ldexp(R.mmax[r], R.mexp[r]) <= 15.0;
+    }
     if (R.R > 0) {
         SPH_CUDA(ctx, cudaMemcpyAsync(R.info, info.data(), sizeof(int4) * R.R, cudaMemcpyHostToDevice, ctx->stream));
+        SPH_CUDA(ctx, cudaMemcpyAsync(R.fixd, fixd.data(), sizeof(int) * R.R, cudaMemcpyHostToDevice, ctx->stream));
         SPH_CUDA(ctx, cudaMemcpyAsync(R.dt_dev, R.dt.data(), sizeof(double) * R.R, cudaMemcpyHostToDevice, ctx->stream));
     }
     if (T > 0)
@@ -378,14 +399,16 @@ int append_run(sph_ctx *ctx, int64_t n, const double *fields, int64_t ld, const 
         SPH_CUDA(ctx, cudaMemsetAsync(ctx->mat + o, 0, sizeof(int32_t) * n, ctx->stream));
     }
     // masses and materials checked on the device, the mass summed in a fixed order
+    // (scratch: CHECK_BLOCKS partial sums, the two first bad indices, the largest mass's bits)
     double *part = ctx->scratch_d;
     int *bad = (int *)(ctx->scratch_d + CHECK_BLOCKS);
-    const int big[2] = {INT_MAX, INT_MAX};
+    unsigned long long *mmax = (unsigned long long *)(ctx->scratch_d + CHECK_BLOCKS + 1);
+    const int big[4] = {INT_MAX, INT_MAX, 0, 0};
     std::memcpy(ctx->host_scalars + CHECK_BLOCKS, big, sizeof(big));
     SPH_CUDA(ctx, cudaMemcpyAsync(bad, ctx->host_scalars + CHECK_BLOCKS, sizeof(big), cudaMemcpyHostToDevice,
                                   ctx->stream));
     k_check_block<<<CHECK_BLOCKS, 256, 0, ctx->stream>>>((int)n, ctx->F + (int64_t)SPH_MASS * c + o, ctx->mat + o,
-                                                         ctx->mats_dev, part, bad); ++ctx->launches;
+                                                         ctx->mats_dev, part, bad, mmax); ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
     SPH_CUDA(ctx, cudaMemcpyAsync(ctx->host_scalars, part, sizeof(double) * CHECK_BLOCKS + sizeof(big),
                                   cudaMemcpyDeviceToHost, ctx->stream));
@@ -406,7 +429,19 @@ int append_run(sph_ctx *ctx, int64_t n, const double *fields, int64_t ld, const 
     double msum = 0.0;
     for (int b = 0; b < CHECK_BLOCKS; ++b) msum += ctx->host_scalars[b];
     // power of two close to 1 / mean mass (exact rescaling of the FP32 mass copies), fixed by the first run
-    if (o == 0) ctx->mscale = std::ldexp(1.0, -(int)std::lround(std::log2(msum / (double)n)));
+    // the run's own mass scale, a power of two close to 1 / its mean mass; the context's is its
+    // first run's (exact rescaling of the FP32 mass copies).  The density sums of a run are
+    // rounded on its own scale, so a run gives the same sums alone and in any mix.
+    const int mexp = -(int)std::lround(std::log2(msum / (double)n));
+    if (o == 0) {
+        ctx->mexp = mexp;
+        ctx->mscale = std::ldexp(1.0, mexp);
+    } else if (std::abs(mexp - ctx->mexp) > 60) {
+        return sph_fail(ctx, SPH_ERR_ARG, "the run's mean particle mass is 2^%d times the first run's (at most 2^60)",
+                        ctx->mexp - mexp);
+    }
+    double mmax_h;
+    std::memcpy(&mmax_h, ctx->host_scalars + CHECK_BLOCKS + 1, sizeof(mmax_h));
     if (flags & SPH_UPLOAD_INIT_SMTH) {
         SPH_TRY(sph_init_smth(ctx, o, n));
         SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -418,6 +453,8 @@ int append_run(sph_ctx *ctx, int64_t n, const double *fields, int64_t ld, const 
     R.steps.push_back(0);
     R.handle.push_back(R.next_handle++);
     R.fresh.push_back(forces ? 0 : 1);
+    R.mexp.push_back(mexp);
+    R.mmax.push_back(mmax_h);
     R.R += 1;
     ctx->n = o + n;
     if (handle) *handle = R.handle.back();
@@ -520,7 +557,7 @@ int sph_ctx_destroy(sph_ctx *ctx) {
                     ctx->sup.units, ctx->tree.cinfo, ctx->sup.r2, ctx->sup.m, ctx->sup.vR, ctx->sup.cvR,
                     ctx->sup.umark, ctx->sup.uoff, ctx->sup.uidx, ctx->runs.prun, ctx->runs.prun2,
                     ctx->runs.tiles, ctx->runs.info, ctx->runs.dt_dev, ctx->runs.part, ctx->runs.out,
-                    ctx->runs.damp, ctx->sup.soff, ctx->sup.need, ctx->sup.uover, ctx->sup.npass, ctx->dl_buf};
+                    ctx->runs.damp, ctx->runs.fixd, ctx->sup.soff, ctx->sup.need, ctx->sup.uover, ctx->sup.npass, ctx->dl_buf};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (void *p : ctx->table_allocs) cudaFree(p);
@@ -708,6 +745,8 @@ int sph_upload(sph_ctx *ctx, int64_t n, const double *fields, int64_t ld, const 
     R.steps.clear();
     R.handle.clear();
     R.fresh.clear();
+    R.mexp.clear();
+    R.mmax.clear();
     ctx->n = 0;
     ctx->uploaded = false;
     ctx->batch = false;
@@ -757,6 +796,8 @@ int sph_remove_run(sph_ctx *ctx, int64_t handle) {
     R.steps.erase(R.steps.begin() + r);
     R.handle.erase(R.handle.begin() + r);
     R.fresh.erase(R.fresh.begin() + r);
+    R.mexp.erase(R.mexp.begin() + r);
+    R.mmax.erase(R.mmax.begin() + r);
     R.R -= 1;
     ctx->n = n_new;
     if (R.R == 0) ctx->uploaded = false;

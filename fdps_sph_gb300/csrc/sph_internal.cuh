@@ -80,6 +80,27 @@ __device__ __forceinline__ int64_t row_seg(const RowMap &m, int64_t i, int seg, 
     return (*len > 0 && m.soff) ? m.main + m.soff[i] : 0;
 }
 
+// particle i's row over its logical positions 0 .. c - 1: positions below K sit in the row
+// block, the others in the spill range.  Kernels that split a row between threads or flush
+// partial sums every so many entries count positions on this view, so how the entries group
+// does not depend on K (which follows the row lengths of every run in the context).  K is a
+// multiple of 8, so an aligned pair or quad of positions never straddles the two parts.
+struct RowView {
+    const int *blk, *spill;   // spill is offset by -K: spill[k] for k >= K
+    int K, c;
+    __device__ __forceinline__ const int *at(int k) const { return (k < K ? blk : spill) + k; }
+};
+
+__device__ __forceinline__ RowView row_view(const int *nbr, const RowMap &m, int64_t i, int c) {
+    RowView v;
+    v.K = m.K;
+    v.blk = nbr + i * m.K;
+    const bool sp = c > m.K && m.soff;
+    v.spill = sp ? nbr + m.main + m.soff[i] - m.K : v.blk;
+    v.c = (c > m.K && !sp) ? m.K : c;
+    return v;
+}
+
 __device__ __forceinline__ int row_spill_cap(const RowMap &m, int64_t i) {
     return m.soff ? m.soff[i + 1] - m.soff[i] : 0;
 }
@@ -235,6 +256,9 @@ struct Runs {
     std::vector<double> time, dt;           // host copies; dt of the coming step
     std::vector<int64_t> steps, handle;
     std::vector<int> fresh;                 // joined since the last step: its first step is its prologue
+    std::vector<int> mexp;                  // the run's own mass scale 2^mexp (~ 1 / its mean mass)
+    std::vector<double> mmax;               // the run's largest particle mass
+    bool fix_split = true;                  // every run's largest mass x its own scale <= 15
     int T = 0;                              // tiles over all runs
     int cap_R = 0, cap_T = 0;
     int4 *tiles = nullptr;                  // device [T]: start, length, histogram base, tiles of its run
@@ -243,6 +267,7 @@ struct Runs {
     double *part = nullptr;                 // device [T * 8]: per-tile partials
     double *out = nullptr;                  // device [R * 8]: per-run results
     unsigned char *damp = nullptr;          // device [R]: external damping applies
+    int *fixd = nullptr;                    // device [R]: log2 of the context's mass scale over the run's
     int *prun = nullptr, *prun2 = nullptr;  // device [cap]: run of each particle (permuted with it)
     int64_t next_handle = 1;
 };
@@ -301,6 +326,7 @@ struct sph_ctx {
     sph::Runs runs;
 
     double mscale = 1.0;   // power of two ~ 1 / particle mass, keeps FP32 pair sums near unity
+    int mexp = 0;          // mscale = 2^mexp, set by the first run of a run set
 
     int64_t step = 0;          // steps taken by sph_step (all runs)
     bool uploaded = false;

@@ -24,6 +24,7 @@
 #include <algorithm>
 #include <cstring>
 
+#include "sph_fixpoint.cuh"
 #include "sph_internal.cuh"
 
 namespace sph {
@@ -676,20 +677,33 @@ k_density_sup32(int n, const int *__restrict__ sup, const float *__restrict__ su
 // rows being too many for the passes to find them in L1 or L2); a particle whose new h
 // leaves the skin stops after that pass, to go on once its row is walked again.  Each term
 // m_j W_ij is rounded to a multiple of 2^-40 and summed as an integer, so the sum depends on
-// neither the order of the terms nor where non-members sit in the row.
+// neither the order of the terms nor where non-members sit in the row.  The multiple is taken on
+// the particle's run's own mass scale (the terms carry the context's, 2^fixd[run] times the
+// run's: a power of two), so a run's sums are the same alone and in any mix of runs.  SPLIT:
+// every run's masses on its own scale are at most 15, so each term is at most 16 and takes
+// sph_fix40_add (FP32 / integer pipes) instead of __float2ll_rn (FP64 pipe); both give the same
+// integers.
 constexpr int DT = 2;
-constexpr float FIX_SCALE = 1099511627776.0f;   // 2^40
+template <bool SPLIT>
 __global__ void __launch_bounds__(128)
 k_density_fused32(int n, int n_pass, const int *__restrict__ sup, const float *__restrict__ sup_r2,
                   const float *__restrict__ sup_m, const int *__restrict__ scnt, RowMap rm,
                   const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
                   const double *__restrict__ m, double *__restrict__ h, const double *__restrict__ hsup,
-                  double *__restrict__ dens, float dscale, int *__restrict__ npass, int *n_stopped) {
+                  double *__restrict__ dens, float dscale, int *__restrict__ npass, int *n_stopped,
+                  const int *__restrict__ prun, const int *__restrict__ fixd) {
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = gt / DT, sub = gt % DT;
     if (i >= n) return;   // whole groups leave together
     int p = npass[i];
     if (p >= n_pass) return;
+    // the fixed-point grid 2^(fd - 40) on the context's scale is 2^-40 on the run's
+    // (powers of two written as bit patterns: exponent fields moved by fd, |fd| <= 60)
+    const int fd = fixd[prun[i]];
+    const unsigned b1 = SPH_FIX_B1 + ((unsigned)fd << 23), b2 = SPH_FIX_B2 + ((unsigned)fd << 23);
+    const float c1 = __uint_as_float(b1), c2 = __uint_as_float(b2);
+    const float to_fix = __uint_as_float((unsigned)(127 + 40 - fd) << 23);                         // 2^(40 - fd)
+    const double from_fix = __longlong_as_double((long long)(1023 + fd - 40) << 52);               // 2^(fd - 40)
     const unsigned gm = __activemask();
     double hi = h[i];
     const double hs = hsup[i], xi = x[i], yi = y[i], zi = z[i], mi = m[i];
@@ -702,12 +716,18 @@ k_density_fused32(int n, int n_pass, const int *__restrict__ sup, const float *_
         const float invH = 1.0f / (float)Hi;
         const float lo_b = H2i * (1.0f - 1.9073486328125e-06f), hi_b = H2i * (1.0f + 1.9073486328125e-06f);
         long long acc = 0;
+        unsigned aH = 0, aL = 0;   // SPLIT: 32-bit sums of at most 64 x 4 terms
+        int it = 0;
         for (int seg = 0; seg < 2; ++seg) {
             int c;
             const int64_t b = row_seg(rm, i, seg, c_all, &c);
             if (c <= 0) break;
             const float *rrow = sup_r2 + b, *mrow = sup_m + b;
             for (int k = 4 * sub; k < c; k += 4 * DT) {
+                if (SPLIT && (++it & (SPH_FIX_TERMS / 4 - 1)) == 0) {
+                    acc += sph_fix40_value(aH, aL);
+                    aH = aL = 0;
+                }
                 const float4 r4 = *reinterpret_cast<const float4 *>(rrow + k);
                 const float4 m4 = *reinterpret_cast<const float4 *>(mrow + k);
                 const float rr[4] = {r4.x, r4.y, r4.z, r4.w}, mj[4] = {m4.x, m4.y, m4.z, m4.w};
@@ -722,14 +742,18 @@ k_density_fused32(int n, int n_pass, const int *__restrict__ sup, const float *_
                     const float q = fmaxf(1.0f - s_, 0.0f);
                     const float q2 = q * q, q4 = q2 * q2;
                     const float term = mj[u] * ((1.0f + s_ * (8.0f + s_ * (25.0f + s_ * 32.0f))) * (q4 * q4));
-                    acc += __float2ll_rn(term * FIX_SCALE);
+                    if (SPLIT)
+                        sph_fix40_add(term, aH, aL, c1, c2, b1, b2);
+                    else
+                        acc += __float2ll_rn(term * to_fix);
                 }
             }
         }
+        if (SPLIT) acc += sph_fix40_value(aH, aL);
 #pragma unroll
         for (int o = DT / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(gm, acc, o, DT);
         double rho, hn;
-        density_tail32((float)((double)acc * (1.0 / 1099511627776.0)), invH, dscale, mi, &rho, &hn);
+        density_tail32((float)((double)acc * from_fix), invH, dscale, mi, &rho, &hn);
         hi = hn;
         if (sub == 0) {
             dens[i] = rho;
@@ -1087,11 +1111,12 @@ int sph_density_fused(sph_ctx *ctx) {
         SPH_TRY(ensure_superset(ctx));
         SPH_TRY(time_mark(ctx, SEG_DENS_LIST));
         SPH_CUDA(ctx, cudaMemsetAsync(stopped, 0, sizeof(int), ctx->stream));
-        k_density_fused32<<<sph_div_up((int64_t)n * DT, 128), 128, 0, ctx->stream>>>(
+        auto kd = ctx->runs.fix_split ? k_density_fused32<true> : k_density_fused32<false>;
+        kd<<<sph_div_up((int64_t)n * DT, 128), 128, 0, ctx->stream>>>(
             n, np, S.nbr, S.r2, S.m, S.cnt, S.map(), FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap),
             FLD(ctx->F, SPH_Z, cap), FLD(ctx->F, SPH_MASS, cap), FLD(ctx->F, SPH_SMTH, cap), S.hsup,
             FLD(ctx->F, SPH_DENS, cap), (float)(1365.0 / 64.0 / (3.141592653589793 * ctx->mscale)), S.npass,
-            stopped);
+            stopped, ctx->runs.prun, ctx->runs.fixd);
         ++ctx->launches;
         SPH_CUDA(ctx, cudaGetLastError());
         SPH_TRY(time_mark(ctx, SEG_DENS));

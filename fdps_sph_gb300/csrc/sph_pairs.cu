@@ -283,10 +283,9 @@ __global__ void __launch_bounds__(PT) k_density32(int n, const float4 *__restric
     const float invH = 1.0f / (float)H;
     float acc_h = 0.0f, acc_l = 0.0f;
     float part = 0.0f;
-    for (int seg = 0, c; seg < 2; ++seg) {
-    const int *row = nbr + row_seg(rm, i, seg, cnt[i], &c);
-    for (int k = 0; k < c; ++k) {
-        const int j = row[k];
+    const RowView row = row_view(nbr, rm, i, cnt[i]);
+    for (int k = 0; k < row.c; ++k) {
+        const int j = *row.at(k);
         const float4 qh = xh[j], ql = xl[j];
         const float dx = df_diff(qh.x, ql.x, pih.x, pil.x);
         const float dy = df_diff(qh.y, ql.y, pih.y, pil.y);
@@ -299,7 +298,6 @@ __global__ void __launch_bounds__(PT) k_density32(int n, const float4 *__restric
             df_add(acc_h, acc_l, part);
             part = 0.0f;
         }
-    }
     }
     df_add(acc_h, acc_l, part);
     density_tail32(acc_h + acc_l, invH, dscale, m[i], dens + i, h + i);
@@ -361,11 +359,11 @@ __global__ void __launch_bounds__(PT) k_drvt32(int n, DrvtArgs32 a) {
     // kernel normalisation folded out of the pair sums and applied once at the end
     float Dh[5] = {0, 0, 0, 0, 0}, Dl[5] = {0, 0, 0, 0, 0};
     float P[5] = {0, 0, 0, 0, 0};
-    for (int seg = 0, c; seg < 2; ++seg) {
-    const int *row = a.nbr + row_seg(a.rm, i, seg, a.cnt[i], &c);
+    const RowView row = row_view(a.nbr, a.rm, i, a.cnt[i]);
+    const int c = row.c;
     int k = 2 * sub, it = 0;
     for (; k + 2 <= c; k += 2 * TPI) {
-        const int2 jp = *reinterpret_cast<const int2 *>(row + k);
+        const int2 jp = *reinterpret_cast<const int2 *>(row.at(k));
         const int j0 = jp.x, j1 = jp.y;
         const float4 qh0 = a.xh[j0], ql0 = a.xl[j0], uh0 = a.vh[j0], ul0 = a.vl[j0];
         const float4 qh1 = a.xh[j1], ql1 = a.xl[j1], uh1 = a.vh[j1], ul1 = a.vl[j1];
@@ -380,9 +378,8 @@ __global__ void __launch_bounds__(PT) k_drvt32(int n, DrvtArgs32 a) {
         }
     }
     if (k < c) {
-        const int j = row[k];
+        const int j = *row.at(k);
         drvt_pair32(pih, pil, vih, vil, a.xh[j], a.xl[j], a.vh[j], a.vl[j], invH, Hf, ceps, P);
-    }
     }
     // per-particle tail of force.h:70-76 in FP32
     const float sc = a.kscale * (invH * invH * invH);
@@ -481,11 +478,11 @@ __global__ void __launch_bounds__(PT) k_hydro32(int n, HydroArgs32 a) {
     float Dh[4] = {0, 0, 0, 0}, Dl[4] = {0, 0, 0, 0};
     float P[4] = {0, 0, 0, 0};
     float vmax = 0.0f;
-    for (int seg = 0, c; seg < 2; ++seg) {
-    const int *row = a.nbr + row_seg(a.rm, i, seg, a.cnt[i], &c);
+    const RowView row = row_view(a.nbr, a.rm, i, a.cnt[i]);
+    const int c = row.c;
     int k = 2 * sub, it = 0;
     for (; k + 2 <= c; k += 2 * TPI) {
-        const int2 jp = *reinterpret_cast<const int2 *>(row + k);
+        const int2 jp = *reinterpret_cast<const int2 *>(row.at(k));
         const int j0 = jp.x, j1 = jp.y;
         const HydroJ32 J0 = load_hydro_j(a, j0), J1 = load_hydro_j(a, j1);
         hydro_pair32(pih, pil, vih, vil, Ai, Bi, J0, P, vmax);
@@ -499,9 +496,8 @@ __global__ void __launch_bounds__(PT) k_hydro32(int n, HydroArgs32 a) {
         }
     }
     if (k < c) {
-        const HydroJ32 J = load_hydro_j(a, row[k]);
+        const HydroJ32 J = load_hydro_j(a, *row.at(k));
         hydro_pair32(pih, pil, vih, vil, Ai, Bi, J, P, vmax);
-    }
     }
     // kernel normalisation of i (Bi.y = 1 / H_i) and the mass scale, in FP32
     const float sc = a.kscale * (Bi.y * Bi.y * Bi.y);

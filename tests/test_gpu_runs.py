@@ -45,6 +45,25 @@ def test_runs_in_a_mix_equal_runs_alone(prec):
         assert info["steps"] == 4 and info["time"] == t and info["dt"] == dt
 
 
+def test_density_sums_do_not_depend_on_the_conversion_path():
+    """A run holding a particle 40 times its mean mass sends the whole context's density sums
+    through the FP64-pipe conversion (__float2ll_rn); the other runs, which alone take the
+    FP32 / integer split, give the same bits in that mix, and so does the heavy run (each run's
+    sums are rounded on its own mass scale)."""
+    from fdps_sph_gb300.ic import FIELD
+    bodies = _bodies()
+    F, ids, mats = small_impact(n_target=900, n_impactor=100, seed=24)[:3]
+    F = F.copy()
+    F[FIELD["mass"], 5] *= 40.0
+    runs = (bodies[0], (F, ids, mats), bodies[1])
+    ctx = device_context(tillotson_materials(), precision=1)
+    hs = [ctx.add_run(*b) for b in runs]
+    ctx.step(1 + 3)
+    for h, b in zip(hs, runs):
+        _same(ctx.download_run(h), _alone(b, 1, 3)[0])
+    ctx.close()
+
+
 @pytest.mark.parametrize("prec", [0, 1])
 def test_runs_removed_and_added_between_steps(prec):
     bodies = _bodies()
