@@ -254,7 +254,10 @@ int sph_diagnostics(sph_ctx *ctx, double out[8]);
  * between steps; a run added without valid forces takes its first sph_step as
  * its prologue (main.cpp:92-105: forces and dt, no kick).  sph_remove_run
  * drops a run's particles; sph_download_run copies one run back in its upload
- * order.  Results of a run do not depend on the other runs in the context. */
+ * order.  Results of a run do not depend on the other runs in the context.
+ * sph_add_run returns SPH_ERR_ARG for a run whose mean particle mass differs
+ * from the run set's first run by more than a factor 2^60 (the FP32 mass
+ * copies share the first run's scale). */
 int sph_add_run(sph_ctx *ctx, int64_t n, const double *fields, int64_t ld, const int64_t *id,
                 const int32_t *material, double time, double dt, int flags, int64_t *handle);
 int sph_remove_run(sph_ctx *ctx, int64_t handle);
