@@ -413,7 +413,7 @@ def main():
     ms_step = mixed["ms"] / a.steps
     value = replica_throughput(world, n, ms_step)
 
-    # algorithmic work of each segment of one step (DESIGN.md section 6): flops on the FP32 pipe
+    # algorithmic work of each segment of one step: flops on the FP32 pipe
     # for the pair kernels, compulsory HBM bytes for the list / tree / streaming kernels
     w = mixed["cnt"]
     seg, st = mixed["seg"], a.steps
