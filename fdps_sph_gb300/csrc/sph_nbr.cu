@@ -482,6 +482,14 @@ __device__ __forceinline__ bool exact_in(float r2, float thr, int j, double xi, 
     return false;
 }
 
+// exact_in behind a call: a loop that decides several entries before summing them would
+// otherwise have the FP64 test if-converted, issuing its FP64 instructions for every entry
+__device__ __noinline__ bool exact_in_call(float r2, float thr, int j, double xi, double yi, double zi, double H2,
+                                           const double *__restrict__ x, const double *__restrict__ y,
+                                           const double *__restrict__ z, const double *__restrict__ h) {
+    return exact_in(r2, thr, j, xi, yi, zi, H2, x, y, z, h, false);
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(128)
 k_filter(int n, const int *__restrict__ sup, const float *__restrict__ sup_r2, const int *__restrict__ scnt,
@@ -673,9 +681,11 @@ k_density_sup32(int n, const int *__restrict__ sup, const float *__restrict__ su
 // Every density pass of a step (CalcDensity, force.h:9-23, main.cpp:138-139) for a particle
 // in one go: the passes only use the particle's own h, and its row holds its gather set as
 // long as h <= KAPPA h_sup.  DT threads share a particle (entries 4 sub .. 4 sub + 3 in steps
-// of 4 DT; measured at 1M: DT 1 1.23 ms, 2 1.22, 4 1.36, 8 1.72 for the four passes, the
-// rows being too many for the passes to find them in L1 or L2); a particle whose new h
-// leaves the skin stops after that pass, to go on once its row is walked again.  Each term
+// of 4 DT; measured at 1M: DT 1 1.07 ms, 2 0.98, 4 0.97 for the four passes before the loop
+// below was made branch-free); a particle whose new h leaves the skin stops after that pass, to
+// go on once its row is walked again.  The four entries of a chunk are decided first (the rare
+// FP64 edge test behind a call), then summed without branches, two at a time in paired FP32
+// arithmetic, non-members as zero terms (0.98 -> 0.69 ms at 1M, bit-identical).  Each term
 // m_j W_ij is rounded to a multiple of 2^-40 and summed as an integer, so the sum depends on
 // neither the order of the terms nor where non-members sit in the row.  The multiple is taken on
 // the particle's run's own mass scale (the terms carry the context's, 2^fixd[run] times the
@@ -716,40 +726,72 @@ k_density_fused32(int n, int n_pass, const int *__restrict__ sup, const float *_
         const float invH = 1.0f / (float)Hi;
         const float lo_b = H2i * (1.0f - 1.9073486328125e-06f), hi_b = H2i * (1.0f + 1.9073486328125e-06f);
         long long acc = 0;
-        unsigned aH = 0, aL = 0;   // SPLIT: 32-bit sums of at most 64 x 4 terms
-        int it = 0;
+        // SPLIT: 32-bit sums of the raw bit patterns of sph_fix40_add's a and b, their offsets
+        // (b1, b2 per term, non-members included: a zero term adds exactly the offsets) taken off
+        // when they are flushed, after at most SPH_FIX_TERMS terms
+        unsigned rH = 0, rL = 0, nt = 0;   // nt: terms in rH / rL
+        const f32x2 ih2 = f2_pack(invH, invH), one2 = f2_pack(1.0f, 1.0f), c1_2 = f2_pack(c1, c1),
+                    c2_2 = f2_pack(c2, c2), k32 = f2_pack(32.0f, 32.0f), k25 = f2_pack(25.0f, 25.0f),
+                    k8 = f2_pack(8.0f, 8.0f);
         for (int seg = 0; seg < 2; ++seg) {
             int c;
             const int64_t b = row_seg(rm, i, seg, c_all, &c);
             if (c <= 0) break;
             const float *rrow = sup_r2 + b, *mrow = sup_m + b;
             for (int k = 4 * sub; k < c; k += 4 * DT) {
-                if (SPLIT && (++it & (SPH_FIX_TERMS / 4 - 1)) == 0) {
-                    acc += sph_fix40_value(aH, aL);
-                    aH = aL = 0;
+                if (SPLIT) {
+                    if (nt == (unsigned)SPH_FIX_TERMS) {
+                        acc += sph_fix40_value(rH - nt * b1, rL - nt * b2);
+                        rH = rL = nt = 0;
+                    }
+                    nt += 4;
                 }
                 const float4 r4 = *reinterpret_cast<const float4 *>(rrow + k);
                 const float4 m4 = *reinterpret_cast<const float4 *>(mrow + k);
-                const float rr[4] = {r4.x, r4.y, r4.z, r4.w}, mj[4] = {m4.x, m4.y, m4.z, m4.w};
+                const float rr[4] = {r4.x, r4.y, r4.z, r4.w};
+                // members: inside the band by FP32, at its edge by the FP64 test; padding out
+                bool in[4];
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
-                    if (k + u >= c) break;
-                    bool in = rr[u] < lo_b;
-                    if (!in && !(rr[u] > hi_b))
-                        in = exact_in(rr[u], H2i, sup[b + k + u], xi, yi, zi, H2, x, y, z, h, false);
-                    if (!in) continue;
-                    const float s_ = sqrt_a(rr[u]) * invH;
-                    const float q = fmaxf(1.0f - s_, 0.0f);
-                    const float q2 = q * q, q4 = q2 * q2;
-                    const float term = mj[u] * ((1.0f + s_ * (8.0f + s_ * (25.0f + s_ * 32.0f))) * (q4 * q4));
-                    if (SPLIT)
-                        sph_fix40_add(term, aH, aL, c1, c2, b1, b2);
-                    else
-                        acc += __float2ll_rn(term * to_fix);
+                    in[u] = k + u < c && rr[u] < lo_b;
+                    if (k + u < c && !in[u] && !(rr[u] > hi_b))
+                        in[u] = exact_in_call(rr[u], H2i, sup[b + k + u], xi, yi, zi, H2, x, y, z, h);
+                }
+                // m_j W(s) for two entries at a time, each lane with the roundings of the scalar
+                // m * ((1 + s (8 + s (25 + 32 s))) (q^4 q^4)), q = max(1 - s, 0), s = sqrt(r^2) / H
+                float t[4];
+#pragma unroll
+                for (int pr = 0; pr < 2; ++pr) {
+                    const f32x2 s2 = f2_mul(f2_pack(sqrt_a(rr[2 * pr]), sqrt_a(rr[2 * pr + 1])), ih2);
+                    float qa, qb;
+                    f2_unpack(f2_sub(one2, s2), qa, qb);
+                    const f32x2 q = f2_pack(fmaxf(qa, 0.0f), fmaxf(qb, 0.0f));
+                    const f32x2 q2 = f2_mul(q, q), q4 = f2_mul(q2, q2);
+                    const f32x2 poly = f2_fma(s2, f2_fma(s2, f2_fma(s2, k32, k25), k8), one2);
+                    const f32x2 mj = pr == 0 ? f2_pack(m4.x, m4.y) : f2_pack(m4.z, m4.w);
+                    f2_unpack(f2_mul(mj, f2_mul(poly, f2_mul(q4, q4))), t[2 * pr], t[2 * pr + 1]);
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) t[u] = in[u] ? t[u] : 0.0f;
+                if (SPLIT) {
+#pragma unroll
+                    for (int pr = 0; pr < 2; ++pr) {
+                        const f32x2 tt = f2_pack(t[2 * pr], t[2 * pr + 1]);
+                        const f32x2 a = f2_add(tt, c1_2);
+                        const f32x2 bb = f2_add(f2_sub(tt, f2_sub(a, c1_2)), c2_2);
+                        float a0, a1, b0, b1f;
+                        f2_unpack(a, a0, a1);
+                        f2_unpack(bb, b0, b1f);
+                        rH += __float_as_uint(a0) + __float_as_uint(a1);
+                        rL += __float_as_uint(b0) + __float_as_uint(b1f);
+                    }
+                } else {
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) acc += __float2ll_rn(t[u] * to_fix);
                 }
             }
         }
-        if (SPLIT) acc += sph_fix40_value(aH, aL);
+        if (SPLIT) acc += sph_fix40_value(rH - nt * b1, rL - nt * b2);
 #pragma unroll
         for (int o = DT / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(gm, acc, o, DT);
         double rho, hn;

@@ -655,33 +655,6 @@ __device__ __forceinline__ void grav_acc(float px, float py, float pz, float e2,
     a3 -= mri;
 }
 
-// packed pairs of FP32 values in one 64-bit register (low half first) and the paired FP32
-// arithmetic of sm_100+ (one instruction, two IEEE round-to-nearest results)
-typedef unsigned long long f32x2;
-__device__ __forceinline__ f32x2 f2_pack(float a, float b) {
-    f32x2 r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-    return r;
-}
-__device__ __forceinline__ void f2_unpack(f32x2 r, float &a, float &b) {
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
-}
-__device__ __forceinline__ f32x2 f2_add(f32x2 a, f32x2 b) {
-    f32x2 r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f32x2 f2_mul(f32x2 a, f32x2 b) {
-    f32x2 r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f32x2 f2_fma(f32x2 a, f32x2 b, f32x2 c) {
-    f32x2 r;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-    return r;
-}
-
 // grav_acc for two j at once (x, y, z, m: the pair's coordinates relative to the group origin and
 // masses), with the i-particle's negated coordinates and softening paired with themselves.  Per
 // interaction the same operations and roundings as grav_acc (q - p = -(p - q) exactly); the two j
