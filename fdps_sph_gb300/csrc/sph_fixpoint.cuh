@@ -81,6 +81,10 @@ SPH_FIX_HD void sph_fix40_add(float t, unsigned &H, unsigned &L, float c1, float
     L += sph_fix_bits(b) - b2;
 }
 
+// The density kernel adds the raw bit patterns of a and b (two terms at a time, in paired FP32
+// arithmetic) and takes nt * b1 and nt * b2 off when it reads the sums (nt terms, zero terms of
+// non-members included, which add exactly b1 and b2): the same sums, mod 2^32, as above.
+
 // the value of the sums after at most SPH_FIX_TERMS additions
 SPH_FIX_HD long long sph_fix40_value(unsigned H, unsigned L) {
     return (long long)(int)H * 8388608LL + (long long)(int)L;
