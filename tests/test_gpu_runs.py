@@ -64,6 +64,30 @@ def test_density_sums_do_not_depend_on_the_conversion_path():
     ctx.close()
 
 
+def test_run_on_another_mass_scale_equals_run_alone():
+    """a run whose particles are 2^10 times heavier than the first run's: its density sums are
+    rounded on its own scale (the context's FP32 masses carry the first run's), so it matches the
+    run advanced alone; a run 2^65 times heavier is refused"""
+    from fdps_sph_gb300 import lib
+    from fdps_sph_gb300.ic import FIELD
+    bodies = _bodies()
+    F, ids, mats = small_impact(n_target=900, n_impactor=100, seed=25)[:3]
+    F = F.copy()
+    F[FIELD["mass"]] *= 1024.0
+    runs = (bodies[0], (F, ids, mats))
+    ctx = device_context(tillotson_materials(), precision=1)
+    hs = [ctx.add_run(*b) for b in runs]
+    ctx.step(1 + 3)
+    for h, b in zip(hs, runs):
+        _same(ctx.download_run(h), _alone(b, 1, 3)[0])
+    G = F.copy()
+    G[FIELD["mass"]] *= 2.0 ** 55
+    with pytest.raises(lib.SphError) as ei:
+        ctx.add_run(G, ids, mats)
+    assert ei.value.code == -1 and "2^" in str(ei.value)
+    ctx.close()
+
+
 @pytest.mark.parametrize("prec", [0, 1])
 def test_runs_removed_and_added_between_steps(prec):
     bodies = _bodies()
