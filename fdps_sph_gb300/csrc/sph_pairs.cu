@@ -402,20 +402,30 @@ __global__ void __launch_bounds__(PT) k_drvt32(int n, DrvtArgs32 a) {
     a.bal[i] = fabsf(dv) / (fabsf(dv) + sqrtf(r0 * r0 + r1 * r1 + r2 * r2) + 1.0e-4f * (float)a.snds[i] / hf);
 }
 
-// mixed hydro: per-particle FP32 packs hA = (f P / rho^2, c_s, f, Bal), hB = (rho, 1/H, H, 1e-6 h).
-// The i-particle's kernel normalisation is factored out of the FP32 sums and
-// applied in FP64; the j-particle's enters as the ratio (H_i / H_j)^3.
+// mixed hydro: per-particle FP32 pack hA = (f P / rho^2, c_s, f, Bal), and rho, 1/H and h in the
+// free .w slots of the velocity and position packs (vh.w, vl.w, xl.w), so a neighbour's data is
+// five float4 (80 B) gathered; H and 1e-6 h follow from h (hydro_b).  The i-particle's kernel
+// normalisation is factored out of the FP32 sums and applied in FP64; the j-particle's enters
+// as the ratio (H_i / H_j)^3.
 __global__ void k_hydro_pack32(int n, const double *h, const double *dens, const double *pres, const double *snds,
-                               const double *gradh, const double *bal, float4 *hA, float4 *hB) {
+                               const double *gradh, const double *bal, float4 *hA, float4 *xl, float4 *vh,
+                               float4 *vl) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const float hi = (float)h[i], H = (float)SUPPORT * hi, rho = (float)dens[i], f = (float)gradh[i];
+    const float hi = (float)h[i], H = __fmul_rn((float)SUPPORT, hi), rho = (float)dens[i], f = (float)gradh[i];
     hA[i] = make_float4(f * (float)pres[i] / (rho * rho), (float)snds[i], f, (float)bal[i]);
-    hB[i] = make_float4(rho, 1.0f / H, H, 1.0e-6f * hi);
+    reinterpret_cast<float *>(xl + i)[3] = hi;
+    reinterpret_cast<float *>(vh + i)[3] = rho;
+    reinterpret_cast<float *>(vl + i)[3] = 1.0f / H;
+}
+
+// (rho, 1/H, H, 1e-6 h) of a particle from its packs (the products not fused into later sums)
+__device__ __forceinline__ float4 hydro_b(const float4 &xl, const float4 &vh, const float4 &vl) {
+    return make_float4(vh.w, vl.w, __fmul_rn((float)SUPPORT, xl.w), __fmul_rn(1.0e-6f, xl.w));
 }
 
 struct HydroArgs32 {
-    const float4 *xh, *xl, *vh, *vl, *hA, *hB;
+    const float4 *xh, *xl, *vh, *vl, *hA;
     const double *h;
     double *ax, *ay, *az, *edot, *dt;
     const int *nbr, *cnt;
@@ -464,7 +474,7 @@ __device__ __forceinline__ HydroJ32 load_hydro_j(const HydroArgs32 &a, int j) {
     J.uh = a.vh[j];
     J.ul = a.vl[j];
     J.A = a.hA[j];
-    J.B = a.hB[j];
+    J.B = hydro_b(J.ql, J.uh, J.ul);
     return J;
 }
 
@@ -476,7 +486,7 @@ __global__ void __launch_bounds__(PT, 6) k_hydro32(int n, HydroArgs32 a) {
     const int i = gt / TPI, sub = gt % TPI;
     if (i >= n) return;   // whole groups of TPI lanes leave together
     const float4 pih = a.xh[i], pil = a.xl[i], vih = a.vh[i], vil = a.vl[i];
-    const float4 Ai = a.hA[i], Bi = a.hB[i];
+    const float4 Ai = a.hA[i], Bi = hydro_b(pil, vih, vil);
     float Dh[4] = {0, 0, 0, 0}, Dl[4] = {0, 0, 0, 0};
     float P[4] = {0, 0, 0, 0};
     float vmax = 0.0f;
@@ -1293,10 +1303,11 @@ int sph_pass_hydro(sph_ctx *ctx, int build_lists) {
     const SphLists &L = ctx->lists[1];
     // scratch: 2 x float4 or 1 x double4 per particle, in the F2 ping-pong block (free between sorts)
     if (ctx->cfg.precision == SPH_PREC_MIXED) {
-        float4 *hA = (float4 *)ctx->F2, *hB = hA + ctx->cap;
+        float4 *hA = (float4 *)ctx->F2;
         k_hydro_pack32<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, CF(SPH_SMTH), CF(SPH_DENS), CF(SPH_PRES),
-                                                                    CF(SPH_SNDS), CF(SPH_GRADH), CF(SPH_BAL), hA, hB); ++ctx->launches;
-        HydroArgs32 a{ctx->xh,    ctx->xl,    ctx->vhf,   ctx->vlf,       hA,         hB,    CF(SPH_SMTH),
+                                                                    CF(SPH_SNDS), CF(SPH_GRADH), CF(SPH_BAL), hA,
+                                                                    ctx->xl, ctx->vhf, ctx->vlf); ++ctx->launches;
+        HydroArgs32 a{ctx->xh,    ctx->xl,    ctx->vhf,   ctx->vlf,       hA,    CF(SPH_SMTH),
                       CF(SPH_AX), CF(SPH_AY), CF(SPH_AZ), CF(SPH_ENGDOT), CF(SPH_DT), L.nbr, L.cnt,
                       ctx->sup.map(),    (float)(WNORM / (PI_D * ctx->mscale))};
         const int tpi = ctx->tune.hydro_tpi;
