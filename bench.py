@@ -169,6 +169,15 @@ def workload(n_total, seed=2024, config="1m", mode=1):
     return F, ids, mats, materials
 
 
+# the headline metric (both arms print it; `batch` carries the batched sweep's p99 step latency)
+METRIC = "SPH particle-steps/s at 1M (plain FP64 vs mixed, same error); batch p99 latency"
+
+
+def workload_name(n, a):
+    return (f"{n:,}-particle {WORKLOADS[a.config]}, theta {a.theta}" +
+            (", mode 2 (constant entropy, 120 x 120 tables)" if a.mode == 2 else ""))
+
+
 WORKLOADS = {"1m": "two-layer impact (90% target, 10% impactor, iron/dunite, 30 deg, 1.2 v_esc)",
              "4m": "three-layer impact (90% target, 10% impactor, iron/dunite/granite crust 5%, 45 deg, 1.0 v_esc)"}
 
@@ -366,12 +375,13 @@ def main():
         el = time.perf_counter() - t0
         v = n_cpu * a.steps / el
         cores = po.lib(True).or_num_threads()
-        out = {"metric": "SPH particle-steps/s (1M two-layer impact; reference CPU path, bounded sample)",
+        out = {"metric": METRIC,
                "value": v, "unit": "particle-steps/s", "impl": "reference", "n_gpus": a.gpus, "steps": a.steps,
                "warmup": a.warmup, "ms_per_step": 1e3 * el / a.steps, "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded IC generator)",
-               "config": {"workload": f"1M-particle impact geometry at {n_cpu} particles (CPU sample)",
-                          "particles": n_cpu, "parallelism": f"OpenMP x{cores}"},
+               "config": {"workload": workload_name(a.n, a), "particles": a.n, "precision": "fp64",
+                          "sample": f"{n_cpu} particles of the same geometry per step (bounded CPU sample)",
+                          "parallelism": f"OpenMP x{cores} (host cores)"},
                "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": cores, "kind": "port",
                                 "sample": f"{n_cpu} particles, {a.steps} steps after {a.warmup} warm-up steps"},
                "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -455,12 +465,11 @@ def main():
                                  "measured FMA-chain probe (sph_probe_peak); MEASURED_PEAKS.json has no FP32 figure")})
 
     out = {
-        "metric": "SPH particle-steps/s at 1M (mixed FP32/FP64; plain FP64 beside it)",
+        "metric": METRIC,
         "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 pair sums + f64", "data": "synthetic (seeded IC generator, synthetic " + ("120x120" if a.mode == 2 else "200x200") + " rho-u tables)",
-        "config": {"workload": f"{n:,}-particle {WORKLOADS[a.config]}, theta {a.theta}" +
-                               (", mode 2 (constant entropy, 120 x 120 tables)" if a.mode == 2 else ""), "particles": n,
+        "config": {"workload": workload_name(n, a), "particles": n,
                    "precision": "mixed",
                    "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas" if world > 1 else "1 GPU"},
         "gpu_launches": int(mixed["launches"]),
