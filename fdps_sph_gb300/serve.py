@@ -87,8 +87,10 @@ class Request:
 class Server:
     """Continuous batching of impact runs on one GPU (see the module docstring)."""
 
-    def __init__(self, precision="mixed", device=0, budget_bytes=None, max_runs=None, keep_results=False):
-        self.ctx = make_context(precision, device)
+    def __init__(self, precision="mixed", device=0, budget_bytes=None, max_runs=None, keep_results=False, ctx=None):
+        # ctx: a context of the lib.Context run interface (add_run, step, download_run, remove_run,
+        # close); by default a new device context with the iron / dunite tables
+        self.ctx = ctx if ctx is not None else make_context(precision, device)
         self.budget = budget_bytes if budget_bytes is not None else hbm_budget(device)
         self.max_particles = max(1, self.budget // BYTES_PER_PARTICLE)
         self.max_runs = max_runs
