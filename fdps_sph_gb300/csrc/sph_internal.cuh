@@ -462,4 +462,36 @@ int sph_init_smth(sph_ctx *ctx, int64_t off, int64_t n);
 
 static inline int sph_div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 
+namespace sph {
+
+// Length argument of the scan kernels: a host value, a device value, or the
+// difference of two device values.
+struct LenArg {
+    const int *p;   // device pointer or null
+    int v;          // host value when p is null
+    int diff;       // if nonzero, length = p[1] - p[0]
+    __device__ int get() const {
+        if (!p) return v;
+        return diff ? (p[1] - p[0]) : p[0];
+    }
+};
+
+// Key-and-sort kernels of sph_tree.cu that sph_noalloc.cu also launches.
+constexpr int RS_THREADS = 256;          // threads of k_rs_hist / k_rs_scatter (one per digit)
+constexpr int RS_ITEMS = 8;
+constexpr int RS_TILE = RS_THREADS * RS_ITEMS;   // keys per radix-sort tile
+__global__ void k_scan_reduce(const int *in, LenArg len, int *part);
+__global__ void k_scan_part(int *part, int nb, int *total);
+__global__ void k_scan_down(const int *in, int *out, LenArg len, const int *part);
+__global__ void k_bbox_partial(const double *x, const double *y, const double *z, int n, double *part);
+__global__ void k_bbox_final(const double *part, int nb, double theta, double *rb);
+__global__ void k_keys(const double *x, const double *y, const double *z, int n, const double *rb, uint64_t *keys,
+                       uint32_t *vals, int *err);
+__global__ void k_rs_hist(const uint64_t *keys, int n, int shift, uint32_t *hist, int nb, const int4 *tiles);
+__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint64_t *kin, const uint32_t *vin, uint64_t *kout,
+                                                           uint32_t *vout, int n, int shift, const uint32_t *off,
+                                                           int nb, const int4 *tiles);
+
+}  // namespace sph
+
 #define FLD(ptr, f, cap) ((ptr) + (int64_t)(f) * (cap))

@@ -1,51 +1,35 @@
 // Allocation-free Morton ordering: the key and sort stage of the octree
 // build (sph_tree.cu) for callers that must not allocate device memory.
 //
-// Who needs this: a host that records its own step into a CUDA graph cannot
-// let a library call cudaMalloc / cudaFree inside the capture (the capture
-// is invalidated), and a host that runs under a fixed device-memory budget
-// or a real-time step loop cannot afford an allocation (or its implicit
-// device synchronisation) in the middle of a step.  This entry point takes
-// device pointers for its inputs and outputs and keeps its scratch in one
-// file-scope device array, sized for at most SPH_NOALLOC_MAX_N particles.
-// That array exists on every GPU that loads the library, for the lifetime of
-// the process, whether or not the entry point is used.
+// Who needs this: a host that runs under a fixed device-memory budget (an
+// embedding application that has handed the rest of the GPU to its own pool
+// allocator, or a service that must not grow its footprint while it runs)
+// cannot let a library call cudaMalloc / cudaFree, and a cudaFree also
+// synchronises the device, which such a host may not allow in the middle of
+// a step.  This entry point takes device pointers for its inputs and
+// outputs and keeps its scratch in one file-scope device array, sized for at
+// most SPH_NOALLOC_MAX_N particles.  That array exists on every GPU that
+// loads the library, for the lifetime of the process, whether or not the
+// entry point is used.
 //
 // The array is shared by every call on a device and keeps the last call's
 // contents; each call rewrites all of it that it reads except the error
 // word, which it clears first.  Two calls whose work overlaps on the GPU
-// (different streams, no ordering between them) race on the array.
+// (different streams, no ordering between them) race on the array.  Each
+// call ends by reading the error word back to the host, so it returns only
+// after its work on `stream` has finished.
 #include <mutex>
 
 #include "sph_internal.cuh"
 
 namespace sph {
 
-// kernels of sph_tree.cu, launched from here unchanged
-struct LenArg {
-    const int *p;
-    int v;
-    int diff;
-    __device__ int get() const {
-        if (!p) return v;
-        return diff ? (p[1] - p[0]) : p[0];
-    }
-};
-__global__ void k_scan_reduce(const int *in, LenArg len, int *part);
-__global__ void k_scan_part(int *part, int nb, int *total);
-__global__ void k_scan_down(const int *in, int *out, LenArg len, const int *part);
-__global__ void k_bbox_partial(const double *x, const double *y, const double *z, int n, double *part);
-__global__ void k_bbox_final(const double *part, int nb, double theta, double *rb);
-__global__ void k_keys(const double *x, const double *y, const double *z, int n, const double *rb, uint64_t *keys,
-                       uint32_t *vals, int *err);
-__global__ void k_rs_hist(const uint64_t *keys, int n, int shift, uint32_t *hist, int nb, const int4 *tiles);
-__global__ void k_rs_scatter(const uint64_t *kin, const uint32_t *vin, uint64_t *kout, uint32_t *vout, int n,
-                             int shift, const uint32_t *off, int nb, const int4 *tiles);
+// the key and sort kernels of sph_tree.cu (declared in sph_internal.cuh) are launched from here unchanged
 
 namespace {
 
 constexpr int NA_MAX = SPH_NOALLOC_MAX_N;
-constexpr int NA_TILE = 2048;                     // radix-sort tile (k_rs_scatter)
+constexpr int NA_TILE = RS_TILE;                  // radix-sort tile (k_rs_scatter)
 constexpr int NA_NB = (NA_MAX + NA_TILE - 1) / NA_TILE;
 constexpr int NA_BOX = 304;                       // blocks of k_bbox_partial
 constexpr int NA_SCAN = 256;                      // blocks of the scan kernels
@@ -99,6 +83,9 @@ extern "C" int sph_morton_order_noalloc(const double *x, const double *y, const 
     using namespace sph;
     if (!x || !y || !z || !keys_out || !order_out || n < 1) return SPH_ERR_ARG;
     if (n > NA_MAX) return SPH_ERR_CAPACITY;   // the scratch holds at most SPH_NOALLOC_MAX_N particles
+    // An error an earlier call left pending on this thread is reported before any work is queued and left
+    // in place for its owner, so the launch checks below see this call's launches only.
+    if (cudaPeekAtLastError() != cudaSuccess) return SPH_ERR_CUDA;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) {
         cudaGetLastError();

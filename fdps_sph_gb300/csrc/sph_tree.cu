@@ -24,16 +24,6 @@ namespace sph {
 constexpr int SCAN_BLOCKS = 256;
 constexpr int SCAN_THREADS = 256;
 
-struct LenArg {
-    const int *p;   // device pointer or null
-    int v;          // host value when p is null
-    int diff;       // if nonzero, length = p[1] - p[0]
-    __device__ int get() const {
-        if (!p) return v;
-        return diff ? (p[1] - p[0]) : p[0];
-    }
-};
-
 __device__ __forceinline__ int warp_incl_scan(int v) {
     const int lane = threadIdx.x & 31;
 #pragma unroll
@@ -321,9 +311,7 @@ __global__ void k_keys_runs(const double *x, const double *y, const double *z, i
 // yields offsets that keep every run in its own range: a segmented sort.
 // Without one, tile b covers [b * RS_TILE, ...) and the layout is digit-major.
 
-constexpr int RS_THREADS = 256;
-constexpr int RS_ITEMS = 8;
-constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
+// RS_THREADS, RS_ITEMS, RS_TILE: sph_internal.cuh
 
 __device__ __forceinline__ int4 rs_tile(const int4 *tiles, int n, int nb) {
     if (tiles) return tiles[blockIdx.x];

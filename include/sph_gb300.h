@@ -315,9 +315,11 @@ int sph_get_counters(sph_ctx *ctx, int64_t out[16]);
 /* ---- allocation-free Morton ordering -------------------------------------
  * No counterpart in the reference: FDPS builds its tree on the host.  This
  * is the key-and-sort stage of the device octree build for callers that
- * must not allocate device memory -- a host recording its step into its own
- * CUDA graph (a cudaMalloc inside the capture would invalidate it), or a
- * host with a fixed device-memory budget or a real-time step loop.  x, y, z
+ * must not allocate device memory: a host that runs under a fixed
+ * device-memory budget (its own pool allocator owns the rest of the GPU),
+ * or one that may not take the device-wide synchronisation of a cudaFree in
+ * the middle of its step.  The call returns after its work on `stream` has
+ * finished (it reads a status word back).  x, y, z
  * (n doubles each), keys_out (n) and order_out (n) are device pointers;
  * stream may be null (the legacy default stream).  keys_out[k] is the k-th
  * smallest 63-bit Morton key over the octree's root cube and order_out[k]
@@ -326,7 +328,9 @@ int sph_get_counters(sph_ctx *ctx, int64_t out[16]);
  * Scratch lives in one file-scope device array for at most
  * SPH_NOALLOC_MAX_N particles (about 3.2 MB, present on every GPU that loads
  * the library); larger n returns SPH_ERR_CAPACITY, null pointers or n < 1
- * SPH_ERR_ARG, a non-finite position SPH_ERR_NONFINITE.  The first call on a
+ * SPH_ERR_ARG, a non-finite position SPH_ERR_NONFINITE, a CUDA error already
+ * pending on the calling thread SPH_ERR_CUDA (before any work is queued; the
+ * error is left in place).  The first call on a
  * device looks up the array's device address (cudaGetSymbolAddress), so make
  * that first call before any stream capture.  Every call on a device shares
  * the array: calls that overlap on the GPU race.  No device memory is

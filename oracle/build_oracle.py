@@ -20,7 +20,9 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
-REF_ROOT = os.environ.get("FDPS_SPH_REFERENCE", "/root/reference")
+# The reference checkout: $FDPS_SPH_REFERENCE, else a directory named "reference"
+# beside this repository's root (absent on hosts that only run the prebuilt oracle).
+REF_ROOT = os.environ.get("FDPS_SPH_REFERENCE") or os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
 
 
 def _cc(out: str, flags: list[str]) -> None:

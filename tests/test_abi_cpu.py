@@ -64,3 +64,15 @@ def test_context_creation_fails_cleanly_without_gpu():
         assert e.code in (-2, -3)
     else:
         raise AssertionError("expected an error without a GPU")
+
+
+def test_header_constants_match_binding():
+    # every #define the Python binding mirrors as a number equals the header's
+    src = open(os.path.join(ROOT, "include", "sph_gb300.h")).read()
+    defs = {m.group(1): m.group(2) for m in re.finditer(r"#define\s+(SPH_[A-Z0-9_]+)\s+\(?(-?\d+)\)?", src)}
+    assert int(defs["SPH_NOALLOC_MAX_N"]) == lib.NOALLOC_MAX_N
+    assert int(defs["SPH_PREC_FP64"]) == lib.PREC_FP64 and int(defs["SPH_PREC_MIXED"]) == lib.PREC_MIXED
+    assert int(defs["SPH_ENTROPY_ABS_INT"]) == lib.ENTROPY_ABS_INT
+    assert int(defs["SPH_ENTROPY_ABS_REAL"]) == lib.ENTROPY_ABS_REAL
+    for code, name in lib.ERRORS.items():
+        assert int(defs[name]) == code, name

@@ -7,7 +7,10 @@ import pytest
 
 from fdps_sph_gb300 import ic, snapshot
 
-REF_SNAPSHOT = "/root/reference/input/tar.dat"   # the reference's initial state, when present
+from oracle import build_oracle
+
+# the reference's initial state, when the reference checkout is present ($FDPS_SPH_REFERENCE, or beside this repo)
+REF_SNAPSHOT = os.path.join(build_oracle.REF_ROOT, "input", "tar.dat")
 
 
 def test_ascii_round_trip(tmp_path):
