@@ -57,8 +57,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=1_000_000, help="total particles (default: the 1M workload)")
-    ap.add_argument("--cpu-n", type=int, default=100_000, help="particles of the bounded CPU sample")
-    ap.add_argument("--cpu-steps", type=int, default=10, help="timed steps of the bounded CPU sample")
+    ap.add_argument("--cpu-n", type=int, default=0,
+                    help="particles of the CPU baseline (default: the workload's own count)")
+    ap.add_argument("--cpu-steps", type=int, default=5, help="timed steps of the cpu_baseline leg")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
@@ -71,7 +72,11 @@ def parse():
                     help="threads per particle of the derivative / hydro kernels instead of autotuning (1, 2, 4)")
     ap.add_argument("--batch-runs", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=100)
-    ap.add_argument("--serve-s", type=float, default=60.0, help="seconds of Poisson arrivals (2 per second)")
+    ap.add_argument("--serve-s", type=float, default=600.0, help="seconds of Poisson arrivals (2 per second)")
+    ap.add_argument("--serve-steps", default="200,2000", help="steps per request, uniform in [lo, hi]")
+    ap.add_argument("--no-4m", action="store_true", help="skip the 4M three-layer case at theta 0.5 / 0.7")
+    ap.add_argument("--contact-steps", type=int, default=20,
+                    help="mixed steps of the 1M contact state before its mixed-vs-FP64 comparison")
     return ap.parse_args()
 
 
@@ -190,7 +195,7 @@ def run_gpu(F, ids, mats, materials, precision, steps, warmup, device, theta=0.5
     ctx.upload(F, ids, mats)
     ctx.prologue()
     Fp, idp, _ = ctx.download()   # the forces of the initial state, for the mixed-vs-FP64 errors
-    first = Fp[:, np.argsort(idp, kind="stable")][[FIELD[k] for k in ERR_FIELDS]].copy()
+    first = Fp[:, np.argsort(idp, kind="stable")]
     del Fp
     for _ in range(warmup):
         ctx.step(1)
@@ -217,34 +222,102 @@ def run_gpu(F, ids, mats, materials, precision, steps, warmup, device, theta=0.5
     return ctx, ms, seg, c1, c1["launches"] - c0, clk.summary(), drift(d0, d1, steps), tune, first
 
 
-ERR_FIELDS = ("dens", "ax", "ay", "az", "eng_dot", "gx", "gy", "gz", "pot")
+def state_errors(a, device, materials, mixed, f64):
+    """the mixed path's forces against the FP64 path's (held to the oracle by the parity tests) on
+    three states of the workload, all particles, bar 1e-5:
+      contact -- the bodies placed in contact and advanced a.contact_steps mixed steps, so the
+                 contact region is shocked (artificial viscosity and du/dt active);
+      warm    -- the state the mixed timed run reached (the prologue, the warm-up, timed and
+                 end-to-end steps), bodies compressing under their own gravity;
+      initial -- the prologue of the initial state (rigid bodies: du/dt is zero in both paths).
+    The top-level numbers are the contact state's."""
+    from fdps_sph_gb300 import accuracy, ic, lib
+    res = {}
+    if a.config == "1m" and a.mode == 1:
+        n = a.n
+        nt = int(round(n * 0.9))
+        F, ids, mats, _ = ic.config_1m_contact(n_target=nt, n_impactor=n - nt)
+        ctx = lib.Context(precision="mixed", device=device, theta=a.theta)
+        try:
+            for k, m in enumerate(materials):
+                ctx.set_material(k, m)
+            ctx.upload(F, ids, mats)
+            ctx.prologue()
+            ctx.step(a.contact_steps)
+            t_c, _, _ = ctx.time()
+            S, sid, smat = ctx.download()
+        finally:
+            ctx.close()
+        e = accuracy.compare_on_state(S, sid, smat, materials, a.theta, device, t_c)
+        e["state"] = (f"{n:,} particles placed in contact (centres 0.98 (R_t + R_i) apart, contact velocity of the "
+                      f"30 deg / 1.2 v_esc orbit), after the prologue and {a.contact_steps} mixed steps")
+        res["contact"] = e
+        del S
+    S, sid, smat, t_w, step_w = mixed["state"]
+    e = accuracy.compare_on_state(S, sid, smat, materials, a.theta, device, t_w)
+    e["state"] = f"the timed run's state after step {step_w} (prologue, warm-up, timed and end-to-end steps)"
+    res["warm"] = e
+    mixed.pop("state")
+    e = accuracy.force_errors(mixed["first"], f64["first"])
+    e["activity"] = accuracy.activity(f64["first"])
+    e["state"] = "the initial state's prologue (rigid bodies 4 R_t apart: no approaching pairs, du/dt = 0)"
+    res["initial"] = e
+    top = res.get("contact", res["warm"])
+    out = {k: v for k, v in top.items() if k not in ("activity",)}
+    out.update(res)
+    out["bar"] = 1e-5
+    out["note"] = ("per-quantity max over particles: density and potential relative, vectors and du/dt "
+                   "relative with the RMS over particles as floor; the FP64 path is held to the oracle by the "
+                   "parity tests; top-level values are the contact state's")
+    return out
 
 
-def mixed_errors(mx, f64):
-    """per-quantity error of the mixed path's initial forces against the FP64 path's (pinned to
-    the oracle by the parity tests): density relative per particle; vectors and du/dt relative
-    per particle, floored at the RMS over particles"""
-    ix = {k: i for i, k in enumerate(ERR_FIELDS)}
-
-    def vec(X, keys):
-        return np.stack([X[ix[k]] for k in keys], 1)
-
-    def vrms(A, B):
-        nb = np.linalg.norm(B, axis=1)
-        rms = max(float(np.sqrt(np.mean(nb * nb))), 1e-300)
-        return float(np.max(np.linalg.norm(A - B, axis=1) / np.maximum(nb, rms)))
-
-    def srms(a, b):   # du/dt is zero in both paths while the bodies move rigidly: then 0
-        rms = max(float(np.sqrt(np.mean(b * b))), 1e-300)
-        return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), rms)))
-
-    return {"dens": float(np.max(np.abs(mx[0] - f64[0]) / np.abs(f64[0]))),
-            "acc_hydro": vrms(vec(mx, ("ax", "ay", "az")), vec(f64, ("ax", "ay", "az"))),
-            "eng_dot": srms(mx[ix["eng_dot"]], f64[ix["eng_dot"]]),
-            "acc_grav": vrms(vec(mx, ("gx", "gy", "gz")), vec(f64, ("gx", "gy", "gz"))),
-            "pot": float(np.max(np.abs(mx[ix["pot"]] - f64[ix["pot"]]) / np.abs(f64[ix["pot"]]))),
-            "acc_total": vrms(vec(mx, ("ax", "ay", "az")) + vec(mx, ("gx", "gy", "gz")),
-                              vec(f64, ("ax", "ay", "az")) + vec(f64, ("gx", "gy", "gz")))}
+def config_4m(device, thetas=(0.5, 0.7), warmup=3, steps=5):
+    """The 4M three-layer impact (3.6M + 0.4M iron / dunite / granite-crust bodies, 45 deg, 1.0 v_esc)
+    at each opening angle: the mixed path timed (CUDA events, `steps` steps after the prologue and
+    `warmup` steps), an FP64 rerun of the same steps from the same initial state, the energy and
+    angular-momentum drift of both, the mixed path's force errors against FP64 on the state the
+    mixed run reached, and how far the two runs' positions have moved apart (in units of h)."""
+    from fdps_sph_gb300 import accuracy
+    F, ids, mats, materials = workload(4_000_000, config="4m")
+    n = F.shape[1]
+    out = {"workload": workload_name(n, argparse.Namespace(config="4m", theta=0.5, mode=1)).rsplit(", theta", 1)[0],
+           "particles": n, "steps": steps, "warmup": warmup}
+    for theta in thetas:
+        row = {}
+        for prec in ("mixed", "fp64"):
+            from fdps_sph_gb300 import lib
+            ctx = lib.Context(precision=prec, device=device, theta=theta)
+            try:
+                for k, m in enumerate(materials):
+                    ctx.set_material(k, m)
+                ctx.upload(F, ids, mats)
+                ctx.prologue()
+                ctx.step(warmup)
+                d0 = ctx.diagnostics()
+                with ClockSampler(device) as clk:
+                    ms = ctx.step_timed(steps)
+                d1 = ctx.diagnostics()
+                t_s, _, step_s = ctx.time()
+                S, sid, smat = ctx.download()
+            finally:
+                ctx.close()
+            row[prec] = {"ms_per_step": ms / steps, "value": n * steps / (ms * 1e-3), "drift": drift(d0, d1, steps),
+                         "clocks": clk.summary()}
+            row[prec + "_state"] = (accuracy.by_id(S, sid), np.sort(sid), smat[np.argsort(sid, kind="stable")],
+                                    t_s, step_s)
+            del S
+        Sm, sid, smat, t_s, step_s = row.pop("mixed_state")
+        Sf = row.pop("fp64_state")[0]
+        e = accuracy.compare_on_state(Sm, sid, smat, materials, theta, device, t_s)
+        e["state"] = f"the mixed run's state after step {step_s}"
+        row["mixed_error_vs_fp64"] = e
+        dx = np.linalg.norm(np.stack([Sm[FIELD[c]] - Sf[FIELD[c]] for c in "xyz"], 1), axis=1)
+        row["divergence_max_dx_over_h"] = float(np.max(dx / Sf[FIELD["smth"]]))
+        row["speedup_mixed_over_fp64"] = row["fp64"]["ms_per_step"] / row["mixed"]["ms_per_step"]
+        out[f"theta_{theta}"] = row
+        del Sm, Sf
+    return out
 
 
 def drift(d0, d1, steps):
@@ -297,11 +370,12 @@ def run_e2e(ctx, F, ids, mats, steps, warmup=2, dist=None):
     return el, h2d, d2h
 
 
-def cpu_sample(n_cpu, steps, fast=True):
+def cpu_sample(n_cpu, steps, fast=True, config="1m", mode=1):
     """the oracle restatement of the path (OpenMP, all host threads) on the
-    same body geometry at n_cpu particles: prologue untimed, `steps` timed"""
+    workload at n_cpu particles (the GPU's own when n_cpu is its count):
+    prologue untimed, `steps` timed"""
     from oracle import pyoracle as po
-    F, ids, mats, materials = workload(n_cpu, seed=77)
+    F, ids, mats, materials = workload(n_cpu, config=config, mode=mode)
     ms = po.MaterialSet([m.as_material() for m in materials])
     cfg = po.make_config(ms)
     s = po.OracleSystem(F, ids, mats, fast=fast)
@@ -360,10 +434,11 @@ def main():
         if rank != 0:
             return
         # the reference's CPU path on this host: the oracle restatement (the reference itself
-        # needs FDPS, which is not vendored, so it cannot be built here); all host threads
-        n_cpu = a.cpu_n
+        # needs FDPS, which is not vendored, so it cannot be built here); all host threads, on the
+        # GPU arm's own workload (the same particles, the same steps)
+        n_cpu = a.cpu_n or a.n
         from oracle import pyoracle as po
-        F, ids, mats, materials = workload(n_cpu, seed=77)
+        F, ids, mats, materials = workload(n_cpu, config=a.config, mode=a.mode)
         ms = po.MaterialSet([m.as_material() for m in materials])
         cfg = po.make_config(ms)
         s = po.OracleSystem(F, ids, mats, fast=True)
@@ -380,10 +455,12 @@ def main():
                "warmup": a.warmup, "ms_per_step": 1e3 * el / a.steps, "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded IC generator)",
                "config": {"workload": workload_name(a.n, a), "particles": a.n, "precision": "fp64",
-                          "sample": f"{n_cpu} particles of the same geometry per step (bounded CPU sample)",
+                          "sample": (f"the workload itself ({n_cpu} particles), every step" if n_cpu == a.n else
+                                     f"{n_cpu} particles of the same geometry per step (bounded CPU sample)"),
                           "parallelism": f"OpenMP x{cores} (host cores)"},
                "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": cores, "kind": "port",
-                                "sample": f"{n_cpu} particles, {a.steps} steps after {a.warmup} warm-up steps"},
+                                "sample": f"{n_cpu} particles, {a.steps} steps after the prologue and "
+                                          f"{a.warmup} warm-up steps"},
                "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(out))
         return
@@ -403,6 +480,9 @@ def main():
         e2e = run_e2e(ctx, F, ids, mats, a.e2e_steps, dist=dist) if prec == "mixed" else None
         results[prec] = dict(ms=ms, seg=seg, cnt=cnt, launches=launches, clocks=clocks, e2e=e2e, drift=dr, tune=tune,
                              first=first)
+        if prec == "mixed" and not a.no_fp64:   # the state the timed steps reached, for the warm comparison
+            t_now, _, step_no = ctx.time()
+            results[prec]["state"] = ctx.download() + (t_now, step_no)
         ctx.close()
 
     results["mixed"]["ms"] = replica_max(results["mixed"]["ms"], dist, f"cuda:{device}")
@@ -502,15 +582,16 @@ def main():
                                     "unit": "TFLOP/s", "frac": ach64 / peak64 if peak64 else None},
                        "clocks": f["clocks"], "gpu_launches": int(f["launches"])}
         out["drift"]["fp64"] = f["drift"]
-        out["mixed_error_vs_fp64"] = dict(mixed_errors(mixed["first"], f["first"]),
-                                          note="forces of the initial state (prologue), all particles; the FP64 "
-                                               "path is held to the oracle by the parity tests; bar 1e-5")
+        out["mixed_error_vs_fp64"] = state_errors(a, device, materials, mixed, f)
+    if not a.no_4m and world == 1 and a.config == "1m" and a.mode == 1:
+        out["config_4m"] = config_4m(device)
     if not a.no_batch and world == 1:
         out.update(batch_and_serving(a, device))
     if not a.no_cpu:
-        v_cpu, el_cpu, cores = cpu_sample(a.cpu_n, a.cpu_steps)
+        n_cpu = a.cpu_n or n
+        v_cpu, el_cpu, cores = cpu_sample(n_cpu, a.cpu_steps, config=a.config, mode=a.mode)
         out["cpu_baseline"] = {"value": v_cpu, "unit": "particle-steps/s", "cores": cores, "kind": "port",
-                               "sample": f"oracle restatement (OpenMP) on the same geometry at {a.cpu_n} particles, "
+                               "sample": f"oracle restatement (OpenMP) on the same workload ({n_cpu} particles), "
                                          f"{a.cpu_steps} steps after the prologue ({el_cpu:.1f} s on {cores} threads)"}
         for k in ("batch", "serving"):
             if k in out:
@@ -519,8 +600,8 @@ def main():
 
 
 def batch_and_serving(a, device):
-    """the batched sweep (256 impacts of uneven size, 100 steps each, one context) and a window of
-    the serving loop (Poisson arrivals at 2 per second, continuous batching), both mixed precision"""
+    """the batched sweep (256 impacts of uneven size, 100 steps each, one context) and the serving
+    loop (Poisson arrivals at 2 per second, continuous batching), both mixed precision"""
     from fdps_sph_gb300 import ic, serve
     res = {}
     bt = serve.sweep(a.batch_runs, a.batch_steps, device=device)
@@ -530,14 +611,17 @@ def batch_and_serving(a, device):
                     "step_latency_s": bt["step_latency_s"], "time_to_completion_s": bt["time_to_completion_s"],
                     "config": "impacts with N log-uniform 5e3-2e5, mass ratio U[0.05, 0.5], angle U[0, 75] deg, "
                               "speed U[1, 2] v_esc, iron/dunite tables; wall time includes the host IC generation"}
-    # steps per request scaled by 1/10 (20-200) so that requests complete inside the short window;
-    # `python -m fdps_sph_gb300.serve serve --duration 600` runs the unscaled stream
-    reqs = serve.poisson_requests(4, 2.0, a.serve_s, 1e4, 5e5, 20, 200)
+    # the serving configuration as specified: Poisson arrivals at 2 per second for a.serve_s seconds,
+    # N log-uniform 1e4-5e5, steps uniform in [lo, hi]; the window ends the measurement
+    lo, hi = (int(x) for x in a.serve_steps.split(","))
+    reqs = serve.poisson_requests(4, 2.0, a.serve_s, 1e4, 5e5, lo, hi)
     srv = serve.Server("mixed", device)
     try:
-        rep = srv.run(reqs, duration=a.serve_s, drain=False)
+        with ClockSampler(device, interval_ms=1000) as clk:
+            rep = srv.run(reqs, duration=a.serve_s, drain=False)
     finally:
         srv.close()
+    offered = sum(r.steps * r.planned_n() for r in reqs)
     # the plain FP64 per-run path on a request-sized impact (100k particles), alone
     F, ids, mats, _ = ic.sweep_impact(np.random.default_rng(5), 1e5, 1e5 + 1, 5)
     ctx = serve.make_context("fp64", device)
@@ -547,16 +631,22 @@ def batch_and_serving(a, device):
     ctx.close()
     v64 = F.shape[1] * 3 / (ms * 1e-3)
     res["serving"] = {"metric": "aggregate particle-steps/s, serving loop", "value": rep["particle_steps_per_s"],
-                      "unit": "particle-steps/s", "requests_arrived": len(reqs), "completed": rep["completed"],
-                      "resident_at_end": rep["resident_at_end"], "queued_at_end": rep["queued_at_end"],
-                      "window_s": a.serve_s, "step_latency_s": rep["step_latency_s"],
-                      "time_to_completion_s": rep["time_to_completion_s"],
+                      "unit": "particle-steps/s", "requests_arrived": rep["arrived"], "admitted": rep["admitted"],
+                      "completed": rep["completed"], "resident_at_end": rep["resident_at_end"],
+                      "queued_at_end": rep["queued_at_end"], "oldest_wait_at_end_s": rep["oldest_wait_at_end_s"],
+                      "window_s": a.serve_s, "steps_per_request": [lo, hi], "batched_steps": rep["batched_steps"],
+                      "step_latency_s": rep["step_latency_s"], "time_to_completion_s": rep["time_to_completion_s"],
+                      "max_resident_particles": rep["max_resident_particles"],
+                      "offered_particle_steps": int(offered),
+                      "offered_particle_steps_per_s": offered / a.serve_s,
                       "fp64_per_run_value": v64, "vs_fp64_per_run": rep["particle_steps_per_s"] / v64,
-                      "config": "Poisson arrivals at 2/s; N log-uniform 1e4-5e5; 20-200 steps per request (the "
-                                "serving configuration's 200-2000 scaled by 1/10 to fit the window); parameters as "
-                                "the sweep; initial states built by a client thread at arrival; admission by HBM "
-                                "footprint, state resident, backfill as runs finish; the window ends the "
-                                "measurement (runs still resident are not drained)"}
+                      "clocks": clk.summary(),
+                      "config": f"Poisson arrivals at 2/s for {a.serve_s:g} s; N log-uniform 1e4-5e5; {lo}-{hi} "
+                                "steps per request; parameters as the sweep; initial states built by a client thread "
+                                "at arrival (at most 32 built ahead of admission); admission by HBM footprint, state "
+                                "resident, backfill as runs finish; the window ends the measurement (runs still "
+                                "resident or queued are counted, not drained); time to completion over the "
+                                "completed requests"}
     return res
 
 

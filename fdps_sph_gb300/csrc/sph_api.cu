@@ -675,22 +675,46 @@ int sph_set_eos_ideal(sph_ctx *ctx, int material, double gamma) {
 
 // Reader with the semantics of EoS.h:121-221 (header "# n_rho n_u", '#' lines
 // skipped, n_u rows per density block, columns rho u T P c_s S).
-int sph_load_eos_table_file(sph_ctx *ctx, int material, const char *path) {
-    if (!ctx || !path) return SPH_ERR_ARG;
-    std::ifstream in(path);
-    if (!in.is_open()) return sph_fail(ctx, SPH_ERR_TABLE, "cannot open EoS table %s", path);
-    std::string line;
+namespace {
+
+// A rho-u text table as EoS.h:121-221 reads it: a header line "# n_rho n_u", comment lines
+// skipped, n_u lines per density block, columns density, energy, temperature, pressure, sound
+// speed and (optionally) entropy.  The density axis is column 0 of each block's first line, the
+// energy axis column 1 of the first block's lines (EoS.h:218-221).
+struct RhoUTable {
     int n_rho = 0, n_u = 0;
-    if (!std::getline(in, line)) return sph_fail(ctx, SPH_ERR_TABLE, "%s: empty file", path);
+    bool six = true;   // every line has the entropy column
+    std::vector<double> rho, u, cols[6];
+};
+
+int parse_rho_u(const char *path, RhoUTable &t, std::string &err) {
+    std::ifstream in(path);
+    char buf[512];
+    if (!in.is_open()) {
+        std::snprintf(buf, sizeof buf, "cannot open EoS table %s", path);
+        err = buf;
+        return SPH_ERR_TABLE;
+    }
+    std::string line;
+    if (!std::getline(in, line)) {
+        std::snprintf(buf, sizeof buf, "%s: empty file", path);
+        err = buf;
+        return SPH_ERR_TABLE;
+    }
     {
         std::istringstream ss(line);
         std::string hash;
-        ss >> hash >> n_rho >> n_u;
-        if (hash != "#" || n_rho < 1 || n_u < 1) return sph_fail(ctx, SPH_ERR_TABLE, "%s: bad header", path);
+        ss >> hash >> t.n_rho >> t.n_u;
+        if (hash != "#" || t.n_rho < 1 || t.n_u < 1) {
+            std::snprintf(buf, sizeof buf, "%s: bad header", path);
+            err = buf;
+            return SPH_ERR_TABLE;
+        }
     }
-    const size_t nl = (size_t)n_rho * n_u;
-    std::vector<double> rho(n_rho), u(n_u), P(nl), C(nl), T(nl), S(nl), LR(nl), LU(nl);
-    bool six = true;   // every line has the temperature and entropy columns
+    const size_t nl = (size_t)t.n_rho * t.n_u;
+    t.rho.assign(t.n_rho, 0.0);
+    t.u.assign(t.n_u, 0.0);
+    for (auto &c : t.cols) c.assign(nl, 0.0);
     size_t row = 0;
     while (std::getline(in, line)) {
         if (line.empty() || line[0] == '#') continue;
@@ -699,25 +723,66 @@ int sph_load_eos_table_file(sph_ctx *ctx, int material, const char *path) {
         int k = 0;
         while (k < 6 && (ss >> v[k])) ++k;
         if (k == 0) continue;
-        if (k < 5) return sph_fail(ctx, SPH_ERR_TABLE, "%s: short row %zu", path, row);
-        if (row >= (size_t)n_rho * n_u) return sph_fail(ctx, SPH_ERR_TABLE, "%s: more rows than the header says", path);
-        const size_t li = row / n_u, ci = row % n_u;
-        if (ci == 0) rho[li] = v[0];
-        if (li == 0) u[ci] = v[1];
-        P[row] = v[3];
-        C[row] = v[4];
-        LR[row] = v[0];
-        LU[row] = v[1];
-        T[row] = v[2];
-        if (k == 6) S[row] = v[5];
-        else six = false;
+        if (k < 5) {
+            std::snprintf(buf, sizeof buf, "%s: short row %zu", path, row);
+            err = buf;
+            return SPH_ERR_TABLE;
+        }
+        if (row >= nl) {
+            std::snprintf(buf, sizeof buf, "%s: more rows than the header says", path);
+            err = buf;
+            return SPH_ERR_TABLE;
+        }
+        const size_t li = row / t.n_u, ci = row % t.n_u;
+        if (ci == 0) t.rho[li] = v[0];
+        if (li == 0) t.u[ci] = v[1];
+        for (int c = 0; c < k; ++c) t.cols[c][row] = v[c];
+        if (k < 6) t.six = false;
         ++row;
     }
-    if (row != nl) return sph_fail(ctx, SPH_ERR_TABLE, "%s: %zu rows, header says %d x %d", path, row, n_rho, n_u);
-    SPH_TRY(sph_set_eos_table(ctx, material, rho.data(), n_rho, u.data(), n_u, P.data(), C.data()));
-    if (!six) return SPH_OK;
-    return sph_set_eos_entropy(ctx, material, T.data(), S.data(), LR.data(), LU.data());
+    if (row != nl) {
+        std::snprintf(buf, sizeof buf, "%s: %zu rows, header says %d x %d", path, row, t.n_rho, t.n_u);
+        err = buf;
+        return SPH_ERR_TABLE;
+    }
+    return SPH_OK;
 }
+
+thread_local std::string g_table_err;
+
+}  // namespace
+
+int sph_load_eos_table_file(sph_ctx *ctx, int material, const char *path) {
+    if (!ctx || !path) return SPH_ERR_ARG;
+    RhoUTable t;
+    std::string err;
+    const int rc = parse_rho_u(path, t, err);
+    if (rc != SPH_OK) return sph_fail(ctx, rc, "%s", err.c_str());
+    SPH_TRY(sph_set_eos_table(ctx, material, t.rho.data(), t.n_rho, t.u.data(), t.n_u, t.cols[3].data(),
+                              t.cols[4].data()));
+    if (!t.six) return SPH_OK;
+    return sph_set_eos_entropy(ctx, material, t.cols[2].data(), t.cols[5].data(), t.cols[0].data(),
+                               t.cols[1].data());
+}
+
+int sph_read_eos_table_file(const char *path, int *n_rho, int *n_u, double *rho, double *u, double *cols,
+                            int *n_cols) {
+    if (!path || !n_rho || !n_u) return SPH_ERR_ARG;
+    RhoUTable t;
+    const int rc = parse_rho_u(path, t, g_table_err);
+    if (rc != SPH_OK) return rc;
+    *n_rho = t.n_rho;
+    *n_u = t.n_u;
+    if (n_cols) *n_cols = t.six ? 6 : 5;
+    const size_t nl = (size_t)t.n_rho * t.n_u;
+    if (rho) std::memcpy(rho, t.rho.data(), sizeof(double) * t.n_rho);
+    if (u) std::memcpy(u, t.u.data(), sizeof(double) * t.n_u);
+    if (cols)
+        for (int c = 0; c < 6; ++c) std::memcpy(cols + (size_t)c * nl, t.cols[c].data(), sizeof(double) * nl);
+    return SPH_OK;
+}
+
+const char *sph_read_eos_table_error(void) { return g_table_err.c_str(); }
 
 int sph_set_eos_tillotson(sph_ctx *ctx, int material, const double par[10]) {
     if (!ctx || !par) return SPH_ERR_ARG;

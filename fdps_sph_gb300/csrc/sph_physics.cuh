@@ -95,13 +95,16 @@ __device__ __forceinline__ double table_lookup1(const DevMaterial &m, const doub
     return plane[(int64_t)li * nu + ci];
 }
 
-// analytic Tillotson, same expressions as the oracle's or_tillotson
+// analytic Tillotson, same expressions as the oracle's or_tillotson: the branches are the
+// reference's P_co / P_ex (EoS.h:91-103) in their operation order; the regime rule (P_co when
+// rho >= rho0 or u <= uiv, P_ex when u >= ucv, linear in u between) and the sound speed
+// c^2 = dP/drho + P/rho^2 dP/du floored at 1e-2 A/rho0 are this project's definitions
 __device__ __forceinline__ void tillotson(const double *p, double rho, double u, double &P, double &cs) {
     const double rho0 = p[0], u0 = p[1], uiv = p[2], ucv = p[3], A = p[4], B = p[5], a = p[6], b = p[7],
                  alpha = p[8], beta = p[9];
     const double eta = rho / rho0;
     const double mu = eta - 1.0;
-    const double om = u / (u0 * eta * eta) + 1.0;
+    const double om = u / u0 / eta / eta + 1.0;   /* operation order of P_co / P_ex, EoS.h:91-103 */
     const double Pc = (a + b / om) * rho * u + A * mu + B * mu * mu;
     const double dPc_drho = (a + b / om) * u + 2.0 * b * u * (om - 1.0) / (om * om) + (A + 2.0 * B * mu) / rho0;
     const double dPc_du = (a + b / om) * rho - rho * b * (om - 1.0) / (om * om);
@@ -111,7 +114,7 @@ __device__ __forceinline__ void tillotson(const double *p, double rho, double u,
         dPdrho = dPc_drho;
         dPdu = dPc_du;
     } else {
-        const double z = rho0 / rho - 1.0;
+        const double z = 1.0 / eta - 1.0;
         const double E1 = exp(-alpha * z);
         const double E2 = exp(-beta * z * z);
         const double Q = b * rho * u / om + A * mu * E1;

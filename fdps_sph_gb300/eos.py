@@ -114,8 +114,10 @@ def write_rho_u(path: str, t: Table) -> None:
 
 
 def tillotson_eval(par, rho, u):
-    """Vectorised analytic Tillotson P and c_s (same expressions as the oracle's
-    or_tillotson and the device EoS kernel)."""
+    """Vectorised analytic Tillotson P and c_s: the generator of the synthetic tables.  The
+    oracle's or_tillotson and the device EoS evaluate the same formulas in the reference's
+    operation order (P_co / P_ex, EoS.h:91-103); this one keeps the order the committed
+    synthetic-table fixtures were made with (the two agree to a few ulps)."""
     rho0, u0, uiv, ucv, A, B, a, b, alpha, beta = par
     rho = np.asarray(rho, dtype=np.float64)
     u = np.asarray(u, dtype=np.float64)

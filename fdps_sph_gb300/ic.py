@@ -161,11 +161,30 @@ def config_small_impact(seed=1234, n_target=9000, n_impactor=1000):
     return make_impact(n_target, n_impactor, 0.89 * M_EARTH, 0.11 * M_EARTH, layers, layers, 45.0, 1.0, seed)
 
 
-def config_1m_impact(seed=2024, n_target=900_000, n_impactor=100_000, angle=30.0, v=1.2):
-    """1M-particle iron core / dunite mantle impact, 30 degrees at 1.2 v_esc;
-    materials 0 = iron table, 1 = dunite table (synthetic 200 x 200)."""
+def contact_separation(m_target, m_impactor, layers, overlap=0.0):
+    """sep_over_rt that starts the impactor at contact: centre distance (1 - overlap) (R_t + R_i)
+    in units of R_t (the layer radii of make_body's uniform-density shells)."""
+    Rt = _layer_radii(Body(1, m_target, layers))[-1]
+    Ri = _layer_radii(Body(1, m_impactor, layers))[-1]
+    return (1.0 - overlap) * (Rt + Ri) / Rt
+
+
+def config_1m_impact(seed=2024, n_target=900_000, n_impactor=100_000, angle=30.0, v=1.2, sep_over_rt=4.0):
+    """1M-particle iron core / dunite mantle impact, 30 degrees at 1.2 v_esc from 4 target radii
+    (``sep_over_rt``; contact_separation gives the bodies in contact); materials 0 = iron table,
+    1 = dunite table (synthetic 200 x 200)."""
     layers = [Layer(0, 0.3, 7800.0), Layer(1, 0.7, 3320.0)]
-    return make_impact(n_target, n_impactor, 0.89 * M_EARTH, 0.11 * M_EARTH, layers, layers, angle, v, seed)
+    return make_impact(n_target, n_impactor, 0.89 * M_EARTH, 0.11 * M_EARTH, layers, layers, angle, v, seed,
+                       sep_over_rt=sep_over_rt)
+
+
+def config_1m_contact(seed=2024, n_target=900_000, n_impactor=100_000, overlap=0.02):
+    """The 1M workload's bodies placed in contact (centres (1 - overlap) (R_t + R_i) apart) with the
+    contact velocity of the 30 degree, 1.2 v_esc orbit: a state whose first steps shock the
+    contact region (artificial viscosity and du/dt active)."""
+    layers = [Layer(0, 0.3, 7800.0), Layer(1, 0.7, 3320.0)]
+    sep = contact_separation(0.89 * M_EARTH, 0.11 * M_EARTH, layers, overlap)
+    return config_1m_impact(seed, n_target, n_impactor, sep_over_rt=sep)
 
 
 def config_4m_impact(seed=4096, n_target=3_600_000, n_impactor=400_000):
@@ -175,18 +194,25 @@ def config_4m_impact(seed=4096, n_target=3_600_000, n_impactor=400_000):
     return make_impact(n_target, n_impactor, 0.89 * M_EARTH, 0.11 * M_EARTH, layers, layers, 45.0, 1.0, seed)
 
 
-def sweep_impact(rng: np.random.Generator, n_lo: float, n_hi: float, seed: int):
-    """One impact of the batched sweep and of the serving stream: total particles
-    log-uniform in [n_lo, n_hi], impactor / target mass ratio U[0.05, 0.5], impact
-    angle U[0, 75] degrees, speed U[1, 2] v_esc; iron core (30%) / dunite mantle
-    bodies of one Earth mass in total, equal-mass particles; materials 0 iron,
-    1 dunite (the 1M workload's synthetic tables).  Returns (F, ids, mats, params)."""
+def sweep_draw(rng: np.random.Generator, n_lo: float, n_hi: float):
+    """The random parameters of one sweep / serving impact, in draw order: (n_target, n_impactor,
+    mass ratio, angle in degrees, speed in v_esc)."""
     n = int(round(np.exp(rng.uniform(np.log(n_lo), np.log(n_hi)))))
     q = float(rng.uniform(0.05, 0.5))
     angle = float(rng.uniform(0.0, 75.0))
     v = float(rng.uniform(1.0, 2.0))
     n_i = max(64, int(round(n * q / (1.0 + q))))
     n_t = max(64, n - n_i)
+    return n_t, n_i, q, angle, v
+
+
+def sweep_impact(rng: np.random.Generator, n_lo: float, n_hi: float, seed: int):
+    """One impact of the batched sweep and of the serving stream: total particles
+    log-uniform in [n_lo, n_hi], impactor / target mass ratio U[0.05, 0.5], impact
+    angle U[0, 75] degrees, speed U[1, 2] v_esc; iron core (30%) / dunite mantle
+    bodies of one Earth mass in total, equal-mass particles; materials 0 iron,
+    1 dunite (the 1M workload's synthetic tables).  Returns (F, ids, mats, params)."""
+    n_t, n_i, q, angle, v = sweep_draw(rng, n_lo, n_hi)
     layers = [Layer(0, 0.3, 7800.0), Layer(1, 0.7, 3320.0)]
     F, ids, mats, info = make_impact(n_t, n_i, M_EARTH / (1.0 + q), q * M_EARTH / (1.0 + q), layers, layers, angle, v,
                                      seed)

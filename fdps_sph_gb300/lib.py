@@ -40,7 +40,7 @@ EXPORTS = [
     "sph_get_counters", "sph_probe_peak", "sph_morton_order_noalloc",
     "sph_add_run", "sph_remove_run", "sph_list_runs", "sph_run_info", "sph_download_run", "sph_run_diagnostics",
     "sph_autotune", "sph_set_eos_ideal", "sph_set_eos_entropy", "sph_eos_eval", "sph_download_fields",
-    "sph_step_download",
+    "sph_step_download", "sph_read_eos_table_file", "sph_read_eos_table_error",
 ]
 # fields a step reads or carries unchanged (SPH_STEP_INPUT_FIELDS): what SPH_UPLOAD_STEP_INPUTS copies
 STEP_INPUT_FIELDS = ["x", "y", "z", "vx", "vy", "vz", "mass", "smth", "eng", "ava", "ax", "ay", "az", "eng_dot",
@@ -98,6 +98,8 @@ def load() -> C.CDLL:
     L.sph_last_error.restype = C.c_char_p
     L.sph_set_eos_table.argtypes = [P, C.c_int, P, C.c_int, P, C.c_int, P, P]
     L.sph_load_eos_table_file.argtypes = [P, C.c_int, C.c_char_p]
+    L.sph_read_eos_table_file.argtypes = [C.c_char_p, i32p, i32p, P, P, P, i32p]
+    L.sph_read_eos_table_error.restype = C.c_char_p
     L.sph_set_eos_tillotson.argtypes = [P, C.c_int, P]
     L.sph_set_eos_ideal.argtypes = [P, C.c_int, C.c_double]
     L.sph_set_eos_entropy.argtypes = [P, C.c_int, P, P, P, P]
@@ -136,6 +138,24 @@ def load() -> C.CDLL:
 
 def _ptr(a):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def read_table_file(path: str):
+    """A rho-u table file read by the library's reader (sph_read_eos_table_file: host only, the
+    reader sph_load_eos_table_file uses).  Returns (rho axis, u axis, columns [6, n_rho * n_u],
+    number of columns in the file)."""
+    L = load()
+    nr, nu, nc = C.c_int(), C.c_int(), C.c_int()
+    rc = L.sph_read_eos_table_file(path.encode(), C.byref(nr), C.byref(nu), None, None, None, C.byref(nc))
+    if rc != SPH_OK:
+        raise SphError(rc, L.sph_read_eos_table_error().decode())
+    rho = np.empty(nr.value)
+    u = np.empty(nu.value)
+    cols = np.empty((6, nr.value * nu.value))
+    rc = L.sph_read_eos_table_file(path.encode(), C.byref(nr), C.byref(nu), _ptr(rho), _ptr(u), _ptr(cols), None)
+    if rc != SPH_OK:
+        raise SphError(rc, L.sph_read_eos_table_error().decode())
+    return rho, u, cols, nc.value
 
 
 def default_config(**kw) -> Config:

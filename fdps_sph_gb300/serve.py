@@ -74,6 +74,11 @@ class Request:
         self.params = None
         self.state = None
 
+    def planned_n(self):
+        """the request's particle count, drawn from its seed without building its state"""
+        n_t, n_i, _, _, _ = ic.sweep_draw(np.random.default_rng(self.rng_seed), self.n_lo, self.n_hi)
+        return n_t + n_i
+
     def initial_state(self):
         """the request's initial particles (the client's part: built once, kept until admission)"""
         if self.state is None:
@@ -87,9 +92,15 @@ class Request:
 class Server:
     """Continuous batching of impact runs on one GPU (see the module docstring)."""
 
-    def __init__(self, precision="mixed", device=0, budget_bytes=None, max_runs=None, keep_results=False, ctx=None):
+    # initial states built ahead of admission at most: under overload the backlog is kept as
+    # arrival records and the client builds the next state once an admission frees a place
+    BUILT_AHEAD = 32
+
+    def __init__(self, precision="mixed", device=0, budget_bytes=None, max_runs=None, keep_results=False, ctx=None,
+                 built_ahead=None):
         # ctx: a context of the lib.Context run interface (add_run, step, download_run, remove_run,
-        # close); by default a new device context with the iron / dunite tables
+        # close); by default a new device context with the iron / dunite tables.  built_ahead:
+        # initial states the client may hold built before admission (default BUILT_AHEAD)
         self.ctx = ctx if ctx is not None else make_context(precision, device)
         self.budget = budget_bytes if budget_bytes is not None else hbm_budget(device)
         self.max_particles = max(1, self.budget // BYTES_PER_PARTICLE)
@@ -101,6 +112,8 @@ class Server:
         self.step_lat, self.ttc, self.completed = [], [], []
         self.particle_steps = 0
         self.steps_taken = 0
+        self.admitted = 0
+        self.built = threading.BoundedSemaphore(built_ahead or self.BUILT_AHEAD)
 
     def _fits(self, n_guess):
         if self.max_runs is not None and len(self.active) >= self.max_runs:
@@ -117,6 +130,8 @@ class Server:
             r.handle = self.ctx.add_run(F, ids, mats)
             r.state = None
             r.t_admit = now
+            self.admitted += 1
+            self.built.release()
             self.active[r.handle] = r
             self.resident += r.n
 
@@ -147,18 +162,26 @@ class Server:
 
     def run(self, requests, duration=None, drain=True):
         """requests: arrival-ordered Request list (t_arrive in seconds from the start).  A client
-        thread builds each request's initial state at its arrival time and hands it over; the
+        thread builds each request's initial state at its arrival time and hands it over, holding
+        at most BUILT_AHEAD built states that wait for admission (a later arrival is built when
+        an admission frees a place; its time to completion still counts from its arrival); the
         loop admits, steps and retires runs."""
         t0 = time.perf_counter()
         now = lambda: time.perf_counter() - t0
         arrived = queue.Queue()
         quit_ = threading.Event()
+        self.window = duration
+        self.requests = requests
 
         def client():
             for r in requests:
                 while not quit_.is_set() and now() < r.t_arrive:
                     time.sleep(min(0.01, max(0.0, r.t_arrive - now())))
                 if quit_.is_set() or (duration is not None and r.t_arrive > duration):
+                    break
+                while not quit_.is_set() and not self.built.acquire(timeout=0.05):
+                    pass
+                if quit_.is_set():
                     break
                 r.initial_state()
                 arrived.put(r)
@@ -195,11 +218,18 @@ class Server:
         return self.report(wall)
 
     def report(self, wall):
+        reqs = getattr(self, "requests", None) or []
+        horizon = min(wall, self.window) if getattr(self, "window", None) is not None else wall
+        arrived = sum(1 for r in reqs if r.t_arrive <= horizon)
+        waiting = [r for r in reqs if r.t_arrive <= horizon and r.t_admit is None]
         return {
             "wall_s": wall,
+            "arrived": arrived,
+            "admitted": self.admitted,
             "completed": len(self.completed),
             "resident_at_end": len(self.active),
-            "queued_at_end": len(self.queue),
+            "queued_at_end": len(waiting) if reqs else len(self.queue),
+            "oldest_wait_at_end_s": max((wall - r.t_arrive for r in waiting), default=0.0),
             "batched_steps": self.steps_taken,
             "particle_steps": int(self.particle_steps),
             "particle_steps_per_s": self.particle_steps / wall if wall > 0 else 0.0,
@@ -226,7 +256,7 @@ def poisson_requests(seed, rate, duration, n_lo, n_hi, steps_lo, steps_hi):
 def sweep(n_runs=256, steps=100, seed=3, n_lo=5_000, n_hi=200_000, precision="mixed", device=0):
     """The batched sweep: n_runs impacts admitted at once (as far as they fit), each for `steps` steps."""
     reqs = [Request(k, 0.0, steps, seed * 100_003 + k, n_lo, n_hi) for k in range(n_runs)]
-    srv = Server(precision, device)
+    srv = Server(precision, device, built_ahead=n_runs)
     try:
         rep = srv.run(reqs)
     finally:

@@ -153,6 +153,16 @@ int sph_set_eos_table(sph_ctx *ctx, int material, const double *rho_axis, int n_
                       int n_u, const double *pres, const double *snds);
 /* Reads a rho-u text table (EoS.h:121-221 format) into material slot `material`. */
 int sph_load_eos_table_file(sph_ctx *ctx, int material, const char *path);
+/* The same reader into host arrays, with no context and no device work (the reference's table
+ * constructor, EoS.h:121-221, reads the file the same way).  Pass null arrays first to get
+ * *n_rho, *n_u and *n_cols (6, or 5 for a file without the entropy column); then rho[n_rho]
+ * (column 0 of each density block's first line), u[n_u] (column 1 of the first block's lines)
+ * and cols[6 * n_rho * n_u], column c of file line l at cols[c * n_rho * n_u + l] (the entropy
+ * column zero when absent).  SPH_ERR_TABLE for a missing or malformed file;
+ * sph_read_eos_table_error() gives the message (per thread). */
+int sph_read_eos_table_file(const char *path, int *n_rho, int *n_u, double *rho, double *u, double *cols,
+                            int *n_cols);
+const char *sph_read_eos_table_error(void);
 /* Analytic Tillotson: rho0 u0 uiv ucv A B a b alpha beta (EoS.h:116-238 parameter order). */
 int sph_set_eos_tillotson(sph_ctx *ctx, int material, const double par[10]);
 /* Ideal gas (EoS.h:37-66) with heat-capacity ratio gamma. */

@@ -17,6 +17,7 @@
 //   balsara  : n, {div_v, rx, ry, rz, grad_smth, snds, smth}[n] -> {Bal, grad_smth, div_v}[n]
 //   integ    : n, dt, damping, record[n]             -> record_out[n]
 //   dtglobal : n, {dt, ax, ay, az, gx, gy, gz}[n]    -> dt
+//   tillotson : par[10], len, path, n, {rho,u}[n]     -> {P_co, P_ex}[n]  (cwd = reference root)
 #include "ps_shim.hpp"
 
 #include "param.h"
@@ -28,6 +29,27 @@
 #define FLAG_GI
 #include "force.h"
 #include "integral.h"
+
+// The analytic Tillotson branches P_co / P_ex (EoS.h:91-103) are private members of the
+// reference's class and never called by it.  The golden generator reads them without touching
+// the reference's headers: an explicit instantiation may name a private member ([temp.explicit]),
+// and the friend function it defines hands out the member pointer.
+namespace tillotson_access {
+using Till = EoS::Tillotson<PS::F64>;
+typedef PS::F64 (Till::*branch_fn)(PS::F64, PS::F64) const;
+template <class Tag, branch_fn M>
+struct Expose {
+    friend branch_fn member(Tag) { return M; }
+};
+struct Pco {
+    friend branch_fn member(Pco);
+};
+struct Pex {
+    friend branch_fn member(Pex);
+};
+template struct Expose<Pco, &Till::P_co>;
+template struct Expose<Pex, &Till::P_ex>;
+}  // namespace tillotson_access
 
 namespace {
 
@@ -267,6 +289,26 @@ int main(int argc, char **argv) {
             sys[i].grav = PS::F64vec(r[4], r[5], r[6]);
         }
         out.put(getTimeStepGlobal<STD::RealPtcl>(sys));
+    } else if (mode == "tillotson") {
+        // P_co and P_ex of a Tillotson object built with the given parameters (constructor order
+        // rho0 u0 uiv ucv A B a b alpha beta, EoS.h:105-107); the table file the constructor also
+        // reads does not enter them.
+        double par[10];
+        in.get(par, 10);
+        const int len = in.get<int32_t>();
+        std::string path(len, '\0');
+        in.get(&path[0], len);
+        const int n = in.get<int32_t>();
+        const tillotson_access::Till t(par[0], par[1], par[2], par[3], par[4], par[5], par[6], par[7], par[8],
+                                       par[9], path);
+        const tillotson_access::branch_fn pco = member(tillotson_access::Pco());
+        const tillotson_access::branch_fn pex = member(tillotson_access::Pex());
+        for (int i = 0; i < n; ++i) {
+            double ru[2];
+            in.get(ru, 2);
+            const double o[2] = {(t.*pco)(ru[0], ru[1]), (t.*pex)(ru[0], ru[1])};
+            out.put(o, 2);
+        }
     } else {
         std::fprintf(stderr, "unknown mode %s\n", mode.c_str());
         return 2;

@@ -107,20 +107,25 @@ double or_table_lookup(const double *rho_ax, int n_rho, const double *u_ax, int 
     return plane[(int64_t)li * n_u + ci];
 }
 
-/* Analytic Tillotson (Tillotson 1962; the formulas of EoS.h:91-103 with the
- * regime selection of the published equation: compressed or cold-expanded
- * states use P_c, hot-expanded states (u >= ucv) use P_e, and the region
- * uiv < u < ucv for rho < rho0 blends the two linearly in u).  The sound
- * speed is c^2 = dP/drho|_u + P/rho^2 dP/du|_rho of the same expressions,
- * floored at 1e-2 A/rho0.  The reference's Tillotson class itself reads a
- * table (EoS.h:241-247); this analytic mode is used when a run asks for the
+/* Analytic Tillotson.  The two branches are the reference's P_co and P_ex
+ * (EoS.h:91-103) in their operation order, pinned to the reference's own
+ * arithmetic by tests/golden/tillotson.npz.  The reference never selects
+ * between them (they are dead code there), so the regime rule is this
+ * project's, taken from the published equation the reference cites
+ * (Brundage 2013, EoS.h:226-227; Tillotson 1962): compressed (rho >= rho0) or
+ * cold-expanded (u <= uiv) states use P_co, hot-expanded states (u >= ucv)
+ * use P_ex, and the region uiv < u < ucv for rho < rho0 blends the two
+ * linearly in u.  The sound speed is also this project's definition:
+ * c^2 = dP/drho|_u + P/rho^2 dP/du|_rho of the same expressions, floored at
+ * 1e-2 A/rho0.  The reference's Tillotson class itself reads a table
+ * (EoS.h:241-247); this analytic mode is used when a run asks for the
  * Tillotson parameters rather than a table. */
 static void or_tillotson(const double *p, double rho, double u, double *P, double *cs) {
     const double rho0 = p[0], u0 = p[1], uiv = p[2], ucv = p[3], A = p[4], B = p[5], a = p[6], b = p[7],
                  alpha = p[8], beta = p[9];
     const double eta = rho / rho0;
     const double mu = eta - 1.0;
-    const double om = u / (u0 * eta * eta) + 1.0;
+    const double om = u / u0 / eta / eta + 1.0;   /* operation order of P_co / P_ex, EoS.h:91-103 */
     /* compressed branch */
     const double Pc = (a + b / om) * rho * u + A * mu + B * mu * mu;
     const double dPc_drho = (a + b / om) * u + 2.0 * b * u * (om - 1.0) / (om * om) + (A + 2.0 * B * mu) / rho0;
@@ -129,7 +134,7 @@ static void or_tillotson(const double *p, double rho, double u, double *P, doubl
     if (rho >= rho0 || u <= uiv) {
         Pv = Pc; dPdrho = dPc_drho; dPdu = dPc_du;
     } else {
-        const double z = rho0 / rho - 1.0;
+        const double z = 1.0 / eta - 1.0;
         const double E1 = exp(-alpha * z);
         const double E2 = exp(-beta * z * z);
         const double Q = b * rho * u / om + A * mu * E1;

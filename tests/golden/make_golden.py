@@ -26,6 +26,12 @@ Fixtures (npz):
                   driver are run) and the 200 x 200 synthetic dunite table;
                   plus points where the reference's lookup is undefined or
                   not finite (checked against the oracle only)
+  tillotson.npz   the analytic branches P_co / P_ex of the reference's
+                  Tillotson class (EoS.h:91-103, private and never called by
+                  the reference; read through the driver's explicit-
+                  instantiation access) with the granite (EoS.h:446) and iron
+                  (EoS.h:448) parameters, on compressed, cold-expanded,
+                  hot-expanded and blend-region points
 The particle state, the walks (group ranges and j indices) and the reference
 outputs are stored; tables are regenerated from their stored parameters.
 """
@@ -445,18 +451,69 @@ def gen_eos_mode2():
     np.savez_compressed(os.path.join(HERE, "eos_mode2.npz"), **out)
 
 
-def main():
+# region codes of tillotson.npz: which of the reference's branches a point's pressure takes
+TIL_COMPRESSED, TIL_COLD, TIL_HOT, TIL_BLEND = 0, 1, 2, 3
+
+
+def gen_tillotson(seed=20261204):
+    """P_co and P_ex of the reference's Tillotson class (EoS.h:91-103) with the granite parameters
+    (EoS.h:446) and the iron ones (EoS.h:448), on points of each region: compressed (rho >= rho0),
+    cold expanded (rho < rho0, u <= uiv), hot expanded (rho < rho0, u >= ucv) and the blend region
+    between them (rho < rho0, uiv < u < ucv).  The constructor reads the named table file, which
+    does not enter the two branches."""
+    rng = np.random.default_rng(seed)
+    out = {}
+    for name, path in (("granite", "eos/granite.rho_u.txt"), ("iron", "eos/iron___.rho_u.txt")):
+        par = np.array(eos.TILLOTSON[name], dtype=np.float64)
+        rho0, uiv, ucv = par[0], par[2], par[3]
+        m = 150
+        groups = [
+            (TIL_COMPRESSED, rho0 * rng.uniform(1.0, 3.0, m), np.exp(rng.uniform(np.log(1e3), np.log(1e9), m))),
+            (TIL_COLD, rho0 * rng.uniform(0.3, 1.0, m), rng.uniform(1e3, uiv, m)),
+            (TIL_HOT, rho0 * rng.uniform(0.05, 1.0, m), np.exp(rng.uniform(np.log(ucv), np.log(1e9), m))),
+            (TIL_BLEND, rho0 * rng.uniform(0.05, 1.0, m), rng.uniform(uiv, ucv, m)),
+        ]
+        # the region edges themselves: rho = rho0, u = uiv, u = ucv
+        edge = [(TIL_COMPRESSED, np.full(4, rho0), np.array([1e3, uiv, ucv, 1e8])),
+                (TIL_COLD, rho0 * np.array([0.5, 0.9]), np.full(2, uiv)),
+                (TIL_HOT, rho0 * np.array([0.5, 0.9]), np.full(2, ucv))]
+        region = np.concatenate([np.full(len(r), g, np.int32) for g, r, _ in groups + edge])
+        rho = np.concatenate([r for _, r, _ in groups + edge])
+        u = np.concatenate([v for _, _, v in groups + edge])
+        pb = path.encode()
+        payload = (par.astype("<f8").tobytes() + struct.pack("<i", len(pb)) + pb + struct.pack("<i", len(rho)) +
+                   np.ascontiguousarray(np.stack([rho, u], 1), dtype="<f8").tobytes())
+        o = np.frombuffer(run_ref("tillotson", payload), dtype="<f8").reshape(-1, 2)
+        out.update({f"{name}_par": par, f"{name}_rho": rho, f"{name}_u": u, f"{name}_region": region,
+                    f"{name}_P_co": o[:, 0].copy(), f"{name}_P_ex": o[:, 1].copy()})
+    np.savez_compressed(os.path.join(HERE, "tillotson.npz"), **out)
+
+
+GENERATORS = ("kernel", "eos", "functors", "integ", "eos_mode2", "tillotson")
+
+
+def main(which=GENERATORS):
     build_oracle.build()
     if not os.path.exists(DRIVER):
         raise SystemExit("reference driver not built (reference sources absent?)")
-    rng = np.random.default_rng(20261203)
-    gen_kernel(rng)
-    gen_eos(rng)
-    gen_functors()
-    gen_integ(rng)
-    gen_eos_mode2()
+    rng = np.random.default_rng(20261203)   # shared, in this order, by the first four generators
+    if "kernel" in which:
+        gen_kernel(rng)
+    if "eos" in which:
+        gen_eos(rng)
+    if "functors" in which:
+        gen_functors()
+    if "integ" in which:
+        gen_integ(rng)
+    if "eos_mode2" in which:
+        gen_eos_mode2()
+    if "tillotson" in which:
+        gen_tillotson()
     print("golden fixtures written to", HERE)
 
 
 if __name__ == "__main__":
-    main()
+    # python tests/golden/make_golden.py [generator ...]   (default: all; a generator sharing the
+    # first four's random stream regenerates only what it would have written in a full run when the
+    # generators before it run too)
+    main(tuple(sys.argv[1:]) or GENERATORS)

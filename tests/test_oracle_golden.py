@@ -214,3 +214,35 @@ def test_mode2_step_sets_entropy_energy_temperature():
         u, und = ms.internal_energy(s.mat[i], s.field("dens")[i], ent[i])
         assert not und and u == s.field("eng")[i]
         assert ms.temperature(s.mat[i], s.field("dens")[i], u) == s.field("temp")[i]
+
+
+TIL_COMPRESSED, TIL_COLD, TIL_HOT, TIL_BLEND = 0, 1, 2, 3
+
+
+def tillotson_expected(g, name):
+    """the pressure the regime rule picks from the reference's own branches (tillotson.npz):
+    P_co where compressed or cold, P_ex where hot, linear in u between them in the blend region"""
+    par = g[f"{name}_par"]
+    uiv, ucv = par[2], par[3]
+    reg, u = g[f"{name}_region"], g[f"{name}_u"]
+    pco, pex = g[f"{name}_P_co"], g[f"{name}_P_ex"]
+    blend = ((u - uiv) * pex + (ucv - u) * pco) / (ucv - uiv)
+    return np.where((reg == TIL_COMPRESSED) | (reg == TIL_COLD), pco, np.where(reg == TIL_HOT, pex, blend))
+
+
+def test_oracle_tillotson_branches_match_reference():
+    """or_tillotson's pressure against the reference's P_co / P_ex (EoS.h:91-103): 1e-14 relative
+    on every pure branch (same operations in the same order), the blend from the same two values
+    to 1e-13 of the larger branch."""
+    from fdps_sph_gb300 import eos
+    g = load("tillotson.npz")
+    for name in ("granite", "iron"):
+        ms = po.MaterialSet([eos.Tillotson(name, eos.TILLOTSON[name]).as_material()])
+        rho, u, reg = g[f"{name}_rho"], g[f"{name}_u"], g[f"{name}_region"]
+        P = np.array([ms.eval(0, r, v)[0] for r, v in zip(rho, u)])
+        want = tillotson_expected(g, name)
+        pure = reg != TIL_BLEND
+        rel = np.abs(P - want) / np.abs(want)
+        assert np.max(rel[pure]) < 1e-14, (name, float(np.max(rel[pure])))
+        scale = np.maximum(np.abs(g[f"{name}_P_co"]), np.abs(g[f"{name}_P_ex"]))
+        assert np.max((np.abs(P - want) / scale)[~pure]) < 1e-13, name
