@@ -255,15 +255,17 @@ def state_errors(a, device, materials, mixed, f64):
         del S
     S, sid, smat, t_w, step_w = mixed["state"]
     e = accuracy.compare_on_state(S, sid, smat, materials, a.theta, device, t_w)
-    e["state"] = f"the timed run's state after step {step_w} (prologue, warm-up, timed and end-to-end steps)"
+    e["state"] = (f"the state the mixed run reached after the prologue and about {step_w} steps (warm-up, "
+                  f"segment-timed, timed and end-to-end steps): bodies compressing under their own gravity")
     res["warm"] = e
     mixed.pop("state")
     e = accuracy.force_errors(mixed["first"], f64["first"])
     e["activity"] = accuracy.activity(f64["first"])
+    e["distribution"] = accuracy.error_distribution(mixed["first"], f64["first"])
     e["state"] = "the initial state's prologue (rigid bodies 4 R_t apart: no approaching pairs, du/dt = 0)"
     res["initial"] = e
     top = res.get("contact", res["warm"])
-    out = {k: v for k, v in top.items() if k not in ("activity",)}
+    out = {k: v for k, v in top.items() if k not in ("activity", "distribution")}
     out.update(res)
     out["bar"] = 1e-5
     out["note"] = ("per-quantity max over particles: density and potential relative, vectors and du/dt "
@@ -481,8 +483,9 @@ def main():
         results[prec] = dict(ms=ms, seg=seg, cnt=cnt, launches=launches, clocks=clocks, e2e=e2e, drift=dr, tune=tune,
                              first=first)
         if prec == "mixed" and not a.no_fp64:   # the state the timed steps reached, for the warm comparison
-            t_now, _, step_no = ctx.time()
-            results[prec]["state"] = ctx.download() + (t_now, step_no)
+            t_now, _, _ = ctx.time()
+            n_steps = a.warmup + 2 * a.steps + 2 + a.e2e_steps   # warm-up, segment-timed, timed, end to end
+            results[prec]["state"] = ctx.download() + (t_now, n_steps)
         ctx.close()
 
     results["mixed"]["ms"] = replica_max(results["mixed"]["ms"], dist, f"cuda:{device}")

@@ -27,29 +27,61 @@ def _vec(F, keys):
     return np.stack([F[FIELD[k]] for k in keys], 1)
 
 
-def vec_err_rms(A, B):
+def vec_err_each(A, B):
+    """per particle |A_i - B_i| / max(|B_i|, rms_k |B_k|)"""
     nb = np.linalg.norm(B, axis=1)
     rms = max(float(np.sqrt(np.mean(nb * nb))), 1e-300)
-    return float(np.max(np.linalg.norm(A - B, axis=1) / np.maximum(nb, rms)))
+    return np.linalg.norm(A - B, axis=1) / np.maximum(nb, rms)
+
+
+def scalar_err_each(a, b, floor_rms=True):
+    """per particle |a_i - b_i| / max(|b_i|, rms_k |b_k|) (floor_rms) or / |b_i|"""
+    rms = max(float(np.sqrt(np.mean(b * b))), 1e-300) if floor_rms else 1e-300
+    return np.abs(a - b) / np.maximum(np.abs(b), rms)
+
+
+def vec_err_rms(A, B):
+    return float(np.max(vec_err_each(A, B)))
 
 
 def scalar_err_rms(a, b):
-    rms = max(float(np.sqrt(np.mean(b * b))), 1e-300)
-    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), rms)))
+    return float(np.max(scalar_err_each(a, b)))
 
 
-def force_errors(Fm, Ff):
-    """per-quantity error of the field block Fm (mixed) against Ff (FP64), both in id order"""
+def _quantities(Fm, Ff):
     acc = ("ax", "ay", "az")
     grav = ("gx", "gy", "gz")
     return {
-        "dens": float(np.max(np.abs(Fm[FIELD["dens"]] - Ff[FIELD["dens"]]) / np.abs(Ff[FIELD["dens"]]))),
-        "acc_hydro": vec_err_rms(_vec(Fm, acc), _vec(Ff, acc)),
-        "eng_dot": scalar_err_rms(Fm[FIELD["eng_dot"]], Ff[FIELD["eng_dot"]]),
-        "acc_grav": vec_err_rms(_vec(Fm, grav), _vec(Ff, grav)),
-        "pot": float(np.max(np.abs(Fm[FIELD["pot"]] - Ff[FIELD["pot"]]) / np.abs(Ff[FIELD["pot"]]))),
-        "acc_total": vec_err_rms(_vec(Fm, acc) + _vec(Fm, grav), _vec(Ff, acc) + _vec(Ff, grav)),
+        "dens": (Fm[FIELD["dens"]], Ff[FIELD["dens"]], False),
+        "acc_hydro": (_vec(Fm, acc), _vec(Ff, acc), True),
+        "eng_dot": (Fm[FIELD["eng_dot"]], Ff[FIELD["eng_dot"]], True),
+        "acc_grav": (_vec(Fm, grav), _vec(Ff, grav), True),
+        "pot": (Fm[FIELD["pot"]], Ff[FIELD["pot"]], False),
+        "acc_total": (_vec(Fm, acc) + _vec(Fm, grav), _vec(Ff, acc) + _vec(Ff, grav), True),
     }
+
+
+def _each(a, b, floored):
+    return vec_err_each(a, b) if a.ndim == 2 else scalar_err_each(a, b, floored)
+
+
+def force_errors(Fm, Ff):
+    """per-quantity error of the field block Fm (mixed) against Ff (FP64), both in id order: the
+    maximum over particles (density and potential relative per particle; vectors and du/dt floored
+    at the RMS over particles)"""
+    return {k: float(np.max(_each(a, b, fl))) for k, (a, b, fl) in _quantities(Fm, Ff).items()}
+
+
+def error_distribution(Fm, Ff):
+    """the per-particle errors of force_errors as quantiles (p50, p99, p99.9, max), and the global
+    relative L2 error ||a - b|| / ||b|| over all particles, per quantity"""
+    out = {}
+    for k, (a, b, fl) in _quantities(Fm, Ff).items():
+        e = _each(a, b, fl)
+        q = np.quantile(e, [0.5, 0.99, 0.999])
+        out[k] = {"p50": float(q[0]), "p99": float(q[1]), "p99.9": float(q[2]), "max": float(np.max(e)),
+                  "l2_rel": float(np.linalg.norm(a - b) / max(float(np.linalg.norm(b)), 1e-300))}
+    return out
 
 
 def activity(F):
@@ -90,4 +122,5 @@ def compare_on_state(F, ids, mats, materials, theta=0.5, device=0, time=0.0):
     Ff = forces_of_state(F, ids, mats, materials, "fp64", theta, device, time)
     out = force_errors(Fm, Ff)
     out["activity"] = activity(Ff)
+    out["distribution"] = error_distribution(Fm, Ff)
     return out
