@@ -648,9 +648,16 @@ __global__ void __launch_bounds__(GT) k_grav32(const int *__restrict__ group_cel
 
 constexpr int GF_T = 256;
 constexpr int GF_Q = 2048;   // BFS ring of opened cell records (power of two)
-constexpr int GF_E = 2048;   // buffered EPJ particle indices
-constexpr int GF_S = 2048;   // buffered SPJ cell indices
+// buffered EPJ particle indices and SPJ cell indices, and the j entries per shared-memory tile (each
+// thread stages GF_TILE / GF_T of them per tile).  Measured at 1M (kernel time): buffers of 2048 and
+// tiles of 256 1.96 ms, 1536 and 512 1.94 ms, 1024 and 1024 2.09 ms, 2048 and 1024 (three blocks
+// per SM) 2.00 ms.
+constexpr int GF_E = 1536;
+constexpr int GF_S = 1536;
+constexpr int GF_TILE = 512;
 constexpr int GF_W = GF_T / 32;
+static_assert(GF_TILE % GF_T == 0, "tile: whole loads per thread");
+static_assert(4 * GF_TILE * 4 >= GF_T * 4 * 8 || GF_E * 4 >= GF_T * 4 * 8, "room for the partition reduction");
 
 __device__ __forceinline__ void grav_acc(float px, float py, float pz, float e2, float4 q, float &a0, float &a1,
                                          float &a2, float &a3) {
@@ -692,10 +699,12 @@ k_grav_fused32(const int *__restrict__ group_cell, const int4 *__restrict__ cinf
                const double *__restrict__ h, const float4 *__restrict__ ch, const float4 *__restrict__ cl, float gms,
                double *gx, double *gy, double *gz, double *pot, int *n_epj, int *n_spj, int *err) {
     __shared__ int4 s_q[GF_Q];
-    __shared__ __align__(16) int s_e[GF_E];   // also the reduction buffer of the partitions
+    __shared__ __align__(16) int s_e[GF_E];
     __shared__ int s_s[GF_S];
-    // the j tile as four arrays, so a thread's four consecutive entries load as two packed pairs
-    __shared__ __align__(16) float s_tx[GF_T], s_ty[GF_T], s_tz[GF_T], s_tm[GF_T];
+    // the j tile as four arrays, so a thread's four consecutive entries load as two packed pairs;
+    // also the reduction buffer of the partitions
+    __shared__ __align__(16) float s_tile[4][GF_TILE];
+    float *s_tx = s_tile[0], *s_ty = s_tile[1], *s_tz = s_tile[2], *s_tm = s_tile[3];
     __shared__ int s_w[2][GF_W][3];            // per warp: leaf particles, far children, near children
     __shared__ double s_rb[MAX_LEVELS];
     __shared__ float s_rbf[MAX_LEVELS];
@@ -754,7 +763,7 @@ k_grav_fused32(const int *__restrict__ group_cell, const int4 *__restrict__ cinf
         // partitions of 8-lane granularity (a warp may hold up to four; their tile reads then take a
         // few shared-memory wavefronts): 84-96% of the slots carry an i-particle for groups of 48-256
         const int Wt = ((cnt + 1) / 2 + 7) & ~7, P = GF_T / Wt;
-        const int TE = GF_T / (4 * P) * (4 * P);   // tile entries: a multiple of every partition's stride
+        const int TE = GF_TILE / (4 * P) * (4 * P);   // tile entries: a multiple of every partition's stride
         const int part = tid / Wt, ii = tid - part * Wt;
         const bool slot = part < P;
         float px[2], py[2], pz[2], e2[2];
@@ -910,29 +919,32 @@ k_grav_fused32(const int *__restrict__ group_cell, const int4 *__restrict__ cinf
             for (int pass = 0; pass < 2; ++pass) {
                 const int nl = pass == 0 ? ne : ns;
                 for (int t0 = 0; t0 < nl; t0 += TE) {
-                    const int kk = t0 + tid;
-                    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);   // zero mass pads the tile
-                    if (tid < TE && kk < nl) {
-                        float4 qh, ql;
-                        float gm;
-                        if (pass == 0) {
-                            const int j = s_e[kk];
-                            qh = xh[j];
-                            ql = xl[j];
-                            gm = qh.w * gms;
-                        } else {
-                            const int cc = s_s[kk];
-                            qh = ch[cc];
-                            ql = cl[cc];
-                            gm = qh.w;
+#pragma unroll
+                    for (int r = 0; r < GF_TILE / GF_T; ++r) {
+                        const int e = tid + r * GF_T, kk = t0 + e;
+                        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);   // zero mass pads the tile
+                        if (e < TE && kk < nl) {
+                            float4 qh, ql;
+                            float gm;
+                            if (pass == 0) {
+                                const int j = s_e[kk];
+                                qh = xh[j];
+                                ql = xl[j];
+                                gm = qh.w * gms;
+                            } else {
+                                const int cc = s_s[kk];
+                                qh = ch[cc];
+                                ql = cl[cc];
+                                gm = qh.w;
+                            }
+                            v = make_float4(df_diff(qh.x, ql.x, c_h.x, c_l.x), df_diff(qh.y, ql.y, c_h.y, c_l.y),
+                                            df_diff(qh.z, ql.z, c_h.z, c_l.z), gm);
                         }
-                        v = make_float4(df_diff(qh.x, ql.x, c_h.x, c_l.x), df_diff(qh.y, ql.y, c_h.y, c_l.y),
-                                        df_diff(qh.z, ql.z, c_h.z, c_l.z), gm);
+                        s_tx[e] = v.x;
+                        s_ty[e] = v.y;
+                        s_tz[e] = v.z;
+                        s_tm[e] = v.w;
                     }
-                    s_tx[tid] = v.x;
-                    s_ty[tid] = v.y;
-                    s_tz[tid] = v.z;
-                    s_tm[tid] = v.w;
                     __syncthreads();
                     if (slot) {
                         const int step = 4 * P;
@@ -965,7 +977,9 @@ k_grav_fused32(const int *__restrict__ group_cell, const int4 *__restrict__ cinf
             if (done) break;
         }
         // ---- sum the partitions of each i-particle
-        double *red = reinterpret_cast<double *>(s_e);   // GF_T x 4 doubles = the size of s_e
+        // GF_T x 4 doubles, in the tile or the EPJ buffer (whichever holds them; both are free here)
+        double *red = 4 * GF_TILE * 4 >= GF_T * 4 * 8 ? reinterpret_cast<double *>(&s_tile[0][0])
+                                                       : reinterpret_cast<double *>(s_e);
         for (int u = 0; u < 2; ++u) {
             for (int c4 = 0; c4 < 4; ++c4) red[c4 * GF_T + tid] = (double)Dh[u][c4] + (double)Dl[u][c4];
             __syncthreads();
