@@ -75,6 +75,8 @@ def parse():
     ap.add_argument("--serve-s", type=float, default=600.0, help="seconds of Poisson arrivals (2 per second)")
     ap.add_argument("--serve-steps", default="200,2000", help="steps per request, uniform in [lo, hi]")
     ap.add_argument("--no-4m", action="store_true", help="skip the 4M three-layer case at theta 0.5 / 0.7")
+    ap.add_argument("--no-multiwalk", action="store_true",
+                    help="skip the drop-in measurement through the MultiWalk dispatch / retrieve callbacks")
     ap.add_argument("--contact-steps", type=int, default=20,
                     help="mixed steps of the 1M contact state before its mixed-vs-FP64 comparison")
     return ap.parse_args()
@@ -588,6 +590,8 @@ def main():
         out["mixed_error_vs_fp64"] = state_errors(a, device, materials, mixed, f)
     if not a.no_4m and world == 1 and a.config == "1m" and a.mode == 1:
         out["config_4m"] = config_4m(device)
+    if not a.no_multiwalk and world == 1 and a.config == "1m" and a.mode == 1:
+        out["multiwalk"] = multiwalk(a, device)
     if not a.no_batch and world == 1:
         out.update(batch_and_serving(a, device))
     if not a.no_cpu:
@@ -596,10 +600,51 @@ def main():
         out["cpu_baseline"] = {"value": v_cpu, "unit": "particle-steps/s", "cores": cores, "kind": "port",
                                "sample": f"oracle restatement (OpenMP) on the same workload ({n_cpu} particles), "
                                          f"{a.cpu_steps} steps after the prologue ({el_cpu:.1f} s on {cores} threads)"}
-        for k in ("batch", "serving"):
+        for k in ("batch", "serving", "multiwalk"):
             if k in out:
                 out[k]["vs_cpu_baseline"] = out[k]["value"] / v_cpu
     print(json.dumps(out))
+
+
+def multiwalk(a, device, n_walk_limit=256, n_tags=4, steps=2):
+    """The drop-in boundary the way a host that keeps FDPS drives it: the functor calls of one step
+    (density x 4, derivative, hydro, gravity) on the walks of every gravity group of the workload's
+    prologue state, through sph_dispatch_* / sph_retrieve_* (batches of n_walk_limit walks over
+    n_tags tags, class.h payloads staged by the library, the reference functors in FP64 on the GPU).
+    The walks are built first (FDPS-style supersets, fdps_sph_gb300.walks), outside the timing."""
+    from fdps_sph_gb300 import lib, walks
+    F, ids, mats, materials = workload(a.n, config=a.config, mode=a.mode)
+    n = F.shape[1]
+    ctx = lib.Context(precision="fp64", device=device, theta=a.theta)
+    try:
+        for k, m in enumerate(materials):
+            ctx.set_material(k, m)
+        ctx.upload(F, ids, mats)
+        ctx.prologue()
+        t0 = time.perf_counter()
+        W = walks.Walks(ctx)
+        build_s = time.perf_counter() - t0
+    finally:
+        ctx.close()
+    del F
+    W.step(n_walk_limit=n_walk_limit, n_tags=n_tags)   # warm-up: the tags' streams and staging
+    runs = [W.step(n_walk_limit=n_walk_limit, n_tags=n_tags) for _ in range(steps)]
+    best = min(runs, key=lambda r: sum(r.values()))
+    t_step = sum(best.values())
+    staged = 4 * W.staged_bytes["dens"] + sum(W.staged_bytes[k] for k in ("drvt", "hydro", "grav"))
+    jl = {k: int(len(W.jlist[k][0])) for k in ("dens", "hydro", "grav")}
+    return {"metric": "particle-steps/s through the MultiWalk dispatch / retrieve callbacks",
+            "value": n / t_step, "unit": "particle-steps/s", "s_per_step": t_step,
+            "s_per_pass": {k: v for k, v in best.items()}, "groups": int(W.n_group),
+            "n_walk_limit": n_walk_limit, "tags": n_tags, "staged_bytes_per_step": int(staged),
+            "j_entries": {"gather": jl["dens"], "symmetric": jl["hydro"], "grav_epj": jl["grav"],
+                          "grav_spj": int(len(W.spj[0]))},
+            "walk_build_s": build_s,
+            "config": f"{n:,}-particle workload after its prologue; i-groups = the octree's gravity groups "
+                      "(<= 256 particles); gravity lists from the device tree (theta " + str(a.theta) + "), SPH "
+                      "j-lists = FDPS-style group supersets; one step = the functor calls of main.cpp:136-147; "
+                      "payloads staged from host memory by the library and results written back to host "
+                      "memory inside the timing; the reference functors in FP64"}
 
 
 def batch_and_serving(a, device):

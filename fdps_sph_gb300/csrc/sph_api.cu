@@ -1168,6 +1168,45 @@ int sph_get_grav_list(sph_ctx *ctx, int64_t g, int64_t *n_group, int32_t *epj, i
     return SPH_OK;
 }
 
+int sph_get_grav_lists(sph_ctx *ctx, int64_t *n_group, int64_t *n_epj_total, int64_t *n_spj_total,
+                       int32_t *group_start, int32_t *group_count, int32_t *epj_off, int32_t *epj_len, int32_t *epj,
+                       int32_t *spj_off, int32_t *spj_len, int32_t *spj_cell) {
+    if (!ctx || !n_group || !n_epj_total || !n_spj_total) return SPH_ERR_ARG;
+    const GravLists &G = ctx->grav;
+    if (!G.valid) return sph_fail(ctx, SPH_ERR_STATE, "no gravity lists (run an FP64 gravity pass first)");
+    cudaSetDevice(ctx->device);
+    const int ng = G.ng;
+    *n_group = ng;
+    std::vector<int> oe(ng), ne(ng), os(ng), ns(ng);
+    if (ng > 0) {
+        SPH_CUDA(ctx, cudaMemcpy(oe.data(), G.off_epj, sizeof(int) * ng, cudaMemcpyDeviceToHost));
+        SPH_CUDA(ctx, cudaMemcpy(ne.data(), G.n_epj, sizeof(int) * ng, cudaMemcpyDeviceToHost));
+        SPH_CUDA(ctx, cudaMemcpy(os.data(), G.off_spj, sizeof(int) * ng, cudaMemcpyDeviceToHost));
+        SPH_CUDA(ctx, cudaMemcpy(ns.data(), G.n_spj, sizeof(int) * ng, cudaMemcpyDeviceToHost));
+    }
+    const int64_t te = ng ? (int64_t)oe[ng - 1] + ne[ng - 1] : 0, ts = ng ? (int64_t)os[ng - 1] + ns[ng - 1] : 0;
+    *n_epj_total = te;
+    *n_spj_total = ts;
+    if (epj_off) std::memcpy(epj_off, oe.data(), sizeof(int) * ng);
+    if (epj_len) std::memcpy(epj_len, ne.data(), sizeof(int) * ng);
+    if (spj_off) std::memcpy(spj_off, os.data(), sizeof(int) * ng);
+    if (spj_len) std::memcpy(spj_len, ns.data(), sizeof(int) * ng);
+    if (epj && te > 0) SPH_CUDA(ctx, cudaMemcpy(epj, G.epj, sizeof(int) * te, cudaMemcpyDeviceToHost));
+    if (spj_cell && ts > 0) SPH_CUDA(ctx, cudaMemcpy(spj_cell, G.spj, sizeof(int) * ts, cudaMemcpyDeviceToHost));
+    if ((group_start || group_count) && ng > 0) {
+        const int nc = ctx->tree.n_cell_host;
+        std::vector<int> gc(ng), st(nc), ct(nc);
+        SPH_CUDA(ctx, cudaMemcpy(gc.data(), G.group_cell, sizeof(int) * ng, cudaMemcpyDeviceToHost));
+        SPH_CUDA(ctx, cudaMemcpy(st.data(), ctx->tree.start, sizeof(int) * nc, cudaMemcpyDeviceToHost));
+        SPH_CUDA(ctx, cudaMemcpy(ct.data(), ctx->tree.count, sizeof(int) * nc, cudaMemcpyDeviceToHost));
+        for (int g = 0; g < ng; ++g) {
+            if (group_start) group_start[g] = st[gc[g]];
+            if (group_count) group_count[g] = ct[gc[g]];
+        }
+    }
+    return SPH_OK;
+}
+
 int sph_get_timings(sph_ctx *ctx, double *ms, int cap, int *n) {
     if (!ctx) return SPH_ERR_ARG;
     if (cap < 0) {   // -1: switch event timing on and reset, -2: off, -3: reset

@@ -42,10 +42,19 @@ struct TagState {
     int pending_walks = 0;
     size_t pending_out_bytes = 0;
     int device = -1;
+    std::mutex mu;   // held by one dispatch or retrieve on this tag at a time
 };
 
-std::mutex g_mu;
+// Each tag has its own stream, staging and lock: calls on different tags (host threads each
+// driving their own tags) stage, launch and wait independently.
 TagState g_tags[MAX_TAGS];
+
+std::mutex *tag_mutex(int tag) { return (tag >= 0 && tag < MAX_TAGS) ? &g_tags[tag].mu : nullptr; }
+
+#define SPH_TAG_LOCK(tag)                                                                  \
+    std::mutex *tm_ = tag_mutex(tag);                                                       \
+    if (!tm_) return batch_fail(SPH_ERR_ARG, "tag out of range [0, 64)");                   \
+    std::lock_guard<std::mutex> lk(*tm_)
 
 int grow(char **h, char **d, size_t *cap, size_t need) {
     if (need <= *cap) return SPH_OK;
@@ -339,15 +348,21 @@ int stage(int tag, int kind, int n_walk, const EPI **epi, const int *n_epi, cons
         m[3] = n_epj[w];
         m[4] = as;
         m[5] = (spj && n_spj) ? n_spj[w] : 0;
-        if (n_epi[w]) std::memcpy(ts->h_in + sizeof(EPI) * ai, epi[w], sizeof(EPI) * n_epi[w]);
-        if (n_epj[w]) std::memcpy(ts->h_in + o_epj + sizeof(EPJ) * aj, epj[w], sizeof(EPJ) * n_epj[w]);
-        if (m[5]) {
-            if (!spj[w]) return batch_fail(SPH_ERR_ARG, "null SPJ walk");
-            std::memcpy(ts->h_in + o_spj + sizeof(sph_spj_monopole) * as, spj[w], sizeof(sph_spj_monopole) * m[5]);
-        }
+        if (m[5] && !spj[w]) return batch_fail(SPH_ERR_ARG, "null SPJ walk");
         ai += n_epi[w];
         aj += n_epj[w];
         as += m[5];
+    }
+    // the walks' payloads into the pinned staging, split over the host threads (a dispatch of a few
+    // hundred walks moves hundreds of MB; one thread copies at a fraction of the memory bandwidth).
+    // Inside a caller's own parallel region (FDPS's OpenMP threads) this runs on the calling thread.
+#pragma omp parallel for schedule(dynamic, 4) if (n_walk > 8 && ai + aj > 65536)
+    for (int w = 0; w < n_walk; ++w) {
+        const int64_t *m = ts->h_meta + 6 * w;
+        if (m[1]) std::memcpy(ts->h_in + sizeof(EPI) * m[0], epi[w], sizeof(EPI) * m[1]);
+        if (m[3]) std::memcpy(ts->h_in + o_epj + sizeof(EPJ) * m[2], epj[w], sizeof(EPJ) * m[3]);
+        if (m[5])
+            std::memcpy(ts->h_in + o_spj + sizeof(sph_spj_monopole) * m[4], spj[w], sizeof(sph_spj_monopole) * m[5]);
     }
     if (cudaMemcpyAsync(ts->d_in, ts->h_in, o_spj + b_spj, cudaMemcpyHostToDevice, ts->stream) != cudaSuccess ||
         cudaMemcpyAsync(ts->d_meta, ts->h_meta, sizeof(int64_t) * 6 * n_walk, cudaMemcpyHostToDevice, ts->stream) !=
@@ -376,22 +391,21 @@ int finish_dispatch(TagState *ts) {
 
 template <class RES>
 int retrieve(int tag, int kind, int n_walk, const int *n_epi, RES **result) {
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (tag < 0 || tag >= MAX_TAGS) return batch_fail(SPH_ERR_ARG, "tag out of range");
+    SPH_TAG_LOCK(tag);
     TagState &ts = g_tags[tag];
     if (ts.pending_kind != kind || ts.pending_walks != n_walk)
         return batch_fail(SPH_ERR_STATE, "retrieve does not match the last dispatch on this tag");
     const cudaError_t e = cudaStreamSynchronize(ts.stream);
     ts.pending_kind = -1;
     if (e != cudaSuccess) return batch_fail(SPH_ERR_CUDA, std::string("batch kernel failed: ") + cudaGetErrorString(e));
-    int64_t off = 0;
+    std::vector<int64_t> off(n_walk + 1, 0);
     for (int w = 0; w < n_walk; ++w) {
-        if (n_epi[w] > 0) {
-            if (!result || !result[w]) return batch_fail(SPH_ERR_ARG, "null result pointer");
-            std::memcpy(result[w], ts.h_out + sizeof(RES) * off, sizeof(RES) * n_epi[w]);
-        }
-        off += n_epi[w];
+        if (n_epi[w] > 0 && (!result || !result[w])) return batch_fail(SPH_ERR_ARG, "null result pointer");
+        off[w + 1] = off[w] + n_epi[w];
     }
+#pragma omp parallel for schedule(dynamic, 8) if (n_walk > 8 && off[n_walk] > 65536)
+    for (int w = 0; w < n_walk; ++w)
+        if (n_epi[w] > 0) std::memcpy(result[w], ts.h_out + sizeof(RES) * off[w], sizeof(RES) * n_epi[w]);
     return SPH_OK;
 }
 
@@ -403,7 +417,7 @@ const char *sph_batch_last_error(void) { return g_batch_err.c_str(); }
 
 int sph_dispatch_dens(int tag, int n_walk, const sph_epi_dens **epi, const int *n_epi, const sph_epj_dens **epj,
                       const int *n_epj) {
-    std::lock_guard<std::mutex> lk(g_mu);
+    SPH_TAG_LOCK(tag);
     TagState *ts = nullptr;
     SPH_TRY((stage<sph_epi_dens, sph_epj_dens, sph_result_dens>(tag, 0, n_walk, epi, n_epi, epj, n_epj, nullptr,
                                                                 nullptr, &ts)));
@@ -424,7 +438,7 @@ int sph_retrieve_dens(int tag, int n_walk, const int *n_epi, sph_result_dens **r
 
 int sph_dispatch_drvt(int tag, int n_walk, const sph_epi_drvt **epi, const int *n_epi, const sph_epj_drvt **epj,
                       const int *n_epj) {
-    std::lock_guard<std::mutex> lk(g_mu);
+    SPH_TAG_LOCK(tag);
     TagState *ts = nullptr;
     SPH_TRY((stage<sph_epi_drvt, sph_epj_drvt, sph_result_drvt>(tag, 1, n_walk, epi, n_epi, epj, n_epj, nullptr,
                                                                 nullptr, &ts)));
@@ -445,7 +459,7 @@ int sph_retrieve_drvt(int tag, int n_walk, const int *n_epi, sph_result_drvt **r
 
 int sph_dispatch_hydro(int tag, int n_walk, const sph_epi_hydro **epi, const int *n_epi, const sph_epj_hydro **epj,
                        const int *n_epj) {
-    std::lock_guard<std::mutex> lk(g_mu);
+    SPH_TAG_LOCK(tag);
     TagState *ts = nullptr;
     SPH_TRY((stage<sph_epi_hydro, sph_epj_hydro, sph_result_hydro>(tag, 2, n_walk, epi, n_epi, epj, n_epj, nullptr,
                                                                    nullptr, &ts)));
@@ -466,7 +480,7 @@ int sph_retrieve_hydro(int tag, int n_walk, const int *n_epi, sph_result_hydro *
 
 int sph_dispatch_grav(int tag, int n_walk, const sph_epi_grav **epi, const int *n_epi, const sph_epj_grav **epj,
                       const int *n_epj, const sph_spj_monopole **spj, const int *n_spj) {
-    std::lock_guard<std::mutex> lk(g_mu);
+    SPH_TAG_LOCK(tag);
     TagState *ts = nullptr;
     SPH_TRY((stage<sph_epi_grav, sph_epj_grav, sph_result_grav>(tag, 3, n_walk, epi, n_epi, epj, n_epj, spj, n_spj,
                                                                 &ts)));

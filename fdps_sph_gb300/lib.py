@@ -40,7 +40,7 @@ EXPORTS = [
     "sph_get_counters", "sph_probe_peak", "sph_morton_order_noalloc",
     "sph_add_run", "sph_remove_run", "sph_list_runs", "sph_run_info", "sph_download_run", "sph_run_diagnostics",
     "sph_autotune", "sph_set_eos_ideal", "sph_set_eos_entropy", "sph_eos_eval", "sph_download_fields",
-    "sph_step_download", "sph_read_eos_table_file", "sph_read_eos_table_error",
+    "sph_step_download", "sph_read_eos_table_file", "sph_read_eos_table_error", "sph_get_grav_lists",
 ]
 # fields a step reads or carries unchanged (SPH_STEP_INPUT_FIELDS): what SPH_UPLOAD_STEP_INPUTS copies
 STEP_INPUT_FIELDS = ["x", "y", "z", "vx", "vy", "vz", "mass", "smth", "eng", "ava", "ax", "ay", "az", "eng_dot",
@@ -132,6 +132,8 @@ def load() -> C.CDLL:
     L.sph_download_run.argtypes = [P, C.c_int64, P, C.c_int64, P, P]
     L.sph_run_diagnostics.argtypes = [P, C.c_int64, P]
     L.sph_autotune.argtypes = [P, C.c_int, P]
+    i64p = C.POINTER(C.c_int64)
+    L.sph_get_grav_lists.argtypes = [P, i64p, i64p, i64p, P, P, P, P, P, P, P, P]
     _lib = L
     return L
 
@@ -400,6 +402,24 @@ class Context:
                                              _ptr(st), len(st), C.byref(ns), _ptr(gs), _ptr(gcnt)))
         return dict(start=int(gs[0]), count=int(gcnt[0]), epj=epj[:ne.value].copy(), spj_level=lev[:ns.value].copy(),
                     spj_start=st[:ns.value].copy())
+
+    def grav_lists(self):
+        """every gravity list of the last FP64 gravity pass: group start / count (sorted indices), EPJ
+        runs (offset, length, sorted particle indices) and SPJ runs (offset, length, cell indices)"""
+        ng, te, ts = C.c_int64(), C.c_int64(), C.c_int64()
+        self._check(self.L.sph_get_grav_lists(self.h, C.byref(ng), C.byref(te), C.byref(ts), None, None, None, None,
+                                              None, None, None, None))
+        g = ng.value
+        out = {k: np.empty(g, np.int32) for k in ("start", "count", "epj_off", "epj_len", "spj_off", "spj_len")}
+        out["epj"] = np.empty(max(1, te.value), np.int32)
+        out["spj"] = np.empty(max(1, ts.value), np.int32)
+        self._check(self.L.sph_get_grav_lists(self.h, C.byref(ng), C.byref(te), C.byref(ts), _ptr(out["start"]),
+                                              _ptr(out["count"]), _ptr(out["epj_off"]), _ptr(out["epj_len"]),
+                                              _ptr(out["epj"]), _ptr(out["spj_off"]), _ptr(out["spj_len"]),
+                                              _ptr(out["spj"])))
+        out["epj"] = out["epj"][:te.value]
+        out["spj"] = out["spj"][:ts.value]
+        return out
 
     def enable_timing(self, on=True):
         self._check(self.L.sph_get_timings(self.h, None, -1 if on else -2, None))

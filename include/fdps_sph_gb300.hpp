@@ -15,6 +15,7 @@
 //    the step of main.cpp:125-173 on the GPU.
 #pragma once
 
+#include <atomic>
 #include <mutex>
 #include <stdexcept>
 #include <string>
@@ -28,11 +29,19 @@ namespace detail {
 inline void check_batch(int rc, const char *what) {
     if (rc != SPH_OK) throw std::runtime_error(std::string(what) + ": " + sph_batch_last_error());
 }
-// FDPS calls functors from several OpenMP threads at once; each wrapper call
-// holds this lock across its dispatch / retrieve pair on the shared tags.
-inline std::mutex &functor_lock() {
-    static std::mutex m;
-    return m;
+// FDPS calls functors from several OpenMP threads at once.  Each calling thread
+// takes a tag of its own (8 .. 63, round robin; 0 .. 7 stay free for a host's
+// own MultiWalk dispatch / retrieve), so the threads' walks overlap on the GPU,
+// one stream per tag.  A wrapper call holds its tag's lock across its dispatch
+// / retrieve pair, which matters only when more than 56 threads share tags.
+inline int thread_tag() {
+    static std::atomic<int> next{0};
+    thread_local const int tag = 8 + next.fetch_add(1) % 56;
+    return tag;
+}
+inline std::mutex &tag_lock(int tag) {
+    static std::mutex m[64];
+    return m[tag];
 }
 template <class T, class C>
 constexpr bool same_layout() {
@@ -51,9 +60,10 @@ struct CalcDensity {   // force.h:6-24
         const sph_epi_dens *pi = reinterpret_cast<const sph_epi_dens *>(ep_i);
         const sph_epj_dens *pj = reinterpret_cast<const sph_epj_dens *>(ep_j);
         sph_result_dens *out = reinterpret_cast<sph_result_dens *>(dens);
-        std::lock_guard<std::mutex> lk(detail::functor_lock());
-        detail::check_batch(sph_dispatch_dens(0, 1, &pi, &n_i, &pj, &n_j), "CalcDensity");
-        detail::check_batch(sph_retrieve_dens(0, 1, &n_i, &out), "CalcDensity");
+        const int tag = detail::thread_tag();
+        std::lock_guard<std::mutex> lk(detail::tag_lock(tag));
+        detail::check_batch(sph_dispatch_dens(tag, 1, &pi, &n_i, &pj, &n_j), "CalcDensity");
+        detail::check_batch(sph_retrieve_dens(tag, 1, &n_i, &out), "CalcDensity");
     }
 };
 
@@ -66,9 +76,10 @@ struct CalcDerivative {   // force.h:86-107
         const sph_epi_drvt *pi = reinterpret_cast<const sph_epi_drvt *>(ep_i);
         const sph_epj_drvt *pj = reinterpret_cast<const sph_epj_drvt *>(ep_j);
         sph_result_drvt *out = reinterpret_cast<sph_result_drvt *>(drvt);
-        std::lock_guard<std::mutex> lk(detail::functor_lock());
-        detail::check_batch(sph_dispatch_drvt(1, 1, &pi, &n_i, &pj, &n_j), "CalcDerivative");
-        detail::check_batch(sph_retrieve_drvt(1, 1, &n_i, &out), "CalcDerivative");
+        const int tag = detail::thread_tag();
+        std::lock_guard<std::mutex> lk(detail::tag_lock(tag));
+        detail::check_batch(sph_dispatch_drvt(tag, 1, &pi, &n_i, &pj, &n_j), "CalcDerivative");
+        detail::check_batch(sph_retrieve_drvt(tag, 1, &n_i, &out), "CalcDerivative");
     }
 };
 
@@ -81,9 +92,10 @@ struct CalcHydroForce {   // force.h:109-148
         const sph_epi_hydro *pi = reinterpret_cast<const sph_epi_hydro *>(ep_i);
         const sph_epj_hydro *pj = reinterpret_cast<const sph_epj_hydro *>(ep_j);
         sph_result_hydro *out = reinterpret_cast<sph_result_hydro *>(hydro);
-        std::lock_guard<std::mutex> lk(detail::functor_lock());
-        detail::check_batch(sph_dispatch_hydro(2, 1, &pi, &n_i, &pj, &n_j), "CalcHydroForce");
-        detail::check_batch(sph_retrieve_hydro(2, 1, &n_i, &out), "CalcHydroForce");
+        const int tag = detail::thread_tag();
+        std::lock_guard<std::mutex> lk(detail::tag_lock(tag));
+        detail::check_batch(sph_dispatch_hydro(tag, 1, &pi, &n_i, &pj, &n_j), "CalcHydroForce");
+        detail::check_batch(sph_retrieve_hydro(tag, 1, &n_i, &out), "CalcHydroForce");
     }
 };
 
@@ -104,17 +116,18 @@ struct CalcGravityForce {
         std::vector<sph_result_grav> tmp(n_i > 0 ? n_i : 1);
         sph_result_grav *out = tmp.data();
         const int zero = 0;
-        std::lock_guard<std::mutex> lk(detail::functor_lock());
+        const int tag = detail::thread_tag();
+        std::lock_guard<std::mutex> lk(detail::tag_lock(tag));
         if (sizeof(TPtclJ) == sizeof(sph_epj_grav)) {
             const sph_epj_grav *pj = reinterpret_cast<const sph_epj_grav *>(ep_j);
             const sph_spj_monopole *ps = nullptr;
-            detail::check_batch(sph_dispatch_grav(3, 1, &pi, &n_i, &pj, &n_j, &ps, &zero), "CalcGravityForce");
+            detail::check_batch(sph_dispatch_grav(tag, 1, &pi, &n_i, &pj, &n_j, &ps, &zero), "CalcGravityForce");
         } else {
             const sph_epj_grav *pj = nullptr;
             const sph_spj_monopole *ps = reinterpret_cast<const sph_spj_monopole *>(ep_j);
-            detail::check_batch(sph_dispatch_grav(3, 1, &pi, &n_i, &pj, &zero, &ps, &n_j), "CalcGravityForce");
+            detail::check_batch(sph_dispatch_grav(tag, 1, &pi, &n_i, &pj, &zero, &ps, &n_j), "CalcGravityForce");
         }
-        detail::check_batch(sph_retrieve_grav(3, 1, &n_i, &out), "CalcGravityForce");
+        detail::check_batch(sph_retrieve_grav(tag, 1, &n_i, &out), "CalcGravityForce");
         sph_result_grav *g = reinterpret_cast<sph_result_grav *>(grav);
         for (int i = 0; i < n_i; ++i) {   // acc -= ..., pot -= ... accumulate into the caller's result
             g[i].acc[0] += out[i].acc[0];

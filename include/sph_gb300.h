@@ -303,6 +303,14 @@ int sph_get_tree(sph_ctx *ctx, int64_t *n_cell, int32_t *start, int32_t *count, 
 int sph_get_grav_list(sph_ctx *ctx, int64_t g, int64_t *n_group, int32_t *epj, int64_t cap_epj, int64_t *n_epj,
                       int32_t *spj_level, int32_t *spj_start, int64_t cap_spj, int64_t *n_spj,
                       int32_t *group_start, int32_t *group_count);
+/* Every gravity interaction list of the last FP64 gravity pass in a few copies (tooling: a host
+ * that builds calcForceAllAndWriteBackMultiWalk walks from the device's tree).  Per group g: its
+ * first sorted particle and count, and the offset and length of its EPJ run (sorted particle
+ * indices in epj) and SPJ run (cell indices into sph_get_tree's arrays in spj_cell).  Null arrays
+ * are skipped; *n_group, *n_epj_total and *n_spj_total are always written. */
+int sph_get_grav_lists(sph_ctx *ctx, int64_t *n_group, int64_t *n_epj_total, int64_t *n_spj_total,
+                       int32_t *group_start, int32_t *group_count, int32_t *epj_off, int32_t *epj_len, int32_t *epj,
+                       int32_t *spj_off, int32_t *spj_len, int32_t *spj_cell);
 /* Device time (CUDA events on the context's stream) accumulated per segment
  * since the last reset, in this order: kick-drift-predict, octree levels and
  * moments, density lists, density kernels, EoS, derivative list, derivative

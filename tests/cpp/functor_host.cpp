@@ -5,6 +5,8 @@
 // results.
 #include <cstdint>
 #include <cstdio>
+#include <cstring>
+#include <thread>
 #include <vector>
 
 #include "fdps_sph_gb300.hpp"
@@ -84,6 +86,29 @@ int main(int argc, char **argv) {
     sph_gb300::CalcGravityForce<PS::SPJMonopole>()(gi.data(), (PS::S32)gi.size(), gs.data(), (PS::S32)gs.size(),
                                                     gr.data());
     std::fwrite(gr.data(), sizeof(gr[0]), gr.size(), out);
+    // the density and hydro functors called from eight threads at once, as FDPS's OpenMP threads
+    // call them: every thread's results equal the single-threaded ones bit for bit
+    const int n_thr = 8, reps = 20;
+    std::vector<std::vector<STD::RESULT::Dens>> tdr(n_thr, dr);
+    std::vector<std::vector<STD::RESULT::Hydro>> thr_(n_thr, hr);
+    std::vector<int> bad(n_thr, 0);
+    std::vector<std::thread> pool;
+    for (int t = 0; t < n_thr; ++t)
+        pool.emplace_back([&, t]() {
+            for (int r = 0; r < reps; ++r) {
+                std::vector<STD::RESULT::Dens> a(di.size(), STD::RESULT::Dens{0, 0});
+                sph_gb300::CalcDensity()(di.data(), (PS::S32)di.size(), dj.data(), (PS::S32)dj.size(), a.data());
+                std::vector<STD::RESULT::Hydro> b(hi.size());
+                sph_gb300::CalcHydroForce()(hi.data(), (PS::S32)hi.size(), hj.data(), (PS::S32)hj.size(), b.data());
+                if (std::memcmp(a.data(), dr.data(), sizeof(a[0]) * a.size()) != 0 ||
+                    std::memcmp(b.data(), hr.data(), sizeof(b[0]) * b.size()) != 0)
+                    bad[t] = 1;
+            }
+        });
+    for (auto &th : pool) th.join();
+    int n_bad = 0;
+    for (int t = 0; t < n_thr; ++t) n_bad += bad[t];
+    std::fwrite(&n_bad, sizeof(n_bad), 1, out);
     std::fclose(in);
     std::fclose(out);
     return 0;

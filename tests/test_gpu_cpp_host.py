@@ -1,7 +1,8 @@
 """The C++ host surface (include/fdps_sph_gb300.hpp) used the way the
 reference's host code calls its functors: a program with class.h-shaped
 payload types calls CalcDensity / CalcHydroForce / CalcGravityForce on golden
-walks; results must match the reference functors' (tests/golden)."""
+walks; results must match the reference functors' (tests/golden), also when
+eight threads call the functors at once."""
 import os
 import struct
 import subprocess
@@ -24,7 +25,7 @@ def _walk(fun, key, w):
 def test_cpp_functors_match_reference(tmp_path):
     lib = build.build()
     exe = str(tmp_path / "functor_host")
-    subprocess.run(["g++", "-std=c++14", "-O2", "-I", os.path.join(ROOT, "include"),
+    subprocess.run(["g++", "-std=c++14", "-O2", "-pthread", "-I", os.path.join(ROOT, "include"),
                     os.path.join(ROOT, "tests", "cpp", "functor_host.cpp"), "-o", exe, "-L", os.path.dirname(lib),
                     "-lsph_gb300", f"-Wl,-rpath,{os.path.dirname(lib)}"], check=True)
     fun = load_golden("functors.npz")
@@ -86,6 +87,10 @@ def test_cpp_functors_match_reference(tmp_path):
     hres = np.frombuffer(raw[o:o + n2 * 40], T.RES_HYDRO)
     o += n2 * 40
     g = np.frombuffer(raw[o:o + n3 * 40], T.RES_GRAV)
+    o += n3 * 40
+    # eight threads calling the density and hydro functors concurrently (each on a tag of its own)
+    # got the single-threaded results bit for bit
+    assert np.frombuffer(raw[o:o + 4], np.int32)[0] == 0
     assert rel_err(d["dens"], dens_ref["dens"], 1e-300) < 1e-12
     assert rel_err(d["smth"], dens_ref["smth"], 1e-300) < 1e-12
     assert vec_rel_err(hres["acc"], hyd_ref["acc"], 1e-6) < 1e-10
