@@ -9,6 +9,7 @@
 // CPU.  One CTA per walk; the walk's j-list is staged through shared memory
 // in tiles and read by every thread (one thread per i).
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -18,7 +19,18 @@
 
 using namespace sph;
 
+namespace sph {
+// the mixed-precision functor kernels (sph_batch32.cu)
+void batch32_dens(int n_walk, cudaStream_t st, const int64_t *meta, const void *epi, const void *epj, void *res);
+void batch32_drvt(int n_walk, cudaStream_t st, const int64_t *meta, const void *epi, const void *epj, void *res);
+void batch32_hydro(int n_walk, cudaStream_t st, const int64_t *meta, const void *epi, const void *epj, void *res);
+void batch32_grav(int n_walk, cudaStream_t st, const int64_t *meta, const void *epi, const void *epj,
+                  const void *spj, void *res);
+}  // namespace sph
+
 namespace {
+
+std::atomic<int> g_batch_prec{SPH_PREC_FP64};   // the arithmetic of the next dispatches
 
 constexpr int MAX_TAGS = 64;
 constexpr int WT = 128;
@@ -415,6 +427,13 @@ extern "C" {
 
 const char *sph_batch_last_error(void) { return g_batch_err.c_str(); }
 
+int sph_batch_set_precision(int precision) {
+    if (precision != SPH_PREC_FP64 && precision != SPH_PREC_MIXED)
+        return batch_fail(SPH_ERR_ARG, "precision must be SPH_PREC_FP64 or SPH_PREC_MIXED");
+    g_batch_prec.store(precision);
+    return SPH_OK;
+}
+
 int sph_dispatch_dens(int tag, int n_walk, const sph_epi_dens **epi, const int *n_epi, const sph_epj_dens **epj,
                       const int *n_epj) {
     SPH_TAG_LOCK(tag);
@@ -425,9 +444,12 @@ int sph_dispatch_dens(int tag, int n_walk, const sph_epi_dens **epi, const int *
         int64_t ni = 0;
         for (int w = 0; w < n_walk; ++w) ni += n_epi[w];
         const size_t o_epj = (sizeof(sph_epi_dens) * ni + 15) & ~size_t(15);
-        k_walk_dens<<<n_walk, WT, 0, ts->stream>>>(ts->d_meta, (const sph_epi_dens *)ts->d_in,
-                                                   (const sph_epj_dens *)(ts->d_in + o_epj),
-                                                   (sph_result_dens *)ts->d_out);
+        if (g_batch_prec.load() == SPH_PREC_MIXED)
+            batch32_dens(n_walk, ts->stream, ts->d_meta, ts->d_in, ts->d_in + o_epj, ts->d_out);
+        else
+            k_walk_dens<<<n_walk, WT, 0, ts->stream>>>(ts->d_meta, (const sph_epi_dens *)ts->d_in,
+                                                       (const sph_epj_dens *)(ts->d_in + o_epj),
+                                                       (sph_result_dens *)ts->d_out);
     }
     return finish_dispatch(ts);
 }
@@ -446,9 +468,12 @@ int sph_dispatch_drvt(int tag, int n_walk, const sph_epi_drvt **epi, const int *
         int64_t ni = 0;
         for (int w = 0; w < n_walk; ++w) ni += n_epi[w];
         const size_t o_epj = (sizeof(sph_epi_drvt) * ni + 15) & ~size_t(15);
-        k_walk_drvt<<<n_walk, WT, 0, ts->stream>>>(ts->d_meta, (const sph_epi_drvt *)ts->d_in,
-                                                   (const sph_epj_drvt *)(ts->d_in + o_epj),
-                                                   (sph_result_drvt *)ts->d_out);
+        if (g_batch_prec.load() == SPH_PREC_MIXED)
+            batch32_drvt(n_walk, ts->stream, ts->d_meta, ts->d_in, ts->d_in + o_epj, ts->d_out);
+        else
+            k_walk_drvt<<<n_walk, WT, 0, ts->stream>>>(ts->d_meta, (const sph_epi_drvt *)ts->d_in,
+                                                       (const sph_epj_drvt *)(ts->d_in + o_epj),
+                                                       (sph_result_drvt *)ts->d_out);
     }
     return finish_dispatch(ts);
 }
@@ -467,9 +492,12 @@ int sph_dispatch_hydro(int tag, int n_walk, const sph_epi_hydro **epi, const int
         int64_t ni = 0;
         for (int w = 0; w < n_walk; ++w) ni += n_epi[w];
         const size_t o_epj = (sizeof(sph_epi_hydro) * ni + 15) & ~size_t(15);
-        k_walk_hydro<<<n_walk, WT, 0, ts->stream>>>(ts->d_meta, (const sph_epi_hydro *)ts->d_in,
-                                                    (const sph_epj_hydro *)(ts->d_in + o_epj),
-                                                    (sph_result_hydro *)ts->d_out);
+        if (g_batch_prec.load() == SPH_PREC_MIXED)
+            batch32_hydro(n_walk, ts->stream, ts->d_meta, ts->d_in, ts->d_in + o_epj, ts->d_out);
+        else
+            k_walk_hydro<<<n_walk, WT, 0, ts->stream>>>(ts->d_meta, (const sph_epi_hydro *)ts->d_in,
+                                                        (const sph_epj_hydro *)(ts->d_in + o_epj),
+                                                        (sph_result_hydro *)ts->d_out);
     }
     return finish_dispatch(ts);
 }
@@ -492,10 +520,13 @@ int sph_dispatch_grav(int tag, int n_walk, const sph_epi_grav **epi, const int *
         }
         const size_t o_epj = (sizeof(sph_epi_grav) * ni + 15) & ~size_t(15);
         const size_t o_spj = (o_epj + sizeof(sph_epj_grav) * nj + 15) & ~size_t(15);
-        k_walk_grav<<<n_walk, WT, 0, ts->stream>>>(ts->d_meta, (const sph_epi_grav *)ts->d_in,
-                                                   (const sph_epj_grav *)(ts->d_in + o_epj),
-                                                   (const sph_spj_monopole *)(ts->d_in + o_spj),
-                                                   (sph_result_grav *)ts->d_out);
+        if (g_batch_prec.load() == SPH_PREC_MIXED)
+            batch32_grav(n_walk, ts->stream, ts->d_meta, ts->d_in, ts->d_in + o_epj, ts->d_in + o_spj, ts->d_out);
+        else
+            k_walk_grav<<<n_walk, WT, 0, ts->stream>>>(ts->d_meta, (const sph_epi_grav *)ts->d_in,
+                                                       (const sph_epj_grav *)(ts->d_in + o_epj),
+                                                       (const sph_spj_monopole *)(ts->d_in + o_spj),
+                                                       (sph_result_grav *)ts->d_out);
     }
     return finish_dispatch(ts);
 }

@@ -244,10 +244,7 @@ __global__ void __launch_bounds__(GT) k_grav64(const int *__restrict__ group_cel
 // ---------------------------------------------------------------------------
 // Mixed precision: double-float packing
 
-__device__ __forceinline__ void split_df(double v, float &hi, float &lo) {
-    hi = (float)v;
-    lo = (float)(v - (double)hi);
-}
+// split_df: sph_physics.cuh
 
 // positions + scaled mass, velocities + h; called after the sort (and h refresh)
 __global__ void k_pack_df(int n, const double *x, const double *y, const double *z, const double *vx,

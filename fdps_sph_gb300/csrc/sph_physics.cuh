@@ -28,6 +28,12 @@ __device__ __forceinline__ void wendland_poly(double s, double &w, double &g) {
     g = -22.0 * s * (1.0 + s * (7.0 + s * 16.0)) * p7;
 }
 
+// a double as a double-float: hi = the nearest float, lo = the nearest float to the remainder
+__device__ __forceinline__ void split_df(double v, float &hi, float &lo) {
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+}
+
 __device__ __forceinline__ void wendland_poly_f(float s, float &w, float &g) {
     const float p = fmaxf(1.0f - s, 0.0f);
     const float poly = 1.0f + s * (8.0f + s * (25.0f + s * 32.0f));

@@ -41,6 +41,7 @@ EXPORTS = [
     "sph_add_run", "sph_remove_run", "sph_list_runs", "sph_run_info", "sph_download_run", "sph_run_diagnostics",
     "sph_autotune", "sph_set_eos_ideal", "sph_set_eos_entropy", "sph_eos_eval", "sph_download_fields",
     "sph_step_download", "sph_read_eos_table_file", "sph_read_eos_table_error", "sph_get_grav_lists",
+    "sph_batch_set_precision",
 ]
 # fields a step reads or carries unchanged (SPH_STEP_INPUT_FIELDS): what SPH_UPLOAD_STEP_INPUTS copies
 STEP_INPUT_FIELDS = ["x", "y", "z", "vx", "vy", "vz", "mass", "smth", "eng", "ava", "ax", "ay", "az", "eng_dot",
@@ -90,6 +91,7 @@ def load() -> C.CDLL:
     L.sph_dispatch_grav.argtypes = [C.c_int, C.c_int, P, i32p, P, i32p, P, i32p]
     L.sph_retrieve_grav.argtypes = [C.c_int, C.c_int, i32p, P]
     L.sph_batch_last_error.restype = C.c_char_p
+    L.sph_batch_set_precision.argtypes = [C.c_int]
     L.sph_config_default.argtypes = [C.POINTER(Config)]
     L.sph_config_default.restype = None
     L.sph_ctx_create.argtypes = [C.POINTER(Config), C.POINTER(C.c_void_p)]
@@ -496,6 +498,15 @@ def retrieve(kind: str, tag: int, n_epi):
     if rc != SPH_OK:
         raise SphError(rc, L.sph_batch_last_error().decode())
     return outs
+
+
+def batch_precision(precision: str):
+    """arithmetic of the batch entry points' next dispatches: "fp64" (the reference functors) or
+    "mixed" (sph_batch_set_precision)"""
+    L = load()
+    rc = L.sph_batch_set_precision(PREC_MIXED if precision == "mixed" else PREC_FP64)
+    if rc != SPH_OK:
+        raise SphError(rc, L.sph_batch_last_error().decode())
 
 
 def run_walks(kind: str, epi_list, epj_list, spj_list=None, tag: int = 0):

@@ -94,6 +94,12 @@ int sph_dispatch_grav(int tag, int n_walk, const sph_epi_grav **epi, const int *
 int sph_retrieve_grav(int tag, int n_walk, const int *n_epi, sph_result_grav **result);
 /* message of the last failed batch call on this thread */
 const char *sph_batch_last_error(void);
+/* Arithmetic of the dispatches that follow (all tags): SPH_PREC_FP64 (default) runs the reference
+ * functors in FP64; SPH_PREC_MIXED runs the same walks with the pair terms in FP32 on coordinates
+ * and velocities relative to each walk's first i-particle (double-float), compensated FP32 sums and
+ * FP64 per-particle epilogues -- the device-resident mixed path's arithmetic, within 1e-5 of FP64
+ * on the functors' results.  No counterpart in the reference (its functors are FP64). */
+int sph_batch_set_precision(int precision);
 
 /* ---- 2. device-resident whole-pass API ----------------------------------- */
 

@@ -132,3 +132,29 @@ def test_batch_empty_and_ragged_walks():
     # an empty j-list gives the FLAG_GI floor (force.h:18-20)
     assert out[1]["dens"][0] == 5.0
     assert lib.run_walks("dens", [], [], tag=7) == []
+
+
+def test_batch_mixed_precision_within_bar(fun):
+    """sph_batch_set_precision(SPH_PREC_MIXED): the same golden walks, FP32 pair terms on
+    walk-relative double-float coordinates, within the mixed path's 1e-5 of the reference functors
+    (density and h relative per particle; vectors, du/dt and div v floored at the RMS); dt (a
+    maximum of v_sig, no cancellation) to 1e-6.  The precision goes back to FP64 afterwards."""
+    from fdps_sph_gb300 import lib
+    from helpers import scalar_err_rms, vec_err_rms
+    lib.batch_precision("mixed")
+    try:
+        d = run("dens", fun, "dens", "state_dens", DENS_I, DENS_J, T.EPI_DENS, T.EPJ_DENS)
+        v = run("drvt", fun, "drvt", "state_drvt", DRVT_I, DRVT_J, T.EPI_DRVT, T.EPJ_DRVT)
+        h = run("hydro", fun, "hydro", "state_hydro", HYD_I, HYD_J, T.EPI_HYDRO, T.EPJ_HYDRO)
+    finally:
+        lib.batch_precision("fp64")
+    assert rel_err(d["dens"], fun["ref_dens"]["dens"], 1e-300) < 1e-5
+    assert rel_err(d["smth"], fun["ref_dens"]["smth"], 1e-300) < 1e-5
+    rv = fun["ref_drvt"]
+    assert scalar_err_rms(v["div_v"], rv["div_v"]) < 1e-5
+    assert vec_err_rms(v["rot_v"], rv["rot_v"]) < 1e-5
+    assert rel_err(v["grad_smth"], rv["grad_smth"], 1e-300) < 1e-5
+    rh = fun["ref_hydro_superset"]
+    assert vec_err_rms(h["acc"], rh["acc"]) < 1e-5
+    assert scalar_err_rms(h["eng_dot"], rh["eng_dot"]) < 1e-5
+    assert rel_err(h["dt"], rh["dt"], 1e-300) < 1e-6

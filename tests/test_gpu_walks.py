@@ -41,3 +41,29 @@ def test_multiwalk_matches_the_device_resident_forces():
     # the density walks run too (their result is the next density pass of the state's h)
     W.run("dens", n_walk_limit=16, n_tags=3)
     assert np.all(W.result["dens"]["dens"] > 0)
+
+
+def test_multiwalk_mixed_precision_within_bar():
+    """the same walks with sph_batch_set_precision(SPH_PREC_MIXED): gravity, hydro acceleration and
+    du/dt and div v within 1e-5 of the FP64 context (floored at the RMS)"""
+    F, ids, mats, _ = small_impact(18000, 2000, seed=42)
+    ctx = device_context(tillotson_materials(), precision=lib.PREC_FP64)
+    try:
+        ctx.upload(F, ids, mats)
+        ctx.prologue()
+        W = walks.Walks(ctx)
+    finally:
+        ctx.close()
+    S = W.sorted_state
+    lib.batch_precision("mixed")
+    try:
+        for kind in ("drvt", "hydro", "grav"):
+            W.run(kind, n_walk_limit=64, n_tags=2)
+    finally:
+        lib.batch_precision("fp64")
+    g, hres, d = W.result["grav"], W.result["hydro"], W.result["drvt"]
+    assert vec_err_rms(g["acc"], np.stack([S[FIELD[c]] for c in ("gx", "gy", "gz")], 1)) < 1e-5
+    assert scalar_err_rms(g["pot"], S[FIELD["pot"]]) < 1e-5
+    assert vec_err_rms(hres["acc"], np.stack([S[FIELD[c]] for c in ("ax", "ay", "az")], 1)) < 1e-5
+    assert scalar_err_rms(hres["eng_dot"], S[FIELD["eng_dot"]]) < 1e-5
+    assert scalar_err_rms(d["div_v"], S[FIELD["div_v"]]) < 1e-5
