@@ -8,6 +8,17 @@
 // to sums but still enter v_sig_max in the hydro functor, exactly as on the
 // CPU.  One CTA per walk; the walk's j-list is staged through shared memory
 // in tiles and read by every thread (one thread per i).
+//
+// Staging: the walks' payloads live in the caller's host memory, one array
+// per walk.  Where the GPU can read pageable host memory (GB300's
+// NVLink-C2C with the host's page tables), a gather kernel copies every walk
+// of a dispatch into the tag's device buffer straight from those arrays over
+// the host link, and the dispatch returns once the gather has finished (the
+// caller may reuse its arrays after the call, as FDPS does); on retrieve a
+// scatter kernel writes the results straight into the caller's RESULT arrays
+// the same way.  Otherwise the host copies the walks into pinned staging and
+// one host-to-device copy follows, and the results come back through pinned
+// memory and are copied to the RESULT arrays by the host.
 #include <algorithm>
 #include <atomic>
 #include <cstring>
@@ -30,7 +41,8 @@ void batch32_grav(int n_walk, cudaStream_t st, const int64_t *meta, const void *
 
 namespace {
 
-std::atomic<int> g_batch_prec{SPH_PREC_FP64};   // the arithmetic of the next dispatches
+std::atomic<int> g_batch_prec{SPH_PREC_FP64};            // the arithmetic of the next dispatches
+std::atomic<int> g_batch_staging{SPH_BATCH_STAGING_AUTO};   // who moves the payloads to the device
 
 constexpr int MAX_TAGS = 64;
 constexpr int WT = 128;
@@ -50,6 +62,14 @@ struct TagState {
     size_t cap_out = 0;
     int64_t *h_meta = nullptr, *d_meta = nullptr;   // per walk: i offset, n_i, j offset, n_j, s offset, n_s
     size_t cap_meta = 0;
+    uint64_t *h_src = nullptr, *d_src = nullptr;    // per walk: the caller's EPI, EPJ, SPJ addresses
+    size_t cap_src = 0;
+    uint64_t *h_dst = nullptr, *d_dst = nullptr;    // per walk: the caller's RESULT address (retrieve)
+    size_t cap_dst = 0;
+    cudaEvent_t gathered = nullptr;                 // the device gather of the pending dispatch is done
+    bool gather_pending = false;
+    bool direct_out = false;                        // results stay on the device until retrieve scatters them
+    int pageable = -1;                              // the device reads pageable host memory (-1: not asked)
     int pending_kind = -1;
     int pending_walks = 0;
     size_t pending_out_bytes = 0;
@@ -90,11 +110,13 @@ int tag_state(int tag, TagState **out) {
     int dev = 0;
     cudaGetDevice(&dev);
     if (!t.stream || t.device != dev) {
-        if (cudaStreamCreateWithFlags(&t.stream, cudaStreamNonBlocking) != cudaSuccess) {
+        if (cudaStreamCreateWithFlags(&t.stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&t.gathered, cudaEventDisableTiming) != cudaSuccess) {
             cudaGetLastError();
             return batch_fail(SPH_ERR_CUDA, "cannot create a CUDA stream (no GPU?)");
         }
         t.device = dev;
+        t.pageable = -1;
     }
     *out = &t;
     return SPH_OK;
@@ -104,6 +126,58 @@ int tag_state(int tag, TagState **out) {
 // kernels: meta[w*6 + {0..5}] = i offset, n_i, j offset, n_j, spj offset, n_spj (element offsets)
 
 __device__ __forceinline__ double3 ld3(const double *p) { return make_double3(p[0], p[1], p[2]); }
+
+static_assert(sizeof(sph_epi_dens) % 8 == 0 && sizeof(sph_epj_dens) % 8 == 0 && sizeof(sph_epi_drvt) % 8 == 0 &&
+                  sizeof(sph_epj_drvt) % 8 == 0 && sizeof(sph_epi_hydro) % 8 == 0 &&
+                  sizeof(sph_epj_hydro) % 8 == 0 && sizeof(sph_epi_grav) % 8 == 0 &&
+                  sizeof(sph_epj_grav) % 8 == 0 && sizeof(sph_spj_monopole) % 8 == 0,
+              "payloads move as 8-byte words");
+
+static_assert(sizeof(sph_result_dens) % 8 == 0 && sizeof(sph_result_drvt) % 8 == 0 &&
+                  sizeof(sph_result_hydro) % 8 == 0 && sizeof(sph_result_grav) % 8 == 0,
+              "results move as 8-byte words");
+
+// a block copies n 8-byte words, four independent loads per thread in flight (the source may be
+// host memory across the host link, where the latency wants many loads outstanding)
+__device__ __forceinline__ void copy_words(const unsigned long long *src, unsigned long long *dst, int64_t n) {
+    const int64_t bd = blockDim.x;
+    int64_t k = threadIdx.x;
+    for (; k + 3 * bd < n; k += 4 * bd) {
+        const unsigned long long a = src[k], b = src[k + bd], c = src[k + 2 * bd], d = src[k + 3 * bd];
+        dst[k] = a;
+        dst[k + bd] = b;
+        dst[k + 2 * bd] = c;
+        dst[k + 3 * bd] = d;
+    }
+    for (; k < n; k += bd) dst[k] = src[k];
+}
+
+// block w copies walk w's EPI, EPJ and SPJ runs from the caller's arrays (host memory, read over
+// the host link) to their places in the tag's device staging; sizes in bytes, multiples of 8
+__global__ void __launch_bounds__(256) k_gather_walks(const int64_t *meta, const uint64_t *src, char *dst,
+                                                      int64_t o_epj, int64_t o_spj, int s_epi, int s_epj,
+                                                      int s_spj) {
+    const int64_t *m = meta + 6 * blockIdx.x;
+    const uint64_t *p = src + 3 * blockIdx.x;
+    if (m[1] > 0)
+        copy_words((const unsigned long long *)p[0], (unsigned long long *)(dst + (int64_t)s_epi * m[0]),
+                   (int64_t)s_epi * m[1] / 8);
+    if (m[3] > 0)
+        copy_words((const unsigned long long *)p[1], (unsigned long long *)(dst + o_epj + (int64_t)s_epj * m[2]),
+                   (int64_t)s_epj * m[3] / 8);
+    if (m[5] > 0)
+        copy_words((const unsigned long long *)p[2], (unsigned long long *)(dst + o_spj + (int64_t)s_spj * m[4]),
+                   (int64_t)s_spj * m[5] / 8);
+}
+
+// block w copies walk w's results from the tag's device buffer to the caller's RESULT array
+__global__ void __launch_bounds__(256) k_scatter_results(const int64_t *meta, const uint64_t *dst, const char *src,
+                                                         int s_res) {
+    const int64_t *m = meta + 6 * blockIdx.x;
+    if (m[1] > 0)
+        copy_words((const unsigned long long *)(src + (int64_t)s_res * m[0]), (unsigned long long *)dst[blockIdx.x],
+                   (int64_t)s_res * m[1] / 8);
+}
 
 // CalcDensity, force.h:9-23
 __global__ void __launch_bounds__(WT) k_walk_dens(const int64_t *meta, const sph_epi_dens *epi, const sph_epj_dens *epj,
@@ -365,22 +439,76 @@ int stage(int tag, int kind, int n_walk, const EPI **epi, const int *n_epi, cons
         aj += n_epj[w];
         as += m[5];
     }
-    // the walks' payloads into the pinned staging, split over the host threads (a dispatch of a few
-    // hundred walks moves hundreds of MB; one thread copies at a fraction of the memory bandwidth).
-    // Inside a caller's own parallel region (FDPS's OpenMP threads) this runs on the calling thread.
-#pragma omp parallel for schedule(dynamic, 4) if (n_walk > 8 && ai + aj > 65536)
-    for (int w = 0; w < n_walk; ++w) {
-        const int64_t *m = ts->h_meta + 6 * w;
-        if (m[1]) std::memcpy(ts->h_in + sizeof(EPI) * m[0], epi[w], sizeof(EPI) * m[1]);
-        if (m[3]) std::memcpy(ts->h_in + o_epj + sizeof(EPJ) * m[2], epj[w], sizeof(EPJ) * m[3]);
-        if (m[5])
-            std::memcpy(ts->h_in + o_spj + sizeof(sph_spj_monopole) * m[4], spj[w], sizeof(sph_spj_monopole) * m[5]);
+    // who moves the payloads: the device gather where this GPU reads pageable host memory and every
+    // array is 8-byte aligned (the gather moves 8-byte words), else the host
+    const int mode = g_batch_staging.load();
+    bool gather = false;
+    if (mode != SPH_BATCH_STAGING_HOST && n_walk > 0) {
+        if (ts->pageable < 0) {
+            int v = 0;
+            if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, ts->device) != cudaSuccess) {
+                cudaGetLastError();
+                v = 0;
+            }
+            ts->pageable = v == 1;
+        }
+        gather = ts->pageable == 1;
+        for (int w = 0; gather && w < n_walk; ++w) {
+            const int64_t *m = ts->h_meta + 6 * w;
+            gather = !(m[1] && ((uintptr_t)epi[w] & 7u)) && !(m[3] && ((uintptr_t)epj[w] & 7u)) &&
+                     !(m[5] && ((uintptr_t)spj[w] & 7u));
+        }
+        if (!gather && mode == SPH_BATCH_STAGING_DEVICE)
+            return batch_fail(SPH_ERR_STATE, ts->pageable == 1
+                                                 ? "SPH_BATCH_STAGING_DEVICE needs 8-byte aligned walk arrays"
+                                                 : "this GPU cannot read pageable host memory "
+                                                   "(SPH_BATCH_STAGING_DEVICE)");
     }
-    if (cudaMemcpyAsync(ts->d_in, ts->h_in, o_spj + b_spj, cudaMemcpyHostToDevice, ts->stream) != cudaSuccess ||
-        cudaMemcpyAsync(ts->d_meta, ts->h_meta, sizeof(int64_t) * 6 * n_walk, cudaMemcpyHostToDevice, ts->stream) !=
-            cudaSuccess) {
-        cudaGetLastError();
-        return batch_fail(SPH_ERR_CUDA, "host-to-device copy failed");
+    if (gather) {
+        SPH_TRY(grow((char **)&ts->h_src, (char **)&ts->d_src, &ts->cap_src, sizeof(uint64_t) * 3 * (n_walk + 1)));
+        for (int w = 0; w < n_walk; ++w) {
+            const int64_t *m = ts->h_meta + 6 * w;
+            ts->h_src[3 * w] = m[1] ? (uint64_t)(uintptr_t)epi[w] : 0;
+            ts->h_src[3 * w + 1] = m[3] ? (uint64_t)(uintptr_t)epj[w] : 0;
+            ts->h_src[3 * w + 2] = m[5] ? (uint64_t)(uintptr_t)spj[w] : 0;
+        }
+        if (cudaMemcpyAsync(ts->d_meta, ts->h_meta, sizeof(int64_t) * 6 * n_walk, cudaMemcpyHostToDevice,
+                            ts->stream) != cudaSuccess ||
+            cudaMemcpyAsync(ts->d_src, ts->h_src, sizeof(uint64_t) * 3 * n_walk, cudaMemcpyHostToDevice,
+                            ts->stream) != cudaSuccess) {
+            cudaGetLastError();
+            return batch_fail(SPH_ERR_CUDA, "host-to-device copy failed");
+        }
+        k_gather_walks<<<n_walk, 256, 0, ts->stream>>>(ts->d_meta, ts->d_src, ts->d_in, (int64_t)o_epj,
+                                                       (int64_t)o_spj, (int)sizeof(EPI), (int)sizeof(EPJ),
+                                                       (int)sizeof(sph_spj_monopole));
+        if (cudaGetLastError() != cudaSuccess || cudaEventRecord(ts->gathered, ts->stream) != cudaSuccess) {
+            cudaGetLastError();
+            return batch_fail(SPH_ERR_CUDA, "walk gather launch failed");
+        }
+        ts->gather_pending = true;
+        ts->direct_out = true;
+    } else {
+        ts->direct_out = false;
+        // the walks' payloads into the pinned staging, split over the host threads (a dispatch of a
+        // few hundred walks moves hundreds of MB; one thread copies at a fraction of the memory
+        // bandwidth).  Inside a caller's own parallel region (FDPS's OpenMP threads) this runs on
+        // the calling thread.
+#pragma omp parallel for schedule(dynamic, 4) if (n_walk > 8 && ai + aj > 65536)
+        for (int w = 0; w < n_walk; ++w) {
+            const int64_t *m = ts->h_meta + 6 * w;
+            if (m[1]) std::memcpy(ts->h_in + sizeof(EPI) * m[0], epi[w], sizeof(EPI) * m[1]);
+            if (m[3]) std::memcpy(ts->h_in + o_epj + sizeof(EPJ) * m[2], epj[w], sizeof(EPJ) * m[3]);
+            if (m[5])
+                std::memcpy(ts->h_in + o_spj + sizeof(sph_spj_monopole) * m[4], spj[w],
+                            sizeof(sph_spj_monopole) * m[5]);
+        }
+        if (cudaMemcpyAsync(ts->d_in, ts->h_in, o_spj + b_spj, cudaMemcpyHostToDevice, ts->stream) != cudaSuccess ||
+            cudaMemcpyAsync(ts->d_meta, ts->h_meta, sizeof(int64_t) * 6 * n_walk, cudaMemcpyHostToDevice,
+                            ts->stream) != cudaSuccess) {
+            cudaGetLastError();
+            return batch_fail(SPH_ERR_CUDA, "host-to-device copy failed");
+        }
     }
     ts->pending_kind = kind;
     ts->pending_walks = n_walk;
@@ -393,10 +521,15 @@ int stage(int tag, int kind, int n_walk, const EPI **epi, const int *n_epi, cons
 int finish_dispatch(TagState *ts) {
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return batch_fail(SPH_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
-    if (ts->pending_out_bytes &&
+    if (!ts->direct_out && ts->pending_out_bytes &&
         cudaMemcpyAsync(ts->h_out, ts->d_out, ts->pending_out_bytes, cudaMemcpyDeviceToHost, ts->stream) != cudaSuccess) {
         cudaGetLastError();
         return batch_fail(SPH_ERR_CUDA, "device-to-host copy failed");
+    }
+    if (ts->gather_pending) {   // the caller may reuse its walk arrays once the call returns
+        ts->gather_pending = false;
+        const cudaError_t g = cudaEventSynchronize(ts->gathered);
+        if (g != cudaSuccess) return batch_fail(SPH_ERR_CUDA, std::string("walk gather failed: ") + cudaGetErrorString(g));
     }
     return SPH_OK;
 }
@@ -407,14 +540,46 @@ int retrieve(int tag, int kind, int n_walk, const int *n_epi, RES **result) {
     TagState &ts = g_tags[tag];
     if (ts.pending_kind != kind || ts.pending_walks != n_walk)
         return batch_fail(SPH_ERR_STATE, "retrieve does not match the last dispatch on this tag");
+    std::vector<int64_t> off(n_walk + 1, 0);
+    bool bad = false, aligned = true;
+    for (int w = 0; w < n_walk; ++w) {
+        bad = bad || (n_epi[w] > 0 && (!result || !result[w])) || n_epi[w] != ts.h_meta[6 * w + 1];
+        aligned = aligned && !(n_epi[w] > 0 && result && ((uintptr_t)result[w] & 7u));
+        off[w + 1] = off[w] + std::max(n_epi[w], 0);
+    }
+    if (bad) {   // the results are dropped with the dispatch
+        cudaStreamSynchronize(ts.stream);
+        ts.pending_kind = -1;
+        return batch_fail(SPH_ERR_ARG, "null result pointer, or walk sizes that differ from the dispatch's");
+    }
+    if (ts.direct_out && aligned && n_walk > 0) {
+        // the scatter kernel writes every walk's results into the caller's arrays
+        const int rc = grow((char **)&ts.h_dst, (char **)&ts.d_dst, &ts.cap_dst, sizeof(uint64_t) * (n_walk + 1));
+        if (rc != SPH_OK) {
+            cudaStreamSynchronize(ts.stream);
+            ts.pending_kind = -1;
+            return rc;
+        }
+        for (int w = 0; w < n_walk; ++w) ts.h_dst[w] = n_epi[w] > 0 ? (uint64_t)(uintptr_t)result[w] : 0;
+        if (cudaMemcpyAsync(ts.d_dst, ts.h_dst, sizeof(uint64_t) * n_walk, cudaMemcpyHostToDevice, ts.stream) ==
+            cudaSuccess)
+            k_scatter_results<<<n_walk, 256, 0, ts.stream>>>(ts.d_meta, ts.d_dst, ts.d_out, (int)sizeof(RES));
+        const cudaError_t e = cudaStreamSynchronize(ts.stream);
+        ts.pending_kind = -1;
+        const cudaError_t l = cudaGetLastError();
+        if (e != cudaSuccess || l != cudaSuccess)
+            return batch_fail(SPH_ERR_CUDA, std::string("batch kernel or result scatter failed: ") +
+                                                 cudaGetErrorString(e != cudaSuccess ? e : l));
+        return SPH_OK;
+    }
+    if (ts.direct_out && ts.pending_out_bytes)   // results left on the device: bring them to the host now
+        cudaMemcpyAsync(ts.h_out, ts.d_out, ts.pending_out_bytes, cudaMemcpyDeviceToHost, ts.stream);
     const cudaError_t e = cudaStreamSynchronize(ts.stream);
     ts.pending_kind = -1;
-    if (e != cudaSuccess) return batch_fail(SPH_ERR_CUDA, std::string("batch kernel failed: ") + cudaGetErrorString(e));
-    std::vector<int64_t> off(n_walk + 1, 0);
-    for (int w = 0; w < n_walk; ++w) {
-        if (n_epi[w] > 0 && (!result || !result[w])) return batch_fail(SPH_ERR_ARG, "null result pointer");
-        off[w + 1] = off[w] + n_epi[w];
-    }
+    const cudaError_t l = cudaGetLastError();
+    if (e != cudaSuccess || l != cudaSuccess)
+        return batch_fail(SPH_ERR_CUDA, std::string("batch kernel failed: ") +
+                                             cudaGetErrorString(e != cudaSuccess ? e : l));
 #pragma omp parallel for schedule(dynamic, 8) if (n_walk > 8 && off[n_walk] > 65536)
     for (int w = 0; w < n_walk; ++w)
         if (n_epi[w] > 0) std::memcpy(result[w], ts.h_out + sizeof(RES) * off[w], sizeof(RES) * n_epi[w]);
@@ -426,6 +591,13 @@ int retrieve(int tag, int kind, int n_walk, const int *n_epi, RES **result) {
 extern "C" {
 
 const char *sph_batch_last_error(void) { return g_batch_err.c_str(); }
+
+int sph_batch_set_staging(int mode) {
+    if (mode != SPH_BATCH_STAGING_AUTO && mode != SPH_BATCH_STAGING_HOST && mode != SPH_BATCH_STAGING_DEVICE)
+        return batch_fail(SPH_ERR_ARG, "staging must be SPH_BATCH_STAGING_AUTO, _HOST or _DEVICE");
+    g_batch_staging.store(mode);
+    return SPH_OK;
+}
 
 int sph_batch_set_precision(int precision) {
     if (precision != SPH_PREC_FP64 && precision != SPH_PREC_MIXED)

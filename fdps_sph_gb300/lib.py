@@ -27,6 +27,7 @@ FIELD = {n: i for i, n in enumerate(FIELDS)}
 SPH_OK = 0
 ERRORS = {-1: "SPH_ERR_ARG", -2: "SPH_ERR_CUDA", -3: "SPH_ERR_OOM", -4: "SPH_ERR_TABLE", -5: "SPH_ERR_NONFINITE",
           -6: "SPH_ERR_CAPACITY", -7: "SPH_ERR_STATE", -8: "SPH_ERR_TIMEOUT"}
+SPH_ERR_ARG, SPH_ERR_STATE = -1, -7
 PREC_FP64 = 0
 PREC_MIXED = 1
 
@@ -41,7 +42,7 @@ EXPORTS = [
     "sph_add_run", "sph_remove_run", "sph_list_runs", "sph_run_info", "sph_download_run", "sph_run_diagnostics",
     "sph_autotune", "sph_set_eos_ideal", "sph_set_eos_entropy", "sph_eos_eval", "sph_download_fields",
     "sph_step_download", "sph_read_eos_table_file", "sph_read_eos_table_error", "sph_get_grav_lists",
-    "sph_batch_set_precision",
+    "sph_batch_set_precision", "sph_batch_set_staging",
 ]
 # fields a step reads or carries unchanged (SPH_STEP_INPUT_FIELDS): what SPH_UPLOAD_STEP_INPUTS copies
 STEP_INPUT_FIELDS = ["x", "y", "z", "vx", "vy", "vz", "mass", "smth", "eng", "ava", "ax", "ay", "az", "eng_dot",
@@ -92,6 +93,7 @@ def load() -> C.CDLL:
     L.sph_retrieve_grav.argtypes = [C.c_int, C.c_int, i32p, P]
     L.sph_batch_last_error.restype = C.c_char_p
     L.sph_batch_set_precision.argtypes = [C.c_int]
+    L.sph_batch_set_staging.argtypes = [C.c_int]
     L.sph_config_default.argtypes = [C.POINTER(Config)]
     L.sph_config_default.restype = None
     L.sph_ctx_create.argtypes = [C.POINTER(Config), C.POINTER(C.c_void_p)]
@@ -503,8 +505,25 @@ def retrieve(kind: str, tag: int, n_epi):
 def batch_precision(precision: str):
     """arithmetic of the batch entry points' next dispatches: "fp64" (the reference functors) or
     "mixed" (sph_batch_set_precision)"""
+    if precision not in ("fp64", "mixed"):
+        raise ValueError(f"precision must be 'fp64' or 'mixed', not {precision!r}")
     L = load()
     rc = L.sph_batch_set_precision(PREC_MIXED if precision == "mixed" else PREC_FP64)
+    if rc != SPH_OK:
+        raise SphError(rc, L.sph_batch_last_error().decode())
+
+
+BATCH_STAGING = {"auto": 0, "host": 1, "device": 2}   # SPH_BATCH_STAGING_*
+
+
+def batch_staging(mode: str):
+    """who moves the next dispatches' walks to the device (sph_batch_set_staging): "auto" (the GPU
+    gathers them from host memory where it can read pageable memory, else the host copies them),
+    "host" or "device" """
+    if mode not in BATCH_STAGING:
+        raise ValueError(f"staging must be one of {sorted(BATCH_STAGING)}, not {mode!r}")
+    L = load()
+    rc = L.sph_batch_set_staging(BATCH_STAGING[mode])
     if rc != SPH_OK:
         raise SphError(rc, L.sph_batch_last_error().decode())
 

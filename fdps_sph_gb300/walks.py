@@ -128,52 +128,65 @@ class Walks:
                              for k in KINDS}
         self.staged_bytes["grav"] += len(spj) * T.SPJ_MONO.itemsize
         self.sorted_state = S
+        self._batch_cache = {}
 
     def _ptrs(self, arr, offs, w0, w1, itemsize):
         base = arr.ctypes.data
         return (C.c_void_p * (w1 - w0))(*[base + int(o) * itemsize for o in offs[w0:w1]])
 
+    def _batches(self, kind, n_walk_limit):
+        """the argument arrays of every batch of `kind` (walk pointers into this object's payload
+        and result arrays, which stay in place, and the walk sizes), built once per (kind,
+        n_walk_limit): FDPS hands its callbacks such arrays, so building them is not the
+        boundary's cost"""
+        key = (kind, n_walk_limit)
+        if key not in self._batch_cache:
+            epi, (ej, jo) = self.epi[kind], self.jlist[kind]
+            res = self.result[kind]
+            out = []
+            for w0 in range(0, self.n_group, n_walk_limit):
+                w1 = min(w0 + n_walk_limit, self.n_group)
+                nw = w1 - w0
+                args = [nw, self._ptrs(epi, self.start, w0, w1, epi.itemsize),
+                        (C.c_int * nw)(*self.count[w0:w1].tolist()),
+                        self._ptrs(ej, jo, w0, w1, ej.itemsize),
+                        (C.c_int * nw)(*(jo[w0 + 1:w1 + 1] - jo[w0:w1]).tolist())]
+                if kind == "grav":
+                    sa, so = self.spj
+                    args += [self._ptrs(sa, so, w0, w1, sa.itemsize),
+                             (C.c_int * nw)(*(so[w0 + 1:w1 + 1] - so[w0:w1]).tolist())]
+                out.append((args, self._ptrs(res, self.start, w0, w1, res.itemsize)))
+            self._batch_cache[key] = out
+        return self._batch_cache[key]
+
     def run(self, kind, n_walk_limit=256, n_tags=4, tag0=0):
         """one pass of `kind` over every walk, the MultiWalk way; returns the host seconds taken"""
         from . import lib
         L = lib.load()
-        epi, (ej, jo) = self.epi[kind], self.jlist[kind]
         res = self.result[kind]
         res[:] = np.zeros(1, _RES[kind])
         if kind == "grav":
             res["dt"] = 1.0e30   # RESULT::Grav::clear()
-        batches = [(w, min(w + n_walk_limit, self.n_group)) for w in range(0, self.n_group, n_walk_limit)]
+        batches = self._batches(kind, n_walk_limit)
         disp = getattr(L, f"sph_dispatch_{kind}")
         retr = getattr(L, f"sph_retrieve_{kind}")
         pend = {}
 
         def retrieve(tag):
-            w0, w1, n_epi = pend.pop(tag)
-            rp = self._ptrs(res, self.start, w0, w1, res.itemsize)
-            rc = retr(tag0 + tag, w1 - w0, n_epi, rp)
+            args, rp = pend.pop(tag)
+            rc = retr(tag0 + tag, args[0], args[2], rp)
             if rc != 0:
                 raise lib.SphError(rc, L.sph_batch_last_error().decode())
 
         t0 = time.perf_counter()
-        for b, (w0, w1) in enumerate(batches):
+        for b, (args, rp) in enumerate(batches):
             tag = b % n_tags
             if tag in pend:
                 retrieve(tag)
-            nw = w1 - w0
-            n_epi = (C.c_int * nw)(*self.count[w0:w1].tolist())
-            n_epj = (C.c_int * nw)(*(jo[w0 + 1:w1 + 1] - jo[w0:w1]).tolist())
-            pi = self._ptrs(epi, self.start, w0, w1, epi.itemsize)
-            pj = self._ptrs(ej, jo, w0, w1, ej.itemsize)
-            if kind == "grav":
-                sa, so = self.spj
-                ps = self._ptrs(sa, so, w0, w1, sa.itemsize)
-                n_spj = (C.c_int * nw)(*(so[w0 + 1:w1 + 1] - so[w0:w1]).tolist())
-                rc = disp(tag0 + tag, nw, pi, n_epi, pj, n_epj, ps, n_spj)
-            else:
-                rc = disp(tag0 + tag, nw, pi, n_epi, pj, n_epj)
+            rc = disp(tag0 + tag, *args)
             if rc != 0:
                 raise lib.SphError(rc, L.sph_batch_last_error().decode())
-            pend[tag] = (w0, w1, n_epi)
+            pend[tag] = (args, rp)
         for tag in list(pend):
             retrieve(tag)
         return time.perf_counter() - t0

@@ -100,6 +100,17 @@ const char *sph_batch_last_error(void);
  * FP64 per-particle epilogues -- the device-resident mixed path's arithmetic, within 1e-5 of FP64
  * on the functors' results.  No counterpart in the reference (its functors are FP64). */
 int sph_batch_set_precision(int precision);
+/* Who moves a dispatch's walks to the device (all tags).  SPH_BATCH_STAGING_AUTO (default): the GPU
+ * reads them from the caller's arrays with a gather kernel where it can read pageable host memory
+ * (cudaDevAttrPageableMemoryAccess; GB300's NVLink-C2C) and every array is 8-byte aligned, else
+ * the host copies them into pinned staging.  _HOST: always the host copy.  _DEVICE: always the
+ * gather; a dispatch that cannot gather fails with SPH_ERR_STATE.  Either way a dispatch returns
+ * after it has read the caller's arrays, so they may be reused at once.  No counterpart in the
+ * reference. */
+#define SPH_BATCH_STAGING_AUTO 0
+#define SPH_BATCH_STAGING_HOST 1
+#define SPH_BATCH_STAGING_DEVICE 2
+int sph_batch_set_staging(int mode);
 
 /* ---- 2. device-resident whole-pass API ----------------------------------- */
 
@@ -355,10 +366,11 @@ int sph_get_counters(sph_ctx *ctx, int64_t out[16]);
  * SPH_ERR_ARG, a non-finite position SPH_ERR_NONFINITE, a CUDA error already
  * pending on the calling thread SPH_ERR_CUDA (before any work is queued; the
  * error is left in place).  The first call on a
- * device looks up the array's device address (cudaGetSymbolAddress), so make
- * that first call before any stream capture.  Every call on a device shares
- * the array: calls that overlap on the GPU race.  No device memory is
- * allocated or freed. */
+ * device looks up the array's device address (cudaGetSymbolAddress).  The
+ * call ends by reading its error word back and synchronising `stream`, so it
+ * returns after its work is done and cannot be recorded into a CUDA graph.
+ * Every call on a device shares the array: calls that overlap on the GPU
+ * race.  No device memory is allocated or freed. */
 #define SPH_NOALLOC_MAX_N 131072
 int sph_morton_order_noalloc(const double *x, const double *y, const double *z, int64_t n, uint64_t *keys_out,
                              int32_t *order_out, void *stream);

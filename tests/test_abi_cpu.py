@@ -72,6 +72,9 @@ def test_header_constants_match_binding():
     defs = {m.group(1): m.group(2) for m in re.finditer(r"#define\s+(SPH_[A-Z0-9_]+)\s+\(?(-?\d+)\)?", src)}
     assert int(defs["SPH_NOALLOC_MAX_N"]) == lib.NOALLOC_MAX_N
     assert int(defs["SPH_PREC_FP64"]) == lib.PREC_FP64 and int(defs["SPH_PREC_MIXED"]) == lib.PREC_MIXED
+    assert int(defs["SPH_ERR_ARG"]) == lib.SPH_ERR_ARG and int(defs["SPH_ERR_STATE"]) == lib.SPH_ERR_STATE
+    for mode, v in lib.BATCH_STAGING.items():
+        assert int(defs["SPH_BATCH_STAGING_" + mode.upper()]) == v
     assert int(defs["SPH_ENTROPY_ABS_INT"]) == lib.ENTROPY_ABS_INT
     assert int(defs["SPH_ENTROPY_ABS_REAL"]) == lib.ENTROPY_ABS_REAL
     for code, name in lib.ERRORS.items():

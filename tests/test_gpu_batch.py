@@ -158,3 +158,78 @@ def test_batch_mixed_precision_within_bar(fun):
     assert vec_err_rms(h["acc"], rh["acc"]) < 1e-5
     assert scalar_err_rms(h["eng_dot"], rh["eng_dot"]) < 1e-5
     assert rel_err(h["dt"], rh["dt"], 1e-300) < 1e-6
+
+
+def _staging_supported(mode):
+    """whether dispatches can run with this staging mode here (the device gather needs a GPU that
+    reads pageable host memory)"""
+    from fdps_sph_gb300 import lib
+    lib.batch_staging(mode)
+    try:
+        a = np.zeros(1, T.EPI_DENS)
+        a["smth"], a["mass"] = 1.0, 1.0
+        b = np.zeros(1, T.EPJ_DENS)
+        b["mass"], b["smth"] = 1.0, 1.0
+        lib.run_walks("dens", [a], [b], tag=9)
+        return True
+    except lib.SphError as e:
+        assert e.code == lib.SPH_ERR_STATE
+        return False
+    finally:
+        lib.batch_staging("auto")
+
+
+def test_batch_staging_modes_agree(fun):
+    """the host copy and the device gather of the walks (sph_batch_set_staging) feed the kernels the
+    same bytes, so every functor gives bit-identical results either way"""
+    from fdps_sph_gb300 import lib
+    if not _staging_supported("device"):
+        pytest.skip("this GPU cannot read pageable host memory")
+    out = {}
+    for mode in ("host", "device"):
+        lib.batch_staging(mode)
+        try:
+            out[mode] = (run("dens", fun, "dens", "state_dens", DENS_I, DENS_J, T.EPI_DENS, T.EPJ_DENS),
+                         run("hydro", fun, "hydro", "state_hydro", HYD_I, HYD_J, T.EPI_HYDRO, T.EPJ_HYDRO))
+        finally:
+            lib.batch_staging("auto")
+    for a, b in zip(out["host"], out["device"]):
+        assert a.tobytes() == b.tobytes()
+
+
+def test_batch_misaligned_walks_fall_back_to_the_host_copy():
+    """a walk or RESULT array that is not 8-byte aligned cannot be moved in 8-byte words by the
+    device: "auto" copies it on the host (same result as an aligned array), "device" refuses the
+    dispatch"""
+    from fdps_sph_gb300 import lib
+    rng = np.random.default_rng(5)
+    a = np.zeros(40, T.EPI_DENS)
+    a["pos"] = rng.normal(size=(40, 3))
+    a["mass"], a["smth"] = 1.0, 0.8
+    b = np.zeros(60, T.EPJ_DENS)
+    b["pos"] = rng.normal(size=(60, 3))
+    b["mass"], b["smth"] = 1.5, 0.8
+    raw = np.zeros(b.nbytes + 8, np.uint8)
+    bm = np.frombuffer(raw.data, T.EPJ_DENS, count=len(b), offset=4)   # 4 bytes off alignment
+    bm[:] = b
+    assert bm.ctypes.data % 8 == 4
+    ref = lib.run_walks("dens", [a], [b], tag=9)[0]
+    got = lib.run_walks("dens", [a], [bm], tag=9)[0]
+    assert got.tobytes() == ref.tobytes()
+    # a RESULT array off alignment: the results come back through the host copy instead
+    import ctypes as C
+    n_epi = lib.dispatch("dens", 9, [a], [b])
+    rraw = np.zeros(len(a) * T.RES_DENS.itemsize + 8, np.uint8)
+    rm = np.frombuffer(rraw.data, T.RES_DENS, count=len(a), offset=4)
+    assert rm.ctypes.data % 8 == 4
+    rc = lib.load().sph_retrieve_dens(9, 1, n_epi, (C.c_void_p * 1)(rm.ctypes.data))
+    assert rc == 0
+    assert rm.tobytes() == ref.tobytes()
+    if _staging_supported("device"):
+        lib.batch_staging("device")
+        try:
+            with pytest.raises(lib.SphError) as e:
+                lib.run_walks("dens", [a], [bm], tag=9)
+            assert e.value.code == lib.SPH_ERR_STATE
+        finally:
+            lib.batch_staging("auto")
