@@ -603,6 +603,8 @@ def main():
         for k in ("batch", "serving", "multiwalk"):
             if k in out:
                 out[k]["vs_cpu_baseline"] = out[k]["value"] / v_cpu
+        if "multiwalk" in out:
+            out["multiwalk"]["index_form"]["vs_cpu_baseline"] = out["multiwalk"]["index_form"]["value"] / v_cpu
     print(json.dumps(out))
 
 
@@ -635,6 +637,9 @@ def multiwalk(a, device, n_walk_limit=256, n_tags=4, steps=2):
     try:
         W.step(n_walk_limit=n_walk_limit, n_tags=n_tags)
         runs32 = [W.step(n_walk_limit=n_walk_limit, n_tags=n_tags) for _ in range(steps)]
+        # the index form: each pass's EPJ / SPJ arrays sent once, the walks as indices into them
+        W.step(n_walk_limit=n_walk_limit, n_tags=n_tags, index=True)
+        runs_ix = [W.step(n_walk_limit=n_walk_limit, n_tags=n_tags, index=True) for _ in range(steps)]
         lib.batch_staging("host")   # the walks copied by the host into pinned staging instead
         W.step(n_walk_limit=n_walk_limit, n_tags=n_tags)
         runs_h = [W.step(n_walk_limit=n_walk_limit, n_tags=n_tags) for _ in range(steps)]
@@ -644,6 +649,9 @@ def multiwalk(a, device, n_walk_limit=256, n_tags=4, steps=2):
     best32 = min(runs32, key=lambda r: sum(r.values()))
     t32 = sum(best32.values())
     t_h = min(sum(r.values()) for r in runs_h)
+    best_ix = min(runs_ix, key=lambda r: sum(r.values()))
+    t_ix = sum(best_ix.values())
+    index_bytes = 4 * W.index_bytes["dens"] + sum(W.index_bytes[k] for k in ("drvt", "hydro", "grav"))
     staged = 4 * W.staged_bytes["dens"] + sum(W.staged_bytes[k] for k in ("drvt", "hydro", "grav"))
     jl = {k: int(len(W.jlist[k][0])) for k in ("dens", "hydro", "grav")}
     return {"metric": "particle-steps/s through the MultiWalk dispatch / retrieve callbacks",
@@ -652,6 +660,11 @@ def multiwalk(a, device, n_walk_limit=256, n_tags=4, steps=2):
             "staging": "auto (sph_batch_set_staging: the GPU gathers the walks from host memory where it "
                        "can read pageable memory)",
             "host_staging": {"value": n / t_h, "s_per_step": t_h},
+            "index_form": {"value": n / t_ix, "s_per_step": t_ix, "s_per_pass": {k: v for k, v in best_ix.items()},
+                           "bytes_per_step": int(index_bytes),
+                           "note": "the dispatch callbacks of calcForceAllAndWriteBackMultiWalkIndex "
+                                   "(sph_dispatch_index_*): each pass's EPJ / SPJ arrays sent once with "
+                                   "send_flag, the walks as int32 indices; mixed precision, same results"},
             "fp64": {"value": n / t_step, "s_per_step": t_step, "s_per_pass": {k: v for k, v in best.items()}},
             "groups": int(W.n_group),
             "n_walk_limit": n_walk_limit, "tags": n_tags, "staged_bytes_per_step": int(staged),

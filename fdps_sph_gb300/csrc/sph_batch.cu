@@ -26,18 +26,9 @@
 #include <string>
 #include <vector>
 
-#include "sph_physics.cuh"
+#include "sph_batch.cuh"
 
 using namespace sph;
-
-namespace sph {
-// the mixed-precision functor kernels (sph_batch32.cu)
-void batch32_dens(int n_walk, cudaStream_t st, const int64_t *meta, const void *epi, const void *epj, void *res);
-void batch32_drvt(int n_walk, cudaStream_t st, const int64_t *meta, const void *epi, const void *epj, void *res);
-void batch32_hydro(int n_walk, cudaStream_t st, const int64_t *meta, const void *epi, const void *epj, void *res);
-void batch32_grav(int n_walk, cudaStream_t st, const int64_t *meta, const void *epi, const void *epj,
-                  const void *spj, void *res);
-}  // namespace sph
 
 namespace {
 
@@ -69,6 +60,8 @@ struct TagState {
     cudaEvent_t gathered = nullptr;                 // the device gather of the pending dispatch is done
     bool gather_pending = false;
     bool direct_out = false;                        // results stay on the device until retrieve scatters them
+    bool pending_index = false;                     // the pending dispatch is of the index form
+    int *d_err = nullptr, *h_err = nullptr;         // index form: bit 0 = an index outside the sent array
     int pageable = -1;                              // the device reads pageable host memory (-1: not asked)
     int pending_kind = -1;
     int pending_walks = 0;
@@ -152,22 +145,38 @@ __device__ __forceinline__ void copy_words(const unsigned long long *src, unsign
     for (; k < n; k += bd) dst[k] = src[k];
 }
 
-// block w copies walk w's EPI, EPJ and SPJ runs from the caller's arrays (host memory, read over
-// the host link) to their places in the tag's device staging; sizes in bytes, multiples of 8
+// the same in 4-byte words (the index form's int32 index arrays)
+__device__ __forceinline__ void copy_words4(const unsigned *src, unsigned *dst, int64_t n) {
+    const int64_t bd = blockDim.x;
+    int64_t k = threadIdx.x;
+    for (; k + 3 * bd < n; k += 4 * bd) {
+        const unsigned a = src[k], b = src[k + bd], c = src[k + 2 * bd], d = src[k + 3 * bd];
+        dst[k] = a;
+        dst[k + bd] = b;
+        dst[k + 2 * bd] = c;
+        dst[k + 3 * bd] = d;
+    }
+    for (; k < n; k += bd) dst[k] = src[k];
+}
+
+// a run of `bytes` bytes in 8-byte words, or in 4-byte words where the element size is not a
+// multiple of 8 (the host checked the alignment)
+__device__ __forceinline__ void copy_run(const void *src, void *dst, int64_t bytes, int elem) {
+    if (elem % 8 == 0) copy_words((const unsigned long long *)src, (unsigned long long *)dst, bytes / 8);
+    else copy_words4((const unsigned *)src, (unsigned *)dst, bytes / 4);
+}
+
+// block w copies walk w's EPI, EPJ and SPJ runs (payloads, or index arrays in the index form) from
+// the caller's arrays (host memory, read over the host link) to their places in the tag's device
+// staging; s_* are the element sizes in bytes
 __global__ void __launch_bounds__(256) k_gather_walks(const int64_t *meta, const uint64_t *src, char *dst,
                                                       int64_t o_epj, int64_t o_spj, int s_epi, int s_epj,
                                                       int s_spj) {
     const int64_t *m = meta + 6 * blockIdx.x;
     const uint64_t *p = src + 3 * blockIdx.x;
-    if (m[1] > 0)
-        copy_words((const unsigned long long *)p[0], (unsigned long long *)(dst + (int64_t)s_epi * m[0]),
-                   (int64_t)s_epi * m[1] / 8);
-    if (m[3] > 0)
-        copy_words((const unsigned long long *)p[1], (unsigned long long *)(dst + o_epj + (int64_t)s_epj * m[2]),
-                   (int64_t)s_epj * m[3] / 8);
-    if (m[5] > 0)
-        copy_words((const unsigned long long *)p[2], (unsigned long long *)(dst + o_spj + (int64_t)s_spj * m[4]),
-                   (int64_t)s_spj * m[5] / 8);
+    if (m[1] > 0) copy_run((const void *)p[0], dst + (int64_t)s_epi * m[0], (int64_t)s_epi * m[1], s_epi);
+    if (m[3] > 0) copy_run((const void *)p[1], dst + o_epj + (int64_t)s_epj * m[2], (int64_t)s_epj * m[3], s_epj);
+    if (m[5] > 0) copy_run((const void *)p[2], dst + o_spj + (int64_t)s_spj * m[4], (int64_t)s_spj * m[5], s_spj);
 }
 
 // block w copies walk w's results from the tag's device buffer to the caller's RESULT array
@@ -180,7 +189,7 @@ __global__ void __launch_bounds__(256) k_scatter_results(const int64_t *meta, co
 }
 
 // CalcDensity, force.h:9-23
-__global__ void __launch_bounds__(WT) k_walk_dens(const int64_t *meta, const sph_epi_dens *epi, const sph_epj_dens *epj,
+__global__ void __launch_bounds__(WT) k_walk_dens(const int64_t *meta, const sph_epi_dens *epi, JSrc<sph_epj_dens> epj,
                                                   sph_result_dens *res) {
     __shared__ double4 tile[WT];
     const int64_t *M = meta + 6 * blockIdx.x;
@@ -222,7 +231,7 @@ __global__ void __launch_bounds__(WT) k_walk_dens(const int64_t *meta, const sph
 }
 
 // CalcDerivative, force.h:89-106
-__global__ void __launch_bounds__(WT) k_walk_drvt(const int64_t *meta, const sph_epi_drvt *epi, const sph_epj_drvt *epj,
+__global__ void __launch_bounds__(WT) k_walk_drvt(const int64_t *meta, const sph_epi_drvt *epi, JSrc<sph_epj_drvt> epj,
                                                   sph_result_drvt *res) {
     __shared__ double4 tp[WT];
     __shared__ double4 tv[WT];
@@ -279,7 +288,7 @@ __global__ void __launch_bounds__(WT) k_walk_drvt(const int64_t *meta, const sph
 
 // CalcHydroForce, force.h:113-147
 __global__ void __launch_bounds__(WT) k_walk_hydro(const int64_t *meta, const sph_epi_hydro *epi,
-                                                   const sph_epj_hydro *epj, sph_result_hydro *res) {
+                                                   JSrc<sph_epj_hydro> epj, sph_result_hydro *res) {
     __shared__ double4 tp[WT];   // pos, mass
     __shared__ double4 tv[WT];   // vel, smth
     __shared__ double4 tq[WT];   // dens, pres, snds, grad_smth
@@ -344,8 +353,8 @@ __global__ void __launch_bounds__(WT) k_walk_hydro(const int64_t *meta, const sp
 }
 
 // CalcGravityForce<EPJ::Grav> then CalcGravityForce<SPJMonopole>, force.h:154-168
-__global__ void __launch_bounds__(WT) k_walk_grav(const int64_t *meta, const sph_epi_grav *epi, const sph_epj_grav *epj,
-                                                  const sph_spj_monopole *spj, sph_result_grav *res) {
+__global__ void __launch_bounds__(WT) k_walk_grav(const int64_t *meta, const sph_epi_grav *epi, JSrc<sph_epj_grav> epj,
+                                                  JSrc<sph_spj_monopole> spj, sph_result_grav *res) {
     __shared__ double4 tile[WT];
     const double G = 6.67e-11;   // force.h:171-172
     const int64_t *M = meta + 6 * blockIdx.x;
@@ -398,10 +407,20 @@ __global__ void __launch_bounds__(WT) k_walk_grav(const int64_t *meta, const sph
     }
 }
 
-template <class EPI, class EPJ, class RES>
-int stage(int tag, int kind, int n_walk, const EPI **epi, const int *n_epi, const EPJ **epj, const int *n_epj,
-          const sph_spj_monopole **spj, const int *n_spj, TagState **ts_out) {
-    if (n_walk < 0 || (n_walk > 0 && (!epi || !n_epi || !epj || !n_epj)))
+// where a dispatch's sections sit in the tag's staging (bytes, 16-byte aligned sections)
+struct Layout {
+    int64_t ni = 0, nj = 0, ns = 0;
+    size_t o_epj = 0, o_spj = 0, end = 0;
+};
+
+// Stages one dispatch's walks on its tag: the EPI payloads, then the j entries of every walk and
+// (gravity) its SPJ entries.  Payload form: the entries are EPJ / SPJ payloads (s_j, s_s their
+// sizes); index form: int32 indices into the arrays sent for the pass (s_j = s_s = 4).
+template <class EPI, class RES>
+int stage(int tag, int kind, int n_walk, const EPI **epi, const int *n_epi, const void *const *jw, size_t s_j,
+          const int *n_epj, const void *const *sw, size_t s_s, const int *n_spj, bool index, TagState **ts_out,
+          Layout *lay) {
+    if (n_walk < 0 || (n_walk > 0 && (!epi || !n_epi || !jw || !n_epj)))
         return batch_fail(SPH_ERR_ARG, "null walk arrays");
     TagState *ts = nullptr;
     SPH_TRY(tag_state(tag, &ts));
@@ -410,21 +429,29 @@ int stage(int tag, int kind, int n_walk, const EPI **epi, const int *n_epi, cons
         cudaStreamSynchronize(ts->stream);
         ts->pending_kind = -1;
     }
-    int64_t ni = 0, nj = 0, ns = 0;
+    Layout L;
     for (int w = 0; w < n_walk; ++w) {
-        if (n_epi[w] < 0 || n_epj[w] < 0 || (spj && n_spj && n_spj[w] < 0))
+        if (n_epi[w] < 0 || n_epj[w] < 0 || (sw && n_spj && n_spj[w] < 0))
             return batch_fail(SPH_ERR_ARG, "negative walk size");
-        if ((n_epi[w] > 0 && !epi[w]) || (n_epj[w] > 0 && !epj[w])) return batch_fail(SPH_ERR_ARG, "null walk");
-        ni += n_epi[w];
-        nj += n_epj[w];
-        if (spj && n_spj) ns += n_spj[w];
+        if ((n_epi[w] > 0 && !epi[w]) || (n_epj[w] > 0 && !jw[w])) return batch_fail(SPH_ERR_ARG, "null walk");
+        L.ni += n_epi[w];
+        L.nj += n_epj[w];
+        if (sw && n_spj) L.ns += n_spj[w];
     }
-    const size_t b_epi = sizeof(EPI) * ni, b_epj = sizeof(EPJ) * nj, b_spj = sizeof(sph_spj_monopole) * ns;
-    // 16-byte aligned sections
-    const size_t o_epj = (b_epi + 15) & ~size_t(15), o_spj = (o_epj + b_epj + 15) & ~size_t(15);
-    SPH_TRY(grow(&ts->h_in, &ts->d_in, &ts->cap_in, o_spj + b_spj + 16));
-    SPH_TRY(grow(&ts->h_out, &ts->d_out, &ts->cap_out, sizeof(RES) * ni + 16));
+    const size_t b_epi = sizeof(EPI) * L.ni, b_epj = s_j * L.nj, b_spj = s_s * L.ns;
+    L.o_epj = (b_epi + 15) & ~size_t(15);
+    L.o_spj = (L.o_epj + b_epj + 15) & ~size_t(15);
+    L.end = L.o_spj + b_spj;
+    SPH_TRY(grow(&ts->h_in, &ts->d_in, &ts->cap_in, L.end + 16));
+    SPH_TRY(grow(&ts->h_out, &ts->d_out, &ts->cap_out, sizeof(RES) * L.ni + 16));
     SPH_TRY(grow((char **)&ts->h_meta, (char **)&ts->d_meta, &ts->cap_meta, sizeof(int64_t) * 6 * (n_walk + 1)));
+    if (index && !ts->d_err) {
+        if (cudaMalloc((void **)&ts->d_err, sizeof(int)) != cudaSuccess ||
+            cudaMallocHost((void **)&ts->h_err, sizeof(int)) != cudaSuccess) {
+            cudaGetLastError();
+            return batch_fail(SPH_ERR_OOM, "batch error-word allocation failed");
+        }
+    }
     int64_t ai = 0, aj = 0, as = 0;
     for (int w = 0; w < n_walk; ++w) {
         int64_t *m = ts->h_meta + 6 * w;
@@ -433,14 +460,14 @@ int stage(int tag, int kind, int n_walk, const EPI **epi, const int *n_epi, cons
         m[2] = aj;
         m[3] = n_epj[w];
         m[4] = as;
-        m[5] = (spj && n_spj) ? n_spj[w] : 0;
-        if (m[5] && !spj[w]) return batch_fail(SPH_ERR_ARG, "null SPJ walk");
+        m[5] = (sw && n_spj) ? n_spj[w] : 0;
+        if (m[5] && !sw[w]) return batch_fail(SPH_ERR_ARG, "null SPJ walk");
         ai += n_epi[w];
         aj += n_epj[w];
         as += m[5];
     }
     // who moves the payloads: the device gather where this GPU reads pageable host memory and every
-    // array is 8-byte aligned (the gather moves 8-byte words), else the host
+    // array is aligned to its word (8 bytes for payloads, 4 for indices), else the host
     const int mode = g_batch_staging.load();
     bool gather = false;
     if (mode != SPH_BATCH_STAGING_HOST && n_walk > 0) {
@@ -453,24 +480,29 @@ int stage(int tag, int kind, int n_walk, const EPI **epi, const int *n_epi, cons
             ts->pageable = v == 1;
         }
         gather = ts->pageable == 1;
+        const uintptr_t aj_mask = s_j % 8 ? 3u : 7u, as_mask = s_s % 8 ? 3u : 7u;
         for (int w = 0; gather && w < n_walk; ++w) {
             const int64_t *m = ts->h_meta + 6 * w;
-            gather = !(m[1] && ((uintptr_t)epi[w] & 7u)) && !(m[3] && ((uintptr_t)epj[w] & 7u)) &&
-                     !(m[5] && ((uintptr_t)spj[w] & 7u));
+            gather = !(m[1] && ((uintptr_t)epi[w] & 7u)) && !(m[3] && ((uintptr_t)jw[w] & aj_mask)) &&
+                     !(m[5] && ((uintptr_t)sw[w] & as_mask));
         }
         if (!gather && mode == SPH_BATCH_STAGING_DEVICE)
             return batch_fail(SPH_ERR_STATE, ts->pageable == 1
-                                                 ? "SPH_BATCH_STAGING_DEVICE needs 8-byte aligned walk arrays"
+                                                 ? "SPH_BATCH_STAGING_DEVICE needs word-aligned walk arrays"
                                                  : "this GPU cannot read pageable host memory "
                                                    "(SPH_BATCH_STAGING_DEVICE)");
+    }
+    if (index && cudaMemsetAsync(ts->d_err, 0, sizeof(int), ts->stream) != cudaSuccess) {
+        cudaGetLastError();
+        return batch_fail(SPH_ERR_CUDA, "cannot clear the batch error word");
     }
     if (gather) {
         SPH_TRY(grow((char **)&ts->h_src, (char **)&ts->d_src, &ts->cap_src, sizeof(uint64_t) * 3 * (n_walk + 1)));
         for (int w = 0; w < n_walk; ++w) {
             const int64_t *m = ts->h_meta + 6 * w;
             ts->h_src[3 * w] = m[1] ? (uint64_t)(uintptr_t)epi[w] : 0;
-            ts->h_src[3 * w + 1] = m[3] ? (uint64_t)(uintptr_t)epj[w] : 0;
-            ts->h_src[3 * w + 2] = m[5] ? (uint64_t)(uintptr_t)spj[w] : 0;
+            ts->h_src[3 * w + 1] = m[3] ? (uint64_t)(uintptr_t)jw[w] : 0;
+            ts->h_src[3 * w + 2] = m[5] ? (uint64_t)(uintptr_t)sw[w] : 0;
         }
         if (cudaMemcpyAsync(ts->d_meta, ts->h_meta, sizeof(int64_t) * 6 * n_walk, cudaMemcpyHostToDevice,
                             ts->stream) != cudaSuccess ||
@@ -479,9 +511,8 @@ int stage(int tag, int kind, int n_walk, const EPI **epi, const int *n_epi, cons
             cudaGetLastError();
             return batch_fail(SPH_ERR_CUDA, "host-to-device copy failed");
         }
-        k_gather_walks<<<n_walk, 256, 0, ts->stream>>>(ts->d_meta, ts->d_src, ts->d_in, (int64_t)o_epj,
-                                                       (int64_t)o_spj, (int)sizeof(EPI), (int)sizeof(EPJ),
-                                                       (int)sizeof(sph_spj_monopole));
+        k_gather_walks<<<n_walk, 256, 0, ts->stream>>>(ts->d_meta, ts->d_src, ts->d_in, (int64_t)L.o_epj,
+                                                       (int64_t)L.o_spj, (int)sizeof(EPI), (int)s_j, (int)s_s);
         if (cudaGetLastError() != cudaSuccess || cudaEventRecord(ts->gathered, ts->stream) != cudaSuccess) {
             cudaGetLastError();
             return batch_fail(SPH_ERR_CUDA, "walk gather launch failed");
@@ -498,12 +529,10 @@ int stage(int tag, int kind, int n_walk, const EPI **epi, const int *n_epi, cons
         for (int w = 0; w < n_walk; ++w) {
             const int64_t *m = ts->h_meta + 6 * w;
             if (m[1]) std::memcpy(ts->h_in + sizeof(EPI) * m[0], epi[w], sizeof(EPI) * m[1]);
-            if (m[3]) std::memcpy(ts->h_in + o_epj + sizeof(EPJ) * m[2], epj[w], sizeof(EPJ) * m[3]);
-            if (m[5])
-                std::memcpy(ts->h_in + o_spj + sizeof(sph_spj_monopole) * m[4], spj[w],
-                            sizeof(sph_spj_monopole) * m[5]);
+            if (m[3]) std::memcpy(ts->h_in + L.o_epj + s_j * m[2], jw[w], s_j * m[3]);
+            if (m[5]) std::memcpy(ts->h_in + L.o_spj + s_s * m[4], sw[w], s_s * m[5]);
         }
-        if (cudaMemcpyAsync(ts->d_in, ts->h_in, o_spj + b_spj, cudaMemcpyHostToDevice, ts->stream) != cudaSuccess ||
+        if (cudaMemcpyAsync(ts->d_in, ts->h_in, L.end, cudaMemcpyHostToDevice, ts->stream) != cudaSuccess ||
             cudaMemcpyAsync(ts->d_meta, ts->h_meta, sizeof(int64_t) * 6 * n_walk, cudaMemcpyHostToDevice,
                             ts->stream) != cudaSuccess) {
             cudaGetLastError();
@@ -511,10 +540,11 @@ int stage(int tag, int kind, int n_walk, const EPI **epi, const int *n_epi, cons
         }
     }
     ts->pending_kind = kind;
+    ts->pending_index = index;
     ts->pending_walks = n_walk;
-    ts->pending_out_bytes = sizeof(RES) * ni;
+    ts->pending_out_bytes = sizeof(RES) * L.ni;
     *ts_out = ts;
-    (void)o_epj;
+    *lay = L;
     return SPH_OK;
 }
 
@@ -534,10 +564,95 @@ int finish_dispatch(TagState *ts) {
     return SPH_OK;
 }
 
+// ---------------------------------------------------------------------------
+// index form: the EPJ (and SPJ) arrays of a pass, sent once and kept on the device
+
+struct Resident {
+    char *d_j = nullptr, *d_s = nullptr;
+    size_t cap_j = 0, cap_s = 0;
+    int64_t n_j = 0, n_s = 0;
+    int device = -1;
+    std::mutex mu;
+};
+Resident g_res[4];   // per kind: density, derivative, hydro, gravity
+
+int grow_dev(char **d, size_t *cap, size_t need) {
+    if (need <= *cap) return SPH_OK;
+    const size_t c = std::max(need, *cap + *cap / 2);
+    if (*d) cudaFree(*d);
+    *d = nullptr;
+    *cap = 0;
+    if (cudaMalloc((void **)d, c) != cudaSuccess) {
+        cudaGetLastError();
+        return batch_fail(SPH_ERR_OOM, "allocation of the sent EPJ / SPJ arrays failed");
+    }
+    *cap = c;
+    return SPH_OK;
+}
+
+// send_flag: the pass's whole EPJ array (and SPJ array) to the device.  Index dispatches of this
+// kind already issued may still read the previous arrays: their tags' streams are waited for first
+// (tag by tag, one lock at a time).  Returns after the copy, so the caller may reuse its arrays.
+int send_resident(int kind, const void *a, int64_t n, size_t sa, const void *b, int64_t nb, size_t sb) {
+    if (n < 0 || nb < 0 || (n > 0 && !a) || (nb > 0 && !b)) return batch_fail(SPH_ERR_ARG, "bad EPJ / SPJ array");
+    for (int t = 0; t < MAX_TAGS; ++t) {
+        std::lock_guard<std::mutex> lk(g_tags[t].mu);
+        if (g_tags[t].pending_kind == kind && g_tags[t].pending_index) cudaStreamSynchronize(g_tags[t].stream);
+    }
+    Resident &R = g_res[kind];
+    std::lock_guard<std::mutex> lk(R.mu);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (R.device != dev) {   // buffers of another device are dropped
+        if (R.device >= 0 && (R.d_j || R.d_s)) {
+            cudaSetDevice(R.device);
+            if (R.d_j) cudaFree(R.d_j);
+            if (R.d_s) cudaFree(R.d_s);
+            cudaSetDevice(dev);
+        }
+        R.d_j = R.d_s = nullptr;
+        R.cap_j = R.cap_s = 0;
+        R.device = dev;
+    }
+    R.n_j = R.n_s = 0;
+    SPH_TRY(grow_dev(&R.d_j, &R.cap_j, sa * (size_t)n + 16));
+    SPH_TRY(grow_dev(&R.d_s, &R.cap_s, sb * (size_t)nb + 16));
+    if ((n > 0 && cudaMemcpy(R.d_j, a, sa * (size_t)n, cudaMemcpyHostToDevice) != cudaSuccess) ||
+        (nb > 0 && cudaMemcpy(R.d_s, b, sb * (size_t)nb, cudaMemcpyHostToDevice) != cudaSuccess)) {
+        cudaGetLastError();
+        return batch_fail(SPH_ERR_CUDA, "copy of the sent EPJ / SPJ arrays failed");
+    }
+    R.n_j = n;
+    R.n_s = nb;
+    return SPH_OK;
+}
+
+// the sent arrays of a kind, as the index walks' j sources (their error word is the tag's, set
+// after staging); walks with entries need a sent array.  Checked before anything is staged, so a
+// refused dispatch leaves nothing reading the caller's arrays.
+template <class EPJ, class SPJ>
+int resident_src(int kind, int n_walk, const int *n_epj, const int *n_spj, JSrc<EPJ> *js, JSrc<SPJ> *ss) {
+    Resident &R = g_res[kind];
+    std::lock_guard<std::mutex> lk(R.mu);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    bool need_j = false, need_s = false;
+    for (int w = 0; w < n_walk && n_epj; ++w) {
+        need_j = need_j || n_epj[w] > 0;
+        need_s = need_s || (n_spj && n_spj[w] > 0);
+    }
+    if ((need_j && (R.n_j == 0 || R.device != dev)) || (need_s && (R.n_s == 0 || R.device != dev)))
+        return batch_fail(SPH_ERR_STATE, "index walks before their EPJ / SPJ array was sent (send_flag)");
+    *js = JSrc<EPJ>{(const EPJ *)R.d_j, nullptr, R.n_j, nullptr};
+    if (ss) *ss = JSrc<SPJ>{(const SPJ *)R.d_s, nullptr, R.n_s, nullptr};
+    return SPH_OK;
+}
+
 template <class RES>
 int retrieve(int tag, int kind, int n_walk, const int *n_epi, RES **result) {
     SPH_TAG_LOCK(tag);
     TagState &ts = g_tags[tag];
+    if (n_walk == 0 && ts.pending_kind < 0) return SPH_OK;   // nothing was dispatched (a send-only call)
     if (ts.pending_kind != kind || ts.pending_walks != n_walk)
         return batch_fail(SPH_ERR_STATE, "retrieve does not match the last dispatch on this tag");
     std::vector<int64_t> off(n_walk + 1, 0);
@@ -552,6 +667,12 @@ int retrieve(int tag, int kind, int n_walk, const int *n_epi, RES **result) {
         ts.pending_kind = -1;
         return batch_fail(SPH_ERR_ARG, "null result pointer, or walk sizes that differ from the dispatch's");
     }
+    const bool index = ts.pending_index;
+    if (index) cudaMemcpyAsync(ts.h_err, ts.d_err, sizeof(int), cudaMemcpyDeviceToHost, ts.stream);
+    auto index_check = [&]() {
+        return (index && *ts.h_err) ? batch_fail(SPH_ERR_ARG, "an index walk names an entry outside the sent array")
+                                    : SPH_OK;
+    };
     if (ts.direct_out && aligned && n_walk > 0) {
         // the scatter kernel writes every walk's results into the caller's arrays
         const int rc = grow((char **)&ts.h_dst, (char **)&ts.d_dst, &ts.cap_dst, sizeof(uint64_t) * (n_walk + 1));
@@ -570,7 +691,7 @@ int retrieve(int tag, int kind, int n_walk, const int *n_epi, RES **result) {
         if (e != cudaSuccess || l != cudaSuccess)
             return batch_fail(SPH_ERR_CUDA, std::string("batch kernel or result scatter failed: ") +
                                                  cudaGetErrorString(e != cudaSuccess ? e : l));
-        return SPH_OK;
+        return index_check();
     }
     if (ts.direct_out && ts.pending_out_bytes)   // results left on the device: bring them to the host now
         cudaMemcpyAsync(ts.h_out, ts.d_out, ts.pending_out_bytes, cudaMemcpyDeviceToHost, ts.stream);
@@ -583,8 +704,73 @@ int retrieve(int tag, int kind, int n_walk, const int *n_epi, RES **result) {
 #pragma omp parallel for schedule(dynamic, 8) if (n_walk > 8 && off[n_walk] > 65536)
     for (int w = 0; w < n_walk; ++w)
         if (n_epi[w] > 0) std::memcpy(result[w], ts.h_out + sizeof(RES) * off[w], sizeof(RES) * n_epi[w]);
-    return SPH_OK;
+    return index_check();
 }
+
+// one dispatch of a kind, payload or index form: stage, launch the functor kernel, start the
+// result copy
+template <class EPI, class EPJ, class RES, class LAUNCH>
+int dispatch_walks(int tag, int kind, int n_walk, const EPI **epi, const int *n_epi, const void *const *jw,
+                   const int *n_epj, bool index, LAUNCH launch) {
+    SPH_TAG_LOCK(tag);
+    TagState *ts = nullptr;
+    Layout L;
+    JSrc<EPJ> rj{};
+    if (index) SPH_TRY((resident_src<EPJ, sph_spj_monopole>(kind, n_walk, n_epj, nullptr, &rj, nullptr)));
+    SPH_TRY((stage<EPI, RES>(tag, kind, n_walk, epi, n_epi, jw, index ? sizeof(int) : sizeof(EPJ), n_epj, nullptr, 0,
+                             nullptr, index, &ts, &L)));
+    // from here on the dispatch runs to finish_dispatch, which waits for a device gather
+    if (n_walk > 0) {
+        JSrc<EPJ> js{(const EPJ *)(ts->d_in + L.o_epj), nullptr, 0, nullptr};
+        if (index) js = JSrc<EPJ>{rj.base, (const int *)(ts->d_in + L.o_epj), rj.n, ts->d_err};
+        launch(ts, (const EPI *)ts->d_in, js, (RES *)ts->d_out, g_batch_prec.load() == SPH_PREC_MIXED);
+    }
+    return finish_dispatch(ts);
+}
+
+int dispatch_grav(int tag, int n_walk, const sph_epi_grav **epi, const int *n_epi, const void *const *jw,
+                  const int *n_epj, const void *const *sw, const int *n_spj, bool index) {
+    SPH_TAG_LOCK(tag);
+    TagState *ts = nullptr;
+    Layout L;
+    const size_t s_j = index ? sizeof(int) : sizeof(sph_epj_grav), s_s = index ? sizeof(int) : sizeof(sph_spj_monopole);
+    JSrc<sph_epj_grav> rj{};
+    JSrc<sph_spj_monopole> rs{};
+    if (index) SPH_TRY((resident_src<sph_epj_grav, sph_spj_monopole>(3, n_walk, n_epj, n_spj, &rj, &rs)));
+    SPH_TRY((stage<sph_epi_grav, sph_result_grav>(tag, 3, n_walk, epi, n_epi, jw, s_j, n_epj, sw, s_s, n_spj, index,
+                                                  &ts, &L)));
+    // from here on the dispatch runs to finish_dispatch, which waits for a device gather
+    if (n_walk > 0) {
+        JSrc<sph_epj_grav> js{(const sph_epj_grav *)(ts->d_in + L.o_epj), nullptr, 0, nullptr};
+        JSrc<sph_spj_monopole> ss{(const sph_spj_monopole *)(ts->d_in + L.o_spj), nullptr, 0, nullptr};
+        if (index) {
+            js = JSrc<sph_epj_grav>{rj.base, (const int *)(ts->d_in + L.o_epj), rj.n, ts->d_err};
+            ss = JSrc<sph_spj_monopole>{rs.base, (const int *)(ts->d_in + L.o_spj), rs.n, ts->d_err};
+        }
+        const sph_epi_grav *ei = (const sph_epi_grav *)ts->d_in;
+        sph_result_grav *res = (sph_result_grav *)ts->d_out;
+        if (g_batch_prec.load() == SPH_PREC_MIXED) batch32_grav(n_walk, ts->stream, ts->d_meta, ei, js, ss, res);
+        else k_walk_grav<<<n_walk, WT, 0, ts->stream>>>(ts->d_meta, ei, js, ss, res);
+    }
+    return finish_dispatch(ts);
+}
+
+auto launch_dens = [](TagState *ts, const sph_epi_dens *ei, JSrc<sph_epj_dens> js, sph_result_dens *res, bool mixed) {
+    const int n_walk = ts->pending_walks;
+    if (mixed) batch32_dens(n_walk, ts->stream, ts->d_meta, ei, js, res);
+    else k_walk_dens<<<n_walk, WT, 0, ts->stream>>>(ts->d_meta, ei, js, res);
+};
+auto launch_drvt = [](TagState *ts, const sph_epi_drvt *ei, JSrc<sph_epj_drvt> js, sph_result_drvt *res, bool mixed) {
+    const int n_walk = ts->pending_walks;
+    if (mixed) batch32_drvt(n_walk, ts->stream, ts->d_meta, ei, js, res);
+    else k_walk_drvt<<<n_walk, WT, 0, ts->stream>>>(ts->d_meta, ei, js, res);
+};
+auto launch_hydro = [](TagState *ts, const sph_epi_hydro *ei, JSrc<sph_epj_hydro> js, sph_result_hydro *res,
+                       bool mixed) {
+    const int n_walk = ts->pending_walks;
+    if (mixed) batch32_hydro(n_walk, ts->stream, ts->d_meta, ei, js, res);
+    else k_walk_hydro<<<n_walk, WT, 0, ts->stream>>>(ts->d_meta, ei, js, res);
+};
 
 }  // namespace
 
@@ -606,101 +792,84 @@ int sph_batch_set_precision(int precision) {
     return SPH_OK;
 }
 
+// ---- payload form (calcForceAllAndWriteBackMultiWalk)
+
 int sph_dispatch_dens(int tag, int n_walk, const sph_epi_dens **epi, const int *n_epi, const sph_epj_dens **epj,
                       const int *n_epj) {
-    SPH_TAG_LOCK(tag);
-    TagState *ts = nullptr;
-    SPH_TRY((stage<sph_epi_dens, sph_epj_dens, sph_result_dens>(tag, 0, n_walk, epi, n_epi, epj, n_epj, nullptr,
-                                                                nullptr, &ts)));
-    if (n_walk > 0) {
-        int64_t ni = 0;
-        for (int w = 0; w < n_walk; ++w) ni += n_epi[w];
-        const size_t o_epj = (sizeof(sph_epi_dens) * ni + 15) & ~size_t(15);
-        if (g_batch_prec.load() == SPH_PREC_MIXED)
-            batch32_dens(n_walk, ts->stream, ts->d_meta, ts->d_in, ts->d_in + o_epj, ts->d_out);
-        else
-            k_walk_dens<<<n_walk, WT, 0, ts->stream>>>(ts->d_meta, (const sph_epi_dens *)ts->d_in,
-                                                       (const sph_epj_dens *)(ts->d_in + o_epj),
-                                                       (sph_result_dens *)ts->d_out);
-    }
-    return finish_dispatch(ts);
+    return dispatch_walks<sph_epi_dens, sph_epj_dens, sph_result_dens>(tag, 0, n_walk, epi, n_epi,
+                                                                       (const void *const *)epj, n_epj, false,
+                                                                       launch_dens);
+}
+
+int sph_dispatch_drvt(int tag, int n_walk, const sph_epi_drvt **epi, const int *n_epi, const sph_epj_drvt **epj,
+                      const int *n_epj) {
+    return dispatch_walks<sph_epi_drvt, sph_epj_drvt, sph_result_drvt>(tag, 1, n_walk, epi, n_epi,
+                                                                       (const void *const *)epj, n_epj, false,
+                                                                       launch_drvt);
+}
+
+int sph_dispatch_hydro(int tag, int n_walk, const sph_epi_hydro **epi, const int *n_epi, const sph_epj_hydro **epj,
+                       const int *n_epj) {
+    return dispatch_walks<sph_epi_hydro, sph_epj_hydro, sph_result_hydro>(tag, 2, n_walk, epi, n_epi,
+                                                                          (const void *const *)epj, n_epj, false,
+                                                                          launch_hydro);
+}
+
+int sph_dispatch_grav(int tag, int n_walk, const sph_epi_grav **epi, const int *n_epi, const sph_epj_grav **epj,
+                      const int *n_epj, const sph_spj_monopole **spj, const int *n_spj) {
+    return dispatch_grav(tag, n_walk, epi, n_epi, (const void *const *)epj, n_epj, (const void *const *)spj, n_spj,
+                         false);
+}
+
+// ---- index form (calcForceAllAndWriteBackMultiWalkIndex)
+
+int sph_dispatch_index_dens(int tag, int n_walk, const sph_epi_dens **epi, const int *n_epi, const int **id_epj,
+                            const int *n_epj, const sph_epj_dens *epj, int n_epj_tot, int send_flag) {
+    if (send_flag) SPH_TRY(send_resident(0, epj, n_epj_tot, sizeof(sph_epj_dens), nullptr, 0, 1));
+    if (n_walk == 0 && send_flag) return SPH_OK;
+    return dispatch_walks<sph_epi_dens, sph_epj_dens, sph_result_dens>(tag, 0, n_walk, epi, n_epi,
+                                                                       (const void *const *)id_epj, n_epj, true,
+                                                                       launch_dens);
+}
+
+int sph_dispatch_index_drvt(int tag, int n_walk, const sph_epi_drvt **epi, const int *n_epi, const int **id_epj,
+                            const int *n_epj, const sph_epj_drvt *epj, int n_epj_tot, int send_flag) {
+    if (send_flag) SPH_TRY(send_resident(1, epj, n_epj_tot, sizeof(sph_epj_drvt), nullptr, 0, 1));
+    if (n_walk == 0 && send_flag) return SPH_OK;
+    return dispatch_walks<sph_epi_drvt, sph_epj_drvt, sph_result_drvt>(tag, 1, n_walk, epi, n_epi,
+                                                                       (const void *const *)id_epj, n_epj, true,
+                                                                       launch_drvt);
+}
+
+int sph_dispatch_index_hydro(int tag, int n_walk, const sph_epi_hydro **epi, const int *n_epi, const int **id_epj,
+                             const int *n_epj, const sph_epj_hydro *epj, int n_epj_tot, int send_flag) {
+    if (send_flag) SPH_TRY(send_resident(2, epj, n_epj_tot, sizeof(sph_epj_hydro), nullptr, 0, 1));
+    if (n_walk == 0 && send_flag) return SPH_OK;
+    return dispatch_walks<sph_epi_hydro, sph_epj_hydro, sph_result_hydro>(tag, 2, n_walk, epi, n_epi,
+                                                                          (const void *const *)id_epj, n_epj, true,
+                                                                          launch_hydro);
+}
+
+int sph_dispatch_index_grav(int tag, int n_walk, const sph_epi_grav **epi, const int *n_epi, const int **id_epj,
+                            const int *n_epj, const int **id_spj, const int *n_spj, const sph_epj_grav *epj,
+                            int n_epj_tot, const sph_spj_monopole *spj, int n_spj_tot, int send_flag) {
+    if (send_flag)
+        SPH_TRY(send_resident(3, epj, n_epj_tot, sizeof(sph_epj_grav), spj, n_spj_tot, sizeof(sph_spj_monopole)));
+    if (n_walk == 0 && send_flag) return SPH_OK;
+    return dispatch_grav(tag, n_walk, epi, n_epi, (const void *const *)id_epj, n_epj, (const void *const *)id_spj,
+                         n_spj, true);
 }
 
 int sph_retrieve_dens(int tag, int n_walk, const int *n_epi, sph_result_dens **result) {
     return retrieve<sph_result_dens>(tag, 0, n_walk, n_epi, result);
 }
 
-int sph_dispatch_drvt(int tag, int n_walk, const sph_epi_drvt **epi, const int *n_epi, const sph_epj_drvt **epj,
-                      const int *n_epj) {
-    SPH_TAG_LOCK(tag);
-    TagState *ts = nullptr;
-    SPH_TRY((stage<sph_epi_drvt, sph_epj_drvt, sph_result_drvt>(tag, 1, n_walk, epi, n_epi, epj, n_epj, nullptr,
-                                                                nullptr, &ts)));
-    if (n_walk > 0) {
-        int64_t ni = 0;
-        for (int w = 0; w < n_walk; ++w) ni += n_epi[w];
-        const size_t o_epj = (sizeof(sph_epi_drvt) * ni + 15) & ~size_t(15);
-        if (g_batch_prec.load() == SPH_PREC_MIXED)
-            batch32_drvt(n_walk, ts->stream, ts->d_meta, ts->d_in, ts->d_in + o_epj, ts->d_out);
-        else
-            k_walk_drvt<<<n_walk, WT, 0, ts->stream>>>(ts->d_meta, (const sph_epi_drvt *)ts->d_in,
-                                                       (const sph_epj_drvt *)(ts->d_in + o_epj),
-                                                       (sph_result_drvt *)ts->d_out);
-    }
-    return finish_dispatch(ts);
-}
-
 int sph_retrieve_drvt(int tag, int n_walk, const int *n_epi, sph_result_drvt **result) {
     return retrieve<sph_result_drvt>(tag, 1, n_walk, n_epi, result);
 }
 
-int sph_dispatch_hydro(int tag, int n_walk, const sph_epi_hydro **epi, const int *n_epi, const sph_epj_hydro **epj,
-                       const int *n_epj) {
-    SPH_TAG_LOCK(tag);
-    TagState *ts = nullptr;
-    SPH_TRY((stage<sph_epi_hydro, sph_epj_hydro, sph_result_hydro>(tag, 2, n_walk, epi, n_epi, epj, n_epj, nullptr,
-                                                                   nullptr, &ts)));
-    if (n_walk > 0) {
-        int64_t ni = 0;
-        for (int w = 0; w < n_walk; ++w) ni += n_epi[w];
-        const size_t o_epj = (sizeof(sph_epi_hydro) * ni + 15) & ~size_t(15);
-        if (g_batch_prec.load() == SPH_PREC_MIXED)
-            batch32_hydro(n_walk, ts->stream, ts->d_meta, ts->d_in, ts->d_in + o_epj, ts->d_out);
-        else
-            k_walk_hydro<<<n_walk, WT, 0, ts->stream>>>(ts->d_meta, (const sph_epi_hydro *)ts->d_in,
-                                                        (const sph_epj_hydro *)(ts->d_in + o_epj),
-                                                        (sph_result_hydro *)ts->d_out);
-    }
-    return finish_dispatch(ts);
-}
-
 int sph_retrieve_hydro(int tag, int n_walk, const int *n_epi, sph_result_hydro **result) {
     return retrieve<sph_result_hydro>(tag, 2, n_walk, n_epi, result);
-}
-
-int sph_dispatch_grav(int tag, int n_walk, const sph_epi_grav **epi, const int *n_epi, const sph_epj_grav **epj,
-                      const int *n_epj, const sph_spj_monopole **spj, const int *n_spj) {
-    SPH_TAG_LOCK(tag);
-    TagState *ts = nullptr;
-    SPH_TRY((stage<sph_epi_grav, sph_epj_grav, sph_result_grav>(tag, 3, n_walk, epi, n_epi, epj, n_epj, spj, n_spj,
-                                                                &ts)));
-    if (n_walk > 0) {
-        int64_t ni = 0, nj = 0;
-        for (int w = 0; w < n_walk; ++w) {
-            ni += n_epi[w];
-            nj += n_epj[w];
-        }
-        const size_t o_epj = (sizeof(sph_epi_grav) * ni + 15) & ~size_t(15);
-        const size_t o_spj = (o_epj + sizeof(sph_epj_grav) * nj + 15) & ~size_t(15);
-        if (g_batch_prec.load() == SPH_PREC_MIXED)
-            batch32_grav(n_walk, ts->stream, ts->d_meta, ts->d_in, ts->d_in + o_epj, ts->d_in + o_spj, ts->d_out);
-        else
-            k_walk_grav<<<n_walk, WT, 0, ts->stream>>>(ts->d_meta, (const sph_epi_grav *)ts->d_in,
-                                                       (const sph_epj_grav *)(ts->d_in + o_epj),
-                                                       (const sph_spj_monopole *)(ts->d_in + o_spj),
-                                                       (sph_result_grav *)ts->d_out);
-    }
-    return finish_dispatch(ts);
 }
 
 int sph_retrieve_grav(int tag, int n_walk, const int *n_epi, sph_result_grav **result) {

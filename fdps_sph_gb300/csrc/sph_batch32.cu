@@ -9,7 +9,7 @@
 // kernel normalisation of the i-particle factored out of the sums, FP32 partial sums of 32 terms
 // added into compensated FP32 accumulators, and the per-particle epilogue (density floor and h, grad-h factor, dt, the normalisation) in FP64.  One
 // block per walk, one thread per i-particle, the walk's j-list staged through shared memory.
-#include "sph_physics.cuh"
+#include "sph_batch.cuh"
 
 using namespace sph;
 
@@ -40,7 +40,7 @@ __device__ __forceinline__ float dfd(float ah, float al, float bh, float bl) { r
 
 // CalcDensity: rho = max(5, norm sum m_j W), h = 1.2 (m / rho)^(1/3)
 __global__ void __launch_bounds__(WT) k_walk_dens32(const int64_t *meta, const sph_epi_dens *epi,
-                                                    const sph_epj_dens *epj, sph_result_dens *res) {
+                                                    JSrc<sph_epj_dens> epj, sph_result_dens *res) {
     __shared__ DF3 sp[WT];
     __shared__ float sm[WT];
     const int64_t *M = meta + 6 * blockIdx.x;
@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(WT) k_walk_dens32(const int64_t *meta, const s
 
 // CalcDerivative + grad-h factor: div v, rot v, grad_smth (force.h:89-106)
 __global__ void __launch_bounds__(WT) k_walk_drvt32(const int64_t *meta, const sph_epi_drvt *epi,
-                                                    const sph_epj_drvt *epj, sph_result_drvt *res) {
+                                                    JSrc<sph_epj_drvt> epj, sph_result_drvt *res) {
     __shared__ DF3 sp[WT], sv[WT];
     __shared__ float sm[WT];
     const int64_t *M = meta + 6 * blockIdx.x;
@@ -183,7 +183,7 @@ struct HJ {
 };
 
 __global__ void __launch_bounds__(WT) k_walk_hydro32(const int64_t *meta, const sph_epi_hydro *epi,
-                                                     const sph_epj_hydro *epj, sph_result_hydro *res) {
+                                                     JSrc<sph_epj_hydro> epj, sph_result_hydro *res) {
     __shared__ HJ sj[WT];
     const int64_t *M = meta + 6 * blockIdx.x;
     const int64_t io = M[0], ni = M[1], jo = M[2], nj = M[3];
@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(WT) k_walk_hydro32(const int64_t *meta, const 
 
 // CalcGravityForce<EPJ::Grav> then <SPJMonopole> (force.h:154-168): G m folded into the tile
 __global__ void __launch_bounds__(WT) k_walk_grav32(const int64_t *meta, const sph_epi_grav *epi,
-                                                    const sph_epj_grav *epj, const sph_spj_monopole *spj,
+                                                    JSrc<sph_epj_grav> epj, JSrc<sph_spj_monopole> spj,
                                                     sph_result_grav *res) {
     __shared__ DF3 sp[WT];
     __shared__ float sg[WT];
@@ -367,22 +367,21 @@ __global__ void __launch_bounds__(WT) k_walk_grav32(const int64_t *meta, const s
 namespace sph {
 
 // launchers for sph_batch.cu: one block per walk on the tag's stream
-void batch32_dens(int n_walk, cudaStream_t st, const int64_t *meta, const void *epi, const void *epj, void *res) {
-    k_walk_dens32<<<n_walk, WT, 0, st>>>(meta, (const sph_epi_dens *)epi, (const sph_epj_dens *)epj,
-                                         (sph_result_dens *)res);
+void batch32_dens(int n_walk, cudaStream_t st, const int64_t *meta, const sph_epi_dens *epi, JSrc<sph_epj_dens> epj,
+                  sph_result_dens *res) {
+    k_walk_dens32<<<n_walk, WT, 0, st>>>(meta, epi, epj, res);
 }
-void batch32_drvt(int n_walk, cudaStream_t st, const int64_t *meta, const void *epi, const void *epj, void *res) {
-    k_walk_drvt32<<<n_walk, WT, 0, st>>>(meta, (const sph_epi_drvt *)epi, (const sph_epj_drvt *)epj,
-                                         (sph_result_drvt *)res);
+void batch32_drvt(int n_walk, cudaStream_t st, const int64_t *meta, const sph_epi_drvt *epi, JSrc<sph_epj_drvt> epj,
+                  sph_result_drvt *res) {
+    k_walk_drvt32<<<n_walk, WT, 0, st>>>(meta, epi, epj, res);
 }
-void batch32_hydro(int n_walk, cudaStream_t st, const int64_t *meta, const void *epi, const void *epj, void *res) {
-    k_walk_hydro32<<<n_walk, WT, 0, st>>>(meta, (const sph_epi_hydro *)epi, (const sph_epj_hydro *)epj,
-                                          (sph_result_hydro *)res);
+void batch32_hydro(int n_walk, cudaStream_t st, const int64_t *meta, const sph_epi_hydro *epi,
+                   JSrc<sph_epj_hydro> epj, sph_result_hydro *res) {
+    k_walk_hydro32<<<n_walk, WT, 0, st>>>(meta, epi, epj, res);
 }
-void batch32_grav(int n_walk, cudaStream_t st, const int64_t *meta, const void *epi, const void *epj,
-                  const void *spj, void *res) {
-    k_walk_grav32<<<n_walk, WT, 0, st>>>(meta, (const sph_epi_grav *)epi, (const sph_epj_grav *)epj,
-                                         (const sph_spj_monopole *)spj, (sph_result_grav *)res);
+void batch32_grav(int n_walk, cudaStream_t st, const int64_t *meta, const sph_epi_grav *epi, JSrc<sph_epj_grav> epj,
+                  JSrc<sph_spj_monopole> spj, sph_result_grav *res) {
+    k_walk_grav32<<<n_walk, WT, 0, st>>>(meta, epi, epj, spj, res);
 }
 
 }  // namespace sph

@@ -42,7 +42,8 @@ EXPORTS = [
     "sph_add_run", "sph_remove_run", "sph_list_runs", "sph_run_info", "sph_download_run", "sph_run_diagnostics",
     "sph_autotune", "sph_set_eos_ideal", "sph_set_eos_entropy", "sph_eos_eval", "sph_download_fields",
     "sph_step_download", "sph_read_eos_table_file", "sph_read_eos_table_error", "sph_get_grav_lists",
-    "sph_batch_set_precision", "sph_batch_set_staging",
+    "sph_batch_set_precision", "sph_batch_set_staging", "sph_dispatch_index_dens", "sph_dispatch_index_drvt",
+    "sph_dispatch_index_hydro", "sph_dispatch_index_grav",
 ]
 # fields a step reads or carries unchanged (SPH_STEP_INPUT_FIELDS): what SPH_UPLOAD_STEP_INPUTS copies
 STEP_INPUT_FIELDS = ["x", "y", "z", "vx", "vy", "vz", "mass", "smth", "eng", "ava", "ax", "ay", "az", "eng_dot",
@@ -90,6 +91,10 @@ def load() -> C.CDLL:
         getattr(L, f"sph_dispatch_{k}").argtypes = [C.c_int, C.c_int, P, i32p, P, i32p]
         getattr(L, f"sph_retrieve_{k}").argtypes = [C.c_int, C.c_int, i32p, P]
     L.sph_dispatch_grav.argtypes = [C.c_int, C.c_int, P, i32p, P, i32p, P, i32p]
+    for k in ("dens", "drvt", "hydro"):
+        getattr(L, f"sph_dispatch_index_{k}").argtypes = [C.c_int, C.c_int, P, i32p, P, i32p, P, C.c_int, C.c_int]
+    L.sph_dispatch_index_grav.argtypes = [C.c_int, C.c_int, P, i32p, P, i32p, P, i32p, P, C.c_int, P, C.c_int,
+                                          C.c_int]
     L.sph_retrieve_grav.argtypes = [C.c_int, C.c_int, i32p, P]
     L.sph_batch_last_error.restype = C.c_char_p
     L.sph_batch_set_precision.argtypes = [C.c_int]
@@ -488,6 +493,37 @@ def dispatch(kind: str, tag: int, epi_list, epj_list, spj_list=None):
     if rc != SPH_OK:
         raise SphError(rc, L.sph_batch_last_error().decode())
     return n_epi
+
+
+def dispatch_index(kind: str, tag: int, epi_list, id_list, epj_all=None, id_spj_list=None, spj_all=None,
+                   send=False):
+    """the index form (sph_dispatch_index_*): walk w's j entries are epj_all[id_list[w]] (and, for
+    gravity, spj_all[id_spj_list[w]]); send=True first copies epj_all (and spj_all) to the device,
+    as the first call of a pass does.  Returns n_epi for retrieve()."""
+    L = load()
+    n_walk = len(epi_list)
+    for e in epi_list:
+        assert e.dtype == _KINDS[kind][0]
+    ids = [np.ascontiguousarray(a, dtype=np.int32) for a in id_list]
+    n_epi = (C.c_int * max(1, n_walk))(*[len(e) for e in epi_list])
+    n_epj = (C.c_int * max(1, n_walk))(*[len(a) for a in ids])
+    pe, pj = _ptr_array(epi_list), _ptr_array(ids)
+    ea = epj_all if epj_all is not None else np.zeros(0, _KINDS[kind][1])
+    assert ea.dtype == _KINDS[kind][1] and ea.flags.c_contiguous
+    if kind == "grav":
+        sids = [np.ascontiguousarray(a, dtype=np.int32) for a in (id_spj_list if id_spj_list is not None
+                                                                    else [np.zeros(0, np.int32)] * n_walk)]
+        sa = spj_all if spj_all is not None else np.zeros(0, T.SPJ_MONO)
+        n_spj = (C.c_int * max(1, n_walk))(*[len(a) for a in sids])
+        rc = L.sph_dispatch_index_grav(tag, n_walk, pe, n_epi, pj, n_epj, _ptr_array(sids), n_spj,
+                                       ea.ctypes.data if len(ea) else None, len(ea),
+                                       sa.ctypes.data if len(sa) else None, len(sa), int(send))
+    else:
+        rc = getattr(L, f"sph_dispatch_index_{kind}")(tag, n_walk, pe, n_epi, pj, n_epj,
+                                                      ea.ctypes.data if len(ea) else None, len(ea), int(send))
+    if rc != SPH_OK:
+        raise SphError(rc, L.sph_batch_last_error().decode())
+    return n_epi   # the call has read the index arrays: they may go
 
 
 def retrieve(kind: str, tag: int, n_epi):

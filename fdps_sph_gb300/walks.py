@@ -17,7 +17,11 @@ MultiWalk loop does, so the boundary can be measured on a full step:
   max(2.5 h_max, 2.5 h_j) of it (symmetric); as in FDPS, out-of-support j add
   zero to the sums and only enter the hydro functor's v_sig;
 * the loop: walks in batches of n_walk_limit, batch b dispatched on tag
-  b mod n_tags after the batch that last used that tag has been retrieved.
+  b mod n_tags after the batch that last used that tag has been retrieved;
+* two forms: the payload form (calcForceAllAndWriteBackMultiWalk: every walk
+  carries copies of its j payloads) and the index form
+  (calcForceAllAndWriteBackMultiWalkIndex: the pass's EPJ / SPJ arrays are
+  sent once, with send_flag, and every walk carries int32 indices into them).
 
 Used by bench.py's drop-in measurement; host-side numpy and scipy only.
 """
@@ -123,10 +127,24 @@ class Walks:
         com = tr["com"][gl["spj"]]
         spj["pos"], spj["mass"] = com[:, :3], com[:, 3]
         self.spj = (spj, np.concatenate([gl["spj_off"], [len(gl["spj"])]]))
+        # the index form: the whole EPJ array of each kind (every particle, sorted order), every cell
+        # as an SPJ, and the walks' j entries as int32 indices into them
+        self.epj_all = epj
+        spj_all = np.zeros(len(tr["com"]), T.SPJ_MONO)
+        spj_all["pos"], spj_all["mass"] = tr["com"][:, :3], tr["com"][:, 3]
+        self.spj_all = spj_all
+        i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
+        self.jindex = {"dens": (i32(g_idx), g_off), "drvt": (i32(g_idx), g_off), "hydro": (i32(s_idx), s_off),
+                       "grav": (i32(gl["epj"]), self.jlist["grav"][1])}
+        self.sindex = (i32(gl["spj"]), self.spj[1])
         self.result = {k: np.zeros(self.n, _RES[k]) for k in KINDS}
         self.staged_bytes = {k: self.n * _EPI[k].itemsize + len(self.jlist[k][0]) * _EPJ[k].itemsize
                              for k in KINDS}
         self.staged_bytes["grav"] += len(spj) * T.SPJ_MONO.itemsize
+        # index form: EPI payloads, 4-byte indices, and the sent arrays once per pass
+        self.index_bytes = {k: self.n * _EPI[k].itemsize + 4 * len(self.jindex[k][0]) + self.n * _EPJ[k].itemsize
+                            for k in KINDS}
+        self.index_bytes["grav"] += 4 * len(self.sindex[0]) + len(spj_all) * T.SPJ_MONO.itemsize
         self.sorted_state = S
         self._batch_cache = {}
 
@@ -134,14 +152,15 @@ class Walks:
         base = arr.ctypes.data
         return (C.c_void_p * (w1 - w0))(*[base + int(o) * itemsize for o in offs[w0:w1]])
 
-    def _batches(self, kind, n_walk_limit):
-        """the argument arrays of every batch of `kind` (walk pointers into this object's payload
-        and result arrays, which stay in place, and the walk sizes), built once per (kind,
-        n_walk_limit): FDPS hands its callbacks such arrays, so building them is not the
+    def _batches(self, kind, n_walk_limit, index=False):
+        """the argument arrays of every batch of `kind` (walk pointers into this object's payload,
+        index and result arrays, which stay in place, and the walk sizes), built once per (kind,
+        n_walk_limit, form): FDPS hands its callbacks such arrays, so building them is not the
         boundary's cost"""
-        key = (kind, n_walk_limit)
+        key = (kind, n_walk_limit, index)
         if key not in self._batch_cache:
-            epi, (ej, jo) = self.epi[kind], self.jlist[kind]
+            epi = self.epi[kind]
+            ej, jo = self.jindex[kind] if index else self.jlist[kind]
             res = self.result[kind]
             out = []
             for w0 in range(0, self.n_group, n_walk_limit):
@@ -152,23 +171,30 @@ class Walks:
                         self._ptrs(ej, jo, w0, w1, ej.itemsize),
                         (C.c_int * nw)(*(jo[w0 + 1:w1 + 1] - jo[w0:w1]).tolist())]
                 if kind == "grav":
-                    sa, so = self.spj
+                    sa, so = self.sindex if index else self.spj
                     args += [self._ptrs(sa, so, w0, w1, sa.itemsize),
                              (C.c_int * nw)(*(so[w0 + 1:w1 + 1] - so[w0:w1]).tolist())]
+                if index:   # the sent arrays (used by the send call only) and send_flag = 0
+                    ea = self.epj_all[kind]
+                    args += [ea.ctypes.data, len(ea)]
+                    if kind == "grav":
+                        args += [self.spj_all.ctypes.data, len(self.spj_all)]
+                    args += [0]
                 out.append((args, self._ptrs(res, self.start, w0, w1, res.itemsize)))
             self._batch_cache[key] = out
         return self._batch_cache[key]
 
-    def run(self, kind, n_walk_limit=256, n_tags=4, tag0=0):
-        """one pass of `kind` over every walk, the MultiWalk way; returns the host seconds taken"""
+    def run(self, kind, n_walk_limit=256, n_tags=4, tag0=0, index=False):
+        """one pass of `kind` over every walk, the MultiWalk way (index: the index form, whose first
+        call sends the pass's EPJ / SPJ arrays); returns the host seconds taken"""
         from . import lib
         L = lib.load()
         res = self.result[kind]
         res[:] = np.zeros(1, _RES[kind])
         if kind == "grav":
             res["dt"] = 1.0e30   # RESULT::Grav::clear()
-        batches = self._batches(kind, n_walk_limit)
-        disp = getattr(L, f"sph_dispatch_{kind}")
+        batches = self._batches(kind, n_walk_limit, index)
+        disp = getattr(L, f"sph_dispatch_index_{kind}" if index else f"sph_dispatch_{kind}")
         retr = getattr(L, f"sph_retrieve_{kind}")
         pend = {}
 
@@ -179,6 +205,12 @@ class Walks:
                 raise lib.SphError(rc, L.sph_batch_last_error().decode())
 
         t0 = time.perf_counter()
+        if index and batches:   # the send call: no walks, the whole arrays, send_flag = 1
+            a0 = batches[0][0]
+            none = [0, None, None, None, None] + ([None, None] if kind == "grav" else [])   # no walks
+            rc = disp(tag0, *none, *a0[len(none):-1], 1)
+            if rc != 0:
+                raise lib.SphError(rc, L.sph_batch_last_error().decode())
         for b, (args, rp) in enumerate(batches):
             tag = b % n_tags
             if tag in pend:
@@ -191,7 +223,7 @@ class Walks:
             retrieve(tag)
         return time.perf_counter() - t0
 
-    def step(self, n_dens_iter=4, **kw):
+    def step(self, n_dens_iter=4, **kw):   # kw: n_walk_limit, n_tags, tag0, index
         """the functor calls of one step of main.cpp:136-147 (density x n_dens_iter, derivative,
         hydro, gravity) on these walks; the seconds of each pass"""
         out = {"dens": sum(self.run("dens", **kw) for _ in range(n_dens_iter))}

@@ -10,7 +10,10 @@
 //    checked at compile time.  The reference functors cannot fail; these
 //    throw std::runtime_error when the GPU call fails (host side only).
 //  * Dispatch* / Retrieve*: the callbacks calcForceAllAndWriteBackMultiWalk
-//    takes, forwarding to sph_dispatch_* / sph_retrieve_*.
+//    takes, forwarding to sph_dispatch_* / sph_retrieve_*; DispatchIndex*:
+//    the dispatch callbacks of calcForceAllAndWriteBackMultiWalkIndex (the
+//    pass's EPJ / SPJ arrays sent once, walks as int32 indices), forwarding to
+//    sph_dispatch_index_*, retrieved with the same Retrieve*.
 //  * Simulation: RAII owner of a device-resident context (sph_ctx) running
 //    the step of main.cpp:125-173 on the GPU.
 #pragma once
@@ -182,6 +185,40 @@ int DispatchGrav(int tag, int n_walk, const EPI **epi, const int *n_epi, const E
 template <class RESULT>
 int RetrieveGrav(int tag, int n_walk, const int *n_epi, RESULT **result) {
     return sph_retrieve_grav(tag, n_walk, n_epi, reinterpret_cast<sph_result_grav **>(result));
+}
+
+// ---- MultiWalkIndex dispatch callbacks (retrieve: the Retrieve* above) ----------
+
+template <class EPI, class EPJ>
+int DispatchIndexDens(int tag, int n_walk, const EPI **epi, const int *n_epi, const int **id_epj, const int *n_epj,
+                      const EPJ *epj, int n_epj_tot, bool send_flag) {
+    static_assert(detail::same_layout<EPI, sph_epi_dens>() && detail::same_layout<EPJ, sph_epj_dens>(), "layout");
+    return sph_dispatch_index_dens(tag, n_walk, reinterpret_cast<const sph_epi_dens **>(epi), n_epi, id_epj, n_epj,
+                                   reinterpret_cast<const sph_epj_dens *>(epj), n_epj_tot, send_flag ? 1 : 0);
+}
+template <class EPI, class EPJ>
+int DispatchIndexDrvt(int tag, int n_walk, const EPI **epi, const int *n_epi, const int **id_epj, const int *n_epj,
+                      const EPJ *epj, int n_epj_tot, bool send_flag) {
+    static_assert(detail::same_layout<EPI, sph_epi_drvt>() && detail::same_layout<EPJ, sph_epj_drvt>(), "layout");
+    return sph_dispatch_index_drvt(tag, n_walk, reinterpret_cast<const sph_epi_drvt **>(epi), n_epi, id_epj, n_epj,
+                                   reinterpret_cast<const sph_epj_drvt *>(epj), n_epj_tot, send_flag ? 1 : 0);
+}
+template <class EPI, class EPJ>
+int DispatchIndexHydro(int tag, int n_walk, const EPI **epi, const int *n_epi, const int **id_epj, const int *n_epj,
+                       const EPJ *epj, int n_epj_tot, bool send_flag) {
+    static_assert(detail::same_layout<EPI, sph_epi_hydro>() && detail::same_layout<EPJ, sph_epj_hydro>(), "layout");
+    return sph_dispatch_index_hydro(tag, n_walk, reinterpret_cast<const sph_epi_hydro **>(epi), n_epi, id_epj, n_epj,
+                                    reinterpret_cast<const sph_epj_hydro *>(epj), n_epj_tot, send_flag ? 1 : 0);
+}
+template <class EPI, class EPJ, class SPJ>
+int DispatchIndexGrav(int tag, int n_walk, const EPI **epi, const int *n_epi, const int **id_epj, const int *n_epj,
+                      const int **id_spj, const int *n_spj, const EPJ *epj, int n_epj_tot, const SPJ *spj,
+                      int n_spj_tot, bool send_flag) {
+    static_assert(detail::same_layout<EPI, sph_epi_grav>() && detail::same_layout<EPJ, sph_epj_grav>() &&
+                      detail::same_layout<SPJ, sph_spj_monopole>(), "layout");
+    return sph_dispatch_index_grav(tag, n_walk, reinterpret_cast<const sph_epi_grav **>(epi), n_epi, id_epj, n_epj,
+                                   id_spj, n_spj, reinterpret_cast<const sph_epj_grav *>(epj), n_epj_tot,
+                                   reinterpret_cast<const sph_spj_monopole *>(spj), n_spj_tot, send_flag ? 1 : 0);
 }
 
 // ---- device-resident run -------------------------------------------------------

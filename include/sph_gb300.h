@@ -71,9 +71,10 @@ typedef struct { double mass; double pos[3]; } sph_spj_monopole;                
 typedef struct { double acc[3]; double pot; double dt; } sph_result_grav;                    /* class.h:75-86, 40 B */
 
 /* ---- 1. functor-compatible batch entry points ----------------------------
- * dispatch: copies the walks into pinned staging memory and launches
- * asynchronously on the stream of `tag` (0 <= tag < 64).  retrieve: waits
- * for that stream and writes result[w][0..n_epi[w]) for every walk.  Results
+ * dispatch: moves the walks to the device (sph_batch_set_staging) and
+ * launches asynchronously on the stream of `tag` (0 <= tag < 64); it returns
+ * once it has read the caller's arrays.  retrieve: waits for that stream and
+ * writes result[w][0..n_epi[w]) for every walk (n_epi as dispatched).  Results
  * are the reference functor's: RESULT::clear() (class.h:41-85) followed by
  * the i x j loop over the walk's full j-list.  Return 0 on success, as
  * FDPS's dispatch / retrieve callbacks do.  The signatures are those of the
@@ -92,6 +93,25 @@ int sph_dispatch_grav(int tag, int n_walk, const sph_epi_grav **epi, const int *
                       const sph_epj_grav **epj, const int *n_epj,
                       const sph_spj_monopole **spj, const int *n_spj);
 int sph_retrieve_grav(int tag, int n_walk, const int *n_epi, sph_result_grav **result);
+/* Index form: the dispatch callbacks of calcForceAllAndWriteBackMultiWalkIndex, retrieved with
+ * the sph_retrieve_* above.  A call with send_flag != 0 first copies the pass's whole EPJ array
+ * (epj[0..n_epj_tot)) and, for gravity, SPJ array to the device, where they stay for the kind's
+ * later index dispatches (FDPS sends them once per pass, with n_walk = 0); it waits for index
+ * dispatches of the same kind already issued, so it must not overlap new ones issued from other
+ * threads.  The walks then carry indices: walk w's j entries are epj[id_epj[w][k]], k <
+ * n_epj[w] (and spj[id_spj[w][k]]), in that order, so each j crosses the host link once per pass
+ * instead of once per walk that lists it.  Index walks before a send fail with SPH_ERR_STATE; an
+ * index outside the sent array makes the retrieve fail with SPH_ERR_ARG (the kernel reads entry
+ * 0 in its place).  Results equal the payload form's bit for bit. */
+int sph_dispatch_index_dens(int tag, int n_walk, const sph_epi_dens **epi, const int *n_epi, const int **id_epj,
+                            const int *n_epj, const sph_epj_dens *epj, int n_epj_tot, int send_flag);
+int sph_dispatch_index_drvt(int tag, int n_walk, const sph_epi_drvt **epi, const int *n_epi, const int **id_epj,
+                            const int *n_epj, const sph_epj_drvt *epj, int n_epj_tot, int send_flag);
+int sph_dispatch_index_hydro(int tag, int n_walk, const sph_epi_hydro **epi, const int *n_epi, const int **id_epj,
+                             const int *n_epj, const sph_epj_hydro *epj, int n_epj_tot, int send_flag);
+int sph_dispatch_index_grav(int tag, int n_walk, const sph_epi_grav **epi, const int *n_epi, const int **id_epj,
+                            const int *n_epj, const int **id_spj, const int *n_spj, const sph_epj_grav *epj,
+                            int n_epj_tot, const sph_spj_monopole *spj, int n_spj_tot, int send_flag);
 /* message of the last failed batch call on this thread */
 const char *sph_batch_last_error(void);
 /* Arithmetic of the dispatches that follow (all tags): SPH_PREC_FP64 (default) runs the reference

@@ -233,3 +233,50 @@ def test_batch_misaligned_walks_fall_back_to_the_host_copy():
             assert e.value.code == lib.SPH_ERR_STATE
         finally:
             lib.batch_staging("auto")
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batch_index_form_equals_payload_form(fun, precision):
+    """sph_dispatch_index_*: the pass's EPJ array sent once, the walks as indices into it -- the
+    same j entries in the same order as the payload form, so bit-identical results"""
+    from fdps_sph_gb300 import lib
+    lib.batch_precision(precision)
+    try:
+        for kind, key, state, fi, fj, dti, dtj in [
+                ("dens", "dens", "state_dens", DENS_I, DENS_J, T.EPI_DENS, T.EPJ_DENS),
+                ("hydro", "hydro", "state_hydro", HYD_I, HYD_J, T.EPI_HYDRO, T.EPJ_HYDRO)]:
+            F, ids = fun[state], fun["ids"]
+            W = walks(fun, key)
+            epi = [make(dti, F, ids, np.arange(s, s + n), fi) for s, n, _ in W]
+            epj_all = make(dtj, F, ids, np.arange(len(ids)), fj)
+            ref = lib.run_walks(kind, epi, [epj_all[j] for _, _, j in W], tag=3)
+            n_epi = lib.dispatch_index(kind, 3, epi, [j for _, _, j in W], epj_all, send=True)
+            got = lib.retrieve(kind, 3, n_epi)
+            for a, b in zip(ref, got):
+                assert a.tobytes() == b.tobytes(), kind
+    finally:
+        lib.batch_precision("fp64")
+
+
+def test_batch_index_form_errors():
+    """index walks before any send of their kind fail (SPH_ERR_STATE); an index outside the sent
+    array fails the retrieve (SPH_ERR_ARG) without reading outside it"""
+    from fdps_sph_gb300 import lib
+    a = np.zeros(4, T.EPI_DRVT)
+    a["smth"], a["dens"] = 1.0, 1.0
+    b = np.zeros(6, T.EPJ_DRVT)
+    b["mass"], b["smth"] = 1.0, 1.0
+    b["pos"] = np.arange(18, dtype=float).reshape(6, 3) * 0.1
+    # a fresh kind state cannot be guaranteed across tests, so the send of an empty array stands in
+    lib.dispatch_index("drvt", 11, [], [], np.zeros(0, T.EPJ_DRVT), send=True)
+    with pytest.raises(lib.SphError) as e:
+        lib.dispatch_index("drvt", 11, [a], [np.arange(3)])
+    assert e.value.code == lib.SPH_ERR_STATE
+    n_epi = lib.dispatch_index("drvt", 11, [a], [np.array([0, 5, 6, 2])], b, send=True)   # 6 is outside
+    with pytest.raises(lib.SphError) as e:
+        lib.retrieve("drvt", 11, n_epi)
+    assert e.value.code == lib.SPH_ERR_ARG
+    n_epi = lib.dispatch_index("drvt", 11, [a], [np.array([0, 5, 1, 2])])   # the array is still there
+    ok = lib.retrieve("drvt", 11, n_epi)[0]
+    ref = lib.run_walks("drvt", [a], [b[[0, 5, 1, 2]]], tag=11)[0]
+    assert ok.tobytes() == ref.tobytes()

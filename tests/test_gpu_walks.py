@@ -67,3 +67,26 @@ def test_multiwalk_mixed_precision_within_bar():
     assert vec_err_rms(hres["acc"], np.stack([S[FIELD[c]] for c in ("ax", "ay", "az")], 1)) < 1e-5
     assert scalar_err_rms(hres["eng_dot"], S[FIELD["eng_dot"]]) < 1e-5
     assert scalar_err_rms(d["div_v"], S[FIELD["div_v"]]) < 1e-5
+
+
+def test_multiwalk_index_form_equals_payload_form():
+    """the same walks through the index form (each pass's EPJ / SPJ arrays sent once, the walks as
+    indices): bit-identical to the payload form in FP64 and in mixed precision"""
+    F, ids, mats, _ = small_impact(18000, 2000, seed=43)
+    ctx = device_context(tillotson_materials(), precision=lib.PREC_FP64)
+    try:
+        ctx.upload(F, ids, mats)
+        ctx.prologue()
+        W = walks.Walks(ctx)
+    finally:
+        ctx.close()
+    for precision in ("fp64", "mixed"):
+        lib.batch_precision(precision)
+        try:
+            for kind in walks.KINDS:
+                W.run(kind, n_walk_limit=64, n_tags=3)
+                ref = W.result[kind].copy()
+                W.run(kind, n_walk_limit=64, n_tags=3, index=True)
+                assert W.result[kind].tobytes() == ref.tobytes(), (precision, kind)
+        finally:
+            lib.batch_precision("fp64")
