@@ -251,6 +251,8 @@ def state_errors(a, device, materials, mixed, f64):
         finally:
             ctx.close()
         e = accuracy.compare_on_state(S, sid, smat, materials, a.theta, device, t_c)
+        # the hydro error split between the density (through P) and the pair arithmetic
+        e["hydro_error_sources"] = accuracy.hydro_error_sources(S, sid, smat, materials, a.theta, device, t_c)
         e["state"] = (f"{n:,} particles placed in contact (centres 0.98 (R_t + R_i) apart, contact velocity of the "
                       f"30 deg / 1.2 v_esc orbit), after the prologue and {a.contact_steps} mixed steps")
         res["contact"] = e

@@ -124,3 +124,55 @@ def compare_on_state(F, ids, mats, materials, theta=0.5, device=0, time=0.0):
     out["activity"] = activity(Ff)
     out["distribution"] = error_distribution(Fm, Ff)
     return out
+
+
+def passes_of_state(F, ids, mats, materials, precision, theta=0.5, device=0, time=0.0):
+    """the derivative and hydro forces of state F evaluated pass by pass (sph_run_pass: sort and
+    octree, EoS, derivative, hydro) on the density and smoothing length F carries, instead of a
+    prologue's own density passes; returned in id order"""
+    from . import lib
+    ctx = lib.Context(precision=precision, device=device, theta=theta)
+    try:
+        for k, m in enumerate(materials):
+            ctx.set_material(k, m)
+        ctx.upload(F, ids, mats, time=time)
+        for p in (0, 2, 3, 4):
+            ctx.run_pass(p)
+        Fo, io, _ = ctx.download()
+    finally:
+        ctx.close()
+    return by_id(Fo, io)
+
+
+def hydro_error_sources(F, ids, mats, materials, theta=0.5, device=0, time=0.0):
+    """where the mixed path's hydro error on state F comes from: the error of a_hydro and du/dt
+    against the FP64 prologue (p99.9 and max, measures of force_errors) for
+      mixed            -- the mixed prologue (density and pairs in mixed precision);
+      mixed_pairs      -- mixed derivative and hydro on the FP64 prologue's density and h;
+      mixed_density    -- FP64 derivative and hydro on the mixed prologue's density and h;
+      fp64_passes      -- FP64 derivative and hydro on the FP64 density and h (zero: the pass
+                          sequence reproduces the prologue)"""
+    Ff = forces_of_state(F, ids, mats, materials, "fp64", theta, device, time)
+    Fm = forces_of_state(F, ids, mats, materials, "mixed", theta, device, time)
+    order = np.argsort(ids, kind="stable")
+    S, sid, smat = F[:, order], ids[order], mats[order]
+
+    def with_dens(src):
+        X = S.copy()
+        for k in ("dens", "smth"):
+            X[FIELD[k]] = src[FIELD[k]]
+        return X
+
+    runs = {"mixed": Fm,
+            "mixed_pairs": passes_of_state(with_dens(Ff), sid, smat, materials, "mixed", theta, device, time),
+            "mixed_density": passes_of_state(with_dens(Fm), sid, smat, materials, "fp64", theta, device, time),
+            "fp64_passes": passes_of_state(with_dens(Ff), sid, smat, materials, "fp64", theta, device, time)}
+    out = {}
+    for name, X in runs.items():
+        q = _quantities(X, Ff)
+        out[name] = {}
+        for k in ("acc_hydro", "eng_dot"):
+            a, b, fl = q[k]
+            e = _each(a, b, fl)
+            out[name][k] = {"p99.9": float(np.quantile(e, 0.999)), "max": float(np.max(e))}
+    return out

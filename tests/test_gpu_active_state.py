@@ -39,3 +39,29 @@ def test_mixed_against_fp64_on_a_shocked_contact_state():
     assert act["frac_compressing"] > 0.01 and act["eng_dot_rms"] > 0.0
     for k, v in errs.items():
         assert v < 1e-5, (k, v)
+
+
+def test_hydro_error_sources_on_a_shocked_contact_state():
+    """the mixed hydro error split between the density (through the pressure) and the pair
+    arithmetic: re-evaluating the derivative and hydro passes on the other path's density.  The
+    FP64 passes on the FP64 density reproduce the FP64 prologue exactly, and each source alone
+    stays within the bar"""
+    F, ids, mats, _ = ic.config_1m_contact(seed=32, n_target=90_000, n_impactor=10_000)
+    materials = [eos.synthetic_table(m) for m in ("iron", "dunite")]
+    ctx = lib.Context(precision="mixed")
+    try:
+        for k, m in enumerate(materials):
+            ctx.set_material(k, m)
+        ctx.upload(F, ids, mats)
+        ctx.prologue()
+        ctx.step(10)
+        t, _, _ = ctx.time()
+        S, sid, smat = ctx.download()
+    finally:
+        ctx.close()
+    src = accuracy.hydro_error_sources(S, sid, smat, materials, time=t)
+    print("hydro error sources:", src)
+    assert src["fp64_passes"]["acc_hydro"]["max"] == 0.0 and src["fp64_passes"]["eng_dot"]["max"] == 0.0
+    for name in ("mixed", "mixed_pairs", "mixed_density"):
+        for k in ("acc_hydro", "eng_dot"):
+            assert src[name][k]["max"] < 1e-5, (name, k)
