@@ -27,7 +27,6 @@ constexpr int ERR_CELL_OVERFLOW = 2;
 constexpr int ERR_GRAV_OVERFLOW = 4;
 constexpr int ERR_NONFINITE = 8;
 constexpr int ERR_SPH_STACK = 32;         // SPH walk stack overflow
-constexpr int ERR_TREE_DEEPER = 64;       // the octree needs more levels than the build launched
 
 // Double-float accumulation in FP32 (Knuth's TwoSum): hi + lo carries a
 // running sum to about 2^-44 relative without touching the FP64 pipe, which
@@ -192,10 +191,7 @@ struct Tree {
     double *rb = nullptr;     // device, per run (stride RB_STRIDE): root_lo[3], root_len, scale, rc2[MAX_LEVELS] at [8..]
     int rb_cap = 0;           // runs rb has room for
     int n_cell_host = 0;
-    // levels split by the next build (the last tree's depth plus two; a deeper tree raises
-    // ERR_TREE_DEEPER and is built again with every level), and the last tree's deepest level
-    int levels = KEY_LEVELS;
-    int depth = KEY_LEVELS;
+    int depth = KEY_LEVELS;   // the last tree's deepest level
 };
 
 struct Sort {

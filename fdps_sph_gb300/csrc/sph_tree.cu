@@ -104,15 +104,6 @@ int sph_scan_exclusive(sph_ctx *ctx, const int *in, int *out, const int *len_dev
     return SPH_OK;
 }
 
-static int scan_exclusive_diff(sph_ctx *ctx, const int *in, int *out, const int *pair_dev, int *total_dev) {
-    LenArg L{pair_dev, 0, 1};
-    k_scan_reduce<<<SCAN_BLOCKS, SCAN_THREADS, 0, ctx->stream>>>(in, L, ctx->scan.part); ++ctx->launches;
-    k_scan_part<<<1, SCAN_BLOCKS, 0, ctx->stream>>>(ctx->scan.part, SCAN_BLOCKS, total_dev); ++ctx->launches;
-    k_scan_down<<<SCAN_BLOCKS, SCAN_THREADS, 0, ctx->stream>>>(in, out, L, ctx->scan.part); ++ctx->launches;
-    SPH_CUDA(ctx, cudaGetLastError());
-    return SPH_OK;
-}
-
 namespace sph {
 
 // ---------------------------------------------------------------------------
@@ -452,223 +443,187 @@ __global__ void k_tree_init(int R, const int4 *info, int *meta, int *start, int 
     }
 }
 
-__device__ __forceinline__ int digit_at(uint64_t key, int level) {
-    return (int)((key >> (3 * (KEY_LEVELS - level))) & 7ULL);
+// ---------------------------------------------------------------------------
+// The octree in one pass over the sorted keys.
+//
+// A cell of level L >= 1 is a maximal run of particles of one run whose keys share their first L
+// octal digits, and it exists exactly when the range of level L - 1 around it (its parent) holds
+// more than n_leaf particles (L <= KEY_LEVELS); level 0 holds one root per run.  Sizes shrink
+// with the level, so for particle i, with l_i the deepest level whose range around i holds more
+// than n_leaf particles, i starts a cell at every level L with d_i < L <= min(l_i + 1, KEY_LEVELS),
+// d_i being the number of leading digits i shares with i - 1 (-1 at a run start, where the root
+// starts too).  l_i is the largest common-digit count over the windows [j, j + n_leaf] of the run
+// that contain i.  Cells are numbered level by level and, inside a level, by start -- the order
+// of a level-by-level split in octant order -- so the tree is the same, cell for cell.
+
+constexpr int OT_B = 256;      // particles per block of the one-pass build
+constexpr int OT_HALO = 16;    // keys staged beyond each side of a block (windows of n_leaf <= 16 stay in it)
+
+// the leading octal digits (levels 1..KEY_LEVELS of a 63-bit key) two keys share
+__device__ __forceinline__ int key_common(uint64_t a, uint64_t b) {
+    const uint64_t x = a ^ b;
+    return x ? min(KEY_LEVELS, (__clzll((long long)x) - 1) / 3) : KEY_LEVELS;
 }
 
-// Children of the cells of level l: the first position of each octant
-// (digit l + 1) in the cell's sorted key range.  Cells of up to SPLIT_SMALL
-// particles are searched by one thread each (binary searches over a range
-// that sits in L1); larger cells, the top of the tree, by a warp each with
-// 32-way searches, so level 0 over all n particles takes a few dependent
-// loads per octant instead of log2 n.
-constexpr int SPLIT_SMALL = 256;
-
-__device__ __forceinline__ void split_store(int *tb, int s, int e, const int *bnd, int *nch) {
-    int prev = s, k = 0;
-    tb[0] = s;
-    for (int oct = 1; oct < 8; ++oct) {
-        tb[oct] = bnd[oct];
-        k += (bnd[oct] > prev);
-        prev = bnd[oct];
+// per particle: the levels at which it starts a cell (lo | hi << 8, empty when hi < lo), and per
+// block and level the number of cells starting in the block (cnt[L * n_blocks + block])
+__global__ void __launch_bounds__(OT_B) k_cell_levels(int n, int n_leaf, const uint64_t *__restrict__ keys,
+                                                      const int *__restrict__ prun, const int4 *__restrict__ info,
+                                                      int *__restrict__ lev, int *__restrict__ cnt) {
+    __shared__ uint64_t sk[OT_B + 2 * OT_HALO];
+    __shared__ int sc[MAX_LEVELS];
+    const int t = threadIdx.x, b0 = blockIdx.x * OT_B, i = b0 + t;
+    for (int k = t; k < OT_B + 2 * OT_HALO; k += OT_B) {
+        const int g = b0 - OT_HALO + k;
+        sk[k] = (g >= 0 && g < n) ? keys[g] : 0ull;
     }
-    tb[8] = e;
-    *nch = k + (e > prev);
-}
-
-// first position in [a, e) whose digit at `lev` is >= oct (keys ascending within the range)
-__device__ __forceinline__ int split_search1(const uint64_t *keys, int lev, int a, int e, int oct) {
-    int len = e - a;
-    while (len > 0) {
-        const int half = len >> 1;
-        if (digit_at(keys[a + half], lev) < oct) {
-            a += half + 1;
-            len -= half + 1;
-        } else {
-            len = half;
-        }
+    if (t < MAX_LEVELS) sc[t] = 0;
+    __syncthreads();
+    auto key_at = [&](int g) { const int k = g - b0 + OT_HALO; return (k >= 0 && k < OT_B + 2 * OT_HALO) ? sk[k] : keys[g]; };
+    int lo = 1, hi = 0;
+    if (i < n) {
+        const int4 ri = info[prun[i]];
+        const int rs = ri.x, re = ri.x + ri.y;
+        const uint64_t ki = key_at(i);
+        const int d = i == rs ? -1 : key_common(key_at(i - 1), ki);
+        int ell = -1;
+        const int j1 = min(i, re - 1 - n_leaf);
+        for (int j = max(rs, i - n_leaf); j <= j1; ++j) ell = max(ell, key_common(key_at(j), key_at(j + n_leaf)));
+        lo = d + 1;
+        hi = min(ell + 1, KEY_LEVELS);
+        if (i == rs) hi = max(hi, 0);
+        lev[i] = lo | (hi << 8);
     }
-    return a;
+    const int lane = t & 31;
+    for (int L = 0; L < MAX_LEVELS; ++L) {
+        const unsigned bal = __ballot_sync(0xffffffffu, L >= lo && L <= hi);
+        if (lane == 0 && bal) atomicAdd(&sc[L], __popc(bal));
+    }
+    __syncthreads();
+    if (t < MAX_LEVELS) cnt[(int64_t)t * gridDim.x + blockIdx.x] = sc[t];
 }
 
-// K independent searches of split_search1 interleaved, so their loads overlap: search q looks
-// in [a[q], e[q]) for digit o[q] and leaves the answer in a[q]
-template <int K>
-__device__ __forceinline__ void split_searchK(const uint64_t *keys, int lev, int (&a)[K], const int (&e)[K],
-                                              const int (&o)[K]) {
-    int len[K];
+// the cells: cell id = the exclusive scan of the block-and-level counts (level-major) plus the
+// rank of the particle among its block's starts at that level; start, count (the end found by
+// a binary search over the run's keys), level.  Also the level offsets in meta; more cells than
+// the capacity sets ERR_CELL_OVERFLOW and leaves no cells.
+__global__ void __launch_bounds__(OT_B) k_cell_emit(int n, int64_t cap, const uint64_t *__restrict__ keys,
+                                                    const int *__restrict__ prun, const int4 *__restrict__ info,
+                                                    const int *__restrict__ lev, const int *__restrict__ cnt,
+                                                    const int *__restrict__ off, int *meta, int *start, int *count,
+                                                    int *level) {
+    __shared__ int sw[MAX_LEVELS][OT_B / 32];
+    const int nb = gridDim.x, t = threadIdx.x, lane = t & 31, warp = t >> 5, i = blockIdx.x * OT_B + t;
+    const int64_t last = (int64_t)(MAX_LEVELS - 1) * nb + nb - 1;
+    const int64_t total = (int64_t)off[last] + cnt[last];
+    const bool overflow = total > cap;
+    if (blockIdx.x == 0 && t <= MAX_LEVELS) {
+        meta[t] = overflow ? 0 : (t < MAX_LEVELS ? off[(int64_t)t * nb] : (int)total);
+        if (t == 0 && overflow) atomicOr(&meta[META_ERR], ERR_CELL_OVERFLOW);
+    }
+    int lo = 1, hi = 0;
+    if (i < n) {
+        const int v = lev[i];
+        lo = v & 255;
+        hi = v >> 8;
+    }
+    unsigned bals[MAX_LEVELS];
 #pragma unroll
-    for (int q = 0; q < K; ++q) len[q] = e[q] - a[q];
-    for (;;) {
-        bool any = false;
-        bool lt[K];
-#pragma unroll
-        for (int q = 0; q < K; ++q) {
-            lt[q] = len[q] > 0 && digit_at(keys[a[q] + (len[q] >> 1)], lev) < o[q];
-            any = any || len[q] > 0;
+    for (int L = 0; L < MAX_LEVELS; ++L) {
+        bals[L] = __ballot_sync(0xffffffffu, L >= lo && L <= hi);
+        if (lane == 0) sw[L][warp] = __popc(bals[L]);
+    }
+    __syncthreads();
+    if (overflow || i >= n || hi < lo) return;
+    const int4 ri = info[prun[i]];
+    const int re = ri.x + ri.y;
+    const uint64_t ki = keys[i];
+    const unsigned below = (1u << lane) - 1u;
+    for (int L = lo; L <= hi; ++L) {
+        int r = __popc(bals[L] & below);
+        for (int w = 0; w < warp; ++w) r += sw[L][w];
+        const int id = off[(int64_t)L * nb + blockIdx.x] + r;
+        // the range's end: the first particle of the run past i whose key differs in the first L digits
+        int a = i + 1, b = re;
+        while (a < b) {
+            const int mid = (a + b) >> 1;
+            if (key_common(keys[mid], ki) >= L) a = mid + 1;
+            else b = mid;
         }
-        if (!any) break;
-#pragma unroll
-        for (int q = 0; q < K; ++q) {
-            if (len[q] <= 0) continue;
-            const int h = len[q] >> 1;
-            if (lt[q]) {
-                a[q] += h + 1;
-                len[q] -= h + 1;
-            } else {
-                len[q] = h;
-            }
-        }
+        start[id] = i;
+        count[id] = a - i;
+        level[id] = L;
     }
 }
 
-
-// the octant boundaries of one big cell [s, e) by a whole warp, 32-way searches
-__device__ __forceinline__ void split_big(const uint64_t *keys, int l, int lane, int c, int L0, int s, int e,
-                                          int *tmp_cnt, int *tmp_b) {
-    int bnd[8];
-    int lo = s;
-    for (int oct = 1; oct < 8; ++oct) {
-        // first position in [lo, e) with digit >= oct; the answer lies in [a, b]
-        int a = lo, b = e;
-        while (b - a > 32) {
-            const int step = (b - a + 31) >> 5;
-            const int p = a + lane * step;
-            const bool below = p < b && digit_at(keys[p], l + 1) < oct;
-            const int kb = __popc(__ballot_sync(0xffffffffu, below));
-            if (kb == 0) {
-                b = a;
-            } else {
-                const int na = a + (kb - 1) * step + 1;
-                b = min(b, a + kb * step);
-                a = na;
+// parent, first child and child count of every cell, by binary searches over the starts of the
+// levels above and below (each level's cells are sorted by start)
+__global__ void k_cell_link(const int *meta, const int *start, const int *count, const int *level, int *parent,
+                            int *first_child, int *n_child) {
+    const int nc = meta[MAX_LEVELS];
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        const int L = level[c], s = start[c], e = s + count[c];
+        int p = -1;
+        if (L > 0) {   // the last cell of level L - 1 starting at or before s
+            int a = meta[L - 1], b = meta[L];
+            while (a < b) {
+                const int mid = (a + b) >> 1;
+                if (start[mid] <= s) a = mid + 1;
+                else b = mid;
             }
+            p = a - 1;
         }
-        if (b > a) {
-            const int p = a + lane;
-            const bool below = p < b && digit_at(keys[p], l + 1) < oct;
-            a += __popc(__ballot_sync(0xffffffffu, below));
-        }
-        bnd[oct] = a;
-        lo = a;
-    }
-    if (lane == 0) {
-        int nch = 0;
-        split_store(tmp_b + (int64_t)(c - L0) * 9, s, e, bnd, &nch);
-        tmp_cnt[c - L0] = nch;
-    }
-}
-
-// Small cells (<= SPLIT_SMALL particles) go to one thread each, big ones to one warp each,
-// spread over all warps of the grid: a level with fewer cells than warps gives every cell its
-// own warp (the top levels hold a few hundred big cells), a larger one is scanned 32 cells at
-// a time per warp.
-__global__ void __launch_bounds__(256) k_split(int l, int n_leaf, const uint64_t *keys, const int *meta,
-                                               const int *start, const int *count, int *tmp_cnt, int *tmp_b) {
-    const int L0 = meta[l], L1 = meta[l + 1], nL = L1 - L0;
-    const int gt = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
-    const int lane = threadIdx.x & 31, gw = gt >> 5, nw = nt >> 5;
-    const bool deep = l < KEY_LEVELS;
-    for (int c = L0 + gt; c < L1; c += nt) {
-        const int s = start[c], cnt = count[c];
-        if (cnt > SPLIT_SMALL && deep) continue;   // a warp's
-        int nch = 0;
-        if (cnt > n_leaf && deep) {
-            // the seven octant boundaries in three rounds of independent searches (octant 4;
-            // then 2 and 6; then 1, 3, 5, 7), each search over the range its neighbours bound
-            int bnd[8];
-            const int e = s + cnt;
-            bnd[4] = split_search1(keys, l + 1, s, e, 4);
-            {
-                int a2[2] = {s, bnd[4]};
-                split_searchK<2>(keys, l + 1, a2, {bnd[4], e}, {2, 6});
-                bnd[2] = a2[0];
-                bnd[6] = a2[1];
+        int f = -1, nch = 0;
+        if (L < KEY_LEVELS) {   // the cells of level L + 1 starting in [s, e)
+            const int a0 = meta[L + 1], b0 = meta[L + 2];
+            int a = a0, b = b0;
+            while (a < b) {
+                const int mid = (a + b) >> 1;
+                if (start[mid] < s) a = mid + 1;
+                else b = mid;
             }
-            {
-                int a4[4] = {s, bnd[2], bnd[4], bnd[6]};
-                split_searchK<4>(keys, l + 1, a4, {bnd[2], bnd[4], bnd[6], e}, {1, 3, 5, 7});
-                bnd[1] = a4[0];
-                bnd[3] = a4[1];
-                bnd[5] = a4[2];
-                bnd[7] = a4[3];
+            const int fl = a;
+            b = b0;
+            while (a < b) {
+                const int mid = (a + b) >> 1;
+                if (start[mid] < e) a = mid + 1;
+                else b = mid;
             }
-            split_store(tmp_b + (int64_t)(c - L0) * 9, s, e, bnd, &nch);
+            nch = a - fl;
+            f = nch ? fl : -1;
         }
-        tmp_cnt[c - L0] = nch;
-    }
-    if (!deep) return;
-    if (nL <= nw) {
-        if (gw < nL) {
-            const int c = L0 + gw;
-            const int s = start[c], cnt = count[c];
-            if (cnt > SPLIT_SMALL) split_big(keys, l, lane, c, L0, s, s + cnt, tmp_cnt, tmp_b);
-        }
-        return;
-    }
-    for (int q0 = gw * 32; q0 < nL; q0 += nw * 32) {
-        const int q = q0 + lane;
-        const int cl = q < nL ? count[L0 + q] : 0;
-        unsigned big = __ballot_sync(0xffffffffu, cl > SPLIT_SMALL);
-        while (big) {
-            const int k = __ffs(big) - 1;
-            big &= big - 1;
-            const int c = L0 + q0 + k;
-            const int s = start[c];
-            split_big(keys, l, lane, c, L0, s, s + __shfl_sync(0xffffffffu, cl, k), tmp_cnt, tmp_b);
-        }
-    }
-}
-
-__global__ void k_emit(int l, int64_t cap, int *meta, const int *tmp_cnt, const int *tmp_off, const int *tmp_b,
-                       const int *total, int *start, int *count, int *level, int *parent, int *first_child,
-                       int *n_child) {
-    const int L0 = meta[l], L1 = meta[l + 1];
-    const int tot = *total;
-    const bool overflow = (int64_t)L1 + tot > cap;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        meta[l + 2] = overflow ? L1 : L1 + tot;
-        if (overflow) atomicOr(&meta[META_ERR], ERR_CELL_OVERFLOW);
-    }
-    for (int c = L0 + blockIdx.x * blockDim.x + threadIdx.x; c < L1; c += gridDim.x * blockDim.x) {
-        const int nch = overflow ? 0 : tmp_cnt[c - L0];
+        parent[c] = p;
+        first_child[c] = f;
         n_child[c] = nch;
-        if (nch == 0) {
-            first_child[c] = -1;
-            continue;
-        }
-        const int first = L1 + tmp_off[c - L0];
-        first_child[c] = first;
-        const int *b = tmp_b + (int64_t)(c - L0) * 9;
-        int k = 0;
-        for (int oct = 0; oct < 8; ++oct) {
-            const int a = b[oct], e = b[oct + 1];
-            if (e <= a) continue;
-            const int ch = first + k++;
-            start[ch] = a;
-            count[ch] = e - a;
-            level[ch] = l + 1;
-            parent[ch] = c;
-            first_child[ch] = -1;
-            n_child[ch] = 0;
-        }
     }
 }
 
-// moments, bounding boxes and hmax of one level (children first)
-__global__ void k_moments(int l, const int *meta, const double *x, const double *y, const double *z, const double *m,
-                          const double *h, const int *start, const int *count, const int *first_child,
-                          const int *n_child, double4 *mom, double4 *com, float4 *blo, float4 *bhi) {
-    const int L0 = meta[l], L1 = meta[l + 1];
-    for (int c = L0 + blockIdx.x * blockDim.x + threadIdx.x; c < L1; c += gridDim.x * blockDim.x) {
-        double ms = 0.0, mx = 0.0, my = 0.0, mz = 0.0;
-        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-        float hm = 0.0f;
-        const int nch = n_child[c];
-        if (nch == 0) {
-            // the box and hmax in FP32: rounding down (up) is monotone, so the min (max) of the
-            // rounded values is the rounded min (max), without FP64 comparisons
-            const int s = start[c], e = s + count[c];
+__device__ __forceinline__ double4 ldcg_d4(const double4 *p) {
+    const double2 *q = reinterpret_cast<const double2 *>(p);
+    const double2 a = __ldcg(q), b = __ldcg(q + 1);
+    return make_double4(a.x, a.y, b.x, b.y);
+}
+
+// Moments, boxes and hmax of every cell in one launch, bottom-up.  A thread takes a leaf, then
+// climbs: after its cell is written it counts itself in at the parent (arrive[], zeroed before the
+// launch), and the child that arrives last sums the parent's children in octant order and climbs
+// on.  The sums and their order are those of a level-by-level pass (leaf particles ascending, then
+// children in octant order, one rounding per operation), independent of which thread arrives last;
+// no thread waits for another (a climb ends at the first parent with children still to come, or
+// at the root, after at most KEY_LEVELS steps).  Children written by other threads are read
+// through L2 after the fence that orders them before their arrival.
+__global__ void k_moments_up(const int *meta, const double *x, const double *y, const double *z, const double *m,
+                             const double *h, const int *start, const int *count, const int *first_child,
+                             const int *n_child, const int *parent, int *arrive, double4 *mom, double4 *com,
+                             float4 *blo, float4 *bhi) {
+    const int nc = meta[MAX_LEVELS];
+    for (int c0 = blockIdx.x * blockDim.x + threadIdx.x; c0 < nc; c0 += gridDim.x * blockDim.x) {
+        if (n_child[c0] != 0) continue;
+        {
+            double ms = 0.0, mx = 0.0, my = 0.0, mz = 0.0;
+            float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+            float hm = 0.0f;
+            const int s = start[c0], e = s + count[c0];
             for (int j = s; j < e; ++j) {
                 const double mj = m[j], xj = x[j], yj = y[j], zj = z[j];
                 ms = __dadd_rn(ms, mj);
@@ -680,24 +635,39 @@ __global__ void k_moments(int l, const int *meta, const double *x, const double 
                 lo[2] = fminf(lo[2], __double2float_rd(zj)); hi[2] = fmaxf(hi[2], __double2float_ru(zj));
                 hm = fmaxf(hm, __double2float_ru(h[j]));
             }
-        } else {
-            const int f = first_child[c];
+            mom[c0] = make_double4(mx, my, mz, ms);
+            com[c0] = make_double4(__ddiv_rn(mx, ms), __ddiv_rn(my, ms), __ddiv_rn(mz, ms), ms);
+            blo[c0] = make_float4(lo[0], lo[1], lo[2], 0.0f);
+            bhi[c0] = make_float4(hi[0], hi[1], hi[2], hm);
+        }
+        int c = c0;
+        for (int up = 0; up < KEY_LEVELS + 1; ++up) {
+            const int p = parent[c];
+            if (p < 0) break;
+            __threadfence();   // this cell's moments before its arrival
+            if (atomicAdd(&arrive[p], 1) != n_child[p] - 1) break;
+            __threadfence();   // every sibling's arrival (and so its moments) before the reads
+            double ms = 0.0, mx = 0.0, my = 0.0, mz = 0.0;
+            float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+            float hm = 0.0f;
+            const int f = first_child[p], nch = n_child[p];
             for (int k = 0; k < nch; ++k) {
-                const double4 q = mom[f + k];
+                const double4 q = ldcg_d4(mom + f + k);
                 ms = __dadd_rn(ms, q.w);
                 mx = __dadd_rn(mx, q.x);
                 my = __dadd_rn(my, q.y);
                 mz = __dadd_rn(mz, q.z);
-                const float4 a = blo[f + k], b = bhi[f + k];
+                const float4 a = __ldcg(blo + f + k), b = __ldcg(bhi + f + k);
                 lo[0] = fminf(lo[0], a.x); lo[1] = fminf(lo[1], a.y); lo[2] = fminf(lo[2], a.z);
                 hi[0] = fmaxf(hi[0], b.x); hi[1] = fmaxf(hi[1], b.y); hi[2] = fmaxf(hi[2], b.z);
                 hm = fmaxf(hm, b.w);
             }
+            mom[p] = make_double4(mx, my, mz, ms);
+            com[p] = make_double4(__ddiv_rn(mx, ms), __ddiv_rn(my, ms), __ddiv_rn(mz, ms), ms);
+            blo[p] = make_float4(lo[0], lo[1], lo[2], 0.0f);
+            bhi[p] = make_float4(hi[0], hi[1], hi[2], hm);
+            c = p;
         }
-        mom[c] = make_double4(mx, my, mz, ms);
-        com[c] = make_double4(__ddiv_rn(mx, ms), __ddiv_rn(my, ms), __ddiv_rn(mz, ms), ms);
-        blo[c] = make_float4(lo[0], lo[1], lo[2], 0.0f);
-        bhi[c] = make_float4(hi[0], hi[1], hi[2], hm);
     }
 }
 
@@ -706,17 +676,6 @@ __global__ void k_pack_cinfo(const int *meta, const int *first_child, const int 
     const int nc = meta[MAX_LEVELS];
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x)
         cinfo[c] = make_int4(first_child[c], n_child[c], start[c], count[c]);
-}
-
-// after the levels [0, Lb) were split: flags a cell of level Lb that would still split (the tree
-// is deeper than this build went) and marks the levels below Lb empty
-__global__ void k_tree_tail(int Lb, int n_leaf, int *meta, const int *count) {
-    const int L0 = meta[Lb], L1 = meta[Lb + 1];
-    if (Lb < KEY_LEVELS)
-        for (int c = L0 + blockIdx.x * blockDim.x + threadIdx.x; c < L1; c += gridDim.x * blockDim.x)
-            if (count[c] > n_leaf) atomicOr(&meta[META_ERR], ERR_TREE_DEEPER);
-    if (blockIdx.x == 0)
-        for (int l = Lb + 2 + threadIdx.x; l <= MAX_LEVELS; l += blockDim.x) meta[l] = L1;
 }
 
 __global__ void k_hmax(int l, const int *meta, const double *h, const int *start, const int *count,
@@ -822,26 +781,31 @@ static int radix_sort(sph_ctx *ctx, int n) {
     return SPH_OK;
 }
 
-// the octree over the sorted particles, level by level (level sizes stay on the device): the
-// levels [0, Lb) are split, then a tail kernel checks that level Lb needs no split (else the
-// host builds again with every level) and marks the deeper levels empty; moments bottom-up
-static int enqueue_tree(sph_ctx *ctx, int Lb) {
+// the octree over the sorted particles in one pass (k_cell_levels, a scan, k_cell_emit,
+// k_cell_link), then the moments bottom-up in one launch and the packed cell records
+static int enqueue_tree(sph_ctx *ctx) {
     const int64_t cap = ctx->cap;
+    const int n = (int)ctx->n;
     Tree &t = ctx->tree;
     cudaStream_t st = ctx->stream;
     const double *x = FLD(ctx->F, SPH_X, cap), *y = FLD(ctx->F, SPH_Y, cap), *z = FLD(ctx->F, SPH_Z, cap);
     const double *m = FLD(ctx->F, SPH_MASS, cap), *h = FLD(ctx->F, SPH_SMTH, cap);
     const int grid = 2 * ctx->num_sms;
-    for (int l = 0; l < Lb; ++l) {
-        k_split<<<grid, 256, 0, st>>>(l, ctx->cfg.n_leaf, ctx->keys, t.meta, t.start, t.count, t.tmp_cnt, t.tmp_b); ++ctx->launches;
-        SPH_TRY(scan_exclusive_diff(ctx, t.tmp_cnt, t.tmp_off, t.meta + l, ctx->scan.total));
-        k_emit<<<grid, 256, 0, st>>>(l, t.cap, t.meta, t.tmp_cnt, t.tmp_off, t.tmp_b, ctx->scan.total, t.start,
-                                     t.count, t.level, t.parent, t.first_child, t.n_child); ++ctx->launches;
-    }
-    k_tree_tail<<<grid, 256, 0, st>>>(Lb, ctx->cfg.n_leaf, t.meta, t.count); ++ctx->launches;
-    for (int l = Lb; l >= 0; --l)
-        k_moments<<<grid, 128, 0, st>>>(l, t.meta, x, y, z, m, h, t.start, t.count, t.first_child, t.n_child,
-                                        t.mom, t.com, t.blo, t.bhi); ++ctx->launches;
+    const int nb = sph_div_up(n, OT_B);
+    // scratch: tmp_off the particles' cell levels, tmp_cnt the block-and-level counts, tmp_b their scan
+    k_cell_levels<<<nb, OT_B, 0, st>>>(n, ctx->cfg.n_leaf, ctx->keys, ctx->runs.prun, ctx->runs.info, t.tmp_off,
+                                       t.tmp_cnt); ++ctx->launches;
+    SPH_TRY(sph_scan_exclusive(ctx, t.tmp_cnt, t.tmp_b, nullptr, MAX_LEVELS * nb, nullptr));
+    k_cell_emit<<<nb, OT_B, 0, st>>>(n, t.cap, ctx->keys, ctx->runs.prun, ctx->runs.info, t.tmp_off, t.tmp_cnt,
+                                     t.tmp_b, t.meta, t.start, t.count, t.level); ++ctx->launches;
+    k_cell_link<<<grid, 256, 0, st>>>(t.meta, t.start, t.count, t.level, t.parent, t.first_child, t.n_child);
+    ++ctx->launches;
+    // moments bottom-up in one launch (tmp_cnt, free again, counts the arrivals)
+    SPH_CUDA(ctx, cudaMemsetAsync(t.tmp_cnt, 0, sizeof(int) * t.cap, st));
+    // one thread per cell: the leaves' fences and arrivals all in flight at once
+    const int grid_up = (int)std::min<int64_t>((t.cap + 127) / 128, 1 << 16);
+    k_moments_up<<<grid_up, 128, 0, st>>>(t.meta, x, y, z, m, h, t.start, t.count, t.first_child, t.n_child,
+                                          t.parent, t.tmp_cnt, t.mom, t.com, t.blo, t.bhi); ++ctx->launches;
     k_pack_cinfo<<<grid, 256, 0, st>>>(t.meta, t.first_child, t.n_child, t.start, t.count, t.cinfo);
     ++ctx->launches;
     SPH_CUDA(ctx, cudaGetLastError());
@@ -877,7 +841,7 @@ static int enqueue_sort_tree(sph_ctx *ctx) {
     std::swap(ctx->mat, ctx->mat2);
     SPH_CUDA(ctx, cudaMemcpyAsync(ctx->keys, ctx->sort.k0, sizeof(uint64_t) * n, cudaMemcpyDeviceToDevice, st));
     SPH_TRY(time_mark(ctx, SEG_SORT));
-    return enqueue_tree(ctx, t.levels);
+    return enqueue_tree(ctx);
 }
 
 // Everything the captured work depends on: sizes and every buffer it touches.  The permutation
@@ -890,7 +854,7 @@ static void graph_key(const sph_ctx *ctx, uintptr_t key[GRAPH_KEY_N]) {
         (uintptr_t)ctx->mat,       (uintptr_t)ctx->runs.prun,  (uintptr_t)ctx->keys,     (uintptr_t)ctx->sort.k0,
         (uintptr_t)ctx->sort.hist, (uintptr_t)t.start,         (uintptr_t)t.rb,          (uintptr_t)t.cap,
         (uintptr_t)ctx->runs.tiles, (uintptr_t)ctx->runs.part, (uintptr_t)ctx->scan.part, (uintptr_t)t.cinfo,
-        (uintptr_t)t.levels};
+        (uintptr_t)ctx->cfg.n_leaf};
     for (int i = 0; i < GRAPH_KEY_N; ++i) key[i] = k[i];
 }
 
@@ -958,20 +922,11 @@ int sph_sort_and_build(sph_ctx *ctx) {
     SPH_CUDA(ctx, cudaStreamSynchronize(st));
     if (hs[META_ERR] & ERR_NONFINITE) return sph_fail(ctx, SPH_ERR_NONFINITE, "non-finite particle position");
     if (hs[META_ERR] & ERR_CELL_OVERFLOW) return sph_fail(ctx, SPH_ERR_CAPACITY, "octree cell capacity exceeded");
-    if (hs[META_ERR] & ERR_TREE_DEEPER) {   // deeper than the last tree plus two levels: every level
-        SPH_CUDA(ctx, cudaMemsetAsync(t.meta + META_ERR, 0, sizeof(int), st));
-        t.levels = KEY_LEVELS;
-        SPH_TRY(enqueue_tree(ctx, KEY_LEVELS));
-        SPH_CUDA(ctx, cudaMemcpyAsync(hs, t.meta, sizeof(int) * META_N, cudaMemcpyDeviceToHost, st));
-        SPH_CUDA(ctx, cudaStreamSynchronize(st));
-        if (hs[META_ERR] & ERR_CELL_OVERFLOW) return sph_fail(ctx, SPH_ERR_CAPACITY, "octree cell capacity exceeded");
-    }
     t.n_cell_host = hs[MAX_LEVELS];
     int depth = 0;
     for (int l = 0; l < MAX_LEVELS; ++l)
         if (hs[l + 1] > hs[l]) depth = l;
     t.depth = depth;
-    t.levels = std::min(KEY_LEVELS, depth + 2);
     ctx->grav.valid = false;
     ctx->grav.counts_valid = false;
     SPH_TRY(time_mark(ctx, SEG_TREE));
