@@ -103,6 +103,28 @@ int tag_state(int tag, TagState **out) {
     int dev = 0;
     cudaGetDevice(&dev);
     if (!t.stream || t.device != dev) {
+        if (t.stream) {   // the tag moves to another device: its buffers and stream stay with the old one
+            cudaSetDevice(t.device);
+            cudaStreamSynchronize(t.stream);
+            for (char **h : {&t.h_in, &t.h_out, (char **)&t.h_meta, (char **)&t.h_src, (char **)&t.h_dst,
+                             (char **)&t.h_err})
+                if (*h) cudaFreeHost(*h);
+            for (char **d : {&t.d_in, &t.d_out, (char **)&t.d_meta, (char **)&t.d_src, (char **)&t.d_dst,
+                             (char **)&t.d_err})
+                if (*d) cudaFree(*d);
+            cudaStreamDestroy(t.stream);
+            if (t.gathered) cudaEventDestroy(t.gathered);
+            cudaSetDevice(dev);
+            t.h_in = t.h_out = t.d_in = t.d_out = nullptr;
+            t.h_meta = t.d_meta = nullptr;
+            t.h_src = t.d_src = t.h_dst = t.d_dst = nullptr;
+            t.h_err = t.d_err = nullptr;
+            t.cap_in = t.cap_out = t.cap_meta = t.cap_src = t.cap_dst = 0;
+            t.stream = nullptr;
+            t.gathered = nullptr;
+            t.pending_kind = -1;
+            t.gather_pending = false;
+        }
         if (cudaStreamCreateWithFlags(&t.stream, cudaStreamNonBlocking) != cudaSuccess ||
             cudaEventCreateWithFlags(&t.gathered, cudaEventDisableTiming) != cudaSuccess) {
             cudaGetLastError();

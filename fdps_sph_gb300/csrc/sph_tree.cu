@@ -644,9 +644,11 @@ __global__ void k_moments_up(const int *meta, const double *x, const double *y, 
         for (int up = 0; up < KEY_LEVELS + 1; ++up) {
             const int p = parent[c];
             if (p < 0) break;
-            __threadfence();   // this cell's moments before its arrival
+            // release: this cell's moments before its arrival; acquire: every sibling's arrival (and
+            // so its moments) before the reads
+            asm volatile("fence.acq_rel.gpu;" ::: "memory");
             if (atomicAdd(&arrive[p], 1) != n_child[p] - 1) break;
-            __threadfence();   // every sibling's arrival (and so its moments) before the reads
+            asm volatile("fence.acq_rel.gpu;" ::: "memory");
             double ms = 0.0, mx = 0.0, my = 0.0, mz = 0.0;
             float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
             float hm = 0.0f;
