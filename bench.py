@@ -693,6 +693,7 @@ def batch_and_serving(a, device):
     res["batch"] = {"metric": "aggregate particle-steps/s, batched sweep", "value": bt["particle_steps_per_s"],
                     "unit": "particle-steps/s", "runs": bt["runs"], "steps_per_run": bt["steps_per_run"],
                     "particles": bt["particles"], "batched_steps": bt["batched_steps"], "wall_s": bt["wall_s"],
+                    "stepping_s": bt["stepping_s"], "value_stepping_only": bt["particle_steps_per_stepping_s"],
                     "step_latency_s": bt["step_latency_s"], "time_to_completion_s": bt["time_to_completion_s"],
                     "config": "impacts with N log-uniform 5e3-2e5, mass ratio U[0.05, 0.5], angle U[0, 75] deg, "
                               "speed U[1, 2] v_esc, iron/dunite tables; wall time includes the host IC generation"}
@@ -722,6 +723,7 @@ def batch_and_serving(a, device):
                       "window_s": a.serve_s, "steps_per_request": [lo, hi], "batched_steps": rep["batched_steps"],
                       "step_latency_s": rep["step_latency_s"], "time_to_completion_s": rep["time_to_completion_s"],
                       "max_resident_particles": rep["max_resident_particles"],
+                      "stepping_s": rep["stepping_s"], "value_stepping_only": rep["particle_steps_per_stepping_s"],
                       "offered_particle_steps": int(offered),
                       "offered_particle_steps_per_s": offered / a.serve_s,
                       "fp64_per_run_value": v64, "vs_fp64_per_run": rep["particle_steps_per_s"] / v64,

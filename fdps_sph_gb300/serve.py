@@ -112,6 +112,7 @@ class Server:
         self.step_lat, self.ttc, self.completed = [], [], []
         self.particle_steps = 0
         self.steps_taken = 0
+        self.stepping_s = 0.0   # wall time inside the batched steps (no admission, IC building or idling)
         self.admitted = 0
         self.built = threading.BoundedSemaphore(built_ahead or self.BUILT_AHEAD)
 
@@ -140,6 +141,7 @@ class Server:
         self.ctx.step(1)
         lat = time.perf_counter() - t0
         self.steps_taken += 1
+        self.stepping_s += lat
         finished = []
         for h, r in self.active.items():
             if r.fresh:           # the run's prologue
@@ -233,6 +235,8 @@ class Server:
             "batched_steps": self.steps_taken,
             "particle_steps": int(self.particle_steps),
             "particle_steps_per_s": self.particle_steps / wall if wall > 0 else 0.0,
+            "stepping_s": self.stepping_s,
+            "particle_steps_per_stepping_s": self.particle_steps / self.stepping_s if self.stepping_s > 0 else 0.0,
             "step_latency_s": percentiles(self.step_lat),
             "time_to_completion_s": percentiles(self.ttc),
             "max_resident_particles": int(self.max_particles),

@@ -61,6 +61,9 @@ def test_admission_budget_prologue_and_backfill():
     assert rep["particle_steps"] == sum(r.n * r.steps for r in reqs)
     assert rep["batched_steps"] == ctx.steps
     assert rep["time_to_completion_s"]["p50"] > 0 and rep["step_latency_s"]["p99"] is not None
+    # the time inside the batched steps is part of the wall time; its throughput excludes admission
+    assert 0.0 < rep["stepping_s"] <= rep["wall_s"]
+    assert rep["particle_steps_per_stepping_s"] >= rep["particle_steps_per_s"]
 
 
 def test_run_slots_limit_and_oversized_first_run():
