@@ -109,6 +109,28 @@ int main(int argc, char **argv) {
     int n_bad = 0;
     for (int t = 0; t < n_thr; ++t) n_bad += bad[t];
     std::fwrite(&n_bad, sizeof(n_bad), 1, out);
+    // the same hydro walk through the MultiWalk callbacks, payload form and index form (the EPJ
+    // array sent first, the walk as indices into it): both bit-identical to the functor's results
+    int mw_bad = 0;
+    {
+        const STD::EPI::Hydro *ep[1] = {hi.data()};
+        const STD::EPJ::Hydro *jp[1] = {hj.data()};
+        int ni[1] = {(int)hi.size()}, nj[1] = {(int)hj.size()};
+        std::vector<STD::RESULT::Hydro> r1(hi.size()), r2(hi.size());
+        STD::RESULT::Hydro *rp1[1] = {r1.data()}, *rp2[1] = {r2.data()};
+        if (sph_gb300::DispatchHydro(6, 1, ep, ni, jp, nj) != 0 || sph_gb300::RetrieveHydro(6, 1, ni, rp1) != 0)
+            mw_bad |= 1;
+        std::vector<int> idx(hj.size());
+        for (size_t k = 0; k < idx.size(); ++k) idx[k] = (int)k;
+        const int *ip[1] = {idx.data()};
+        if (sph_gb300::DispatchIndexHydro(6, 0, ep, ni, ip, nj, hj.data(), (int)hj.size(), true) != 0 ||
+            sph_gb300::DispatchIndexHydro(6, 1, ep, ni, ip, nj, hj.data(), (int)hj.size(), false) != 0 ||
+            sph_gb300::RetrieveHydro(6, 1, ni, rp2) != 0)
+            mw_bad |= 2;
+        if (std::memcmp(r1.data(), hr.data(), sizeof(hr[0]) * hr.size()) != 0) mw_bad |= 4;
+        if (std::memcmp(r2.data(), hr.data(), sizeof(hr[0]) * hr.size()) != 0) mw_bad |= 8;
+    }
+    std::fwrite(&mw_bad, sizeof(mw_bad), 1, out);
     std::fclose(in);
     std::fclose(out);
     return 0;

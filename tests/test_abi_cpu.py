@@ -79,3 +79,17 @@ def test_header_constants_match_binding():
     assert int(defs["SPH_ENTROPY_ABS_REAL"]) == lib.ENTROPY_ABS_REAL
     for code, name in lib.ERRORS.items():
         assert int(defs[name]) == code, name
+
+
+def test_cpp_host_surface_compiles():
+    # the C++ surface (include/fdps_sph_gb300.hpp: functors, MultiWalk payload and index callbacks)
+    # instantiated with class.h-shaped payload types, as the GPU test's host program uses it
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        import pytest
+        pytest.skip("no g++")
+    subprocess.run([gxx, "-std=c++14", "-fsyntax-only", "-Wall", "-Werror=return-type", "-I",
+                    os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "cpp", "functor_host.cpp")],
+                   check=True)

@@ -2,7 +2,8 @@
 reference's host code calls its functors: a program with class.h-shaped
 payload types calls CalcDensity / CalcHydroForce / CalcGravityForce on golden
 walks; results must match the reference functors' (tests/golden), also when
-eight threads call the functors at once."""
+eight threads call the functors at once, and through the MultiWalk dispatch /
+retrieve callbacks in payload and index form."""
 import os
 import struct
 import subprocess
@@ -90,6 +91,10 @@ def test_cpp_functors_match_reference(tmp_path):
     o += n3 * 40
     # eight threads calling the density and hydro functors concurrently (each on a tag of its own)
     # got the single-threaded results bit for bit
+    assert np.frombuffer(raw[o:o + 4], np.int32)[0] == 0
+    o += 4
+    # the hydro walk through DispatchHydro / RetrieveHydro and through DispatchIndexHydro (send, then
+    # the walk as indices): both bit-identical to the functor call (0: no flag raised)
     assert np.frombuffer(raw[o:o + 4], np.int32)[0] == 0
     assert rel_err(d["dens"], dens_ref["dens"], 1e-300) < 1e-12
     assert rel_err(d["smth"], dens_ref["smth"], 1e-300) < 1e-12
