@@ -35,7 +35,8 @@ constexpr int NB_WARPS = 4;
 constexpr int ROW_K_MAX = 512;   // widest row block; longer rows continue in spill ranges (RowMap)
 constexpr int NB_CAND = 128;   // raw candidate indices per warp
 constexpr int NB_SURV = 64;    // culled candidates staged for the pair test
-constexpr int NB_STACK = 176;   // depth-first: at most 21 levels x 7 pending siblings + 8
+constexpr int NB_STACK = 264;   // depth-first from any stack of <= NB_MULTI entries: + 21 levels x 7 pending siblings + 1
+constexpr int NB_MULTI = 116;   // the stack may reach this with several cells expanded at once
 constexpr unsigned FULLM = 0xffffffffu;
 
 __device__ __forceinline__ float df_sub(float ah, float al, float bh, float bl) { return (ah - bh) + (al - bl); }
@@ -316,9 +317,10 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
         __syncwarp();
     }
     while (sp > 0) {
-        const int2 ci = stack[--sp];
-        __syncwarp();
+        const int2 ci = stack[sp - 1];
         if (ci.y > 0) {   // a leaf
+            --sp;
+            __syncwarp();
             const int s = ci.x, ct = ci.y;
             for (int b0 = 0; b0 < ct; b0 += 32) {
                 if (nc + 32 > NB_CAND) flush();
@@ -327,16 +329,29 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
                 __syncwarp();
             }
         } else {
-            const int f = ci.x, nch = -ci.y;
+            // up to four internal cells from the top of the stack expanded at once, eight lanes per
+            // cell: their children are pushed so that the top cell's come first, as the one-cell
+            // expansion would visit them (the leaves, and so the rows, keep their order).  More
+            // than one only while the stack stays below NB_MULTI, so a depth-first continuation
+            // (at most 7 pending siblings per level below) still fits NB_STACK.
+            int k = 1;
+            while (k < 4 && sp - 1 - k >= 0 && stack[sp - 1 - k].y <= 0 && sp - (k + 1) + 8 * (k + 1) <= NB_MULTI) ++k;
+            const int g = lane >> 3, q = lane & 7;
             bool ok = false;
             int2 chi = make_int2(0, 0);
-            if (lane < nch) {
-                const float4 a = T.blo[f + lane], b = T.bhi[f + lane];
-                const int4 r = T.cinfo[f + lane];   // independent of the box loads: one round trip
-                chi = r.y == 0 ? make_int2(r.z, r.w) : make_int2(r.x, -r.y);
-                const float R = fmaxf(Rg, __fmul_ru(2.5f * KAPPA * 1.00390625f, b.w));
-                ok = gap2_rd(a, b, glo, ghi) < __fmul_ru(R, R);
+            if (g < k) {
+                const int2 cg = stack[sp - 1 - g];
+                const int f = cg.x, nch = -cg.y;
+                if (q < nch) {
+                    const float4 a = T.blo[f + q], b = T.bhi[f + q];
+                    const int4 r = T.cinfo[f + q];   // independent of the box loads: one round trip
+                    chi = r.y == 0 ? make_int2(r.z, r.w) : make_int2(r.x, -r.y);
+                    const float R = fmaxf(Rg, __fmul_ru(2.5f * KAPPA * 1.00390625f, b.w));
+                    ok = gap2_rd(a, b, glo, ghi) < __fmul_ru(R, R);
+                }
             }
+            sp -= k;
+            __syncwarp();
             const unsigned mask = __ballot_sync(FULLM, ok);
             const int np = __popc(mask);
             if (sp + np > NB_STACK) {
