@@ -318,15 +318,38 @@ k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ 
     }
     while (sp > 0) {
         const int2 ci = stack[sp - 1];
-        if (ci.y > 0) {   // a leaf
-            --sp;
-            __syncwarp();
-            const int s = ci.x, ct = ci.y;
-            for (int b0 = 0; b0 < ct; b0 += 32) {
-                if (nc + 32 > NB_CAND) flush();
-                if (b0 + lane < ct) cand[nc + lane] = s + b0 + lane;
-                nc += min(32, ct - b0);
+        if (ci.y > 0) {   // a leaf: with the leaves right below it, while their particles fit 32 lanes
+            if (nc + 32 > NB_CAND) flush();
+            int k = 1, tot = ci.y;
+            while (k < 8 && sp - 1 - k >= 0) {
+                const int2 nx = stack[sp - 1 - k];
+                if (nx.y <= 0 || tot + nx.y > 32) break;
+                tot += nx.y;
+                ++k;
+            }
+            if (tot <= 32) {
+                // lane -> (leaf, offset): leaves in stack order from the top, particles in order
+                int acc = 0, src = -1;
+                for (int g = 0; g < k; ++g) {
+                    const int2 lf = stack[sp - 1 - g];
+                    if (src < 0 && lane < acc + lf.y) src = lf.x + (lane - acc);
+                    acc += lf.y;
+                }
                 __syncwarp();
+                if (lane < tot) cand[nc + lane] = src;
+                nc += tot;
+                sp -= k;
+                __syncwarp();
+            } else {   // a leaf above 32 particles (only at the deepest level)
+                --sp;
+                __syncwarp();
+                const int s = ci.x, ct = ci.y;
+                for (int b0 = 0; b0 < ct; b0 += 32) {
+                    if (nc + 32 > NB_CAND) flush();
+                    if (b0 + lane < ct) cand[nc + lane] = s + b0 + lane;
+                    nc += min(32, ct - b0);
+                    __syncwarp();
+                }
             }
         } else {
             // up to four internal cells from the top of the stack expanded at once, eight lanes per
