@@ -3,7 +3,7 @@ the same seeded inputs.
 
 Bit-exact: Morton keys, sorted order, octree cells and monopole moments,
 SPH neighbour lists (gather and symmetric) and gravity interaction lists.
-FP64 values (spec tolerance 1e-10, summation order and FMA only):
+FP64 values (tolerance 1e-10: summation order and FMA only):
 density, h, pressure, sound speed, grad-h, div v, curl v, Balsara,
 acceleration, du/dt, dt, gravity and potential."""
 import numpy as np
@@ -189,7 +189,7 @@ def test_steps_match_oracle(eos_kind):
 @pytest.mark.parametrize("tpi", [1, 4])
 def test_mixed_precision_against_fp64_oracle(impact, tpi):
     """FP32 pair sums on double-float coordinates: rho, acc, du/dt and
-    gravity within 1e-5 relative of the FP64 oracle (spec bar), with
+    gravity within 1e-5 relative of the FP64 oracle (the mixed path's bar), with
     one and with four threads per particle in the derivative and hydro
     kernels.  Density: relative per particle.  Vectors and du/dt: relative
     per particle, floored at the RMS over particles (vec_err_rms)."""
