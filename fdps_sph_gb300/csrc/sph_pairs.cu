@@ -7,10 +7,10 @@
 // Mixed path (SPH_PREC_MIXED): the same lists and epilogues, with the pair
 // arithmetic in FP32 on double-float positions / velocities (hi + lo floats,
 // so x_i - x_j is formed without FP64 arithmetic), partial sums of at most
-// 32 neighbours (SPH) or one 128-entry tile (gravity) accumulated in FP32 and
-// flushed into FP64 accumulators.  Epilogues (density floor, h update,
-// grad-h normalisation, Balsara, dt), the EoS, the integrator and every
-// reduction stay in FP64.
+// 32 neighbours (SPH) or one shared-memory tile of j (gravity) accumulated in
+// FP32 and flushed into double-float or FP64 accumulators.  Epilogues
+// (density floor, h update, grad-h normalisation, Balsara, dt), the EoS, the
+// integrator and every reduction stay in FP64.
 #include "sph_physics.cuh"
 
 namespace sph {
@@ -628,33 +628,50 @@ __global__ void __launch_bounds__(GT) k_grav32(const int *__restrict__ group_cel
 
 // ---------------------------------------------------------------------------
 // Mixed-precision tree gravity with the walk fused in: one CTA per i-group.
-// All warps walk the octree breadth-first together, 32 opened cells per
-// iteration (eight lanes per cell, one child per lane), with the opening rule
-// and append order of k_grav_lists / or_grav_walk, into shared-memory EPJ and
-// SPJ buffers; when the buffers are full, or the walk has ended, every thread
-// accumulates the buffered interactions.  No interaction list reaches global
-// memory.  The queue holds whole cell records (first child, children | level
-// << 8, start, count), loaded together with the child's centre of mass when
-// the child is tested, so an iteration waits on one global load.
+// All warps walk the octree breadth-first together, T / 4 opened cells per
+// iteration (four lanes per cell, two children per lane), with the opening
+// rule and append order of k_grav_lists / or_grav_walk, into shared-memory EPJ
+// and SPJ buffers; when the buffers are full, or the walk has ended, every
+// thread accumulates the buffered interactions.  No interaction list reaches
+// global memory.  The queue holds whole cell records (first child, children |
+// level << 8, start, count), loaded together with the child's centre of mass
+// when the child is tested, so an iteration waits on one global load.
 //
 // Accumulation: each thread carries two i-particles (ii and ii + Wt, Wt =
-// roundup(count / 2, 8)), and the block's P = 256 / Wt copies of the group
+// roundup(count / 2, 8)), and the block's P = T / Wt copies of the group
 // split each tile of j between them, four consecutive j per round in paired
 // FP32 arithmetic; small groups keep the FP32 lanes busy and every
 // shared-memory read feeds two interactions.
-
-constexpr int GF_T = 256;
-constexpr int GF_Q = 2048;   // BFS ring of opened cell records (power of two)
-// buffered EPJ particle indices and SPJ cell indices, and the j entries per shared-memory tile (each
-// thread stages GF_TILE / GF_T of them per tile).  Measured at 1M (kernel time): buffers of 2048 and
-// tiles of 256 1.96 ms, 1536 and 512 1.94 ms, 1024 and 1024 2.09 ms, 2048 and 1024 (three blocks
-// per SM) 2.00 ms.
-constexpr int GF_E = 1536;
-constexpr int GF_S = 1536;
-constexpr int GF_TILE = 512;
-constexpr int GF_W = GF_T / 32;
-static_assert(GF_TILE % GF_T == 0, "tile: whole loads per thread");
-static_assert(4 * GF_TILE * 4 >= GF_T * 4 * 8 || GF_E * 4 >= GF_T * 4 * 8, "room for the partition reduction");
+//
+// Two block shapes (T threads): 128 threads with a ring of 1,024 cell records,
+// eight blocks per SM, the one launched; 256 threads with 2,048 records, four
+// blocks per SM, relaunched for the whole pass when a walk's breadth-first
+// front outgrows the smaller ring (opening angles near 0 on large bodies).  The
+// widest front of the 1M and 4M impacts at theta 0.5 is 456 records.  Measured
+// at 1M (kernel time): 128 threads, eight blocks per SM 1.75 ms; seven (no
+// spills) 1.82 ms; 128 threads, 1,024-entry buffers, six blocks 1.83 ms; 128
+// threads with the 2,048 ring (five blocks) 1.94 ms; 256 threads 1.94 ms
+// (buffers of 2,048 and tiles of 256 1.96 ms, 1,024 and 1,024 2.09 ms, 2,048
+// and 1,024 at three blocks per SM 2.00 ms).  More independent blocks let one
+// block's walk overlap another's sums.
+template <int T>
+struct GravShape;
+template <>
+struct GravShape<128> {
+    static constexpr int Q = 1024;     // BFS ring of opened cell records (power of two)
+    static constexpr int E = 768;      // buffered EPJ particle indices
+    static constexpr int S = 768;      // buffered SPJ cell indices
+    static constexpr int TILE = 256;   // j entries per shared-memory tile (TILE / T staged per thread)
+    static constexpr int MIN_BLOCKS = 8;
+};
+template <>
+struct GravShape<256> {
+    static constexpr int Q = 2048;
+    static constexpr int E = 1536;
+    static constexpr int S = 1536;
+    static constexpr int TILE = 512;
+    static constexpr int MIN_BLOCKS = 4;
+};
 
 __device__ __forceinline__ void grav_acc(float px, float py, float pz, float e2, float4 q, float &a0, float &a1,
                                          float &a2, float &a3) {
@@ -688,13 +705,18 @@ __device__ __forceinline__ void grav_acc2(f32x2 nx, f32x2 ny, f32x2 nz, f32x2 e2
     a3 = f2_add(a3, mri);
 }
 
-__global__ void __launch_bounds__(GF_T, 4)
+template <int GF_T>
+__global__ void __launch_bounds__(GF_T, GravShape<GF_T>::MIN_BLOCKS)
 k_grav_fused32(const int *__restrict__ group_cell, const int4 *__restrict__ cinfo, const double4 *__restrict__ com,
                const double *__restrict__ rb_all, const int *__restrict__ prun, const double *__restrict__ x,
                const double *__restrict__ y,
                const double *__restrict__ z, const float4 *__restrict__ xh, const float4 *__restrict__ xl,
                const double *__restrict__ h, const float4 *__restrict__ ch, const float4 *__restrict__ cl, float gms,
                double *gx, double *gy, double *gz, double *pot, int *n_epj, int *n_spj, int *err) {
+    constexpr int GF_Q = GravShape<GF_T>::Q, GF_E = GravShape<GF_T>::E, GF_S = GravShape<GF_T>::S;
+    constexpr int GF_TILE = GravShape<GF_T>::TILE, GF_W = GF_T / 32;
+    static_assert(GF_TILE % GF_T == 0, "tile: whole loads per thread");
+    static_assert(4 * GF_TILE * 4 >= GF_T * 4 * 8 || GF_E * 4 >= GF_T * 4 * 8, "room for the partition reduction");
     __shared__ int4 s_q[GF_Q];
     __shared__ __align__(16) int s_e[GF_E];
     __shared__ int s_s[GF_S];
@@ -1487,20 +1509,26 @@ int sph_gravity_fused(sph_ctx *ctx) {
     float4 *chp = (float4 *)ctx->F2, *clp = chp + t.n_cell_host;
     k_pack_cells32<<<2 * ctx->num_sms, 256, 0, ctx->stream>>>(t.meta, t.com, ctx->cfg.G, 1.0, chp, clp);
     ++ctx->launches;
-    SPH_CUDA(ctx, cudaMemsetAsync(t.meta + META_ERR, 0, sizeof(int), ctx->stream));
     // xh.w holds m * mscale: G m = xh.w * (G / mscale)
     const float gms = (float)(ctx->cfg.G / ctx->mscale);
-    k_grav_fused32<<<G.ng, GF_T, 0, ctx->stream>>>(G.group_cell, t.cinfo, t.com, t.rb, ctx->runs.prun, CF(SPH_X),
-                                                   CF(SPH_Y), CF(SPH_Z),
-                                                   ctx->xh, ctx->xl, CF(SPH_SMTH), chp, clp, gms, CF(SPH_GX),
-                                                   CF(SPH_GY), CF(SPH_GZ), CF(SPH_POT), G.n_epj, G.n_spj,
-                                                   t.meta + META_ERR);
-    ++ctx->launches;
-    SPH_CUDA(ctx, cudaGetLastError());
     int *hs = (int *)ctx->host_scalars;
-    SPH_CUDA(ctx, cudaMemcpyAsync(hs, t.meta + META_ERR, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    if (hs[0] & ERR_GRAV_OVERFLOW) return sph_fail(ctx, SPH_ERR_CAPACITY, "gravity walk buffers overflowed");
+    // the 128-thread shape first; a walk whose front outgrew its ring (or a batch its buffers) flags
+    // the error word, and the whole pass runs again with the 256-thread shape, which rewrites every
+    // group's forces and counts
+    for (int wide = 0; wide < 2; ++wide) {
+        SPH_CUDA(ctx, cudaMemsetAsync(t.meta + META_ERR, 0, sizeof(int), ctx->stream));
+        auto kern = wide ? k_grav_fused32<256> : k_grav_fused32<128>;
+        kern<<<G.ng, wide ? 256 : 128, 0, ctx->stream>>>(G.group_cell, t.cinfo, t.com, t.rb, ctx->runs.prun, CF(SPH_X),
+                                                         CF(SPH_Y), CF(SPH_Z), ctx->xh, ctx->xl, CF(SPH_SMTH), chp, clp,
+                                                         gms, CF(SPH_GX), CF(SPH_GY), CF(SPH_GZ), CF(SPH_POT), G.n_epj,
+                                                         G.n_spj, t.meta + META_ERR);
+        ++ctx->launches;
+        SPH_CUDA(ctx, cudaGetLastError());
+        SPH_CUDA(ctx, cudaMemcpyAsync(hs, t.meta + META_ERR, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        SPH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (!(hs[0] & ERR_GRAV_OVERFLOW)) break;
+        if (wide) return sph_fail(ctx, SPH_ERR_CAPACITY, "gravity walk buffers overflowed");
+    }
     G.counts_valid = true;
     return SPH_OK;
 }

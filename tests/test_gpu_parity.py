@@ -319,6 +319,63 @@ def test_fused_gravity_walk_matches_lists(impact):
     assert rel_err(Fa[f["pot"]], Fb[f["pot"]], 1e-300) < 1e-6
 
 
+def _bfs_front(tree, cells_per_iteration):
+    """the widest queue of the fused gravity walk at theta = 0 (every cell opened): the walk takes
+    ``cells_per_iteration`` queued cells per iteration and appends their children; the queue's
+    length after each iteration, at most"""
+    c = tree.cells()
+    fc, nch = c["first_child"], c["n_child"]
+    q, head, widest = [0], 0, 1
+    while head < len(q):
+        take = q[head:head + cells_per_iteration]
+        head += len(take)
+        for k in take:
+            q.extend(range(fc[k], fc[k] + nch[k]))
+        widest = max(widest, len(q) - head)
+    return widest
+
+
+def test_fused_gravity_relaunches_wide_blocks():
+    """The fused gravity walk runs in 128-thread blocks whose breadth-first ring holds 1,024 cell
+    records (32 cells per iteration); a pass in which a walk outgrows it runs again in 256-thread
+    blocks with 2,048.  At theta = 0 every cell is opened, and for this 8,000-particle impact the
+    front (walked here on the oracle's octree, which the device's equals cell for cell) lies
+    between the two.  The mixed prologue then takes exactly one launch more than at theta = 0.5,
+    and its gravity equals the FP64 direct sum within 1e-5 (acceleration relative per particle,
+    floored at the RMS; potential relative per particle)."""
+    from oracle import pyoracle as po
+    F, ids, mats, _ = small_impact(n_target=7200, n_impactor=800)
+    front = _bfs_front(po.OracleTree(po.OracleSystem(F, ids, mats), n_leaf=8), 32)
+    assert 1024 < front <= 2048, front
+    mats_l = tillotson_materials()
+    launches, out = {}, {}
+    for theta in (0.5, 0.0):
+        ctx = device_context(mats_l, precision=1, theta=theta)
+        ctx.upload(F, ids, mats)
+        l0 = ctx.counters()["launches"]
+        ctx.prologue()
+        launches[theta] = ctx.counters()["launches"] - l0
+        Fd, idd, _ = ctx.download()
+        ctx.close()
+        out[theta] = by_id(Fd, idd)
+    assert launches[0.0] == launches[0.5] + 1, launches
+    # direct sum in FP64 on the host, every pair (the particle itself adds -G m / h to the potential)
+    Fs = by_id(F, ids)
+    f = po.FIELD
+    x = Fs[[f["x"], f["y"], f["z"]]].T
+    m, h = Fs[f["mass"]], out[0.0][f["smth"]]
+    acc = np.zeros_like(x)
+    pot = np.zeros(len(m))
+    for a in range(0, len(m), 500):
+        d = x[a:a + 500, None, :] - x[None, :, :]
+        ri = 1.0 / np.sqrt((d * d).sum(-1) + (h[a:a + 500] ** 2)[:, None])
+        acc[a:a + 500] = -6.67e-11 * (m[None, :, None] * d * (ri ** 3)[:, :, None]).sum(1)
+        pot[a:a + 500] = -6.67e-11 * (m[None, :] * ri).sum(1)
+    g = np.stack([out[0.0][f[c]] for c in ("gx", "gy", "gz")], 1)
+    assert vec_err_rms(g, acc) < 1e-5
+    assert rel_err(out[0.0][f["pot"]], pot, 1e-300) < 1e-5
+
+
 def test_mixed_energy_and_angular_momentum_drift(impact):
     """Over 20 steps the mixed path's energy and angular-momentum drift stay
     at the level of the FP64 path's (which is set by the time integration)."""
