@@ -648,12 +648,13 @@ __global__ void __launch_bounds__(GT) k_grav32(const int *__restrict__ group_cel
 // blocks per SM, relaunched for the whole pass when a walk's breadth-first
 // front outgrows the smaller ring (opening angles near 0 on large bodies).  The
 // widest front of the 1M and 4M impacts at theta 0.5 is 456 records.  Measured
-// at 1M (kernel time): 128 threads, eight blocks per SM 1.75 ms; seven (no
-// spills) 1.82 ms; 128 threads, 1,024-entry buffers, six blocks 1.83 ms; 128
-// threads with the 2,048 ring (five blocks) 1.94 ms; 256 threads 1.94 ms
-// (buffers of 2,048 and tiles of 256 1.96 ms, 1,024 and 1,024 2.09 ms, 2,048
-// and 1,024 at three blocks per SM 2.00 ms).  More independent blocks let one
-// block's walk overlap another's sums.
+// at 1M (kernel time), 128 threads: eight blocks per SM 1.75 ms; seven (no
+// spills) 1.82 ms; nine or ten (56 / 48 registers, smaller buffers and tiles,
+// more spills) 1.80 / 2.65 ms; six with 1,024-entry buffers 1.83 ms; five with
+// the 2,048 ring 1.94 ms.  256 threads, four per SM: 1.94 ms (buffers of 2,048
+// and tiles of 256 1.96 ms, 1,024 and 1,024 2.09 ms, 2,048 and 1,024 at three
+// blocks per SM 2.00 ms).  More independent blocks let one block's walk
+// overlap another's sums.
 template <int T>
 struct GravShape;
 template <>
