@@ -490,8 +490,12 @@ __global__ void __launch_bounds__(PT, 6) k_hydro32(int n, HydroArgs32 a) {
     const RowView row = row_view(a.nbr, a.rm, i, a.cnt[i]);
     const int c = row.c;
     int k = 2 * sub, it = 0;
+    // the next pair's indices load while this pair is gathered and summed (1M: 0.79 -> 0.74 ms; the
+    // derivative kernel, which gathers 64 B per neighbour instead of 80, gained nothing from it)
+    int2 jn = k + 2 <= c ? *reinterpret_cast<const int2 *>(row.at(k)) : make_int2(0, 0);
     for (; k + 2 <= c; k += 2 * TPI) {
-        const int2 jp = *reinterpret_cast<const int2 *>(row.at(k));
+        const int2 jp = jn;
+        if (k + 2 * TPI + 2 <= c) jn = *reinterpret_cast<const int2 *>(row.at(k + 2 * TPI));
         const int j0 = jp.x, j1 = jp.y;
         const HydroJ32 J0 = load_hydro_j(a, j0), J1 = load_hydro_j(a, j1);
         hydro_pair32(pih, pil, vih, vil, Ai, Bi, J0, P, vmax);
