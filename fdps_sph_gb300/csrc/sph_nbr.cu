@@ -799,6 +799,9 @@ k_density_fused32(int n, int n_pass, const int *__restrict__ sup, const float *_
             const int64_t b = row_seg(rm, i, seg, c_all, &c);
             if (c <= 0) break;
             const float *rrow = sup_r2 + b, *mrow = sup_m + b;
+            // the next chunk's r^2 loads while this chunk is summed (1M, four passes: 0.69 -> 0.67
+            // ms; r^2 and m both ahead: 0.68 ms, more registers)
+            float4 rn = 4 * sub < c ? *reinterpret_cast<const float4 *>(rrow + 4 * sub) : make_float4(0.f, 0.f, 0.f, 0.f);
             for (int k = 4 * sub; k < c; k += 4 * DT) {
                 if (SPLIT) {
                     if (nt == (unsigned)SPH_FIX_TERMS) {
@@ -807,8 +810,9 @@ k_density_fused32(int n, int n_pass, const int *__restrict__ sup, const float *_
                     }
                     nt += 4;
                 }
-                const float4 r4 = *reinterpret_cast<const float4 *>(rrow + k);
+                const float4 r4 = rn;
                 const float4 m4 = *reinterpret_cast<const float4 *>(mrow + k);
+                if (k + 4 * DT < c) rn = *reinterpret_cast<const float4 *>(rrow + k + 4 * DT);
                 const float rr[4] = {r4.x, r4.y, r4.z, r4.w};
                 // members: inside the band by FP32, at its edge by the FP64 test; padding out
                 bool in[4];
