@@ -15,9 +15,12 @@
 // The array is shared by every call on a device and keeps the last call's
 // contents; each call rewrites all of it that it reads except the error
 // word, which it clears first.  Two calls whose work overlaps on the GPU
-// (different streams, no ordering between them) race on the array.  Each
-// call ends by reading the error word back to the host, so it returns only
-// after its work on `stream` has finished.
+// (different streams, no ordering between them) race on the array.  Called
+// eagerly, a call ends by reading the error word back to the host, so it
+// returns only after its work on `stream` has finished.  Called while
+// `stream` is being captured into a CUDA graph, it only records its work (the
+// memset, the launches and the device-to-device copies are all capturable)
+// and returns at once: a replay reports no status.
 #include <mutex>
 
 #include "sph_internal.cuh"
@@ -76,6 +79,13 @@ int noalloc_setup(int dev, unsigned char **out) {
     return SPH_OK;
 }
 
+// the array's address is known on this device (a capture may not make the first call: it looks
+// the address up)
+bool noalloc_ready(int dev) {
+    std::lock_guard<std::mutex> lk(g_na_mu);
+    return dev >= 0 && dev < 64 && g_na_ptr[dev] != nullptr;
+}
+
 }  // namespace
 
 extern "C" int sph_morton_order_noalloc(const double *x, const double *y, const double *z, int64_t n,
@@ -91,10 +101,17 @@ extern "C" int sph_morton_order_noalloc(const double *x, const double *y, const 
         cudaGetLastError();
         return SPH_ERR_CUDA;
     }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &capture) != cudaSuccess) {
+        cudaGetLastError();
+        return SPH_ERR_CUDA;
+    }
+    const bool capturing = capture == cudaStreamCaptureStatusActive;
+    if (capturing && !noalloc_ready(dev)) return SPH_ERR_STATE;   // nothing recorded
     unsigned char *base = nullptr;
     const int rc = noalloc_setup(dev, &base);
     if (rc != SPH_OK) return rc;
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
     double *box = reinterpret_cast<double *>(base + OFF_BOX);
     double *rb = reinterpret_cast<double *>(base + OFF_RB);
     uint64_t *ka = reinterpret_cast<uint64_t *>(base + OFF_K0), *kb = reinterpret_cast<uint64_t *>(base + OFF_K1);
@@ -136,6 +153,7 @@ extern "C" int sph_morton_order_noalloc(const double *x, const double *y, const 
         cudaGetLastError();
         return SPH_ERR_CUDA;
     }
+    if (capturing) return SPH_OK;   // recorded; a replay's status is not read back
     int herr = 0;
     if (cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess) {

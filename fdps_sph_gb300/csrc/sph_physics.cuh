@@ -44,12 +44,23 @@ __device__ __forceinline__ void wendland_poly_f(float s, float &w, float &g) {
     g = -22.0f * s * (1.0f + s * (7.0f + s * 16.0f)) * p7;
 }
 
-// std::lower_bound over an ascending axis
+// a double's bit pattern as an integer of the same order: a < b for doubles (neither a NaN)
+// exactly when key(a) < key(b), with -0 and +0 both 0 (they compare equal)
+__device__ __forceinline__ long long dorder_key(double d) {
+    const long long b = __double_as_longlong(d);
+    return b >= 0 ? b : -(b & 0x7fffffffffffffffLL);
+}
+
+// std::lower_bound over an ascending axis (no NaN in it).  The comparisons run on the integer
+// pipe through dorder_key, with the same outcome as the FP64 comparisons (a NaN v compares false
+// with everything: index 0); on this GPU the FP64 pipe is the bound of the EoS kernel.
 __device__ __forceinline__ int lower_bound_d(const double *ax, int n, double v) {
+    if (v != v) return 0;
+    const long long kv = dorder_key(v);
     int lo = 0, len = n;
     while (len > 0) {
         const int half = len >> 1;
-        if (ax[lo + half] < v) {
+        if (dorder_key(ax[lo + half]) < kv) {
             lo += half + 1;
             len -= half + 1;
         } else {

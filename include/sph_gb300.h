@@ -365,7 +365,7 @@ int sph_step_timed(sph_ctx *ctx, int n_steps, double *device_ms);
  * full neighbour-superset walks; out[9] partial (repair) walks; out[10]
  * particles whose h outgrew the superset skin; out[11] walk units walked;
  * out[12] walk units; out[13] superset row capacity; out[14] superset entries;
- * out[15] reserved. */
+ * out[15] superset entries in spill ranges (rows longer than the capacity). */
 int sph_get_counters(sph_ctx *ctx, int64_t out[16]);
 /* ---- allocation-free Morton ordering -------------------------------------
  * No counterpart in the reference: FDPS builds its tree on the host.  This
@@ -374,7 +374,7 @@ int sph_get_counters(sph_ctx *ctx, int64_t out[16]);
  * device-memory budget (its own pool allocator owns the rest of the GPU),
  * or one that may not take the device-wide synchronisation of a cudaFree in
  * the middle of its step.  The call returns after its work on `stream` has
- * finished (it reads a status word back).  x, y, z
+ * finished when called eagerly (it reads a status word back).  x, y, z
  * (n doubles each), keys_out (n) and order_out (n) are device pointers;
  * stream may be null (the legacy default stream).  keys_out[k] is the k-th
  * smallest 63-bit Morton key over the octree's root cube and order_out[k]
@@ -386,11 +386,16 @@ int sph_get_counters(sph_ctx *ctx, int64_t out[16]);
  * SPH_ERR_ARG, a non-finite position SPH_ERR_NONFINITE, a CUDA error already
  * pending on the calling thread SPH_ERR_CUDA (before any work is queued; the
  * error is left in place).  The first call on a
- * device looks up the array's device address (cudaGetSymbolAddress).  The
- * call ends by reading its error word back and synchronising `stream`, so it
- * returns after its work is done and cannot be recorded into a CUDA graph.
- * Every call on a device shares the array: calls that overlap on the GPU
- * race.  No device memory is allocated or freed. */
+ * device looks up the array's device address (cudaGetSymbolAddress) and must
+ * not be made while `stream` is being captured (SPH_ERR_STATE, nothing
+ * recorded).  Called eagerly, the call ends by reading its error word back
+ * and synchronising `stream`, so it returns after its work is done.  Called
+ * while `stream` is being captured into a CUDA graph, it records its work
+ * (a memset, kernel launches, device-to-device copies) and returns SPH_OK at
+ * once; a replay of the graph reports no status (a non-finite position then
+ * leaves its key undefined).  Every call on a device shares the array: calls
+ * (or replays) that overlap on the GPU race.  No device memory is allocated
+ * or freed. */
 #define SPH_NOALLOC_MAX_N 131072
 int sph_morton_order_noalloc(const double *x, const double *y, const double *z, int64_t n, uint64_t *keys_out,
                              int32_t *order_out, void *stream);

@@ -52,9 +52,10 @@ def _oracle_order(F):
     return perm.astype(np.int32), keys[perm]
 
 
-def _noalloc(L, x, y, z, n, k_out, o_out):
+def _noalloc(L, x, y, z, n, k_out, o_out, stream=None):
     return L.sph_morton_order_noalloc(C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), C.c_void_p(z.data_ptr()),
-                                      n, C.c_void_p(k_out.data_ptr()), C.c_void_p(o_out.data_ptr()), None)
+                                      n, C.c_void_p(k_out.data_ptr()), C.c_void_p(o_out.data_ptr()),
+                                      None if stream is None else C.c_void_p(stream))
 
 
 def _check_twice(F, ids, mats, against_tree=True):
@@ -124,3 +125,38 @@ def test_morton_order_without_allocation_rejects_a_nonfinite_position():
     o_out = torch.empty((n,), dtype=torch.int32, device=dev)
     assert _noalloc(L, x, y, z, n, k_out, o_out) == SPH_ERR_NONFINITE
     _check_twice(F, ids, mats)
+
+
+def test_morton_order_without_allocation_recorded_into_a_cuda_graph():
+    """captured on a side stream into a CUDA graph (after an eager call has looked the scratch up),
+    the call only records its work and returns SPH_OK; two replays, each into freshly cleared
+    outputs, give the oracle's order exactly"""
+    import torch
+
+    from fdps_sph_gb300 import lib
+
+    F, ids, mats, _ = small_impact(9000, 1000, seed=26)
+    n = F.shape[1]
+    slot, keys = _oracle_order(F)
+    L = lib.load()
+    dev = torch.device("cuda:0")
+    x, y, z = (torch.tensor(F[c], dtype=torch.float64, device=dev) for c in range(3))
+    k_out = torch.full((n,), -1, dtype=torch.int64, device=dev)
+    o_out = torch.full((n,), -1, dtype=torch.int32, device=dev)
+    assert _noalloc(L, x, y, z, n, k_out, o_out) == lib.SPH_OK   # eager: resolves the scratch array
+    torch.cuda.synchronize()
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        rc = _noalloc(L, x, y, z, n, k_out, o_out, stream=s.cuda_stream)
+    assert rc == lib.SPH_OK
+    for replay in range(2):
+        k_out.fill_(-1)
+        o_out.fill_(-1)
+        torch.cuda.synchronize()
+        g.replay()
+        torch.cuda.synchronize()
+        assert np.array_equal(k_out.cpu().numpy().view(np.uint64), keys), replay
+        assert np.array_equal(o_out.cpu().numpy(), slot), replay
+    # an eager call after the replays still reads its status back
+    assert _noalloc(L, x, y, z, n, k_out, o_out) == lib.SPH_OK
