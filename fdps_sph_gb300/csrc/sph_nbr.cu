@@ -928,6 +928,16 @@ static int dalloc_n(sph_ctx *ctx, T **p, int64_t n) {
     return SPH_OK;
 }
 
+// the double-float positions the walks read: in the mixed path the packs of sph_pack_mixed
+// (written after every sort, before any walk, with the same split and the same mass in .w),
+// in the FP64 path the walk's own
+static const float4 *walk_xh(const sph_ctx *ctx) {
+    return ctx->cfg.precision == SPH_PREC_MIXED ? ctx->xh : ctx->sup.pxh;
+}
+static const float4 *walk_xl(const sph_ctx *ctx) {
+    return ctx->cfg.precision == SPH_PREC_MIXED ? ctx->xl : ctx->sup.pxl;
+}
+
 // h-dependent float copies; called after every density pass and after the sort
 int sph_nbr_refresh_h(sph_ctx *ctx) {
     SphSuper &S = ctx->sup;
@@ -954,10 +964,12 @@ int sph_nbr_prepare(sph_ctx *ctx) {
         S.cap_particles = pitch;
     }
     const int64_t cap = ctx->cap;
-    k_pack_pos<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap),
-                                                            FLD(ctx->F, SPH_Z, cap), FLD(ctx->F, SPH_MASS, cap),
-                                                            ctx->mscale, S.pxh, S.pxl);
-    ++ctx->launches;
+    if (ctx->cfg.precision != SPH_PREC_MIXED) {   // the mixed path walks on sph_pack_mixed's packs
+        k_pack_pos<<<sph_div_up(n, 256), 256, 0, ctx->stream>>>(n, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap),
+                                                                FLD(ctx->F, SPH_Z, cap), FLD(ctx->F, SPH_MASS, cap),
+                                                                ctx->mscale, S.pxh, S.pxl);
+        ++ctx->launches;
+    }
     SPH_TRY(sph_nbr_refresh_h(ctx));
     // units
     Tree &t = ctx->tree;
@@ -1041,7 +1053,7 @@ static int walk_units(sph_ctx *ctx, const int *uidx, int n_walk) {
             auto walk = S.spill_on ? k_sup_walk<true> : k_sup_walk<false>;
             walk<<<blocks, NB_WARPS * 32, 0, ctx->stream>>>(
                 n_walk, S.units, uidx, FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap), FLD(ctx->F, SPH_Z, cap),
-                FLD(ctx->F, SPH_SMTH, cap), S.hsup, S.pxh, S.pxl, S.H2f, ctx->runs.prun, T, S.nbr, S.r2, S.m,
+                FLD(ctx->F, SPH_SMTH, cap), S.hsup, walk_xh(ctx), walk_xl(ctx), S.H2f, ctx->runs.prun, T, S.nbr, S.r2, S.m,
                 S.cnt, S.map(), S.uover, meta + META_ERR, meta + META_MAXCNT);
             ++ctx->launches;
         }
@@ -1140,7 +1152,7 @@ static int ensure_superset(sph_ctx *ctx) {
         ++ctx->launches;
     }
     const int blocks = (S.n_units + NB_WARPS - 1) / NB_WARPS;
-    k_unit_mark<<<blocks, NB_WARPS * 32, 0, ctx->stream>>>(S.n_units, S.units, S.pxh, S.pxl, vR, S.cvR,
+    k_unit_mark<<<blocks, NB_WARPS * 32, 0, ctx->stream>>>(S.n_units, S.units, walk_xh(ctx), walk_xl(ctx), vR, S.cvR,
                                                            t.cinfo, t.blo, t.bhi, ctx->runs.prun, S.umark);
     ++ctx->launches;
     SPH_TRY(sph_scan_exclusive(ctx, S.umark, S.uoff, nullptr, S.n_units, ctx->scan.total));
