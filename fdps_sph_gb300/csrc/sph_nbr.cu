@@ -31,7 +31,10 @@ namespace sph {
 
 constexpr int UNIT = 32;
 constexpr float KAPPA = 1.06f;   // measured at 1M: 1.15 -> 13.7 ms, 1.10 -> 12.9, 1.06 -> 12.6, 1.03 -> 13.0 (repairs)
-constexpr int NB_WARPS = 4;
+// walk warps per block: one, so a block's SM slot is freed as soon as its walk unit is done (the
+// units' walks differ in length); 1M walk: 1.95 ms with four warps per block, 1.97 with two,
+// 1.92 with one (about 30 blocks per SM, limited by shared memory)
+constexpr int NB_WARPS = 1;
 constexpr int ROW_K_MAX = 512;   // widest row block; longer rows continue in spill ranges (RowMap)
 constexpr int NB_CAND = 256;   // raw candidate indices per warp (flushes half as often as with 128: -0.02 ms at 1M)
 constexpr int NB_SURV = 64;    // culled candidates staged for the pair test
@@ -120,7 +123,7 @@ __device__ __forceinline__ float gap2_rd(float4 a_lo, float4 a_hi, float3 glo, f
 // SPILL: rows may continue in spill ranges (walks after this step's spill layout); without it
 // the hot loop carries no spill code (a row longer than K only raises the overflow flag)
 template <bool SPILL>
-__global__ void __launch_bounds__(NB_WARPS * 32, 8)
+__global__ void __launch_bounds__(NB_WARPS * 32, 32 / NB_WARPS)
 k_sup_walk(int n_units, const int2 *__restrict__ units, const int *__restrict__ uidx, const double *__restrict__ x,
            const double *__restrict__ y, const double *__restrict__ z, const double *__restrict__ h,
            double *__restrict__ hsup, const float4 *__restrict__ xh,
@@ -753,10 +756,10 @@ k_density_sup32(int n, const int *__restrict__ sup, const float *__restrict__ su
 // run's: a power of two), so a run's sums are the same alone and in any mix of runs.  SPLIT:
 // every run's masses on its own scale are at most 15, so each term is at most 16 and takes
 // sph_fix40_add (FP32 / integer pipes) instead of __float2ll_rn (FP64 pipe); both give the same
-// integers.
+// integers.  Blocks of 64 threads (32 particles): 0.67 -> 0.65 ms at 1M against 128.
 constexpr int DT = 2;
 template <bool SPLIT>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(64)
 k_density_fused32(int n, int n_pass, const int *__restrict__ sup, const float *__restrict__ sup_r2,
                   const float *__restrict__ sup_m, const int *__restrict__ scnt, RowMap rm,
                   const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
@@ -1231,7 +1234,7 @@ int sph_density_fused(sph_ctx *ctx) {
         SPH_TRY(time_mark(ctx, SEG_DENS_LIST));
         SPH_CUDA(ctx, cudaMemsetAsync(stopped, 0, sizeof(int), ctx->stream));
         auto kd = ctx->runs.fix_split ? k_density_fused32<true> : k_density_fused32<false>;
-        kd<<<sph_div_up((int64_t)n * DT, 128), 128, 0, ctx->stream>>>(
+        kd<<<sph_div_up((int64_t)n * DT, 64), 64, 0, ctx->stream>>>(
             n, np, S.nbr, S.r2, S.m, S.cnt, S.map(), FLD(ctx->F, SPH_X, cap), FLD(ctx->F, SPH_Y, cap),
             FLD(ctx->F, SPH_Z, cap), FLD(ctx->F, SPH_MASS, cap), FLD(ctx->F, SPH_SMTH, cap), S.hsup,
             FLD(ctx->F, SPH_DENS, cap), (float)(1365.0 / 64.0 / (3.141592653589793 * ctx->mscale)), S.npass,
