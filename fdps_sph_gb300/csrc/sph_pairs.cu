@@ -475,8 +475,9 @@ __device__ __forceinline__ HydroJ32 load_hydro_j(const HydroArgs32 &a, int j) {
     return J;
 }
 
-// six blocks per SM (80 registers, 8 bytes spilled; measured at 1M: 0.91 ms against 0.97 at the
-// 86 registers of five blocks; seven blocks would spill 88 bytes)
+// six blocks per SM, 80 registers (measured at 1M: 0.91 ms against 0.97 at the 86 registers of
+// five blocks, when first tuned; with the index prefetch, 0.74 ms against 0.80 at seven blocks,
+// 72 registers and spills)
 template <int TPI>
 __global__ void __launch_bounds__(PT, 6) k_hydro32(int n, HydroArgs32 a) {
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
